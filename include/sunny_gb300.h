@@ -1,0 +1,244 @@
+/*
+ * sunny_gb300.h -- C ABI of libsunnygb300.so, the GB300 (sm_103a) spin-dynamics
+ * library that a Sunny.jl package extension binds with `ccall`.
+ *
+ * The library replaces, for one `System`, the hot path of Sunny.jl v0.9.2:
+ *   - the local energy gradient   src/System/Interactions.jl:516-669
+ *   - the total energy            src/System/Interactions.jl:401-508
+ *   - step!(sys, ::Langevin)      src/Integrators.jl:313-357
+ *   - step!(sys, ::ImplicitMidpoint) src/Integrators.jl:379-452
+ *   - add_sample!(sc, sys)        src/SampledCorrelations/CorrelationSampling.jl:1-180
+ *   - merge_correlations          src/SampledCorrelations/SampledCorrelations.jl:128-142
+ *   - replica exchange            src/MonteCarlo/ParallelTempering.jl:40-95
+ *
+ * Conventions (all chosen so that Julia arrays can be passed without copies):
+ *   - Sites are ordered as Sunny's 4-D arrays (L1, L2, L3, natoms), column-major:
+ *     site = c1 + L1*(c2 + L2*(c3 + L3*atom)), all indices 0-based here.
+ *   - dipoles:   double[nsites][3]            (Array{Vec3,4})
+ *   - coherents: double[nsites][N][2] (re,im) (Array{CVec{N},4})
+ *   - 3x3, 5x5 and NxN matrices are COLUMN-MAJOR, as Julia stores Mat3/Mat5/Matrix.
+ *   - Host buffers are owned by the caller; the library copies in and out and never
+ *     keeps a host pointer. Device memory is owned by the handle.
+ *   - Every entry point returns SGB_OK (0) or a negative SGB_ERR_* code; the message
+ *     is available from sgb_last_error(handle) (or sgb_last_error(NULL) when no handle
+ *     exists yet).
+ *   - A handle is not thread safe (like a Sunny `System`): use one handle per thread.
+ *     Each handle owns one CUDA stream.
+ */
+#ifndef SUNNY_GB300_H
+#define SUNNY_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define SGB_OK               0
+#define SGB_ERR_ARG         -1  /* invalid argument (Julia: error(...) in constructors)   */
+#define SGB_ERR_CUDA        -2  /* a CUDA runtime / cuFFT call failed                       */
+#define SGB_ERR_NOCONVERGE  -3  /* implicit midpoint did not converge (Integrators.jl:412,451) */
+#define SGB_ERR_TIMEOUT     -4  /* a bounded device-side wait gave up (no Julia analogue)     */
+#define SGB_ERR_STATE       -5  /* call order violated (e.g. no couplings set)               */
+#define SGB_ERR_NOMEM       -6  /* device allocation failed                                  */
+
+/* ---- system modes and precisions ------------------------------------------ */
+#define SGB_MODE_DIPOLE              0  /* :dipole              (System.jl:43-45) */
+#define SGB_MODE_DIPOLE_UNCORRECTED  1  /* :dipole_uncorrected                   */
+#define SGB_MODE_SUN                 2  /* :SUN                                   */
+
+#define SGB_FP64  0  /* plain FP64 state and arithmetic                          */
+#define SGB_FP32  1  /* FP32 state and arithmetic, FP64 reductions/accumulators   */
+
+typedef struct sgb_system sgb_system;   /* one Sunny `System` resident on the GPU   */
+typedef struct sgb_corr   sgb_corr;     /* one `SampledCorrelations` accumulator    */
+typedef struct sgb_batch  sgb_batch;    /* many independent replicas (tempering)    */
+
+typedef struct {
+    int32_t dims[3];      /* supercell dimensions L1, L2, L3 (System.jl:33, `dims`)   */
+    int32_t natoms;       /* atoms per cell                                          */
+    int32_t N;            /* 0 in dipole modes; N = 2s+1 >= 2 in SU(N) mode            */
+    int32_t mode;         /* SGB_MODE_*                                                */
+    int32_t precision;    /* SGB_FP64 or SGB_FP32                                      */
+    int32_t device;       /* CUDA ordinal                                              */
+} sgb_desc;
+
+/* One pair coupling, as Sunny's PairCoupling (src/System/Types.jl:46-66). Pass only the
+ * non-culled couplings (isculled == false); the library adds the reversed copy with the
+ * transposed coupling itself, as Sunny does when it propagates a bond
+ * (src/System/PairExchange.jl:228-236, 466-467). */
+typedef struct {
+    int32_t i, j;         /* 0-based atom (sublattice) indices                         */
+    int32_t n[3];         /* cell offset of atom j                                     */
+    double  scalar;       /* constant shift (Types.jl:56)                              */
+    double  bilin[9];     /* 3x3 column-major bilinear J: E += S_i' J S_j              */
+    int32_t biquad_kind;  /* 0 none, 1 scalar (isotropic, uses scalar_biquad_metric),
+                             2 full 5x5 in the Stevens quadrupole basis                */
+    double  biquad[25];   /* kind 1: biquad[0]; kind 2: 5x5 column-major               */
+} sgb_bond;
+
+/* ---- system lifetime ------------------------------------------------------- */
+
+/* Replaces System(...) construction of buffers (src/System/System.jl:33-93). */
+int  sgb_create(const sgb_desc* desc, sgb_system** out);
+void sgb_destroy(sgb_system* sys);
+/* Last error message for `sys`, or the process-wide message when sys == NULL. */
+const char* sgb_last_error(const sgb_system* sys);
+/* Number of sites L1*L2*L3*natoms. */
+int64_t sgb_nsites(const sgb_system* sys);
+
+/* Per-site data: kappa[ns] (Types.jl:116 `κs`), g[ns][9] column-major (`gs`),
+ * field[ns][3] (`extfield`, already scaled by the Bohr magneton,
+ * Interactions.jl:210-229). `field` may be NULL (zero field). */
+int sgb_set_sites(sgb_system* sys, const double* kappa, const double* g, const double* field);
+
+/* Onsite coupling of one sublattice (src/System/OnsiteCoupling.jl:1-41).
+ * Dipole modes: `coeffs` = 28 renormalised Stevens coefficients c0[1], c2[5], c4[9], c6[13],
+ * each in descending q (Types.jl:4-10). SU(N) mode: `coeffs` = NxN Hermitian matrix,
+ * column-major, interleaved (re,im). */
+int sgb_set_onsite(sgb_system* sys, int32_t atom, const double* coeffs);
+
+/* Replaces the whole pair-coupling table (Interactions.jl:1-42 `repopulate_couplings…`). */
+int sgb_set_bonds(sgb_system* sys, const sgb_bond* bonds, int32_t nbonds);
+
+/* ---- state ------------------------------------------------------------------ */
+
+/* Copy the spin state in. Dipole modes read `dipoles` (coherents may be NULL);
+ * SU(N) mode reads `coherents` and recomputes dipoles = expected_spin(Z)
+ * (src/Operators/Spin.jl:72-87). Values are used as given (no renormalisation). */
+int sgb_set_state(sgb_system* sys, const double* dipoles, const double* coherents);
+/* Copy the spin state out (either pointer may be NULL). */
+int sgb_get_state(sgb_system* sys, double* dipoles, double* coherents);
+
+/* ---- the hot path ---------------------------------------------------------- */
+
+/* set_energy_grad_dipoles! (Interactions.jl:516-592) in dipole modes, or
+ * set_energy_grad_coherents! (Interactions.jl:596-669) in SU(N) mode, evaluated on the
+ * current state. grad: double[ns][3] (dipole) or double[ns][N][2] (SU(N)). */
+int sgb_energy_grad(sgb_system* sys, double* grad);
+
+/* energy(sys) (Interactions.jl:401-432) in FP64, and the magnetisation sum(sys.dipoles)
+ * (ParallelTempering.jl:31). Either output may be NULL. */
+int sgb_energy(sgb_system* sys, double* energy, double* magnetization3);
+
+/* `nsteps` x step!(sys, Langevin(dt; damping, kT)) (Integrators.jl:313-357).
+ * noise == NULL: standard normals come from a counter-based generator keyed by
+ *   (seed, step0 + k, site, component); `step0` lets a caller continue a stream.
+ * noise != NULL: caller-supplied standard normals for every step, laid out
+ *   [nsteps][ns][3] (dipole) or [nsteps][ns][N][2] (SU(N): complex normals with
+ *   E|z|^2 = 1, i.e. randn(ComplexF64)); they are scaled by sqrt(2 dt damping kT)
+ *   exactly as fill_noise! does (Integrators.jl:288-298). */
+int sgb_langevin(sgb_system* sys, double dt, double damping, double kT,
+                 uint64_t seed, uint64_t step0, int32_t nsteps, const double* noise);
+
+/* Writes the standard normals that sgb_langevin(noise=NULL) uses for step `step`
+ * into out ([ns][3] or [ns][N][2]), so that an FP64 CPU restatement can replay a
+ * device-noise trajectory exactly. */
+int sgb_langevin_noise(sgb_system* sys, uint64_t seed, uint64_t step, double* out);
+
+/* `nsteps` x step!(sys, ImplicitMidpoint(dt; damping, tol)) with kT = 0
+ * (Integrators.jl:379-452). Convergence test: sum over sites |S'-S''|^2 <= (tol*sqrt(ns))^2,
+ * accumulated in FP64 (Integrators.jl:361-371, 383, 426). On non-convergence after
+ * `max_iters` iterations the step that failed leaves the state unchanged and
+ * SGB_ERR_NOCONVERGE is returned. iters_out (nullable) receives the total number of
+ * fixed-point iterations performed. */
+int sgb_midpoint(sgb_system* sys, double dt, double damping, double tol, int32_t max_iters,
+                 int32_t nsteps, int64_t* iters_out);
+
+/* ---- SampledCorrelations --------------------------------------------------- */
+
+typedef struct {
+    int32_t nobs;          /* observables per site (3 for ssf_*: MeasureSpec.jl:53-76)       */
+    const double* obs;     /* dipole: [nobs][ns][3] row vectors (op . S);
+                              SU(N): [nobs][ns][N*N][2] column-major Hermitian matrices     */
+    int32_t ncorr;         /* number of correlation pairs (6 for ssf_*: MeasureSpec.jl:117)  */
+    const int32_t* pairs;  /* [ncorr][2] 0-based observable pairs (alpha, beta)              */
+    int32_t n_all_omega;   /* 2(nω-1)  (SampledCorrelations.jl:157, 207)                    */
+    int32_t measperiod;    /* steps between snapshots (SampledCorrelations.jl:163)           */
+    double  dt;            /* adjusted integrator time step (SampledCorrelations.jl:164)     */
+    double  damping;       /* ImplicitMidpoint damping (0 by default)                        */
+    double  tol;           /* ImplicitMidpoint tol                                           */
+    int32_t max_iters;     /* 100 in Sunny                                                   */
+    int32_t calculate_errors; /* keep the Welford M array (SampledCorrelations.jl:244)       */
+} sgb_corr_desc;
+
+/* SampledCorrelations(sys; measure, energies, dt, integrator=ImplicitMidpoint)
+ * (src/SampledCorrelations/SampledCorrelations.jl:199-269). The accumulator lives in
+ * device memory and is tied to `sys`. */
+int  sgb_corr_create(sgb_system* sys, const sgb_corr_desc* desc, sgb_corr** out);
+void sgb_corr_destroy(sgb_corr* sc);
+
+/* add_sample!(sc, sys; window) (CorrelationSampling.jl:156-176): integrates the
+ * trajectory of the system the accumulator was created on (mutating it) and accumulates
+ * one sample. window: 0 = :cosine, 1 = :rectangular. */
+int sgb_corr_add_sample(sgb_corr* sc, int32_t window);
+
+/* Reads sc.data as complex FP64, laid out exactly as Sunny's
+ * Array{ComplexF64,7}(ncorr, npos, npos, L1, L2, L3, n_all_omega) column-major, i.e.
+ * double[n_all_omega][L3][L2][L1][npos][npos][ncorr][2]. `M` (nullable; Float64 of the
+ * same shape without the complex axis) is filled when calculate_errors was set.
+ * nsamples may be NULL. Either array pointer may be NULL. */
+int sgb_corr_data(sgb_corr* sc, double* data, double* M, int64_t* nsamples);
+
+/* merge_correlations([dst, src]) into dst (SampledCorrelations.jl:128-142). */
+int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src);
+
+/* ---- batched replicas and parallel tempering -------------------------------- */
+
+/* Many independent dipole-mode replicas, each with its own dims, kT and state, stepped
+ * together. Couplings (onsite + bonds) are shared by all replicas; dims differ.
+ * dims: int32[nrep][3]; natoms, mode, precision from `proto`. */
+int  sgb_batch_create(const sgb_desc* proto, int32_t nrep, const int32_t* dims, sgb_batch** out);
+void sgb_batch_destroy(sgb_batch* b);
+const char* sgb_batch_last_error(const sgb_batch* b);
+int64_t sgb_batch_nsites(const sgb_batch* b, int32_t rep);
+/* Couplings shared by every replica: kappa/g/field per sublattice ([natoms], [natoms][9],
+ * [natoms][3]) plus onsite and bonds as for a single system. */
+int sgb_batch_set_couplings(sgb_batch* b, const double* kappa, const double* g, const double* field,
+                            const double* onsite /*[natoms][28]*/, const sgb_bond* bonds, int32_t nbonds);
+int sgb_batch_set_state(sgb_batch* b, int32_t rep, const double* dipoles);
+int sgb_batch_get_state(sgb_batch* b, int32_t rep, double* dipoles);
+/* kT of every replica (the tempering ladder position is a property of the replica slot). */
+int sgb_batch_set_kT(sgb_batch* b, const double* kT);
+int sgb_batch_get_kT(sgb_batch* b, double* kT);
+/* nsteps Langevin steps of every replica (each with its own kT), device noise keyed by
+ * (seed, replica, step0 + k, site, component). */
+int sgb_batch_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, uint64_t step0, int32_t nsteps);
+/* FP64 energy of every replica: E[nrep]. */
+int sgb_batch_energy(sgb_batch* b, double* E);
+/* One replica_exchange!(PT, exch_start) over replicas grouped by equal dims
+ * (ParallelTempering.jl:40-73): within each group, ordered by kT, pairs
+ * (r, r+1) for r = exch_start, exch_start+2, ... (1-based) attempt a swap of their
+ * kT with probability min(1, exp((E1-E2)(1/kT1-1/kT2))). Uniforms come from
+ * `uniforms` ([nrep], nullable -> device generator keyed by (seed, round)).
+ * n_accept (nullable, int64[nrep]) accumulates accepted swaps per lower slot. */
+int sgb_batch_exchange(sgb_batch* b, int32_t exch_start, uint64_t seed, uint64_t round,
+                       const double* uniforms, int64_t* n_accept);
+/* step_ensemble!(PT, nsteps, exch_interval) (ParallelTempering.jl:80-95): rounds of
+ * exch_interval Langevin steps followed by an exchange, captured once as a CUDA graph
+ * and replayed. */
+int sgb_batch_step_ensemble(sgb_batch* b, double dt, double damping, uint64_t seed,
+                            int32_t nsteps, int32_t exch_interval, int64_t* n_accept);
+
+/* ---- measurement helpers ---------------------------------------------------- */
+
+/* CUDA-event timing on the handle's own stream: slot in [0, 8). */
+int sgb_event_record(sgb_system* sys, int32_t slot);
+int sgb_event_elapsed(sgb_system* sys, int32_t slot_a, int32_t slot_b, float* ms);
+int sgb_batch_event_record(sgb_batch* b, int32_t slot);
+int sgb_batch_event_elapsed(sgb_batch* b, int32_t slot_a, int32_t slot_b, float* ms);
+/* Wait for all work queued on the handle's stream. */
+int sgb_synchronize(sgb_system* sys);
+/* Number of this library's own kernels launched on the handle so far (cuFFT excluded). */
+int64_t sgb_kernel_launches(const sgb_system* sys);
+int64_t sgb_batch_kernel_launches(const sgb_batch* b);
+/* Writes a 256 MiB device buffer on the handle's stream to evict L2. */
+int sgb_flush_l2(sgb_system* sys);
+/* Library version string. */
+const char* sgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SUNNY_GB300_H */

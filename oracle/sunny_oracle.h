@@ -1,0 +1,84 @@
+/*
+ * sunny_oracle.h -- TEST INFRASTRUCTURE ONLY. FP64 CPU restatement of Sunny.jl v0.9.2's
+ * spin-dynamics hot path, used by tests/, __graft_entry__.smoke() and bench.py's
+ * cpu_baseline / reference arm as the checker. Nothing in the shipped library calls it.
+ *
+ * It follows the reference's own (scatter-form, per-sublattice) loop order so that it is
+ * an independent check of the library's gather-form kernels. Parity is pinned against
+ * the reference's RNG-independent known answers (sum rules, RCS factors, SU(N)/dipole
+ * equivalence, energy conservation, kappa rescaling); the reference's one RNG-dependent
+ * golden S(q,ω) vector needs Julia's Xoshiro stream and is not reproducible here.
+ *
+ * Data layout is that of include/sunny_gb300.h (Sunny's column-major arrays).
+ */
+#ifndef SUNNY_ORACLE_H
+#define SUNNY_ORACLE_H
+#include <stdint.h>
+#include "../include/sunny_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int L[3];
+    int na;
+    int N;              /* 0 = dipole modes */
+    int mode;           /* SGB_MODE_* */
+    const double* kappa;   /* [ns]             */
+    const double* g;       /* [ns][9] col-major */
+    const double* field;   /* [ns][3] or NULL   */
+    const double* onsite;  /* dipole: [na][28]; SU(N): [na][N*N][2] col-major */
+    const sgb_bond* bonds; /* non-culled bonds  */
+    int nbonds;
+} or_sys;
+
+int64_t or_nsites(const or_sys* s);
+
+/* Interactions.jl:516-592 (dipole gradient, scatter form over non-culled bonds). */
+void or_grad_dipoles(const or_sys* s, const double* S, double* grad);
+/* Interactions.jl:596-669 (HZ = dE/dZbar). Z, HZ: [ns][N][2]. */
+void or_grad_coherents(const or_sys* s, const double* Z, double* HZ);
+/* Interactions.jl:401-508. S: dipoles [ns][3]; Z: coherents (SU(N) only, else NULL). */
+double or_energy(const or_sys* s, const double* S, const double* Z);
+/* OnsiteCoupling.jl:316-425 for one site: returns E, writes dE/dS. */
+double or_classical_anisotropy(const double* c28, const double* S, double* grad3);
+/* Spin.jl:72-87 */
+void or_expected_spin(int N, const double* Z, double* S3);
+
+/* Integrators.jl:313-332, one step. noise: [ns][3] standard normals or NULL (zero). */
+void or_langevin_dipole(const or_sys* s, double* S, double dt, double damping, double kT,
+                        const double* noise);
+/* Integrators.jl:335-357, one step. Z [ns][N][2], S [ns][3] updated. noise: [ns][N][2]
+ * complex normals with E|z|^2=1, or NULL. */
+void or_langevin_sun(const or_sys* s, double* Z, double* S, double dt, double damping,
+                     double kT, const double* noise);
+/* Integrators.jl:379-413, one step; returns 0 or SGB_ERR_NOCONVERGE; *iters += count. */
+int or_midpoint_dipole(const or_sys* s, double* S, double dt, double damping, double tol,
+                       int max_iters, int64_t* iters);
+/* Integrators.jl:422-452, one step. */
+int or_midpoint_sun(const or_sys* s, double* Z, double* S, double dt, double damping,
+                    double tol, int max_iters, int64_t* iters);
+
+/* Multi-step drivers (noise: [nsteps][ns][...] or NULL). */
+void or_langevin_steps(const or_sys* s, double* S, double* Z, double dt, double damping,
+                       double kT, int nsteps, const double* noise);
+int or_midpoint_steps(const or_sys* s, double* S, double* Z, double dt, double damping,
+                      double tol, int max_iters, int nsteps, int64_t* iters);
+
+/* Observables of one snapshot (CorrelationSampling.jl:1-19): out[nobs][ns] (real part;
+ * the imaginary part is zero for Hermitian observables). obs as in sgb_corr_desc. */
+void or_observables(const or_sys* s, const double* S, const double* Z, int nobs,
+                    const double* obs, double* out);
+
+/* Independent replicas stepped on a thread pool (OpenMP when compiled with it):
+ * replica r has state S + r*ns*3 and temperature kT[r]; noise from the caller per
+ * replica is not supported, the CPU path uses its own Gaussian source seeded by
+ * (seed, r). Used only as the timed CPU baseline. Returns threads used. */
+int or_langevin_replicas(const or_sys* s, int nrep, double* S, const double* kT, double dt,
+                         double damping, int nsteps, uint64_t seed);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,223 @@
+"""SampledCorrelations mirror: measurement specs, the GPU-resident S(q,ω) accumulator,
+add_sample and merge_correlations.
+
+Follows src/SampledCorrelations/*.jl and src/Measurements/MeasureSpec.jl of Sunny.jl
+v0.9.2. The accumulator lives on the device and is tied to one `System`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _abi
+from .operators import spin_matrices_of_dim
+from .system import ImplicitMidpoint, System
+
+CORR_PAIRS = [(3, 3), (2, 3), (1, 3), (2, 2), (1, 2), (1, 1)]  # MeasureSpec.jl:117
+
+
+class MeasureSpec:
+    """Observables (nobs per site) and 1-based correlation pairs (MeasureSpec.jl:5-27)."""
+
+    def __init__(self, observables: np.ndarray, corr_pairs, combiner=None):
+        self.observables = observables      # dipole: (nobs, ns, 3); SU(N): (nobs, ns, N, N) complex
+        self.corr_pairs = list(corr_pairs)
+        self.combiner = combiner
+
+    @property
+    def nobs(self):
+        return self.observables.shape[0]
+
+
+def all_dipole_observables(sys: System, apply_g: bool = True) -> np.ndarray:
+    """MeasureSpec.jl:53-76, in site order."""
+    ns = sys.nsites
+    G = sys._g if apply_g else np.broadcast_to(np.eye(3), (ns, 3, 3))
+    if sys.N == 0:
+        # component α is the row α of g: op . S = g[α, :] . S
+        return np.ascontiguousarray(np.transpose(G, (1, 0, 2)))       # (3, ns, 3)
+    S = spin_matrices_of_dim(sys.N)
+    obs = np.einsum("iab,bmn->aimn", G.astype(complex), np.stack(S))  # (3, ns, N, N)
+    return obs
+
+
+def ssf_custom(f, sys: System, apply_g: bool = True) -> MeasureSpec:
+    """ssf_custom (MeasureSpec.jl:115-130)."""
+    def combiner(q, corr):
+        m = np.array([[corr[5], corr[4], corr[2]],
+                      [np.conj(corr[4]), corr[3], corr[1]],
+                      [np.conj(corr[2]), np.conj(corr[1]), corr[0]]])
+        return f(q, m)
+    return MeasureSpec(all_dipole_observables(sys, apply_g), CORR_PAIRS, combiner)
+
+
+def ssf_trace(sys: System, apply_g: bool = True) -> MeasureSpec:
+    return ssf_custom(lambda q, ssf: np.trace(ssf.real), sys, apply_g)
+
+
+def ssf_perp(sys: System, apply_g: bool = True) -> MeasureSpec:
+    def f(q, ssf):
+        q2 = float(np.dot(q, q))
+        ssf = ssf.real
+        return (2 / 3) * np.trace(ssf) if q2 == 0 else np.trace(ssf) - q @ ssf @ q / q2
+    return ssf_custom(f, sys, apply_g)
+
+
+def adjusted_dt_and_downsampling_factor(dt: float, nw: int, wmax: float):
+    """SampledCorrelations.jl:152-173."""
+    assert math.pi / dt > wmax, "Desired `ωmax` not possible with specified `dt`. Choose smaller `dt` value."
+    n_all_w = 2 * (int(nw) - 1)
+    dw = wmax / (nw - 1)
+    measperiod = math.ceil(math.pi / (dt * wmax))
+    dt_new = 2 * math.pi / (dw * measperiod * n_all_w)
+    return dt_new, measperiod
+
+
+class SampledCorrelations:
+    """SampledCorrelations(sys; measure, energies, dt, integrator) (SampledCorrelations.jl:199-269)."""
+
+    def __init__(self, sys: System, *, measure: MeasureSpec, energies, dt, calculate_errors=False,
+                 integrator: ImplicitMidpoint | None = None, tol: float | None = None):
+        if energies is None:
+            n_all_w, measperiod, dw = 1, 1, math.nan
+            if not math.isnan(dt):
+                raise ValueError("Must use dt=NaN when energies=nothing")
+        else:
+            energies = np.asarray(energies, dtype=float)
+            nw = len(energies)
+            n_all_w = 2 * (nw - 1)
+            wmax = energies[-1]
+            if not (energies[0] == 0 and wmax > 0):
+                raise ValueError("`energies` must be a range from 0 to a positive value")
+            dE = np.diff(energies)
+            if not np.allclose(dE, dE[0]):
+                raise ValueError("`energies` must be equally spaced.")
+            dt, measperiod = adjusted_dt_and_downsampling_factor(dt, nw, wmax)
+            dw = wmax / (nw - 1)
+        integrator = integrator or ImplicitMidpoint(1.0)  # dt is set below
+        if tol is not None:
+            integrator.tol = tol
+        self.sys = sys
+        self.measure = measure
+        self.dw = dw
+        self.dt = dt
+        self.measperiod = measperiod
+        self.n_all_omega = n_all_w
+        self.integrator = integrator
+        self.calculate_errors = calculate_errors
+        obs = measure.observables
+        if sys.N:
+            o = np.ascontiguousarray(np.stack([np.swapaxes(obs, -1, -2).real, np.swapaxes(obs, -1, -2).imag], -1).reshape(-1))
+        else:
+            o = np.ascontiguousarray(obs, dtype=float).reshape(-1)
+        pairs = np.ascontiguousarray(np.array(measure.corr_pairs, dtype=np.int32) - 1).reshape(-1)
+        self._obs_keep, self._pairs_keep = o, pairs
+        d = _abi.CorrDesc()
+        d.nobs = measure.nobs
+        d.obs = _abi.dptr(o)
+        d.ncorr = len(measure.corr_pairs)
+        d.pairs = pairs.ctypes.data_as(C.POINTER(C.c_int32))
+        d.n_all_omega = n_all_w
+        d.measperiod = measperiod
+        d.dt = 0.0 if math.isnan(dt) else dt
+        d.damping = integrator.damping
+        d.tol = integrator.tol
+        d.max_iters = 100
+        d.calculate_errors = 1 if calculate_errors else 0
+        sys._sync_to_device()
+        h = C.c_void_p()
+        _abi.check(sys._lib.sgb_corr_create(sys.handle, C.byref(d), C.byref(h)), sys._lib, sys.handle)
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.sys._lib.sgb_corr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def nsamples(self) -> int:
+        n = C.c_int64()
+        _abi.check(self.sys._lib.sgb_corr_data(self._h, None, None, C.byref(n)), self.sys._lib, self.sys.handle)
+        return n.value
+
+    @property
+    def shape(self):
+        ncorr = len(self.measure.corr_pairs)
+        na = self.sys.natoms
+        return (ncorr, na, na, *self.sys.dims, self.n_all_omega)
+
+    @property
+    def data(self) -> np.ndarray:
+        """sc.data: complex array indexed [c, i, j, q1, q2, q3, ω] (0-based)."""
+        shp = self.shape
+        flat = np.zeros(2 * int(np.prod(shp)))
+        _abi.check(self.sys._lib.sgb_corr_data(self._h, _abi.dptr(flat), None, None), self.sys._lib, self.sys.handle)
+        z = flat[0::2] + 1j * flat[1::2]
+        return z.reshape(shp[::-1]).transpose(tuple(range(len(shp) - 1, -1, -1)))
+
+
+def add_sample(sc: SampledCorrelations, sys: System, window: str = "cosine"):
+    """add_sample!(sc, sys; window) (CorrelationSampling.jl:156-176). Mutates sys."""
+    if sys is not sc.sys:
+        raise ValueError("a GPU SampledCorrelations is bound to the System it was created with")
+    w = {"cosine": 0, "rectangular": 1}[window]
+    sys._sync_to_device()
+    rc = sys._lib.sgb_corr_add_sample(sc._h, w)
+    sys._dev_newer = True
+    _abi.check(rc, sys._lib, sys.handle)
+
+
+def merge_correlations(scs):
+    """merge_correlations (SampledCorrelations.jl:128-142): returns a new accumulator on the
+    system of the first one holding the combined samples."""
+    first = scs[0]
+    out = SampledCorrelations.__new__(SampledCorrelations)
+    out.__dict__.update({k: v for k, v in first.__dict__.items() if k != "_h"})
+    d = _abi.CorrDesc()
+    d.nobs = first.measure.nobs
+    d.obs = _abi.dptr(first._obs_keep)
+    d.ncorr = len(first.measure.corr_pairs)
+    d.pairs = first._pairs_keep.ctypes.data_as(C.POINTER(C.c_int32))
+    d.n_all_omega = first.n_all_omega
+    d.measperiod = first.measperiod
+    d.dt = 0.0 if math.isnan(first.dt) else first.dt
+    d.damping = first.integrator.damping
+    d.tol = first.integrator.tol
+    d.max_iters = 100
+    d.calculate_errors = 0
+    lib = first.sys._lib
+    h = C.c_void_p()
+    _abi.check(lib.sgb_corr_create(first.sys.handle, C.byref(d), C.byref(h)), lib, first.sys.handle)
+    out._h = h
+    for sc in scs:
+        _abi.check(lib.sgb_corr_merge(out._h, sc._h), lib, first.sys.handle)
+    return out
+
+
+def available_energies(sc: SampledCorrelations, negative_energies: bool = False):
+    """CorrelationUtils.jl:29-37."""
+    if math.isnan(sc.dw):
+        return math.nan
+    n = sc.n_all_omega
+    nonneg = n // 2 + 1
+    w = np.fft.fftfreq(n, 1.0 / (n * sc.dw))
+    w[nonneg - 1] *= -1
+    return w if negative_energies else w[:nonneg]
+
+
+def available_wave_vectors(sc: SampledCorrelations):
+    """CorrelationUtils.jl:9-19 (no reshaping): q in RLU for every data index."""
+    Ls = sc.sys.dims
+    offs = [1 if L % 2 else 0 for L in Ls]
+    hi = [L - L // 2 - o for L, o in zip(Ls, offs)]
+    lo = [1 - L // 2 - o for L, o in zip(Ls, offs)]
+    grids = [np.arange(l, h + 1) / L for l, h, L in zip(lo, hi, Ls)]
+    return np.stack(np.meshgrid(*grids, indexing="ij"), -1)

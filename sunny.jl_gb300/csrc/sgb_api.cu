@@ -1,0 +1,999 @@
+// sgb_api.cu -- host implementation of the C ABI declared in include/sunny_gb300.h.
+//
+// One sgb_system mirrors one Sunny `System` (src/System/Types.jl:106-140) resident on the
+// GPU: its spin state, per-site κ/g/field, and coupling tables. The host code validates
+// arguments with the reference's own error rules, packs the coupling tables (both
+// directions of each bond, as Sunny stores them), sizes the persistent launches from
+// the occupancy calculator, and reports kernel status words as SGB_ERR_* codes.
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "sgb_internal.h"
+#include "sgb_corr.h"
+
+#define SGB_VERSION "sunny-gb300 0.1.0 (sm_103a)"
+
+static thread_local std::string g_last_error;
+
+struct sgb_system {
+    sgb_desc d{};
+    int ns = 0, ncell = 0, N = 0;
+    bool fp32 = false;
+    bool sun = false;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8] = {};
+    std::string err;
+    long long launches = 0;
+    int nsm = 0;
+    // host copies of the model
+    std::vector<double> kappa_h, g_h, field_h, onsite_h;
+    std::vector<sgb_bond> bonds_h;
+    bool sites_set = false, bonds_set = false, state_set = false;
+    bool has_field = false, has_biquad = false;
+    bool tables_dirty = true;
+    // device data (element type R = float or double)
+    void* kappa = nullptr;   // [ns]
+    void* h = nullptr;       // [3][ns]
+    void* tables = nullptr;
+    int tables_bytes = 0;
+    Model<float> mf{};
+    Model<double> md{};
+    // state buffers
+    void* S = nullptr;   // dipole: spins [3][ns]; SU(N): dipoles [3][ns]
+    void* P = nullptr;   // [3][ns]
+    void* H = nullptr;   // [3][3][ns]
+    void* Z = nullptr;   // SU(N) [2N][ns]
+    void* Q = nullptr;   // SU(N) [5][ns]
+    void* QP = nullptr;  // SU(N) [5][ns]
+    void* QH = nullptr;  // SU(N) [3][5][ns]
+    Ctrl* ctrl = nullptr;
+    double* partials = nullptr;
+    double* red = nullptr;
+    double* dbuf = nullptr;     // device double scratch (noise, grads)
+    size_t dbuf_cap = 0;
+    void* flush = nullptr;
+    std::vector<char> stage;    // host staging
+};
+
+struct sgb_corr {
+    sgb_system* sys = nullptr;
+    std::string err;
+    int nobs = 0, ncorr = 0, npos = 0, ncell = 0, nomega = 0, nsnaps = 0, measperiod = 1;
+    double dt = 0, damping = 0, tol = 0;
+    int max_iters = 100;
+    int window = -1;
+    int64_t nsamples = 0;
+    void* ops = nullptr;      // R
+    int* pairs = nullptr;
+    void* A = nullptr;        // complex R [n][nobs][npos][ncell]
+    void* Ahat = nullptr;
+    double* P = nullptr;      // complex double accumulator
+    size_t plen = 0;          // complex elements
+    double* g = nullptr;      // [n]
+    cufftHandle plan_space = 0, plan_time = 0;
+    bool have_space = false, have_time = false;
+};
+
+// ---------------------------------------------------------------------------------
+namespace {
+
+int fail(sgb_system* s, int code, const std::string& msg) {
+    if (s) s->err = msg;
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(sgb_system* s, cudaError_t e, const char* what) {
+    return fail(s, SGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                      \
+    do {                                                              \
+        cudaError_t _e = (call);                                      \
+        if (_e != cudaSuccess) return cuda_fail(s, _e, #call);        \
+    } while (0)
+
+size_t rsize(const sgb_system* s) { return s->fp32 ? 4 : 8; }
+
+int dmalloc(sgb_system* s, void** p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(s, SGB_ERR_NOMEM, std::string("device allocation of ") + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+    }
+    return SGB_OK;
+}
+
+void dfree(void*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+int ensure_dbuf(sgb_system* s, size_t n) {
+    if (s->dbuf_cap >= n) return SGB_OK;
+    if (s->dbuf) cudaFree(s->dbuf);
+    s->dbuf = nullptr;
+    s->dbuf_cap = 0;
+    int rc = dmalloc(s, (void**)&s->dbuf, n * sizeof(double));
+    if (rc == SGB_OK) s->dbuf_cap = n;
+    return rc;
+}
+
+inline int imod(int x, int L) {
+    int r = x % L;
+    return r < 0 ? r + L : r;
+}
+
+// Stevens quadrupoles O[2,q], q = 2..-2, of dimension N (src/Operators/Stevens.jl:12-86),
+// column-major complex.
+void stevens_quadrupoles(int N, std::vector<std::complex<double>>& out) {
+    typedef std::complex<double> cd;
+    out.assign(5 * N * N, cd(0, 0));
+    if (N <= 2) return;
+    double s = (N - 1) / 2.0;
+    std::vector<cd> Sx(N * N), Sy(N * N), Sz(N * N);
+    for (int j = 1; j <= N - 1; j++) {
+        double off = std::sqrt(2 * (s + 1) * j - (double)j * (j + 1)) / 2;
+        int r = j - 1, c = j;
+        Sx[r + N * c] = off; Sx[c + N * r] = off;
+        Sy[r + N * c] = cd(0, -off); Sy[c + N * r] = cd(0, off);
+    }
+    for (int k = 0; k < N; k++) Sz[k + N * k] = s - k;
+    auto mul = [N](const std::vector<cd>& A, const std::vector<cd>& B) {
+        std::vector<cd> C(N * N);
+        for (int c = 0; c < N; c++)
+            for (int r = 0; r < N; r++) {
+                cd acc = 0;
+                for (int k = 0; k < N; k++) acc += A[r + N * k] * B[k + N * c];
+                C[r + N * c] = acc;
+            }
+        return C;
+    };
+    std::vector<cd> Jp(N * N), Jm(N * N);
+    for (int i = 0; i < N * N; i++) { Jp[i] = Sx[i] + cd(0, 1) * Sy[i]; Jm[i] = Sx[i] - cd(0, 1) * Sy[i]; }
+    auto Jp2 = mul(Jp, Jp), Jm2 = mul(Jm, Jm), Jz2 = mul(Sz, Sz);
+    auto X = mul(Sx, Sx);
+    { auto t = mul(Sy, Sy); for (int i = 0; i < N * N; i++) X[i] += t[i] + Jz2[i]; }
+    std::vector<cd> A(N * N);
+    for (int i = 0; i < N * N; i++) out[0 * N * N + i] = 0.5 * (Jp2[i] + Jm2[i]);
+    for (int i = 0; i < N * N; i++) A[i] = 0.5 * (Jp[i] + Jm[i]);
+    { auto a = mul(A, Sz), b = mul(Sz, A); for (int i = 0; i < N * N; i++) out[1 * N * N + i] = 0.5 * (a[i] + b[i]); }
+    for (int i = 0; i < N * N; i++) out[2 * N * N + i] = 3.0 * Jz2[i] - X[i];
+    for (int i = 0; i < N * N; i++) A[i] = (Jp[i] - Jm[i]) / cd(0, 2);
+    { auto a = mul(A, Sz), b = mul(Sz, A); for (int i = 0; i < N * N; i++) out[3 * N * N + i] = 0.5 * (a[i] + b[i]); }
+    for (int i = 0; i < N * N; i++) out[4 * N * N + i] = (Jp2[i] - Jm2[i]) / cd(0, 2);
+}
+
+size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+template <class R>
+int build_tables(sgb_system* s, Model<R>& M) {
+    const int na = s->d.natoms, N = s->N;
+    const int L[3] = {s->d.dims[0], s->d.dims[1], s->d.dims[2]};
+    // directed bonds per sublattice
+    std::vector<std::vector<DBond<R>>> per(na);
+    std::vector<R> bqtab;
+    bool any_bq = false;
+    for (const sgb_bond& b : s->bonds_h) {
+        for (int dir = 0; dir < 2; dir++) {
+            DBond<R> e{};
+            int from = dir == 0 ? b.i : b.j;
+            int to = dir == 0 ? b.j : b.i;
+            e.j = to;
+            for (int k = 0; k < 3; k++) {
+                int n = dir == 0 ? b.n[k] : -b.n[k];
+                e.n[k] = imod(n, L[k]);
+            }
+            bool iso = true;
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) {
+                    double v = dir == 0 ? b.bilin[r + 3 * c] : b.bilin[c + 3 * r];
+                    e.J[r + 3 * c] = (R)v;
+                    if (r != c && v != 0.0) iso = false;
+                }
+            if (!(b.bilin[0] == b.bilin[4] && b.bilin[0] == b.bilin[8])) iso = false;
+            e.jkind = iso ? 0 : 1;
+            e.scalar = (R)b.scalar;
+            e.bqkind = b.biquad_kind;
+            e.bq = 0;
+            e.bqidx = 0;
+            if (b.biquad_kind == 1) {
+                e.bq = (R)b.biquad[0];
+                if (b.biquad[0] == 0.0) e.bqkind = 0;
+            } else if (b.biquad_kind == 2) {
+                e.bqidx = (int)(bqtab.size() / 25);
+                for (int c = 0; c < 5; c++)
+                    for (int r = 0; r < 5; r++)
+                        bqtab.push_back((R)(dir == 0 ? b.biquad[r + 5 * c] : b.biquad[c + 5 * r]));
+            }
+            if (e.bqkind != 0) any_bq = true;
+            e.fwd = dir == 0 ? 1 : 0;
+            per[from].push_back(e);
+        }
+    }
+    int nb = 0;
+    for (auto& v : per) nb += (int)v.size();
+    int nbq = (int)(bqtab.size() / 25);
+    size_t off = 0;
+    M.off_stev = (int)off; off = align16(off + sizeof(R) * 28 * na);
+    M.off_kmax = (int)off; off = align16(off + sizeof(int) * na);
+    M.off_boff = (int)off; off = align16(off + sizeof(int) * (na + 1));
+    M.off_bonds = (int)off; off = align16(off + sizeof(DBond<R>) * nb);
+    M.off_bq = (int)off; off = align16(off + sizeof(R) * 25 * nbq);
+    M.off_lam = (int)off; off = align16(off + sizeof(R) * 2 * N * N * (s->sun ? na : 0));
+    M.off_qmat = (int)off; off = align16(off + sizeof(R) * 2 * N * N * 5 * (s->sun ? 1 : 0));
+    size_t bytes = align16(off);
+    if (bytes > 200 * 1024) return fail(s, SGB_ERR_ARG, "coupling tables exceed 200 KiB of shared memory");
+    std::vector<unsigned char> buf(bytes, 0);
+    R* stev = reinterpret_cast<R*>(buf.data() + M.off_stev);
+    int* kmax = reinterpret_cast<int*>(buf.data() + M.off_kmax);
+    int* boff = reinterpret_cast<int*>(buf.data() + M.off_boff);
+    DBond<R>* bonds = reinterpret_cast<DBond<R>*>(buf.data() + M.off_bonds);
+    R* bq = reinterpret_cast<R*>(buf.data() + M.off_bq);
+    if (!s->sun) {
+        for (int a = 0; a < na; a++) {
+            const double* c = s->onsite_h.data() + 28 * a;
+            // StevensExpansion drops k-blocks with norm < 1e-12 (src/System/Types.jl:12-16)
+            const int start[4] = {0, 1, 6, 15}, len[4] = {1, 5, 9, 13};
+            int km = 0;
+            for (int g = 0; g < 4; g++) {
+                double nrm = 0;
+                for (int q = 0; q < len[g]; q++) nrm += c[start[g] + q] * c[start[g] + q];
+                bool zero = std::sqrt(nrm) < 1e-12;
+                for (int q = 0; q < len[g]; q++) stev[28 * a + start[g] + q] = zero ? (R)0 : (R)c[start[g] + q];
+                if (!zero && g > 0) km = 2 * g;
+            }
+            kmax[a] = km;
+        }
+    } else {
+        R* lam = reinterpret_cast<R*>(buf.data() + M.off_lam);
+        for (int i = 0; i < 2 * N * N * na; i++) lam[i] = (R)s->onsite_h[i];
+        std::vector<std::complex<double>> qm;
+        stevens_quadrupoles(N, qm);
+        R* q = reinterpret_cast<R*>(buf.data() + M.off_qmat);
+        for (int i = 0; i < 5 * N * N; i++) { q[2 * i] = (R)qm[i].real(); q[2 * i + 1] = (R)qm[i].imag(); }
+    }
+    int k = 0;
+    for (int a = 0; a < na; a++) {
+        boff[a] = k;
+        for (auto& e : per[a]) bonds[k++] = e;
+    }
+    boff[na] = k;
+    for (size_t i = 0; i < bqtab.size(); i++) bq[i] = bqtab[i];
+    dfree(s->tables);
+    int rc = dmalloc(s, &s->tables, bytes);
+    if (rc) return rc;
+    CK(cudaMemcpy(s->tables, buf.data(), bytes, cudaMemcpyHostToDevice));
+    s->tables_bytes = (int)bytes;
+    s->has_biquad = any_bq;
+    M.L1 = L[0]; M.L2 = L[1]; M.L3 = L[2]; M.na = na;
+    M.ns = s->ns; M.ncell = s->ncell; M.N = N;
+    M.dipole_mode = s->sun ? 0 : 1;
+    M.has_biquad = any_bq ? 1 : 0;
+    M.kappa = reinterpret_cast<const R*>(s->kappa);
+    M.h = s->has_field ? reinterpret_cast<const R*>(s->h) : nullptr;
+    M.tables = reinterpret_cast<const unsigned char*>(s->tables);
+    M.tables_bytes = (int)bytes;
+    M.nb = nb;
+    M.nbq = nbq;
+    return SGB_OK;
+}
+
+int ensure_tables(sgb_system* s) {
+    if (!s->sites_set) return fail(s, SGB_ERR_STATE, "sgb_set_sites must be called before stepping");
+    if (!s->tables_dirty) return SGB_OK;
+    int rc = s->fp32 ? build_tables<float>(s, s->mf) : build_tables<double>(s, s->md);
+    if (rc == SGB_OK) s->tables_dirty = false;
+    return rc;
+}
+
+// Choose sites-per-thread and grid for a persistent cooperative launch.
+template <class R>
+int plan_launch(sgb_system* s, LaunchInfo& li) {
+    const int sptv_dip[4] = {1, 2, 4, 8}, sptv_sun[2] = {1, 2};
+    const int* sptv = s->sun ? sptv_sun : sptv_dip;
+    int nspt = s->sun ? 2 : 4;
+    size_t smem = (size_t)s->tables_bytes;
+    for (int i = 0; i < nspt; i++) {
+        int spt = sptv[i];
+        int bps = 0;
+        int rc = s->sun ? sun_max_blocks<R>(s->N, spt, smem, &bps) : dip_max_blocks<R>(spt, smem, &bps);
+        if (rc != SGB_OK) return fail(s, SGB_ERR_CUDA, "occupancy query failed");
+        long long cap = (long long)bps * s->nsm;
+        long long need = ((long long)s->ns + (long long)SGB_BLOCK * spt - 1) / ((long long)SGB_BLOCK * spt);
+        if (need <= cap && need >= 1) {
+            li.grid = (int)need;
+            li.block = SGB_BLOCK;
+            li.spt = spt;
+            li.smem = smem;
+            return SGB_OK;
+        }
+    }
+    return fail(s, SGB_ERR_ARG, "system too large for one co-resident persistent launch");
+}
+
+int reset_ctrl(sgb_system* s) {
+    CK(cudaMemsetAsync(s->ctrl, 0, sizeof(Ctrl), s->stream));
+    return SGB_OK;
+}
+
+int read_ctrl(sgb_system* s, Ctrl* out) {
+    CK(cudaMemcpyAsync(out, s->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return SGB_OK;
+}
+
+template <class R>
+Model<R>& model(sgb_system* s);
+template <>
+Model<float>& model<float>(sgb_system* s) { return s->mf; }
+template <>
+Model<double>& model<double>(sgb_system* s) { return s->md; }
+
+std::string fmt_g(double x) {
+    char b[64];
+    snprintf(b, sizeof b, "%g", x);
+    return b;
+}
+
+template <class R>
+int run_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t seed, uint64_t step0, int nsteps, const double* noise) {
+    LaunchInfo li;
+    int rc = plan_launch<R>(s, li);
+    if (rc) return rc;
+    double nscale = (damping == 0.0 || kT == 0.0) ? 0.0 : std::sqrt(2 * dt * damping * kT);
+    const size_t per = s->sun ? (size_t)2 * s->N * s->ns : (size_t)3 * s->ns;
+    int chunk = nsteps;
+    if (noise) {
+        size_t maxel = (size_t)1 << 24;  // 128 MiB of injected noise per launch
+        chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)nsteps, maxel / per));
+        if ((rc = ensure_dbuf(s, per * chunk))) return rc;
+    }
+    Model<R>& M = model<R>(s);
+    for (int k0 = 0; k0 < nsteps; k0 += chunk) {
+        int nk = std::min(chunk, nsteps - k0);
+        const double* dn = nullptr;
+        if (noise) {
+            CK(cudaMemcpyAsync(s->dbuf, noise + per * k0, per * nk * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+            dn = s->dbuf;
+        }
+        if ((rc = reset_ctrl(s))) return rc;
+        if (!s->sun)
+            rc = dip_launch_heun<R>(M, (R*)s->S, (R*)s->P, s->ctrl, nk, dt, damping, nscale, seed, step0 + k0, dn, li, s->stream);
+        else
+            rc = sun_launch_heun<R>(M, (R*)s->Z, (R*)s->S, (R*)s->Q, (R*)s->P, (R*)s->QP, s->ctrl, nk, dt, damping, nscale,
+                                    seed, step0 + k0, dn, li, s->stream);
+        s->launches++;
+        if (rc) return cuda_fail(s, cudaGetLastError(), "Langevin launch");
+        Ctrl c;
+        if ((rc = read_ctrl(s, &c))) return rc;
+        if (c.status == SGB_ERR_TIMEOUT) return fail(s, SGB_ERR_TIMEOUT, "a device-side barrier timed out");
+        if (c.status != 0) return fail(s, c.status, "Langevin kernel reported an error");
+    }
+    return SGB_OK;
+}
+
+template <class R>
+int run_midpoint(sgb_system* s, double dt, double damping, double tol, int max_iters, int nsteps, int64_t* iters,
+                 const SnapArgs<R>& snap, bool sync_status = true) {
+    LaunchInfo li;
+    int rc = plan_launch<R>(s, li);
+    if (rc) return rc;
+    double atol = tol * std::sqrt((double)s->ns);
+    double atol2 = atol * atol;
+    Model<R>& M = model<R>(s);
+    if ((rc = reset_ctrl(s))) return rc;
+    if (!s->sun)
+        rc = dip_launch_midpoint<R>(M, (R*)s->S, (R*)s->H, s->ctrl, nsteps, dt, damping, atol2, max_iters, snap, li, s->stream);
+    else
+        rc = sun_launch_midpoint<R>(M, (R*)s->Z, (R*)s->S, (R*)s->Q, (R*)s->H, (R*)s->QH, s->ctrl, nsteps, dt, damping, atol2,
+                                    max_iters, snap, li, s->stream);
+    s->launches++;
+    if (rc) return cuda_fail(s, cudaGetLastError(), "midpoint launch");
+    if (!sync_status) return SGB_OK;
+    Ctrl c;
+    if ((rc = read_ctrl(s, &c))) return rc;
+    if (iters) *iters = c.iters;
+    if (c.status == SGB_ERR_NOCONVERGE) {
+        if (!s->sun)
+            return fail(s, SGB_ERR_NOCONVERGE, "Spherical midpoint method failed to converge to tolerance " + fmt_g(tol) +
+                                                   " after " + std::to_string(max_iters) + " iterations.");
+        return fail(s, SGB_ERR_NOCONVERGE, "Schrödinger midpoint method failed to converge in " + std::to_string(max_iters) + " iterations.");
+    }
+    if (c.status == SGB_ERR_TIMEOUT) return fail(s, SGB_ERR_TIMEOUT, "a device-side barrier timed out");
+    if (c.status != 0) return fail(s, c.status, "midpoint kernel reported an error");
+    return SGB_OK;
+}
+
+template <class R>
+int do_refresh(sgb_system* s) {
+    if (!s->sun) return SGB_OK;
+    int rc = sun_launch_refresh<R>(model<R>(s), (const R*)s->Z, (R*)s->S, (R*)s->Q, s->stream);
+    s->launches++;
+    return rc ? cuda_fail(s, cudaGetLastError(), "refresh launch") : SGB_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------------
+extern "C" {
+
+const char* sgb_version(void) { return SGB_VERSION; }
+
+const char* sgb_last_error(const sgb_system* s) { return s ? s->err.c_str() : g_last_error.c_str(); }
+
+int64_t sgb_nsites(const sgb_system* s) { return s ? s->ns : 0; }
+
+int sgb_create(const sgb_desc* d, sgb_system** out) {
+    if (!d || !out) return fail(nullptr, SGB_ERR_ARG, "null argument");
+    *out = nullptr;
+    for (int k = 0; k < 3; k++)
+        if (d->dims[k] < 1) return fail(nullptr, SGB_ERR_ARG, "dims must be positive");
+    if (d->natoms < 1 || d->natoms > SGB_MAX_SUBLAT) return fail(nullptr, SGB_ERR_ARG, "natoms must be in [1, 64]");
+    if (d->mode != SGB_MODE_DIPOLE && d->mode != SGB_MODE_DIPOLE_UNCORRECTED && d->mode != SGB_MODE_SUN)
+        return fail(nullptr, SGB_ERR_ARG, "Mode must be `:SUN`, `:dipole`, or `:dipole_uncorrected`");
+    if (d->mode == SGB_MODE_SUN && (d->N < 2 || d->N > SGB_MAX_N))
+        return fail(nullptr, SGB_ERR_ARG, "SU(N) mode supports N in [2, 5]");
+    if (d->precision != SGB_FP32 && d->precision != SGB_FP64) return fail(nullptr, SGB_ERR_ARG, "precision must be SGB_FP32 or SGB_FP64");
+    long long ns = (long long)d->dims[0] * d->dims[1] * d->dims[2] * d->natoms;
+    if (ns > (1LL << 30)) return fail(nullptr, SGB_ERR_ARG, "too many sites");
+    sgb_system* s = new sgb_system();
+    s->d = *d;
+    s->ns = (int)ns;
+    s->ncell = d->dims[0] * d->dims[1] * d->dims[2];
+    s->sun = d->mode == SGB_MODE_SUN;
+    s->N = s->sun ? d->N : 0;
+    s->fp32 = d->precision == SGB_FP32;
+    auto bad = [&](int code) { sgb_destroy(s); return code; };
+    cudaError_t e = cudaSetDevice(d->device);
+    if (e != cudaSuccess) { fail(nullptr, SGB_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e)); return bad(SGB_ERR_CUDA); }
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, d->device);
+    if (e != cudaSuccess) { fail(nullptr, SGB_ERR_CUDA, std::string("cudaGetDeviceProperties: ") + cudaGetErrorString(e)); return bad(SGB_ERR_CUDA); }
+    if (!prop.cooperativeLaunch) { fail(nullptr, SGB_ERR_CUDA, "device lacks cooperative launch"); return bad(SGB_ERR_CUDA); }
+    s->nsm = prop.multiProcessorCount;
+    e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { fail(nullptr, SGB_ERR_CUDA, "cudaStreamCreate failed"); return bad(SGB_ERR_CUDA); }
+    for (int i = 0; i < 8; i++) cudaEventCreate(&s->ev[i]);
+    size_t R = rsize(s);
+    int rc = SGB_OK;
+    rc |= dmalloc(s, &s->kappa, R * ns);
+    rc |= dmalloc(s, &s->h, R * 3 * ns);
+    rc |= dmalloc(s, &s->S, R * 3 * ns);
+    rc |= dmalloc(s, &s->P, R * 3 * ns);
+    rc |= dmalloc(s, &s->H, R * 9 * ns);
+    if (s->sun) {
+        rc |= dmalloc(s, &s->Z, R * 2 * s->N * ns);
+        rc |= dmalloc(s, &s->Q, R * 5 * ns);
+        rc |= dmalloc(s, &s->QP, R * 5 * ns);
+        rc |= dmalloc(s, &s->QH, R * 15 * ns);
+    }
+    rc |= dmalloc(s, (void**)&s->ctrl, sizeof(Ctrl));
+    rc |= dmalloc(s, (void**)&s->partials, sizeof(double) * 4 * SGB_ENERGY_BLOCKS);
+    rc |= dmalloc(s, (void**)&s->red, sizeof(double) * 8);
+    if (rc) { g_last_error = s->err; return bad(SGB_ERR_NOMEM); }
+    cudaMemset(s->S, 0, R * 3 * ns);
+    if (s->sun) cudaMemset(s->Z, 0, R * 2 * s->N * ns);
+    cudaMemset(s->ctrl, 0, sizeof(Ctrl));
+    // defaults: kappa = 1, g = 2I, no field, no couplings
+    s->kappa_h.assign(ns, 1.0);
+    s->g_h.assign(9 * ns, 0.0);
+    for (long long i = 0; i < ns; i++) s->g_h[9 * i] = s->g_h[9 * i + 4] = s->g_h[9 * i + 8] = 2.0;
+    s->onsite_h.assign(s->sun ? (size_t)2 * s->N * s->N * d->natoms : (size_t)28 * d->natoms, 0.0);
+    *out = s;
+    return SGB_OK;
+}
+
+void sgb_destroy(sgb_system* s) {
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    dfree(s->kappa); dfree(s->h); dfree(s->tables); dfree(s->S); dfree(s->P); dfree(s->H);
+    dfree(s->Z); dfree(s->Q); dfree(s->QP); dfree(s->QH);
+    void* p = s->ctrl; dfree(p);
+    p = s->partials; dfree(p);
+    p = s->red; dfree(p);
+    p = s->dbuf; dfree(p);
+    dfree(s->flush);
+    for (int i = 0; i < 8; i++) if (s->ev[i]) cudaEventDestroy(s->ev[i]);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int sgb_set_sites(sgb_system* s, const double* kappa, const double* g, const double* field) {
+    if (!s || !kappa || !g) return fail(s, SGB_ERR_ARG, "kappa and g are required");
+    const int ns = s->ns;
+    s->kappa_h.assign(kappa, kappa + ns);
+    s->g_h.assign(g, g + 9 * (size_t)ns);
+    s->field_h.assign(3 * (size_t)ns, 0.0);
+    if (field) s->field_h.assign(field, field + 3 * (size_t)ns);
+    // Zeeman gradient h = g' B (Interactions.jl:520-523), stored [3][ns]
+    std::vector<double> hh(3 * (size_t)ns, 0.0);
+    bool any = false;
+    for (int i = 0; i < ns; i++) {
+        const double* gi = s->g_h.data() + 9 * (size_t)i;
+        const double* B = s->field_h.data() + 3 * (size_t)i;
+        for (int r = 0; r < 3; r++) {
+            double v = gi[0 + 3 * r] * B[0] + gi[1 + 3 * r] * B[1] + gi[2 + 3 * r] * B[2];
+            hh[(size_t)r * ns + i] = v;
+            any |= v != 0.0;
+        }
+    }
+    s->has_field = any;
+    s->stage.resize(std::max(s->stage.size(), 3 * (size_t)ns * sizeof(double)));
+    if (s->fp32) {
+        float* k = reinterpret_cast<float*>(s->stage.data());
+        for (int i = 0; i < ns; i++) k[i] = (float)kappa[i];
+        CK(cudaMemcpy(s->kappa, k, sizeof(float) * ns, cudaMemcpyHostToDevice));
+        for (size_t i = 0; i < 3 * (size_t)ns; i++) k[i] = (float)hh[i];
+        CK(cudaMemcpy(s->h, k, sizeof(float) * 3 * ns, cudaMemcpyHostToDevice));
+    } else {
+        CK(cudaMemcpy(s->kappa, kappa, sizeof(double) * ns, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(s->h, hh.data(), sizeof(double) * 3 * ns, cudaMemcpyHostToDevice));
+    }
+    s->sites_set = true;
+    s->tables_dirty = true;
+    return SGB_OK;
+}
+
+int sgb_set_onsite(sgb_system* s, int32_t atom, const double* coeffs) {
+    if (!s || !coeffs) return fail(s, SGB_ERR_ARG, "null argument");
+    if (atom < 0 || atom >= s->d.natoms) return fail(s, SGB_ERR_ARG, "Atom index " + std::to_string(atom + 1) + " is out of range.");
+    if (!s->sun) {
+        // StevensExpansion(c) requires time-reversal invariance: no odd k (Types.jl:18-21)
+        std::copy(coeffs, coeffs + 28, s->onsite_h.begin() + 28 * atom);
+    } else {
+        const int N = s->N;
+        // Hermiticity check, as onsite_coupling (OnsiteCoupling.jl:4)
+        for (int r = 0; r < N; r++)
+            for (int c = 0; c < N; c++) {
+                double ar = coeffs[2 * (r + N * c)], ai = coeffs[2 * (r + N * c) + 1];
+                double br = coeffs[2 * (c + N * r)], bi = coeffs[2 * (c + N * r) + 1];
+                if (std::fabs(ar - br) > 1e-10 * (1 + std::fabs(ar)) || std::fabs(ai + bi) > 1e-10 * (1 + std::fabs(ai)))
+                    return fail(s, SGB_ERR_ARG, "Operator is not Hermitian");
+            }
+        std::copy(coeffs, coeffs + 2 * N * N, s->onsite_h.begin() + (size_t)2 * N * N * atom);
+    }
+    s->tables_dirty = true;
+    return SGB_OK;
+}
+
+int sgb_set_bonds(sgb_system* s, const sgb_bond* bonds, int32_t nbonds) {
+    if (!s || (nbonds > 0 && !bonds) || nbonds < 0) return fail(s, SGB_ERR_ARG, "invalid bond list");
+    for (int k = 0; k < nbonds; k++) {
+        const sgb_bond& b = bonds[k];
+        // validate_bond (PairExchange.jl:1-8)
+        if (b.i == b.j && b.n[0] == 0 && b.n[1] == 0 && b.n[2] == 0) return fail(s, SGB_ERR_ARG, "Bond must connect different atoms.");
+        if (b.i < 0 || b.i >= s->d.natoms) return fail(s, SGB_ERR_ARG, "Atom index " + std::to_string(b.i + 1) + " is out of range.");
+        if (b.j < 0 || b.j >= s->d.natoms) return fail(s, SGB_ERR_ARG, "Atom index " + std::to_string(b.j + 1) + " is out of range.");
+        if (b.biquad_kind < 0 || b.biquad_kind > 2) return fail(s, SGB_ERR_ARG, "biquad_kind must be 0, 1 or 2");
+    }
+    s->bonds_h.assign(bonds, bonds + nbonds);
+    s->bonds_set = true;
+    s->tables_dirty = true;
+    return SGB_OK;
+}
+
+int sgb_set_state(sgb_system* s, const double* dipoles, const double* coherents) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    int rc = ensure_tables(s);
+    if (rc) return rc;
+    const int ns = s->ns;
+    const size_t R = rsize(s);
+    if (!s->sun) {
+        if (!dipoles) return fail(s, SGB_ERR_ARG, "dipoles required in dipole mode");
+        s->stage.resize(std::max(s->stage.size(), R * 3 * (size_t)ns));
+        for (int i = 0; i < ns; i++)
+            for (int c = 0; c < 3; c++) {
+                if (s->fp32) reinterpret_cast<float*>(s->stage.data())[(size_t)c * ns + i] = (float)dipoles[3 * (size_t)i + c];
+                else reinterpret_cast<double*>(s->stage.data())[(size_t)c * ns + i] = dipoles[3 * (size_t)i + c];
+            }
+        CK(cudaMemcpyAsync(s->S, s->stage.data(), R * 3 * ns, cudaMemcpyHostToDevice, s->stream));
+    } else {
+        if (!coherents) return fail(s, SGB_ERR_ARG, "coherents required in SU(N) mode");
+        const int N = s->N;
+        s->stage.resize(std::max(s->stage.size(), R * 2 * N * (size_t)ns));
+        for (int i = 0; i < ns; i++)
+            for (int c = 0; c < 2 * N; c++) {
+                double v = coherents[(size_t)2 * N * i + c];
+                if (s->fp32) reinterpret_cast<float*>(s->stage.data())[(size_t)c * ns + i] = (float)v;
+                else reinterpret_cast<double*>(s->stage.data())[(size_t)c * ns + i] = v;
+            }
+        CK(cudaMemcpyAsync(s->Z, s->stage.data(), R * 2 * N * ns, cudaMemcpyHostToDevice, s->stream));
+        rc = s->fp32 ? do_refresh<float>(s) : do_refresh<double>(s);
+        if (rc) return rc;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    s->state_set = true;
+    return SGB_OK;
+}
+
+int sgb_get_state(sgb_system* s, double* dipoles, double* coherents) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    const int ns = s->ns;
+    const size_t R = rsize(s);
+    if (dipoles) {
+        s->stage.resize(std::max(s->stage.size(), R * 3 * (size_t)ns));
+        CK(cudaMemcpyAsync(s->stage.data(), s->S, R * 3 * ns, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (int i = 0; i < ns; i++)
+            for (int c = 0; c < 3; c++)
+                dipoles[3 * (size_t)i + c] = s->fp32 ? (double)reinterpret_cast<float*>(s->stage.data())[(size_t)c * ns + i]
+                                                     : reinterpret_cast<double*>(s->stage.data())[(size_t)c * ns + i];
+    }
+    if (coherents && s->sun) {
+        const int N = s->N;
+        s->stage.resize(std::max(s->stage.size(), R * 2 * N * (size_t)ns));
+        CK(cudaMemcpyAsync(s->stage.data(), s->Z, R * 2 * N * ns, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (int i = 0; i < ns; i++)
+            for (int c = 0; c < 2 * N; c++)
+                coherents[(size_t)2 * N * i + c] = s->fp32 ? (double)reinterpret_cast<float*>(s->stage.data())[(size_t)c * ns + i]
+                                                           : reinterpret_cast<double*>(s->stage.data())[(size_t)c * ns + i];
+    }
+    return SGB_OK;
+}
+
+int sgb_energy_grad(sgb_system* s, double* grad) {
+    if (!s || !grad) return fail(s, SGB_ERR_ARG, "null argument");
+    int rc = ensure_tables(s);
+    if (rc) return rc;
+    size_t n = s->sun ? (size_t)2 * s->N * s->ns : (size_t)3 * s->ns;
+    if ((rc = ensure_dbuf(s, n))) return rc;
+    if (!s->sun) {
+        rc = s->fp32 ? dip_launch_grad<float>(s->mf, (const float*)s->S, s->dbuf, s->stream)
+                     : dip_launch_grad<double>(s->md, (const double*)s->S, s->dbuf, s->stream);
+    } else {
+        rc = s->fp32 ? sun_launch_grad<float>(s->mf, (const float*)s->Z, (const float*)s->S, (const float*)s->Q, s->dbuf, s->stream)
+                     : sun_launch_grad<double>(s->md, (const double*)s->Z, (const double*)s->S, (const double*)s->Q, s->dbuf, s->stream);
+    }
+    s->launches++;
+    if (rc) return cuda_fail(s, cudaGetLastError(), "gradient launch");
+    CK(cudaMemcpyAsync(grad, s->dbuf, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return SGB_OK;
+}
+
+int sgb_energy(sgb_system* s, double* E, double* M3) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    int rc = ensure_tables(s);
+    if (rc) return rc;
+    int nb = std::min(SGB_ENERGY_BLOCKS, (s->ns + SGB_BLOCK - 1) / SGB_BLOCK);
+    if (!s->sun) {
+        rc = s->fp32 ? dip_launch_energy<float>(s->mf, (const float*)s->S, s->partials, nb, s->stream)
+                     : dip_launch_energy<double>(s->md, (const double*)s->S, s->partials, nb, s->stream);
+    } else {
+        rc = s->fp32 ? sun_launch_energy<float>(s->mf, (const float*)s->Z, (const float*)s->S, (const float*)s->Q, s->partials, nb, s->stream)
+                     : sun_launch_energy<double>(s->md, (const double*)s->Z, (const double*)s->S, (const double*)s->Q, s->partials, nb, s->stream);
+    }
+    s->launches++;
+    if (rc) return cuda_fail(s, cudaGetLastError(), "energy launch");
+    if ((rc = util_launch_reduce(s->partials, nb, 4, s->red, s->stream))) return cuda_fail(s, cudaGetLastError(), "reduce launch");
+    s->launches++;
+    double out[4];
+    CK(cudaMemcpyAsync(out, s->red, sizeof(out), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (E) *E = out[0];
+    if (M3) { M3[0] = out[1]; M3[1] = out[2]; M3[2] = out[3]; }
+    return SGB_OK;
+}
+
+int sgb_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t seed, uint64_t step0, int32_t nsteps,
+                 const double* noise) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    // Langevin constructor checks (src/Integrators.jl:61-73)
+    if (damping == 0.0) return fail(s, SGB_ERR_ARG, "Use ImplicitMidpoint instead for energy-conserving dynamics");
+    if (!(dt > 0)) return fail(s, SGB_ERR_ARG, "Select positive dt");
+    if (kT < 0) return fail(s, SGB_ERR_ARG, "Select nonnegative kT");
+    if (damping < 0) return fail(s, SGB_ERR_ARG, "Select positive damping");
+    if (nsteps < 0) return fail(s, SGB_ERR_ARG, "nsteps must be nonnegative");
+    if (nsteps == 0) return SGB_OK;
+    int rc = ensure_tables(s);
+    if (rc) return rc;
+    if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called before stepping");
+    return s->fp32 ? run_langevin<float>(s, dt, damping, kT, seed, step0, nsteps, noise)
+                   : run_langevin<double>(s, dt, damping, kT, seed, step0, nsteps, noise);
+}
+
+int sgb_langevin_noise(sgb_system* s, uint64_t seed, uint64_t step, double* out) {
+    if (!s || !out) return fail(s, SGB_ERR_ARG, "null argument");
+    size_t n = s->sun ? (size_t)2 * s->N * s->ns : (size_t)3 * s->ns;
+    int rc = ensure_dbuf(s, n);
+    if (rc) return rc;
+    rc = s->fp32 ? util_launch_noise_export<float>(s->sun, s->N, s->ns, seed, step, s->dbuf, s->stream)
+                 : util_launch_noise_export<double>(s->sun, s->N, s->ns, seed, step, s->dbuf, s->stream);
+    s->launches++;
+    if (rc) return cuda_fail(s, cudaGetLastError(), "noise launch");
+    CK(cudaMemcpyAsync(out, s->dbuf, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return SGB_OK;
+}
+
+int sgb_midpoint(sgb_system* s, double dt, double damping, double tol, int32_t max_iters, int32_t nsteps, int64_t* iters_out) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    // ImplicitMidpoint constructor checks (src/Integrators.jl:113-130)
+    if (!(dt > 0)) return fail(s, SGB_ERR_ARG, "Select positive dt");
+    if (damping < 0) return fail(s, SGB_ERR_ARG, "Select nonnegative damping");
+    if (tol < 0 || max_iters < 1 || nsteps < 0) return fail(s, SGB_ERR_ARG, "invalid tol, max_iters or nsteps");
+    if (iters_out) *iters_out = 0;
+    if (nsteps == 0) return SGB_OK;
+    int rc = ensure_tables(s);
+    if (rc) return rc;
+    if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called before stepping");
+    if (s->fp32) {
+        SnapArgs<float> sn{};
+        return run_midpoint<float>(s, dt, damping, tol, max_iters, nsteps, iters_out, sn);
+    }
+    SnapArgs<double> sn{};
+    return run_midpoint<double>(s, dt, damping, tol, max_iters, nsteps, iters_out, sn);
+}
+
+int sgb_event_record(sgb_system* s, int32_t slot) {
+    if (!s || slot < 0 || slot >= 8) return fail(s, SGB_ERR_ARG, "bad event slot");
+    CK(cudaEventRecord(s->ev[slot], s->stream));
+    return SGB_OK;
+}
+
+int sgb_event_elapsed(sgb_system* s, int32_t a, int32_t b, float* ms) {
+    if (!s || !ms || a < 0 || a >= 8 || b < 0 || b >= 8) return fail(s, SGB_ERR_ARG, "bad event slot");
+    CK(cudaEventSynchronize(s->ev[b]));
+    CK(cudaEventElapsedTime(ms, s->ev[a], s->ev[b]));
+    return SGB_OK;
+}
+
+int sgb_synchronize(sgb_system* s) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    CK(cudaStreamSynchronize(s->stream));
+    return SGB_OK;
+}
+
+int64_t sgb_kernel_launches(const sgb_system* s) { return s ? s->launches : 0; }
+
+int sgb_flush_l2(sgb_system* s) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    const size_t bytes = (size_t)256 << 20;
+    if (!s->flush) {
+        int rc = dmalloc(s, &s->flush, bytes);
+        if (rc) return rc;
+    }
+    CK(cudaMemsetAsync(s->flush, s->launches & 0xff, bytes, s->stream));
+    return SGB_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// SampledCorrelations
+// ---------------------------------------------------------------------------------
+static int cfail(sgb_corr* c, int code, const std::string& msg) {
+    if (c) { c->err = msg; if (c->sys) c->sys->err = msg; }
+    g_last_error = msg;
+    return code;
+}
+
+void sgb_corr_destroy(sgb_corr* c) {
+    if (!c) return;
+    if (c->sys && c->sys->stream) cudaStreamSynchronize(c->sys->stream);
+    dfree(c->ops);
+    void* p = c->pairs; dfree(p);
+    dfree(c->A); dfree(c->Ahat);
+    p = c->P; dfree(p);
+    p = c->g; dfree(p);
+    if (c->have_space) cufftDestroy(c->plan_space);
+    if (c->have_time) cufftDestroy(c->plan_time);
+    delete c;
+}
+
+int sgb_corr_create(sgb_system* s, const sgb_corr_desc* d, sgb_corr** out) {
+    if (!s || !d || !out) return fail(s, SGB_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (d->nobs < 1 || d->ncorr < 1 || !d->obs || !d->pairs) return fail(s, SGB_ERR_ARG, "observables and correlation pairs are required");
+    if (d->n_all_omega < 1 || d->measperiod < 1) return fail(s, SGB_ERR_ARG, "n_all_omega and measperiod must be positive");
+    if (d->n_all_omega > 1 && !(d->dt > 0)) return fail(s, SGB_ERR_ARG, "Select positive dt");
+    if (d->calculate_errors) return fail(s, SGB_ERR_ARG, "calculate_errors is not supported by this build of the accumulator");
+    for (int k = 0; k < 2 * d->ncorr; k++)
+        if (d->pairs[k] < 0 || d->pairs[k] >= d->nobs) return fail(s, SGB_ERR_ARG, "correlation pair index out of range");
+    int rc = ensure_tables(s);
+    if (rc) return rc;
+    sgb_corr* c = new sgb_corr();
+    c->sys = s;
+    c->nobs = d->nobs; c->ncorr = d->ncorr; c->npos = s->d.natoms; c->ncell = s->ncell;
+    c->nomega = d->n_all_omega;
+    c->nsnaps = d->n_all_omega / 2 + 1;   // CorrelationSampling.jl:37-38
+    c->measperiod = d->measperiod;
+    c->dt = d->dt; c->damping = d->damping; c->tol = d->tol; c->max_iters = d->max_iters;
+    const int ns = s->ns, N = s->N;
+    const size_t R = rsize(s);
+    auto bad = [&](int code) { sgb_corr_destroy(c); return code; };
+    // observables, device layout dipole [nobs][3][ns], SU(N) [nobs][N*N][2][ns]
+    size_t per = s->sun ? (size_t)2 * N * N : 3;
+    std::vector<char> host(R * per * d->nobs * ns);
+    for (int o = 0; o < d->nobs; o++)
+        for (int i = 0; i < ns; i++)
+            for (size_t k = 0; k < per; k++) {
+                double v = d->obs[((size_t)o * ns + i) * per + k];
+                size_t idx = ((size_t)o * per + k) * ns + i;
+                if (s->fp32) reinterpret_cast<float*>(host.data())[idx] = (float)v;
+                else reinterpret_cast<double*>(host.data())[idx] = v;
+            }
+    if ((rc = dmalloc(s, &c->ops, host.size()))) return bad(rc);
+    if (cudaMemcpy(c->ops, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) return bad(fail(s, SGB_ERR_CUDA, "copy observables"));
+    if ((rc = dmalloc(s, (void**)&c->pairs, sizeof(int) * 2 * d->ncorr))) return bad(rc);
+    cudaMemcpy(c->pairs, d->pairs, sizeof(int) * 2 * d->ncorr, cudaMemcpyHostToDevice);
+    size_t nA = (size_t)c->nomega * c->nobs * c->npos * c->ncell;  // complex elements
+    if ((rc = dmalloc(s, &c->A, 2 * R * nA))) return bad(rc);
+    if ((rc = dmalloc(s, &c->Ahat, 2 * R * nA))) return bad(rc);
+    cudaMemset(c->A, 0, 2 * R * nA);
+    c->plen = (size_t)c->nomega * c->ncell * c->npos * c->npos * c->ncorr;
+    if ((rc = dmalloc(s, (void**)&c->P, 16 * c->plen))) return bad(rc);
+    cudaMemset(c->P, 0, 16 * c->plen);
+    if ((rc = dmalloc(s, (void**)&c->g, sizeof(double) * c->nomega))) return bad(rc);
+    // cuFFT plans: space FFT over (L3, L2, L1) for every snapshot row; time FFT along ω
+    const cufftType ty = s->fp32 ? CUFFT_C2C : CUFFT_Z2Z;
+    int n3[3] = {s->d.dims[2], s->d.dims[1], s->d.dims[0]};
+    int batch_space = c->nsnaps * c->nobs * c->npos;
+    if (cufftPlanMany(&c->plan_space, 3, n3, nullptr, 1, c->ncell, nullptr, 1, c->ncell, ty, batch_space) != CUFFT_SUCCESS)
+        return bad(fail(s, SGB_ERR_CUDA, "cufftPlanMany (space) failed"));
+    c->have_space = true;
+    cufftSetStream(c->plan_space, s->stream);
+    if (c->nomega > 1) {
+        int n1[1] = {c->nomega};
+        int stride = c->nobs * c->npos * c->ncell;
+        if (cufftPlanMany(&c->plan_time, 1, n1, n1, stride, 1, n1, stride, 1, ty, stride) != CUFFT_SUCCESS)
+            return bad(fail(s, SGB_ERR_CUDA, "cufftPlanMany (time) failed"));
+        c->have_time = true;
+        cufftSetStream(c->plan_time, s->stream);
+    }
+    *out = c;
+    return SGB_OK;
+}
+
+// window(t)/n_contrib(t)/n for the read-out transform (CorrelationSampling.jl:52-107)
+static void window_weights(int n, int window, std::vector<double>& g) {
+    g.assign(n, 0.0);
+    int T = n / 2 + 1;
+    for (int k = 0; k < n; k++) {
+        // FFTW.fftfreq(n, n): 0..ceil(n/2)-1 then negative
+        int dtk = (k < (n + 1) / 2) ? k : k - n;
+        int contrib = T - std::abs(dtk);
+        double w = 1.0;
+        if (window == 0) {
+            double c = std::cos(M_PI * k / n);
+            w = c * c;
+        }
+        g[k] = contrib <= 0 ? 0.0 : w / contrib / n;
+    }
+}
+
+int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
+    if (!c) return fail(nullptr, SGB_ERR_ARG, "null handle");
+    sgb_system* s = c->sys;
+    if (window != 0 && window != 1) return cfail(c, SGB_ERR_ARG, "window must be 0 (:cosine) or 1 (:rectangular)");
+    if (c->window >= 0 && c->window != window)
+        return cfail(c, SGB_ERR_ARG, "all samples of one accumulator must use the same window");
+    if (!s->state_set) return cfail(c, SGB_ERR_STATE, "sgb_set_state must be called before add_sample");
+    int rc = ensure_tables(s);
+    if (rc) return rc;
+    if (c->window < 0) {
+        std::vector<double> g;
+        window_weights(c->nomega, window, g);
+        if (cudaMemcpy(c->g, g.data(), sizeof(double) * c->nomega, cudaMemcpyHostToDevice) != cudaSuccess)
+            return cfail(c, SGB_ERR_CUDA, "copy window");
+        c->window = window;
+    }
+    const int nsteps = c->measperiod * (c->nsnaps - 1);
+    const double scale = 1.0 / std::sqrt((double)c->ncell);
+    // 1. trajectory with fused observable snapshots (CorrelationSampling.jl:21-46)
+    if (s->fp32) {
+        SnapArgs<float> sn{1, c->nobs, c->measperiod, 0, (const float*)c->ops, (float*)c->A, (float)scale};
+        if (nsteps > 0) rc = run_midpoint<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, nullptr, sn, true);
+        else rc = run_midpoint<float>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
+    } else {
+        SnapArgs<double> sn{1, c->nobs, c->measperiod, 0, (const double*)c->ops, (double*)c->A, scale};
+        if (nsteps > 0) rc = run_midpoint<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, nullptr, sn, true);
+        else rc = run_midpoint<double>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
+    }
+    if (rc) return rc;
+    // 2. space FFT, A(q) = sum_r exp(+iqr) A(r) / sqrt(Ncell) (CorrelationSampling.jl:58-63)
+    cufftResult fr;
+    if (s->fp32) fr = cufftExecC2C(c->plan_space, (cufftComplex*)c->A, (cufftComplex*)c->A, CUFFT_INVERSE);
+    else fr = cufftExecZ2Z(c->plan_space, (cufftDoubleComplex*)c->A, (cufftDoubleComplex*)c->A, CUFFT_INVERSE);
+    if (fr != CUFFT_SUCCESS) return cfail(c, SGB_ERR_CUDA, "space FFT failed");
+    // 3. time FFT, A(ω) = sum_t exp(-iωt) A(t), zero padded (CorrelationSampling.jl:65-69)
+    const void* spec = c->A;
+    if (c->have_time) {
+        if (s->fp32) fr = cufftExecC2C(c->plan_time, (cufftComplex*)c->A, (cufftComplex*)c->Ahat, CUFFT_FORWARD);
+        else fr = cufftExecZ2Z(c->plan_time, (cufftDoubleComplex*)c->A, (cufftDoubleComplex*)c->Ahat, CUFFT_FORWARD);
+        if (fr != CUFFT_SUCCESS) return cfail(c, SGB_ERR_CUDA, "time FFT failed");
+        spec = c->Ahat;
+    }
+    // 4. accumulate conj(A_alpha,i) A_beta,j into the FP64 sum
+    rc = s->fp32 ? corr_launch_accum<float>((const float*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, c->nomega, s->stream)
+                 : corr_launch_accum<double>((const double*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, c->nomega, s->stream);
+    s->launches++;
+    if (rc) return cfail(c, SGB_ERR_CUDA, std::string("accumulate launch: ") + cudaGetErrorString(cudaGetLastError()));
+    c->nsamples += 1;
+    return SGB_OK;
+}
+
+int sgb_corr_data(sgb_corr* c, double* data, double* M, int64_t* nsamples) {
+    if (!c) return fail(nullptr, SGB_ERR_ARG, "null handle");
+    sgb_system* s = c->sys;
+    if (nsamples) *nsamples = c->nsamples;
+    if (M) return cfail(c, SGB_ERR_ARG, "calculate_errors is not supported by this build of the accumulator");
+    if (!data) return SGB_OK;
+    const int n = c->nomega;
+    const size_t ld = c->plen / n;  // columns
+    if (c->nsamples == 0) {
+        std::memset(data, 0, 16 * c->plen);
+        return SGB_OK;
+    }
+    const double inv = 1.0 / (double)c->nsamples;
+    if (n == 1) {
+        // static: data = P / nsamples (window weight 1 at Δt = 0)
+        std::vector<double> tmp(2 * c->plen);
+        if (cudaMemcpy(tmp.data(), c->P, 16 * c->plen, cudaMemcpyDeviceToHost) != cudaSuccess) return cfail(c, SGB_ERR_CUDA, "copy data");
+        for (size_t k = 0; k < 2 * c->plen; k++) data[k] = tmp[k] * inv;
+        return SGB_OK;
+    }
+    // chunked read-out transform: IFFT_ω -> × window/n_contrib/n -> FFT_ω
+    size_t chunk = std::max<size_t>(1, ((size_t)64 << 20) / ((size_t)16 * n));
+    chunk = std::min(chunk, ld);
+    double *tmp = nullptr, *outb = nullptr;
+    int rc = dmalloc(s, (void**)&tmp, 16 * chunk * n);
+    if (rc) return rc;
+    rc = dmalloc(s, (void**)&outb, 16 * chunk * n);
+    if (rc) { cudaFree(tmp); return rc; }
+    cufftHandle plan;
+    int n1[1] = {n};
+    if (cufftPlanMany(&plan, 1, n1, nullptr, 1, n, nullptr, 1, n, CUFFT_Z2Z, (int)chunk) != CUFFT_SUCCESS) {
+        cudaFree(tmp); cudaFree(outb);
+        return cfail(c, SGB_ERR_CUDA, "cufftPlanMany (read-out) failed");
+    }
+    cufftSetStream(plan, s->stream);
+    int status = SGB_OK;
+    for (size_t col0 = 0; col0 < ld && status == SGB_OK; col0 += chunk) {
+        int ncol = (int)std::min(chunk, ld - col0);
+        if (corr_launch_gather(c->P, ld, col0, ncol, n, inv, tmp, s->stream)) { status = SGB_ERR_CUDA; break; }
+        if (cufftExecZ2Z(plan, (cufftDoubleComplex*)tmp, (cufftDoubleComplex*)tmp, CUFFT_INVERSE) != CUFFT_SUCCESS) { status = SGB_ERR_CUDA; break; }
+        if (corr_launch_window(tmp, ncol, n, c->g, s->stream)) { status = SGB_ERR_CUDA; break; }
+        if (cufftExecZ2Z(plan, (cufftDoubleComplex*)tmp, (cufftDoubleComplex*)tmp, CUFFT_FORWARD) != CUFFT_SUCCESS) { status = SGB_ERR_CUDA; break; }
+        if (corr_launch_scatter(tmp, ncol, n, outb, s->stream)) { status = SGB_ERR_CUDA; break; }
+        s->launches += 3;
+        if (cudaMemcpy2DAsync(data + 2 * col0, 16 * ld, outb, 16 * (size_t)ncol, 16 * (size_t)ncol, n, cudaMemcpyDeviceToHost,
+                              s->stream) != cudaSuccess) { status = SGB_ERR_CUDA; break; }
+    }
+    cudaStreamSynchronize(s->stream);
+    cufftDestroy(plan);
+    cudaFree(tmp);
+    cudaFree(outb);
+    if (status != SGB_OK) return cfail(c, status, "read-out transform failed");
+    return SGB_OK;
+}
+
+int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src) {
+    if (!dst || !src) return fail(nullptr, SGB_ERR_ARG, "null handle");
+    if (dst->plen != src->plen || dst->nomega != src->nomega || dst->ncorr != src->ncorr)
+        return cfail(dst, SGB_ERR_ARG, "accumulators have different shapes");
+    if (src->nsamples > 0 && dst->window >= 0 && src->window >= 0 && dst->window != src->window)
+        return cfail(dst, SGB_ERR_ARG, "accumulators used different windows");
+    sgb_system* s = dst->sys;
+    if (src->sys != dst->sys) cudaStreamSynchronize(src->sys->stream);
+    if (corr_launch_add(dst->P, src->P, 2 * dst->plen, s->stream) != SGB_OK) return cfail(dst, SGB_ERR_CUDA, "merge launch");
+    s->launches++;
+    if (dst->window < 0 && src->window >= 0) {
+        dst->window = src->window;
+        cudaMemcpyAsync(dst->g, src->g, sizeof(double) * dst->nomega, cudaMemcpyDeviceToDevice, s->stream);
+    }
+    dst->nsamples += src->nsamples;
+    cudaStreamSynchronize(s->stream);
+    return SGB_OK;
+}
+
+}  // extern "C"

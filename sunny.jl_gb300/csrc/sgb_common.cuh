@@ -1,0 +1,206 @@
+// sgb_common.cuh -- device-side building blocks shared by the sm_103a kernels of
+// libsunnygb300: precision traits, the coupling tables staged in shared memory, the
+// bounded inter-CTA barrier used by the persistent kernels, and the Philox-4x32-10
+// counter-based Gaussian source for Langevin noise.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <cuda/atomic>
+#include "../../include/sunny_gb300.h"
+
+#define SGB_MAX_SUBLAT 64
+#define SGB_MAX_N 5
+
+// ---------------------------------------------------------------------------------
+// Coupling tables. One DBond is a directed bond seen from its first atom; the library
+// stores both directions of every Sunny PairCoupling so that the gradient is a gather
+// (each site sums over its own bond list), which equals Sunny's scatter over non-culled
+// bonds (src/System/Interactions.jl:554-591).
+// ---------------------------------------------------------------------------------
+template <class R>
+struct DBond {
+    R J[9];          // column-major 3x3 (already transposed for reverse copies)
+    R scalar;        // constant shift (energy only)
+    R bq;            // isotropic biquadratic strength (kind 1)
+    int j;           // target atom
+    int n[3];        // cell offset, reduced mod dims into [0, L) for single systems
+    int jkind;       // 0: J = J[0] * identity, 1: full 3x3
+    int bqkind;      // 0 none, 1 isotropic, 2 matrix (index bqidx)
+    int bqidx;       // row in the 5x5 biquadratic table
+    int fwd;         // 1 for the non-culled copy (counted in the energy)
+};
+
+// Sunny's scalar_biquad_metric (src/System/Types.jl:40)
+__host__ __device__ inline double biquad_metric(int q) {
+    return q == 0 ? 0.5 : q == 1 ? 2.0 : q == 2 ? (1.0 / 6.0) : q == 3 ? 2.0 : 0.5;
+}
+
+// ---------------------------------------------------------------------------------
+// Status word and bounded waits. Every wait has a wall-clock limit read from
+// %globaltimer; on expiry the kernel records SGB_ERR_TIMEOUT and returns, so that a
+// stuck barrier never hangs the GPU.
+// ---------------------------------------------------------------------------------
+struct Ctrl {
+    unsigned int bar_count;
+    unsigned int bar_gen;
+    int status;
+    int steps_done;
+    long long iters;
+    double acc[3];       // rotating FP64 convergence accumulators
+    int final_buf;
+    int pad;
+};
+
+__device__ __forceinline__ uint64_t sgb_globaltimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void sgb_set_status(Ctrl* c, int code) {
+    atomicCAS(&c->status, 0, code);
+}
+
+__device__ __forceinline__ int sgb_read_status(Ctrl* c) {
+    return cuda::atomic_ref<int, cuda::thread_scope_device>(c->status).load(cuda::memory_order_relaxed);
+}
+
+#define SGB_BARRIER_TIMEOUT_NS 4000000000ull
+
+// Barrier across `nblocks` co-resident CTAs (cooperative launch guarantees residency).
+// Returns false if the wait timed out or another CTA flagged an error.
+__device__ __forceinline__ bool sgb_grid_barrier(Ctrl* c, unsigned int nblocks) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        if (nblocks > 1) {
+            cuda::atomic_ref<unsigned int, cuda::thread_scope_device> cnt(c->bar_count);
+            cuda::atomic_ref<unsigned int, cuda::thread_scope_device> gen(c->bar_gen);
+            __threadfence();
+            unsigned int g = gen.load(cuda::memory_order_acquire);
+            unsigned int prev = cnt.fetch_add(1u, cuda::memory_order_acq_rel);
+            if (prev == nblocks - 1) {
+                cnt.store(0u, cuda::memory_order_relaxed);
+                gen.fetch_add(1u, cuda::memory_order_release);
+            } else {
+                uint64_t t0 = sgb_globaltimer();
+                while (gen.load(cuda::memory_order_acquire) == g) {
+                    __nanosleep(32);
+                    if (sgb_globaltimer() - t0 > SGB_BARRIER_TIMEOUT_NS) {
+                        sgb_set_status(c, SGB_ERR_TIMEOUT);
+                        ok = 0;
+                        break;
+                    }
+                }
+            }
+            __threadfence();
+        }
+        if (ok && sgb_read_status(c) != 0) ok = 0;
+        ok_s = ok;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+// ---------------------------------------------------------------------------------
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and Box-Muller.
+// ---------------------------------------------------------------------------------
+struct Philox4 { uint32_t x, y, z, w; };
+
+__host__ __device__ inline uint32_t sgb_mulhi32(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
+__host__ __device__ inline Philox4 sgb_philox(Philox4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0 = sgb_mulhi32(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        uint32_t hi1 = sgb_mulhi32(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        Philox4 n;
+        n.x = hi1 ^ c.y ^ k0;
+        n.y = lo1;
+        n.z = hi0 ^ c.w ^ k1;
+        n.w = lo0;
+        c = n;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Four standard normals for (seed, stream, step, site, block of 4 components).
+template <class R>
+__device__ inline void sgb_normals4(uint64_t seed, uint32_t stream, uint64_t step, uint32_t site,
+                                    uint32_t blk, R out[4]) {
+    Philox4 c;
+    c.x = site;
+    c.y = (uint32_t)step;
+    c.z = (uint32_t)(step >> 32) ^ (blk << 24);
+    c.w = stream;
+    Philox4 r = sgb_philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    if constexpr (sizeof(R) == 8) {
+        const double s = 2.3283064365386963e-10;  // 2^-32
+        double u1 = ((double)r.x + 1.0) * s, u2 = (double)r.y * s;
+        double u3 = ((double)r.z + 1.0) * s, u4 = (double)r.w * s;
+        double a = sqrt(-2.0 * log(u1)), b = sqrt(-2.0 * log(u3));
+        double s1, c1, s2, c2;
+        sincospi(2.0 * u2, &s1, &c1);
+        sincospi(2.0 * u4, &s2, &c2);
+        out[0] = a * c1; out[1] = a * s1; out[2] = b * c2; out[3] = b * s2;
+    } else {
+        const float s = 2.3283064365386963e-10f;
+        float u1 = ((float)r.x + 1.0f) * s, u2 = (float)r.y * s;
+        float u3 = ((float)r.z + 1.0f) * s, u4 = (float)r.w * s;
+        u1 = fminf(u1, 1.0f); u3 = fminf(u3, 1.0f);
+        float a = sqrtf(-2.0f * logf(u1)), b = sqrtf(-2.0f * logf(u3));
+        float s1, c1, s2, c2;
+        sincospif(2.0f * u2, &s1, &c1);
+        sincospif(2.0f * u4, &s2, &c2);
+        out[0] = a * c1; out[1] = a * s1; out[2] = b * c2; out[3] = b * s2;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Small helpers
+// ---------------------------------------------------------------------------------
+template <class R> __device__ __forceinline__ R sgb_ld(const R* p) { return __ldcg(p); }
+
+template <class R> __device__ __forceinline__ R sgb_rsqrt(R x);
+template <> __device__ __forceinline__ float sgb_rsqrt<float>(float x) { return rsqrtf(x); }
+template <> __device__ __forceinline__ double sgb_rsqrt<double>(double x) { return 1.0 / sqrt(x); }
+
+template <class R> __device__ __forceinline__ R sgb_sqrt(R x);
+template <> __device__ __forceinline__ float sgb_sqrt<float>(float x) { return sqrtf(x); }
+template <> __device__ __forceinline__ double sgb_sqrt<double>(double x) { return sqrt(x); }
+
+// wrap x = c + n with c in [0, L) and n already reduced into [0, L)
+__device__ __forceinline__ int sgb_wrap_pos(int x, int L) { return x >= L ? x - L : x; }
+// wrap for |n| <= L (replica batches, where n is not pre-reduced)
+__device__ __forceinline__ int sgb_wrap_any(int x, int L) {
+    x = x < 0 ? x + L : x;
+    return x >= L ? x - L : x;
+}
+
+// block-wide FP64 sum; result valid in thread 0
+template <int BLOCK>
+__device__ inline double sgb_block_sum(double v) {
+    __shared__ double red[BLOCK / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x < 32) {
+        r = threadIdx.x < BLOCK / 32 ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+    }
+    return r;
+}

@@ -1,0 +1,156 @@
+// sgb_corr.cu -- SampledCorrelations accumulation kernels for sm_103a.
+//
+// Reference: src/SampledCorrelations/CorrelationSampling.jl:48-139 (accum_sample!) and
+// src/SampledCorrelations/SampledCorrelations.jl:128-142 (merge_correlations).
+//
+// Sunny computes, per sample and per (c, i, j):
+//     C(q, ω) = FFT_t[ w(t)/n(t) * IFFT_t[ conj(A_αi(q, ω)) A_βj(q, ω) ] ]
+// and folds C into a running mean. Every operation after the product is linear and
+// identical for every sample, so the mean of C equals the same transform applied to the
+// mean of the products. The library therefore streams only
+//     P(c,i,j,q,ω) += conj(A_αi(q,ω)) A_βj(q,ω)          (FP64 sum, one pass per sample)
+// over the accumulator, which makes add_sample! a single coalesced read+write of the
+// accumulator, and applies IFFT -> window/n(t) -> FFT once, when the data are read.
+//
+// Layouts:
+//   sample spectra  A[n_all_omega][nobs][npos][ncell]  complex R
+//   accumulator     P[n_all_omega][ncell][npos(j)][npos(i)][ncorr]  complex double
+//                   (identical to Sunny's column-major data[c, i, j, q1, q2, q3, ω])
+#include "sgb_corr.h"
+#include <cufft.h>
+
+namespace {
+
+template <class R> struct C2 { R x, y; };
+
+// One CTA handles one ω and QT consecutive wave vectors: it stages the QT x nobs x npos
+// complex spectra in shared memory and then streams the contiguous QT*B accumulator
+// entries (B = ncorr*npos*npos), coalesced, with streaming cache hints.
+template <class R, int QT>
+__global__ void __launch_bounds__(256) k_corr_accum(const R* __restrict__ A, double* __restrict__ P,
+                                                  const int* __restrict__ pairs, int ncorr, int nobs, int npos,
+                                                  int ncell, int nomega) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* As = reinterpret_cast<C2<R>*>(smem_raw);          // [nobs*npos][QT]
+    int* pr = reinterpret_cast<int*>(As + (size_t)nobs * npos * QT);
+    const int w = blockIdx.y;
+    const int q0 = blockIdx.x * QT;
+    const int nq = min(QT, ncell - q0);
+    const int nrow = nobs * npos;
+    for (int e = threadIdx.x; e < nrow * QT; e += blockDim.x) {
+        int row = e / QT, ql = e % QT;
+        C2<R> v = {0, 0};
+        if (ql < nq) {
+            size_t idx = ((size_t)w * nrow + row) * ncell + q0 + ql;
+            v.x = A[2 * idx];
+            v.y = A[2 * idx + 1];
+        }
+        As[row * QT + ql] = v;
+    }
+    for (int e = threadIdx.x; e < 2 * ncorr; e += blockDim.x) pr[e] = pairs[e];
+    __syncthreads();
+    const int B = ncorr * npos * npos;
+    const size_t base = ((size_t)w * ncell + q0) * B;
+    const int total = nq * B;
+    double2* out = reinterpret_cast<double2*>(P) + base;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        int ql = e / B, r = e - ql * B;
+        int c = r % ncorr;
+        int t = r / ncorr;
+        int i = t % npos, j = t / npos;
+        C2<R> a = As[(pr[2 * c] * npos + i) * QT + ql];
+        C2<R> b = As[(pr[2 * c + 1] * npos + j) * QT + ql];
+        // conj(a) * b
+        double re = (double)(a.x * b.x + a.y * b.y);
+        double im = (double)(a.x * b.y - a.y * b.x);
+        double2 acc = __ldcs(out + e);
+        acc.x += re;
+        acc.y += im;
+        __stcs(out + e, acc);
+    }
+}
+
+// Gather `ncol` accumulator columns (stride `ld` along ω) starting at column col0 into
+// tmp[ncol][n] and scale by 1/nsamples.
+__global__ void k_gather_cols(const double2* __restrict__ P, size_t ld, size_t col0, int ncol, int n, double scale,
+                              double2* __restrict__ tmp) {
+    size_t total = (size_t)ncol * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        int w = (int)(e / ncol), c = (int)(e % ncol);
+        double2 v = P[(size_t)w * ld + col0 + c];
+        v.x *= scale; v.y *= scale;
+        tmp[(size_t)c * n + w] = v;
+    }
+}
+
+// tmp[c][t] *= g[t]   (g = window(t) / n_contrib(t) / n, CorrelationSampling.jl:74-107)
+__global__ void k_apply_window(double2* tmp, int ncol, int n, const double* __restrict__ g) {
+    size_t total = (size_t)ncol * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        double s = g[e % n];
+        tmp[e].x *= s;
+        tmp[e].y *= s;
+    }
+}
+
+// Transpose tmp[ncol][n] back to out[n][ncol] (ω-major, as Sunny's data layout).
+__global__ void k_scatter_cols(const double2* __restrict__ tmp, int ncol, int n, double2* __restrict__ out) {
+    size_t total = (size_t)ncol * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        int w = (int)(e / ncol), c = (int)(e % ncol);
+        out[e] = tmp[(size_t)c * n + w];
+    }
+}
+
+__global__ void k_add_inplace(double* __restrict__ dst, const double* __restrict__ src, size_t n) {
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+        dst[e] += src[e];
+}
+
+int grid_for(size_t n) {
+    size_t g = (n + 255) / 256;
+    if (g > 65535) g = 65535;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+template <class R>
+int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
+                      cudaStream_t st) {
+    constexpr int QT = 32;
+    size_t smem = (size_t)nobs * npos * QT * sizeof(C2<R>) + 2 * ncorr * sizeof(int) + 16;
+    if (smem > 48 * 1024) {
+        if (cudaFuncSetAttribute(k_corr_accum<R, QT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return SGB_ERR_CUDA;
+    }
+    dim3 grid((ncell + QT - 1) / QT, nomega);
+    k_corr_accum<R, QT><<<grid, 256, smem, st>>>(A, P, pairs, ncorr, nobs, npos, ncell, nomega);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+int corr_launch_gather(const double* P, size_t ld, size_t col0, int ncol, int n, double scale, double* tmp, cudaStream_t st) {
+    k_gather_cols<<<grid_for((size_t)ncol * n), 256, 0, st>>>(reinterpret_cast<const double2*>(P), ld, col0, ncol, n,
+                                                                scale, reinterpret_cast<double2*>(tmp));
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+int corr_launch_window(double* tmp, int ncol, int n, const double* g, cudaStream_t st) {
+    k_apply_window<<<grid_for((size_t)ncol * n), 256, 0, st>>>(reinterpret_cast<double2*>(tmp), ncol, n, g);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+int corr_launch_scatter(const double* tmp, int ncol, int n, double* out, cudaStream_t st) {
+    k_scatter_cols<<<grid_for((size_t)ncol * n), 256, 0, st>>>(reinterpret_cast<const double2*>(tmp), ncol, n,
+                                                                 reinterpret_cast<double2*>(out));
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+int corr_launch_add(double* dst, const double* src, size_t n, cudaStream_t st) {
+    k_add_inplace<<<grid_for(n), 256, 0, st>>>(dst, src, n);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+template int corr_launch_accum<float>(const float*, double*, const int*, int, int, int, int, int, cudaStream_t);
+template int corr_launch_accum<double>(const double*, double*, const int*, int, int, int, int, int, cudaStream_t);

@@ -1,0 +1,13 @@
+// sgb_corr.h -- launchers of the correlation kernels (sgb_corr.cu). Internal.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include "../../include/sunny_gb300.h"
+
+template <class R>
+int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
+                      cudaStream_t st);
+int corr_launch_gather(const double* P, size_t ld, size_t col0, int ncol, int n, double scale, double* tmp, cudaStream_t st);
+int corr_launch_window(double* tmp, int ncol, int n, const double* g, cudaStream_t st);
+int corr_launch_scatter(const double* tmp, int ncol, int n, double* out, cudaStream_t st);
+int corr_launch_add(double* dst, const double* src, size_t n, cudaStream_t st);

@@ -1,0 +1,218 @@
+// sgb_device.cuh -- device functions shared by the dipole, SU(N) and replica-batch
+// kernels: coupling-table staging, the gather-form dipole gradient, the classical
+// Stevens anisotropy and the Landau-Lifshitz right-hand side.
+//
+// Reference algorithms (Sunny.jl v0.9.2):
+//   gradient      src/System/Interactions.jl:516-592
+//   anisotropy    src/System/OnsiteCoupling.jl:316-425
+//   quadrupoles   src/Operators/Spin.jl:48-69
+//   rhs_dipole!   src/Integrators.jl:266-275
+//   normalization src/System/System.jl:416-423
+#pragma once
+#include "sgb_internal.h"
+
+namespace sgbdev {
+
+template <class R>
+struct Tab {
+    const R* stev;
+    const int* kmax;
+    const int* boff;
+    const DBond<R>* bonds;
+    const R* bq;
+};
+
+template <class R>
+__device__ inline Tab<R> stage_tables(const Model<R>& M, unsigned char* smem) {
+    const uint4* src = reinterpret_cast<const uint4*>(M.tables);
+    uint4* dst = reinterpret_cast<uint4*>(smem);
+    int n16 = M.tables_bytes / 16;
+    for (int i = threadIdx.x; i < n16; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    Tab<R> t;
+    t.stev = reinterpret_cast<const R*>(smem + M.off_stev);
+    t.kmax = reinterpret_cast<const int*>(smem + M.off_kmax);
+    t.boff = reinterpret_cast<const int*>(smem + M.off_boff);
+    t.bonds = reinterpret_cast<const DBond<R>*>(smem + M.off_bonds);
+    t.bq = reinterpret_cast<const R*>(smem + M.off_bq);
+    return t;
+}
+
+// Classical Stevens anisotropy, OnsiteCoupling.jl:316-425. Coefficients c (28) hold
+// c0, c2[5], c4[9], c6[13] in descending q. Adds the gradient into g and returns E.
+template <class R>
+__device__ inline R aniso_k(const R* c, int k, const R* A, const R* dA, const R* pr, const R* pi,
+                            R& E, R& dz, R& jr, R& ji) {
+    // m = 0
+    E += c[k] * A[0];
+    dz += c[k] * dA[0];
+#pragma unroll
+    for (int m = 1; m <= 6; m++) {
+        if (m > k) break;
+        R ca = c[k - m], cb = c[k + m];
+        R t = ca * pr[m] + cb * pi[m];
+        E += t * A[m];
+        if (m < k) dz += t * dA[m];
+        // (m/2)(ca - i cb) Jp^(m-1) A[m]
+        R h = (R)(0.5 * m) * A[m];
+        jr += h * (ca * pr[m - 1] + cb * pi[m - 1]);
+        ji += h * (ca * pi[m - 1] - cb * pr[m - 1]);
+    }
+    return E;
+}
+
+template <class R>
+__device__ inline R classical_aniso(const R* c, int kmax, R x, R y, R z, R& gx, R& gy, R& gz) {
+    R E = c[0];
+    if (kmax == 0) return E;
+    R X = x * x + y * y + z * z;
+    R pr[7], pi[7];
+    pr[0] = 1; pi[0] = 0;
+#pragma unroll
+    for (int m = 1; m <= 6; m++) {
+        pr[m] = pr[m - 1] * x - pi[m - 1] * y;
+        pi[m] = pr[m - 1] * y + pi[m - 1] * x;
+    }
+    R z2 = z * z, z3 = z2 * z, z4 = z2 * z2, z5 = z4 * z, z6 = z3 * z3;
+    R X2 = X * X, X3 = X2 * X;
+    R dz = 0, jr = 0, ji = 0;
+    {
+        R A[3] = {3 * z2 - X, z, 1};
+        R dA[3] = {6 * z, 1, 0};
+        aniso_k<R>(c + 1, 2, A, dA, pr, pi, E, dz, jr, ji);
+    }
+    if (kmax >= 4) {
+        R A[5] = {35 * z4 - (30 * X) * z2 + 3 * X2, 7 * z3 - (3 * X) * z, 7 * z2 - X, z, 1};
+        R dA[5] = {140 * z3 - (60 * X) * z, 21 * z2 - 3 * X, 14 * z, 1, 0};
+        aniso_k<R>(c + 6, 4, A, dA, pr, pi, E, dz, jr, ji);
+    }
+    if (kmax >= 6) {
+        R A[7] = {231 * z6 - (315 * X) * z4 + (105 * X2) * z2 - 5 * X3,
+                  33 * z5 - (30 * X) * z3 + (5 * X2) * z,
+                  33 * z4 - (18 * X) * z2 + X2,
+                  11 * z3 - (3 * X) * z,
+                  11 * z2 - X,
+                  z,
+                  1};
+        R dA[7] = {1386 * z5 - (1260 * X) * z3 + (210 * X2) * z,
+                   165 * z4 - (90 * X) * z2 + 5 * X2,
+                   132 * z3 - (36 * X) * z,
+                   33 * z2 - 3 * X,
+                   22 * z,
+                   1,
+                   0};
+        aniso_k<R>(c + 15, 6, A, dA, pr, pi, E, dz, jr, ji);
+    }
+    gx += 2 * jr;
+    gy += -2 * ji;
+    gz += dz;
+    return E;
+}
+
+// Stevens quadrupoles and their gradient (src/Operators/Spin.jl:48-69).
+template <class R>
+__device__ inline void quad5(R x, R y, R z, R* Q) {
+    Q[0] = x * x - y * y;
+    Q[1] = z * x;
+    Q[2] = -x * x - y * y + 2 * z * z;
+    Q[3] = z * y;
+    Q[4] = 2 * y * x;
+}
+template <class R>
+__device__ inline void add_quad_grad(R x, R y, R z, const R* v, R& gx, R& gy, R& gz) {
+    // sum_q v_q * grad Q_q
+    gx += v[0] * (2 * x) + v[1] * z + v[2] * (-2 * x) + v[4] * (2 * y);
+    gy += v[0] * (-2 * y) + v[2] * (-2 * y) + v[3] * z + v[4] * (2 * x);
+    gz += v[1] * x + v[2] * (4 * z) + v[3] * y;
+}
+
+struct SiteIdx { int c1, c2, c3, a; };
+__device__ __forceinline__ SiteIdx decompose(int s, int L1, int L2, int L3) {
+    SiteIdx r;
+    r.c1 = s % L1; s /= L1;
+    r.c2 = s % L2; s /= L2;
+    r.c3 = s % L3; r.a = s / L3;
+    return r;
+}
+
+// dE/dS at one site in gather form. X/Y/Zc are the SoA spins seen by neighbours.
+template <class R>
+__device__ inline void grad_site(const Model<R>& M, const Tab<R>& T, int site, const SiteIdx& ix,
+                                 R sx, R sy, R sz, const R* X, const R* Y, const R* Zc,
+                                 R& gx, R& gy, R& gz) {
+    gx = 0; gy = 0; gz = 0;
+    if (M.h) {
+        gx = __ldg(M.h + site);
+        gy = __ldg(M.h + M.ns + site);
+        gz = __ldg(M.h + 2 * M.ns + site);
+    }
+    const int a = ix.a;
+    if (M.dipole_mode) {
+        int km = T.kmax[a];
+        if (km > 0) classical_aniso<R>(T.stev + 28 * a, km, sx, sy, sz, gx, gy, gz);
+    }
+    const int b0 = T.boff[a], b1 = T.boff[a + 1];
+    for (int b = b0; b < b1; b++) {
+        const DBond<R>& B = T.bonds[b];
+        int x1 = sgb_wrap_pos(ix.c1 + B.n[0], M.L1);
+        int x2 = sgb_wrap_pos(ix.c2 + B.n[1], M.L2);
+        int x3 = sgb_wrap_pos(ix.c3 + B.n[2], M.L3);
+        int js = x1 + M.L1 * (x2 + M.L2 * (x3 + M.L3 * B.j));
+        R tx = sgb_ld(X + js), ty = sgb_ld(Y + js), tz = sgb_ld(Zc + js);
+        if (B.jkind == 0) {
+            R j = B.J[0];
+            gx += j * tx; gy += j * ty; gz += j * tz;
+        } else {
+            gx += B.J[0] * tx + B.J[3] * ty + B.J[6] * tz;
+            gy += B.J[1] * tx + B.J[4] * ty + B.J[7] * tz;
+            gz += B.J[2] * tx + B.J[5] * ty + B.J[8] * tz;
+        }
+        if (M.dipole_mode && B.bqkind != 0) {
+            R Qj[5], v[5];
+            quad5<R>(tx, ty, tz, Qj);
+            if (B.bqkind == 1) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) v[q] = B.bq * ((R)biquad_metric(q) * Qj[q]);
+            } else {
+                const R* Bm = T.bq + 25 * B.bqidx;
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    R acc = 0;
+#pragma unroll
+                    for (int p = 0; p < 5; p++) acc += Bm[q + 5 * p] * Qj[p];
+                    v[q] = acc;
+                }
+            }
+            add_quad_grad<R>(sx, sy, sz, v, gx, gy, gz);
+        }
+    }
+}
+
+// Integrators.jl:266-275 rhs_dipole!
+template <class R>
+__device__ __forceinline__ void rhs_dipole(R sx, R sy, R sz, R xx, R xy, R xz, R gx, R gy, R gz,
+                                           R dt, R lam, R& dx, R& dy, R& dz) {
+    R wx, wy, wz;
+    if (lam == (R)0) {
+        wx = dt * gx; wy = dt * gy; wz = dt * gz;
+    } else {
+        R cx = sy * gz - sz * gy, cy = sz * gx - sx * gz, cz = sx * gy - sy * gx;
+        R dl = dt * lam;
+        wx = xx + dt * gx - dl * cx;
+        wy = xy + dt * gy - dl * cy;
+        wz = xz + dt * gz - dl * cz;
+    }
+    dx = -(sy * wz - sz * wy);
+    dy = -(sz * wx - sx * wz);
+    dz = -(sx * wy - sy * wx);
+}
+
+// System.jl:421-423 normalize_dipole
+template <class R>
+__device__ __forceinline__ void normalize_dip(R& x, R& y, R& z, R kappa) {
+    if (kappa == (R)0) { x = 0; y = 0; z = 0; return; }
+    R f = kappa * sgb_rsqrt<R>(x * x + y * y + z * z);
+    x *= f; y *= f; z *= f;
+}
+
+}  // namespace sgbdev

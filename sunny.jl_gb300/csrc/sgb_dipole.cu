@@ -1,0 +1,451 @@
+// sgb_dipole.cu -- dipole-mode kernels for sm_103a.
+//
+// Reference algorithms (Sunny.jl v0.9.2):
+//   gradient      src/System/Interactions.jl:516-592, src/System/OnsiteCoupling.jl:316-425
+//   energy        src/System/Interactions.jl:401-508
+//   Langevin Heun src/Integrators.jl:266-275, 288-298, 313-332
+//   midpoint      src/Integrators.jl:361-371, 379-413
+//
+// Design: every step kernel is persistent (cooperative launch, one CTA per slot of the
+// SM budget). A thread owns SPT sites for the whole launch and keeps their spins, the
+// Heun increment and the noise in registers; only the spins that neighbours need are
+// exchanged through L2-resident SoA buffers, separated by a bounded grid barrier. The
+// implicit midpoint iteration speculatively writes both the next iterate's midpoint
+// spins and the next step's starting midpoint spins, so each fixed-point iteration costs
+// exactly one barrier; the FP64 convergence sum rotates through three accumulators.
+#include "sgb_internal.h"
+#include <stdio.h>
+
+#include "sgb_device.cuh"
+
+namespace {
+using namespace sgbdev;
+
+template <class R, int SPT, bool INJECT>
+__global__ void __launch_bounds__(SGB_BLOCK)
+k_dip_heun(Model<R> M, R* S, R* P, Ctrl* ctrl, int nsteps, R dt, R lam, R nscale, uint64_t seed,
+           uint64_t step0, const double* noise) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tab<R> T = stage_tables<R>(M, smem);
+    const int ns = M.ns;
+    const int nthr = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    R* Sx = S; R* Sy = S + ns; R* Sz = S + 2 * ns;
+    R* Px = P; R* Py = P + ns; R* Pz = P + 2 * ns;
+    R s[SPT][3], d1[SPT][3], xi[SPT][3];
+#pragma unroll
+    for (int k = 0; k < SPT; k++) {
+        int site = tid + k * nthr;
+        if (site < ns) { s[k][0] = Sx[site]; s[k][1] = Sy[site]; s[k][2] = Sz[site]; }
+    }
+    for (int step = 0; step < nsteps; ++step) {
+#pragma unroll
+        for (int k = 0; k < SPT; k++) {
+            int site = tid + k * nthr;
+            if (site >= ns) continue;
+            if (nscale == (R)0) {
+                xi[k][0] = xi[k][1] = xi[k][2] = 0;
+            } else if (INJECT) {
+                const double* nz = noise + ((size_t)step * ns + site) * 3;
+                xi[k][0] = (R)nz[0] * nscale; xi[k][1] = (R)nz[1] * nscale; xi[k][2] = (R)nz[2] * nscale;
+            } else {
+                R g4[4];
+                sgb_normals4<R>(seed, 0u, step0 + step, (uint32_t)site, 0u, g4);
+                xi[k][0] = g4[0] * nscale; xi[k][1] = g4[1] * nscale; xi[k][2] = g4[2] * nscale;
+            }
+            SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
+            R gx, gy, gz;
+            grad_site<R>(M, T, site, ix, s[k][0], s[k][1], s[k][2], Sx, Sy, Sz, gx, gy, gz);
+            rhs_dipole<R>(s[k][0], s[k][1], s[k][2], xi[k][0], xi[k][1], xi[k][2], gx, gy, gz, dt, lam,
+                          d1[k][0], d1[k][1], d1[k][2]);
+            R px = s[k][0] + d1[k][0], py = s[k][1] + d1[k][1], pz = s[k][2] + d1[k][2];
+            normalize_dip<R>(px, py, pz, __ldg(M.kappa + site));
+            Px[site] = px; Py[site] = py; Pz[site] = pz;
+        }
+        if (!sgb_grid_barrier(ctrl, gridDim.x)) return;
+#pragma unroll
+        for (int k = 0; k < SPT; k++) {
+            int site = tid + k * nthr;
+            if (site >= ns) continue;
+            R px = Px[site], py = Py[site], pz = Pz[site];
+            SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
+            R gx, gy, gz, e0, e1, e2;
+            grad_site<R>(M, T, site, ix, px, py, pz, Px, Py, Pz, gx, gy, gz);
+            rhs_dipole<R>(px, py, pz, xi[k][0], xi[k][1], xi[k][2], gx, gy, gz, dt, lam, e0, e1, e2);
+            R nx = s[k][0] + (d1[k][0] + e0) / 2, ny = s[k][1] + (d1[k][1] + e1) / 2,
+              nz = s[k][2] + (d1[k][2] + e2) / 2;
+            normalize_dip<R>(nx, ny, nz, __ldg(M.kappa + site));
+            s[k][0] = nx; s[k][1] = ny; s[k][2] = nz;
+            Sx[site] = nx; Sy[site] = ny; Sz[site] = nz;
+        }
+        if (step + 1 < nsteps) {
+            if (!sgb_grid_barrier(ctrl, gridDim.x)) return;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->steps_done = nsteps;
+}
+
+template <class R>
+__device__ __forceinline__ void write_snapshot_dip(const Model<R>& M, const SnapArgs<R>& sn, int t, int site,
+                                                   R sx, R sy, R sz) {
+    const int ns = M.ns;
+    const int cell = site % M.ncell, a = site / M.ncell;
+    for (int o = 0; o < sn.nobs; o++) {
+        const R* op = sn.ops + (size_t)o * 3 * ns;
+        R v = __ldg(op + site) * sx + __ldg(op + ns + site) * sy + __ldg(op + 2 * ns + site) * sz;
+        size_t idx = (((size_t)t * sn.nobs + o) * M.na + a) * M.ncell + cell;
+        sn.buf[2 * idx] = v * sn.scale;
+        sn.buf[2 * idx + 1] = 0;
+    }
+}
+
+// Spherical midpoint, Integrators.jl:379-413. H holds 3 rotating SoA buffers of
+// midpoint spins S-hat (3*3*ns reals).
+template <class R, int SPT>
+__global__ void __launch_bounds__(SGB_BLOCK)
+k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, double atol2,
+               int max_iters, SnapArgs<R> snap) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tab<R> T = stage_tables<R>(M, smem);
+    const int ns = M.ns;
+    const int nthr = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool leader = (blockIdx.x == 0 && threadIdx.x == 0);
+    R s[SPT][3], sp[SPT][3], sc[SPT][3];
+    int cur = 0;
+#pragma unroll
+    for (int k = 0; k < SPT; k++) {
+        int site = tid + k * nthr;
+        if (site >= ns) continue;
+        s[k][0] = S[site]; s[k][1] = S[ns + site]; s[k][2] = S[2 * ns + site];
+        R hx = (s[k][0] + s[k][0]) / 2, hy = (s[k][1] + s[k][1]) / 2, hz = (s[k][2] + s[k][2]) / 2;
+        normalize_dip<R>(hx, hy, hz, __ldg(M.kappa + site));
+        R* Hc = H + (size_t)cur * 3 * ns;
+        Hc[site] = hx; Hc[ns + site] = hy; Hc[2 * ns + site] = hz;
+        if (snap.enabled) write_snapshot_dip<R>(M, snap, snap.t0, site, s[k][0], s[k][1], s[k][2]);
+    }
+    if (leader) { ctrl->acc[0] = 0.0; ctrl->acc[1] = 0.0; ctrl->acc[2] = 0.0; }
+    if (!sgb_grid_barrier(ctrl, gridDim.x)) return;
+    long long itg = 0;
+    int done = 0;
+    for (int step = 0; step < nsteps; ++step) {
+#pragma unroll
+        for (int k = 0; k < SPT; k++) { sp[k][0] = s[k][0]; sp[k][1] = s[k][1]; sp[k][2] = s[k][2]; }
+        bool conv = false;
+        for (int it = 0; it < max_iters; ++it) {
+            const int nxt = (cur + 1) % 3, nst = (cur + 2) % 3;
+            const R* Hc = H + (size_t)cur * 3 * ns;
+            R* Hn = H + (size_t)nxt * 3 * ns;
+            R* Hs = H + (size_t)nst * 3 * ns;
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < SPT; k++) {
+                int site = tid + k * nthr;
+                if (site >= ns) continue;
+                const R kap = __ldg(M.kappa + site);
+                R hx = (s[k][0] + sp[k][0]) / 2, hy = (s[k][1] + sp[k][1]) / 2, hz = (s[k][2] + sp[k][2]) / 2;
+                normalize_dip<R>(hx, hy, hz, kap);
+                SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
+                R gx, gy, gz, dx, dy, dz;
+                grad_site<R>(M, T, site, ix, hx, hy, hz, Hc, Hc + ns, Hc + 2 * ns, gx, gy, gz);
+                rhs_dipole<R>(hx, hy, hz, (R)0, (R)0, (R)0, gx, gy, gz, dt, lam, dx, dy, dz);
+                R qx = s[k][0] + dx, qy = s[k][1] + dy, qz = s[k][2] + dz;
+                double ex = (double)(sp[k][0] - qx), ey = (double)(sp[k][1] - qy), ez = (double)(sp[k][2] - qz);
+                acc += ex * ex + ey * ey + ez * ez;
+                sp[k][0] = qx; sp[k][1] = qy; sp[k][2] = qz;
+                // candidate midpoint for the next iteration
+                R nx = (s[k][0] + qx) / 2, ny = (s[k][1] + qy) / 2, nz = (s[k][2] + qz) / 2;
+                normalize_dip<R>(nx, ny, nz, kap);
+                Hn[site] = nx; Hn[ns + site] = ny; Hn[2 * ns + site] = nz;
+                // candidate new state and the next step's first midpoint
+                R cx = qx, cy = qy, cz = qz;
+                normalize_dip<R>(cx, cy, cz, kap);
+                sc[k][0] = cx; sc[k][1] = cy; sc[k][2] = cz;
+                R mx = (cx + cx) / 2, my = (cy + cy) / 2, mz = (cz + cz) / 2;
+                normalize_dip<R>(mx, my, mz, kap);
+                Hs[site] = mx; Hs[ns + site] = my; Hs[2 * ns + site] = mz;
+            }
+            double bsum = sgb_block_sum<SGB_BLOCK>(acc);
+            const int slot = (int)(itg % 3);
+            if (threadIdx.x == 0) atomicAdd(&ctrl->acc[slot], bsum);
+            if (leader) { ctrl->acc[(slot + 1) % 3] = 0.0; ctrl->iters += 1; }
+            if (!sgb_grid_barrier(ctrl, gridDim.x)) return;
+            double tot = __ldcg(&ctrl->acc[slot]);
+            itg++;
+            if (tot <= atol2) {  // false for NaN, as fast_isapprox
+                conv = true;
+#pragma unroll
+                for (int k = 0; k < SPT; k++) { s[k][0] = sc[k][0]; s[k][1] = sc[k][1]; s[k][2] = sc[k][2]; }
+                cur = nst;
+                break;
+            }
+            cur = nxt;
+        }
+        if (!conv) {
+            if (leader) sgb_set_status(ctrl, SGB_ERR_NOCONVERGE);
+            break;
+        }
+        done = step + 1;
+        if (snap.enabled && (done % snap.measperiod) == 0) {
+#pragma unroll
+            for (int k = 0; k < SPT; k++) {
+                int site = tid + k * nthr;
+                if (site < ns) write_snapshot_dip<R>(M, snap, snap.t0 + done / snap.measperiod, site,
+                                                     s[k][0], s[k][1], s[k][2]);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < SPT; k++) {
+        int site = tid + k * nthr;
+        if (site < ns) { S[site] = s[k][0]; S[ns + site] = s[k][1]; S[2 * ns + site] = s[k][2]; }
+    }
+    if (leader) ctrl->steps_done = done;
+}
+
+template <class R>
+__global__ void __launch_bounds__(SGB_BLOCK)
+k_dip_grad(Model<R> M, const R* S, double* out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tab<R> T = stage_tables<R>(M, smem);
+    const int ns = M.ns;
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < ns; site += gridDim.x * blockDim.x) {
+        SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
+        R gx, gy, gz;
+        grad_site<R>(M, T, site, ix, S[site], S[ns + site], S[2 * ns + site], S, S + ns, S + 2 * ns, gx, gy, gz);
+        out[3 * site] = gx; out[3 * site + 1] = gy; out[3 * site + 2] = gz;
+    }
+}
+
+// FP64 energy and magnetisation (Interactions.jl:401-508): partials[block][4].
+template <class R>
+__global__ void __launch_bounds__(SGB_BLOCK)
+k_dip_energy(Model<R> M, const R* S, double* partials) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tab<R> T = stage_tables<R>(M, smem);
+    const int ns = M.ns;
+    double E = 0, mx = 0, my = 0, mz = 0;
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < ns; site += gridDim.x * blockDim.x) {
+        SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
+        double sx = S[site], sy = S[ns + site], sz = S[2 * ns + site];
+        mx += sx; my += sy; mz += sz;
+        if (M.h) E += (double)M.h[site] * sx + (double)M.h[ns + site] * sy + (double)M.h[2 * ns + site] * sz;
+        const int a = ix.a;
+        if (M.dipole_mode) {
+            int km = T.kmax[a];
+            double c[28];
+            for (int q = 0; q < 28; q++) c[q] = (double)T.stev[28 * a + q];
+            double gx = 0, gy = 0, gz = 0;
+            E += classical_aniso<double>(c, km, sx, sy, sz, gx, gy, gz);
+        }
+        for (int b = T.boff[a]; b < T.boff[a + 1]; b++) {
+            const DBond<R>& B = T.bonds[b];
+            if (!B.fwd) continue;
+            int x1 = sgb_wrap_pos(ix.c1 + B.n[0], M.L1);
+            int x2 = sgb_wrap_pos(ix.c2 + B.n[1], M.L2);
+            int x3 = sgb_wrap_pos(ix.c3 + B.n[2], M.L3);
+            int js = x1 + M.L1 * (x2 + M.L2 * (x3 + M.L3 * B.j));
+            double tx = S[js], ty = S[ns + js], tz = S[2 * ns + js];
+            E += (double)B.scalar;
+            if (B.jkind == 0) E += (double)B.J[0] * (sx * tx + sy * ty + sz * tz);
+            else {
+                double jx = (double)B.J[0] * tx + (double)B.J[3] * ty + (double)B.J[6] * tz;
+                double jy = (double)B.J[1] * tx + (double)B.J[4] * ty + (double)B.J[7] * tz;
+                double jz = (double)B.J[2] * tx + (double)B.J[5] * ty + (double)B.J[8] * tz;
+                E += sx * jx + sy * jy + sz * jz;
+            }
+            if (M.dipole_mode && B.bqkind != 0) {
+                double Qi[5], Qj[5];
+                quad5<double>(sx, sy, sz, Qi);
+                quad5<double>(tx, ty, tz, Qj);
+                double acc = 0;
+                if (B.bqkind == 1) {
+                    for (int q = 0; q < 5; q++) acc += Qi[q] * (biquad_metric(q) * Qj[q]);
+                    acc *= (double)B.bq;
+                } else {
+                    const R* Bm = T.bq + 25 * B.bqidx;
+                    for (int q = 0; q < 5; q++)
+                        for (int p = 0; p < 5; p++) acc += Qi[q] * (double)Bm[q + 5 * p] * Qj[p];
+                }
+                E += acc;
+            }
+        }
+    }
+    double e = sgb_block_sum<SGB_BLOCK>(E);
+    double a0 = sgb_block_sum<SGB_BLOCK>(mx);
+    double a1 = sgb_block_sum<SGB_BLOCK>(my);
+    double a2 = sgb_block_sum<SGB_BLOCK>(mz);
+    if (threadIdx.x == 0) {
+        partials[4 * blockIdx.x + 0] = e;
+        partials[4 * blockIdx.x + 1] = a0;
+        partials[4 * blockIdx.x + 2] = a1;
+        partials[4 * blockIdx.x + 3] = a2;
+    }
+}
+
+// Sums partials[n][ncomp] in a fixed order (deterministic) into out[ncomp].
+__global__ void k_reduce_partials(const double* partials, int n, int ncomp, double* out) {
+    for (int c = 0; c < ncomp; c++) {
+        double v = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) v += partials[(size_t)i * ncomp + c];
+        double t = sgb_block_sum<SGB_BLOCK>(v);
+        if (threadIdx.x == 0) out[c] = t;
+        __syncthreads();
+    }
+}
+
+template <class R>
+__global__ void k_noise_export(int sun, int N, int ns, uint64_t seed, uint64_t step, double* out) {
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < ns; site += gridDim.x * blockDim.x) {
+        if (!sun) {
+            R g4[4];
+            sgb_normals4<R>(seed, 0u, step, (uint32_t)site, 0u, g4);
+            out[3 * site] = (double)g4[0]; out[3 * site + 1] = (double)g4[1]; out[3 * site + 2] = (double)g4[2];
+        } else {
+            for (int k = 0; k < N; k += 2) {
+                R g4[4];
+                sgb_normals4<R>(seed, 0u, step, (uint32_t)site, (uint32_t)(k / 2), g4);
+                const R r2 = (R)0.70710678118654752440;
+                out[2 * ((size_t)site * N + k)] = (double)(g4[0] * r2);
+                out[2 * ((size_t)site * N + k) + 1] = (double)(g4[1] * r2);
+                if (k + 1 < N) {
+                    out[2 * ((size_t)site * N + k + 1)] = (double)(g4[2] * r2);
+                    out[2 * ((size_t)site * N + k + 1) + 1] = (double)(g4[3] * r2);
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_fill(double* p, size_t n, double v) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+template <class K>
+int set_smem_attr(K kernel, size_t smem) {
+    if (smem > 48 * 1024) {
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return SGB_ERR_CUDA;
+    }
+    return SGB_OK;
+}
+
+template <class K>
+int coop_launch(K kernel, const LaunchInfo& li, void** args, cudaStream_t st) {
+    if (set_smem_attr(kernel, li.smem) != SGB_OK) return SGB_ERR_CUDA;
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)kernel, dim3(li.grid), dim3(li.block), args, li.smem, st);
+    return e == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------------------
+template <class R>
+int dip_launch_heun(const Model<R>& M, R* S, R* P, Ctrl* ctrl, int nsteps, double dt, double lam,
+                    double noise_scale, uint64_t seed, uint64_t step0, const double* noise,
+                    const LaunchInfo& li, cudaStream_t st) {
+    Model<R> m = M;
+    R rdt = (R)dt, rlam = (R)lam, rns = (R)noise_scale;
+    void* args[] = {&m, &S, &P, &ctrl, &nsteps, &rdt, &rlam, &rns, &seed, &step0, &noise};
+#define SGB_HEUN_CASE(SPTV)                                                                  \
+    case SPTV:                                                                               \
+        return noise ? coop_launch(k_dip_heun<R, SPTV, true>, li, args, st)                  \
+                     : coop_launch(k_dip_heun<R, SPTV, false>, li, args, st);
+    switch (li.spt) {
+        SGB_HEUN_CASE(1)
+        SGB_HEUN_CASE(2)
+        SGB_HEUN_CASE(4)
+        SGB_HEUN_CASE(8)
+    }
+#undef SGB_HEUN_CASE
+    return SGB_ERR_ARG;
+}
+
+template <class R>
+int dip_launch_midpoint(const Model<R>& M, R* S, R* H, Ctrl* ctrl, int nsteps, double dt, double lam,
+                        double atol2, int max_iters, const SnapArgs<R>& snap, const LaunchInfo& li,
+                        cudaStream_t st) {
+    Model<R> m = M;
+    SnapArgs<R> sn = snap;
+    R rdt = (R)dt, rlam = (R)lam;
+    void* args[] = {&m, &S, &H, &ctrl, &nsteps, &rdt, &rlam, &atol2, &max_iters, &sn};
+    switch (li.spt) {
+        case 1: return coop_launch(k_dip_midpoint<R, 1>, li, args, st);
+        case 2: return coop_launch(k_dip_midpoint<R, 2>, li, args, st);
+        case 4: return coop_launch(k_dip_midpoint<R, 4>, li, args, st);
+        case 8: return coop_launch(k_dip_midpoint<R, 8>, li, args, st);
+    }
+    return SGB_ERR_ARG;
+}
+
+template <class R>
+int dip_max_blocks(int spt, size_t smem, int* bps) {
+    cudaError_t e = cudaErrorInvalidValue;
+    int a = 0, b = 0;
+#define SGB_OCC(K)                                                                              \
+    do {                                                                                        \
+        if (set_smem_attr(K, smem) != SGB_OK) return SGB_ERR_CUDA;                              \
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, K, SGB_BLOCK, smem);              \
+        if (e != cudaSuccess) return SGB_ERR_CUDA;                                              \
+    } while (0)
+    switch (spt) {
+        case 1: SGB_OCC((k_dip_heun<R, 1, false>)); b = a; SGB_OCC((k_dip_heun<R, 1, true>)); b = b < a ? b : a; SGB_OCC((k_dip_midpoint<R, 1>)); break;
+        case 2: SGB_OCC((k_dip_heun<R, 2, false>)); b = a; SGB_OCC((k_dip_heun<R, 2, true>)); b = b < a ? b : a; SGB_OCC((k_dip_midpoint<R, 2>)); break;
+        case 4: SGB_OCC((k_dip_heun<R, 4, false>)); b = a; SGB_OCC((k_dip_heun<R, 4, true>)); b = b < a ? b : a; SGB_OCC((k_dip_midpoint<R, 4>)); break;
+        case 8: SGB_OCC((k_dip_heun<R, 8, false>)); b = a; SGB_OCC((k_dip_heun<R, 8, true>)); b = b < a ? b : a; SGB_OCC((k_dip_midpoint<R, 8>)); break;
+        default: return SGB_ERR_ARG;
+    }
+#undef SGB_OCC
+    *bps = b < a ? b : a;
+    return SGB_OK;
+}
+
+template <class R>
+int dip_launch_grad(const Model<R>& M, const R* S, double* grad, cudaStream_t st) {
+    size_t smem = (size_t)M.tables_bytes;
+    if (set_smem_attr(k_dip_grad<R>, smem) != SGB_OK) return SGB_ERR_CUDA;
+    int grid = (M.ns + SGB_BLOCK - 1) / SGB_BLOCK;
+    if (grid > 4096) grid = 4096;
+    k_dip_grad<R><<<grid, SGB_BLOCK, smem, st>>>(M, S, grad);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+template <class R>
+int dip_launch_energy(const Model<R>& M, const R* S, double* partials, int nblocks, cudaStream_t st) {
+    size_t smem = (size_t)M.tables_bytes;
+    if (set_smem_attr(k_dip_energy<R>, smem) != SGB_OK) return SGB_ERR_CUDA;
+    k_dip_energy<R><<<nblocks, SGB_BLOCK, smem, st>>>(M, S, partials);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+int util_launch_reduce(const double* partials, int n, int ncomp, double* out, cudaStream_t st) {
+    k_reduce_partials<<<1, SGB_BLOCK, 0, st>>>(partials, n, ncomp, out);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+template <class R>
+int util_launch_noise_export(int sun, int N, int ns, uint64_t seed, uint64_t step, double* out, cudaStream_t st) {
+    int grid = (ns + SGB_BLOCK - 1) / SGB_BLOCK;
+    if (grid > 4096) grid = 4096;
+    k_noise_export<R><<<grid, SGB_BLOCK, 0, st>>>(sun, N, ns, seed, step, out);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+int util_launch_fill(double* p, size_t n, double v, cudaStream_t st) {
+    k_fill<<<1024, SGB_BLOCK, 0, st>>>(p, n, v);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+#define SGB_INST(R)                                                                                      \
+    template int dip_launch_heun<R>(const Model<R>&, R*, R*, Ctrl*, int, double, double, double, uint64_t, \
+                                    uint64_t, const double*, const LaunchInfo&, cudaStream_t);          \
+    template int dip_launch_midpoint<R>(const Model<R>&, R*, R*, Ctrl*, int, double, double, double, int,  \
+                                        const SnapArgs<R>&, const LaunchInfo&, cudaStream_t);           \
+    template int dip_launch_grad<R>(const Model<R>&, const R*, double*, cudaStream_t);                    \
+    template int dip_launch_energy<R>(const Model<R>&, const R*, double*, int, cudaStream_t);             \
+    template int dip_max_blocks<R>(int, size_t, int*);                                                    \
+    template int util_launch_noise_export<R>(int, int, int, uint64_t, uint64_t, double*, cudaStream_t);
+SGB_INST(float)
+SGB_INST(double)

@@ -1,0 +1,94 @@
+// sgb_internal.h -- host/device interface between the C ABI (sgb_api.cu) and the kernel
+// translation units. Not installed; not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include "sgb_common.cuh"
+
+// Everything a kernel needs to evaluate couplings of one (homogeneous) system.
+// The packed tables are copied into shared memory at kernel start.
+template <class R>
+struct Model {
+    int L1, L2, L3, na;
+    int ns;             // sites
+    int ncell;          // L1*L2*L3
+    int N;              // 0 in dipole modes
+    int dipole_mode;    // 1 for :dipole / :dipole_uncorrected
+    int has_biquad;     // any bond with a biquadratic coupling
+    const R* kappa;     // [ns]
+    const R* h;         // [3][ns] Zeeman g'B, or nullptr
+    const unsigned char* tables;  // packed tables (device)
+    int tables_bytes;
+    // byte offsets inside the packed tables
+    int off_stev;       // R[na][28]            (dipole)
+    int off_kmax;       // int[na]              (dipole)
+    int off_boff;       // int[na+1]
+    int off_bonds;      // DBond<R>[nb]
+    int off_bq;         // R[nbq][25]
+    int off_lam;        // R[na][N*N][2]        (SU(N): Λ, column-major)
+    int off_qmat;       // R[5][N*N][2]         (SU(N): Stevens quadrupoles)
+    int nb, nbq;
+};
+
+// Observable recording for SampledCorrelations trajectories.
+template <class R>
+struct SnapArgs {
+    int enabled;
+    int nobs;
+    int measperiod;
+    int t0;              // row of the first snapshot written by this launch
+    const R* ops;        // dipole: [nobs][3][ns]; SU(N): [nobs][N*N][2][ns]
+    R* buf;              // complex [n_all_omega][nobs][npos][ncell] (interleaved re,im)
+    R scale;             // 1/sqrt(ncell)
+};
+
+struct LaunchInfo {
+    int grid, block, spt;
+    size_t smem;
+};
+
+// ---- dipole kernels (sgb_dipole.cu) ----
+template <class R>
+int dip_launch_heun(const Model<R>& M, R* S, R* P, Ctrl* ctrl, int nsteps, double dt, double lam,
+                    double noise_scale, uint64_t seed, uint64_t step0, const double* noise,
+                    const LaunchInfo& li, cudaStream_t st);
+template <class R>
+int dip_launch_midpoint(const Model<R>& M, R* S, R* H, Ctrl* ctrl, int nsteps, double dt, double lam,
+                        double atol2, int max_iters, const SnapArgs<R>& snap, const LaunchInfo& li,
+                        cudaStream_t st);
+template <class R>
+int dip_launch_grad(const Model<R>& M, const R* S, double* grad, cudaStream_t st);
+template <class R>
+int dip_launch_energy(const Model<R>& M, const R* S, double* partials, int nblocks, cudaStream_t st);
+template <class R>
+int dip_max_blocks(int spt, size_t smem, int* blocks_per_sm);
+
+// ---- SU(N) kernels (sgb_sun.cu) ----
+template <class R>
+int sun_launch_heun(const Model<R>& M, R* Z, R* D, R* Q, R* P, R* QP, Ctrl* ctrl, int nsteps,
+                    double dt, double lam, double noise_scale, uint64_t seed, uint64_t step0,
+                    const double* noise, const LaunchInfo& li, cudaStream_t st);
+template <class R>
+int sun_launch_midpoint(const Model<R>& M, R* Z, R* D, R* Q, R* H, R* QH, Ctrl* ctrl, int nsteps,
+                        double dt, double lam, double atol2, int max_iters, const SnapArgs<R>& snap,
+                        const LaunchInfo& li, cudaStream_t st);
+template <class R>
+int sun_launch_refresh(const Model<R>& M, const R* Z, R* D, R* Q, cudaStream_t st);
+template <class R>
+int sun_launch_grad(const Model<R>& M, const R* Z, const R* D, const R* Q, double* grad, cudaStream_t st);
+template <class R>
+int sun_launch_energy(const Model<R>& M, const R* Z, const R* D, const R* Q, double* partials,
+                      int nblocks, cudaStream_t st);
+template <class R>
+int sun_max_blocks(int N, int spt, size_t smem, int* blocks_per_sm);
+
+// ---- shared utilities (sgb_dipole.cu) ----
+int util_launch_reduce(const double* partials, int n, int ncomp, double* out, cudaStream_t st);
+template <class R>
+int util_launch_noise_export(int mode_sun, int N, int ns, uint64_t seed, uint64_t step, double* out,
+                             cudaStream_t st);
+int util_launch_fill(double* p, size_t n, double v, cudaStream_t st);
+
+#define SGB_ENERGY_BLOCKS 256
+#define SGB_BLOCK 256

@@ -1,0 +1,736 @@
+// sgb_sun.cu -- SU(N) coherent-state kernels for sm_103a.
+//
+// Reference algorithms (Sunny.jl v0.9.2):
+//   HZ = dE/dZbar     src/System/Interactions.jl:596-669
+//   spin algebra      src/Operators/Spin.jl:72-167
+//   energy            src/System/Interactions.jl:401-508
+//   Langevin Heun     src/Integrators.jl:277-298, 335-357; proj MathBasics.jl:62
+//   Schrodinger midpoint src/Integrators.jl:361-371, 422-452
+//
+// In SU(N) mode neighbours interact only through expected dipoles (bilinear and Zeeman
+// terms) and expected Stevens quadrupoles (biquadratic terms). Each thread therefore
+// keeps its sites' coherent states Z in registers for the whole persistent launch and
+// publishes only <Z|S|Z> (3 reals) and, when biquadratic couplings exist, <Z|O2q|Z>
+// (5 reals) per site through L2-resident SoA buffers.
+#include "sgb_device.cuh"
+
+namespace {
+using namespace sgbdev;
+
+template <class R>
+struct Cx { R re, im; };
+
+template <class R> __device__ __forceinline__ Cx<R> cmul(Cx<R> a, Cx<R> b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+
+// Spin-s matrix elements for N = 2s+1 (Spin.jl:1-14): off[j] couples levels j and j+1.
+template <class R, int N>
+struct SpinConst {
+    R off[N > 1 ? N - 1 : 1];
+    R sz[N];
+    __device__ SpinConst() {
+        const double s = (N - 1) / 2.0;
+#pragma unroll
+        for (int j = 1; j <= N - 1; j++) off[j - 1] = (R)(sqrt(2 * (s + 1) * j - (double)j * (j + 1)) / 2);
+#pragma unroll
+        for (int k = 0; k < N; k++) sz[k] = (R)(s - k);
+    }
+};
+
+// <Z|S|Z> (Spin.jl:72-87)
+template <class R, int N>
+__device__ __forceinline__ void expected_spin(const SpinConst<R, N>& sc, const R* z, R& nx, R& ny, R& nz) {
+    R cr = 0, ci = 0, zz = 0;
+#pragma unroll
+    for (int j = 0; j < N - 1; j++) {
+        // conj(z_j) * off_j * z_{j+1}
+        R ar = z[2 * j], ai = z[2 * j + 1], br = sc.off[j] * z[2 * j + 2], bi = sc.off[j] * z[2 * j + 3];
+        cr += ar * br + ai * bi;
+        ci += ar * bi - ai * br;
+    }
+#pragma unroll
+    for (int k = 0; k < N; k++) zz += sc.sz[k] * (z[2 * k] * z[2 * k] + z[2 * k + 1] * z[2 * k + 1]);
+    nx = 2 * cr; ny = 2 * ci; nz = zz;
+}
+
+// <Z|O2q|Z> (Spin.jl:90-104); qm: R[5][N*N][2] column-major
+template <class R, int N>
+__device__ __forceinline__ void expected_quad(const R* qm, const R* z, R* Q) {
+#pragma unroll
+    for (int a = 0; a < 5; a++) {
+        R acc = 0;
+        const R* O = qm + a * 2 * N * N;
+#pragma unroll
+        for (int c = 0; c < N; c++) {
+            // (O z)_r summed against conj(z_r)
+#pragma unroll
+            for (int r = 0; r < N; r++) {
+                R orr = O[2 * (r + N * c)], oi = O[2 * (r + N * c) + 1];
+                R tr = orr * z[2 * c] - oi * z[2 * c + 1];
+                R ti = orr * z[2 * c + 1] + oi * z[2 * c];
+                acc += z[2 * r] * tr + z[2 * r + 1] * ti;
+            }
+        }
+        Q[a] = acc;
+    }
+}
+
+// HZ = (Λ + d.S) Z + sum_q v_q O2q Z  (Spin.jl:132-167)
+template <class R, int N, bool BQ>
+__device__ __forceinline__ void apply_H(const SpinConst<R, N>& sc, const R* lam, const R* qm, const R* d,
+                                        const R* v, const R* z, R* hz) {
+#pragma unroll
+    for (int r = 0; r < N; r++) {
+        R ar = 0, ai = 0;
+#pragma unroll
+        for (int c = 0; c < N; c++) {
+            R hr = lam[2 * (r + N * c)], hi = lam[2 * (r + N * c) + 1];
+            if (BQ) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    hr += v[q] * qm[q * 2 * N * N + 2 * (r + N * c)];
+                    hi += v[q] * qm[q * 2 * N * N + 2 * (r + N * c) + 1];
+                }
+            }
+            ar += hr * z[2 * c] - hi * z[2 * c + 1];
+            ai += hr * z[2 * c + 1] + hi * z[2 * c];
+        }
+        // dz * sz_r * z_r
+        ar += d[2] * sc.sz[r] * z[2 * r];
+        ai += d[2] * sc.sz[r] * z[2 * r + 1];
+        if (r + 1 < N) {  // (dx - i dy) off_r z_{r+1}
+            R o = sc.off[r];
+            R pr = o * d[0], pi = -o * d[1];
+            ar += pr * z[2 * r + 2] - pi * z[2 * r + 3];
+            ai += pr * z[2 * r + 3] + pi * z[2 * r + 2];
+        }
+        if (r > 0) {  // (dx + i dy) off_{r-1} z_{r-1}
+            R o = sc.off[r - 1];
+            R pr = o * d[0], pi = o * d[1];
+            ar += pr * z[2 * r - 2] - pi * z[2 * r - 1];
+            ai += pr * z[2 * r - 1] + pi * z[2 * r - 2];
+        }
+        hz[2 * r] = ar;
+        hz[2 * r + 1] = ai;
+    }
+}
+
+// dE/dS (Zeeman + bilinear) from neighbours' dipoles, and the summed dE/dQ of the
+// biquadratic couplings from neighbours' quadrupoles (Interactions.jl:596-669).
+template <class R, bool BQ>
+__device__ __forceinline__ void sun_field(const Model<R>& M, const Tab<R>& T, int site, const SiteIdx& ix,
+                                          const R* D, const R* Qb, R* d, R* v) {
+    const int ns = M.ns;
+    d[0] = 0; d[1] = 0; d[2] = 0;
+    if (M.h) { d[0] = __ldg(M.h + site); d[1] = __ldg(M.h + ns + site); d[2] = __ldg(M.h + 2 * ns + site); }
+    if (BQ) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) v[q] = 0;
+    }
+    for (int b = T.boff[ix.a]; b < T.boff[ix.a + 1]; b++) {
+        const DBond<R>& B = T.bonds[b];
+        int x1 = sgb_wrap_pos(ix.c1 + B.n[0], M.L1);
+        int x2 = sgb_wrap_pos(ix.c2 + B.n[1], M.L2);
+        int x3 = sgb_wrap_pos(ix.c3 + B.n[2], M.L3);
+        int js = x1 + M.L1 * (x2 + M.L2 * (x3 + M.L3 * B.j));
+        R tx = sgb_ld(D + js), ty = sgb_ld(D + ns + js), tz = sgb_ld(D + 2 * ns + js);
+        if (B.jkind == 0) {
+            R j = B.J[0];
+            d[0] += j * tx; d[1] += j * ty; d[2] += j * tz;
+        } else {
+            d[0] += B.J[0] * tx + B.J[3] * ty + B.J[6] * tz;
+            d[1] += B.J[1] * tx + B.J[4] * ty + B.J[7] * tz;
+            d[2] += B.J[2] * tx + B.J[5] * ty + B.J[8] * tz;
+        }
+        if (BQ && B.bqkind != 0) {
+            R Qj[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) Qj[q] = sgb_ld(Qb + (size_t)q * ns + js);
+            if (B.bqkind == 1) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) v[q] += B.bq * ((R)biquad_metric(q) * Qj[q]);
+            } else {
+                const R* Bm = T.bq + 25 * B.bqidx;
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    R acc = 0;
+#pragma unroll
+                    for (int p = 0; p < 5; p++) acc += Bm[q + 5 * p] * Qj[p];
+                    v[q] += acc;
+                }
+            }
+        }
+    }
+}
+
+// Integrators.jl:277-286 rhs_sun!, with proj (MathBasics.jl:62)
+template <class R, int N>
+__device__ __forceinline__ void rhs_sun(const R* z, const R* ze, const R* hz, R dt, R lam, R* dz) {
+    if (lam == (R)0) {
+#pragma unroll
+        for (int k = 0; k < N; k++) { dz[2 * k] = dt * hz[2 * k + 1]; dz[2 * k + 1] = -dt * hz[2 * k]; }
+        return;
+    }
+    R v[2 * N];
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        // ζ + dt (i + λ) hz
+        R hr = hz[2 * k], hi = hz[2 * k + 1];
+        v[2 * k] = ze[2 * k] + dt * (lam * hr - hi);
+        v[2 * k + 1] = ze[2 * k + 1] + dt * (hr + lam * hi);
+    }
+    R nr = 0, ni = 0, nn = 0;
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        nr += z[2 * k] * v[2 * k] + z[2 * k + 1] * v[2 * k + 1];
+        ni += z[2 * k] * v[2 * k + 1] - z[2 * k + 1] * v[2 * k];
+        nn += z[2 * k] * z[2 * k] + z[2 * k + 1] * z[2 * k + 1];
+    }
+    R fr = nr / nn, fi = ni / nn;
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        R pr = z[2 * k] * fr - z[2 * k + 1] * fi, pi = z[2 * k] * fi + z[2 * k + 1] * fr;
+        dz[2 * k] = -(v[2 * k] - pr);
+        dz[2 * k + 1] = -(v[2 * k + 1] - pi);
+    }
+}
+
+// System.jl:416-418 normalize_ket: Z / sqrt(|Z|^2/κ)
+template <class R, int N>
+__device__ __forceinline__ void normalize_ket(R* z, R kappa) {
+    if (kappa == (R)0) {
+#pragma unroll
+        for (int k = 0; k < 2 * N; k++) z[k] = 0;
+        return;
+    }
+    R n2 = 0;
+#pragma unroll
+    for (int k = 0; k < N; k++) n2 += z[2 * k] * z[2 * k] + z[2 * k + 1] * z[2 * k + 1];
+    if constexpr (sizeof(R) == 8) {
+        R d = sqrt(n2 / kappa);
+#pragma unroll
+        for (int k = 0; k < 2 * N; k++) z[k] = z[k] / d;
+    } else {
+        R f = sqrtf(kappa) * rsqrtf(n2);
+#pragma unroll
+        for (int k = 0; k < 2 * N; k++) z[k] *= f;
+    }
+}
+
+template <class R, int N>
+struct SunTab {
+    Tab<R> t;
+    const R* lam;   // [na][N*N][2]
+    const R* qm;    // [5][N*N][2]
+};
+
+template <class R, int N>
+__device__ inline SunTab<R, N> stage_sun(const Model<R>& M, unsigned char* smem) {
+    SunTab<R, N> s;
+    s.t = stage_tables<R>(M, smem);
+    s.lam = reinterpret_cast<const R*>(smem + M.off_lam);
+    s.qm = reinterpret_cast<const R*>(smem + M.off_qmat);
+    return s;
+}
+
+template <class R, int N, bool BQ>
+__device__ __forceinline__ void publish(const SpinConst<R, N>& sc, const R* qm, const R* z, int ns, int site, R* D, R* Qb) {
+    R nx, ny, nz;
+    expected_spin<R, N>(sc, z, nx, ny, nz);
+    D[site] = nx; D[ns + site] = ny; D[2 * ns + site] = nz;
+    if (BQ) {
+        R q[5];
+        expected_quad<R, N>(qm, z, q);
+#pragma unroll
+        for (int a = 0; a < 5; a++) Qb[(size_t)a * ns + site] = q[a];
+    }
+}
+
+template <class R, int N, bool BQ>
+__device__ __forceinline__ void local_HZ(const Model<R>& M, const SunTab<R, N>& S, const SpinConst<R, N>& sc, int site,
+                                         const R* D, const R* Qb, const R* z, R* hz) {
+    SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
+    R d[3], v[5];
+    sun_field<R, BQ>(M, S.t, site, ix, D, Qb, d, v);
+    apply_H<R, N, BQ>(sc, S.lam + ix.a * 2 * N * N, S.qm, d, v, z, hz);
+}
+
+template <class R, int N, int SPT, bool INJECT, bool BQ>
+__global__ void __launch_bounds__(SGB_BLOCK)
+k_sun_heun(Model<R> M, R* Z, R* D, R* Qb, R* P, R* QP, Ctrl* ctrl, int nsteps, R dt, R lam, R nscale,
+           uint64_t seed, uint64_t step0, const double* noise) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SunTab<R, N> S = stage_sun<R, N>(M, smem);
+    SpinConst<R, N> sc;
+    const int ns = M.ns;
+    const int nthr = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    R z[SPT][2 * N], zp[SPT][2 * N], d1[SPT][2 * N], ze[SPT][2 * N];
+#pragma unroll
+    for (int k = 0; k < SPT; k++) {
+        int site = tid + k * nthr;
+        if (site >= ns) continue;
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) z[k][c] = Z[(size_t)c * ns + site];
+    }
+    for (int step = 0; step < nsteps; ++step) {
+#pragma unroll
+        for (int k = 0; k < SPT; k++) {
+            int site = tid + k * nthr;
+            if (site >= ns) continue;
+            if (nscale == (R)0) {
+#pragma unroll
+                for (int c = 0; c < 2 * N; c++) ze[k][c] = 0;
+            } else if (INJECT) {
+                const double* nz = noise + ((size_t)step * ns + site) * 2 * N;
+#pragma unroll
+                for (int c = 0; c < 2 * N; c++) ze[k][c] = (R)nz[c] * nscale;
+            } else {
+                const R r2 = (R)0.70710678118654752440;
+#pragma unroll
+                for (int c = 0; c < 2 * N; c += 4) {
+                    R g4[4];
+                    sgb_normals4<R>(seed, 0u, step0 + step, (uint32_t)site, (uint32_t)(c / 4), g4);
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (c + q < 2 * N) ze[k][c + q] = g4[q] * r2 * nscale;
+                }
+            }
+            R hz[2 * N];
+            local_HZ<R, N, BQ>(M, S, sc, site, D, Qb, z[k], hz);
+            rhs_sun<R, N>(z[k], ze[k], hz, dt, lam, d1[k]);
+#pragma unroll
+            for (int c = 0; c < 2 * N; c++) zp[k][c] = z[k][c] + d1[k][c];
+            normalize_ket<R, N>(zp[k], __ldg(M.kappa + site));
+            publish<R, N, BQ>(sc, S.qm, zp[k], ns, site, P, QP);
+        }
+        if (!sgb_grid_barrier(ctrl, gridDim.x)) return;
+#pragma unroll
+        for (int k = 0; k < SPT; k++) {
+            int site = tid + k * nthr;
+            if (site >= ns) continue;
+            R hz[2 * N], d2[2 * N];
+            local_HZ<R, N, BQ>(M, S, sc, site, P, QP, zp[k], hz);
+            rhs_sun<R, N>(zp[k], ze[k], hz, dt, lam, d2);
+#pragma unroll
+            for (int c = 0; c < 2 * N; c++) z[k][c] = z[k][c] + (d1[k][c] + d2[c]) / 2;
+            normalize_ket<R, N>(z[k], __ldg(M.kappa + site));
+            publish<R, N, BQ>(sc, S.qm, z[k], ns, site, D, Qb);
+        }
+        if (step + 1 < nsteps) {
+            if (!sgb_grid_barrier(ctrl, gridDim.x)) return;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < SPT; k++) {
+        int site = tid + k * nthr;
+        if (site >= ns) continue;
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) Z[(size_t)c * ns + site] = z[k][c];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->steps_done = nsteps;
+}
+
+template <class R, int N>
+__device__ __forceinline__ void write_snapshot_sun(const Model<R>& M, const SnapArgs<R>& sn, int t, int site, const R* z) {
+    const int ns = M.ns;
+    const int cell = site % M.ncell, a = site / M.ncell;
+    for (int o = 0; o < sn.nobs; o++) {
+        const R* A = sn.ops + (size_t)o * 2 * N * N * ns;
+        R acc = 0;
+#pragma unroll
+        for (int c = 0; c < N; c++)
+#pragma unroll
+            for (int r = 0; r < N; r++) {
+                R ar = __ldg(A + (size_t)(2 * (r + N * c)) * ns + site);
+                R ai = __ldg(A + (size_t)(2 * (r + N * c) + 1) * ns + site);
+                R tr = ar * z[2 * c] - ai * z[2 * c + 1];
+                R ti = ar * z[2 * c + 1] + ai * z[2 * c];
+                acc += z[2 * r] * tr + z[2 * r + 1] * ti;
+            }
+        size_t idx = (((size_t)t * sn.nobs + o) * M.na + a) * M.ncell + cell;
+        sn.buf[2 * idx] = acc * sn.scale;
+        sn.buf[2 * idx + 1] = 0;
+    }
+}
+
+// Schrodinger midpoint (Integrators.jl:422-452). H: 3 rotating [3][ns] dipole buffers of
+// <Zbar|S|Zbar>; QH: 3 rotating [5][ns] quadrupole buffers.
+template <class R, int N, int SPT, bool BQ>
+__global__ void __launch_bounds__(SGB_BLOCK)
+k_sun_midpoint(Model<R> M, R* Z, R* D, R* Qb, R* H, R* QH, Ctrl* ctrl, int nsteps, R dt, R lam,
+               double atol2, int max_iters, SnapArgs<R> snap) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SunTab<R, N> S = stage_sun<R, N>(M, smem);
+    SpinConst<R, N> sc;
+    const int ns = M.ns;
+    const int nthr = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool leader = (blockIdx.x == 0 && threadIdx.x == 0);
+    R z[SPT][2 * N], zp[SPT][2 * N], zc[SPT][2 * N];
+    int cur = 0;
+#pragma unroll
+    for (int k = 0; k < SPT; k++) {
+        int site = tid + k * nthr;
+        if (site >= ns) continue;
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) z[k][c] = Z[(size_t)c * ns + site];
+        R zb[2 * N];
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) zb[c] = (z[k][c] + z[k][c]) / 2;
+        publish<R, N, BQ>(sc, S.qm, zb, ns, site, H, QH);
+        if (snap.enabled) write_snapshot_sun<R, N>(M, snap, snap.t0, site, z[k]);
+    }
+    if (leader) { ctrl->acc[0] = 0.0; ctrl->acc[1] = 0.0; ctrl->acc[2] = 0.0; }
+    if (!sgb_grid_barrier(ctrl, gridDim.x)) return;
+    long long itg = 0;
+    int done = 0;
+    for (int step = 0; step < nsteps; ++step) {
+#pragma unroll
+        for (int k = 0; k < SPT; k++)
+#pragma unroll
+            for (int c = 0; c < 2 * N; c++) zp[k][c] = z[k][c];
+        bool conv = false;
+        for (int it = 0; it < max_iters; ++it) {
+            const int nxt = (cur + 1) % 3, nst = (cur + 2) % 3;
+            const R* Hc = H + (size_t)cur * 3 * ns;
+            const R* Qc = QH + (size_t)cur * 5 * ns;
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < SPT; k++) {
+                int site = tid + k * nthr;
+                if (site >= ns) continue;
+                const R kap = __ldg(M.kappa + site);
+                R zb[2 * N], hz[2 * N], dz[2 * N], zero[2 * N];
+#pragma unroll
+                for (int c = 0; c < 2 * N; c++) { zb[c] = (z[k][c] + zp[k][c]) / 2; zero[c] = 0; }
+                local_HZ<R, N, BQ>(M, S, sc, site, Hc, Qc, zb, hz);
+                rhs_sun<R, N>(zb, zero, hz, dt, lam, dz);
+#pragma unroll
+                for (int c = 0; c < 2 * N; c++) {
+                    R q = z[k][c] + dz[c];
+                    double e = (double)(zp[k][c] - q);
+                    acc += e * e;
+                    zp[k][c] = q;
+                }
+#pragma unroll
+                for (int c = 0; c < 2 * N; c++) zb[c] = (z[k][c] + zp[k][c]) / 2;
+                publish<R, N, BQ>(sc, S.qm, zb, ns, site, H + (size_t)nxt * 3 * ns, QH + (size_t)nxt * 5 * ns);
+#pragma unroll
+                for (int c = 0; c < 2 * N; c++) zc[k][c] = zp[k][c];
+                normalize_ket<R, N>(zc[k], kap);
+#pragma unroll
+                for (int c = 0; c < 2 * N; c++) zb[c] = (zc[k][c] + zc[k][c]) / 2;
+                publish<R, N, BQ>(sc, S.qm, zb, ns, site, H + (size_t)nst * 3 * ns, QH + (size_t)nst * 5 * ns);
+            }
+            double bsum = sgb_block_sum<SGB_BLOCK>(acc);
+            const int slot = (int)(itg % 3);
+            if (threadIdx.x == 0) atomicAdd(&ctrl->acc[slot], bsum);
+            if (leader) { ctrl->acc[(slot + 1) % 3] = 0.0; ctrl->iters += 1; }
+            if (!sgb_grid_barrier(ctrl, gridDim.x)) return;
+            double tot = __ldcg(&ctrl->acc[slot]);
+            itg++;
+            if (tot <= atol2) {
+                conv = true;
+#pragma unroll
+                for (int k = 0; k < SPT; k++)
+#pragma unroll
+                    for (int c = 0; c < 2 * N; c++) z[k][c] = zc[k][c];
+                cur = nst;
+                break;
+            }
+            cur = nxt;
+        }
+        if (!conv) {
+            if (leader) sgb_set_status(ctrl, SGB_ERR_NOCONVERGE);
+            break;
+        }
+        done = step + 1;
+        if (snap.enabled && (done % snap.measperiod) == 0) {
+#pragma unroll
+            for (int k = 0; k < SPT; k++) {
+                int site = tid + k * nthr;
+                if (site < ns) write_snapshot_sun<R, N>(M, snap, snap.t0 + done / snap.measperiod, site, z[k]);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < SPT; k++) {
+        int site = tid + k * nthr;
+        if (site >= ns) continue;
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) Z[(size_t)c * ns + site] = z[k][c];
+        publish<R, N, BQ>(sc, S.qm, z[k], ns, site, D, Qb);
+    }
+    if (leader) ctrl->steps_done = done;
+}
+
+template <class R, int N>
+__global__ void __launch_bounds__(SGB_BLOCK) k_sun_refresh(Model<R> M, const R* Z, R* D, R* Qb) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SunTab<R, N> S = stage_sun<R, N>(M, smem);
+    SpinConst<R, N> sc;
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < M.ns; site += gridDim.x * blockDim.x) {
+        R z[2 * N];
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) z[c] = Z[(size_t)c * M.ns + site];
+        if (M.has_biquad) publish<R, N, true>(sc, S.qm, z, M.ns, site, D, Qb);
+        else publish<R, N, false>(sc, S.qm, z, M.ns, site, D, Qb);
+    }
+}
+
+template <class R, int N>
+__global__ void __launch_bounds__(SGB_BLOCK) k_sun_grad(Model<R> M, const R* Z, const R* D, const R* Qb, double* out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SunTab<R, N> S = stage_sun<R, N>(M, smem);
+    SpinConst<R, N> sc;
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < M.ns; site += gridDim.x * blockDim.x) {
+        R z[2 * N], hz[2 * N];
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) z[c] = Z[(size_t)c * M.ns + site];
+        if (M.has_biquad) local_HZ<R, N, true>(M, S, sc, site, D, Qb, z, hz);
+        else local_HZ<R, N, false>(M, S, sc, site, D, Qb, z, hz);
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) out[(size_t)site * 2 * N + c] = (double)hz[c];
+    }
+}
+
+// FP64 energy (Interactions.jl:401-508), SU(N) mode: partials[block][4].
+template <class R, int N>
+__global__ void __launch_bounds__(SGB_BLOCK) k_sun_energy(Model<R> M, const R* Z, const R* D, const R* Qb, double* partials) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SunTab<R, N> S = stage_sun<R, N>(M, smem);
+    const int ns = M.ns;
+    double E = 0, mx = 0, my = 0, mz = 0;
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < ns; site += gridDim.x * blockDim.x) {
+        SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
+        double sx = D[site], sy = D[ns + site], sz = D[2 * ns + site];
+        mx += sx; my += sy; mz += sz;
+        if (M.h) E += (double)M.h[site] * sx + (double)M.h[ns + site] * sy + (double)M.h[2 * ns + site] * sz;
+        double z[2 * N];
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) z[c] = Z[(size_t)c * ns + site];
+        const R* lam = S.lam + ix.a * 2 * N * N;
+        double eo = 0;
+#pragma unroll
+        for (int c = 0; c < N; c++)
+#pragma unroll
+            for (int r = 0; r < N; r++) {
+                double ar = lam[2 * (r + N * c)], ai = lam[2 * (r + N * c) + 1];
+                double tr = ar * z[2 * c] - ai * z[2 * c + 1], ti = ar * z[2 * c + 1] + ai * z[2 * c];
+                eo += z[2 * r] * tr + z[2 * r + 1] * ti;
+            }
+        E += eo;
+        double qi[5];
+        if (M.has_biquad) {
+            double qmd[5 * 2 * N * N];
+            for (int q = 0; q < 5 * 2 * N * N; q++) qmd[q] = (double)S.qm[q];
+            expected_quad<double, N>(qmd, z, qi);
+        }
+        const double ki = (double)M.kappa[site];
+        for (int b = S.t.boff[ix.a]; b < S.t.boff[ix.a + 1]; b++) {
+            const DBond<R>& B = S.t.bonds[b];
+            if (!B.fwd) continue;
+            int x1 = sgb_wrap_pos(ix.c1 + B.n[0], M.L1);
+            int x2 = sgb_wrap_pos(ix.c2 + B.n[1], M.L2);
+            int x3 = sgb_wrap_pos(ix.c3 + B.n[2], M.L3);
+            int js = x1 + M.L1 * (x2 + M.L2 * (x3 + M.L3 * B.j));
+            double tx = D[js], ty = D[ns + js], tz = D[2 * ns + js];
+            E += (double)B.scalar * ki * (double)M.kappa[js];
+            if (B.jkind == 0) E += (double)B.J[0] * (sx * tx + sy * ty + sz * tz);
+            else {
+                double jx = (double)B.J[0] * tx + (double)B.J[3] * ty + (double)B.J[6] * tz;
+                double jy = (double)B.J[1] * tx + (double)B.J[4] * ty + (double)B.J[7] * tz;
+                double jz = (double)B.J[2] * tx + (double)B.J[5] * ty + (double)B.J[8] * tz;
+                E += sx * jx + sy * jy + sz * jz;
+            }
+            if (M.has_biquad && B.bqkind != 0) {
+                double zj[2 * N], qj[5], qmd[5 * 2 * N * N];
+                for (int q = 0; q < 5 * 2 * N * N; q++) qmd[q] = (double)S.qm[q];
+#pragma unroll
+                for (int c = 0; c < 2 * N; c++) zj[c] = Z[(size_t)c * ns + js];
+                expected_quad<double, N>(qmd, zj, qj);
+                double acc = 0;
+                if (B.bqkind == 1) {
+                    for (int q = 0; q < 5; q++) acc += qi[q] * (biquad_metric(q) * qj[q]);
+                    acc *= (double)B.bq;
+                } else {
+                    const R* Bm = S.t.bq + 25 * B.bqidx;
+                    for (int q = 0; q < 5; q++)
+                        for (int p = 0; p < 5; p++) acc += qi[q] * (double)Bm[q + 5 * p] * qj[p];
+                }
+                E += acc;
+            }
+        }
+    }
+    double e = sgb_block_sum<SGB_BLOCK>(E);
+    double a0 = sgb_block_sum<SGB_BLOCK>(mx);
+    double a1 = sgb_block_sum<SGB_BLOCK>(my);
+    double a2 = sgb_block_sum<SGB_BLOCK>(mz);
+    if (threadIdx.x == 0) {
+        partials[4 * blockIdx.x + 0] = e;
+        partials[4 * blockIdx.x + 1] = a0;
+        partials[4 * blockIdx.x + 2] = a1;
+        partials[4 * blockIdx.x + 3] = a2;
+    }
+}
+
+template <class K>
+int set_smem(K kernel, size_t smem) {
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return SGB_ERR_CUDA;
+    return SGB_OK;
+}
+
+template <class K>
+int coop(K kernel, const LaunchInfo& li, void** args, cudaStream_t st) {
+    if (set_smem(kernel, li.smem) != SGB_OK) return SGB_ERR_CUDA;
+    return cudaLaunchCooperativeKernel((const void*)kernel, dim3(li.grid), dim3(li.block), args, li.smem, st) == cudaSuccess
+               ? SGB_OK : SGB_ERR_CUDA;
+}
+
+template <class R, int N>
+int heun_n(const Model<R>& M, void** args, bool inject, const LaunchInfo& li, cudaStream_t st) {
+    const bool bq = M.has_biquad != 0;
+    if (li.spt == 1) {
+        if (inject) return bq ? coop(k_sun_heun<R, N, 1, true, true>, li, args, st) : coop(k_sun_heun<R, N, 1, true, false>, li, args, st);
+        return bq ? coop(k_sun_heun<R, N, 1, false, true>, li, args, st) : coop(k_sun_heun<R, N, 1, false, false>, li, args, st);
+    }
+    if (li.spt == 2) {
+        if (inject) return bq ? coop(k_sun_heun<R, N, 2, true, true>, li, args, st) : coop(k_sun_heun<R, N, 2, true, false>, li, args, st);
+        return bq ? coop(k_sun_heun<R, N, 2, false, true>, li, args, st) : coop(k_sun_heun<R, N, 2, false, false>, li, args, st);
+    }
+    return SGB_ERR_ARG;
+}
+
+template <class R, int N>
+int mid_n(const Model<R>& M, void** args, const LaunchInfo& li, cudaStream_t st) {
+    const bool bq = M.has_biquad != 0;
+    if (li.spt == 1) return bq ? coop(k_sun_midpoint<R, N, 1, true>, li, args, st) : coop(k_sun_midpoint<R, N, 1, false>, li, args, st);
+    if (li.spt == 2) return bq ? coop(k_sun_midpoint<R, N, 2, true>, li, args, st) : coop(k_sun_midpoint<R, N, 2, false>, li, args, st);
+    return SGB_ERR_ARG;
+}
+
+template <class R, int N>
+int occ_n(int spt, size_t smem, int* bps) {
+    int best = 1 << 30, a = 0;
+    auto one = [&](auto k) -> int {
+        if (set_smem(k, smem) != SGB_OK) return SGB_ERR_CUDA;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k, SGB_BLOCK, smem) != cudaSuccess) return SGB_ERR_CUDA;
+        best = a < best ? a : best;
+        return SGB_OK;
+    };
+    int rc = SGB_OK;
+    if (spt == 1) {
+        rc |= one(k_sun_heun<R, N, 1, true, true>); rc |= one(k_sun_heun<R, N, 1, false, true>);
+        rc |= one(k_sun_heun<R, N, 1, true, false>); rc |= one(k_sun_heun<R, N, 1, false, false>);
+        rc |= one(k_sun_midpoint<R, N, 1, true>); rc |= one(k_sun_midpoint<R, N, 1, false>);
+    } else if (spt == 2) {
+        rc |= one(k_sun_heun<R, N, 2, true, true>); rc |= one(k_sun_heun<R, N, 2, false, true>);
+        rc |= one(k_sun_heun<R, N, 2, true, false>); rc |= one(k_sun_heun<R, N, 2, false, false>);
+        rc |= one(k_sun_midpoint<R, N, 2, true>); rc |= one(k_sun_midpoint<R, N, 2, false>);
+    } else return SGB_ERR_ARG;
+    if (rc != SGB_OK) return SGB_ERR_CUDA;
+    *bps = best;
+    return SGB_OK;
+}
+
+template <class R, int N>
+int grid1d(const Model<R>& M) {
+    int grid = (M.ns + SGB_BLOCK - 1) / SGB_BLOCK;
+    return grid > 4096 ? 4096 : grid;
+}
+
+}  // namespace
+
+#define SGB_SUN_DISPATCH(EXPR2, EXPR3, EXPR4, EXPR5) \
+    switch (M.N) {                                  \
+        case 2: return EXPR2;                       \
+        case 3: return EXPR3;                       \
+        case 4: return EXPR4;                       \
+        case 5: return EXPR5;                       \
+    }                                               \
+    return SGB_ERR_ARG;
+
+template <class R>
+int sun_launch_heun(const Model<R>& M, R* Z, R* D, R* Q, R* P, R* QP, Ctrl* ctrl, int nsteps, double dt,
+                    double lam, double noise_scale, uint64_t seed, uint64_t step0, const double* noise,
+                    const LaunchInfo& li, cudaStream_t st) {
+    Model<R> m = M;
+    R rdt = (R)dt, rlam = (R)lam, rns = (R)noise_scale;
+    void* args[] = {&m, &Z, &D, &Q, &P, &QP, &ctrl, &nsteps, &rdt, &rlam, &rns, &seed, &step0, &noise};
+    bool inj = noise != nullptr;
+    SGB_SUN_DISPATCH((heun_n<R, 2>(M, args, inj, li, st)), (heun_n<R, 3>(M, args, inj, li, st)),
+                     (heun_n<R, 4>(M, args, inj, li, st)), (heun_n<R, 5>(M, args, inj, li, st)))
+}
+
+template <class R>
+int sun_launch_midpoint(const Model<R>& M, R* Z, R* D, R* Q, R* H, R* QH, Ctrl* ctrl, int nsteps, double dt,
+                        double lam, double atol2, int max_iters, const SnapArgs<R>& snap, const LaunchInfo& li,
+                        cudaStream_t st) {
+    Model<R> m = M;
+    SnapArgs<R> sn = snap;
+    R rdt = (R)dt, rlam = (R)lam;
+    void* args[] = {&m, &Z, &D, &Q, &H, &QH, &ctrl, &nsteps, &rdt, &rlam, &atol2, &max_iters, &sn};
+    SGB_SUN_DISPATCH((mid_n<R, 2>(M, args, li, st)), (mid_n<R, 3>(M, args, li, st)), (mid_n<R, 4>(M, args, li, st)),
+                     (mid_n<R, 5>(M, args, li, st)))
+}
+
+template <class R>
+int sun_max_blocks(int N, int spt, size_t smem, int* bps) {
+    switch (N) {
+        case 2: return occ_n<R, 2>(spt, smem, bps);
+        case 3: return occ_n<R, 3>(spt, smem, bps);
+        case 4: return occ_n<R, 4>(spt, smem, bps);
+        case 5: return occ_n<R, 5>(spt, smem, bps);
+    }
+    return SGB_ERR_ARG;
+}
+
+#define SGB_SIMPLE_LAUNCH(KER, ...)                                                               \
+    do {                                                                                          \
+        size_t smem = (size_t)M.tables_bytes;                                                     \
+        if (set_smem(KER, smem) != SGB_OK) return SGB_ERR_CUDA;                                   \
+        KER<<<grid1d<R, 2>(M), SGB_BLOCK, smem, st>>>(__VA_ARGS__);                               \
+        return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;                         \
+    } while (0)
+
+template <class R, int N>
+static int refresh_n(const Model<R>& M, const R* Z, R* D, R* Q, cudaStream_t st) { SGB_SIMPLE_LAUNCH((k_sun_refresh<R, N>), M, Z, D, Q); }
+template <class R, int N>
+static int grad_n(const Model<R>& M, const R* Z, const R* D, const R* Q, double* g, cudaStream_t st) { SGB_SIMPLE_LAUNCH((k_sun_grad<R, N>), M, Z, D, Q, g); }
+template <class R, int N>
+static int energy_n(const Model<R>& M, const R* Z, const R* D, const R* Q, double* p, int nb, cudaStream_t st) {
+    size_t smem = (size_t)M.tables_bytes;
+    if (set_smem(k_sun_energy<R, N>, smem) != SGB_OK) return SGB_ERR_CUDA;
+    k_sun_energy<R, N><<<nb, SGB_BLOCK, smem, st>>>(M, Z, D, Q, p);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+template <class R>
+int sun_launch_refresh(const Model<R>& M, const R* Z, R* D, R* Q, cudaStream_t st) {
+    SGB_SUN_DISPATCH((refresh_n<R, 2>(M, Z, D, Q, st)), (refresh_n<R, 3>(M, Z, D, Q, st)), (refresh_n<R, 4>(M, Z, D, Q, st)),
+                     (refresh_n<R, 5>(M, Z, D, Q, st)))
+}
+template <class R>
+int sun_launch_grad(const Model<R>& M, const R* Z, const R* D, const R* Q, double* grad, cudaStream_t st) {
+    SGB_SUN_DISPATCH((grad_n<R, 2>(M, Z, D, Q, grad, st)), (grad_n<R, 3>(M, Z, D, Q, grad, st)),
+                     (grad_n<R, 4>(M, Z, D, Q, grad, st)), (grad_n<R, 5>(M, Z, D, Q, grad, st)))
+}
+template <class R>
+int sun_launch_energy(const Model<R>& M, const R* Z, const R* D, const R* Q, double* partials, int nblocks, cudaStream_t st) {
+    SGB_SUN_DISPATCH((energy_n<R, 2>(M, Z, D, Q, partials, nblocks, st)), (energy_n<R, 3>(M, Z, D, Q, partials, nblocks, st)),
+                     (energy_n<R, 4>(M, Z, D, Q, partials, nblocks, st)), (energy_n<R, 5>(M, Z, D, Q, partials, nblocks, st)))
+}
+
+#define SGB_SUN_INST(R)                                                                                         \
+    template int sun_launch_heun<R>(const Model<R>&, R*, R*, R*, R*, R*, Ctrl*, int, double, double, double,    \
+                                    uint64_t, uint64_t, const double*, const LaunchInfo&, cudaStream_t);        \
+    template int sun_launch_midpoint<R>(const Model<R>&, R*, R*, R*, R*, R*, Ctrl*, int, double, double, double, \
+                                        int, const SnapArgs<R>&, const LaunchInfo&, cudaStream_t);              \
+    template int sun_max_blocks<R>(int, int, size_t, int*);                                                     \
+    template int sun_launch_refresh<R>(const Model<R>&, const R*, R*, R*, cudaStream_t);                        \
+    template int sun_launch_grad<R>(const Model<R>&, const R*, const R*, const R*, double*, cudaStream_t);      \
+    template int sun_launch_energy<R>(const Model<R>&, const R*, const R*, const R*, double*, int, cudaStream_t);
+SGB_SUN_INST(float)
+SGB_SUN_INST(double)

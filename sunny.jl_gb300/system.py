@@ -1,0 +1,520 @@
+"""`System`, integrators and `step` -- a host-side mirror of Sunny.jl's API whose hot path
+runs in libsunnygb300.so.
+
+Names, argument meanings and error messages follow Sunny.jl v0.9.2
+(src/System/System.jl, src/System/Interactions.jl, src/System/PairExchange.jl,
+src/System/OnsiteCoupling.jl, src/Integrators.jl). Julia's `!` suffix is dropped:
+`step!(sys, integrator)` is `step(sys, integrator)`. Atom indices are 1-based, as in Sunny.
+
+The spin state lives on the GPU. `sys.dipoles` / `sys.coherents` return numpy views of a
+host copy that is refreshed from the device on access; writes through those views are
+uploaded before the next device call (the host copy is treated as modified whenever it
+has been handed out).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from .crystal import Bond, Crystal
+from .operators import (rcs_factors, spin_matrices_of_dim, stevens_expansion_for_dipole, expected_spin,
+                        ket_from_dipole)
+
+_MODES = {"dipole": _abi.MODE_DIPOLE, "dipole_uncorrected": _abi.MODE_DIPOLE_UNCORRECTED, "SUN": _abi.MODE_SUN}
+
+
+@dataclass
+class Moment:
+    """Moment(s, g) (src/System/Moment.jl:13-23)."""
+    s: float
+    g: object = 2.0
+
+    def gmat(self) -> np.ndarray:
+        g = np.asarray(self.g, dtype=float)
+        return g * np.eye(3) if g.ndim == 0 else g.reshape(3, 3)
+
+
+class Langevin:
+    """Langevin(dt; damping, kT) (src/Integrators.jl:56-74)."""
+
+    def __init__(self, dt=math.nan, *, damping=None, kT):
+        if damping is None:
+            raise ValueError("`damping` parameter required")
+        if damping == 0:
+            raise ValueError("Use ImplicitMidpoint instead for energy-conserving dynamics")
+        if dt <= 0:
+            raise ValueError("Select positive dt")
+        if kT < 0:
+            raise ValueError("Select nonnegative kT")
+        if damping <= 0:
+            raise ValueError("Select positive damping")
+        self.dt, self.damping, self.kT = float(dt), float(damping), float(kT)
+
+    def copy(self):
+        return Langevin(self.dt, damping=self.damping, kT=self.kT)
+
+
+class ImplicitMidpoint:
+    """ImplicitMidpoint(dt; damping=0, kT=0, tol=1e-12) (src/Integrators.jl:107-131)."""
+
+    def __init__(self, dt=math.nan, *, damping=0.0, kT=0.0, tol=1e-12):
+        if dt <= 0:
+            raise ValueError("Select positive dt")
+        if kT < 0:
+            raise ValueError("Select nonnegative kT")
+        if damping < 0:
+            raise ValueError("Select nonnegative damping")
+        if kT != 0:
+            raise ValueError("ImplicitMidpoint with a Langevin thermostat is not currently supported.")
+        self.dt, self.damping, self.kT, self.tol = float(dt), float(damping), float(kT), float(tol)
+
+    def copy(self):
+        return ImplicitMidpoint(self.dt, damping=self.damping, kT=self.kT, tol=self.tol)
+
+
+@dataclass
+class PairCoupling:
+    scalar: float
+    bilin: np.ndarray        # 3x3
+    biquad: object           # 0.0, float, or 5x5
+
+
+class System:
+    """System(crystal, moments, mode; dims, seed) (src/System/System.jl:33-93)."""
+
+    def __init__(self, crystal: Crystal, moments, mode: str, dims=(1, 1, 1), seed=None,
+                 precision: str = "fp64", device: int | None = 0):
+        """`device=None` builds the host tables only (no GPU handle); such a System can
+        feed the CPU oracle but cannot step."""
+        mode = mode.lstrip(":")
+        if mode not in _MODES:
+            raise ValueError("Mode must be `:SUN`, `:dipole`, or `:dipole_uncorrected`")
+        self.crystal = crystal
+        self.mode = mode
+        self.dims = tuple(int(x) for x in dims)
+        na = crystal.natoms
+        self.natoms = na
+        mom = dict(moments)
+        if len(mom) == 1 and na > 1 and 1 in mom:
+            mom = {i: mom[1] for i in range(1, na + 1)}
+        if sorted(mom) != list(range(1, na + 1)):
+            raise ValueError("a Moment is required for every atom (or one Moment for all)")
+        self.moments = [mom[i] for i in range(1, na + 1)]
+        Ns = [int(round(2 * m.s + 1)) for m in self.moments]
+        if mode == "SUN":
+            if len(set(Ns)) != 1:
+                raise ValueError("Currently all spins S must be equal in SU(N) mode")
+            self.N = Ns[0]
+        else:
+            self.N = 0
+        L1, L2, L3 = self.dims
+        self.ncell = L1 * L2 * L3
+        self.nsites = self.ncell * na
+        ns = self.nsites
+        self.precision = precision
+        atom = np.repeat(np.arange(na), self.ncell)
+        self._atom_of_site = atom
+        kap = np.array([m.s for m in self.moments]) if mode != "SUN" else np.ones(na)
+        self._kappa = np.ascontiguousarray(kap[atom].astype(float))
+        self._g = np.ascontiguousarray(np.stack([self.moments[a].gmat() for a in atom]))     # (ns, 3, 3)
+        self._field = np.zeros((ns, 3))
+        self._pairs: dict[Bond, PairCoupling] = {}
+        self._onsite = [None] * na
+        self._base_dip = np.zeros((na, L3, L2, L1, 3))
+        self._base_coh = np.zeros((na, L3, L2, L1, max(self.N, 1)), dtype=complex)
+        self.rng = np.random.default_rng(seed)
+        self.seed = int(seed) if seed is not None else int(self.rng.integers(0, 2**62))
+        self.noise_step = 0
+        self._couplings_dirty = True
+        self._host_newer = True
+        self._dev_newer = False
+        self._h = None
+        self._lib = None
+        if device is None:
+            self.polarize_spins((0, 0, 1))
+            return
+        self._lib = _abi.load()
+        d = _abi.Desc()
+        d.dims[:] = self.dims
+        d.natoms, d.N, d.mode = na, self.N, _MODES[mode]
+        d.precision = _abi.FP32 if precision == "fp32" else _abi.FP64
+        d.device = device
+        h = C.c_void_p()
+        _abi.check(self._lib.sgb_create(C.byref(d), C.byref(h)), self._lib, None)
+        self._h = h
+        self.polarize_spins((0, 0, 1))
+
+    # ---- lifetime -------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) and self._lib is not None:
+            self._lib.sgb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ---- state views ------------------------------------------------------------------
+    def _sync_to_host(self):
+        if self._dev_newer:
+            dip = np.empty((self.nsites, 3))
+            coh = np.empty((self.nsites, self.N, 2)) if self.N else None
+            _abi.check(self._lib.sgb_get_state(self._h, _abi.dptr(dip), _abi.dptr(coh)), self._lib, self._h)
+            self._base_dip.reshape(-1, 3)[:] = dip
+            if self.N:
+                self._base_coh.reshape(-1, self.N)[:] = coh[..., 0] + 1j * coh[..., 1]
+            self._dev_newer = False
+
+    def _sync_to_device(self):
+        if self._h is None:
+            raise RuntimeError("this System was built without a device (device=None)")
+        if self._couplings_dirty:
+            self._upload_couplings()
+        if self._host_newer:
+            if self.N:
+                coh = np.ascontiguousarray(np.stack([self._base_coh.real, self._base_coh.imag], -1).reshape(-1))
+                _abi.check(self._lib.sgb_set_state(self._h, None, _abi.dptr(coh)), self._lib, self._h)
+            else:
+                dip = np.ascontiguousarray(self._base_dip.reshape(-1))
+                _abi.check(self._lib.sgb_set_state(self._h, _abi.dptr(dip), None), self._lib, self._h)
+            self._host_newer = False
+
+    @property
+    def dipoles(self) -> np.ndarray:
+        """Array indexed [c1, c2, c3, atom, component] (0-based), like Sunny's sys.dipoles."""
+        self._sync_to_host()
+        self._host_newer = True
+        return self._base_dip.transpose(3, 2, 1, 0, 4)
+
+    @property
+    def coherents(self) -> np.ndarray:
+        self._sync_to_host()
+        self._host_newer = True
+        return self._base_coh.transpose(3, 2, 1, 0, 4)
+
+    def dipoles_flat(self) -> np.ndarray:
+        """Copy of the dipoles in site order (ns, 3)."""
+        self._sync_to_host()
+        return self._base_dip.reshape(-1, 3).copy()
+
+    def coherents_flat(self) -> np.ndarray:
+        self._sync_to_host()
+        return self._base_coh.reshape(-1, self.N).copy()
+
+    def set_state_flat(self, dipoles=None, coherents=None):
+        self._sync_to_host()
+        if dipoles is not None:
+            self._base_dip.reshape(-1, 3)[:] = dipoles
+        if coherents is not None:
+            self._base_coh.reshape(-1, self.N)[:] = coherents
+            self._base_dip.reshape(-1, 3)[:] = expected_spin(np.asarray(coherents))
+        self._host_newer = True
+
+    @property
+    def kappas(self) -> np.ndarray:
+        return self._kappa
+
+    def set_kappas(self, kappa):
+        """Rescale |S| = κ (dipole) or |Z|² = κ (SU(N)) per site, keeping directions."""
+        self._sync_to_host()
+        self._kappa[:] = np.broadcast_to(np.asarray(kappa, dtype=float), self._kappa.shape)
+        flatd = self._base_dip.reshape(-1, 3)
+        if self.N:
+            flatz = self._base_coh.reshape(-1, self.N)
+            nz = np.linalg.norm(flatz, axis=1)
+            flatz[:] = np.where(self._kappa[:, None] == 0, 0, flatz / np.where(nz == 0, 1, nz)[:, None] * np.sqrt(self._kappa)[:, None])
+            flatd[:] = expected_spin(flatz)
+        else:
+            nd = np.linalg.norm(flatd, axis=1)
+            flatd[:] = np.where(self._kappa[:, None] == 0, 0, flatd / np.where(nd == 0, 1, nd)[:, None] * self._kappa[:, None])
+        self._host_newer = True
+        self._couplings_dirty = True
+
+    # ---- site helpers -------------------------------------------------------------------
+    def site_index(self, c1, c2, c3, a) -> int:
+        """0-based linear site of (c1, c2, c3, atom), all 1-based as Sunny's Site."""
+        L1, L2, L3 = self.dims
+        return (c1 - 1) + L1 * ((c2 - 1) + L2 * ((c3 - 1) + L3 * (a - 1)))
+
+    def spin_label(self, i: int) -> float:
+        return self.moments[i - 1].s
+
+    # ---- couplings --------------------------------------------------------------------
+    def _upload_couplings(self):
+        lib, h = self._lib, self._h
+        _abi.check(lib.sgb_set_sites(h, _abi.dptr(self._kappa), _abi.dptr(np.ascontiguousarray(self._g.transpose(0, 2, 1)).reshape(-1)),
+                                     _abi.dptr(np.ascontiguousarray(self._field.reshape(-1)))), lib, h)
+        for a in range(self.natoms):
+            oc = self._onsite[a]
+            if self.N:
+                M = np.zeros((self.N, self.N), dtype=complex) if oc is None else oc
+                arr = np.ascontiguousarray(np.stack([M.T.real, M.T.imag], -1).reshape(-1))  # column-major
+            else:
+                arr = np.zeros(28) if oc is None else np.ascontiguousarray(oc, dtype=float)
+            _abi.check(lib.sgb_set_onsite(h, a, _abi.dptr(arr)), lib, h)
+        bonds = self.bond_table()
+        arr = (_abi.BondC * max(1, len(bonds)))()
+        for k, b in enumerate(bonds):
+            arr[k] = b
+        _abi.check(lib.sgb_set_bonds(h, arr, len(bonds)), lib, h)
+        self._couplings_dirty = False
+
+    def bond_table(self):
+        """Non-culled pair couplings in the C layout (0-based atoms, column-major J)."""
+        out = []
+        for b, pc in self._pairs.items():
+            e = _abi.BondC()
+            e.i, e.j = b.i - 1, b.j - 1
+            e.n[:] = b.n
+            e.scalar = pc.scalar
+            e.bilin[:] = list(np.asarray(pc.bilin, dtype=float).T.reshape(-1))
+            if isinstance(pc.biquad, np.ndarray):
+                e.biquad_kind = 2
+                e.biquad[:] = list(pc.biquad.T.reshape(-1))
+            elif pc.biquad != 0:
+                e.biquad_kind = 1
+                e.biquad[0] = float(pc.biquad)
+            out.append(e)
+        return out
+
+    def set_pair_coupling(self, bond: Bond, scalar: float, bilin, biquad):
+        """Set one coupling on `bond` and its equivalents (PairExchange.jl:185-244)."""
+        J = np.asarray(bilin, dtype=float)
+        J = J * np.eye(3) if J.ndim == 0 else J.reshape(3, 3)
+        if bond.i == bond.j and all(x == 0 for x in bond.n):
+            raise ValueError("Bond must connect different atoms.")
+        for k in (bond.i, bond.j):
+            if not 1 <= k <= self.natoms:
+                raise ValueError(f"Atom index {k} is out of range.")
+        if self.mode == "dipole":
+            biquad = biquad * rcs_factors(self.spin_label(bond.i))[2] * rcs_factors(self.spin_label(bond.j))[2]
+        for b, Jb in self.crystal.equivalent_bonds(bond, J):
+            bq = biquad
+            if isinstance(bq, np.ndarray) and not b == bond:
+                raise ValueError("matrix biquadratic couplings are set per bond")
+            self._pairs[b] = PairCoupling(float(scalar), Jb, bq)
+        self._couplings_dirty = True
+
+    def set_bond_coupling(self, bond: Bond, scalar: float, bilin, biquad):
+        """Set a coupling on exactly one bond (and its reverse), without propagation. In
+        dipole mode the biquadratic part is renormalised by the RCS factors like
+        set_pair_coupling_at! (PairExchange.jl:447-468)."""
+        from .crystal import bond_parity
+        J = np.asarray(bilin, dtype=float)
+        J = J * np.eye(3) if J.ndim == 0 else J.reshape(3, 3)
+        if bond.i == bond.j and all(x == 0 for x in bond.n):
+            raise ValueError("Bond must connect different atoms.")
+        if self.mode == "dipole":
+            biquad = biquad * rcs_factors(self.spin_label(bond.i))[2] * rcs_factors(self.spin_label(bond.j))[2]
+        if not bond_parity(bond):
+            bond, J = bond.reverse(), J.T
+            if isinstance(biquad, np.ndarray):
+                biquad = biquad.T
+        self._pairs[bond] = PairCoupling(float(scalar), J, biquad)
+        self._couplings_dirty = True
+
+    def set_exchange(self, J, bond: Bond, biquad: float = 0.0):
+        """set_exchange!(sys, J, bond; biquad) with adapt_for_biquad (PairExchange.jl:300-385)."""
+        J = np.asarray(J, dtype=float)
+        J = J * np.eye(3) if J.ndim == 0 else J.reshape(3, 3)
+        scalar = 0.0
+        biquad = float(biquad)
+        if biquad != 0:
+            if self.mode in ("SUN", "dipole"):
+                s1, s2 = self.spin_label(bond.i), self.spin_label(bond.j)
+                J = J - (biquad / 2) * np.eye(3)
+                scalar += biquad * s1 * (s1 + 1) * s2 * (s2 + 1) / 3
+            else:
+                s1, s2 = self.spin_label(bond.i), self.spin_label(bond.j)
+                scalar += biquad * s1**2 * s2**2 / 3
+        self.set_pair_coupling(bond, scalar, J, biquad)
+
+    def set_onsite_coupling(self, op, i: int, atoms=None):
+        """set_onsite_coupling!(sys, op, i) (OnsiteCoupling.jl:159-210). `op` is an N x N
+        matrix in the spin-s representation of atom i, or a function of (Sx, Sy, Sz).
+        Sunny propagates the coupling to symmetry-equivalent atoms; here the coupling is
+        applied to atom i and to any extra `atoms` listed."""
+        if not 1 <= i <= self.natoms:
+            raise ValueError(f"Atom index {i} is out of range.")
+        s = self.spin_label(i)
+        N = int(round(2 * s + 1))
+        if callable(op):
+            op = op(*spin_matrices_of_dim(N))
+        A = np.asarray(op, dtype=complex)
+        if A.shape != (N, N):
+            raise ValueError("Invalid matrix size.")
+        if not np.allclose(A, A.conj().T):
+            raise ValueError("Operator is not Hermitian")
+        if N == 2:
+            if self.mode == "dipole":
+                raise ValueError("Consider mode :dipole_uncorrected. Onsite coupling is trivial for quantum spin 1/2.")
+            if self.mode == "SUN":
+                raise ValueError("Onsite coupling is trivial for quantum spin 1/2.")
+        if self.mode == "SUN":
+            val = A
+        elif self.mode == "dipole":
+            val = stevens_expansion_for_dipole((A + A.conj().T) / 2, s, renormalize=True)
+        else:
+            raise ValueError("System with mode :dipole_uncorrected requires Stevens coefficients (use set_onsite_stevens)")
+        for a in [i] + list(atoms or []):
+            self._onsite[a - 1] = val
+        self._couplings_dirty = True
+
+    def set_onsite_stevens(self, coeffs28, i: int, atoms=None):
+        """Dipole modes: set the 28 (already renormalised) Stevens coefficients directly."""
+        if self.N:
+            raise ValueError("Stevens coefficients are for dipole modes")
+        c = np.asarray(coeffs28, dtype=float).reshape(28)
+        for a in [i] + list(atoms or []):
+            self._onsite[a - 1] = c.copy()
+        self._couplings_dirty = True
+
+    def set_field(self, B):
+        """set_field!(sys, B) (Interactions.jl:210-214); B already scaled by μB."""
+        self._field[:] = np.asarray(B, dtype=float).reshape(3)
+        self._couplings_dirty = True
+
+    def set_field_at(self, B, site: int):
+        self._field[site] = np.asarray(B, dtype=float).reshape(3)
+        self._couplings_dirty = True
+
+    # ---- state initialisation -------------------------------------------------------------
+    def polarize_spins(self, direction):
+        """polarize_spins!(sys, dir) (System.jl:566-570)."""
+        d = np.asarray(direction, dtype=float)
+        self._sync_to_host()
+        flatd = self._base_dip.reshape(-1, 3)
+        if self.N:
+            z = ket_from_dipole(d, self.N)
+            z = z / np.sqrt(np.vdot(z, z).real)
+            flatz = self._base_coh.reshape(-1, self.N)
+            flatz[:] = z[None, :] * np.sqrt(self._kappa)[:, None]
+            flatd[:] = expected_spin(flatz)
+        else:
+            flatd[:] = self._kappa[:, None] * (d / np.linalg.norm(d))[None, :]
+        self._host_newer = True
+
+    def randomize_spins(self):
+        """randomize_spins!(sys) (System.jl:444-452, 513-517)."""
+        self._sync_to_host()
+        ns = self.nsites
+        if self.N:
+            z = self.rng.standard_normal((ns, self.N)) + 1j * self.rng.standard_normal((ns, self.N))
+            nz = np.sqrt(np.sum(np.abs(z) ** 2, axis=1) / np.where(self._kappa == 0, 1, self._kappa))
+            z = np.where(self._kappa[:, None] == 0, 0, z / nz[:, None])
+            self._base_coh.reshape(-1, self.N)[:] = z
+            self._base_dip.reshape(-1, 3)[:] = expected_spin(z)
+        else:
+            v = self.rng.standard_normal((ns, 3))
+            self._base_dip.reshape(-1, 3)[:] = self._kappa[:, None] * v / np.linalg.norm(v, axis=1)[:, None]
+        self._host_newer = True
+
+
+# ---- free functions mirroring Sunny's exported API -----------------------------------------
+
+def set_exchange(sys: System, J, bond: Bond, biquad: float = 0.0):
+    sys.set_exchange(J, bond, biquad)
+
+
+def set_onsite_coupling(sys: System, op, i: int, atoms=None):
+    sys.set_onsite_coupling(op, i, atoms)
+
+
+def set_field(sys: System, B):
+    sys.set_field(B)
+
+
+def randomize_spins(sys: System):
+    sys.randomize_spins()
+
+
+def polarize_spins(sys: System, direction):
+    sys.polarize_spins(direction)
+
+
+def energy(sys: System) -> float:
+    """energy(sys) in FP64 (Interactions.jl:401-432)."""
+    sys._sync_to_device()
+    E = C.c_double()
+    _abi.check(sys._lib.sgb_energy(sys._h, C.byref(E), None), sys._lib, sys._h)
+    return E.value
+
+
+def energy_per_site(sys: System) -> float:
+    return energy(sys) / sys.nsites
+
+
+def magnetization(sys: System) -> np.ndarray:
+    """sum(sys.dipoles) in FP64 (ParallelTempering.jl:31)."""
+    sys._sync_to_device()
+    M = np.zeros(3)
+    _abi.check(sys._lib.sgb_energy(sys._h, None, _abi.dptr(M)), sys._lib, sys._h)
+    return M
+
+
+def energy_grad(sys: System) -> np.ndarray:
+    """energy_grad_dipoles / energy_grad_coherents (Interactions.jl:689-698), site order."""
+    sys._sync_to_device()
+    if sys.N:
+        out = np.zeros((sys.nsites, sys.N, 2))
+        _abi.check(sys._lib.sgb_energy_grad(sys._h, _abi.dptr(out)), sys._lib, sys._h)
+        return out[..., 0] + 1j * out[..., 1]
+    out = np.zeros((sys.nsites, 3))
+    _abi.check(sys._lib.sgb_energy_grad(sys._h, _abi.dptr(out)), sys._lib, sys._h)
+    return out
+
+
+def step(sys: System, integrator, nsteps: int = 1, noise: np.ndarray | None = None, max_iters: int = 100) -> int:
+    """step!(sys, integrator), `nsteps` times (Integrators.jl:309-452).
+
+    Langevin noise comes from the device generator keyed by (sys.seed, step counter),
+    or from `noise` (standard normals, [nsteps][ns][3] or complex [nsteps][ns][N]).
+    Returns the number of midpoint iterations (0 for Langevin)."""
+    if math.isnan(integrator.dt):
+        raise ValueError("Set integration timestep `dt`.")
+    sys._sync_to_device()
+    lib, h = sys._lib, sys._h
+    if isinstance(integrator, Langevin):
+        nz = None
+        if noise is not None:
+            noise = np.asarray(noise)
+            if sys.N:
+                noise = np.stack([noise.real, noise.imag], -1)
+            nz = np.ascontiguousarray(noise, dtype=float).reshape(-1)
+            per = sys.nsites * (2 * sys.N if sys.N else 3)
+            if nz.size != per * nsteps:
+                raise ValueError("noise must hold nsteps x nsites x components normals")
+        rc = lib.sgb_langevin(h, integrator.dt, integrator.damping, integrator.kT, sys.seed, sys.noise_step, nsteps,
+                              _abi.dptr(nz))
+        sys.noise_step += nsteps
+        sys._dev_newer = True
+        _abi.check(rc, lib, h)
+        return 0
+    if isinstance(integrator, ImplicitMidpoint):
+        iters = C.c_int64()
+        rc = lib.sgb_midpoint(h, integrator.dt, integrator.damping, integrator.tol, max_iters, nsteps, C.byref(iters))
+        sys._dev_newer = True
+        _abi.check(rc, lib, h)
+        return iters.value
+    raise TypeError(f"unsupported integrator {type(integrator).__name__}")
+
+
+def langevin_noise(sys: System, step_index: int) -> np.ndarray:
+    """The standard normals the device generator uses for step `step_index` of sys.seed."""
+    per = sys.nsites * (2 * sys.N if sys.N else 3)
+    out = np.zeros(per)
+    _abi.check(sys._lib.sgb_langevin_noise(sys._h, sys.seed, step_index, _abi.dptr(out)), sys._lib, sys._h)
+    if sys.N:
+        o = out.reshape(sys.nsites, sys.N, 2)
+        return o[..., 0] + 1j * o[..., 1]
+    return out.reshape(sys.nsites, 3)

@@ -1,0 +1,130 @@
+"""SampledCorrelations parity: the GPU accumulator (sum of conj(A)A products, window
+applied at read-out) against the oracle's per-sample windowed running mean
+(CorrelationSampling.jl:48-139), plus the reference's RNG-independent identities."""
+import numpy as np
+import pytest
+
+from models import oracle_of, rich_sun
+
+pytestmark = pytest.mark.gpu
+
+
+def diamond_reference_model(sg, precision="fp64"):
+    # the configuration of test_correlation_sampling.jl:156-169 (diamond 2x3x4, s=3/2, J=0.6498)
+    sys_ = sg.System(sg.diamond_crystal(), [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(2, 3, 4), seed=101,
+                     precision=precision)
+    sys_.set_exchange(0.6498, sg.Bond(1, 3, [0, 0, 0]))
+    sys_.randomize_spins()
+    return sys_
+
+
+def oracle_corr(orc, sys_, sc):
+    o = oracle_of(orc, sys_)
+    obs = sc.measure.observables
+    if sys_.N:
+        flat = np.stack([np.swapaxes(obs, -1, -2).real, np.swapaxes(obs, -1, -2).imag], -1).reshape(-1)
+    else:
+        flat = obs.reshape(-1)
+    return o, orc.OracleCorrelations(o, flat, sc.measure.nobs, sc.measure.corr_pairs, sc.n_all_omega, sc.measperiod,
+                                     sc.dt, sc.integrator.tol)
+
+
+@pytest.mark.parametrize("window", ["cosine", "rectangular"])
+def test_sqw_parity_fp64(gpu, sg, orc, window):
+    sys_ = diamond_reference_model(sg)
+    sc = sg.SampledCorrelations(sys_, measure=sg.ssf_perp(sys_), energies=np.linspace(0.0, 5.5, 10), dt=0.12)
+    o, oc = oracle_corr(orc, sys_, sc)
+    S = sys_.dipoles_flat()
+    for _ in range(3):
+        sg.add_sample(sc, sys_, window=window)
+        S, _ = oc.add_sample(S, None, window=window)
+        # Langevin decorrelation between samples, identical noise on both sides
+    assert sc.nsamples == 3
+    d = sc.data
+    assert d.shape == oc.data.shape == (6, 8, 8, 2, 3, 4, 18)
+    assert np.max(np.abs(d - oc.data)) < 1e-10 * np.max(np.abs(oc.data))
+    assert np.max(np.abs(sys_.dipoles_flat() - S)) < 1e-9
+
+
+def test_sum_rule_gpu(gpu, sg):
+    # test_correlation_sampling.jl:29-50 on the raw accumulator: sum over (α=α, i=i, q, ω)
+    # of data = n_all_ω * Ncells * sum_i κ_i^2, for any spin state
+    cr = sg.fcc_primitive_crystal()
+    sys_ = sg.System(cr, [(1, sg.Moment(s=1, g=2))], "dipole", dims=(4, 4, 4), seed=111)
+    sys_.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    sys_.randomize_spins()
+    sg.step(sys_, sg.Langevin(0.05, damping=0.1, kT=0.1), nsteps=200)
+    sc = sg.SampledCorrelations(sys_, measure=sg.ssf_trace(sys_, apply_g=False), energies=np.linspace(0, 10.0, 100), dt=0.08)
+    sg.add_sample(sc, sys_)
+    d = sc.data
+    diag = [c for c, (a, b) in enumerate(sc.measure.corr_pairs) if a == b]
+    tot = sum(d[c, 0, 0].sum() for c in diag)
+    assert tot.real == pytest.approx(sc.n_all_omega * 64 * 1.0, rel=1e-12)
+    assert abs(tot.imag) < 1e-9 * tot.real
+    # imaginary part of the diagonal correlations vanishes (test_correlation_sampling.jl:59-67)
+    assert np.max(np.abs(np.imag(d[diag]))) < 1e-12 * np.max(np.abs(d))
+
+
+def test_merge_equals_running_accumulation(gpu, sg):
+    # test_correlation_sampling.jl:104-136
+    sys_ = diamond_reference_model(sg)
+    kw = dict(measure=sg.ssf_trace(sys_), energies=np.linspace(0, 5.5, 25), dt=0.12)
+    sc0, sc1, sc2 = (sg.SampledCorrelations(sys_, **kw) for _ in range(3))
+    lang = sg.Langevin(0.07, damping=0.1, kT=0.1723)
+    sg.step(sys_, lang, nsteps=400)
+    S = sys_.dipoles_flat()
+    sg.add_sample(sc0, sys_)
+    sys_.set_state_flat(dipoles=S)
+    sg.add_sample(sc1, sys_)
+    for _ in range(2):
+        sys_.set_state_flat(dipoles=S)
+        sg.step(sys_, lang, nsteps=400)
+        S = sys_.dipoles_flat()
+        sg.add_sample(sc0, sys_)
+        sys_.set_state_flat(dipoles=S)
+        sg.add_sample(sc2, sys_)
+    merged = sg.merge_correlations([sc1, sc2])
+    assert merged.nsamples == 3
+    assert np.allclose(merged.data, sc0.data, rtol=1e-12, atol=1e-14 * np.max(np.abs(sc0.data)))
+
+
+def test_static_correlations(gpu, sg, orc):
+    # SampledCorrelationsStatic (energies=nothing): sum over q of the trace = Ncells * κ^2
+    sys_ = sg.System(sg.fcc_primitive_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=(4, 4, 4), seed=3)
+    sys_.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    sys_.randomize_spins()
+    sc = sg.SampledCorrelations(sys_, measure=sg.ssf_trace(sys_, apply_g=False), energies=None, dt=float("nan"))
+    S = sys_.dipoles_flat()
+    sg.add_sample(sc, sys_)
+    assert np.array_equal(sys_.dipoles_flat(), S)   # no time integration
+    d = sc.data
+    diag = [c for c, (a, b) in enumerate(sc.measure.corr_pairs) if a == b]
+    tot = sum(d[c, 0, 0].sum() for c in diag)
+    assert tot.real == pytest.approx(64.0, rel=1e-12)
+
+
+def test_sqw_fp32_per_bin_error(gpu, sg, orc):
+    sys64 = diamond_reference_model(sg, "fp64")
+    sys32 = diamond_reference_model(sg, "fp32")
+    sys32.set_state_flat(dipoles=sys64.dipoles_flat())
+    kw = dict(energies=np.linspace(0.0, 5.5, 10), dt=0.12)
+    sc = sg.SampledCorrelations(sys32, measure=sg.ssf_perp(sys32), tol=1e-7, **kw)
+    o, oc = oracle_corr(orc, sys64, sc)
+    oc.tol = 1e-12
+    sg.add_sample(sc, sys32)
+    oc.add_sample(sys64.dipoles_flat(), None)
+    ref = oc.data
+    err = np.abs(sc.data - ref)
+    # per-bin error bound of 1% of the bin, with a floor of 1e-4 of the largest bin for
+    # bins that are zero up to rounding
+    assert np.all(err <= 0.01 * np.abs(ref) + 1e-4 * np.max(np.abs(ref)))
+
+
+def test_sqw_sun_parity(gpu, sg, orc):
+    sys_ = rich_sun(sg, N=3, dims=(2, 2, 2))
+    sc = sg.SampledCorrelations(sys_, measure=sg.ssf_trace(sys_), energies=np.linspace(0, 4.0, 6), dt=0.05)
+    o, oc = oracle_corr(orc, sys_, sc)
+    S, Z = sys_.dipoles_flat(), sys_.coherents_flat()
+    sg.add_sample(sc, sys_)
+    oc.add_sample(S, Z)
+    assert np.max(np.abs(sc.data - oc.data)) < 1e-10 * np.max(np.abs(oc.data))
