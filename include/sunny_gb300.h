@@ -184,6 +184,13 @@ int sgb_corr_data(sgb_corr* sc, double* data, double* M, int64_t* nsamples);
 /* merge_correlations([dst, src]) into dst (SampledCorrelations.jl:128-142). */
 int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src);
 
+/* Per-phase device time of add_sample!, summed over the samples taken while profiling is
+ * on (CUDA events between phases; no Julia analogue): ms4[0] trajectory with snapshots,
+ * [1] space FFT, [2] time FFT, [3] accumulation. sgb_corr_profile(sc, 1) enables and
+ * resets the sums. */
+int sgb_corr_profile(sgb_corr* sc, int32_t enable);
+int sgb_corr_phase_times(sgb_corr* sc, double* ms4, int64_t* nsamples_timed);
+
 /* ---- batched replicas and parallel tempering -------------------------------- */
 
 /* Many independent dipole-mode replicas, each with its own dims, kT and state, stepped

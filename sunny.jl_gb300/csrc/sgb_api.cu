@@ -58,7 +58,8 @@ struct sgb_system {
     double* dbuf = nullptr;     // device double scratch (noise, grads)
     size_t dbuf_cap = 0;
     void* flush = nullptr;
-    std::vector<char> stage;    // host staging
+    char* stage = nullptr;      // pinned host staging
+    size_t stage_cap = 0;
 };
 
 struct sgb_corr {
@@ -78,6 +79,10 @@ struct sgb_corr {
     double* g = nullptr;      // [n]
     cufftHandle plan_space = 0, plan_time = 0;
     bool have_space = false, have_time = false;
+    bool profile = false;
+    cudaEvent_t ev[5] = {};
+    double phase_ms[4] = {0, 0, 0, 0};
+    int64_t nprof = 0;
 };
 
 // ---------------------------------------------------------------------------------
@@ -100,6 +105,18 @@ int cuda_fail(sgb_system* s, cudaError_t e, const char* what) {
     } while (0)
 
 size_t rsize(const sgb_system* s) { return s->fp32 ? 4 : 8; }
+
+// Pinned host staging buffer used for every state upload and download.
+int ensure_stage(sgb_system* s, size_t bytes) {
+    if (s->stage_cap >= bytes) return SGB_OK;
+    if (s->stage) cudaFreeHost(s->stage);
+    s->stage = nullptr;
+    s->stage_cap = 0;
+    cudaError_t e = cudaMallocHost((void**)&s->stage, bytes);
+    if (e != cudaSuccess) return fail(s, SGB_ERR_NOMEM, std::string("pinned host allocation failed: ") + cudaGetErrorString(e));
+    s->stage_cap = bytes;
+    return SGB_OK;
+}
 
 int dmalloc(sgb_system* s, void** p, size_t bytes) {
     if (bytes == 0) bytes = 16;
@@ -503,6 +520,7 @@ void sgb_destroy(sgb_system* s) {
     p = s->red; dfree(p);
     p = s->dbuf; dfree(p);
     dfree(s->flush);
+    if (s->stage) cudaFreeHost(s->stage);
     for (int i = 0; i < 8; i++) if (s->ev[i]) cudaEventDestroy(s->ev[i]);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -528,9 +546,9 @@ int sgb_set_sites(sgb_system* s, const double* kappa, const double* g, const dou
         }
     }
     s->has_field = any;
-    s->stage.resize(std::max(s->stage.size(), 3 * (size_t)ns * sizeof(double)));
+    if (int rc0 = ensure_stage(s, 3 * (size_t)ns * sizeof(double))) return rc0;
     if (s->fp32) {
-        float* k = reinterpret_cast<float*>(s->stage.data());
+        float* k = reinterpret_cast<float*>(s->stage);
         for (int i = 0; i < ns; i++) k[i] = (float)kappa[i];
         CK(cudaMemcpy(s->kappa, k, sizeof(float) * ns, cudaMemcpyHostToDevice));
         for (size_t i = 0; i < 3 * (size_t)ns; i++) k[i] = (float)hh[i];
@@ -590,24 +608,24 @@ int sgb_set_state(sgb_system* s, const double* dipoles, const double* coherents)
     const size_t R = rsize(s);
     if (!s->sun) {
         if (!dipoles) return fail(s, SGB_ERR_ARG, "dipoles required in dipole mode");
-        s->stage.resize(std::max(s->stage.size(), R * 3 * (size_t)ns));
+        if ((rc = ensure_stage(s, R * 3 * (size_t)ns))) return rc;
         for (int i = 0; i < ns; i++)
             for (int c = 0; c < 3; c++) {
-                if (s->fp32) reinterpret_cast<float*>(s->stage.data())[(size_t)c * ns + i] = (float)dipoles[3 * (size_t)i + c];
-                else reinterpret_cast<double*>(s->stage.data())[(size_t)c * ns + i] = dipoles[3 * (size_t)i + c];
+                if (s->fp32) reinterpret_cast<float*>(s->stage)[(size_t)c * ns + i] = (float)dipoles[3 * (size_t)i + c];
+                else reinterpret_cast<double*>(s->stage)[(size_t)c * ns + i] = dipoles[3 * (size_t)i + c];
             }
-        CK(cudaMemcpyAsync(s->S, s->stage.data(), R * 3 * ns, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->S, s->stage, R * 3 * ns, cudaMemcpyHostToDevice, s->stream));
     } else {
         if (!coherents) return fail(s, SGB_ERR_ARG, "coherents required in SU(N) mode");
         const int N = s->N;
-        s->stage.resize(std::max(s->stage.size(), R * 2 * N * (size_t)ns));
+        if ((rc = ensure_stage(s, R * 2 * N * (size_t)ns))) return rc;
         for (int i = 0; i < ns; i++)
             for (int c = 0; c < 2 * N; c++) {
                 double v = coherents[(size_t)2 * N * i + c];
-                if (s->fp32) reinterpret_cast<float*>(s->stage.data())[(size_t)c * ns + i] = (float)v;
-                else reinterpret_cast<double*>(s->stage.data())[(size_t)c * ns + i] = v;
+                if (s->fp32) reinterpret_cast<float*>(s->stage)[(size_t)c * ns + i] = (float)v;
+                else reinterpret_cast<double*>(s->stage)[(size_t)c * ns + i] = v;
             }
-        CK(cudaMemcpyAsync(s->Z, s->stage.data(), R * 2 * N * ns, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->Z, s->stage, R * 2 * N * ns, cudaMemcpyHostToDevice, s->stream));
         rc = s->fp32 ? do_refresh<float>(s) : do_refresh<double>(s);
         if (rc) return rc;
     }
@@ -620,24 +638,25 @@ int sgb_get_state(sgb_system* s, double* dipoles, double* coherents) {
     if (!s) return fail(s, SGB_ERR_ARG, "null handle");
     const int ns = s->ns;
     const size_t R = rsize(s);
+    int rc = SGB_OK;
     if (dipoles) {
-        s->stage.resize(std::max(s->stage.size(), R * 3 * (size_t)ns));
-        CK(cudaMemcpyAsync(s->stage.data(), s->S, R * 3 * ns, cudaMemcpyDeviceToHost, s->stream));
+        if ((rc = ensure_stage(s, R * 3 * (size_t)ns))) return rc;
+        CK(cudaMemcpyAsync(s->stage, s->S, R * 3 * ns, cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
         for (int i = 0; i < ns; i++)
             for (int c = 0; c < 3; c++)
-                dipoles[3 * (size_t)i + c] = s->fp32 ? (double)reinterpret_cast<float*>(s->stage.data())[(size_t)c * ns + i]
-                                                     : reinterpret_cast<double*>(s->stage.data())[(size_t)c * ns + i];
+                dipoles[3 * (size_t)i + c] = s->fp32 ? (double)reinterpret_cast<float*>(s->stage)[(size_t)c * ns + i]
+                                                     : reinterpret_cast<double*>(s->stage)[(size_t)c * ns + i];
     }
     if (coherents && s->sun) {
         const int N = s->N;
-        s->stage.resize(std::max(s->stage.size(), R * 2 * N * (size_t)ns));
-        CK(cudaMemcpyAsync(s->stage.data(), s->Z, R * 2 * N * ns, cudaMemcpyDeviceToHost, s->stream));
+        if ((rc = ensure_stage(s, R * 2 * N * (size_t)ns))) return rc;
+        CK(cudaMemcpyAsync(s->stage, s->Z, R * 2 * N * ns, cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
         for (int i = 0; i < ns; i++)
             for (int c = 0; c < 2 * N; c++)
-                coherents[(size_t)2 * N * i + c] = s->fp32 ? (double)reinterpret_cast<float*>(s->stage.data())[(size_t)c * ns + i]
-                                                           : reinterpret_cast<double*>(s->stage.data())[(size_t)c * ns + i];
+                coherents[(size_t)2 * N * i + c] = s->fp32 ? (double)reinterpret_cast<float*>(s->stage)[(size_t)c * ns + i]
+                                                           : reinterpret_cast<double*>(s->stage)[(size_t)c * ns + i];
     }
     return SGB_OK;
 }
@@ -787,6 +806,7 @@ void sgb_corr_destroy(sgb_corr* c) {
     p = c->g; dfree(p);
     if (c->have_space) cufftDestroy(c->plan_space);
     if (c->have_time) cufftDestroy(c->plan_time);
+    for (int i = 0; i < 5; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     delete c;
 }
 
@@ -889,6 +909,7 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
     }
     const int nsteps = c->measperiod * (c->nsnaps - 1);
     const double scale = 1.0 / std::sqrt((double)c->ncell);
+    if (c->profile) cudaEventRecord(c->ev[0], s->stream);
     // 1. trajectory with fused observable snapshots (CorrelationSampling.jl:21-46)
     if (s->fp32) {
         SnapArgs<float> sn{1, c->nobs, c->measperiod, 0, (const float*)c->ops, (float*)c->A, (float)scale};
@@ -900,11 +921,13 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
         else rc = run_midpoint<double>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
     }
     if (rc) return rc;
+    if (c->profile) cudaEventRecord(c->ev[1], s->stream);
     // 2. space FFT, A(q) = sum_r exp(+iqr) A(r) / sqrt(Ncell) (CorrelationSampling.jl:58-63)
     cufftResult fr;
     if (s->fp32) fr = cufftExecC2C(c->plan_space, (cufftComplex*)c->A, (cufftComplex*)c->A, CUFFT_INVERSE);
     else fr = cufftExecZ2Z(c->plan_space, (cufftDoubleComplex*)c->A, (cufftDoubleComplex*)c->A, CUFFT_INVERSE);
     if (fr != CUFFT_SUCCESS) return cfail(c, SGB_ERR_CUDA, "space FFT failed");
+    if (c->profile) cudaEventRecord(c->ev[2], s->stream);
     // 3. time FFT, A(ω) = sum_t exp(-iωt) A(t), zero padded (CorrelationSampling.jl:65-69)
     const void* spec = c->A;
     if (c->have_time) {
@@ -913,12 +936,41 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
         if (fr != CUFFT_SUCCESS) return cfail(c, SGB_ERR_CUDA, "time FFT failed");
         spec = c->Ahat;
     }
+    if (c->profile) cudaEventRecord(c->ev[3], s->stream);
     // 4. accumulate conj(A_alpha,i) A_beta,j into the FP64 sum
     rc = s->fp32 ? corr_launch_accum<float>((const float*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, c->nomega, s->stream)
                  : corr_launch_accum<double>((const double*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, c->nomega, s->stream);
     s->launches++;
     if (rc) return cfail(c, SGB_ERR_CUDA, std::string("accumulate launch: ") + cudaGetErrorString(cudaGetLastError()));
     c->nsamples += 1;
+    if (c->profile) {
+        cudaEventRecord(c->ev[4], s->stream);
+        if (cudaEventSynchronize(c->ev[4]) != cudaSuccess) return cfail(c, SGB_ERR_CUDA, "profiling event failed");
+        for (int k = 0; k < 4; k++) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]);
+            c->phase_ms[k] += ms;
+        }
+        c->nprof += 1;
+    }
+    return SGB_OK;
+}
+
+int sgb_corr_profile(sgb_corr* c, int32_t enable) {
+    if (!c) return fail(nullptr, SGB_ERR_ARG, "null handle");
+    if (enable && !c->ev[0])
+        for (int i = 0; i < 5; i++)
+            if (cudaEventCreate(&c->ev[i]) != cudaSuccess) return cfail(c, SGB_ERR_CUDA, "cudaEventCreate failed");
+    c->profile = enable != 0;
+    for (int k = 0; k < 4; k++) c->phase_ms[k] = 0;
+    c->nprof = 0;
+    return SGB_OK;
+}
+
+int sgb_corr_phase_times(sgb_corr* c, double* ms4, int64_t* n) {
+    if (!c || !ms4) return fail(nullptr, SGB_ERR_ARG, "null argument");
+    for (int k = 0; k < 4; k++) ms4[k] = c->phase_ms[k];
+    if (n) *n = c->nprof;
     return SGB_OK;
 }
 

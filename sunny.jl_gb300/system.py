@@ -212,7 +212,11 @@ class System:
         return self._base_coh.reshape(-1, self.N).copy()
 
     def set_state_flat(self, dipoles=None, coherents=None):
-        self._sync_to_host()
+        """Overwrite the state from site-ordered arrays (dipoles (ns, 3) or coherents (ns, N))."""
+        full = (self.N == 0 and dipoles is not None) or (self.N > 0 and coherents is not None)
+        if not full:
+            self._sync_to_host()
+        self._dev_newer = False
         if dipoles is not None:
             self._base_dip.reshape(-1, 3)[:] = dipoles
         if coherents is not None:

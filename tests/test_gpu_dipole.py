@@ -28,7 +28,7 @@ def test_gradient_and_energy_fp64(gpu, sg, orc, builder):
     else:
         # L=1 and L=2 axes: bonds wrap onto the site itself or onto the same neighbour twice
         sys_ = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=2, g=2))], "dipole", dims=(1, 2, 3), seed=5)
-        sys_.set_exchange(np.array([[1.0, 0.3, 0], [0.3, 0.7, 0.1], [0, 0.1, 0.2]]) * 0 + 0.8, sg.Bond(1, 1, [1, 0, 0]))
+        sys_.set_exchange(0.8, sg.Bond(1, 1, [1, 0, 0]))
         sys_.set_bond_coupling(sg.Bond(1, 1, [1, 1, 0]), 0.2, np.array([[0.1, 0.2, 0.3], [0.0, -0.4, 0.5], [0.6, 0.0, 0.7]]), 0.3)
         sys_.set_bond_coupling(sg.Bond(1, 1, [0, 2, 1]), 0.0, 0.5, 0.0)
         sys_.randomize_spins()
