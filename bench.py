@@ -118,11 +118,13 @@ def run_arm(sg, precision, device, warmup, steps, tol, thermal_steps=2000, e2e_s
     launches = lib.sgb_kernel_launches(sys_.handle) - launches0
     ph = np.zeros(4)
     n = C.c_int64()
-    lib.sgb_corr_phase_times(sc._h, ph.ctypes.data_as(C.POINTER(C.c_double)), C.byref(n))
+    its = C.c_int64()
+    lib.sgb_corr_phase_times(sc._h, ph.ctypes.data_as(C.POINTER(C.c_double)), C.byref(n), C.byref(its))
     lib.sgb_corr_profile(sc._h, 0)
     res = {"ms": ms.value, "phase_ms": (ph / max(1, n.value)).tolist(), "launches": launches, "clocks": clk,
            "nsamples": sc.nsamples, "nsteps_per_sample": sc.measperiod * (sc.n_all_omega // 2), "ns": sys_.nsites,
-           "measperiod": sc.measperiod, "n_all_omega": sc.n_all_omega, "dt": sc.dt}
+           "measperiod": sc.measperiod, "n_all_omega": sc.n_all_omega, "dt": sc.dt,
+           "iters_per_step": its.value / max(1, n.value) / (sc.measperiod * (sc.n_all_omega // 2))}
     if e2e_steps:
         # end to end through the public API: pinned-host state in, add_sample, state out
         S = sys_.dipoles_flat()
@@ -141,6 +143,45 @@ def run_arm(sg, precision, device, warmup, steps, tol, thermal_steps=2000, e2e_s
     sc.close()
     sys_.close()
     return res
+
+
+def dynamics_rate(sg, kind, precision, device, nsteps):
+    """Site-steps/s of plain Langevin dynamics for the other two single-system workloads:
+    'sc'  -- simple cubic 16^3, s=1, J=1, -0.1 Sz^2, dt=0.02, damping 0.1, kT=0.5 (dipole)
+    'tri' -- layered triangular 48x48x4 SU(3), anisotropic J1, J2, J3, Jc, -2.2 Sz^2,
+             dt=0.02 (assumed), damping 0.1, kT=0.3."""
+    import ctypes as C
+    lib = sg.load_library()
+    if kind == "sc":
+        sys_ = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=(16, 16, 16), seed=1,
+                         precision=precision, device=device)
+        sys_.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+        sys_.set_onsite_coupling(lambda Sx, Sy, Sz: -0.1 * Sz @ Sz, 1)
+        integ = sg.Langevin(0.02, damping=0.1, kT=0.5)
+    else:
+        cr = sg.triangular_crystal(a=4.05, c=6.75)
+        sys_ = sg.System(cr, [(1, sg.Moment(s=1, g=2))], "SUN", dims=(48, 48, 4), seed=1, precision=precision,
+                         device=device)
+        J1 = np.array([[-0.24, 0, 0], [0, -0.24, 0.1], [0, 0.1, -0.24]])
+        sys_.set_exchange(J1, sg.Bond(1, 1, [1, 0, 0]))
+        sys_.set_exchange(0.05, sg.Bond(1, 1, [1, 2, 0]))
+        sys_.set_exchange(0.32, sg.Bond(1, 1, [2, 0, 0]))
+        sys_.set_exchange(-0.05, sg.Bond(1, 1, [0, 0, 1]))
+        sys_.set_onsite_coupling(lambda Sx, Sy, Sz: -2.2 * Sz @ Sz, 1)
+        integ = sg.Langevin(0.02, damping=0.1, kT=0.3)
+    sys_.randomize_spins()
+    sg.step(sys_, integ, nsteps=200)
+    lib.sgb_synchronize(sys_.handle)
+    lib.sgb_event_record(sys_.handle, 0)
+    sg.step(sys_, integ, nsteps=nsteps)
+    lib.sgb_event_record(sys_.handle, 1)
+    ms = C.c_float()
+    lib.sgb_event_elapsed(sys_.handle, 0, 1, C.byref(ms))
+    E = sg.energy_per_site(sys_)
+    ns = sys_.nsites
+    sys_.close()
+    return {"site_steps_per_s": ns * nsteps / (ms.value / 1000.0), "us_per_step": 1000.0 * ms.value / nsteps,
+            "nsites": ns, "steps": nsteps, "energy_per_site": E}
 
 
 # ---- CPU restatement (oracle) timing ----------------------------------------------------------
@@ -272,6 +313,11 @@ def main():
     r32 = run_arm(sg, "fp32", local, args.warmup, args.steps, tol=1e-6, e2e_steps=max(2, args.steps // 2))
     barrier()
     r64 = run_arm(sg, "fp64", local, 1, args.fp64_steps, tol=1e-12) if args.fp64_steps > 0 else None
+    extra = {}
+    for kind, n in (("sc", 10000), ("tri", 2000)):
+        a = dynamics_rate(sg, kind, "fp32", local, n)
+        b = dynamics_rate(sg, kind, "fp64", local, n // 4)
+        extra[kind] = {"fp32": a, "fp64": b, "speedup": a["site_steps_per_s"] / b["site_steps_per_s"]}
     barrier()
     ms = maxall(r32["ms"])
     value = world * args.steps / (ms / 1000.0)
@@ -316,7 +362,10 @@ def main():
              "ms_per_step": r64["ms"] / args.fp64_steps, "phase_ms": r64["phase_ms"]},
             "speedup_vs_fp64_plain": None if r64 is None else value / v64,
             "phase_ms": {"trajectory": ph[0], "space_fft": ph[1], "time_fft": ph[2], "accumulate": ph[3]},
+            "midpoint_iters_per_step": {"fp32": r32["iters_per_step"], "fp64": None if r64 is None else r64["iters_per_step"]},
+            "us_per_midpoint_iteration": 1000.0 * ph[0] / (r32["iters_per_step"] * nsteps_sample),
             "kernels": kernels,
+            "langevin_site_steps": {"simple_cubic_16^3_dipole": extra["sc"], "triangular_48x48x4_SU3": extra["tri"]},
             "roofline": roof,
             "gpu_launches": r32["launches"],
             "clocks": r32["clocks"],

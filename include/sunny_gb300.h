@@ -186,10 +186,11 @@ int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src);
 
 /* Per-phase device time of add_sample!, summed over the samples taken while profiling is
  * on (CUDA events between phases; no Julia analogue): ms4[0] trajectory with snapshots,
- * [1] space FFT, [2] time FFT, [3] accumulation. sgb_corr_profile(sc, 1) enables and
- * resets the sums. */
+ * [1] space FFT, [2] time FFT, [3] accumulation; iterations (nullable) receives the
+ * implicit-midpoint fixed-point iterations of those samples. sgb_corr_profile(sc, 1)
+ * enables and resets the sums. */
 int sgb_corr_profile(sgb_corr* sc, int32_t enable);
-int sgb_corr_phase_times(sgb_corr* sc, double* ms4, int64_t* nsamples_timed);
+int sgb_corr_phase_times(sgb_corr* sc, double* ms4, int64_t* nsamples_timed, int64_t* iterations);
 
 /* ---- batched replicas and parallel tempering -------------------------------- */
 

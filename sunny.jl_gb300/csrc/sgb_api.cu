@@ -83,6 +83,7 @@ struct sgb_corr {
     cudaEvent_t ev[5] = {};
     double phase_ms[4] = {0, 0, 0, 0};
     int64_t nprof = 0;
+    int64_t prof_iters = 0;
 };
 
 // ---------------------------------------------------------------------------------
@@ -311,28 +312,32 @@ int ensure_tables(sgb_system* s) {
     return rc;
 }
 
-// Choose sites-per-thread and grid for a persistent cooperative launch.
+// Choose sites-per-thread, block and grid for a persistent cooperative launch: the
+// smallest SPT whose grid fits on the device, with the block sized so that the sites
+// spread evenly, one block per SM (latency, not throughput, bounds these kernels).
 template <class R>
 int plan_launch(sgb_system* s, LaunchInfo& li) {
     const int sptv_dip[4] = {1, 2, 4, 8}, sptv_sun[2] = {1, 2};
     const int* sptv = s->sun ? sptv_sun : sptv_dip;
     int nspt = s->sun ? 2 : 4;
     size_t smem = (size_t)s->tables_bytes;
+    LaunchInfo fallback{0, 0, 0, 0};
     for (int i = 0; i < nspt; i++) {
         int spt = sptv[i];
+        int maxblock = sgb_maxblock(sizeof(R) == 8, s->sun, spt);
+        long long per_sm = ((long long)s->ns + (long long)s->nsm * spt - 1) / ((long long)s->nsm * spt);
+        int block = (int)std::min<long long>(maxblock, std::max<long long>(128, (per_sm + 31) / 32 * 32));
         int bps = 0;
-        int rc = s->sun ? sun_max_blocks<R>(s->N, spt, smem, &bps) : dip_max_blocks<R>(spt, smem, &bps);
+        int rc = s->sun ? sun_max_blocks<R>(s->N, spt, block, smem, &bps) : dip_max_blocks<R>(spt, block, smem, &bps);
         if (rc != SGB_OK) return fail(s, SGB_ERR_CUDA, "occupancy query failed");
         long long cap = (long long)bps * s->nsm;
-        long long need = ((long long)s->ns + (long long)SGB_BLOCK * spt - 1) / ((long long)SGB_BLOCK * spt);
-        if (need <= cap && need >= 1) {
-            li.grid = (int)need;
-            li.block = SGB_BLOCK;
-            li.spt = spt;
-            li.smem = smem;
-            return SGB_OK;
-        }
+        long long need = ((long long)s->ns + (long long)block * spt - 1) / ((long long)block * spt);
+        if (need < 1 || need > cap) continue;
+        LaunchInfo cand{(int)need, block, spt, smem};
+        if (need <= s->nsm) { li = cand; return SGB_OK; }   // at most one block per SM
+        if (fallback.grid == 0) fallback = cand;
     }
+    if (fallback.grid) { li = fallback; return SGB_OK; }
     return fail(s, SGB_ERR_ARG, "system too large for one co-resident persistent launch");
 }
 
@@ -910,14 +915,15 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
     const int nsteps = c->measperiod * (c->nsnaps - 1);
     const double scale = 1.0 / std::sqrt((double)c->ncell);
     if (c->profile) cudaEventRecord(c->ev[0], s->stream);
+    int64_t iters = 0;
     // 1. trajectory with fused observable snapshots (CorrelationSampling.jl:21-46)
     if (s->fp32) {
         SnapArgs<float> sn{1, c->nobs, c->measperiod, 0, (const float*)c->ops, (float*)c->A, (float)scale};
-        if (nsteps > 0) rc = run_midpoint<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, nullptr, sn, true);
+        if (nsteps > 0) rc = run_midpoint<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true);
         else rc = run_midpoint<float>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
     } else {
         SnapArgs<double> sn{1, c->nobs, c->measperiod, 0, (const double*)c->ops, (double*)c->A, scale};
-        if (nsteps > 0) rc = run_midpoint<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, nullptr, sn, true);
+        if (nsteps > 0) rc = run_midpoint<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true);
         else rc = run_midpoint<double>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
     }
     if (rc) return rc;
@@ -952,6 +958,7 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
             c->phase_ms[k] += ms;
         }
         c->nprof += 1;
+        c->prof_iters += iters;
     }
     return SGB_OK;
 }
@@ -964,13 +971,15 @@ int sgb_corr_profile(sgb_corr* c, int32_t enable) {
     c->profile = enable != 0;
     for (int k = 0; k < 4; k++) c->phase_ms[k] = 0;
     c->nprof = 0;
+    c->prof_iters = 0;
     return SGB_OK;
 }
 
-int sgb_corr_phase_times(sgb_corr* c, double* ms4, int64_t* n) {
+int sgb_corr_phase_times(sgb_corr* c, double* ms4, int64_t* n, int64_t* iters) {
     if (!c || !ms4) return fail(nullptr, SGB_ERR_ARG, "null argument");
     for (int k = 0; k < 4; k++) ms4[k] = c->phase_ms[k];
     if (n) *n = c->nprof;
+    if (iters) *iters = c->prof_iters;
     return SGB_OK;
 }
 

@@ -40,15 +40,21 @@ __host__ __device__ inline double biquad_metric(int q) {
 // %globaltimer; on expiry the kernel records SGB_ERR_TIMEOUT and returns, so that a
 // stuck barrier never hangs the GPU.
 // ---------------------------------------------------------------------------------
-struct Ctrl {
+// Control words of one persistent launch. The barrier words, the convergence sums and
+// the status live on separate 128-byte lines so that spinning, atomics and flag reads
+// do not contend for one L2 line.
+struct alignas(128) Ctrl {
     unsigned int bar_count;
+    unsigned int pad0[31];
     unsigned int bar_gen;
+    unsigned int pad1[31];
+    double acc[3];       // rotating FP64 convergence accumulators
+    double pad2[13];
     int status;
     int steps_done;
     long long iters;
-    double acc[3];       // rotating FP64 convergence accumulators
     int final_buf;
-    int pad;
+    int pad3[27];
 };
 
 __device__ __forceinline__ uint64_t sgb_globaltimer() {
@@ -68,6 +74,8 @@ __device__ __forceinline__ int sgb_read_status(Ctrl* c) {
 #define SGB_BARRIER_TIMEOUT_NS 4000000000ull
 
 // Barrier across `nblocks` co-resident CTAs (cooperative launch guarantees residency).
+// Memory written before the barrier by any CTA is visible to plain loads of every CTA
+// after it (fences around the arrival, as cooperative-groups grid sync does).
 // Returns false if the wait timed out or another CTA flagged an error.
 __device__ __forceinline__ bool sgb_grid_barrier(Ctrl* c, unsigned int nblocks) {
     __shared__ int ok_s;
@@ -84,13 +92,17 @@ __device__ __forceinline__ bool sgb_grid_barrier(Ctrl* c, unsigned int nblocks) 
                 cnt.store(0u, cuda::memory_order_relaxed);
                 gen.fetch_add(1u, cuda::memory_order_release);
             } else {
-                uint64_t t0 = sgb_globaltimer();
+                uint64_t t0 = 0;
+                unsigned int spins = 0;
                 while (gen.load(cuda::memory_order_acquire) == g) {
-                    __nanosleep(32);
-                    if (sgb_globaltimer() - t0 > SGB_BARRIER_TIMEOUT_NS) {
-                        sgb_set_status(c, SGB_ERR_TIMEOUT);
-                        ok = 0;
-                        break;
+                    if ((++spins & 255u) == 0) {
+                        uint64_t t = sgb_globaltimer();
+                        if (t0 == 0) t0 = t;
+                        else if (t - t0 > SGB_BARRIER_TIMEOUT_NS) {
+                            sgb_set_status(c, SGB_ERR_TIMEOUT);
+                            ok = 0;
+                            break;
+                        }
                     }
                 }
             }
@@ -168,7 +180,9 @@ __device__ inline void sgb_normals4(uint64_t seed, uint32_t stream, uint64_t ste
 // ---------------------------------------------------------------------------------
 // Small helpers
 // ---------------------------------------------------------------------------------
-template <class R> __device__ __forceinline__ R sgb_ld(const R* p) { return __ldcg(p); }
+// Loads of state that other CTAs wrote before the last grid barrier: plain (L1-cacheable)
+// loads, made coherent by the barrier's fences. Never the read-only (.nc) path.
+template <class R> __device__ __forceinline__ R sgb_ld(const R* p) { return *p; }
 
 template <class R> __device__ __forceinline__ R sgb_rsqrt(R x);
 template <> __device__ __forceinline__ float sgb_rsqrt<float>(float x) { return rsqrtf(x); }
@@ -186,19 +200,19 @@ __device__ __forceinline__ int sgb_wrap_any(int x, int L) {
     return x >= L ? x - L : x;
 }
 
-// block-wide FP64 sum; result valid in thread 0
-template <int BLOCK>
+// block-wide FP64 sum (any blockDim up to 1024); result valid in thread 0
 __device__ inline double sgb_block_sum(double v) {
-    __shared__ double red[BLOCK / 32];
+    __shared__ double red[32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int nw = (blockDim.x + 31) >> 5;
     __syncthreads();
     if (l == 0) red[w] = v;
     __syncthreads();
     double r = 0.0;
     if (threadIdx.x < 32) {
-        r = threadIdx.x < BLOCK / 32 ? red[threadIdx.x] : 0.0;
+        r = threadIdx.x < nw ? red[threadIdx.x] : 0.0;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
     }

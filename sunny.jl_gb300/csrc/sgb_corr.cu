@@ -53,20 +53,30 @@ __global__ void __launch_bounds__(256) k_corr_accum(const R* __restrict__ A, dou
     const size_t base = ((size_t)w * ncell + q0) * B;
     const int total = nq * B;
     double2* out = reinterpret_cast<double2*>(P) + base;
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        int ql = e / B, r = e - ql * B;
-        int c = r % ncorr;
-        int t = r / ncorr;
-        int i = t % npos, j = t / npos;
-        C2<R> a = As[(pr[2 * c] * npos + i) * QT + ql];
-        C2<R> b = As[(pr[2 * c + 1] * npos + j) * QT + ql];
-        // conj(a) * b
-        double re = (double)(a.x * b.x + a.y * b.y);
-        double im = (double)(a.x * b.y - a.y * b.x);
-        double2 acc = __ldcs(out + e);
-        acc.x += re;
-        acc.y += im;
-        __stcs(out + e, acc);
+    // four independent 16-byte loads in flight per thread before any use
+    constexpr int U = 4;
+    for (int e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
+        double2 acc[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            int e = e0 + u * blockDim.x;
+            if (e < total) acc[u] = __ldcs(out + e);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            int e = e0 + u * blockDim.x;
+            if (e >= total) break;
+            int ql = e / B, r = e - ql * B;
+            int c = r % ncorr;
+            int t = r / ncorr;
+            int i = t % npos, j = t / npos;
+            C2<R> a = As[(pr[2 * c] * npos + i) * QT + ql];
+            C2<R> b = As[(pr[2 * c + 1] * npos + j) * QT + ql];
+            // conj(a) * b
+            acc[u].x += (double)(a.x * b.x + a.y * b.y);
+            acc[u].y += (double)(a.x * b.y - a.y * b.x);
+            __stcs(out + e, acc[u]);
+        }
     }
 }
 

@@ -152,38 +152,51 @@ __device__ inline void grad_site(const Model<R>& M, const Tab<R>& T, int site, c
         if (km > 0) classical_aniso<R>(T.stev + 28 * a, km, sx, sy, sz, gx, gy, gz);
     }
     const int b0 = T.boff[a], b1 = T.boff[a + 1];
-    for (int b = b0; b < b1; b++) {
-        const DBond<R>& B = T.bonds[b];
-        int x1 = sgb_wrap_pos(ix.c1 + B.n[0], M.L1);
-        int x2 = sgb_wrap_pos(ix.c2 + B.n[1], M.L2);
-        int x3 = sgb_wrap_pos(ix.c3 + B.n[2], M.L3);
-        int js = x1 + M.L1 * (x2 + M.L2 * (x3 + M.L3 * B.j));
-        R tx = sgb_ld(X + js), ty = sgb_ld(Y + js), tz = sgb_ld(Zc + js);
-        if (B.jkind == 0) {
-            R j = B.J[0];
-            gx += j * tx; gy += j * ty; gz += j * tz;
-        } else {
-            gx += B.J[0] * tx + B.J[3] * ty + B.J[6] * tz;
-            gy += B.J[1] * tx + B.J[4] * ty + B.J[7] * tz;
-            gz += B.J[2] * tx + B.J[5] * ty + B.J[8] * tz;
-        }
-        if (M.dipole_mode && B.bqkind != 0) {
-            R Qj[5], v[5];
-            quad5<R>(tx, ty, tz, Qj);
-            if (B.bqkind == 1) {
+    // Gather in chunks: issue every neighbour load of a chunk before consuming any, so
+    // that the L1/L2 latencies of up to 3*SGB_GATHER loads overlap.
+    for (int b = b0; b < b1; b += SGB_GATHER) {
+        R tx[SGB_GATHER], ty[SGB_GATHER], tz[SGB_GATHER];
 #pragma unroll
-                for (int q = 0; q < 5; q++) v[q] = B.bq * ((R)biquad_metric(q) * Qj[q]);
-            } else {
-                const R* Bm = T.bq + 25 * B.bqidx;
-#pragma unroll
-                for (int q = 0; q < 5; q++) {
-                    R acc = 0;
-#pragma unroll
-                    for (int p = 0; p < 5; p++) acc += Bm[q + 5 * p] * Qj[p];
-                    v[q] = acc;
-                }
+        for (int k = 0; k < SGB_GATHER; k++) {
+            if (b + k < b1) {
+                const DBond<R>& B = T.bonds[b + k];
+                int x1 = sgb_wrap_pos(ix.c1 + B.n[0], M.L1);
+                int x2 = sgb_wrap_pos(ix.c2 + B.n[1], M.L2);
+                int x3 = sgb_wrap_pos(ix.c3 + B.n[2], M.L3);
+                int js = x1 + M.L1 * (x2 + M.L2 * (x3 + M.L3 * B.j));
+                tx[k] = sgb_ld(X + js); ty[k] = sgb_ld(Y + js); tz[k] = sgb_ld(Zc + js);
             }
-            add_quad_grad<R>(sx, sy, sz, v, gx, gy, gz);
+        }
+#pragma unroll
+        for (int k = 0; k < SGB_GATHER; k++) {
+            if (b + k >= b1) break;
+            const DBond<R>& B = T.bonds[b + k];
+            if (B.jkind == 0) {
+                R j = B.J[0];
+                gx += j * tx[k]; gy += j * ty[k]; gz += j * tz[k];
+            } else {
+                gx += B.J[0] * tx[k] + B.J[3] * ty[k] + B.J[6] * tz[k];
+                gy += B.J[1] * tx[k] + B.J[4] * ty[k] + B.J[7] * tz[k];
+                gz += B.J[2] * tx[k] + B.J[5] * ty[k] + B.J[8] * tz[k];
+            }
+            if (M.dipole_mode && B.bqkind != 0) {
+                R Qj[5], v[5];
+                quad5<R>(tx[k], ty[k], tz[k], Qj);
+                if (B.bqkind == 1) {
+#pragma unroll
+                    for (int q = 0; q < 5; q++) v[q] = B.bq * ((R)biquad_metric(q) * Qj[q]);
+                } else {
+                    const R* Bm = T.bq + 25 * B.bqidx;
+#pragma unroll
+                    for (int q = 0; q < 5; q++) {
+                        R acc = 0;
+#pragma unroll
+                        for (int p = 0; p < 5; p++) acc += Bm[q + 5 * p] * Qj[p];
+                        v[q] = acc;
+                    }
+                }
+                add_quad_grad<R>(sx, sy, sz, v, gx, gy, gz);
+            }
         }
     }
 }

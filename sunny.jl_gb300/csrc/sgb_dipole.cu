@@ -22,7 +22,7 @@ namespace {
 using namespace sgbdev;
 
 template <class R, int SPT, bool INJECT>
-__global__ void __launch_bounds__(SGB_BLOCK)
+__global__ void __launch_bounds__(sgb_maxblock(sizeof(R) == 8, false, SPT))
 k_dip_heun(Model<R> M, R* S, R* P, Ctrl* ctrl, int nsteps, R dt, R lam, R nscale, uint64_t seed,
            uint64_t step0, const double* noise) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -102,7 +102,7 @@ __device__ __forceinline__ void write_snapshot_dip(const Model<R>& M, const Snap
 // Spherical midpoint, Integrators.jl:379-413. H holds 3 rotating SoA buffers of
 // midpoint spins S-hat (3*3*ns reals).
 template <class R, int SPT>
-__global__ void __launch_bounds__(SGB_BLOCK)
+__global__ void __launch_bounds__(sgb_maxblock(sizeof(R) == 8, false, SPT))
 k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, double atol2,
                int max_iters, SnapArgs<R> snap) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -165,7 +165,7 @@ k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, doub
                 normalize_dip<R>(mx, my, mz, kap);
                 Hs[site] = mx; Hs[ns + site] = my; Hs[2 * ns + site] = mz;
             }
-            double bsum = sgb_block_sum<SGB_BLOCK>(acc);
+            double bsum = sgb_block_sum(acc);
             const int slot = (int)(itg % 3);
             if (threadIdx.x == 0) atomicAdd(&ctrl->acc[slot], bsum);
             if (leader) { ctrl->acc[(slot + 1) % 3] = 0.0; ctrl->iters += 1; }
@@ -271,10 +271,10 @@ k_dip_energy(Model<R> M, const R* S, double* partials) {
             }
         }
     }
-    double e = sgb_block_sum<SGB_BLOCK>(E);
-    double a0 = sgb_block_sum<SGB_BLOCK>(mx);
-    double a1 = sgb_block_sum<SGB_BLOCK>(my);
-    double a2 = sgb_block_sum<SGB_BLOCK>(mz);
+    double e = sgb_block_sum(E);
+    double a0 = sgb_block_sum(mx);
+    double a1 = sgb_block_sum(my);
+    double a2 = sgb_block_sum(mz);
     if (threadIdx.x == 0) {
         partials[4 * blockIdx.x + 0] = e;
         partials[4 * blockIdx.x + 1] = a0;
@@ -288,7 +288,7 @@ __global__ void k_reduce_partials(const double* partials, int n, int ncomp, doub
     for (int c = 0; c < ncomp; c++) {
         double v = 0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) v += partials[(size_t)i * ncomp + c];
-        double t = sgb_block_sum<SGB_BLOCK>(v);
+        double t = sgb_block_sum(v);
         if (threadIdx.x == 0) out[c] = t;
         __syncthreads();
     }
@@ -381,24 +381,24 @@ int dip_launch_midpoint(const Model<R>& M, R* S, R* H, Ctrl* ctrl, int nsteps, d
 }
 
 template <class R>
-int dip_max_blocks(int spt, size_t smem, int* bps) {
-    cudaError_t e = cudaErrorInvalidValue;
-    int a = 0, b = 0;
-#define SGB_OCC(K)                                                                              \
-    do {                                                                                        \
-        if (set_smem_attr(K, smem) != SGB_OK) return SGB_ERR_CUDA;                              \
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, K, SGB_BLOCK, smem);              \
-        if (e != cudaSuccess) return SGB_ERR_CUDA;                                              \
-    } while (0)
+int dip_max_blocks(int spt, int block, size_t smem, int* bps) {
+    int best = 1 << 30, a = 0;
+    auto one = [&](auto k) -> int {
+        if (set_smem_attr(k, smem) != SGB_OK) return SGB_ERR_CUDA;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k, block, smem) != cudaSuccess) return SGB_ERR_CUDA;
+        best = a < best ? a : best;
+        return SGB_OK;
+    };
+    int rc = SGB_OK;
     switch (spt) {
-        case 1: SGB_OCC((k_dip_heun<R, 1, false>)); b = a; SGB_OCC((k_dip_heun<R, 1, true>)); b = b < a ? b : a; SGB_OCC((k_dip_midpoint<R, 1>)); break;
-        case 2: SGB_OCC((k_dip_heun<R, 2, false>)); b = a; SGB_OCC((k_dip_heun<R, 2, true>)); b = b < a ? b : a; SGB_OCC((k_dip_midpoint<R, 2>)); break;
-        case 4: SGB_OCC((k_dip_heun<R, 4, false>)); b = a; SGB_OCC((k_dip_heun<R, 4, true>)); b = b < a ? b : a; SGB_OCC((k_dip_midpoint<R, 4>)); break;
-        case 8: SGB_OCC((k_dip_heun<R, 8, false>)); b = a; SGB_OCC((k_dip_heun<R, 8, true>)); b = b < a ? b : a; SGB_OCC((k_dip_midpoint<R, 8>)); break;
+        case 1: rc |= one(k_dip_heun<R, 1, false>); rc |= one(k_dip_heun<R, 1, true>); rc |= one(k_dip_midpoint<R, 1>); break;
+        case 2: rc |= one(k_dip_heun<R, 2, false>); rc |= one(k_dip_heun<R, 2, true>); rc |= one(k_dip_midpoint<R, 2>); break;
+        case 4: rc |= one(k_dip_heun<R, 4, false>); rc |= one(k_dip_heun<R, 4, true>); rc |= one(k_dip_midpoint<R, 4>); break;
+        case 8: rc |= one(k_dip_heun<R, 8, false>); rc |= one(k_dip_heun<R, 8, true>); rc |= one(k_dip_midpoint<R, 8>); break;
         default: return SGB_ERR_ARG;
     }
-#undef SGB_OCC
-    *bps = b < a ? b : a;
+    if (rc != SGB_OK) return SGB_ERR_CUDA;
+    *bps = best;
     return SGB_OK;
 }
 
@@ -445,7 +445,7 @@ int util_launch_fill(double* p, size_t n, double v, cudaStream_t st) {
                                         const SnapArgs<R>&, const LaunchInfo&, cudaStream_t);           \
     template int dip_launch_grad<R>(const Model<R>&, const R*, double*, cudaStream_t);                    \
     template int dip_launch_energy<R>(const Model<R>&, const R*, double*, int, cudaStream_t);             \
-    template int dip_max_blocks<R>(int, size_t, int*);                                                    \
+    template int dip_max_blocks<R>(int, int, size_t, int*);                                                    \
     template int util_launch_noise_export<R>(int, int, int, uint64_t, uint64_t, double*, cudaStream_t);
 SGB_INST(float)
 SGB_INST(double)

@@ -62,7 +62,7 @@ int dip_launch_grad(const Model<R>& M, const R* S, double* grad, cudaStream_t st
 template <class R>
 int dip_launch_energy(const Model<R>& M, const R* S, double* partials, int nblocks, cudaStream_t st);
 template <class R>
-int dip_max_blocks(int spt, size_t smem, int* blocks_per_sm);
+int dip_max_blocks(int spt, int block, size_t smem, int* blocks_per_sm);
 
 // ---- SU(N) kernels (sgb_sun.cu) ----
 template <class R>
@@ -81,7 +81,7 @@ template <class R>
 int sun_launch_energy(const Model<R>& M, const R* Z, const R* D, const R* Q, double* partials,
                       int nblocks, cudaStream_t st);
 template <class R>
-int sun_max_blocks(int N, int spt, size_t smem, int* blocks_per_sm);
+int sun_max_blocks(int N, int spt, int block, size_t smem, int* blocks_per_sm);
 
 // ---- shared utilities (sgb_dipole.cu) ----
 int util_launch_reduce(const double* partials, int n, int ncomp, double* out, cudaStream_t st);
@@ -91,4 +91,10 @@ int util_launch_noise_export(int mode_sun, int N, int ns, uint64_t seed, uint64_
 int util_launch_fill(double* p, size_t n, double v, cudaStream_t st);
 
 #define SGB_ENERGY_BLOCKS 256
-#define SGB_BLOCK 256
+#define SGB_BLOCK 256          // block size of the non-persistent kernels
+#define SGB_MAXBLOCK 512       // largest block of any persistent kernel
+
+// Largest block of a persistent kernel: 512 threads (128 registers each) only where the
+// kernel fits that budget without spilling (FP32 dipole, SPT <= 2), else 256.
+constexpr int sgb_maxblock(bool dbl, bool sun, int spt) { return (!dbl && !sun && spt <= 2) ? 512 : 256; }
+#define SGB_GATHER 8           // neighbour loads issued per gather chunk

@@ -126,36 +126,50 @@ __device__ __forceinline__ void sun_field(const Model<R>& M, const Tab<R>& T, in
 #pragma unroll
         for (int q = 0; q < 5; q++) v[q] = 0;
     }
-    for (int b = T.boff[ix.a]; b < T.boff[ix.a + 1]; b++) {
-        const DBond<R>& B = T.bonds[b];
-        int x1 = sgb_wrap_pos(ix.c1 + B.n[0], M.L1);
-        int x2 = sgb_wrap_pos(ix.c2 + B.n[1], M.L2);
-        int x3 = sgb_wrap_pos(ix.c3 + B.n[2], M.L3);
-        int js = x1 + M.L1 * (x2 + M.L2 * (x3 + M.L3 * B.j));
-        R tx = sgb_ld(D + js), ty = sgb_ld(D + ns + js), tz = sgb_ld(D + 2 * ns + js);
-        if (B.jkind == 0) {
-            R j = B.J[0];
-            d[0] += j * tx; d[1] += j * ty; d[2] += j * tz;
-        } else {
-            d[0] += B.J[0] * tx + B.J[3] * ty + B.J[6] * tz;
-            d[1] += B.J[1] * tx + B.J[4] * ty + B.J[7] * tz;
-            d[2] += B.J[2] * tx + B.J[5] * ty + B.J[8] * tz;
+    const int b0 = T.boff[ix.a], b1 = T.boff[ix.a + 1];
+    for (int b = b0; b < b1; b += SGB_GATHER) {
+        R tx[SGB_GATHER], ty[SGB_GATHER], tz[SGB_GATHER];
+        int jsv[SGB_GATHER];
+#pragma unroll
+        for (int k = 0; k < SGB_GATHER; k++) {
+            if (b + k < b1) {
+                const DBond<R>& B = T.bonds[b + k];
+                int x1 = sgb_wrap_pos(ix.c1 + B.n[0], M.L1);
+                int x2 = sgb_wrap_pos(ix.c2 + B.n[1], M.L2);
+                int x3 = sgb_wrap_pos(ix.c3 + B.n[2], M.L3);
+                int js = x1 + M.L1 * (x2 + M.L2 * (x3 + M.L3 * B.j));
+                jsv[k] = js;
+                tx[k] = sgb_ld(D + js); ty[k] = sgb_ld(D + ns + js); tz[k] = sgb_ld(D + 2 * ns + js);
+            }
         }
-        if (BQ && B.bqkind != 0) {
-            R Qj[5];
 #pragma unroll
-            for (int q = 0; q < 5; q++) Qj[q] = sgb_ld(Qb + (size_t)q * ns + js);
-            if (B.bqkind == 1) {
-#pragma unroll
-                for (int q = 0; q < 5; q++) v[q] += B.bq * ((R)biquad_metric(q) * Qj[q]);
+        for (int k = 0; k < SGB_GATHER; k++) {
+            if (b + k >= b1) break;
+            const DBond<R>& B = T.bonds[b + k];
+            if (B.jkind == 0) {
+                R j = B.J[0];
+                d[0] += j * tx[k]; d[1] += j * ty[k]; d[2] += j * tz[k];
             } else {
-                const R* Bm = T.bq + 25 * B.bqidx;
+                d[0] += B.J[0] * tx[k] + B.J[3] * ty[k] + B.J[6] * tz[k];
+                d[1] += B.J[1] * tx[k] + B.J[4] * ty[k] + B.J[7] * tz[k];
+                d[2] += B.J[2] * tx[k] + B.J[5] * ty[k] + B.J[8] * tz[k];
+            }
+            if (BQ && B.bqkind != 0) {
+                R Qj[5];
 #pragma unroll
-                for (int q = 0; q < 5; q++) {
-                    R acc = 0;
+                for (int q = 0; q < 5; q++) Qj[q] = sgb_ld(Qb + (size_t)q * ns + jsv[k]);
+                if (B.bqkind == 1) {
 #pragma unroll
-                    for (int p = 0; p < 5; p++) acc += Bm[q + 5 * p] * Qj[p];
-                    v[q] += acc;
+                    for (int q = 0; q < 5; q++) v[q] += B.bq * ((R)biquad_metric(q) * Qj[q]);
+                } else {
+                    const R* Bm = T.bq + 25 * B.bqidx;
+#pragma unroll
+                    for (int q = 0; q < 5; q++) {
+                        R acc = 0;
+#pragma unroll
+                        for (int p = 0; p < 5; p++) acc += Bm[q + 5 * p] * Qj[p];
+                        v[q] += acc;
+                    }
                 }
             }
         }
@@ -255,7 +269,7 @@ __device__ __forceinline__ void local_HZ(const Model<R>& M, const SunTab<R, N>& 
 }
 
 template <class R, int N, int SPT, bool INJECT, bool BQ>
-__global__ void __launch_bounds__(SGB_BLOCK)
+__global__ void __launch_bounds__(sgb_maxblock(sizeof(R) == 8, true, SPT))
 k_sun_heun(Model<R> M, R* Z, R* D, R* Qb, R* P, R* QP, Ctrl* ctrl, int nsteps, R dt, R lam, R nscale,
            uint64_t seed, uint64_t step0, const double* noise) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -356,7 +370,7 @@ __device__ __forceinline__ void write_snapshot_sun(const Model<R>& M, const Snap
 // Schrodinger midpoint (Integrators.jl:422-452). H: 3 rotating [3][ns] dipole buffers of
 // <Zbar|S|Zbar>; QH: 3 rotating [5][ns] quadrupole buffers.
 template <class R, int N, int SPT, bool BQ>
-__global__ void __launch_bounds__(SGB_BLOCK)
+__global__ void __launch_bounds__(sgb_maxblock(sizeof(R) == 8, true, SPT))
 k_sun_midpoint(Model<R> M, R* Z, R* D, R* Qb, R* H, R* QH, Ctrl* ctrl, int nsteps, R dt, R lam,
                double atol2, int max_iters, SnapArgs<R> snap) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -422,7 +436,7 @@ k_sun_midpoint(Model<R> M, R* Z, R* D, R* Qb, R* H, R* QH, Ctrl* ctrl, int nstep
                 for (int c = 0; c < 2 * N; c++) zb[c] = (zc[k][c] + zc[k][c]) / 2;
                 publish<R, N, BQ>(sc, S.qm, zb, ns, site, H + (size_t)nst * 3 * ns, QH + (size_t)nst * 5 * ns);
             }
-            double bsum = sgb_block_sum<SGB_BLOCK>(acc);
+            double bsum = sgb_block_sum(acc);
             const int slot = (int)(itg % 3);
             if (threadIdx.x == 0) atomicAdd(&ctrl->acc[slot], bsum);
             if (leader) { ctrl->acc[(slot + 1) % 3] = 0.0; ctrl->iters += 1; }
@@ -562,10 +576,10 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_sun_energy(Model<R> M, const R* Z
             }
         }
     }
-    double e = sgb_block_sum<SGB_BLOCK>(E);
-    double a0 = sgb_block_sum<SGB_BLOCK>(mx);
-    double a1 = sgb_block_sum<SGB_BLOCK>(my);
-    double a2 = sgb_block_sum<SGB_BLOCK>(mz);
+    double e = sgb_block_sum(E);
+    double a0 = sgb_block_sum(mx);
+    double a1 = sgb_block_sum(my);
+    double a2 = sgb_block_sum(mz);
     if (threadIdx.x == 0) {
         partials[4 * blockIdx.x + 0] = e;
         partials[4 * blockIdx.x + 1] = a0;
@@ -612,11 +626,11 @@ int mid_n(const Model<R>& M, void** args, const LaunchInfo& li, cudaStream_t st)
 }
 
 template <class R, int N>
-int occ_n(int spt, size_t smem, int* bps) {
+int occ_n(int spt, int block, size_t smem, int* bps) {
     int best = 1 << 30, a = 0;
     auto one = [&](auto k) -> int {
         if (set_smem(k, smem) != SGB_OK) return SGB_ERR_CUDA;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k, SGB_BLOCK, smem) != cudaSuccess) return SGB_ERR_CUDA;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k, block, smem) != cudaSuccess) return SGB_ERR_CUDA;
         best = a < best ? a : best;
         return SGB_OK;
     };
@@ -677,12 +691,12 @@ int sun_launch_midpoint(const Model<R>& M, R* Z, R* D, R* Q, R* H, R* QH, Ctrl* 
 }
 
 template <class R>
-int sun_max_blocks(int N, int spt, size_t smem, int* bps) {
+int sun_max_blocks(int N, int spt, int block, size_t smem, int* bps) {
     switch (N) {
-        case 2: return occ_n<R, 2>(spt, smem, bps);
-        case 3: return occ_n<R, 3>(spt, smem, bps);
-        case 4: return occ_n<R, 4>(spt, smem, bps);
-        case 5: return occ_n<R, 5>(spt, smem, bps);
+        case 2: return occ_n<R, 2>(spt, block, smem, bps);
+        case 3: return occ_n<R, 3>(spt, block, smem, bps);
+        case 4: return occ_n<R, 4>(spt, block, smem, bps);
+        case 5: return occ_n<R, 5>(spt, block, smem, bps);
     }
     return SGB_ERR_ARG;
 }
@@ -728,7 +742,7 @@ int sun_launch_energy(const Model<R>& M, const R* Z, const R* D, const R* Q, dou
                                     uint64_t, uint64_t, const double*, const LaunchInfo&, cudaStream_t);        \
     template int sun_launch_midpoint<R>(const Model<R>&, R*, R*, R*, R*, R*, Ctrl*, int, double, double, double, \
                                         int, const SnapArgs<R>&, const LaunchInfo&, cudaStream_t);              \
-    template int sun_max_blocks<R>(int, int, size_t, int*);                                                     \
+    template int sun_max_blocks<R>(int, int, int, size_t, int*);                                                     \
     template int sun_launch_refresh<R>(const Model<R>&, const R*, R*, R*, cudaStream_t);                        \
     template int sun_launch_grad<R>(const Model<R>&, const R*, const R*, const R*, double*, cudaStream_t);      \
     template int sun_launch_energy<R>(const Model<R>&, const R*, const R*, const R*, double*, int, cudaStream_t);

@@ -110,8 +110,15 @@ def test_midpoint_fp64(gpu, sg, orc):
 
 
 def test_midpoint_energy_conservation_gpu(gpu, sg):
-    # test_energy_consistency.jl:37-55 on the GPU path, FP64
-    sys_ = rich_dipole(sg, dims=(2, 2, 2), biquad_matrix=False)
+    # test_energy_consistency.jl:37-55 on the GPU path, FP64: s=2 diamond with exchange,
+    # quartic anisotropy and a field
+    sys_ = sg.System(sg.diamond_crystal(), [(1, sg.Moment(s=2, g=2))], "dipole", dims=(2, 2, 2), seed=0)
+    sys_.set_exchange(0.5, sg.Bond(1, 2, [0, 0, 0]))
+    O4 = sg.stevens_matrices_of_dim(4, 5)
+    for a in range(1, 9):
+        sys_.set_onsite_coupling(0.2 * ((1 / 20) * O4[4] + (1 / 4) * O4[0]), a)
+    sys_.set_field([0.0, 0.2, 0.3])
+    sys_.randomize_spins()
     Es = []
     integ = sg.ImplicitMidpoint(0.002)
     for _ in range(150):
