@@ -145,6 +145,83 @@ def run_arm(sg, precision, device, warmup, steps, tol, thermal_steps=2000, e2e_s
     return res
 
 
+def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000):
+    """Batched FP32 sampling: `nrep` replicas of the pyrochlore model advance in one
+    persistent launch; each add_sample adds nrep samples with a rank-nrep accumulator pass."""
+    import ctypes as C
+    lib = sg.load_library()
+    proto = build_system(sg, "fp32", None)
+    b = sg.ReplicaBatch(proto, [proto.dims] * nrep, kT=[0.2] * nrep, precision="fp32", device=device, seed=7)
+    b.randomize_spins()
+    b.langevin(DT, 0.1, thermal_steps)
+    sc = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), energies=np.linspace(0, WMAX, NOMEGA), dt=DT, tol=tol)
+    for _ in range(warmup):
+        sg.add_sample(sc, b)
+    lib.sgb_corr_profile(sc._h, 1)
+    launches0 = lib.sgb_batch_kernel_launches(b.handle)
+    clocks = Clocks(device)
+    lib.sgb_batch_event_record(b.handle, 0)
+    for _ in range(steps):
+        sg.add_sample(sc, b)
+    lib.sgb_batch_event_record(b.handle, 1)
+    ms = C.c_float()
+    lib.sgb_batch_event_elapsed(b.handle, 0, 1, C.byref(ms))
+    clk = clocks.stop()
+    ph = np.zeros(4)
+    n = C.c_int64()
+    its = C.c_int64()
+    lib.sgb_corr_phase_times(sc._h, ph.ctypes.data_as(C.POINTER(C.c_double)), C.byref(n), C.byref(its))
+    nsteps_sample = sc.measperiod * (sc.n_all_omega // 2)
+    res = {"ms": ms.value, "phase_ms": (ph / max(1, n.value)).tolist(), "launches": lib.sgb_batch_kernel_launches(b.handle) - launches0,
+           "clocks": clk, "nrep": nrep, "ns": proto.nsites, "nsteps_per_sample": nsteps_sample,
+           "iters_per_step": its.value / max(1, n.value) / nsteps_sample, "n_all_omega": sc.n_all_omega}
+    # end to end: every replica's state in from host memory, add_sample, every state out
+    states = [b.get_state(r) for r in range(nrep)]
+    t0 = time.perf_counter()
+    e2e_steps = max(2, steps // 2)
+    for _ in range(e2e_steps):
+        for r in range(nrep):
+            b.set_state(r, states[r])
+        sg.add_sample(sc, b)
+        states = [b.get_state(r) for r in range(nrep)]
+    res["e2e_s"] = time.perf_counter() - t0
+    res["e2e_steps"] = e2e_steps
+    res["h2d"] = res["d2h"] = nrep * proto.nsites * 3 * 4
+    sc.close()
+    b.close()
+    return res
+
+
+def run_tempering(sg, device, nsteps=5000, exch_interval=100, seed=2024):
+    """256 simple-cubic replicas, L drawn uniformly from {8,12,16,24,32}, kT on a geometric
+    0.1-2.0 ladder, J=1, -0.1 Sz^2, Langevin damping 0.2, exchanges every 100 steps within
+    groups of equal L; FP32 state, FP64 energies; one CUDA graph per exchange round."""
+    import ctypes as C
+    lib = sg.load_library()
+    rng = np.random.default_rng(seed)
+    Ls = rng.choice([8, 12, 16, 24, 32], size=256)
+    kT = np.geomspace(0.1, 2.0, 256)
+    proto = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=(8, 8, 8), seed=1, device=None)
+    proto.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    proto.set_onsite_coupling(lambda Sx, Sy, Sz: -0.1 * Sz @ Sz, 1)
+    b = sg.ReplicaBatch(proto, [(int(L),) * 3 for L in Ls], kT=kT, precision="fp32", device=device, seed=seed)
+    b.randomize_spins()
+    pt = sg.ParallelTempering(b, 0.02, 0.2)
+    pt.step_ensemble(2 * exch_interval, exch_interval)          # warm-up (graph capture)
+    lib.sgb_batch_event_record(b.handle, 0)
+    pt.step_ensemble(nsteps, exch_interval)
+    lib.sgb_batch_event_record(b.handle, 1)
+    ms = C.c_float()
+    lib.sgb_batch_event_elapsed(b.handle, 0, 1, C.byref(ms))
+    nsites = int(sum(int(L) ** 3 for L in Ls))
+    acc = pt.n_accept.sum()
+    out = {"site_steps_per_s": nsites * nsteps / (ms.value / 1000.0), "ms": ms.value, "steps": nsteps,
+           "replicas": 256, "total_sites": nsites, "graph": pt.graph_active, "accepted_swaps": int(acc),
+           "us_per_step": 1000.0 * ms.value / nsteps}
+    b.close()
+    return out
+
+
 def dynamics_rate(sg, kind, precision, device, nsteps):
     """Site-steps/s of plain Langevin dynamics for the other two single-system workloads:
     'sc'  -- simple cubic 16^3, s=1, J=1, -0.1 Sz^2, dt=0.02, damping 0.1, kT=0.5 (dipole)
@@ -275,6 +352,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=2, help="samples timed on the plain FP64 path (0 skips it)")
     ap.add_argument("--L", type=int, default=16, help="cells per axis (16 is the benchmark; smaller for profiling)")
+    ap.add_argument("--nrep", type=int, default=8, help="replicas sampled per batched add_sample")
+    ap.add_argument("--no-extra", action="store_true", help="skip the tempering and Langevin site-step arms")
     args = ap.parse_args()
     global L
     L = args.L
@@ -310,34 +389,42 @@ def main():
         return float(t.item())
 
     barrier()
-    r32 = run_arm(sg, "fp32", local, args.warmup, args.steps, tol=1e-6, e2e_steps=max(2, args.steps // 2))
+    rb = run_batched(sg, local, args.nrep, args.warmup, args.steps, tol=1e-6)
+    barrier()
+    r32 = run_arm(sg, "fp32", local, args.warmup, max(2, args.steps // 2), tol=1e-6)
+    # (single-system FP32 path: one replica per add_sample)
     barrier()
     r64 = run_arm(sg, "fp64", local, 1, args.fp64_steps, tol=1e-12) if args.fp64_steps > 0 else None
     extra = {}
-    for kind, n in (("sc", 10000), ("tri", 2000)):
-        a = dynamics_rate(sg, kind, "fp32", local, n)
-        b = dynamics_rate(sg, kind, "fp64", local, n // 4)
-        extra[kind] = {"fp32": a, "fp64": b, "speedup": a["site_steps_per_s"] / b["site_steps_per_s"]}
+    pt = None
+    if not args.no_extra:
+        for kind, n in (("sc", 10000), ("tri", 2000)):
+            a = dynamics_rate(sg, kind, "fp32", local, n)
+            bb = dynamics_rate(sg, kind, "fp64", local, n // 4)
+            extra[kind] = {"fp32": a, "fp64": bb, "speedup": a["site_steps_per_s"] / bb["site_steps_per_s"]}
+        pt = run_tempering(sg, local)
     barrier()
-    ms = maxall(r32["ms"])
-    value = world * args.steps / (ms / 1000.0)
-    nsteps_sample = r32["nsteps_per_sample"]
-    site_steps = value * r32["ns"] * nsteps_sample
+    ms = maxall(rb["ms"])
+    value = world * args.steps * rb["nrep"] / (ms / 1000.0)
+    nsteps_sample = rb["nsteps_per_sample"]
+    site_steps = value * rb["ns"] * nsteps_sample
+    v32 = world * max(2, args.steps // 2) / (maxall(r32["ms"]) / 1000.0)
     v64 = world * args.fp64_steps / (maxall(r64["ms"]) / 1000.0) if r64 else None
-    e2e_s = maxall(r32["e2e_s"])
-    e2e_val = world * r32["e2e_steps"] / e2e_s
+    e2e_s = maxall(rb["e2e_s"])
+    e2e_val = world * rb["e2e_steps"] * rb["nrep"] / e2e_s
     # roofline of the dominant phase, from the live per-phase CUDA events
     hbm, peak_kind = peaks()
-    ph = r32["phase_ms"]
-    ncorr, npos, ncell, nw = 6, 16, L**3, r32["n_all_omega"]
-    bytes_accum = 2 * 16 * ncorr * npos * npos * ncell * nw + 8 * 3 * npos * ncell * nw
-    bytes_traj = 24 * r32["ns"] * nsteps_sample
+    ph = rb["phase_ms"]
+    R = rb["nrep"]
+    ncorr, npos, ncell, nw = 6, 16, L**3, rb["n_all_omega"]
+    bytes_accum = 2 * 16 * ncorr * npos * npos * ncell * nw + R * 8 * 3 * npos * ncell * nw
+    bytes_traj = R * 24 * rb["ns"] * nsteps_sample
     kernels = [
-        {"kernel": "k_dip_midpoint (trajectory + snapshots)", "ms_per_launch": ph[0], "alg_bytes": bytes_traj,
-         "achieved_gbs": bytes_traj / (ph[0] * 1e6) if ph[0] else None},
-        {"kernel": "cuFFT space (3-D, 200 x 48 transforms)", "ms_per_launch": ph[1]},
-        {"kernel": "cuFFT time (1-D n=398, 196,608 transforms)", "ms_per_launch": ph[2]},
-        {"kernel": "k_corr_accum (FP64 accumulator stream)", "ms_per_launch": ph[3], "alg_bytes": bytes_accum,
+        {"kernel": f"k_batch_midpoint ({R} replicas: trajectories + snapshots)", "ms_per_launch": ph[0],
+         "alg_bytes": bytes_traj, "achieved_gbs": bytes_traj / (ph[0] * 1e6) if ph[0] else None},
+        {"kernel": f"cuFFT space (3-D, {R} x 200 x 48 transforms)", "ms_per_launch": ph[1]},
+        {"kernel": f"cuFFT time (1-D n=398, {R} x 196,608 transforms)", "ms_per_launch": ph[2]},
+        {"kernel": f"k_corr_accum (rank-{R} FP64 accumulator stream)", "ms_per_launch": ph[3], "alg_bytes": bytes_accum,
          "achieved_gbs": bytes_accum / (ph[3] * 1e6) if ph[3] else None},
     ]
     dom = max((k for k in kernels if "alg_bytes" in k), key=lambda k: k["ms_per_launch"])
@@ -352,25 +439,30 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "pyrochlore 16x16x16x16 (65,536 spins, s=3/2, J1=1, J2=0.05) S(q,w) sampling: "
                                    "ImplicitMidpoint dt=0.024933, 21 steps per snapshot, 200 snapshots, nw=200 to 6 meV, "
-                                   "6 correlation pairs x 16 x 16 sublattices, FP64 accumulator",
-                       "global_batch": world, "seq_len": nsteps_sample, "parallelism": f"replicas x{world}",
+                                   "6 correlation pairs x 16 x 16 sublattices, FP64 accumulator; "
+                                   f"{R} replicas per batched add_sample ({R * args.steps} samples timed)",
+                       "global_batch": world * R, "seq_len": nsteps_sample, "parallelism": f"replicas x{world * R}",
                        "l2": "inputs larger than L2 (40 GB accumulator streamed every step)",
                        "midpoint_tol": {"fp32": 1e-6, "fp64": 1e-12}},
             "site_steps_per_s": site_steps,
+            "fp32_single": {"value": v32, "unit": "samples/s", "ms_per_step": r32["ms"] / max(2, args.steps // 2),
+                            "phase_ms": r32["phase_ms"], "iters_per_step": r32["iters_per_step"]},
             "fp64_plain": None if r64 is None else
             {"value": v64, "unit": "samples/s", "site_steps_per_s": v64 * r32["ns"] * nsteps_sample,
              "ms_per_step": r64["ms"] / args.fp64_steps, "phase_ms": r64["phase_ms"]},
             "speedup_vs_fp64_plain": None if r64 is None else value / v64,
             "phase_ms": {"trajectory": ph[0], "space_fft": ph[1], "time_fft": ph[2], "accumulate": ph[3]},
-            "midpoint_iters_per_step": {"fp32": r32["iters_per_step"], "fp64": None if r64 is None else r64["iters_per_step"]},
-            "us_per_midpoint_iteration": 1000.0 * ph[0] / (r32["iters_per_step"] * nsteps_sample),
+            "midpoint_iters_per_step": {"fp32_batched": rb["iters_per_step"], "fp32": r32["iters_per_step"],
+                                        "fp64": None if r64 is None else r64["iters_per_step"]},
+            "us_per_midpoint_iteration": 1000.0 * ph[0] / (rb["iters_per_step"] * nsteps_sample),
             "kernels": kernels,
-            "langevin_site_steps": {"simple_cubic_16^3_dipole": extra["sc"], "triangular_48x48x4_SU3": extra["tri"]},
+            "langevin_site_steps": {"simple_cubic_16^3_dipole": extra.get("sc"), "triangular_48x48x4_SU3": extra.get("tri"),
+                                    "tempering_256_replicas": pt},
             "roofline": roof,
-            "gpu_launches": r32["launches"],
-            "clocks": r32["clocks"],
-            "e2e": {"value": e2e_val, "unit": "samples/s", "h2d_bytes_per_step": r32["h2d"],
-                    "d2h_bytes_per_step": r32["d2h"]}}
+            "gpu_launches": rb["launches"],
+            "clocks": rb["clocks"],
+            "e2e": {"value": e2e_val, "unit": "samples/s", "h2d_bytes_per_step": rb["h2d"],
+                    "d2h_bytes_per_step": rb["d2h"]}}
     if L != 16:
         line["config"]["workload"] = f"REDUCED SIZE L={L} (profiling case, not the benchmark): " + line["config"]["workload"]
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

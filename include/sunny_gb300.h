@@ -223,11 +223,23 @@ int sgb_batch_energy(sgb_batch* b, double* E);
  * n_accept (nullable, int64[nrep]) accumulates accepted swaps per lower slot. */
 int sgb_batch_exchange(sgb_batch* b, int32_t exch_start, uint64_t seed, uint64_t round,
                        const double* uniforms, int64_t* n_accept);
-/* step_ensemble!(PT, nsteps, exch_interval) (ParallelTempering.jl:80-95): rounds of
- * exch_interval Langevin steps followed by an exchange, captured once as a CUDA graph
- * and replayed. */
+/* step_ensemble!(PT, nsteps, exch_interval) (ParallelTempering.jl:80-95): cld(nsteps,
+ * exch_interval) rounds of exch_interval Langevin steps, FP64 energies and one exchange
+ * (round i uses exch_start = i % 2 + 1), captured once as a CUDA graph and replayed.
+ * Langevin noise continues from the step counter of the last sgb_batch_langevin call. */
 int sgb_batch_step_ensemble(sgb_batch* b, double dt, double damping, uint64_t seed,
                             int32_t nsteps, int32_t exch_interval, int64_t* n_accept);
+/* 1 if the last step_ensemble ran from a captured CUDA graph, 0 if it fell back to
+ * direct launches. */
+int sgb_batch_graph_active(const sgb_batch* b);
+/* The standard normals that replica `rep` uses at Langevin step `step`: [ns][3]. */
+int sgb_batch_langevin_noise(sgb_batch* b, int32_t rep, uint64_t seed, uint64_t step, double* out);
+
+/* SampledCorrelations over a batch of equal-size replicas: each sgb_corr_add_sample call
+ * integrates every replica's trajectory in one persistent launch and adds nrep samples
+ * (the parallel add_sample! pattern of Sunny's docs/src/parallelism.md:82-125, merged
+ * on device). The accumulator is then used with sgb_corr_data / merge / destroy. */
+int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* desc, sgb_corr** out);
 
 /* ---- measurement helpers ---------------------------------------------------- */
 

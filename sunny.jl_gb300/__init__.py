@@ -14,6 +14,7 @@ from .system import (System, Moment, Langevin, ImplicitMidpoint, step, energy, e
 from .correlations import (SampledCorrelations, MeasureSpec, ssf_trace, ssf_perp, ssf_custom, add_sample,
                            merge_correlations, available_energies, available_wave_vectors,
                            adjusted_dt_and_downsampling_factor, all_dipole_observables)
+from .tempering import ReplicaBatch, ParallelTempering
 from ._abi import SunnyGPUError, load as load_library
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -87,6 +87,9 @@ SIGNATURES = {
     "sgb_batch_energy": (C.c_int, [_P, _D]),
     "sgb_batch_exchange": (C.c_int, [_P, _I32, _U64, _U64, _D, C.POINTER(_I64)]),
     "sgb_batch_step_ensemble": (C.c_int, [_P, C.c_double, C.c_double, _U64, _I32, _I32, C.POINTER(_I64)]),
+    "sgb_batch_graph_active": (C.c_int, [_P]),
+    "sgb_batch_langevin_noise": (C.c_int, [_P, _I32, _U64, _U64, _D]),
+    "sgb_batch_corr_create": (C.c_int, [_P, C.POINTER(CorrDesc), C.POINTER(_P)]),
     "sgb_event_record": (C.c_int, [_P, _I32]),
     "sgb_event_elapsed": (C.c_int, [_P, _I32, _I32, C.POINTER(C.c_float)]),
     "sgb_batch_event_record": (C.c_int, [_P, _I32]),

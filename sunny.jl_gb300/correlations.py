@@ -76,9 +76,13 @@ def adjusted_dt_and_downsampling_factor(dt: float, nw: int, wmax: float):
 
 
 class SampledCorrelations:
-    """SampledCorrelations(sys; measure, energies, dt, integrator) (SampledCorrelations.jl:199-269)."""
+    """SampledCorrelations(sys; measure, energies, dt, integrator) (SampledCorrelations.jl:199-269).
 
-    def __init__(self, sys: System, *, measure: MeasureSpec, energies, dt, calculate_errors=False,
+    `sys` may also be a ReplicaBatch of equal-size replicas: each add_sample then
+    integrates every replica and accumulates one sample per replica (the parallel
+    sampling pattern of Sunny's docs/src/parallelism.md, merged on the device)."""
+
+    def __init__(self, sys, *, measure: MeasureSpec, energies, dt, calculate_errors=False,
                  integrator: ImplicitMidpoint | None = None, tol: float | None = None):
         if energies is None:
             n_all_w, measperiod, dw = 1, 1, math.nan
@@ -126,15 +130,31 @@ class SampledCorrelations:
         d.tol = integrator.tol
         d.max_iters = 100
         d.calculate_errors = 1 if calculate_errors else 0
-        sys._sync_to_device()
         h = C.c_void_p()
-        _abi.check(sys._lib.sgb_corr_create(sys.handle, C.byref(d), C.byref(h)), sys._lib, sys.handle)
+        self._batch = None
+        from .tempering import ReplicaBatch
+        if isinstance(sys, ReplicaBatch):
+            if len(set(sys.dims_list)) != 1 or sys.dims_list[0] != sys.proto.dims:
+                raise ValueError("batched sampling needs replicas with the prototype's dims")
+            self._batch = sys
+            sys._check(sys._lib.sgb_batch_corr_create(sys.handle, C.byref(d), C.byref(h)))
+            self._lib, self._errh = sys._lib, None
+        else:
+            sys._sync_to_device()
+            _abi.check(sys._lib.sgb_corr_create(sys.handle, C.byref(d), C.byref(h)), sys._lib, sys.handle)
+            self._lib, self._errh = sys._lib, sys.handle
         self._h = h
 
     def close(self):
         if getattr(self, "_h", None):
-            self.sys._lib.sgb_corr_destroy(self._h)
+            self._lib.sgb_corr_destroy(self._h)
             self._h = None
+
+    def _check(self, rc):
+        if rc != _abi.SGB_OK:
+            if self._batch is not None:
+                self._batch._check(rc)
+            _abi.check(rc, self._lib, self._errh)
 
     def __del__(self):
         try:
@@ -145,30 +165,35 @@ class SampledCorrelations:
     @property
     def nsamples(self) -> int:
         n = C.c_int64()
-        _abi.check(self.sys._lib.sgb_corr_data(self._h, None, None, C.byref(n)), self.sys._lib, self.sys.handle)
+        self._check(self._lib.sgb_corr_data(self._h, None, None, C.byref(n)))
         return n.value
 
     @property
     def shape(self):
         ncorr = len(self.measure.corr_pairs)
-        na = self.sys.natoms
-        return (ncorr, na, na, *self.sys.dims, self.n_all_omega)
+        proto = self._batch.proto if self._batch is not None else self.sys
+        na = proto.natoms
+        return (ncorr, na, na, *proto.dims, self.n_all_omega)
 
     @property
     def data(self) -> np.ndarray:
         """sc.data: complex array indexed [c, i, j, q1, q2, q3, ω] (0-based)."""
         shp = self.shape
         flat = np.zeros(2 * int(np.prod(shp)))
-        _abi.check(self.sys._lib.sgb_corr_data(self._h, _abi.dptr(flat), None, None), self.sys._lib, self.sys.handle)
+        self._check(self._lib.sgb_corr_data(self._h, _abi.dptr(flat), None, None))
         z = flat[0::2] + 1j * flat[1::2]
         return z.reshape(shp[::-1]).transpose(tuple(range(len(shp) - 1, -1, -1)))
 
 
-def add_sample(sc: SampledCorrelations, sys: System, window: str = "cosine"):
-    """add_sample!(sc, sys; window) (CorrelationSampling.jl:156-176). Mutates sys."""
+def add_sample(sc: SampledCorrelations, sys, window: str = "cosine"):
+    """add_sample!(sc, sys; window) (CorrelationSampling.jl:156-176). Mutates sys (or
+    every replica of a ReplicaBatch, adding one sample per replica)."""
     if sys is not sc.sys:
         raise ValueError("a GPU SampledCorrelations is bound to the System it was created with")
     w = {"cosine": 0, "rectangular": 1}[window]
+    if sc._batch is not None:
+        sc._check(sc._lib.sgb_corr_add_sample(sc._h, w))
+        return
     sys._sync_to_device()
     rc = sys._lib.sgb_corr_add_sample(sc._h, w)
     sys._dev_newer = True
@@ -193,12 +218,15 @@ def merge_correlations(scs):
     d.tol = first.integrator.tol
     d.max_iters = 100
     d.calculate_errors = 0
-    lib = first.sys._lib
+    lib = first._lib
     h = C.c_void_p()
-    _abi.check(lib.sgb_corr_create(first.sys.handle, C.byref(d), C.byref(h)), lib, first.sys.handle)
+    if first._batch is not None:
+        first._batch._check(lib.sgb_batch_corr_create(first._batch.handle, C.byref(d), C.byref(h)))
+    else:
+        _abi.check(lib.sgb_corr_create(first.sys.handle, C.byref(d), C.byref(h)), lib, first.sys.handle)
     out._h = h
     for sc in scs:
-        _abi.check(lib.sgb_corr_merge(out._h, sc._h), lib, first.sys.handle)
+        out._check(lib.sgb_corr_merge(out._h, sc._h))
     return out
 
 

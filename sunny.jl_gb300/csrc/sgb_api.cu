@@ -16,75 +16,12 @@
 #include <vector>
 #include "sgb_internal.h"
 #include "sgb_corr.h"
+#include "sgb_tables.h"
+#include "sgb_handles.h"
 
 #define SGB_VERSION "sunny-gb300 0.1.0 (sm_103a)"
 
 static thread_local std::string g_last_error;
-
-struct sgb_system {
-    sgb_desc d{};
-    int ns = 0, ncell = 0, N = 0;
-    bool fp32 = false;
-    bool sun = false;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev[8] = {};
-    std::string err;
-    long long launches = 0;
-    int nsm = 0;
-    // host copies of the model
-    std::vector<double> kappa_h, g_h, field_h, onsite_h;
-    std::vector<sgb_bond> bonds_h;
-    bool sites_set = false, bonds_set = false, state_set = false;
-    bool has_field = false, has_biquad = false;
-    bool tables_dirty = true;
-    // device data (element type R = float or double)
-    void* kappa = nullptr;   // [ns]
-    void* h = nullptr;       // [3][ns]
-    void* tables = nullptr;
-    int tables_bytes = 0;
-    Model<float> mf{};
-    Model<double> md{};
-    // state buffers
-    void* S = nullptr;   // dipole: spins [3][ns]; SU(N): dipoles [3][ns]
-    void* P = nullptr;   // [3][ns]
-    void* H = nullptr;   // [3][3][ns]
-    void* Z = nullptr;   // SU(N) [2N][ns]
-    void* Q = nullptr;   // SU(N) [5][ns]
-    void* QP = nullptr;  // SU(N) [5][ns]
-    void* QH = nullptr;  // SU(N) [3][5][ns]
-    Ctrl* ctrl = nullptr;
-    double* partials = nullptr;
-    double* red = nullptr;
-    double* dbuf = nullptr;     // device double scratch (noise, grads)
-    size_t dbuf_cap = 0;
-    void* flush = nullptr;
-    char* stage = nullptr;      // pinned host staging
-    size_t stage_cap = 0;
-};
-
-struct sgb_corr {
-    sgb_system* sys = nullptr;
-    std::string err;
-    int nobs = 0, ncorr = 0, npos = 0, ncell = 0, nomega = 0, nsnaps = 0, measperiod = 1;
-    double dt = 0, damping = 0, tol = 0;
-    int max_iters = 100;
-    int window = -1;
-    int64_t nsamples = 0;
-    void* ops = nullptr;      // R
-    int* pairs = nullptr;
-    void* A = nullptr;        // complex R [n][nobs][npos][ncell]
-    void* Ahat = nullptr;
-    double* P = nullptr;      // complex double accumulator
-    size_t plen = 0;          // complex elements
-    double* g = nullptr;      // [n]
-    cufftHandle plan_space = 0, plan_time = 0;
-    bool have_space = false, have_time = false;
-    bool profile = false;
-    cudaEvent_t ev[5] = {};
-    double phase_ms[4] = {0, 0, 0, 0};
-    int64_t nprof = 0;
-    int64_t prof_iters = 0;
-};
 
 // ---------------------------------------------------------------------------------
 namespace {
@@ -144,163 +81,23 @@ int ensure_dbuf(sgb_system* s, size_t n) {
     return rc;
 }
 
-inline int imod(int x, int L) {
-    int r = x % L;
-    return r < 0 ? r + L : r;
-}
-
-// Stevens quadrupoles O[2,q], q = 2..-2, of dimension N (src/Operators/Stevens.jl:12-86),
-// column-major complex.
-void stevens_quadrupoles(int N, std::vector<std::complex<double>>& out) {
-    typedef std::complex<double> cd;
-    out.assign(5 * N * N, cd(0, 0));
-    if (N <= 2) return;
-    double s = (N - 1) / 2.0;
-    std::vector<cd> Sx(N * N), Sy(N * N), Sz(N * N);
-    for (int j = 1; j <= N - 1; j++) {
-        double off = std::sqrt(2 * (s + 1) * j - (double)j * (j + 1)) / 2;
-        int r = j - 1, c = j;
-        Sx[r + N * c] = off; Sx[c + N * r] = off;
-        Sy[r + N * c] = cd(0, -off); Sy[c + N * r] = cd(0, off);
-    }
-    for (int k = 0; k < N; k++) Sz[k + N * k] = s - k;
-    auto mul = [N](const std::vector<cd>& A, const std::vector<cd>& B) {
-        std::vector<cd> C(N * N);
-        for (int c = 0; c < N; c++)
-            for (int r = 0; r < N; r++) {
-                cd acc = 0;
-                for (int k = 0; k < N; k++) acc += A[r + N * k] * B[k + N * c];
-                C[r + N * c] = acc;
-            }
-        return C;
-    };
-    std::vector<cd> Jp(N * N), Jm(N * N);
-    for (int i = 0; i < N * N; i++) { Jp[i] = Sx[i] + cd(0, 1) * Sy[i]; Jm[i] = Sx[i] - cd(0, 1) * Sy[i]; }
-    auto Jp2 = mul(Jp, Jp), Jm2 = mul(Jm, Jm), Jz2 = mul(Sz, Sz);
-    auto X = mul(Sx, Sx);
-    { auto t = mul(Sy, Sy); for (int i = 0; i < N * N; i++) X[i] += t[i] + Jz2[i]; }
-    std::vector<cd> A(N * N);
-    for (int i = 0; i < N * N; i++) out[0 * N * N + i] = 0.5 * (Jp2[i] + Jm2[i]);
-    for (int i = 0; i < N * N; i++) A[i] = 0.5 * (Jp[i] + Jm[i]);
-    { auto a = mul(A, Sz), b = mul(Sz, A); for (int i = 0; i < N * N; i++) out[1 * N * N + i] = 0.5 * (a[i] + b[i]); }
-    for (int i = 0; i < N * N; i++) out[2 * N * N + i] = 3.0 * Jz2[i] - X[i];
-    for (int i = 0; i < N * N; i++) A[i] = (Jp[i] - Jm[i]) / cd(0, 2);
-    { auto a = mul(A, Sz), b = mul(Sz, A); for (int i = 0; i < N * N; i++) out[3 * N * N + i] = 0.5 * (a[i] + b[i]); }
-    for (int i = 0; i < N * N; i++) out[4 * N * N + i] = (Jp2[i] - Jm2[i]) / cd(0, 2);
-}
-
-size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
-
 template <class R>
 int build_tables(sgb_system* s, Model<R>& M) {
-    const int na = s->d.natoms, N = s->N;
-    const int L[3] = {s->d.dims[0], s->d.dims[1], s->d.dims[2]};
-    // directed bonds per sublattice
-    std::vector<std::vector<DBond<R>>> per(na);
-    std::vector<R> bqtab;
+    std::vector<unsigned char> buf;
     bool any_bq = false;
-    for (const sgb_bond& b : s->bonds_h) {
-        for (int dir = 0; dir < 2; dir++) {
-            DBond<R> e{};
-            int from = dir == 0 ? b.i : b.j;
-            int to = dir == 0 ? b.j : b.i;
-            e.j = to;
-            for (int k = 0; k < 3; k++) {
-                int n = dir == 0 ? b.n[k] : -b.n[k];
-                e.n[k] = imod(n, L[k]);
-            }
-            bool iso = true;
-            for (int r = 0; r < 3; r++)
-                for (int c = 0; c < 3; c++) {
-                    double v = dir == 0 ? b.bilin[r + 3 * c] : b.bilin[c + 3 * r];
-                    e.J[r + 3 * c] = (R)v;
-                    if (r != c && v != 0.0) iso = false;
-                }
-            if (!(b.bilin[0] == b.bilin[4] && b.bilin[0] == b.bilin[8])) iso = false;
-            e.jkind = iso ? 0 : 1;
-            e.scalar = (R)b.scalar;
-            e.bqkind = b.biquad_kind;
-            e.bq = 0;
-            e.bqidx = 0;
-            if (b.biquad_kind == 1) {
-                e.bq = (R)b.biquad[0];
-                if (b.biquad[0] == 0.0) e.bqkind = 0;
-            } else if (b.biquad_kind == 2) {
-                e.bqidx = (int)(bqtab.size() / 25);
-                for (int c = 0; c < 5; c++)
-                    for (int r = 0; r < 5; r++)
-                        bqtab.push_back((R)(dir == 0 ? b.biquad[r + 5 * c] : b.biquad[c + 5 * r]));
-            }
-            if (e.bqkind != 0) any_bq = true;
-            e.fwd = dir == 0 ? 1 : 0;
-            per[from].push_back(e);
-        }
-    }
-    int nb = 0;
-    for (auto& v : per) nb += (int)v.size();
-    int nbq = (int)(bqtab.size() / 25);
-    size_t off = 0;
-    M.off_stev = (int)off; off = align16(off + sizeof(R) * 28 * na);
-    M.off_kmax = (int)off; off = align16(off + sizeof(int) * na);
-    M.off_boff = (int)off; off = align16(off + sizeof(int) * (na + 1));
-    M.off_bonds = (int)off; off = align16(off + sizeof(DBond<R>) * nb);
-    M.off_bq = (int)off; off = align16(off + sizeof(R) * 25 * nbq);
-    M.off_lam = (int)off; off = align16(off + sizeof(R) * 2 * N * N * (s->sun ? na : 0));
-    M.off_qmat = (int)off; off = align16(off + sizeof(R) * 2 * N * N * 5 * (s->sun ? 1 : 0));
-    size_t bytes = align16(off);
-    if (bytes > 200 * 1024) return fail(s, SGB_ERR_ARG, "coupling tables exceed 200 KiB of shared memory");
-    std::vector<unsigned char> buf(bytes, 0);
-    R* stev = reinterpret_cast<R*>(buf.data() + M.off_stev);
-    int* kmax = reinterpret_cast<int*>(buf.data() + M.off_kmax);
-    int* boff = reinterpret_cast<int*>(buf.data() + M.off_boff);
-    DBond<R>* bonds = reinterpret_cast<DBond<R>*>(buf.data() + M.off_bonds);
-    R* bq = reinterpret_cast<R*>(buf.data() + M.off_bq);
-    if (!s->sun) {
-        for (int a = 0; a < na; a++) {
-            const double* c = s->onsite_h.data() + 28 * a;
-            // StevensExpansion drops k-blocks with norm < 1e-12 (src/System/Types.jl:12-16)
-            const int start[4] = {0, 1, 6, 15}, len[4] = {1, 5, 9, 13};
-            int km = 0;
-            for (int g = 0; g < 4; g++) {
-                double nrm = 0;
-                for (int q = 0; q < len[g]; q++) nrm += c[start[g] + q] * c[start[g] + q];
-                bool zero = std::sqrt(nrm) < 1e-12;
-                for (int q = 0; q < len[g]; q++) stev[28 * a + start[g] + q] = zero ? (R)0 : (R)c[start[g] + q];
-                if (!zero && g > 0) km = 2 * g;
-            }
-            kmax[a] = km;
-        }
-    } else {
-        R* lam = reinterpret_cast<R*>(buf.data() + M.off_lam);
-        for (int i = 0; i < 2 * N * N * na; i++) lam[i] = (R)s->onsite_h[i];
-        std::vector<std::complex<double>> qm;
-        stevens_quadrupoles(N, qm);
-        R* q = reinterpret_cast<R*>(buf.data() + M.off_qmat);
-        for (int i = 0; i < 5 * N * N; i++) { q[2 * i] = (R)qm[i].real(); q[2 * i + 1] = (R)qm[i].imag(); }
-    }
-    int k = 0;
-    for (int a = 0; a < na; a++) {
-        boff[a] = k;
-        for (auto& e : per[a]) bonds[k++] = e;
-    }
-    boff[na] = k;
-    for (size_t i = 0; i < bqtab.size(); i++) bq[i] = bqtab[i];
+    std::string e = sgbhost::pack_tables<R>(s->d.natoms, s->N, s->sun, s->d.dims, s->bonds_h, s->onsite_h, M, buf, any_bq);
+    if (!e.empty()) return fail(s, SGB_ERR_ARG, e);
     dfree(s->tables);
-    int rc = dmalloc(s, &s->tables, bytes);
+    int rc = dmalloc(s, &s->tables, buf.size());
     if (rc) return rc;
-    CK(cudaMemcpy(s->tables, buf.data(), bytes, cudaMemcpyHostToDevice));
-    s->tables_bytes = (int)bytes;
+    CK(cudaMemcpy(s->tables, buf.data(), buf.size(), cudaMemcpyHostToDevice));
+    s->tables_bytes = (int)buf.size();
     s->has_biquad = any_bq;
-    M.L1 = L[0]; M.L2 = L[1]; M.L3 = L[2]; M.na = na;
-    M.ns = s->ns; M.ncell = s->ncell; M.N = N;
-    M.dipole_mode = s->sun ? 0 : 1;
-    M.has_biquad = any_bq ? 1 : 0;
+    M.L1 = s->d.dims[0]; M.L2 = s->d.dims[1]; M.L3 = s->d.dims[2];
+    M.ns = s->ns; M.ncell = s->ncell;
     M.kappa = reinterpret_cast<const R*>(s->kappa);
     M.h = s->has_field ? reinterpret_cast<const R*>(s->h) : nullptr;
     M.tables = reinterpret_cast<const unsigned char*>(s->tables);
-    M.tables_bytes = (int)bytes;
-    M.nb = nb;
-    M.nbq = nbq;
     return SGB_OK;
 }
 
@@ -796,14 +593,14 @@ int sgb_flush_l2(sgb_system* s) {
 // SampledCorrelations
 // ---------------------------------------------------------------------------------
 static int cfail(sgb_corr* c, int code, const std::string& msg) {
-    if (c) { c->err = msg; if (c->sys) c->sys->err = msg; }
+    if (c) { c->err = msg; if (c->sys) c->sys->err = msg; if (c->batch) c->batch->err = msg; }
     g_last_error = msg;
     return code;
 }
 
 void sgb_corr_destroy(sgb_corr* c) {
     if (!c) return;
-    if (c->sys && c->sys->stream) cudaStreamSynchronize(c->sys->stream);
+    if (c->stream) cudaStreamSynchronize(c->stream);
     dfree(c->ops);
     void* p = c->pairs; dfree(p);
     dfree(c->A); dfree(c->Ahat);
@@ -815,66 +612,114 @@ void sgb_corr_destroy(sgb_corr* c) {
     delete c;
 }
 
-int sgb_corr_create(sgb_system* s, const sgb_corr_desc* d, sgb_corr** out) {
-    if (!s || !d || !out) return fail(s, SGB_ERR_ARG, "null argument");
-    *out = nullptr;
-    if (d->nobs < 1 || d->ncorr < 1 || !d->obs || !d->pairs) return fail(s, SGB_ERR_ARG, "observables and correlation pairs are required");
-    if (d->n_all_omega < 1 || d->measperiod < 1) return fail(s, SGB_ERR_ARG, "n_all_omega and measperiod must be positive");
-    if (d->n_all_omega > 1 && !(d->dt > 0)) return fail(s, SGB_ERR_ARG, "Select positive dt");
-    if (d->calculate_errors) return fail(s, SGB_ERR_ARG, "calculate_errors is not supported by this build of the accumulator");
-    for (int k = 0; k < 2 * d->ncorr; k++)
-        if (d->pairs[k] < 0 || d->pairs[k] >= d->nobs) return fail(s, SGB_ERR_ARG, "correlation pair index out of range");
-    int rc = ensure_tables(s);
-    if (rc) return rc;
-    sgb_corr* c = new sgb_corr();
-    c->sys = s;
-    c->nobs = d->nobs; c->ncorr = d->ncorr; c->npos = s->d.natoms; c->ncell = s->ncell;
+// Shared set-up of an accumulator for `nrep` identical systems of `ns` sites.
+static int corr_setup(sgb_corr* c, const sgb_corr_desc* d, bool fp32, bool sun, int N, int ns, int natoms,
+                      const int* dims, int nrep) {
+    const size_t R = fp32 ? 4 : 8;
+    c->nobs = d->nobs; c->ncorr = d->ncorr; c->npos = natoms; c->ncell = dims[0] * dims[1] * dims[2];
     c->nomega = d->n_all_omega;
     c->nsnaps = d->n_all_omega / 2 + 1;   // CorrelationSampling.jl:37-38
     c->measperiod = d->measperiod;
     c->dt = d->dt; c->damping = d->damping; c->tol = d->tol; c->max_iters = d->max_iters;
-    const int ns = s->ns, N = s->N;
-    const size_t R = rsize(s);
-    auto bad = [&](int code) { sgb_corr_destroy(c); return code; };
+    c->nrep = nrep;
     // observables, device layout dipole [nobs][3][ns], SU(N) [nobs][N*N][2][ns]
-    size_t per = s->sun ? (size_t)2 * N * N : 3;
+    size_t per = sun ? (size_t)2 * N * N : 3;
     std::vector<char> host(R * per * d->nobs * ns);
     for (int o = 0; o < d->nobs; o++)
         for (int i = 0; i < ns; i++)
             for (size_t k = 0; k < per; k++) {
                 double v = d->obs[((size_t)o * ns + i) * per + k];
                 size_t idx = ((size_t)o * per + k) * ns + i;
-                if (s->fp32) reinterpret_cast<float*>(host.data())[idx] = (float)v;
+                if (fp32) reinterpret_cast<float*>(host.data())[idx] = (float)v;
                 else reinterpret_cast<double*>(host.data())[idx] = v;
             }
-    if ((rc = dmalloc(s, &c->ops, host.size()))) return bad(rc);
-    if (cudaMemcpy(c->ops, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) return bad(fail(s, SGB_ERR_CUDA, "copy observables"));
-    if ((rc = dmalloc(s, (void**)&c->pairs, sizeof(int) * 2 * d->ncorr))) return bad(rc);
+    auto alloc = [&](void** p, size_t bytes) -> int {
+        if (cudaMalloc(p, bytes ? bytes : 16) != cudaSuccess) { *p = nullptr; return cfail(c, SGB_ERR_NOMEM, "device allocation failed"); }
+        return SGB_OK;
+    };
+    int rc;
+    if ((rc = alloc(&c->ops, host.size()))) return rc;
+    if (cudaMemcpy(c->ops, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) return cfail(c, SGB_ERR_CUDA, "copy observables");
+    if ((rc = alloc((void**)&c->pairs, sizeof(int) * 2 * d->ncorr))) return rc;
     cudaMemcpy(c->pairs, d->pairs, sizeof(int) * 2 * d->ncorr, cudaMemcpyHostToDevice);
-    size_t nA = (size_t)c->nomega * c->nobs * c->npos * c->ncell;  // complex elements
-    if ((rc = dmalloc(s, &c->A, 2 * R * nA))) return bad(rc);
-    if ((rc = dmalloc(s, &c->Ahat, 2 * R * nA))) return bad(rc);
+    size_t nA = (size_t)nrep * c->nomega * c->nobs * c->npos * c->ncell;  // complex elements
+    if ((rc = alloc(&c->A, 2 * R * nA))) return rc;
+    if ((rc = alloc(&c->Ahat, 2 * R * nA))) return rc;
     cudaMemset(c->A, 0, 2 * R * nA);
     c->plen = (size_t)c->nomega * c->ncell * c->npos * c->npos * c->ncorr;
-    if ((rc = dmalloc(s, (void**)&c->P, 16 * c->plen))) return bad(rc);
+    if ((rc = alloc((void**)&c->P, 16 * c->plen))) return rc;
     cudaMemset(c->P, 0, 16 * c->plen);
-    if ((rc = dmalloc(s, (void**)&c->g, sizeof(double) * c->nomega))) return bad(rc);
+    if ((rc = alloc((void**)&c->g, sizeof(double) * c->nomega))) return rc;
     // cuFFT plans: space FFT over (L3, L2, L1) for every snapshot row; time FFT along ω
-    const cufftType ty = s->fp32 ? CUFFT_C2C : CUFFT_Z2Z;
-    int n3[3] = {s->d.dims[2], s->d.dims[1], s->d.dims[0]};
+    const cufftType ty = fp32 ? CUFFT_C2C : CUFFT_Z2Z;
+    int n3[3] = {dims[2], dims[1], dims[0]};
     int batch_space = c->nsnaps * c->nobs * c->npos;
     if (cufftPlanMany(&c->plan_space, 3, n3, nullptr, 1, c->ncell, nullptr, 1, c->ncell, ty, batch_space) != CUFFT_SUCCESS)
-        return bad(fail(s, SGB_ERR_CUDA, "cufftPlanMany (space) failed"));
+        return cfail(c, SGB_ERR_CUDA, "cufftPlanMany (space) failed");
     c->have_space = true;
-    cufftSetStream(c->plan_space, s->stream);
+    cufftSetStream(c->plan_space, c->stream);
     if (c->nomega > 1) {
         int n1[1] = {c->nomega};
         int stride = c->nobs * c->npos * c->ncell;
         if (cufftPlanMany(&c->plan_time, 1, n1, n1, stride, 1, n1, stride, 1, ty, stride) != CUFFT_SUCCESS)
-            return bad(fail(s, SGB_ERR_CUDA, "cufftPlanMany (time) failed"));
+            return cfail(c, SGB_ERR_CUDA, "cufftPlanMany (time) failed");
         c->have_time = true;
-        cufftSetStream(c->plan_time, s->stream);
+        cufftSetStream(c->plan_time, c->stream);
     }
+    return SGB_OK;
+}
+
+static int corr_check_desc(const sgb_corr_desc* d) {
+    if (d->nobs < 1 || d->ncorr < 1 || !d->obs || !d->pairs) return fail(nullptr, SGB_ERR_ARG, "observables and correlation pairs are required");
+    if (d->n_all_omega < 1 || d->measperiod < 1) return fail(nullptr, SGB_ERR_ARG, "n_all_omega and measperiod must be positive");
+    if (d->n_all_omega > 1 && !(d->dt > 0)) return fail(nullptr, SGB_ERR_ARG, "Select positive dt");
+    if (d->calculate_errors) return fail(nullptr, SGB_ERR_ARG, "calculate_errors is not supported by this build of the accumulator");
+    for (int k = 0; k < 2 * d->ncorr; k++)
+        if (d->pairs[k] < 0 || d->pairs[k] >= d->nobs) return fail(nullptr, SGB_ERR_ARG, "correlation pair index out of range");
+    return SGB_OK;
+}
+
+int sgb_corr_create(sgb_system* s, const sgb_corr_desc* d, sgb_corr** out) {
+    if (!s || !d || !out) return fail(s, SGB_ERR_ARG, "null argument");
+    *out = nullptr;
+    int rc = corr_check_desc(d);
+    if (rc) { s->err = g_last_error; return rc; }
+    if ((rc = ensure_tables(s))) return rc;
+    sgb_corr* c = new sgb_corr();
+    c->sys = s;
+    c->stream = s->stream;
+    c->launches = &s->launches;
+    rc = corr_setup(c, d, s->fp32, s->sun, s->N, s->ns, s->d.natoms, s->d.dims, 1);
+    if (rc) { sgb_corr_destroy(c); return rc; }
+    *out = c;
+    return SGB_OK;
+}
+
+int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* d, sgb_corr** out) {
+    if (!b || !d || !out) return fail(nullptr, SGB_ERR_ARG, "null argument");
+    *out = nullptr;
+    int rc = corr_check_desc(d);
+    if (rc) { b->err = g_last_error; return rc; }
+    for (int r = 1; r < b->nrep; r++)
+        for (int k = 0; k < 3; k++)
+            if (b->dims[3 * r + k] != b->dims[k]) { b->err = "batched sampling needs replicas of equal size"; return SGB_ERR_ARG; }
+    if (!b->coup_set) { b->err = "couplings must be set first"; return SGB_ERR_STATE; }
+    const size_t R = b->fp32 ? 4 : 8;
+    auto lazy = [&](void** p, size_t bytes) -> int {
+        if (*p) return SGB_OK;
+        if (cudaMalloc(p, bytes) != cudaSuccess) { *p = nullptr; b->err = "device allocation failed"; return SGB_ERR_NOMEM; }
+        return SGB_OK;
+    };
+    if ((rc = lazy(&b->Sp, R * 3 * b->NS)) || (rc = lazy(&b->H, R * 9 * b->NS)) || (rc = lazy(&b->Sc, R * 3 * b->NS)) ||
+        (rc = lazy((void**)&b->racc, sizeof(double) * 3 * b->nrep)))
+        return rc;
+    sgb_corr* c = new sgb_corr();
+    c->batch = b;
+    c->stream = b->stream;
+    c->launches = &b->launches;
+    const int ns = b->off[1] - b->off[0];
+    rc = corr_setup(c, d, b->fp32, false, 0, ns, b->na, b->dims.data(), b->nrep);
+    if (rc) { b->err = c->err; sgb_corr_destroy(c); return rc; }
     *out = c;
     return SGB_OK;
 }
@@ -899,12 +744,18 @@ static void window_weights(int n, int window, std::vector<double>& g) {
 int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
     if (!c) return fail(nullptr, SGB_ERR_ARG, "null handle");
     sgb_system* s = c->sys;
+    sgb_batch* b = c->batch;
     if (window != 0 && window != 1) return cfail(c, SGB_ERR_ARG, "window must be 0 (:cosine) or 1 (:rectangular)");
     if (c->window >= 0 && c->window != window)
         return cfail(c, SGB_ERR_ARG, "all samples of one accumulator must use the same window");
-    if (!s->state_set) return cfail(c, SGB_ERR_STATE, "sgb_set_state must be called before add_sample");
-    int rc = ensure_tables(s);
-    if (rc) return rc;
+    int rc = SGB_OK;
+    if (s) {
+        if (!s->state_set) return cfail(c, SGB_ERR_STATE, "sgb_set_state must be called before add_sample");
+        if ((rc = ensure_tables(s))) return rc;
+    } else if (!b->state_set) {
+        return cfail(c, SGB_ERR_STATE, "replica states must be set before add_sample");
+    }
+    const bool fp32 = s ? s->fp32 : b->fp32;
     if (c->window < 0) {
         std::vector<double> g;
         window_weights(c->nomega, window, g);
@@ -914,10 +765,14 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
     }
     const int nsteps = c->measperiod * (c->nsnaps - 1);
     const double scale = 1.0 / std::sqrt((double)c->ncell);
-    if (c->profile) cudaEventRecord(c->ev[0], s->stream);
+    if (c->profile) cudaEventRecord(c->ev[0], c->stream);
     int64_t iters = 0;
     // 1. trajectory with fused observable snapshots (CorrelationSampling.jl:21-46)
-    if (s->fp32) {
+    if (b) {
+        rc = batch_corr_trajectory(c);
+        iters = c->prof_iters_last;
+        if (rc) return cfail(c, rc, batch_error(b));
+    } else if (fp32) {
         SnapArgs<float> sn{1, c->nobs, c->measperiod, 0, (const float*)c->ops, (float*)c->A, (float)scale};
         if (nsteps > 0) rc = run_midpoint<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true);
         else rc = run_midpoint<float>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
@@ -927,30 +782,40 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
         else rc = run_midpoint<double>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
     }
     if (rc) return rc;
-    if (c->profile) cudaEventRecord(c->ev[1], s->stream);
+    if (c->profile) cudaEventRecord(c->ev[1], c->stream);
+    const size_t rep_stride = (size_t)c->nomega * c->nobs * c->npos * c->ncell;  // complex elements
+    const size_t esz = fp32 ? 8 : 16;                                              // bytes per complex
     // 2. space FFT, A(q) = sum_r exp(+iqr) A(r) / sqrt(Ncell) (CorrelationSampling.jl:58-63)
-    cufftResult fr;
-    if (s->fp32) fr = cufftExecC2C(c->plan_space, (cufftComplex*)c->A, (cufftComplex*)c->A, CUFFT_INVERSE);
-    else fr = cufftExecZ2Z(c->plan_space, (cufftDoubleComplex*)c->A, (cufftDoubleComplex*)c->A, CUFFT_INVERSE);
-    if (fr != CUFFT_SUCCESS) return cfail(c, SGB_ERR_CUDA, "space FFT failed");
-    if (c->profile) cudaEventRecord(c->ev[2], s->stream);
+    for (int r = 0; r < c->nrep; r++) {
+        void* Ar = (char*)c->A + esz * rep_stride * r;
+        cufftResult fr = fp32 ? cufftExecC2C(c->plan_space, (cufftComplex*)Ar, (cufftComplex*)Ar, CUFFT_INVERSE)
+                              : cufftExecZ2Z(c->plan_space, (cufftDoubleComplex*)Ar, (cufftDoubleComplex*)Ar, CUFFT_INVERSE);
+        if (fr != CUFFT_SUCCESS) return cfail(c, SGB_ERR_CUDA, "space FFT failed");
+    }
+    if (c->profile) cudaEventRecord(c->ev[2], c->stream);
     // 3. time FFT, A(ω) = sum_t exp(-iωt) A(t), zero padded (CorrelationSampling.jl:65-69)
     const void* spec = c->A;
     if (c->have_time) {
-        if (s->fp32) fr = cufftExecC2C(c->plan_time, (cufftComplex*)c->A, (cufftComplex*)c->Ahat, CUFFT_FORWARD);
-        else fr = cufftExecZ2Z(c->plan_time, (cufftDoubleComplex*)c->A, (cufftDoubleComplex*)c->Ahat, CUFFT_FORWARD);
-        if (fr != CUFFT_SUCCESS) return cfail(c, SGB_ERR_CUDA, "time FFT failed");
+        for (int r = 0; r < c->nrep; r++) {
+            void* Ar = (char*)c->A + esz * rep_stride * r;
+            void* Hr = (char*)c->Ahat + esz * rep_stride * r;
+            cufftResult fr = fp32 ? cufftExecC2C(c->plan_time, (cufftComplex*)Ar, (cufftComplex*)Hr, CUFFT_FORWARD)
+                                  : cufftExecZ2Z(c->plan_time, (cufftDoubleComplex*)Ar, (cufftDoubleComplex*)Hr, CUFFT_FORWARD);
+            if (fr != CUFFT_SUCCESS) return cfail(c, SGB_ERR_CUDA, "time FFT failed");
+        }
         spec = c->Ahat;
     }
-    if (c->profile) cudaEventRecord(c->ev[3], s->stream);
-    // 4. accumulate conj(A_alpha,i) A_beta,j into the FP64 sum
-    rc = s->fp32 ? corr_launch_accum<float>((const float*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, c->nomega, s->stream)
-                 : corr_launch_accum<double>((const double*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, c->nomega, s->stream);
-    s->launches++;
+    if (c->profile) cudaEventRecord(c->ev[3], c->stream);
+    // 4. accumulate sum_r conj(A_alpha,i) A_beta,j into the FP64 sum
+    rc = fp32 ? corr_launch_accum<float>((const float*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, c->nomega,
+                                         c->nrep, rep_stride, c->stream)
+              : corr_launch_accum<double>((const double*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, c->nomega,
+                                          c->nrep, rep_stride, c->stream);
+    (*c->launches)++;
     if (rc) return cfail(c, SGB_ERR_CUDA, std::string("accumulate launch: ") + cudaGetErrorString(cudaGetLastError()));
-    c->nsamples += 1;
+    c->nsamples += c->nrep;
     if (c->profile) {
-        cudaEventRecord(c->ev[4], s->stream);
+        cudaEventRecord(c->ev[4], c->stream);
         if (cudaEventSynchronize(c->ev[4]) != cudaSuccess) return cfail(c, SGB_ERR_CUDA, "profiling event failed");
         for (int k = 0; k < 4; k++) {
             float ms = 0;
@@ -985,7 +850,7 @@ int sgb_corr_phase_times(sgb_corr* c, double* ms4, int64_t* n, int64_t* iters) {
 
 int sgb_corr_data(sgb_corr* c, double* data, double* M, int64_t* nsamples) {
     if (!c) return fail(nullptr, SGB_ERR_ARG, "null handle");
-    sgb_system* s = c->sys;
+    cudaStream_t stream = c->stream;
     if (nsamples) *nsamples = c->nsamples;
     if (M) return cfail(c, SGB_ERR_ARG, "calculate_errors is not supported by this build of the accumulator");
     if (!data) return SGB_OK;
@@ -1007,30 +872,28 @@ int sgb_corr_data(sgb_corr* c, double* data, double* M, int64_t* nsamples) {
     size_t chunk = std::max<size_t>(1, ((size_t)64 << 20) / ((size_t)16 * n));
     chunk = std::min(chunk, ld);
     double *tmp = nullptr, *outb = nullptr;
-    int rc = dmalloc(s, (void**)&tmp, 16 * chunk * n);
-    if (rc) return rc;
-    rc = dmalloc(s, (void**)&outb, 16 * chunk * n);
-    if (rc) { cudaFree(tmp); return rc; }
+    if (cudaMalloc((void**)&tmp, 16 * chunk * n) != cudaSuccess) return cfail(c, SGB_ERR_NOMEM, "device allocation failed");
+    if (cudaMalloc((void**)&outb, 16 * chunk * n) != cudaSuccess) { cudaFree(tmp); return cfail(c, SGB_ERR_NOMEM, "device allocation failed"); }
     cufftHandle plan;
     int n1[1] = {n};
     if (cufftPlanMany(&plan, 1, n1, nullptr, 1, n, nullptr, 1, n, CUFFT_Z2Z, (int)chunk) != CUFFT_SUCCESS) {
         cudaFree(tmp); cudaFree(outb);
         return cfail(c, SGB_ERR_CUDA, "cufftPlanMany (read-out) failed");
     }
-    cufftSetStream(plan, s->stream);
+    cufftSetStream(plan, stream);
     int status = SGB_OK;
     for (size_t col0 = 0; col0 < ld && status == SGB_OK; col0 += chunk) {
         int ncol = (int)std::min(chunk, ld - col0);
-        if (corr_launch_gather(c->P, ld, col0, ncol, n, inv, tmp, s->stream)) { status = SGB_ERR_CUDA; break; }
+        if (corr_launch_gather(c->P, ld, col0, ncol, n, inv, tmp, stream)) { status = SGB_ERR_CUDA; break; }
         if (cufftExecZ2Z(plan, (cufftDoubleComplex*)tmp, (cufftDoubleComplex*)tmp, CUFFT_INVERSE) != CUFFT_SUCCESS) { status = SGB_ERR_CUDA; break; }
-        if (corr_launch_window(tmp, ncol, n, c->g, s->stream)) { status = SGB_ERR_CUDA; break; }
+        if (corr_launch_window(tmp, ncol, n, c->g, stream)) { status = SGB_ERR_CUDA; break; }
         if (cufftExecZ2Z(plan, (cufftDoubleComplex*)tmp, (cufftDoubleComplex*)tmp, CUFFT_FORWARD) != CUFFT_SUCCESS) { status = SGB_ERR_CUDA; break; }
-        if (corr_launch_scatter(tmp, ncol, n, outb, s->stream)) { status = SGB_ERR_CUDA; break; }
-        s->launches += 3;
+        if (corr_launch_scatter(tmp, ncol, n, outb, stream)) { status = SGB_ERR_CUDA; break; }
+        (*c->launches) += 3;
         if (cudaMemcpy2DAsync(data + 2 * col0, 16 * ld, outb, 16 * (size_t)ncol, 16 * (size_t)ncol, n, cudaMemcpyDeviceToHost,
-                              s->stream) != cudaSuccess) { status = SGB_ERR_CUDA; break; }
+                              stream) != cudaSuccess) { status = SGB_ERR_CUDA; break; }
     }
-    cudaStreamSynchronize(s->stream);
+    cudaStreamSynchronize(stream);
     cufftDestroy(plan);
     cudaFree(tmp);
     cudaFree(outb);
@@ -1044,16 +907,15 @@ int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src) {
         return cfail(dst, SGB_ERR_ARG, "accumulators have different shapes");
     if (src->nsamples > 0 && dst->window >= 0 && src->window >= 0 && dst->window != src->window)
         return cfail(dst, SGB_ERR_ARG, "accumulators used different windows");
-    sgb_system* s = dst->sys;
-    if (src->sys != dst->sys) cudaStreamSynchronize(src->sys->stream);
-    if (corr_launch_add(dst->P, src->P, 2 * dst->plen, s->stream) != SGB_OK) return cfail(dst, SGB_ERR_CUDA, "merge launch");
-    s->launches++;
+    if (src->stream != dst->stream) cudaStreamSynchronize(src->stream);
+    if (corr_launch_add(dst->P, src->P, 2 * dst->plen, dst->stream) != SGB_OK) return cfail(dst, SGB_ERR_CUDA, "merge launch");
+    (*dst->launches)++;
     if (dst->window < 0 && src->window >= 0) {
         dst->window = src->window;
-        cudaMemcpyAsync(dst->g, src->g, sizeof(double) * dst->nomega, cudaMemcpyDeviceToDevice, s->stream);
+        cudaMemcpyAsync(dst->g, src->g, sizeof(double) * dst->nomega, cudaMemcpyDeviceToDevice, dst->stream);
     }
     dst->nsamples += src->nsamples;
-    cudaStreamSynchronize(s->stream);
+    cudaStreamSynchronize(dst->stream);
     return SGB_OK;
 }
 

@@ -1,34 +1,1004 @@
-// sgb_batch.cu -- replica batches and parallel tempering (ParallelTempering.jl:2-95).
-#include <cuda_runtime.h>
+// sgb_batch.cu -- replica batches: many independent dipole-mode systems (possibly of
+// different sizes) that share their couplings, advanced together by persistent kernels.
+//
+// Reference semantics:
+//   Langevin Heun per replica   src/Integrators.jl:313-332
+//   energy per replica           src/System/Interactions.jl:401-508
+//   replica_exchange!           src/MonteCarlo/ParallelTempering.jl:40-73
+//   step_ensemble!              src/MonteCarlo/ParallelTempering.jl:80-95
+//   midpoint per replica        src/Integrators.jl:379-413 (for batched add_sample!)
+//
+// Design: the replicas' states are concatenated in L2-resident SoA arrays and cut into
+// tiles of up to 256 sites of one replica. A persistent cooperative grid walks its tiles
+// between bounded grid barriers, so one barrier serves every replica and the latency of
+// a single small system is amortised over the batch. Per-replica reductions (energies,
+// midpoint convergence sums) are formed per tile in FP64. Parallel tempering keeps a
+// device-side ladder (replica at each temperature position) per group of equal-size
+// replicas, swaps temperatures on device, and step_ensemble! replays one captured CUDA
+// graph per exchange round.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
 #include <string>
-#include "sgb_internal.h"
+#include <vector>
+#include "sgb_device.cuh"
+#include "sgb_tables.h"
+#include "sgb_handles.h"
+#include "sgb_corr.h"
 
-struct sgb_batch {
-    std::string err;
+namespace {
+using namespace sgbdev;
+
+#define SGB_TILE 256
+#define SGB_MAXT 8
+
+template <class R>
+struct BatchArgs {
+    Model<R> M;
+    const int4* tiles;
+    int ntiles;
+    const int4* rd;     // (L1, L2, L3, ncell)
+    const int* roff;
+    int NS;
+    const R* kap;       // [na]
+    const R* h;         // [3][na] or nullptr
+    R* S;
+    R* P;
+    R* D1;
+    Ctrl* ctrl;
 };
 
+struct TileCtx {
+    int r, s, off;
+    int4 d;
+    SiteIdx ix;
+};
+
+__device__ __forceinline__ TileCtx tile_ctx(const int4* tiles, const int4* rd, const int* roff, int t) {
+    TileCtx c;
+    int4 tl = tiles[t];
+    c.r = tl.x;
+    c.s = tl.y + threadIdx.x;
+    c.d = rd[c.r];
+    c.off = roff[c.r];
+    c.ix = decompose(c.s, c.d.x, c.d.y, c.d.z);
+    return c;
+}
+
+__device__ __forceinline__ bool tile_has(const int4* tiles, int t) { return (int)threadIdx.x < tiles[t].z; }
+
+template <class R>
+__device__ __forceinline__ void site_field(const BatchArgs<R>& A, int a, R& hx, R& hy, R& hz) {
+    if (A.h) { hx = A.h[a]; hy = A.h[A.M.na + a]; hz = A.h[2 * A.M.na + a]; }
+    else { hx = 0; hy = 0; hz = 0; }
+}
+
+template <class R>
+__device__ __forceinline__ void batch_noise(uint64_t seed, int r, uint64_t step, int s, R scale, R& x, R& y, R& z) {
+    if (scale == (R)0) { x = 0; y = 0; z = 0; return; }
+    R g4[4];
+    sgb_normals4<R>(seed, (uint32_t)r, step, (uint32_t)s, 0u, g4);
+    x = g4[0] * scale; y = g4[1] * scale; z = g4[2] * scale;
+}
+
+// Heun over every replica (Integrators.jl:313-332); each replica uses its own kT.
+template <class R>
+__global__ void __launch_bounds__(SGB_TILE) k_batch_heun(BatchArgs<R> A, const double* kT, int nsteps, double dt,
+                                                         double lam, uint64_t seed, unsigned long long* counters) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tab<R> T = stage_tables<R>(A.M, smem);
+    const uint64_t step0 = *((volatile unsigned long long*)counters);
+    const int NS = A.NS;
+    for (int step = 0; step < nsteps; ++step) {
+        for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+            if (!tile_has(A.tiles, t)) continue;
+            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+            const R* X = A.S + c.off;
+            const R* Y = A.S + NS + c.off;
+            const R* Z = A.S + 2 * NS + c.off;
+            R sx = X[c.s], sy = Y[c.s], sz = Z[c.s];
+            const double kt = kT[c.r];
+            R scale = (lam == 0.0 || kt == 0.0) ? (R)0 : (R)sqrt(2 * dt * lam * kt);
+            R xx, xy, xz;
+            batch_noise<R>(seed, c.r, step0 + step, c.s, scale, xx, xy, xz);
+            R hx, hy, hz, gx, gy, gz, d0, d1, d2;
+            site_field(A, c.ix.a, hx, hy, hz);
+            grad_site_L<R, true>(A.M, T, c.ix, c.d.x, c.d.y, c.d.z, hx, hy, hz, sx, sy, sz, X, Y, Z, gx, gy, gz);
+            rhs_dipole<R>(sx, sy, sz, xx, xy, xz, gx, gy, gz, (R)dt, (R)lam, d0, d1, d2);
+            const int g = c.off + c.s;
+            A.D1[g] = d0; A.D1[NS + g] = d1; A.D1[2 * NS + g] = d2;
+            R px = sx + d0, py = sy + d1, pz = sz + d2;
+            normalize_dip<R>(px, py, pz, A.kap[c.ix.a]);
+            A.P[g] = px; A.P[NS + g] = py; A.P[2 * NS + g] = pz;
+        }
+        if (!sgb_grid_barrier(A.ctrl, gridDim.x)) return;
+        for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+            if (!tile_has(A.tiles, t)) continue;
+            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+            const int g = c.off + c.s;
+            const R* X = A.P + c.off;
+            const R* Y = A.P + NS + c.off;
+            const R* Z = A.P + 2 * NS + c.off;
+            R px = X[c.s], py = Y[c.s], pz = Z[c.s];
+            const double kt = kT[c.r];
+            R scale = (lam == 0.0 || kt == 0.0) ? (R)0 : (R)sqrt(2 * dt * lam * kt);
+            R xx, xy, xz;
+            batch_noise<R>(seed, c.r, step0 + step, c.s, scale, xx, xy, xz);
+            R hx, hy, hz, gx, gy, gz, e0, e1, e2;
+            site_field(A, c.ix.a, hx, hy, hz);
+            grad_site_L<R, true>(A.M, T, c.ix, c.d.x, c.d.y, c.d.z, hx, hy, hz, px, py, pz, X, Y, Z, gx, gy, gz);
+            rhs_dipole<R>(px, py, pz, xx, xy, xz, gx, gy, gz, (R)dt, (R)lam, e0, e1, e2);
+            R nx = A.S[g] + (A.D1[g] + e0) / 2;
+            R ny = A.S[NS + g] + (A.D1[NS + g] + e1) / 2;
+            R nz = A.S[2 * NS + g] + (A.D1[2 * NS + g] + e2) / 2;
+            normalize_dip<R>(nx, ny, nz, A.kap[c.ix.a]);
+            A.S[g] = nx; A.S[NS + g] = ny; A.S[2 * NS + g] = nz;
+        }
+        if (step + 1 < nsteps) {
+            if (!sgb_grid_barrier(A.ctrl, gridDim.x)) return;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *counters = step0 + nsteps;
+}
+
+// FP64 energy of every tile (one CTA per tile); k_batch_reduce sums a replica's tiles in
+// order, so energies are deterministic.
+template <class R>
+__global__ void __launch_bounds__(SGB_TILE) k_batch_energy(BatchArgs<R> A, double* Epart) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tab<R> T = stage_tables<R>(A.M, smem);
+    const int t = blockIdx.x;
+    double E = 0;
+    if (tile_has(A.tiles, t)) {
+        TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+        const int NS = A.NS;
+        const R* X = A.S + c.off;
+        const R* Y = A.S + NS + c.off;
+        const R* Z = A.S + 2 * NS + c.off;
+        double sx = X[c.s], sy = Y[c.s], sz = Z[c.s];
+        const int a = c.ix.a;
+        if (A.h) E += (double)A.h[a] * sx + (double)A.h[A.M.na + a] * sy + (double)A.h[2 * A.M.na + a] * sz;
+        if (A.M.dipole_mode) {
+            double cc[28];
+            for (int q = 0; q < 28; q++) cc[q] = (double)T.stev[28 * a + q];
+            double gx = 0, gy = 0, gz = 0;
+            E += classical_aniso<double>(cc, T.kmax[a], sx, sy, sz, gx, gy, gz);
+        }
+        for (int b = T.boff[a]; b < T.boff[a + 1]; b++) {
+            const DBond<R>& B = T.bonds[b];
+            if (!B.fwd) continue;
+            int x1 = sgb_wrap_any(c.ix.c1 + B.n[0], c.d.x);
+            int x2 = sgb_wrap_any(c.ix.c2 + B.n[1], c.d.y);
+            int x3 = sgb_wrap_any(c.ix.c3 + B.n[2], c.d.z);
+            int js = x1 + c.d.x * (x2 + c.d.y * (x3 + c.d.z * B.j));
+            double tx = X[js], ty = Y[js], tz = Z[js];
+            E += (double)B.scalar;
+            if (B.jkind == 0) E += (double)B.J[0] * (sx * tx + sy * ty + sz * tz);
+            else {
+                double jx = (double)B.J[0] * tx + (double)B.J[3] * ty + (double)B.J[6] * tz;
+                double jy = (double)B.J[1] * tx + (double)B.J[4] * ty + (double)B.J[7] * tz;
+                double jz = (double)B.J[2] * tx + (double)B.J[5] * ty + (double)B.J[8] * tz;
+                E += sx * jx + sy * jy + sz * jz;
+            }
+            if (A.M.dipole_mode && B.bqkind != 0) {
+                double Qi[5], Qj[5], acc = 0;
+                quad5<double>(sx, sy, sz, Qi);
+                quad5<double>(tx, ty, tz, Qj);
+                if (B.bqkind == 1) {
+                    for (int q = 0; q < 5; q++) acc += Qi[q] * (biquad_metric(q) * Qj[q]);
+                    acc *= (double)B.bq;
+                } else {
+                    const R* Bm = T.bq + 25 * B.bqidx;
+                    for (int q = 0; q < 5; q++)
+                        for (int p = 0; p < 5; p++) acc += Qi[q] * (double)Bm[q + 5 * p] * Qj[p];
+                }
+                E += acc;
+            }
+        }
+    }
+    double e = sgb_block_sum(E);
+    if (threadIdx.x == 0) Epart[t] = e;
+}
+
+__global__ void k_batch_reduce(const double* Epart, const int* tfirst, const int* tcount, double* E) {
+    const int r = blockIdx.x;
+    double v = 0;
+    for (int k = threadIdx.x; k < tcount[r]; k += blockDim.x) v += Epart[tfirst[r] + k];
+    double t = sgb_block_sum(v);
+    if (threadIdx.x == 0) E[r] = t;
+}
+
+// replica_exchange! (ParallelTempering.jl:40-73) on device. Positions are ladder slots
+// (group-major); ladder[p] is the replica currently at slot p, which holds kT[ladder[p]].
+// exch_start <= 0 takes the round from counters[1] (step_ensemble! alternation).
+__global__ void k_batch_exchange(int ngroups, const int* gstart, const int* gcount, int* ladder, double* kT,
+                                 const double* E, int exch_start, uint64_t seed, uint64_t round_arg,
+                                 unsigned long long* counters, const double* uniforms, long long* n_accept) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    uint64_t round = round_arg;
+    int start = exch_start;
+    if (exch_start <= 0) {
+        round = counters[1];
+        long long i = (long long)round + 1;   // 1-based round of step_ensemble!
+        start = (int)(i % 2) + 1;
+        counters[1] = round + 1;
+    }
+    for (int g = 0; g < ngroups; g++) {
+        const int p0 = gstart[g], n = gcount[g];
+        for (int rank = start - 1; rank + 1 < n; rank += 2) {
+            const int p = p0 + rank;
+            const int r1 = ladder[p], r2 = ladder[p + 1];
+            const double E1 = E[r1], E2 = E[r2];
+            const double kT1 = kT[r1], kT2 = kT[r2];
+            const double dS1 = E1 / kT1 - E2 / kT1;
+            const double dS2 = E2 / kT2 - E1 / kT2;
+            const double lnP = dS1 + dS2;
+            double u;
+            if (uniforms) u = uniforms[p];
+            else {
+                Philox4 c;
+                c.x = (uint32_t)p; c.y = (uint32_t)round; c.z = (uint32_t)(round >> 32); c.w = 0x7E4Cu;
+                Philox4 o = sgb_philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+                u = ((double)o.x + 0.5) * 2.3283064365386963e-10;
+            }
+            if (lnP >= 0 || u < exp(lnP)) {
+                kT[r1] = kT2;
+                kT[r2] = kT1;
+                ladder[p] = r2;
+                ladder[p + 1] = r1;
+                n_accept[p] += 1;
+            }
+        }
+    }
+}
+
+template <class R>
+__global__ void k_batch_noise(int ns, int rep, uint64_t seed, uint64_t step, double* out) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        R g4[4];
+        sgb_normals4<R>(seed, (uint32_t)rep, step, (uint32_t)s, 0u, g4);
+        out[3 * s] = (double)g4[0]; out[3 * s + 1] = (double)g4[1]; out[3 * s + 2] = (double)g4[2];
+    }
+}
+
+// ---- batched implicit midpoint with snapshots (batched add_sample!) ---------------------
+
+template <class R>
+struct MidArgs {
+    R* Sp;          // current iterate S'
+    R* H;           // 3 rotating buffers of midpoint spins, [3][3][NS]
+    R* Sc;          // candidate new state
+    double* racc;   // [3][nrep] FP64 convergence sums
+    int nrep;
+    double atol2;
+    int max_iters;
+};
+
+template <class R>
+struct BSnap {
+    int enabled, nobs, measperiod, t0, ncell, na;
+    const R* ops;        // [nobs][3][ns_rep] of one replica (identical replicas)
+    R* buf;              // replica r at buf + r*rep_stride (complex)
+    size_t rep_stride;   // complex elements between replicas
+    R scale;
+};
+
+template <class R>
+__device__ __forceinline__ void snap_write(const BSnap<R>& sn, int r, int t, int s, int nsr, R x, R y, R z) {
+    const int cell = s % sn.ncell, a = s / sn.ncell;
+    R* buf = sn.buf + 2 * (size_t)r * sn.rep_stride;
+    for (int o = 0; o < sn.nobs; o++) {
+        const R* op = sn.ops + (size_t)o * 3 * nsr;
+        R v = op[s] * x + op[nsr + s] * y + op[2 * nsr + s] * z;
+        size_t idx = (((size_t)t * sn.nobs + o) * sn.na + a) * sn.ncell + cell;
+        buf[2 * idx] = v * sn.scale;
+        buf[2 * idx + 1] = 0;
+    }
+}
+
+template <class R>
+__global__ void __launch_bounds__(SGB_TILE) k_batch_midpoint(BatchArgs<R> A, MidArgs<R> X, int nsteps, double dt,
+                                                             double lam, BSnap<R> sn) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tab<R> T = stage_tables<R>(A.M, smem);
+    const int NS = A.NS;
+    const bool leader = (blockIdx.x == 0 && threadIdx.x == 0);
+    bool act[SGB_MAXT];
+    int cur = 0;
+    // first midpoint spins normalize((S + S)/2) and the first snapshot
+    for (int k = 0; k < SGB_MAXT; k++) {
+        const int t = blockIdx.x + k * gridDim.x;
+        if (t >= A.ntiles || !tile_has(A.tiles, t)) continue;
+        TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+        const int g = c.off + c.s;
+        R sx = A.S[g], sy = A.S[NS + g], sz = A.S[2 * NS + g];
+        R hx = (sx + sx) / 2, hy = (sy + sy) / 2, hz = (sz + sz) / 2;
+        normalize_dip<R>(hx, hy, hz, A.kap[c.ix.a]);
+        X.H[g] = hx; X.H[NS + g] = hy; X.H[2 * NS + g] = hz;
+        if (sn.enabled) snap_write<R>(sn, c.r, sn.t0, c.s, c.d.w * A.M.na, sx, sy, sz);
+    }
+    if (leader) {
+        for (int q = 0; q < 3 * X.nrep; q++) X.racc[q] = 0.0;
+    }
+    if (!sgb_grid_barrier(A.ctrl, gridDim.x)) return;
+    long long itg = 0;
+    int done = 0;
+    for (int step = 0; step < nsteps; ++step) {
+        for (int k = 0; k < SGB_MAXT; k++) {
+            act[k] = true;
+            const int t = blockIdx.x + k * gridDim.x;
+            if (t >= A.ntiles || !tile_has(A.tiles, t)) continue;
+            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+            const int g = c.off + c.s;
+            X.Sp[g] = A.S[g]; X.Sp[NS + g] = A.S[NS + g]; X.Sp[2 * NS + g] = A.S[2 * NS + g];
+        }
+        bool all_done = false;
+        for (int it = 0; it < X.max_iters; ++it) {
+            const int nxt = (cur + 1) % 3, nst = (cur + 2) % 3;
+            const R* Hc = X.H + (size_t)cur * 3 * NS;
+            R* Hn = X.H + (size_t)nxt * 3 * NS;
+            R* Hs = X.H + (size_t)nst * 3 * NS;
+            const int slot = (int)(itg % 3);
+            for (int k = 0; k < SGB_MAXT; k++) {
+                const int t = blockIdx.x + k * gridDim.x;
+                if (t >= A.ntiles) break;
+                double acc = 0.0;
+                int r = A.tiles[t].x;
+                if (tile_has(A.tiles, t)) {
+                    TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+                    const int g = c.off + c.s;
+                    if (act[k]) {
+                        const R kap = A.kap[c.ix.a];
+                        R sx = A.S[g], sy = A.S[NS + g], sz = A.S[2 * NS + g];
+                        R qx = X.Sp[g], qy = X.Sp[NS + g], qz = X.Sp[2 * NS + g];
+                        R hx = (sx + qx) / 2, hy = (sy + qy) / 2, hz = (sz + qz) / 2;
+                        normalize_dip<R>(hx, hy, hz, kap);
+                        R fx, fy, fz, gx, gy, gz, dx, dy, dz;
+                        site_field(A, c.ix.a, fx, fy, fz);
+                        grad_site_L<R, true>(A.M, T, c.ix, c.d.x, c.d.y, c.d.z, fx, fy, fz, hx, hy, hz, Hc + c.off,
+                                             Hc + NS + c.off, Hc + 2 * NS + c.off, gx, gy, gz);
+                        rhs_dipole<R>(hx, hy, hz, (R)0, (R)0, (R)0, gx, gy, gz, (R)dt, (R)lam, dx, dy, dz);
+                        R nx = sx + dx, ny = sy + dy, nz = sz + dz;
+                        double ex = (double)(qx - nx), ey = (double)(qy - ny), ez = (double)(qz - nz);
+                        acc = ex * ex + ey * ey + ez * ez;
+                        X.Sp[g] = nx; X.Sp[NS + g] = ny; X.Sp[2 * NS + g] = nz;
+                        R mx = (sx + nx) / 2, my = (sy + ny) / 2, mz = (sz + nz) / 2;
+                        normalize_dip<R>(mx, my, mz, kap);
+                        Hn[g] = mx; Hn[NS + g] = my; Hn[2 * NS + g] = mz;
+                        R cx = nx, cy = ny, cz = nz;
+                        normalize_dip<R>(cx, cy, cz, kap);
+                        X.Sc[g] = cx; X.Sc[NS + g] = cy; X.Sc[2 * NS + g] = cz;
+                        R wx = (cx + cx) / 2, wy = (cy + cy) / 2, wz = (cz + cz) / 2;
+                        normalize_dip<R>(wx, wy, wz, kap);
+                        Hs[g] = wx; Hs[NS + g] = wy; Hs[2 * NS + g] = wz;
+                    } else {
+                        // converged replica: carry its next-step midpoint spins forward
+                        Hs[g] = Hn[g]; Hs[NS + g] = Hn[NS + g]; Hs[2 * NS + g] = Hn[2 * NS + g];
+                    }
+                }
+                double bsum = sgb_block_sum(acc);
+                if (threadIdx.x == 0 && act[k]) atomicAdd(&X.racc[slot * X.nrep + r], bsum);
+            }
+            if (leader) {
+                for (int q = 0; q < X.nrep; q++) X.racc[((slot + 1) % 3) * X.nrep + q] = 0.0;
+                A.ctrl->iters += 1;
+            }
+            if (!sgb_grid_barrier(A.ctrl, gridDim.x)) return;
+            itg++;
+            all_done = true;
+            for (int q = 0; q < X.nrep; q++)
+                if (!(X.racc[slot * X.nrep + q] <= X.atol2)) { all_done = false; break; }
+            for (int k = 0; k < SGB_MAXT; k++) {
+                const int t = blockIdx.x + k * gridDim.x;
+                if (t >= A.ntiles) break;
+                const int r = A.tiles[t].x;
+                if (act[k] && X.racc[slot * X.nrep + r] <= X.atol2) {
+                    act[k] = false;
+                    if (tile_has(A.tiles, t)) {
+                        const int g = A.roff[r] + A.tiles[t].y + threadIdx.x;
+                        A.S[g] = X.Sc[g]; A.S[NS + g] = X.Sc[NS + g]; A.S[2 * NS + g] = X.Sc[2 * NS + g];
+                    }
+                }
+            }
+            if (all_done) {
+                cur = nst;
+                break;
+            }
+            cur = nxt;
+        }
+        if (!all_done) {
+            if (leader) sgb_set_status(A.ctrl, SGB_ERR_NOCONVERGE);
+            break;
+        }
+        done = step + 1;
+        if (sn.enabled && (done % sn.measperiod) == 0) {
+            for (int k = 0; k < SGB_MAXT; k++) {
+                const int t = blockIdx.x + k * gridDim.x;
+                if (t >= A.ntiles || !tile_has(A.tiles, t)) continue;
+                TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+                const int g = c.off + c.s;
+                snap_write<R>(sn, c.r, sn.t0 + done / sn.measperiod, c.s, c.d.w * A.M.na, A.S[g], A.S[NS + g],
+                              A.S[2 * NS + g]);
+            }
+        }
+    }
+    if (leader) A.ctrl->steps_done = done;
+}
+
+// ---- host helpers --------------------------------------------------------------------------
+
+thread_local std::string g_batch_error;
+
+int bfail(sgb_batch* b, int code, const std::string& msg) {
+    if (b) b->err = msg;
+    g_batch_error = msg;
+    return code;
+}
+
+#define BCK(call)                                                                                 \
+    do {                                                                                          \
+        cudaError_t _e = (call);                                                                  \
+        if (_e != cudaSuccess) return bfail(b, SGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+int bmalloc(sgb_batch* b, void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return bfail(b, SGB_ERR_NOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+    }
+    return SGB_OK;
+}
+
+void bfree(void*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+size_t bsize(const sgb_batch* b) { return b->fp32 ? 4 : 8; }
+
+template <class R>
+Model<R>& bmodel(sgb_batch* b);
+template <>
+Model<float>& bmodel<float>(sgb_batch* b) { return b->mf; }
+template <>
+Model<double>& bmodel<double>(sgb_batch* b) { return b->md; }
+
+template <class R>
+BatchArgs<R> bargs(sgb_batch* b) {
+    BatchArgs<R> A;
+    A.M = bmodel<R>(b);
+    A.tiles = b->tiles;
+    A.ntiles = b->ntiles;
+    A.rd = b->rd;
+    A.roff = b->roff;
+    A.NS = b->NS;
+    A.kap = (const R*)b->kap;
+    A.h = b->has_field ? (const R*)b->h : nullptr;
+    A.S = (R*)b->S;
+    A.P = (R*)b->P;
+    A.D1 = (R*)b->D1;
+    A.ctrl = b->ctrl;
+    return A;
+}
+
+template <class K>
+int bcoop(sgb_batch* b, K kernel, int grid, size_t smem, void** args) {
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return bfail(b, SGB_ERR_CUDA, "cudaFuncSetAttribute failed");
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)kernel, dim3(grid), dim3(SGB_TILE), args, smem, b->stream);
+    b->launches++;
+    if (e != cudaSuccess) return bfail(b, SGB_ERR_CUDA, std::string("cooperative launch: ") + cudaGetErrorString(e));
+    return SGB_OK;
+}
+
+template <class K>
+int bgrid(sgb_batch* b, K kernel, size_t smem, int maxtiles_per_block, int* grid) {
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return bfail(b, SGB_ERR_CUDA, "cudaFuncSetAttribute failed");
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, SGB_TILE, smem) != cudaSuccess)
+        return bfail(b, SGB_ERR_CUDA, "occupancy query failed");
+    long long cap = (long long)bps * b->nsm;
+    long long g = std::min<long long>(cap, b->ntiles);
+    if (maxtiles_per_block > 0 && g * maxtiles_per_block < b->ntiles)
+        return bfail(b, SGB_ERR_ARG, "replica batch too large for one persistent launch of the midpoint kernel");
+    *grid = (int)std::max<long long>(1, g);
+    return SGB_OK;
+}
+
+int read_status(sgb_batch* b, Ctrl* out) {
+    BCK(cudaMemcpyAsync(out, b->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    return SGB_OK;
+}
+
+template <class R>
+int enqueue_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, int nsteps) {
+    BatchArgs<R> A = bargs<R>(b);
+    int grid = 0;
+    size_t smem = (size_t)b->tables_bytes;
+    int rc = bgrid(b, k_batch_heun<R>, smem, 0, &grid);
+    if (rc) return rc;
+    double* kT = b->kT;
+    unsigned long long* ctr = b->counters;
+    void* args[] = {&A, &kT, &nsteps, &dt, &damping, &seed, &ctr};
+    return bcoop(b, k_batch_heun<R>, grid, smem, args);
+}
+
+template <class R>
+int enqueue_energy(sgb_batch* b) {
+    BatchArgs<R> A = bargs<R>(b);
+    size_t smem = (size_t)b->tables_bytes;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_batch_energy<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return bfail(b, SGB_ERR_CUDA, "cudaFuncSetAttribute failed");
+    k_batch_energy<R><<<b->ntiles, SGB_TILE, smem, b->stream>>>(A, b->Epart);
+    k_batch_reduce<<<b->nrep, SGB_TILE, 0, b->stream>>>(b->Epart, b->tfirst_d, b->tcount_d, b->E);
+    b->launches += 2;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? SGB_OK : bfail(b, SGB_ERR_CUDA, std::string("energy launch: ") + cudaGetErrorString(e));
+}
+
+int enqueue_exchange(sgb_batch* b, int exch_start, uint64_t seed, uint64_t round, const double* uniforms_dev) {
+    k_batch_exchange<<<1, 32, 0, b->stream>>>(b->ngroups, b->gstart, b->gcount, b->ladder, b->kT, b->E, exch_start, seed,
+                                              round, b->counters, uniforms_dev, b->n_accept);
+    b->launches++;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? SGB_OK : bfail(b, SGB_ERR_CUDA, std::string("exchange launch: ") + cudaGetErrorString(e));
+}
+
+int ensure_bstage(sgb_batch* b, size_t bytes) {
+    if (b->stage_cap >= bytes) return SGB_OK;
+    if (b->stage) cudaFreeHost(b->stage);
+    b->stage = nullptr;
+    b->stage_cap = 0;
+    if (cudaMallocHost((void**)&b->stage, bytes) != cudaSuccess) return bfail(b, SGB_ERR_NOMEM, "pinned allocation failed");
+    b->stage_cap = bytes;
+    return SGB_OK;
+}
+
+int rebuild_groups(sgb_batch* b) {
+    // groups of equal dims, in order of first appearance; each sorted by kT ascending
+    std::vector<int> gid(b->nrep, -1);
+    std::vector<std::vector<int>> groups;
+    for (int r = 0; r < b->nrep; r++) {
+        if (gid[r] >= 0) continue;
+        groups.push_back({});
+        for (int q = r; q < b->nrep; q++)
+            if (gid[q] < 0 && b->dims[3 * q] == b->dims[3 * r] && b->dims[3 * q + 1] == b->dims[3 * r + 1] &&
+                b->dims[3 * q + 2] == b->dims[3 * r + 2]) {
+                gid[q] = (int)groups.size() - 1;
+                groups.back().push_back(q);
+            }
+    }
+    b->ladder_h.clear();
+    b->gstart_h.clear();
+    b->gcount_h.clear();
+    for (auto& g : groups) {
+        std::stable_sort(g.begin(), g.end(), [&](int x, int y) { return b->kT_h[x] < b->kT_h[y]; });
+        b->gstart_h.push_back((int)b->ladder_h.size());
+        b->gcount_h.push_back((int)g.size());
+        for (int r : g) b->ladder_h.push_back(r);
+    }
+    b->ngroups = (int)groups.size();
+    BCK(cudaMemcpy(b->ladder, b->ladder_h.data(), sizeof(int) * b->nrep, cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->gstart, b->gstart_h.data(), sizeof(int) * b->ngroups, cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->gcount, b->gcount_h.data(), sizeof(int) * b->ngroups, cudaMemcpyHostToDevice));
+    return SGB_OK;
+}
+
+}  // namespace
+
+// ---- batched add_sample! (called from sgb_corr_add_sample) ----------------------------------
+template <class R>
+static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
+    BatchArgs<R> A = bargs<R>(b);
+    MidArgs<R> X;
+    X.Sp = (R*)b->Sp;
+    X.H = (R*)b->H;
+    X.Sc = (R*)b->Sc;
+    X.racc = b->racc;
+    X.nrep = b->nrep;
+    double atol = c->tol * std::sqrt((double)(b->off[1] - b->off[0]));
+    X.atol2 = atol * atol;
+    X.max_iters = c->max_iters;
+    BSnap<R> sn;
+    sn.enabled = 1;
+    sn.nobs = c->nobs;
+    sn.measperiod = c->measperiod;
+    sn.t0 = 0;
+    sn.ncell = c->ncell;
+    sn.na = c->npos;
+    sn.ops = (const R*)c->ops;
+    sn.buf = (R*)c->A;
+    sn.rep_stride = (size_t)c->nomega * c->nobs * c->npos * c->ncell;
+    sn.scale = (R)(1.0 / std::sqrt((double)c->ncell));
+    int nsteps = c->measperiod * (c->nsnaps - 1);
+    int grid = 0;
+    size_t smem = (size_t)b->tables_bytes;
+    int rc = bgrid(b, k_batch_midpoint<R>, smem, SGB_MAXT, &grid);
+    if (rc) return rc;
+    BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
+    double dt = c->dt, lam = c->damping;
+    void* args[] = {&A, &X, &nsteps, &dt, &lam, &sn};
+    rc = bcoop(b, k_batch_midpoint<R>, grid, smem, args);
+    if (rc) return rc;
+    Ctrl st;
+    if ((rc = read_status(b, &st))) return rc;
+    c->prof_iters_last = st.iters;
+    if (st.status == SGB_ERR_NOCONVERGE)
+        return bfail(b, SGB_ERR_NOCONVERGE, "Spherical midpoint method failed to converge to tolerance " +
+                                                std::to_string(c->tol) + " after " + std::to_string(c->max_iters) +
+                                                " iterations.");
+    if (st.status != 0) return bfail(b, st.status, "batched midpoint kernel reported an error");
+    return SGB_OK;
+}
+
+int batch_corr_trajectory(sgb_corr* c) {
+    sgb_batch* b = c->batch;
+    return b->fp32 ? batch_trajectory<float>(c, b) : batch_trajectory<double>(c, b);
+}
+
+const char* batch_error(sgb_batch* b) { return b->err.c_str(); }
+
+// ---------------------------------------------------------------------------------------------
 extern "C" {
 
-static const char* k_unimpl = "replica batches are not available in this build";
+const char* sgb_batch_last_error(const sgb_batch* b) { return b ? b->err.c_str() : g_batch_error.c_str(); }
 
-int sgb_batch_create(const sgb_desc*, int32_t, const int32_t*, sgb_batch** out) {
-    if (out) *out = nullptr;
-    return SGB_ERR_STATE;
+void sgb_batch_destroy(sgb_batch* b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    bfree(b->tables); bfree(b->kap); bfree(b->h);
+    void* p;
+    p = b->rd; bfree(p); p = b->roff; bfree(p); p = b->kT; bfree(p); p = b->ladder; bfree(p);
+    p = b->gstart; bfree(p); p = b->gcount; bfree(p); p = b->tiles; bfree(p); p = b->tfirst_d; bfree(p);
+    p = b->tcount_d; bfree(p);
+    bfree(b->S); bfree(b->P); bfree(b->D1); bfree(b->Sp); bfree(b->H); bfree(b->Sc);
+    p = b->racc; bfree(p); p = b->ctrl; bfree(p); p = b->Epart; bfree(p); p = b->E; bfree(p);
+    p = b->counters; bfree(p); p = b->n_accept; bfree(p);
+    if (b->stage) cudaFreeHost(b->stage);
+    for (int i = 0; i < 8; i++) if (b->ev[i]) cudaEventDestroy(b->ev[i]);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
 }
-void sgb_batch_destroy(sgb_batch* b) { delete b; }
-const char* sgb_batch_last_error(const sgb_batch*) { return k_unimpl; }
-int64_t sgb_batch_nsites(const sgb_batch*, int32_t) { return 0; }
-int sgb_batch_set_couplings(sgb_batch*, const double*, const double*, const double*, const double*, const sgb_bond*, int32_t) { return SGB_ERR_STATE; }
-int sgb_batch_set_state(sgb_batch*, int32_t, const double*) { return SGB_ERR_STATE; }
-int sgb_batch_get_state(sgb_batch*, int32_t, double*) { return SGB_ERR_STATE; }
-int sgb_batch_set_kT(sgb_batch*, const double*) { return SGB_ERR_STATE; }
-int sgb_batch_get_kT(sgb_batch*, double*) { return SGB_ERR_STATE; }
-int sgb_batch_langevin(sgb_batch*, double, double, uint64_t, uint64_t, int32_t) { return SGB_ERR_STATE; }
-int sgb_batch_energy(sgb_batch*, double*) { return SGB_ERR_STATE; }
-int sgb_batch_exchange(sgb_batch*, int32_t, uint64_t, uint64_t, const double*, int64_t*) { return SGB_ERR_STATE; }
-int sgb_batch_step_ensemble(sgb_batch*, double, double, uint64_t, int32_t, int32_t, int64_t*) { return SGB_ERR_STATE; }
-int sgb_batch_event_record(sgb_batch*, int32_t) { return SGB_ERR_STATE; }
-int sgb_batch_event_elapsed(sgb_batch*, int32_t, int32_t, float*) { return SGB_ERR_STATE; }
-int64_t sgb_batch_kernel_launches(const sgb_batch*) { return 0; }
+
+int sgb_batch_create(const sgb_desc* d, int32_t nrep, const int32_t* dims, sgb_batch** out) {
+    if (!d || !dims || !out || nrep < 1) return bfail(nullptr, SGB_ERR_ARG, "invalid arguments");
+    *out = nullptr;
+    if (d->mode == SGB_MODE_SUN) return bfail(nullptr, SGB_ERR_ARG, "replica batches support the dipole modes");
+    if (d->natoms < 1 || d->natoms > SGB_MAX_SUBLAT) return bfail(nullptr, SGB_ERR_ARG, "natoms must be in [1, 64]");
+    if (d->precision != SGB_FP32 && d->precision != SGB_FP64) return bfail(nullptr, SGB_ERR_ARG, "bad precision");
+    sgb_batch* b = new sgb_batch();
+    b->proto = *d;
+    b->nrep = nrep;
+    b->na = d->natoms;
+    b->fp32 = d->precision == SGB_FP32;
+    b->dims.assign(dims, dims + 3 * nrep);
+    b->off.assign(nrep + 1, 0);
+    long long tot = 0;
+    for (int r = 0; r < nrep; r++) {
+        for (int k = 0; k < 3; k++)
+            if (dims[3 * r + k] < 1) { sgb_batch_destroy(b); return bfail(nullptr, SGB_ERR_ARG, "dims must be positive"); }
+        b->off[r] = (int)tot;
+        tot += (long long)dims[3 * r] * dims[3 * r + 1] * dims[3 * r + 2] * b->na;
+        if (tot > (1LL << 30)) { sgb_batch_destroy(b); return bfail(nullptr, SGB_ERR_ARG, "too many sites"); }
+    }
+    b->off[nrep] = (int)tot;
+    b->NS = (int)tot;
+    auto bad = [&](int code) { std::string m = b->err; sgb_batch_destroy(b); g_batch_error = m; return code; };
+    if (cudaSetDevice(d->device) != cudaSuccess) { bfail(b, SGB_ERR_CUDA, "cudaSetDevice failed"); return bad(SGB_ERR_CUDA); }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, d->device) != cudaSuccess) { bfail(b, SGB_ERR_CUDA, "no device"); return bad(SGB_ERR_CUDA); }
+    b->nsm = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) { bfail(b, SGB_ERR_CUDA, "stream"); return bad(SGB_ERR_CUDA); }
+    for (int i = 0; i < 8; i++) cudaEventCreate(&b->ev[i]);
+    // tiles: contiguous per replica
+    std::vector<int4> tiles;
+    b->tfirst.assign(nrep, 0);
+    b->tcount.assign(nrep, 0);
+    for (int r = 0; r < nrep; r++) {
+        int ns = b->off[r + 1] - b->off[r];
+        b->tfirst[r] = (int)tiles.size();
+        for (int s0 = 0; s0 < ns; s0 += SGB_TILE) tiles.push_back(make_int4(r, s0, std::min(SGB_TILE, ns - s0), 0));
+        b->tcount[r] = (int)tiles.size() - b->tfirst[r];
+    }
+    b->ntiles = (int)tiles.size();
+    std::vector<int4> rd(nrep);
+    for (int r = 0; r < nrep; r++) rd[r] = make_int4(dims[3 * r], dims[3 * r + 1], dims[3 * r + 2], dims[3 * r] * dims[3 * r + 1] * dims[3 * r + 2]);
+    size_t R = bsize(b);
+    int rc = SGB_OK;
+    rc |= bmalloc(b, (void**)&b->rd, sizeof(int4) * nrep);
+    rc |= bmalloc(b, (void**)&b->roff, sizeof(int) * (nrep + 1));
+    rc |= bmalloc(b, (void**)&b->kT, sizeof(double) * nrep);
+    rc |= bmalloc(b, (void**)&b->ladder, sizeof(int) * nrep);
+    rc |= bmalloc(b, (void**)&b->gstart, sizeof(int) * nrep);
+    rc |= bmalloc(b, (void**)&b->gcount, sizeof(int) * nrep);
+    rc |= bmalloc(b, (void**)&b->tiles, sizeof(int4) * b->ntiles);
+    rc |= bmalloc(b, (void**)&b->tfirst_d, sizeof(int) * nrep);
+    rc |= bmalloc(b, (void**)&b->tcount_d, sizeof(int) * nrep);
+    rc |= bmalloc(b, &b->S, R * 3 * b->NS);
+    rc |= bmalloc(b, &b->P, R * 3 * b->NS);
+    rc |= bmalloc(b, &b->D1, R * 3 * b->NS);
+    rc |= bmalloc(b, (void**)&b->ctrl, sizeof(Ctrl));
+    rc |= bmalloc(b, (void**)&b->Epart, sizeof(double) * b->ntiles);
+    rc |= bmalloc(b, (void**)&b->E, sizeof(double) * nrep);
+    rc |= bmalloc(b, (void**)&b->counters, sizeof(unsigned long long) * 2);
+    rc |= bmalloc(b, (void**)&b->n_accept, sizeof(long long) * nrep);
+    if (rc) return bad(SGB_ERR_NOMEM);
+    cudaMemcpy(b->rd, rd.data(), sizeof(int4) * nrep, cudaMemcpyHostToDevice);
+    cudaMemcpy(b->roff, b->off.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice);
+    cudaMemcpy(b->tiles, tiles.data(), sizeof(int4) * b->ntiles, cudaMemcpyHostToDevice);
+    cudaMemcpy(b->tfirst_d, b->tfirst.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice);
+    cudaMemcpy(b->tcount_d, b->tcount.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice);
+    cudaMemset(b->S, 0, R * 3 * b->NS);
+    cudaMemset(b->ctrl, 0, sizeof(Ctrl));
+    cudaMemset(b->counters, 0, sizeof(unsigned long long) * 2);
+    cudaMemset(b->n_accept, 0, sizeof(long long) * nrep);
+    b->kT_h.assign(nrep, 0.0);
+    cudaMemset(b->kT, 0, sizeof(double) * nrep);
+    if (rebuild_groups(b)) return bad(SGB_ERR_CUDA);
+    *out = b;
+    return SGB_OK;
+}
+
+int64_t sgb_batch_nsites(const sgb_batch* b, int32_t rep) {
+    if (!b || rep < 0 || rep >= b->nrep) return 0;
+    return b->off[rep + 1] - b->off[rep];
+}
+
+int sgb_batch_set_couplings(sgb_batch* b, const double* kappa, const double* g, const double* field,
+                            const double* onsite, const sgb_bond* bonds, int32_t nbonds) {
+    if (!b || !kappa || !g || (nbonds > 0 && !bonds) || nbonds < 0) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    const int na = b->na;
+    for (int k = 0; k < nbonds; k++) {
+        const sgb_bond& e = bonds[k];
+        if (e.i == e.j && e.n[0] == 0 && e.n[1] == 0 && e.n[2] == 0) return bfail(b, SGB_ERR_ARG, "Bond must connect different atoms.");
+        if (e.i < 0 || e.i >= na || e.j < 0 || e.j >= na) return bfail(b, SGB_ERR_ARG, "atom index out of range");
+        for (int r = 0; r < b->nrep; r++)
+            for (int q = 0; q < 3; q++)
+                if (std::abs(e.n[q]) > b->dims[3 * r + q])
+                    return bfail(b, SGB_ERR_ARG, "bond offset larger than a replica's supercell");
+    }
+    b->kappa_a.assign(kappa, kappa + na);
+    b->g_a.assign(g, g + 9 * na);
+    b->field_a.assign(3 * na, 0.0);
+    if (field) b->field_a.assign(field, field + 3 * na);
+    b->onsite.assign(28 * na, 0.0);
+    if (onsite) b->onsite.assign(onsite, onsite + 28 * na);
+    b->bonds.assign(bonds, bonds + nbonds);
+    std::vector<double> hh(3 * na, 0.0);
+    b->has_field = false;
+    for (int a = 0; a < na; a++)
+        for (int r = 0; r < 3; r++) {
+            const double* ga = b->g_a.data() + 9 * a;
+            const double* B = b->field_a.data() + 3 * a;
+            double v = ga[0 + 3 * r] * B[0] + ga[1 + 3 * r] * B[1] + ga[2 + 3 * r] * B[2];
+            hh[r * na + a] = v;
+            b->has_field |= v != 0.0;
+        }
+    size_t R = bsize(b);
+    bfree(b->kap);
+    bfree(b->h);
+    int rc = bmalloc(b, &b->kap, R * na);
+    rc |= bmalloc(b, &b->h, R * 3 * na);
+    if (rc) return SGB_ERR_NOMEM;
+    std::vector<unsigned char> buf;
+    bool any_bq = false;
+    std::string e;
+    if (b->fp32) {
+        std::vector<float> k(na), hf(3 * na);
+        for (int a = 0; a < na; a++) k[a] = (float)kappa[a];
+        for (int i = 0; i < 3 * na; i++) hf[i] = (float)hh[i];
+        BCK(cudaMemcpy(b->kap, k.data(), 4 * na, cudaMemcpyHostToDevice));
+        BCK(cudaMemcpy(b->h, hf.data(), 4 * 3 * na, cudaMemcpyHostToDevice));
+        e = sgbhost::pack_tables<float>(na, 0, false, nullptr, b->bonds, b->onsite, b->mf, buf, any_bq);
+    } else {
+        BCK(cudaMemcpy(b->kap, kappa, 8 * na, cudaMemcpyHostToDevice));
+        BCK(cudaMemcpy(b->h, hh.data(), 8 * 3 * na, cudaMemcpyHostToDevice));
+        e = sgbhost::pack_tables<double>(na, 0, false, nullptr, b->bonds, b->onsite, b->md, buf, any_bq);
+    }
+    if (!e.empty()) return bfail(b, SGB_ERR_ARG, e);
+    bfree(b->tables);
+    if ((rc = bmalloc(b, &b->tables, buf.size()))) return rc;
+    BCK(cudaMemcpy(b->tables, buf.data(), buf.size(), cudaMemcpyHostToDevice));
+    b->tables_bytes = (int)buf.size();
+    for (Model<float>* m : {&b->mf}) { m->tables = (const unsigned char*)b->tables; m->dipole_mode = 1; m->na = na; }
+    for (Model<double>* m : {&b->md}) { m->tables = (const unsigned char*)b->tables; m->dipole_mode = 1; m->na = na; }
+    if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+    b->coup_set = true;
+    return SGB_OK;
+}
+
+int sgb_batch_set_state(sgb_batch* b, int32_t rep, const double* dip) {
+    if (!b || !dip || rep < 0 || rep >= b->nrep) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    const int ns = b->off[rep + 1] - b->off[rep], NS = b->NS, o = b->off[rep];
+    size_t R = bsize(b);
+    int rc = ensure_bstage(b, R * 3 * ns);
+    if (rc) return rc;
+    for (int c = 0; c < 3; c++) {
+        for (int i = 0; i < ns; i++) {
+            if (b->fp32) reinterpret_cast<float*>(b->stage)[i] = (float)dip[3 * (size_t)i + c];
+            else reinterpret_cast<double*>(b->stage)[i] = dip[3 * (size_t)i + c];
+        }
+        BCK(cudaMemcpyAsync((char*)b->S + R * ((size_t)c * NS + o), b->stage, R * ns, cudaMemcpyHostToDevice, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+    }
+    b->state_set = true;
+    return SGB_OK;
+}
+
+int sgb_batch_get_state(sgb_batch* b, int32_t rep, double* dip) {
+    if (!b || !dip || rep < 0 || rep >= b->nrep) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    const int ns = b->off[rep + 1] - b->off[rep], NS = b->NS, o = b->off[rep];
+    size_t R = bsize(b);
+    int rc = ensure_bstage(b, R * 3 * ns);
+    if (rc) return rc;
+    for (int c = 0; c < 3; c++) {
+        BCK(cudaMemcpyAsync(b->stage, (char*)b->S + R * ((size_t)c * NS + o), R * ns, cudaMemcpyDeviceToHost, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+        for (int i = 0; i < ns; i++)
+            dip[3 * (size_t)i + c] = b->fp32 ? (double)reinterpret_cast<float*>(b->stage)[i] : reinterpret_cast<double*>(b->stage)[i];
+    }
+    return SGB_OK;
+}
+
+int sgb_batch_set_kT(sgb_batch* b, const double* kT) {
+    if (!b || !kT) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    for (int r = 0; r < b->nrep; r++)
+        if (!(kT[r] >= 0)) return bfail(b, SGB_ERR_ARG, "Select nonnegative kT");
+    b->kT_h.assign(kT, kT + b->nrep);
+    BCK(cudaMemcpy(b->kT, kT, sizeof(double) * b->nrep, cudaMemcpyHostToDevice));
+    return rebuild_groups(b);
+}
+
+int sgb_batch_get_kT(sgb_batch* b, double* kT) {
+    if (!b || !kT) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    BCK(cudaMemcpyAsync(kT, b->kT, sizeof(double) * b->nrep, cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    return SGB_OK;
+}
+
+int sgb_batch_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, uint64_t step0, int32_t nsteps) {
+    if (!b) return bfail(b, SGB_ERR_ARG, "null handle");
+    if (damping == 0.0) return bfail(b, SGB_ERR_ARG, "Use ImplicitMidpoint instead for energy-conserving dynamics");
+    if (!(dt > 0)) return bfail(b, SGB_ERR_ARG, "Select positive dt");
+    if (damping < 0) return bfail(b, SGB_ERR_ARG, "Select positive damping");
+    if (!b->coup_set || !b->state_set) return bfail(b, SGB_ERR_STATE, "couplings and states must be set first");
+    if (nsteps <= 0) return nsteps == 0 ? SGB_OK : bfail(b, SGB_ERR_ARG, "nsteps must be nonnegative");
+    unsigned long long s0 = step0;
+    BCK(cudaMemcpyAsync(b->counters, &s0, sizeof(s0), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
+    int rc = b->fp32 ? enqueue_langevin<float>(b, dt, damping, seed, nsteps) : enqueue_langevin<double>(b, dt, damping, seed, nsteps);
+    if (rc) return rc;
+    Ctrl st;
+    if ((rc = read_status(b, &st))) return rc;
+    if (st.status != 0) return bfail(b, st.status, "batched Langevin kernel reported an error");
+    return SGB_OK;
+}
+
+int sgb_batch_langevin_noise(sgb_batch* b, int32_t rep, uint64_t seed, uint64_t step, double* out) {
+    if (!b || !out || rep < 0 || rep >= b->nrep) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    const int ns = b->off[rep + 1] - b->off[rep];
+    double* d = nullptr;
+    if (bmalloc(b, (void**)&d, sizeof(double) * 3 * ns)) return SGB_ERR_NOMEM;
+    int grid = std::min(4096, (ns + 255) / 256);
+    if (b->fp32) k_batch_noise<float><<<grid, 256, 0, b->stream>>>(ns, rep, seed, step, d);
+    else k_batch_noise<double><<<grid, 256, 0, b->stream>>>(ns, rep, seed, step, d);
+    b->launches++;
+    cudaError_t e = cudaMemcpyAsync(out, d, sizeof(double) * 3 * ns, cudaMemcpyDeviceToHost, b->stream);
+    cudaStreamSynchronize(b->stream);
+    cudaFree(d);
+    return e == cudaSuccess ? SGB_OK : bfail(b, SGB_ERR_CUDA, "noise export failed");
+}
+
+int sgb_batch_energy(sgb_batch* b, double* E) {
+    if (!b || !E) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    if (!b->coup_set) return bfail(b, SGB_ERR_STATE, "couplings must be set first");
+    int rc = b->fp32 ? enqueue_energy<float>(b) : enqueue_energy<double>(b);
+    if (rc) return rc;
+    BCK(cudaMemcpyAsync(E, b->E, sizeof(double) * b->nrep, cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    return SGB_OK;
+}
+
+int sgb_batch_exchange(sgb_batch* b, int32_t exch_start, uint64_t seed, uint64_t round, const double* uniforms,
+                       int64_t* n_accept) {
+    if (!b || (exch_start != 1 && exch_start != 2)) return bfail(b, SGB_ERR_ARG, "exch_start must be 1 or 2");
+    if (!b->coup_set) return bfail(b, SGB_ERR_STATE, "couplings must be set first");
+    int rc = b->fp32 ? enqueue_energy<float>(b) : enqueue_energy<double>(b);
+    if (rc) return rc;
+    double* u = nullptr;
+    if (uniforms) {
+        if (bmalloc(b, (void**)&u, sizeof(double) * b->nrep)) return SGB_ERR_NOMEM;
+        BCK(cudaMemcpyAsync(u, uniforms, sizeof(double) * b->nrep, cudaMemcpyHostToDevice, b->stream));
+    }
+    rc = enqueue_exchange(b, exch_start, seed, round, u);
+    cudaStreamSynchronize(b->stream);
+    if (u) cudaFree(u);
+    if (rc) return rc;
+    if (n_accept) {
+        std::vector<long long> na(b->nrep);
+        BCK(cudaMemcpy(na.data(), b->n_accept, sizeof(long long) * b->nrep, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < b->nrep; i++) n_accept[i] = na[i];
+    }
+    return SGB_OK;
+}
+
+int sgb_batch_step_ensemble(sgb_batch* b, double dt, double damping, uint64_t seed, int32_t nsteps, int32_t exch_interval,
+                            int64_t* n_accept) {
+    if (!b || exch_interval < 1 || nsteps < 0) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    if (damping <= 0 || !(dt > 0)) return bfail(b, SGB_ERR_ARG, "Select positive dt and damping");
+    if (!b->coup_set || !b->state_set) return bfail(b, SGB_ERR_STATE, "couplings and states must be set first");
+    const int n_exch = (nsteps + exch_interval - 1) / exch_interval;
+    int rc = SGB_OK;
+    BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
+    BCK(cudaMemsetAsync(b->counters + 1, 0, sizeof(unsigned long long), b->stream));
+    const bool reuse = b->graph && b->graph_interval == exch_interval && b->graph_dt == dt && b->graph_damping == damping &&
+                       b->graph_seed == seed;
+    if (!reuse) {
+        if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+        // capture one round: exch_interval Langevin steps, energies, one exchange
+        cudaGraph_t g = nullptr;
+        bool captured = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (captured) {
+            rc = b->fp32 ? enqueue_langevin<float>(b, dt, damping, seed, exch_interval)
+                         : enqueue_langevin<double>(b, dt, damping, seed, exch_interval);
+            if (!rc) rc = b->fp32 ? enqueue_energy<float>(b) : enqueue_energy<double>(b);
+            if (!rc) rc = enqueue_exchange(b, 0, seed, 0, nullptr);
+            cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+            if (rc || e != cudaSuccess || !g || cudaGraphInstantiate(&b->graph, g, 0) != cudaSuccess) {
+                b->graph = nullptr;
+                cudaGetLastError();
+            }
+            if (g) cudaGraphDestroy(g);
+        }
+        b->graph_interval = exch_interval;
+        b->graph_dt = dt;
+        b->graph_damping = damping;
+        b->graph_seed = seed;
+    }
+    for (int i = 0; i < n_exch; i++) {
+        if (b->graph) {
+            if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) return bfail(b, SGB_ERR_CUDA, "cudaGraphLaunch failed");
+            b->launches += 4;
+        } else {
+            rc = b->fp32 ? enqueue_langevin<float>(b, dt, damping, seed, exch_interval)
+                         : enqueue_langevin<double>(b, dt, damping, seed, exch_interval);
+            if (!rc) rc = b->fp32 ? enqueue_energy<float>(b) : enqueue_energy<double>(b);
+            if (!rc) rc = enqueue_exchange(b, 0, seed, 0, nullptr);
+            if (rc) return rc;
+        }
+    }
+    Ctrl st;
+    if ((rc = read_status(b, &st))) return rc;
+    if (st.status != 0) return bfail(b, st.status, "step_ensemble kernel reported an error");
+    if (n_accept) {
+        std::vector<long long> na(b->nrep);
+        BCK(cudaMemcpy(na.data(), b->n_accept, sizeof(long long) * b->nrep, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < b->nrep; i++) n_accept[i] = na[i];
+    }
+    return SGB_OK;
+}
+
+int sgb_batch_graph_active(const sgb_batch* b) { return b && b->graph ? 1 : 0; }
+
+int sgb_batch_event_record(sgb_batch* b, int32_t slot) {
+    if (!b || slot < 0 || slot >= 8) return bfail(b, SGB_ERR_ARG, "bad event slot");
+    BCK(cudaEventRecord(b->ev[slot], b->stream));
+    return SGB_OK;
+}
+
+int sgb_batch_event_elapsed(sgb_batch* b, int32_t a, int32_t c, float* ms) {
+    if (!b || !ms || a < 0 || a >= 8 || c < 0 || c >= 8) return bfail(b, SGB_ERR_ARG, "bad event slot");
+    BCK(cudaEventSynchronize(b->ev[c]));
+    BCK(cudaEventElapsedTime(ms, b->ev[a], b->ev[c]));
+    return SGB_OK;
+}
+
+int64_t sgb_batch_kernel_launches(const sgb_batch* b) { return b ? b->launches : 0; }
 
 }  // extern "C"

@@ -24,28 +24,31 @@ namespace {
 template <class R> struct C2 { R x, y; };
 
 // One CTA handles one ω and QT consecutive wave vectors: it stages the QT x nobs x npos
-// complex spectra in shared memory and then streams the contiguous QT*B accumulator
-// entries (B = ncorr*npos*npos), coalesced, with streaming cache hints.
+// complex spectra of every replica in shared memory and then streams the contiguous
+// QT*B accumulator entries (B = ncorr*npos*npos), coalesced, with streaming cache hints.
+// With nrep replicas the products of all of them are summed before the single FP64
+// read-modify-write, so the accumulator traffic per sample falls as 1/nrep.
 template <class R, int QT>
 __global__ void __launch_bounds__(256) k_corr_accum(const R* __restrict__ A, double* __restrict__ P,
                                                   const int* __restrict__ pairs, int ncorr, int nobs, int npos,
-                                                  int ncell, int nomega) {
+                                                  int ncell, int nomega, int nrep, size_t rep_stride) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    C2<R>* As = reinterpret_cast<C2<R>*>(smem_raw);          // [nobs*npos][QT]
-    int* pr = reinterpret_cast<int*>(As + (size_t)nobs * npos * QT);
+    const int nrow = nobs * npos;
+    C2<R>* As = reinterpret_cast<C2<R>*>(smem_raw);          // [nrep][nrow][QT]
+    int* pr = reinterpret_cast<int*>(As + (size_t)nrep * nrow * QT);
     const int w = blockIdx.y;
     const int q0 = blockIdx.x * QT;
     const int nq = min(QT, ncell - q0);
-    const int nrow = nobs * npos;
-    for (int e = threadIdx.x; e < nrow * QT; e += blockDim.x) {
-        int row = e / QT, ql = e % QT;
+    for (int e = threadIdx.x; e < nrep * nrow * QT; e += blockDim.x) {
+        int r = e / (nrow * QT), rem = e - r * nrow * QT;
+        int row = rem / QT, ql = rem % QT;
         C2<R> v = {0, 0};
         if (ql < nq) {
-            size_t idx = ((size_t)w * nrow + row) * ncell + q0 + ql;
+            size_t idx = (size_t)r * rep_stride + ((size_t)w * nrow + row) * ncell + q0 + ql;
             v.x = A[2 * idx];
             v.y = A[2 * idx + 1];
         }
-        As[row * QT + ql] = v;
+        As[e] = v;
     }
     for (int e = threadIdx.x; e < 2 * ncorr; e += blockDim.x) pr[e] = pairs[e];
     __syncthreads();
@@ -70,11 +73,18 @@ __global__ void __launch_bounds__(256) k_corr_accum(const R* __restrict__ A, dou
             int c = r % ncorr;
             int t = r / ncorr;
             int i = t % npos, j = t / npos;
-            C2<R> a = As[(pr[2 * c] * npos + i) * QT + ql];
-            C2<R> b = As[(pr[2 * c + 1] * npos + j) * QT + ql];
-            // conj(a) * b
-            acc[u].x += (double)(a.x * b.x + a.y * b.y);
-            acc[u].y += (double)(a.x * b.y - a.y * b.x);
+            const int ia = (pr[2 * c] * npos + i) * QT + ql;
+            const int ib = (pr[2 * c + 1] * npos + j) * QT + ql;
+            R sre = 0, sim = 0;
+            for (int rr = 0; rr < nrep; rr++) {
+                C2<R> a = As[rr * nrow * QT + ia];
+                C2<R> b = As[rr * nrow * QT + ib];
+                // conj(a) * b
+                sre += a.x * b.x + a.y * b.y;
+                sim += a.x * b.y - a.y * b.x;
+            }
+            acc[u].x += (double)sre;
+            acc[u].y += (double)sim;
             __stcs(out + e, acc[u]);
         }
     }
@@ -128,15 +138,16 @@ int grid_for(size_t n) {
 
 template <class R>
 int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
-                      cudaStream_t st) {
+                      int nrep, size_t rep_stride, cudaStream_t st) {
     constexpr int QT = 32;
-    size_t smem = (size_t)nobs * npos * QT * sizeof(C2<R>) + 2 * ncorr * sizeof(int) + 16;
+    size_t smem = (size_t)nrep * nobs * npos * QT * sizeof(C2<R>) + 2 * ncorr * sizeof(int) + 16;
+    if (smem > 200 * 1024) return SGB_ERR_ARG;
     if (smem > 48 * 1024) {
         if (cudaFuncSetAttribute(k_corr_accum<R, QT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return SGB_ERR_CUDA;
     }
     dim3 grid((ncell + QT - 1) / QT, nomega);
-    k_corr_accum<R, QT><<<grid, 256, smem, st>>>(A, P, pairs, ncorr, nobs, npos, ncell, nomega);
+    k_corr_accum<R, QT><<<grid, 256, smem, st>>>(A, P, pairs, ncorr, nobs, npos, ncell, nomega, nrep, rep_stride);
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
@@ -162,5 +173,5 @@ int corr_launch_add(double* dst, const double* src, size_t n, cudaStream_t st) {
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
-template int corr_launch_accum<float>(const float*, double*, const int*, int, int, int, int, int, cudaStream_t);
-template int corr_launch_accum<double>(const double*, double*, const int*, int, int, int, int, int, cudaStream_t);
+template int corr_launch_accum<float>(const float*, double*, const int*, int, int, int, int, int, int, size_t, cudaStream_t);
+template int corr_launch_accum<double>(const double*, double*, const int*, int, int, int, int, int, int, size_t, cudaStream_t);

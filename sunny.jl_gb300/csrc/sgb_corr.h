@@ -6,7 +6,7 @@
 
 template <class R>
 int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
-                      cudaStream_t st);
+                      int nrep, size_t rep_stride, cudaStream_t st);
 int corr_launch_gather(const double* P, size_t ld, size_t col0, int ncol, int n, double scale, double* tmp, cudaStream_t st);
 int corr_launch_window(double* tmp, int ncol, int n, const double* g, cudaStream_t st);
 int corr_launch_scatter(const double* tmp, int ncol, int n, double* out, cudaStream_t st);

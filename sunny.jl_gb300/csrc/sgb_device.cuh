@@ -135,17 +135,16 @@ __device__ __forceinline__ SiteIdx decompose(int s, int L1, int L2, int L3) {
     return r;
 }
 
-// dE/dS at one site in gather form. X/Y/Zc are the SoA spins seen by neighbours.
-template <class R>
-__device__ inline void grad_site(const Model<R>& M, const Tab<R>& T, int site, const SiteIdx& ix,
-                                 R sx, R sy, R sz, const R* X, const R* Y, const R* Zc,
-                                 R& gx, R& gy, R& gz) {
-    gx = 0; gy = 0; gz = 0;
-    if (M.h) {
-        gx = __ldg(M.h + site);
-        gy = __ldg(M.h + M.ns + site);
-        gz = __ldg(M.h + 2 * M.ns + site);
-    }
+// dE/dS at one site in gather form. X/Y/Zc are the SoA spins seen by neighbours (already
+// offset to the replica's first site); (L1, L2, L3) are the replica's dims. ANYWRAP
+// selects the wrap for raw bond offsets |n| <= L (replica batches) instead of offsets
+// pre-reduced into [0, L) (single systems). h/kap are per-site (single system) or per
+// sublattice (batch).
+template <class R, bool ANYWRAP>
+__device__ inline void grad_site_L(const Model<R>& M, const Tab<R>& T, const SiteIdx& ix, int L1, int L2, int L3,
+                                   R hx, R hy, R hz, R sx, R sy, R sz, const R* X, const R* Y, const R* Zc,
+                                   R& gx, R& gy, R& gz) {
+    gx = hx; gy = hy; gz = hz;
     const int a = ix.a;
     if (M.dipole_mode) {
         int km = T.kmax[a];
@@ -160,10 +159,17 @@ __device__ inline void grad_site(const Model<R>& M, const Tab<R>& T, int site, c
         for (int k = 0; k < SGB_GATHER; k++) {
             if (b + k < b1) {
                 const DBond<R>& B = T.bonds[b + k];
-                int x1 = sgb_wrap_pos(ix.c1 + B.n[0], M.L1);
-                int x2 = sgb_wrap_pos(ix.c2 + B.n[1], M.L2);
-                int x3 = sgb_wrap_pos(ix.c3 + B.n[2], M.L3);
-                int js = x1 + M.L1 * (x2 + M.L2 * (x3 + M.L3 * B.j));
+                int x1, x2, x3;
+                if (ANYWRAP) {
+                    x1 = sgb_wrap_any(ix.c1 + B.n[0], L1);
+                    x2 = sgb_wrap_any(ix.c2 + B.n[1], L2);
+                    x3 = sgb_wrap_any(ix.c3 + B.n[2], L3);
+                } else {
+                    x1 = sgb_wrap_pos(ix.c1 + B.n[0], L1);
+                    x2 = sgb_wrap_pos(ix.c2 + B.n[1], L2);
+                    x3 = sgb_wrap_pos(ix.c3 + B.n[2], L3);
+                }
+                int js = x1 + L1 * (x2 + L2 * (x3 + L3 * B.j));
                 tx[k] = sgb_ld(X + js); ty[k] = sgb_ld(Y + js); tz[k] = sgb_ld(Zc + js);
             }
         }
@@ -199,6 +205,20 @@ __device__ inline void grad_site(const Model<R>& M, const Tab<R>& T, int site, c
             }
         }
     }
+}
+
+// Single-system form: per-site Zeeman field from M.h, offsets pre-reduced mod dims.
+template <class R>
+__device__ inline void grad_site(const Model<R>& M, const Tab<R>& T, int site, const SiteIdx& ix,
+                                 R sx, R sy, R sz, const R* X, const R* Y, const R* Zc,
+                                 R& gx, R& gy, R& gz) {
+    R hx = 0, hy = 0, hz = 0;
+    if (M.h) {
+        hx = __ldg(M.h + site);
+        hy = __ldg(M.h + M.ns + site);
+        hz = __ldg(M.h + 2 * M.ns + site);
+    }
+    grad_site_L<R, false>(M, T, ix, M.L1, M.L2, M.L3, hx, hy, hz, sx, sy, sz, X, Y, Zc, gx, gy, gz);
 }
 
 // Integrators.jl:266-275 rhs_dipole!

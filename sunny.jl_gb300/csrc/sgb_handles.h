@@ -1,0 +1,142 @@
+// sgb_handles.h -- definitions of the opaque C-ABI handles (internal).
+#pragma once
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <string>
+#include <vector>
+#include "sgb_internal.h"
+
+
+struct sgb_system {
+    sgb_desc d{};
+    int ns = 0, ncell = 0, N = 0;
+    bool fp32 = false;
+    bool sun = false;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8] = {};
+    std::string err;
+    long long launches = 0;
+    int nsm = 0;
+    // host copies of the model
+    std::vector<double> kappa_h, g_h, field_h, onsite_h;
+    std::vector<sgb_bond> bonds_h;
+    bool sites_set = false, bonds_set = false, state_set = false;
+    bool has_field = false, has_biquad = false;
+    bool tables_dirty = true;
+    // device data (element type R = float or double)
+    void* kappa = nullptr;   // [ns]
+    void* h = nullptr;       // [3][ns]
+    void* tables = nullptr;
+    int tables_bytes = 0;
+    Model<float> mf{};
+    Model<double> md{};
+    // state buffers
+    void* S = nullptr;   // dipole: spins [3][ns]; SU(N): dipoles [3][ns]
+    void* P = nullptr;   // [3][ns]
+    void* H = nullptr;   // [3][3][ns]
+    void* Z = nullptr;   // SU(N) [2N][ns]
+    void* Q = nullptr;   // SU(N) [5][ns]
+    void* QP = nullptr;  // SU(N) [5][ns]
+    void* QH = nullptr;  // SU(N) [3][5][ns]
+    Ctrl* ctrl = nullptr;
+    double* partials = nullptr;
+    double* red = nullptr;
+    double* dbuf = nullptr;     // device double scratch (noise, grads)
+    size_t dbuf_cap = 0;
+    void* flush = nullptr;
+    char* stage = nullptr;      // pinned host staging
+    size_t stage_cap = 0;
+};
+
+struct sgb_corr {
+    sgb_system* sys = nullptr;
+    std::string err;
+    int nobs = 0, ncorr = 0, npos = 0, ncell = 0, nomega = 0, nsnaps = 0, measperiod = 1;
+    double dt = 0, damping = 0, tol = 0;
+    int max_iters = 100;
+    int window = -1;
+    int64_t nsamples = 0;
+    void* ops = nullptr;      // R
+    int* pairs = nullptr;
+    void* A = nullptr;        // complex R [n][nobs][npos][ncell]
+    void* Ahat = nullptr;
+    double* P = nullptr;      // complex double accumulator
+    size_t plen = 0;          // complex elements
+    double* g = nullptr;      // [n]
+    cufftHandle plan_space = 0, plan_time = 0;
+    bool have_space = false, have_time = false;
+    bool profile = false;
+    cudaEvent_t ev[5] = {};
+    double phase_ms[4] = {0, 0, 0, 0};
+    int64_t nprof = 0;
+    int64_t prof_iters = 0;
+    sgb_batch* batch = nullptr;   // set when the accumulator samples a replica batch
+    int nrep = 1;                 // replicas sampled per add_sample call
+    int64_t prof_iters_last = 0;
+    cudaStream_t stream = nullptr;
+    long long* launches = nullptr;
+};
+
+
+struct sgb_batch {
+    sgb_desc proto{};
+    int nrep = 0, na = 0, nsm = 0;
+    bool fp32 = false;
+    std::vector<int> dims;          // [nrep][3]
+    std::vector<int> off;           // [nrep + 1] first site of each replica
+    int NS = 0;                     // total sites
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8] = {};
+    std::string err;
+    long long launches = 0;
+    // couplings per sublattice
+    std::vector<double> kappa_a, g_a, field_a, onsite;
+    std::vector<sgb_bond> bonds;
+    bool coup_set = false;
+    void* tables = nullptr;
+    int tables_bytes = 0;
+    Model<float> mf{};
+    Model<double> md{};
+    void* kap = nullptr;            // R[na]
+    void* h = nullptr;              // R[3][na]
+    bool has_field = false;
+    // per replica device data
+    int4* rd = nullptr;             // (L1, L2, L3, ncell)
+    int* roff = nullptr;
+    double* kT = nullptr;
+    std::vector<double> kT_h;
+    int* ladder = nullptr;          // replica at each ladder position (group-major)
+    int* gstart = nullptr;          // first ladder position of each group
+    int* gcount = nullptr;
+    int ngroups = 0;
+    std::vector<int> ladder_h, gstart_h, gcount_h;
+    int4* tiles = nullptr;          // (replica, first site, count, 0)
+    int ntiles = 0;
+    std::vector<int> tfirst, tcount;  // tiles of each replica (contiguous)
+    int* tfirst_d = nullptr;
+    int* tcount_d = nullptr;
+    // state
+    void* S = nullptr;
+    void* P = nullptr;
+    void* D1 = nullptr;
+    void* Sp = nullptr;             // midpoint iterate
+    void* H = nullptr;              // midpoint rotating buffers [3][3][NS]
+    void* Sc = nullptr;             // midpoint candidate
+    double* racc = nullptr;         // [3][nrep] convergence sums
+    Ctrl* ctrl = nullptr;
+    double* Epart = nullptr;        // [ntiles]
+    double* E = nullptr;            // [nrep]
+    unsigned long long* counters = nullptr;   // [0] Langevin step, [1] exchange round
+    long long* n_accept = nullptr;  // [nrep]
+    char* stage = nullptr;
+    size_t stage_cap = 0;
+    bool state_set = false;
+    cudaGraphExec_t graph = nullptr;
+    int graph_interval = -1;
+    double graph_dt = 0, graph_damping = 0;
+    uint64_t graph_seed = 0;
+};
+
+// batched add_sample! trajectory (sgb_batch.cu)
+int batch_corr_trajectory(sgb_corr* c);
+const char* batch_error(sgb_batch* b);

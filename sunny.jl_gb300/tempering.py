@@ -1,0 +1,163 @@
+"""Replica batches and parallel tempering on the GPU.
+
+`ReplicaBatch` holds many independent dipole-mode replicas that share the couplings of a
+prototype `System` but may differ in supercell size and temperature; they advance
+together in one persistent launch. `ParallelTempering` mirrors Sunny's
+(src/MonteCarlo/ParallelTempering.jl:2-95): replica exchange over a kT ladder, here one
+ladder per group of equal-size replicas, with step_ensemble! replayed from a captured
+CUDA graph.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from .system import System
+
+
+class ReplicaBatch:
+    N = 0  # dipole modes only
+
+    def __init__(self, proto: System, dims_list, kT=None, precision: str | None = None, device: int = 0, seed: int = 0):
+        if proto.N:
+            raise ValueError("replica batches support the dipole modes")
+        self.proto = proto
+        self.dims_list = [tuple(int(x) for x in d) for d in dims_list]
+        self.nrep = len(self.dims_list)
+        self.natoms = proto.natoms
+        self.precision = precision or proto.precision
+        self.seed = int(seed)
+        self.noise_step = 0
+        self._lib = _abi.load()
+        d = _abi.Desc()
+        d.dims[:] = self.dims_list[0]
+        d.natoms, d.N = proto.natoms, 0
+        d.mode = {"dipole": _abi.MODE_DIPOLE, "dipole_uncorrected": _abi.MODE_DIPOLE_UNCORRECTED}[proto.mode]
+        d.precision = _abi.FP32 if self.precision == "fp32" else _abi.FP64
+        d.device = device
+        dims = (C.c_int32 * (3 * self.nrep))(*[x for dd in self.dims_list for x in dd])
+        h = C.c_void_p()
+        self._check(self._lib.sgb_batch_create(C.byref(d), self.nrep, dims, C.byref(h)), None)
+        self._h = h
+        self._upload_couplings()
+        self.rng = np.random.default_rng(seed)
+        self.kT = np.zeros(self.nrep) if kT is None else np.asarray(kT, dtype=float)
+        self.set_kT(self.kT)
+
+    def _check(self, rc, h="self"):
+        if rc != _abi.SGB_OK:
+            hh = self._h if h == "self" else h
+            msg = self._lib.sgb_batch_last_error(hh)
+            raise _abi.SunnyGPUError(rc, (msg or b"").decode() or f"error {rc}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.sgb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def nsites(self, r: int) -> int:
+        return int(self._lib.sgb_batch_nsites(self._h, r))
+
+    def _upload_couplings(self):
+        p = self.proto
+        na = p.natoms
+        # couplings are per sublattice: take the first cell's values
+        first = np.arange(na) * p.ncell
+        kap = np.ascontiguousarray(p._kappa[first])
+        g = np.ascontiguousarray(p._g[first].transpose(0, 2, 1)).reshape(-1)
+        field = np.ascontiguousarray(p._field[first]).reshape(-1)
+        onsite = np.concatenate([p._onsite[a] if p._onsite[a] is not None else np.zeros(28) for a in range(na)])
+        bonds = p.bond_table()
+        arr = (_abi.BondC * max(1, len(bonds)))()
+        for k, b in enumerate(bonds):
+            arr[k] = b
+        self._check(self._lib.sgb_batch_set_couplings(self._h, _abi.dptr(kap), _abi.dptr(g), _abi.dptr(field),
+                                                      _abi.dptr(np.ascontiguousarray(onsite)), arr, len(bonds)))
+        self._kappa_a = kap
+
+    def set_kT(self, kT):
+        self.kT = np.ascontiguousarray(kT, dtype=float)
+        self._check(self._lib.sgb_batch_set_kT(self._h, _abi.dptr(self.kT)))
+
+    def get_kT(self) -> np.ndarray:
+        out = np.zeros(self.nrep)
+        self._check(self._lib.sgb_batch_get_kT(self._h, _abi.dptr(out)))
+        return out
+
+    def set_state(self, r: int, dipoles: np.ndarray):
+        self._check(self._lib.sgb_batch_set_state(self._h, r, _abi.dptr(np.ascontiguousarray(dipoles, dtype=float).reshape(-1))))
+
+    def get_state(self, r: int) -> np.ndarray:
+        out = np.zeros((self.nsites(r), 3))
+        self._check(self._lib.sgb_batch_get_state(self._h, r, _abi.dptr(out)))
+        return out
+
+    def randomize_spins(self):
+        """randomize_spins! on every replica (System.jl:513-517)."""
+        for r in range(self.nrep):
+            ns = self.nsites(r)
+            v = self.rng.standard_normal((ns, 3))
+            kap = np.repeat(self._kappa_a, ns // self.natoms)
+            self.set_state(r, kap[:, None] * v / np.linalg.norm(v, axis=1)[:, None])
+
+    def langevin(self, dt: float, damping: float, nsteps: int):
+        self._check(self._lib.sgb_batch_langevin(self._h, dt, damping, self.seed, self.noise_step, nsteps))
+        self.noise_step += nsteps
+
+    def noise(self, r: int, step: int) -> np.ndarray:
+        out = np.zeros((self.nsites(r), 3))
+        self._check(self._lib.sgb_batch_langevin_noise(self._h, r, self.seed, step, _abi.dptr(out)))
+        return out
+
+    def energies(self) -> np.ndarray:
+        out = np.zeros(self.nrep)
+        self._check(self._lib.sgb_batch_energy(self._h, _abi.dptr(out)))
+        return out
+
+
+class ParallelTempering:
+    """ParallelTempering(system, Langevin, kT_sched) over replicas of (possibly) several
+    sizes (ParallelTempering.jl:18-37). Each group of equal dims has its own ladder."""
+
+    def __init__(self, batch: ReplicaBatch, dt: float, damping: float):
+        self.batch = batch
+        self.dt, self.damping = float(dt), float(damping)
+        self.n_accept = np.zeros(batch.nrep, dtype=np.int64)
+        self.n_exch_rounds = 0
+
+    def replica_exchange(self, exch_start: int, uniforms=None, round_index: int = 0):
+        """replica_exchange!(PT, exch_start) (ParallelTempering.jl:40-73); `uniforms`
+        (indexed by ladder position) replaces the device generator."""
+        b = self.batch
+        na = np.zeros(b.nrep, dtype=np.int64)
+        u = None if uniforms is None else np.ascontiguousarray(uniforms, dtype=float)
+        b._check(b._lib.sgb_batch_exchange(b._h, exch_start, b.seed, round_index, _abi.dptr(u),
+                                           na.ctypes.data_as(C.POINTER(C.c_int64))))
+        self.n_accept = na
+
+    def step_ensemble(self, nsteps: int, exch_interval: int):
+        """step_ensemble!(PT, nsteps, exch_interval) (ParallelTempering.jl:80-95)."""
+        b = self.batch
+        na = np.zeros(b.nrep, dtype=np.int64)
+        b._check(b._lib.sgb_batch_step_ensemble(b._h, self.dt, self.damping, b.seed, nsteps, exch_interval,
+                                                na.ctypes.data_as(C.POINTER(C.c_int64))))
+        rounds = -(-nsteps // exch_interval)
+        b.noise_step += rounds * exch_interval
+        self.n_exch_rounds += rounds
+        self.n_accept = na
+
+    @property
+    def graph_active(self) -> bool:
+        return bool(self.batch._lib.sgb_batch_graph_active(self.batch._h))

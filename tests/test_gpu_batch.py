@@ -1,0 +1,119 @@
+"""Replica batches, parallel tempering and batched S(q,ω) sampling against the FP64
+oracle and against the single-system path."""
+import numpy as np
+import pytest
+
+from models import oracle_of
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(1e-300, np.max(np.abs(b)))
+
+
+def sc_proto(sg, dims, precision="fp64", D=0.1, J=1.0):
+    s = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=dims, seed=1, precision=precision,
+                  device=None)
+    s.set_exchange(J, sg.Bond(1, 1, [1, 0, 0]))
+    s.set_onsite_coupling(lambda Sx, Sy, Sz: -D * Sz @ Sz, 1)
+    s.set_field([0.0, 0.05, 0.1])
+    return s
+
+
+def oracle_for_dims(sg, orc, dims, precision="fp64"):
+    return oracle_of(orc, sc_proto(sg, dims, precision))
+
+
+def test_batch_langevin_and_energy_fp64(gpu, sg, orc):
+    dims = [(4, 4, 4), (3, 5, 2), (4, 4, 4), (2, 2, 6)]
+    proto = sc_proto(sg, dims[0])
+    b = sg.ReplicaBatch(proto, dims, kT=[0.3, 0.5, 0.7, 0.2], seed=11)
+    b.randomize_spins()
+    S0 = [b.get_state(r) for r in range(b.nrep)]
+    E = b.energies()
+    for r, d in enumerate(dims):
+        o = oracle_for_dims(sg, orc, d)
+        assert E[r] == pytest.approx(o.energy(S0[r]), rel=1e-12, abs=1e-12)
+    b.langevin(0.02, 0.1, 25)
+    for r, d in enumerate(dims):
+        o = oracle_for_dims(sg, orc, d)
+        noise = np.stack([b.noise(r, k) for k in range(25)])
+        S_ref, _ = o.langevin(S0[r], None, 0.02, 0.1, b.kT[r], 25, noise)
+        assert rel(b.get_state(r), S_ref) < 1e-11
+
+
+def test_replica_exchange_matches_oracle(gpu, sg, orc):
+    dims = [(4, 4, 4)] * 4 + [(3, 3, 3)] * 3
+    kT = [0.4, 0.1, 0.8, 0.2, 0.3, 0.15, 0.6]
+    proto = sc_proto(sg, dims[0])
+    b = sg.ReplicaBatch(proto, dims, kT=kT, seed=5)
+    b.randomize_spins()
+    b.langevin(0.02, 0.1, 50)
+    E = b.energies()
+    pt = sg.ParallelTempering(b, 0.02, 0.1)
+    rng = np.random.default_rng(0)
+    for exch_start in (1, 2, 1):
+        kT_before = b.get_kT()
+        E = b.energies()
+        u = rng.random(b.nrep)
+        pt.replica_exchange(exch_start, uniforms=u)
+        kT_after = b.get_kT()
+        # oracle, per group of equal dims, ladder = replicas sorted by kT
+        expect = kT_before.copy()
+        pos = 0
+        for grp in ([0, 1, 2, 3], [4, 5, 6]):
+            ladder = sorted(grp, key=lambda r: kT_before[r])
+            kts = [kT_before[r] for r in ladder]
+            ids, acc = orc.replica_exchange(E, kts, list(ladder), exch_start, u[pos:pos + len(grp)])
+            for p, r in enumerate(ids):
+                expect[r] = kts[p]
+            pos += len(grp)
+        assert np.array_equal(kT_after, expect)
+
+
+def test_step_ensemble_graph_equals_direct_loop(gpu, sg):
+    dims = [(4, 4, 4)] * 3 + [(6, 6, 6)] * 3
+    kT = [0.1, 0.3, 0.9, 0.2, 0.5, 1.2]
+    proto = sc_proto(sg, dims[0])
+    bA = sg.ReplicaBatch(proto, dims, kT=kT, seed=3)
+    bB = sg.ReplicaBatch(proto, dims, kT=kT, seed=3)
+    bA.randomize_spins()
+    for r in range(bA.nrep):
+        bB.set_state(r, bA.get_state(r))
+    bA.langevin(0.02, 0.2, 1)
+    bB.langevin(0.02, 0.2, 1)
+    ptA = sg.ParallelTempering(bA, 0.02, 0.2)
+    ptA.step_ensemble(300, 100)
+    ptB = sg.ParallelTempering(bB, 0.02, 0.2)
+    for i in range(1, 4):
+        bB.langevin(0.02, 0.2, 100)
+        ptB.replica_exchange((i % 2) + 1, round_index=i - 1)
+    assert ptA.graph_active
+    assert np.array_equal(bA.get_kT(), bB.get_kT())
+    for r in range(bA.nrep):
+        assert np.array_equal(bA.get_state(r), bB.get_state(r))
+    assert np.array_equal(ptA.n_accept, ptB.n_accept)
+
+
+def test_batched_sampling_equals_single_samples(gpu, sg):
+    # one batched add_sample over 3 replicas == 3 single-system add_samples
+    cr = sg.diamond_crystal()
+    proto = sg.System(cr, [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(2, 3, 2), seed=101, device=None)
+    proto.set_exchange(0.6498, sg.Bond(1, 3, [0, 0, 0]))
+    b = sg.ReplicaBatch(proto, [(2, 3, 2)] * 3, kT=[0.2] * 3, seed=2)
+    b.randomize_spins()
+    states = [b.get_state(r) for r in range(3)]
+    kw = dict(energies=np.linspace(0, 5.5, 10), dt=0.12)
+    scb = sg.SampledCorrelations(b, measure=sg.ssf_perp(proto), **kw)
+    sg.add_sample(scb, b)
+    assert scb.nsamples == 3
+    single = sg.System(cr, [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(2, 3, 2), seed=101)
+    single.set_exchange(0.6498, sg.Bond(1, 3, [0, 0, 0]))
+    scs = sg.SampledCorrelations(single, measure=sg.ssf_perp(single), **kw)
+    for r in range(3):
+        single.set_state_flat(dipoles=states[r])
+        sg.add_sample(scs, single)
+        assert rel(b.get_state(r), single.dipoles_flat()) < 1e-12
+    assert scs.nsamples == 3
+    assert rel(scb.data, scs.data) < 1e-11
