@@ -40,6 +40,7 @@ struct BatchArgs {
     int ntiles;
     const int4* rd;     // (L1, L2, L3, ncell)
     const int* roff;
+    const int* pc;      // [NS] packed (c1 | c2<<8 | c3<<16 | atom<<24) of every site
     int NS;
     const R* kap;       // [na]
     const R* h;         // [3][na] or nullptr
@@ -55,14 +56,18 @@ struct TileCtx {
     SiteIdx ix;
 };
 
-__device__ __forceinline__ TileCtx tile_ctx(const int4* tiles, const int4* rd, const int* roff, int t) {
+__device__ __forceinline__ TileCtx tile_ctx(const int4* tiles, const int4* rd, const int* roff, const int* pc, int t) {
     TileCtx c;
     int4 tl = tiles[t];
     c.r = tl.x;
     c.s = tl.y + threadIdx.x;
     c.d = rd[c.r];
     c.off = roff[c.r];
-    c.ix = decompose(c.s, c.d.x, c.d.y, c.d.z);
+    const int p = pc[c.off + c.s];
+    c.ix.c1 = p & 0xff;
+    c.ix.c2 = (p >> 8) & 0xff;
+    c.ix.c3 = (p >> 16) & 0xff;
+    c.ix.a = (int)((unsigned)p >> 24);
     return c;
 }
 
@@ -83,9 +88,9 @@ __device__ __forceinline__ void batch_noise(uint64_t seed, int r, uint64_t step,
 }
 
 // Heun over every replica (Integrators.jl:313-332); each replica uses its own kT.
-template <class R>
-__global__ void __launch_bounds__(SGB_TILE) k_batch_heun(BatchArgs<R> A, const double* kT, int nsteps, double dt,
-                                                         double lam, uint64_t seed, unsigned long long* counters) {
+template <class R, bool GEN>
+__global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_heun(BatchArgs<R> A, const double* kT, int nsteps, double dt,
+                                                            double lam, uint64_t seed, unsigned long long* counters) {
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(A.M, smem);
     const uint64_t step0 = *((volatile unsigned long long*)counters);
@@ -93,7 +98,7 @@ __global__ void __launch_bounds__(SGB_TILE) k_batch_heun(BatchArgs<R> A, const d
     for (int step = 0; step < nsteps; ++step) {
         for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
             if (!tile_has(A.tiles, t)) continue;
-            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
             const R* X = A.S + c.off;
             const R* Y = A.S + NS + c.off;
             const R* Z = A.S + 2 * NS + c.off;
@@ -104,7 +109,8 @@ __global__ void __launch_bounds__(SGB_TILE) k_batch_heun(BatchArgs<R> A, const d
             batch_noise<R>(seed, c.r, step0 + step, c.s, scale, xx, xy, xz);
             R hx, hy, hz, gx, gy, gz, d0, d1, d2;
             site_field(A, c.ix.a, hx, hy, hz);
-            grad_site_L<R, true>(A.M, T, c.ix, c.d.x, c.d.y, c.d.z, hx, hy, hz, sx, sy, sz, X, Y, Z, gx, gy, gz);
+            grad_batch<R, GEN>(A.M, T, c.ix.c1, c.ix.c2, c.ix.c3, c.ix.a, c.d.x, c.d.y, c.d.z, hx, hy, hz, sx, sy, sz, X,
+                               Y, Z, gx, gy, gz);
             rhs_dipole<R>(sx, sy, sz, xx, xy, xz, gx, gy, gz, (R)dt, (R)lam, d0, d1, d2);
             const int g = c.off + c.s;
             A.D1[g] = d0; A.D1[NS + g] = d1; A.D1[2 * NS + g] = d2;
@@ -115,7 +121,7 @@ __global__ void __launch_bounds__(SGB_TILE) k_batch_heun(BatchArgs<R> A, const d
         if (!sgb_grid_barrier(A.ctrl, gridDim.x)) return;
         for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
             if (!tile_has(A.tiles, t)) continue;
-            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
             const int g = c.off + c.s;
             const R* X = A.P + c.off;
             const R* Y = A.P + NS + c.off;
@@ -127,7 +133,8 @@ __global__ void __launch_bounds__(SGB_TILE) k_batch_heun(BatchArgs<R> A, const d
             batch_noise<R>(seed, c.r, step0 + step, c.s, scale, xx, xy, xz);
             R hx, hy, hz, gx, gy, gz, e0, e1, e2;
             site_field(A, c.ix.a, hx, hy, hz);
-            grad_site_L<R, true>(A.M, T, c.ix, c.d.x, c.d.y, c.d.z, hx, hy, hz, px, py, pz, X, Y, Z, gx, gy, gz);
+            grad_batch<R, GEN>(A.M, T, c.ix.c1, c.ix.c2, c.ix.c3, c.ix.a, c.d.x, c.d.y, c.d.z, hx, hy, hz, px, py, pz, X,
+                               Y, Z, gx, gy, gz);
             rhs_dipole<R>(px, py, pz, xx, xy, xz, gx, gy, gz, (R)dt, (R)lam, e0, e1, e2);
             R nx = A.S[g] + (A.D1[g] + e0) / 2;
             R ny = A.S[NS + g] + (A.D1[NS + g] + e1) / 2;
@@ -151,7 +158,7 @@ __global__ void __launch_bounds__(SGB_TILE) k_batch_energy(BatchArgs<R> A, doubl
     const int t = blockIdx.x;
     double E = 0;
     if (tile_has(A.tiles, t)) {
-        TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+        TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
         const int NS = A.NS;
         const R* X = A.S + c.off;
         const R* Y = A.S + NS + c.off;
@@ -297,11 +304,14 @@ __device__ __forceinline__ void snap_write(const BSnap<R>& sn, int r, int t, int
     }
 }
 
-template <class R>
-__global__ void __launch_bounds__(SGB_TILE) k_batch_midpoint(BatchArgs<R> A, MidArgs<R> X, int nsteps, double dt,
-                                                             double lam, BSnap<R> sn) {
+#define SGB_MAXREP_CORR 64
+
+template <class R, bool GEN>
+__global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midpoint(BatchArgs<R> A, MidArgs<R> X, int nsteps, double dt,
+                                                                double lam, BSnap<R> sn) {
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(A.M, smem);
+    __shared__ double sacc[SGB_MAXREP_CORR];
     const int NS = A.NS;
     const bool leader = (blockIdx.x == 0 && threadIdx.x == 0);
     bool act[SGB_MAXT];
@@ -310,7 +320,7 @@ __global__ void __launch_bounds__(SGB_TILE) k_batch_midpoint(BatchArgs<R> A, Mid
     for (int k = 0; k < SGB_MAXT; k++) {
         const int t = blockIdx.x + k * gridDim.x;
         if (t >= A.ntiles || !tile_has(A.tiles, t)) continue;
-        TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+        TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
         const int g = c.off + c.s;
         R sx = A.S[g], sy = A.S[NS + g], sz = A.S[2 * NS + g];
         R hx = (sx + sx) / 2, hy = (sy + sy) / 2, hz = (sz + sz) / 2;
@@ -329,7 +339,7 @@ __global__ void __launch_bounds__(SGB_TILE) k_batch_midpoint(BatchArgs<R> A, Mid
             act[k] = true;
             const int t = blockIdx.x + k * gridDim.x;
             if (t >= A.ntiles || !tile_has(A.tiles, t)) continue;
-            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
             const int g = c.off + c.s;
             X.Sp[g] = A.S[g]; X.Sp[NS + g] = A.S[NS + g]; X.Sp[2 * NS + g] = A.S[2 * NS + g];
         }
@@ -340,13 +350,15 @@ __global__ void __launch_bounds__(SGB_TILE) k_batch_midpoint(BatchArgs<R> A, Mid
             R* Hn = X.H + (size_t)nxt * 3 * NS;
             R* Hs = X.H + (size_t)nst * 3 * NS;
             const int slot = (int)(itg % 3);
+            for (int q = threadIdx.x; q < X.nrep; q += blockDim.x) sacc[q] = 0.0;
+            __syncthreads();
             for (int k = 0; k < SGB_MAXT; k++) {
                 const int t = blockIdx.x + k * gridDim.x;
                 if (t >= A.ntiles) break;
                 double acc = 0.0;
-                int r = A.tiles[t].x;
+                const int r = A.tiles[t].x;
                 if (tile_has(A.tiles, t)) {
-                    TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+                    TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
                     const int g = c.off + c.s;
                     if (act[k]) {
                         const R kap = A.kap[c.ix.a];
@@ -356,8 +368,8 @@ __global__ void __launch_bounds__(SGB_TILE) k_batch_midpoint(BatchArgs<R> A, Mid
                         normalize_dip<R>(hx, hy, hz, kap);
                         R fx, fy, fz, gx, gy, gz, dx, dy, dz;
                         site_field(A, c.ix.a, fx, fy, fz);
-                        grad_site_L<R, true>(A.M, T, c.ix, c.d.x, c.d.y, c.d.z, fx, fy, fz, hx, hy, hz, Hc + c.off,
-                                             Hc + NS + c.off, Hc + 2 * NS + c.off, gx, gy, gz);
+                        grad_batch<R, GEN>(A.M, T, c.ix.c1, c.ix.c2, c.ix.c3, c.ix.a, c.d.x, c.d.y, c.d.z, fx, fy, fz, hx,
+                                           hy, hz, Hc + c.off, Hc + NS + c.off, Hc + 2 * NS + c.off, gx, gy, gz);
                         rhs_dipole<R>(hx, hy, hz, (R)0, (R)0, (R)0, gx, gy, gz, (R)dt, (R)lam, dx, dy, dz);
                         R nx = sx + dx, ny = sy + dy, nz = sz + dz;
                         double ex = (double)(qx - nx), ey = (double)(qy - ny), ez = (double)(qz - nz);
@@ -377,9 +389,16 @@ __global__ void __launch_bounds__(SGB_TILE) k_batch_midpoint(BatchArgs<R> A, Mid
                         Hs[g] = Hn[g]; Hs[NS + g] = Hn[NS + g]; Hs[2 * NS + g] = Hn[2 * NS + g];
                     }
                 }
-                double bsum = sgb_block_sum(acc);
-                if (threadIdx.x == 0 && act[k]) atomicAdd(&X.racc[slot * X.nrep + r], bsum);
+                if (act[k]) {
+                    // warp sum, then one shared-memory atomic per warp (tiles never straddle replicas)
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+                    if ((threadIdx.x & 31) == 0) atomicAdd(&sacc[r], acc);
+                }
             }
+            __syncthreads();
+            for (int q = threadIdx.x; q < X.nrep; q += blockDim.x)
+                if (sacc[q] != 0.0) atomicAdd(&X.racc[slot * X.nrep + q], sacc[q]);
             if (leader) {
                 for (int q = 0; q < X.nrep; q++) X.racc[((slot + 1) % 3) * X.nrep + q] = 0.0;
                 A.ctrl->iters += 1;
@@ -416,7 +435,7 @@ __global__ void __launch_bounds__(SGB_TILE) k_batch_midpoint(BatchArgs<R> A, Mid
             for (int k = 0; k < SGB_MAXT; k++) {
                 const int t = blockIdx.x + k * gridDim.x;
                 if (t >= A.ntiles || !tile_has(A.tiles, t)) continue;
-                TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, t);
+                TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
                 const int g = c.off + c.s;
                 snap_write<R>(sn, c.r, sn.t0 + done / sn.measperiod, c.s, c.d.w * A.M.na, A.S[g], A.S[NS + g],
                               A.S[2 * NS + g]);
@@ -473,6 +492,7 @@ BatchArgs<R> bargs(sgb_batch* b) {
     A.ntiles = b->ntiles;
     A.rd = b->rd;
     A.roff = b->roff;
+    A.pc = b->pc;
     A.NS = b->NS;
     A.kap = (const R*)b->kap;
     A.h = b->has_field ? (const R*)b->h : nullptr;
@@ -519,12 +539,15 @@ int enqueue_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, int
     BatchArgs<R> A = bargs<R>(b);
     int grid = 0;
     size_t smem = (size_t)b->tables_bytes;
-    int rc = bgrid(b, k_batch_heun<R>, smem, 0, &grid);
-    if (rc) return rc;
     double* kT = b->kT;
     unsigned long long* ctr = b->counters;
     void* args[] = {&A, &kT, &nsteps, &dt, &damping, &seed, &ctr};
-    return bcoop(b, k_batch_heun<R>, grid, smem, args);
+    if (A.M.general) {
+        int rc = bgrid(b, k_batch_heun<R, true>, smem, 0, &grid);
+        return rc ? rc : bcoop(b, k_batch_heun<R, true>, grid, smem, args);
+    }
+    int rc = bgrid(b, k_batch_heun<R, false>, smem, 0, &grid);
+    return rc ? rc : bcoop(b, k_batch_heun<R, false>, grid, smem, args);
 }
 
 template <class R>
@@ -618,12 +641,18 @@ static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
     int nsteps = c->measperiod * (c->nsnaps - 1);
     int grid = 0;
     size_t smem = (size_t)b->tables_bytes;
-    int rc = bgrid(b, k_batch_midpoint<R>, smem, SGB_MAXT, &grid);
-    if (rc) return rc;
+    if (b->nrep > SGB_MAXREP_CORR) return bfail(b, SGB_ERR_ARG, "batched sampling supports at most 64 replicas");
     BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
     double dt = c->dt, lam = c->damping;
     void* args[] = {&A, &X, &nsteps, &dt, &lam, &sn};
-    rc = bcoop(b, k_batch_midpoint<R>, grid, smem, args);
+    int rc;
+    if (A.M.general) {
+        rc = bgrid(b, k_batch_midpoint<R, true>, smem, SGB_MAXT, &grid);
+        if (!rc) rc = bcoop(b, k_batch_midpoint<R, true>, grid, smem, args);
+    } else {
+        rc = bgrid(b, k_batch_midpoint<R, false>, smem, SGB_MAXT, &grid);
+        if (!rc) rc = bcoop(b, k_batch_midpoint<R, false>, grid, smem, args);
+    }
     if (rc) return rc;
     Ctrl st;
     if ((rc = read_status(b, &st))) return rc;
@@ -657,6 +686,7 @@ void sgb_batch_destroy(sgb_batch* b) {
     p = b->rd; bfree(p); p = b->roff; bfree(p); p = b->kT; bfree(p); p = b->ladder; bfree(p);
     p = b->gstart; bfree(p); p = b->gcount; bfree(p); p = b->tiles; bfree(p); p = b->tfirst_d; bfree(p);
     p = b->tcount_d; bfree(p);
+    p = b->pc; bfree(p);
     bfree(b->S); bfree(b->P); bfree(b->D1); bfree(b->Sp); bfree(b->H); bfree(b->Sc);
     p = b->racc; bfree(p); p = b->ctrl; bfree(p); p = b->Epart; bfree(p); p = b->E; bfree(p);
     p = b->counters; bfree(p); p = b->n_accept; bfree(p);
@@ -682,7 +712,10 @@ int sgb_batch_create(const sgb_desc* d, int32_t nrep, const int32_t* dims, sgb_b
     long long tot = 0;
     for (int r = 0; r < nrep; r++) {
         for (int k = 0; k < 3; k++)
-            if (dims[3 * r + k] < 1) { sgb_batch_destroy(b); return bfail(nullptr, SGB_ERR_ARG, "dims must be positive"); }
+            if (dims[3 * r + k] < 1 || dims[3 * r + k] > 255) {
+                sgb_batch_destroy(b);
+                return bfail(nullptr, SGB_ERR_ARG, "replica dims must be in [1, 255]");
+            }
         b->off[r] = (int)tot;
         tot += (long long)dims[3 * r] * dims[3 * r + 1] * dims[3 * r + 2] * b->na;
         if (tot > (1LL << 30)) { sgb_batch_destroy(b); return bfail(nullptr, SGB_ERR_ARG, "too many sites"); }
@@ -720,6 +753,7 @@ int sgb_batch_create(const sgb_desc* d, int32_t nrep, const int32_t* dims, sgb_b
     rc |= bmalloc(b, (void**)&b->tiles, sizeof(int4) * b->ntiles);
     rc |= bmalloc(b, (void**)&b->tfirst_d, sizeof(int) * nrep);
     rc |= bmalloc(b, (void**)&b->tcount_d, sizeof(int) * nrep);
+    rc |= bmalloc(b, (void**)&b->pc, sizeof(int) * b->NS);
     rc |= bmalloc(b, &b->S, R * 3 * b->NS);
     rc |= bmalloc(b, &b->P, R * 3 * b->NS);
     rc |= bmalloc(b, &b->D1, R * 3 * b->NS);
@@ -734,6 +768,18 @@ int sgb_batch_create(const sgb_desc* d, int32_t nrep, const int32_t* dims, sgb_b
     cudaMemcpy(b->tiles, tiles.data(), sizeof(int4) * b->ntiles, cudaMemcpyHostToDevice);
     cudaMemcpy(b->tfirst_d, b->tfirst.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice);
     cudaMemcpy(b->tcount_d, b->tcount.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice);
+    {
+        std::vector<int> pcv(b->NS);
+        for (int r = 0; r < nrep; r++) {
+            const int L1 = dims[3 * r], L2 = dims[3 * r + 1], L3 = dims[3 * r + 2];
+            int k = b->off[r];
+            for (int a = 0; a < b->na; a++)
+                for (int c3 = 0; c3 < L3; c3++)
+                    for (int c2 = 0; c2 < L2; c2++)
+                        for (int c1 = 0; c1 < L1; c1++) pcv[k++] = c1 | (c2 << 8) | (c3 << 16) | (a << 24);
+        }
+        cudaMemcpy(b->pc, pcv.data(), sizeof(int) * b->NS, cudaMemcpyHostToDevice);
+    }
     cudaMemset(b->S, 0, R * 3 * b->NS);
     cudaMemset(b->ctrl, 0, sizeof(Ctrl));
     cudaMemset(b->counters, 0, sizeof(unsigned long long) * 2);

@@ -28,6 +28,7 @@ struct DBond {
     int bqkind;      // 0 none, 1 isotropic, 2 matrix (index bqidx)
     int bqidx;       // row in the 5x5 biquadratic table
     int fwd;         // 1 for the non-culled copy (counted in the energy)
+    int pk;          // raw offsets and target packed as bytes: (n0+128) | (n1+128)<<8 | (n2+128)<<16 | j<<24
 };
 
 // Sunny's scalar_biquad_metric (src/System/Types.jl:40)

@@ -54,38 +54,45 @@ __global__ void __launch_bounds__(256) k_corr_accum(const R* __restrict__ A, dou
     __syncthreads();
     const int B = ncorr * npos * npos;
     const size_t base = ((size_t)w * ncell + q0) * B;
-    const int total = nq * B;
     double2* out = reinterpret_cast<double2*>(P) + base;
-    // four independent 16-byte loads in flight per thread before any use
-    constexpr int U = 4;
-    for (int e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
-        double2 acc[U];
+    // Element (ql, r) of the tile is out[ql*B + r] with r = c + ncorr*(i + npos*j). A thread
+    // owns the r values threadIdx.x + k*blockDim.x for every ql, so their shared-memory
+    // offsets are computed once, outside the streaming loop (no divisions per element).
+    constexpr int KMAX = 8;
+    int ia[KMAX], ib[KMAX];
+    const int nk = (B + blockDim.x - 1) / blockDim.x;
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-            int e = e0 + u * blockDim.x;
-            if (e < total) acc[u] = __ldcs(out + e);
-        }
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-            int e = e0 + u * blockDim.x;
-            if (e >= total) break;
-            int ql = e / B, r = e - ql * B;
-            int c = r % ncorr;
-            int t = r / ncorr;
+    for (int k = 0; k < KMAX; k++) {
+        int r = threadIdx.x + k * blockDim.x;
+        ia[k] = -1; ib[k] = -1;
+        if (k < nk && r < B) {
+            int c = r % ncorr, t = r / ncorr;
             int i = t % npos, j = t / npos;
-            const int ia = (pr[2 * c] * npos + i) * QT + ql;
-            const int ib = (pr[2 * c + 1] * npos + j) * QT + ql;
+            ia[k] = (pr[2 * c] * npos + i) * QT;
+            ib[k] = (pr[2 * c + 1] * npos + j) * QT;
+        }
+    }
+    const int rstride = nrow * QT;
+    for (int ql = 0; ql < nq; ql++) {
+        double2* row = out + (size_t)ql * B;
+        double2 acc[KMAX];
+#pragma unroll
+        for (int k = 0; k < KMAX; k++)
+            if (ia[k] >= 0) acc[k] = __ldcs(row + threadIdx.x + k * blockDim.x);
+#pragma unroll
+        for (int k = 0; k < KMAX; k++) {
+            if (ia[k] < 0) continue;
             R sre = 0, sim = 0;
             for (int rr = 0; rr < nrep; rr++) {
-                C2<R> a = As[rr * nrow * QT + ia];
-                C2<R> b = As[rr * nrow * QT + ib];
+                C2<R> a = As[rr * rstride + ia[k] + ql];
+                C2<R> b = As[rr * rstride + ib[k] + ql];
                 // conj(a) * b
                 sre += a.x * b.x + a.y * b.y;
                 sim += a.x * b.y - a.y * b.x;
             }
-            acc[u].x += (double)sre;
-            acc[u].y += (double)sim;
-            __stcs(out + e, acc[u]);
+            acc[k].x += (double)sre;
+            acc[k].y += (double)sim;
+            __stcs(row + threadIdx.x + k * blockDim.x, acc[k]);
         }
     }
 }
@@ -142,6 +149,7 @@ int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int no
     constexpr int QT = 32;
     size_t smem = (size_t)nrep * nobs * npos * QT * sizeof(C2<R>) + 2 * ncorr * sizeof(int) + 16;
     if (smem > 200 * 1024) return SGB_ERR_ARG;
+    if (ncorr * npos * npos > 8 * 256) return SGB_ERR_ARG;   // at most 8 accumulator entries per thread and row
     if (smem > 48 * 1024) {
         if (cudaFuncSetAttribute(k_corr_accum<R, QT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return SGB_ERR_CUDA;

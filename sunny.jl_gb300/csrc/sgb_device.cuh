@@ -207,6 +207,72 @@ __device__ inline void grad_site_L(const Model<R>& M, const Tab<R>& T, const Sit
     }
 }
 
+// Batch form: site coordinates given directly, bond offsets unpacked from DBond::pk (one
+// shared-memory load per bond), raw offsets wrapped for |n| <= L. GEN = false is the fast
+// path for isotropic bilinear couplings without biquadratic terms.
+template <class R, bool GEN>
+__device__ inline void grad_batch(const Model<R>& M, const Tab<R>& T, int c1, int c2, int c3, int a, int L1, int L2,
+                                  int L3, R hx, R hy, R hz, R sx, R sy, R sz, const R* X, const R* Y, const R* Zc,
+                                  R& gx, R& gy, R& gz) {
+    gx = hx; gy = hy; gz = hz;
+    {
+        int km = T.kmax[a];
+        if (km > 0) classical_aniso<R>(T.stev + 28 * a, km, sx, sy, sz, gx, gy, gz);
+    }
+    const int b0 = T.boff[a], b1 = T.boff[a + 1];
+    constexpr int G = 6;
+    for (int b = b0; b < b1; b += G) {
+        R tx[G], ty[G], tz[G];
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            if (b + k < b1) {
+                const int pk = T.bonds[b + k].pk;
+                int x1 = sgb_wrap_any(c1 + (int)(pk & 0xff) - 128, L1);
+                int x2 = sgb_wrap_any(c2 + (int)((pk >> 8) & 0xff) - 128, L2);
+                int x3 = sgb_wrap_any(c3 + (int)((pk >> 16) & 0xff) - 128, L3);
+                int js = x1 + L1 * (x2 + L2 * (x3 + L3 * (int)((unsigned)pk >> 24)));
+                tx[k] = sgb_ld(X + js); ty[k] = sgb_ld(Y + js); tz[k] = sgb_ld(Zc + js);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            if (b + k >= b1) break;
+            const DBond<R>& B = T.bonds[b + k];
+            if (!GEN) {
+                R j = B.J[0];
+                gx += j * tx[k]; gy += j * ty[k]; gz += j * tz[k];
+                continue;
+            }
+            if (B.jkind == 0) {
+                R j = B.J[0];
+                gx += j * tx[k]; gy += j * ty[k]; gz += j * tz[k];
+            } else {
+                gx += B.J[0] * tx[k] + B.J[3] * ty[k] + B.J[6] * tz[k];
+                gy += B.J[1] * tx[k] + B.J[4] * ty[k] + B.J[7] * tz[k];
+                gz += B.J[2] * tx[k] + B.J[5] * ty[k] + B.J[8] * tz[k];
+            }
+            if (M.dipole_mode && B.bqkind != 0) {
+                R Qj[5], v[5];
+                quad5<R>(tx[k], ty[k], tz[k], Qj);
+                if (B.bqkind == 1) {
+#pragma unroll
+                    for (int q = 0; q < 5; q++) v[q] = B.bq * ((R)biquad_metric(q) * Qj[q]);
+                } else {
+                    const R* Bm = T.bq + 25 * B.bqidx;
+#pragma unroll
+                    for (int q = 0; q < 5; q++) {
+                        R acc = 0;
+#pragma unroll
+                        for (int p = 0; p < 5; p++) acc += Bm[q + 5 * p] * Qj[p];
+                        v[q] = acc;
+                    }
+                }
+                add_quad_grad<R>(sx, sy, sz, v, gx, gy, gz);
+            }
+        }
+    }
+}
+
 // Single-system form: per-site Zeeman field from M.h, offsets pre-reduced mod dims.
 template <class R>
 __device__ inline void grad_site(const Model<R>& M, const Tab<R>& T, int site, const SiteIdx& ix,

@@ -115,6 +115,7 @@ struct sgb_batch {
     std::vector<int> tfirst, tcount;  // tiles of each replica (contiguous)
     int* tfirst_d = nullptr;
     int* tcount_d = nullptr;
+    int* pc = nullptr;              // [NS] packed site coordinates
     // state
     void* S = nullptr;
     void* P = nullptr;

@@ -16,6 +16,7 @@ struct Model {
     int N;              // 0 in dipole modes
     int dipole_mode;    // 1 for :dipole / :dipole_uncorrected
     int has_biquad;     // any bond with a biquadratic coupling
+    int general;        // any anisotropic (3x3) or biquadratic bond; 0 selects the isotropic fast path
     const R* kappa;     // [ns]
     const R* h;         // [3][ns] Zeeman g'B, or nullptr
     const unsigned char* tables;  // packed tables (device)

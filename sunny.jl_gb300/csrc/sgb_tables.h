@@ -104,6 +104,11 @@ std::string pack_tables(int na, int N, bool sun, const int* dims, const std::vec
             }
             if (e.bqkind != 0) any_bq = true;
             e.fwd = dir == 0 ? 1 : 0;
+            {
+                int n0 = dir == 0 ? b.n[0] : -b.n[0], n1 = dir == 0 ? b.n[1] : -b.n[1], n2 = dir == 0 ? b.n[2] : -b.n[2];
+                if (n0 < -128 || n0 > 127 || n1 < -128 || n1 > 127 || n2 < -128 || n2 > 127) return "bond offset exceeds 127 cells";
+                e.pk = (n0 + 128) | ((n1 + 128) << 8) | ((n2 + 128) << 16) | (to << 24);
+            }
             per[from].push_back(e);
         }
     }
@@ -159,6 +164,10 @@ std::string pack_tables(int na, int N, bool sun, const int* dims, const std::vec
     M.N = N;
     M.dipole_mode = sun ? 0 : 1;
     M.has_biquad = any_bq ? 1 : 0;
+    M.general = 0;
+    for (auto& v : per)
+        for (auto& e : v)
+            if (e.jkind != 0 || e.bqkind != 0) M.general = 1;
     M.tables_bytes = (int)bytes;
     M.nb = nb;
     M.nbq = nbq;
