@@ -17,6 +17,8 @@
 // replicas, swaps temperatures on device, and step_ensemble! replays one captured CUDA
 // graph per exchange round.
 #include <algorithm>
+#include <array>
+#include <cstddef>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -41,6 +43,8 @@ struct BatchArgs {
     const int4* rd;     // (L1, L2, L3, ncell)
     const int* roff;
     const int* pc;      // [NS] packed (c1 | c2<<8 | c3<<16 | atom<<24) of every site
+    const int* nbr;     // neighbour tables
+    const int* nbo;     // [nrep] table offset of each replica
     int NS;
     const R* kap;       // [na]
     const R* h;         // [3][na] or nullptr
@@ -109,8 +113,8 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_heun
             batch_noise<R>(seed, c.r, step0 + step, c.s, scale, xx, xy, xz);
             R hx, hy, hz, gx, gy, gz, d0, d1, d2;
             site_field(A, c.ix.a, hx, hy, hz);
-            grad_batch<R, GEN>(A.M, T, c.ix.c1, c.ix.c2, c.ix.c3, c.ix.a, c.d.x, c.d.y, c.d.z, hx, hy, hz, sx, sy, sz, X,
-                               Y, Z, gx, gy, gz);
+            grad_table<R, GEN>(A.M, T, c.ix.a, c.s, A.nbr + A.nbo[c.r], c.d.w * A.M.na, hx, hy, hz, sx, sy, sz, X, Y, Z,
+                               gx, gy, gz);
             rhs_dipole<R>(sx, sy, sz, xx, xy, xz, gx, gy, gz, (R)dt, (R)lam, d0, d1, d2);
             const int g = c.off + c.s;
             A.D1[g] = d0; A.D1[NS + g] = d1; A.D1[2 * NS + g] = d2;
@@ -133,8 +137,8 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_heun
             batch_noise<R>(seed, c.r, step0 + step, c.s, scale, xx, xy, xz);
             R hx, hy, hz, gx, gy, gz, e0, e1, e2;
             site_field(A, c.ix.a, hx, hy, hz);
-            grad_batch<R, GEN>(A.M, T, c.ix.c1, c.ix.c2, c.ix.c3, c.ix.a, c.d.x, c.d.y, c.d.z, hx, hy, hz, px, py, pz, X,
-                               Y, Z, gx, gy, gz);
+            grad_table<R, GEN>(A.M, T, c.ix.a, c.s, A.nbr + A.nbo[c.r], c.d.w * A.M.na, hx, hy, hz, px, py, pz, X, Y, Z,
+                               gx, gy, gz);
             rhs_dipole<R>(px, py, pz, xx, xy, xz, gx, gy, gz, (R)dt, (R)lam, e0, e1, e2);
             R nx = A.S[g] + (A.D1[g] + e0) / 2;
             R ny = A.S[NS + g] + (A.D1[NS + g] + e1) / 2;
@@ -355,7 +359,7 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
             for (int k = 0; k < SGB_MAXT; k++) {
                 const int t = blockIdx.x + k * gridDim.x;
                 if (t >= A.ntiles) break;
-                double acc = 0.0;
+                R acc = 0;   // per-site terms in R; the warp, block and grid sums are FP64
                 const int r = A.tiles[t].x;
                 if (tile_has(A.tiles, t)) {
                     TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
@@ -368,11 +372,11 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                         normalize_dip<R>(hx, hy, hz, kap);
                         R fx, fy, fz, gx, gy, gz, dx, dy, dz;
                         site_field(A, c.ix.a, fx, fy, fz);
-                        grad_batch<R, GEN>(A.M, T, c.ix.c1, c.ix.c2, c.ix.c3, c.ix.a, c.d.x, c.d.y, c.d.z, fx, fy, fz, hx,
-                                           hy, hz, Hc + c.off, Hc + NS + c.off, Hc + 2 * NS + c.off, gx, gy, gz);
+                        grad_table<R, GEN>(A.M, T, c.ix.a, c.s, A.nbr + A.nbo[c.r], c.d.w * A.M.na, fx, fy, fz, hx, hy, hz,
+                                           Hc + c.off, Hc + NS + c.off, Hc + 2 * NS + c.off, gx, gy, gz);
                         rhs_dipole<R>(hx, hy, hz, (R)0, (R)0, (R)0, gx, gy, gz, (R)dt, (R)lam, dx, dy, dz);
                         R nx = sx + dx, ny = sy + dy, nz = sz + dz;
-                        double ex = (double)(qx - nx), ey = (double)(qy - ny), ez = (double)(qz - nz);
+                        R ex = qx - nx, ey = qy - ny, ez = qz - nz;
                         acc = ex * ex + ey * ey + ez * ez;
                         X.Sp[g] = nx; X.Sp[NS + g] = ny; X.Sp[2 * NS + g] = nz;
                         R mx = (sx + nx) / 2, my = (sy + ny) / 2, mz = (sz + nz) / 2;
@@ -390,10 +394,10 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                     }
                 }
                 if (act[k]) {
-                    // warp sum, then one shared-memory atomic per warp (tiles never straddle replicas)
+                    // warp sum, then one shared-memory FP64 atomic per warp (tiles never straddle replicas)
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-                    if ((threadIdx.x & 31) == 0) atomicAdd(&sacc[r], acc);
+                    if ((threadIdx.x & 31) == 0) atomicAdd(&sacc[r], (double)acc);
                 }
             }
             __syncthreads();
@@ -493,6 +497,8 @@ BatchArgs<R> bargs(sgb_batch* b) {
     A.rd = b->rd;
     A.roff = b->roff;
     A.pc = b->pc;
+    A.nbr = b->nbr;
+    A.nbo = b->nbo;
     A.NS = b->NS;
     A.kap = (const R*)b->kap;
     A.h = b->has_field ? (const R*)b->h : nullptr;
@@ -687,6 +693,8 @@ void sgb_batch_destroy(sgb_batch* b) {
     p = b->gstart; bfree(p); p = b->gcount; bfree(p); p = b->tiles; bfree(p); p = b->tfirst_d; bfree(p);
     p = b->tcount_d; bfree(p);
     p = b->pc; bfree(p);
+    p = b->nbr; bfree(p);
+    p = b->nbo; bfree(p);
     bfree(b->S); bfree(b->P); bfree(b->D1); bfree(b->Sp); bfree(b->H); bfree(b->Sc);
     p = b->racc; bfree(p); p = b->ctrl; bfree(p); p = b->Epart; bfree(p); p = b->E; bfree(p);
     p = b->counters; bfree(p); p = b->n_accept; bfree(p);
@@ -852,6 +860,51 @@ int sgb_batch_set_couplings(sgb_batch* b, const double* kappa, const double* g, 
     if ((rc = bmalloc(b, &b->tables, buf.size()))) return rc;
     BCK(cudaMemcpy(b->tables, buf.data(), buf.size(), cudaMemcpyHostToDevice));
     b->tables_bytes = (int)buf.size();
+    {
+        // neighbour tables: one per distinct replica size, [k][s] for bond k of the site's sublattice
+        const int off_boff = b->fp32 ? b->mf.off_boff : b->md.off_boff;
+        const int off_bonds = b->fp32 ? b->mf.off_bonds : b->md.off_bonds;
+        const size_t bsz = b->fp32 ? sizeof(DBond<float>) : sizeof(DBond<double>);
+        const size_t pk_off = b->fp32 ? offsetof(DBond<float>, pk) : offsetof(DBond<double>, pk);
+        const int* boff = reinterpret_cast<const int*>(buf.data() + off_boff);
+        int kb = 0;
+        for (int a = 0; a < na; a++) kb = std::max(kb, boff[a + 1] - boff[a]);
+        std::vector<int> table, nbo(b->nrep, 0);
+        std::vector<std::array<int, 4>> seen;   // (L1, L2, L3, offset)
+        for (int r = 0; r < b->nrep; r++) {
+            const int L1 = b->dims[3 * r], L2 = b->dims[3 * r + 1], L3 = b->dims[3 * r + 2];
+            int found = -1;
+            for (auto& e : seen)
+                if (e[0] == L1 && e[1] == L2 && e[2] == L3) found = e[3];
+            if (found >= 0) { nbo[r] = found; continue; }
+            const int nsr = L1 * L2 * L3 * na;
+            const int base = (int)table.size();
+            table.resize(table.size() + (size_t)std::max(kb, 1) * nsr, 0);
+            for (int a = 0; a < na; a++)
+                for (int c3 = 0; c3 < L3; c3++)
+                    for (int c2 = 0; c2 < L2; c2++)
+                        for (int c1 = 0; c1 < L1; c1++) {
+                            const int site = c1 + L1 * (c2 + L2 * (c3 + L3 * a));
+                            for (int k = 0; k < boff[a + 1] - boff[a]; k++) {
+                                int pk;
+                                std::memcpy(&pk, buf.data() + off_bonds + (size_t)(boff[a] + k) * bsz + pk_off, sizeof(int));
+                                int x1 = sgbhost::imod(c1 + (pk & 0xff) - 128, L1);
+                                int x2 = sgbhost::imod(c2 + ((pk >> 8) & 0xff) - 128, L2);
+                                int x3 = sgbhost::imod(c3 + ((pk >> 16) & 0xff) - 128, L3);
+                                int j = (int)((unsigned)pk >> 24);
+                                table[base + (size_t)k * nsr + site] = x1 + L1 * (x2 + L2 * (x3 + L3 * j));
+                            }
+                        }
+            seen.push_back({L1, L2, L3, base});
+            nbo[r] = base;
+        }
+        void* p;
+        p = b->nbr; bfree(p); p = b->nbo; bfree(p);
+        if ((rc = bmalloc(b, (void**)&b->nbr, sizeof(int) * std::max<size_t>(1, table.size())))) return rc;
+        if ((rc = bmalloc(b, (void**)&b->nbo, sizeof(int) * b->nrep))) return rc;
+        if (!table.empty()) BCK(cudaMemcpy(b->nbr, table.data(), sizeof(int) * table.size(), cudaMemcpyHostToDevice));
+        BCK(cudaMemcpy(b->nbo, nbo.data(), sizeof(int) * b->nrep, cudaMemcpyHostToDevice));
+    }
     for (Model<float>* m : {&b->mf}) { m->tables = (const unsigned char*)b->tables; m->dipole_mode = 1; m->na = na; }
     for (Model<double>* m : {&b->md}) { m->tables = (const unsigned char*)b->tables; m->dipole_mode = 1; m->na = na; }
     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }

@@ -219,3 +219,21 @@ __device__ inline double sgb_block_sum(double v) {
     }
     return r;
 }
+
+// Block-wide sum of per-thread terms given in the working precision R: warps reduce in R
+// (32 terms), the per-warp partials are summed in FP64. Result valid in thread 0.
+template <class R>
+__device__ inline double sgb_block_sum_r(R v) {
+    __shared__ double redr[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (l == 0) redr[w] = (double)v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < nw; k++) r += redr[k];
+    return r;
+}

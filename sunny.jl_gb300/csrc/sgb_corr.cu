@@ -34,8 +34,12 @@ __global__ void __launch_bounds__(256) k_corr_accum(const R* __restrict__ A, dou
                                                   int ncell, int nomega, int nrep, size_t rep_stride) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nrow = nobs * npos;
-    C2<R>* As = reinterpret_cast<C2<R>*>(smem_raw);          // [nrep][nrow][QT]
-    int* pr = reinterpret_cast<int*>(As + (size_t)nrep * nrow * QT);
+    // Shared layout [rep][ql][obs][pos], each observable block padded by one element: the
+    // threads of a warp read different (obs, pos) at one ql, which then fall in distinct
+    // banks instead of a 256-byte stride on one bank.
+    const int rowpad = nobs * (npos + 1);
+    C2<R>* As = reinterpret_cast<C2<R>*>(smem_raw);          // [nrep][QT][rowpad]
+    int* pr = reinterpret_cast<int*>(As + (size_t)nrep * QT * rowpad);
     const int w = blockIdx.y;
     const int q0 = blockIdx.x * QT;
     const int nq = min(QT, ncell - q0);
@@ -48,7 +52,8 @@ __global__ void __launch_bounds__(256) k_corr_accum(const R* __restrict__ A, dou
             v.x = A[2 * idx];
             v.y = A[2 * idx + 1];
         }
-        As[e] = v;
+        const int o = row / npos, p = row - o * npos;
+        As[((size_t)r * QT + ql) * rowpad + o * (npos + 1) + p] = v;
     }
     for (int e = threadIdx.x; e < 2 * ncorr; e += blockDim.x) pr[e] = pairs[e];
     __syncthreads();
@@ -68,11 +73,10 @@ __global__ void __launch_bounds__(256) k_corr_accum(const R* __restrict__ A, dou
         if (k < nk && r < B) {
             int c = r % ncorr, t = r / ncorr;
             int i = t % npos, j = t / npos;
-            ia[k] = (pr[2 * c] * npos + i) * QT;
-            ib[k] = (pr[2 * c + 1] * npos + j) * QT;
+            ia[k] = pr[2 * c] * (npos + 1) + i;
+            ib[k] = pr[2 * c + 1] * (npos + 1) + j;
         }
     }
-    const int rstride = nrow * QT;
     for (int ql = 0; ql < nq; ql++) {
         double2* row = out + (size_t)ql * B;
         double2 acc[KMAX];
@@ -84,8 +88,9 @@ __global__ void __launch_bounds__(256) k_corr_accum(const R* __restrict__ A, dou
             if (ia[k] < 0) continue;
             R sre = 0, sim = 0;
             for (int rr = 0; rr < nrep; rr++) {
-                C2<R> a = As[rr * rstride + ia[k] + ql];
-                C2<R> b = As[rr * rstride + ib[k] + ql];
+                const C2<R>* Ar = As + ((size_t)rr * QT + ql) * rowpad;
+                C2<R> a = Ar[ia[k]];
+                C2<R> b = Ar[ib[k]];
                 // conj(a) * b
                 sre += a.x * b.x + a.y * b.y;
                 sim += a.x * b.y - a.y * b.x;
@@ -147,7 +152,7 @@ template <class R>
 int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
                       int nrep, size_t rep_stride, cudaStream_t st) {
     constexpr int QT = 32;
-    size_t smem = (size_t)nrep * nobs * npos * QT * sizeof(C2<R>) + 2 * ncorr * sizeof(int) + 16;
+    size_t smem = (size_t)nrep * nobs * (npos + 1) * QT * sizeof(C2<R>) + 2 * ncorr * sizeof(int) + 16;
     if (smem > 200 * 1024) return SGB_ERR_ARG;
     if (ncorr * npos * npos > 8 * 256) return SGB_ERR_ARG;   // at most 8 accumulator entries per thread and row
     if (smem > 48 * 1024) {

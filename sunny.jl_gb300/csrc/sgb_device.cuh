@@ -273,6 +273,69 @@ __device__ inline void grad_batch(const Model<R>& M, const Tab<R>& T, int c1, in
     }
 }
 
+// Table form: the neighbour of local site s along the k-th bond of its sublattice is
+// nb[k * nsr + s] (precomputed with the periodic wrap), so a bond costs one coalesced
+// index load instead of the wrap arithmetic. Used by the replica-batch kernels.
+template <class R, bool GEN>
+__device__ inline void grad_table(const Model<R>& M, const Tab<R>& T, int a, int s, const int* nb, int nsr,
+                                  R hx, R hy, R hz, R sx, R sy, R sz, const R* X, const R* Y, const R* Zc,
+                                  R& gx, R& gy, R& gz) {
+    gx = hx; gy = hy; gz = hz;
+    {
+        int km = T.kmax[a];
+        if (km > 0) classical_aniso<R>(T.stev + 28 * a, km, sx, sy, sz, gx, gy, gz);
+    }
+    const int b0 = T.boff[a], b1 = T.boff[a + 1];
+    constexpr int G = 6;
+    for (int b = b0; b < b1; b += G) {
+        int js[G];
+#pragma unroll
+        for (int k = 0; k < G; k++)
+            if (b + k < b1) js[k] = __ldg(nb + (size_t)(b + k - b0) * nsr + s);
+        R tx[G], ty[G], tz[G];
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            if (b + k < b1) { tx[k] = sgb_ld(X + js[k]); ty[k] = sgb_ld(Y + js[k]); tz[k] = sgb_ld(Zc + js[k]); }
+        }
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            if (b + k >= b1) break;
+            const DBond<R>& B = T.bonds[b + k];
+            if (!GEN) {
+                R j = B.J[0];
+                gx += j * tx[k]; gy += j * ty[k]; gz += j * tz[k];
+                continue;
+            }
+            if (B.jkind == 0) {
+                R j = B.J[0];
+                gx += j * tx[k]; gy += j * ty[k]; gz += j * tz[k];
+            } else {
+                gx += B.J[0] * tx[k] + B.J[3] * ty[k] + B.J[6] * tz[k];
+                gy += B.J[1] * tx[k] + B.J[4] * ty[k] + B.J[7] * tz[k];
+                gz += B.J[2] * tx[k] + B.J[5] * ty[k] + B.J[8] * tz[k];
+            }
+            if (M.dipole_mode && B.bqkind != 0) {
+                R Qj[5], v[5];
+                quad5<R>(tx[k], ty[k], tz[k], Qj);
+                if (B.bqkind == 1) {
+#pragma unroll
+                    for (int q = 0; q < 5; q++) v[q] = B.bq * ((R)biquad_metric(q) * Qj[q]);
+                } else {
+                    const R* Bm = T.bq + 25 * B.bqidx;
+#pragma unroll
+                    for (int q = 0; q < 5; q++) {
+                        R acc = 0;
+#pragma unroll
+                        for (int p = 0; p < 5; p++) acc += Bm[q + 5 * p] * Qj[p];
+                        v[q] = acc;
+                    }
+                }
+                add_quad_grad<R>(sx, sy, sz, v, gx, gy, gz);
+            }
+        }
+    }
+}
+
 // Single-system form: per-site Zeeman field from M.h, offsets pre-reduced mod dims.
 template <class R>
 __device__ inline void grad_site(const Model<R>& M, const Tab<R>& T, int site, const SiteIdx& ix,

@@ -137,7 +137,7 @@ k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, doub
             const R* Hc = H + (size_t)cur * 3 * ns;
             R* Hn = H + (size_t)nxt * 3 * ns;
             R* Hs = H + (size_t)nst * 3 * ns;
-            double acc = 0.0;
+            R acc = 0;   // per-site terms in R, block and grid sums in FP64
 #pragma unroll
             for (int k = 0; k < SPT; k++) {
                 int site = tid + k * nthr;
@@ -150,7 +150,7 @@ k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, doub
                 grad_site<R>(M, T, site, ix, hx, hy, hz, Hc, Hc + ns, Hc + 2 * ns, gx, gy, gz);
                 rhs_dipole<R>(hx, hy, hz, (R)0, (R)0, (R)0, gx, gy, gz, dt, lam, dx, dy, dz);
                 R qx = s[k][0] + dx, qy = s[k][1] + dy, qz = s[k][2] + dz;
-                double ex = (double)(sp[k][0] - qx), ey = (double)(sp[k][1] - qy), ez = (double)(sp[k][2] - qz);
+                R ex = sp[k][0] - qx, ey = sp[k][1] - qy, ez = sp[k][2] - qz;
                 acc += ex * ex + ey * ey + ez * ez;
                 sp[k][0] = qx; sp[k][1] = qy; sp[k][2] = qz;
                 // candidate midpoint for the next iteration
@@ -165,7 +165,7 @@ k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, doub
                 normalize_dip<R>(mx, my, mz, kap);
                 Hs[site] = mx; Hs[ns + site] = my; Hs[2 * ns + site] = mz;
             }
-            double bsum = sgb_block_sum(acc);
+            double bsum = sgb_block_sum_r<R>(acc);
             const int slot = (int)(itg % 3);
             if (threadIdx.x == 0) atomicAdd(&ctrl->acc[slot], bsum);
             if (leader) { ctrl->acc[(slot + 1) % 3] = 0.0; ctrl->iters += 1; }

@@ -116,6 +116,8 @@ struct sgb_batch {
     int* tfirst_d = nullptr;
     int* tcount_d = nullptr;
     int* pc = nullptr;              // [NS] packed site coordinates
+    int* nbr = nullptr;             // neighbour tables, one per distinct replica size
+    int* nbo = nullptr;             // [nrep] offset of each replica's table in nbr
     // state
     void* S = nullptr;
     void* P = nullptr;

@@ -408,7 +408,7 @@ k_sun_midpoint(Model<R> M, R* Z, R* D, R* Qb, R* H, R* QH, Ctrl* ctrl, int nstep
             const int nxt = (cur + 1) % 3, nst = (cur + 2) % 3;
             const R* Hc = H + (size_t)cur * 3 * ns;
             const R* Qc = QH + (size_t)cur * 5 * ns;
-            double acc = 0.0;
+            R acc = 0;   // per-site terms in R, block and grid sums in FP64
 #pragma unroll
             for (int k = 0; k < SPT; k++) {
                 int site = tid + k * nthr;
@@ -422,7 +422,7 @@ k_sun_midpoint(Model<R> M, R* Z, R* D, R* Qb, R* H, R* QH, Ctrl* ctrl, int nstep
 #pragma unroll
                 for (int c = 0; c < 2 * N; c++) {
                     R q = z[k][c] + dz[c];
-                    double e = (double)(zp[k][c] - q);
+                    R e = zp[k][c] - q;
                     acc += e * e;
                     zp[k][c] = q;
                 }
@@ -436,7 +436,7 @@ k_sun_midpoint(Model<R> M, R* Z, R* D, R* Qb, R* H, R* QH, Ctrl* ctrl, int nstep
                 for (int c = 0; c < 2 * N; c++) zb[c] = (zc[k][c] + zc[k][c]) / 2;
                 publish<R, N, BQ>(sc, S.qm, zb, ns, site, H + (size_t)nst * 3 * ns, QH + (size_t)nst * 5 * ns);
             }
-            double bsum = sgb_block_sum(acc);
+            double bsum = sgb_block_sum_r<R>(acc);
             const int slot = (int)(itg % 3);
             if (threadIdx.x == 0) atomicAdd(&ctrl->acc[slot], bsum);
             if (leader) { ctrl->acc[(slot + 1) % 3] = 0.0; ctrl->iters += 1; }
