@@ -353,10 +353,12 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2, help="samples timed on the plain FP64 path (0 skips it)")
     ap.add_argument("--L", type=int, default=16, help="cells per axis (16 is the benchmark; smaller for profiling)")
     ap.add_argument("--nrep", type=int, default=8, help="replicas sampled per batched add_sample")
+    ap.add_argument("--nomega", type=int, default=200, help="energy bins (200 is the benchmark; fewer for profiling)")
     ap.add_argument("--no-extra", action="store_true", help="skip the tempering and Langevin site-step arms")
     args = ap.parse_args()
-    global L
+    global L, NOMEGA
     L = args.L
+    NOMEGA = args.nomega
     if args.warmup < 3:
         args.warmup = 3
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -463,8 +465,9 @@ def main():
             "clocks": rb["clocks"],
             "e2e": {"value": e2e_val, "unit": "samples/s", "h2d_bytes_per_step": rb["h2d"],
                     "d2h_bytes_per_step": rb["d2h"]}}
-    if L != 16:
-        line["config"]["workload"] = f"REDUCED SIZE L={L} (profiling case, not the benchmark): " + line["config"]["workload"]
+    if L != 16 or NOMEGA != 200:
+        line["config"]["workload"] = (f"REDUCED SIZE L={L}, nw={NOMEGA} (profiling case, not the benchmark): "
+                                      + line["config"]["workload"])
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, cores, t_step = cpu_baseline(1, 20, 12)
         line["cpu_baseline"] = {"value": v, "unit": "samples/s", "cores": cores, "kind": "port",

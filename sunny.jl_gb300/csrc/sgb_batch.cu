@@ -45,6 +45,8 @@ struct BatchArgs {
     const int* pc;      // [NS] packed (c1 | c2<<8 | c3<<16 | atom<<24) of every site
     const int* nbr;     // neighbour tables
     const int* nbo;     // [nrep] table offset of each replica
+    const int4* td;     // [ntiles][2] descriptors: (replica, first site, count, uniform atom or -1),
+                        //                          (replica offset, replica sites, table offset, 0)
     int NS;
     const R* kap;       // [na]
     const R* h;         // [3][na] or nullptr
@@ -77,6 +79,19 @@ __device__ __forceinline__ TileCtx tile_ctx(const int4* tiles, const int4* rd, c
 
 __device__ __forceinline__ bool tile_has(const int4* tiles, int t) { return (int)threadIdx.x < tiles[t].z; }
 
+// Per-tile context from the two-int4 descriptor (one 32-byte load, no coordinate math).
+struct TileD {
+    int r, s, cnt, a, off, nsr, nbo;
+};
+__device__ __forceinline__ TileD tile_d(const int4* td, const int* pc, int t) {
+    int4 u = td[2 * t], v = td[2 * t + 1];
+    TileD c;
+    c.r = u.x; c.s = u.y + threadIdx.x; c.cnt = u.z; c.a = u.w;
+    c.off = v.x; c.nsr = v.y; c.nbo = v.z;
+    if (c.a < 0 && (int)threadIdx.x < c.cnt) c.a = (int)((unsigned)pc[c.off + c.s] >> 24);
+    return c;
+}
+
 template <class R>
 __device__ __forceinline__ void site_field(const BatchArgs<R>& A, int a, R& hx, R& hy, R& hz) {
     if (A.h) { hx = A.h[a]; hy = A.h[A.M.na + a]; hz = A.h[2 * A.M.na + a]; }
@@ -101,8 +116,8 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_heun
     const int NS = A.NS;
     for (int step = 0; step < nsteps; ++step) {
         for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
-            if (!tile_has(A.tiles, t)) continue;
-            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
+            TileD c = tile_d(A.td, A.pc, t);
+            if ((int)threadIdx.x >= c.cnt) continue;
             const R* X = A.S + c.off;
             const R* Y = A.S + NS + c.off;
             const R* Z = A.S + 2 * NS + c.off;
@@ -112,20 +127,19 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_heun
             R xx, xy, xz;
             batch_noise<R>(seed, c.r, step0 + step, c.s, scale, xx, xy, xz);
             R hx, hy, hz, gx, gy, gz, d0, d1, d2;
-            site_field(A, c.ix.a, hx, hy, hz);
-            grad_table<R, GEN>(A.M, T, c.ix.a, c.s, A.nbr + A.nbo[c.r], c.d.w * A.M.na, hx, hy, hz, sx, sy, sz, X, Y, Z,
-                               gx, gy, gz);
+            site_field(A, c.a, hx, hy, hz);
+            grad_table<R, GEN>(A.M, T, c.a, c.s, A.nbr + c.nbo, c.nsr, hx, hy, hz, sx, sy, sz, X, Y, Z, gx, gy, gz);
             rhs_dipole<R>(sx, sy, sz, xx, xy, xz, gx, gy, gz, (R)dt, (R)lam, d0, d1, d2);
             const int g = c.off + c.s;
             A.D1[g] = d0; A.D1[NS + g] = d1; A.D1[2 * NS + g] = d2;
             R px = sx + d0, py = sy + d1, pz = sz + d2;
-            normalize_dip<R>(px, py, pz, A.kap[c.ix.a]);
+            normalize_dip<R>(px, py, pz, A.kap[c.a]);
             A.P[g] = px; A.P[NS + g] = py; A.P[2 * NS + g] = pz;
         }
         if (!sgb_grid_barrier(A.ctrl, gridDim.x)) return;
         for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
-            if (!tile_has(A.tiles, t)) continue;
-            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
+            TileD c = tile_d(A.td, A.pc, t);
+            if ((int)threadIdx.x >= c.cnt) continue;
             const int g = c.off + c.s;
             const R* X = A.P + c.off;
             const R* Y = A.P + NS + c.off;
@@ -136,14 +150,13 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_heun
             R xx, xy, xz;
             batch_noise<R>(seed, c.r, step0 + step, c.s, scale, xx, xy, xz);
             R hx, hy, hz, gx, gy, gz, e0, e1, e2;
-            site_field(A, c.ix.a, hx, hy, hz);
-            grad_table<R, GEN>(A.M, T, c.ix.a, c.s, A.nbr + A.nbo[c.r], c.d.w * A.M.na, hx, hy, hz, px, py, pz, X, Y, Z,
-                               gx, gy, gz);
+            site_field(A, c.a, hx, hy, hz);
+            grad_table<R, GEN>(A.M, T, c.a, c.s, A.nbr + c.nbo, c.nsr, hx, hy, hz, px, py, pz, X, Y, Z, gx, gy, gz);
             rhs_dipole<R>(px, py, pz, xx, xy, xz, gx, gy, gz, (R)dt, (R)lam, e0, e1, e2);
             R nx = A.S[g] + (A.D1[g] + e0) / 2;
             R ny = A.S[NS + g] + (A.D1[NS + g] + e1) / 2;
             R nz = A.S[2 * NS + g] + (A.D1[2 * NS + g] + e2) / 2;
-            normalize_dip<R>(nx, ny, nz, A.kap[c.ix.a]);
+            normalize_dip<R>(nx, ny, nz, A.kap[c.a]);
             A.S[g] = nx; A.S[NS + g] = ny; A.S[2 * NS + g] = nz;
         }
         if (step + 1 < nsteps) {
@@ -360,20 +373,20 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                 const int t = blockIdx.x + k * gridDim.x;
                 if (t >= A.ntiles) break;
                 R acc = 0;   // per-site terms in R; the warp, block and grid sums are FP64
-                const int r = A.tiles[t].x;
-                if (tile_has(A.tiles, t)) {
-                    TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
+                TileD c = tile_d(A.td, A.pc, t);
+                const int r = c.r;
+                if ((int)threadIdx.x < c.cnt) {
                     const int g = c.off + c.s;
                     if (act[k]) {
-                        const R kap = A.kap[c.ix.a];
+                        const R kap = A.kap[c.a];
                         R sx = A.S[g], sy = A.S[NS + g], sz = A.S[2 * NS + g];
                         R qx = X.Sp[g], qy = X.Sp[NS + g], qz = X.Sp[2 * NS + g];
                         R hx = (sx + qx) / 2, hy = (sy + qy) / 2, hz = (sz + qz) / 2;
                         normalize_dip<R>(hx, hy, hz, kap);
                         R fx, fy, fz, gx, gy, gz, dx, dy, dz;
-                        site_field(A, c.ix.a, fx, fy, fz);
-                        grad_table<R, GEN>(A.M, T, c.ix.a, c.s, A.nbr + A.nbo[c.r], c.d.w * A.M.na, fx, fy, fz, hx, hy, hz,
-                                           Hc + c.off, Hc + NS + c.off, Hc + 2 * NS + c.off, gx, gy, gz);
+                        site_field(A, c.a, fx, fy, fz);
+                        grad_table<R, GEN>(A.M, T, c.a, c.s, A.nbr + c.nbo, c.nsr, fx, fy, fz, hx, hy, hz, Hc + c.off,
+                                           Hc + NS + c.off, Hc + 2 * NS + c.off, gx, gy, gz);
                         rhs_dipole<R>(hx, hy, hz, (R)0, (R)0, (R)0, gx, gy, gz, (R)dt, (R)lam, dx, dy, dz);
                         R nx = sx + dx, ny = sy + dy, nz = sz + dz;
                         R ex = qx - nx, ey = qy - ny, ez = qz - nz;
@@ -499,6 +512,7 @@ BatchArgs<R> bargs(sgb_batch* b) {
     A.pc = b->pc;
     A.nbr = b->nbr;
     A.nbo = b->nbo;
+    A.td = b->td;
     A.NS = b->NS;
     A.kap = (const R*)b->kap;
     A.h = b->has_field ? (const R*)b->h : nullptr;
@@ -695,6 +709,7 @@ void sgb_batch_destroy(sgb_batch* b) {
     p = b->pc; bfree(p);
     p = b->nbr; bfree(p);
     p = b->nbo; bfree(p);
+    p = b->td; bfree(p);
     bfree(b->S); bfree(b->P); bfree(b->D1); bfree(b->Sp); bfree(b->H); bfree(b->Sc);
     p = b->racc; bfree(p); p = b->ctrl; bfree(p); p = b->Epart; bfree(p); p = b->E; bfree(p);
     p = b->counters; bfree(p); p = b->n_accept; bfree(p);
@@ -904,6 +919,20 @@ int sgb_batch_set_couplings(sgb_batch* b, const double* kappa, const double* g, 
         if ((rc = bmalloc(b, (void**)&b->nbo, sizeof(int) * b->nrep))) return rc;
         if (!table.empty()) BCK(cudaMemcpy(b->nbr, table.data(), sizeof(int) * table.size(), cudaMemcpyHostToDevice));
         BCK(cudaMemcpy(b->nbo, nbo.data(), sizeof(int) * b->nrep, cudaMemcpyHostToDevice));
+        // tile descriptors
+        std::vector<int4> td(2 * (size_t)b->ntiles);
+        std::vector<int4> tl(b->ntiles);
+        BCK(cudaMemcpy(tl.data(), b->tiles, sizeof(int4) * b->ntiles, cudaMemcpyDeviceToHost));
+        for (int t = 0; t < b->ntiles; t++) {
+            const int r = tl[t].x, s0 = tl[t].y, cnt = tl[t].z;
+            const int ncell = b->dims[3 * r] * b->dims[3 * r + 1] * b->dims[3 * r + 2];
+            const int a0 = s0 / ncell, a1 = (s0 + cnt - 1) / ncell;
+            td[2 * t] = make_int4(r, s0, cnt, a0 == a1 ? a0 : -1);
+            td[2 * t + 1] = make_int4(b->off[r], b->off[r + 1] - b->off[r], nbo[r], 0);
+        }
+        p = b->td; bfree(p);
+        if ((rc = bmalloc(b, (void**)&b->td, sizeof(int4) * td.size()))) return rc;
+        BCK(cudaMemcpy(b->td, td.data(), sizeof(int4) * td.size(), cudaMemcpyHostToDevice));
     }
     for (Model<float>* m : {&b->mf}) { m->tables = (const unsigned char*)b->tables; m->dipole_mode = 1; m->na = na; }
     for (Model<double>* m : {&b->md}) { m->tables = (const unsigned char*)b->tables; m->dipole_mode = 1; m->na = na; }

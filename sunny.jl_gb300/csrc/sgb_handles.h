@@ -118,6 +118,7 @@ struct sgb_batch {
     int* pc = nullptr;              // [NS] packed site coordinates
     int* nbr = nullptr;             // neighbour tables, one per distinct replica size
     int* nbo = nullptr;             // [nrep] offset of each replica's table in nbr
+    int4* td = nullptr;             // [ntiles][2] tile descriptors
     // state
     void* S = nullptr;
     void* P = nullptr;
