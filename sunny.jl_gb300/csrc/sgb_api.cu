@@ -93,6 +93,32 @@ int build_tables(sgb_system* s, Model<R>& M) {
     CK(cudaMemcpy(s->tables, buf.data(), buf.size(), cudaMemcpyHostToDevice));
     s->tables_bytes = (int)buf.size();
     s->has_biquad = any_bq;
+    {
+        // neighbour table [k][site] for the k-th bond of each site's sublattice
+        const int na = s->d.natoms, L1 = s->d.dims[0], L2 = s->d.dims[1], L3 = s->d.dims[2];
+        const int* boff = reinterpret_cast<const int*>(buf.data() + M.off_boff);
+        const DBond<R>* bonds = reinterpret_cast<const DBond<R>*>(buf.data() + M.off_bonds);
+        int kb = 1;
+        for (int a = 0; a < na; a++) kb = std::max(kb, boff[a + 1] - boff[a]);
+        std::vector<int> tab((size_t)kb * s->ns, 0);
+        for (int a = 0; a < na; a++)
+            for (int c3 = 0; c3 < L3; c3++)
+                for (int c2 = 0; c2 < L2; c2++)
+                    for (int c1 = 0; c1 < L1; c1++) {
+                        const int site = c1 + L1 * (c2 + L2 * (c3 + L3 * a));
+                        for (int k = 0; k < boff[a + 1] - boff[a]; k++) {
+                            const DBond<R>& B = bonds[boff[a] + k];
+                            int x1 = (c1 + B.n[0]) % L1, x2 = (c2 + B.n[1]) % L2, x3 = (c3 + B.n[2]) % L3;
+                            tab[(size_t)k * s->ns + site] = x1 + L1 * (x2 + L2 * (x3 + L3 * B.j));
+                        }
+                    }
+        void* p = s->nbr;
+        dfree(p);
+        s->nbr = nullptr;
+        if ((rc = dmalloc(s, (void**)&s->nbr, sizeof(int) * tab.size()))) return rc;
+        CK(cudaMemcpy(s->nbr, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice));
+        M.nbr = s->nbr;
+    }
     M.L1 = s->d.dims[0]; M.L2 = s->d.dims[1]; M.L3 = s->d.dims[2];
     M.ns = s->ns; M.ncell = s->ncell;
     M.kappa = reinterpret_cast<const R*>(s->kappa);
@@ -315,7 +341,8 @@ int sgb_create(const sgb_desc* d, sgb_system** out) {
 void sgb_destroy(sgb_system* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
-    dfree(s->kappa); dfree(s->h); dfree(s->tables); dfree(s->S); dfree(s->P); dfree(s->H);
+    dfree(s->kappa); dfree(s->h); dfree(s->tables);
+    { void* p = s->nbr; dfree(p); } dfree(s->S); dfree(s->P); dfree(s->H);
     dfree(s->Z); dfree(s->Q); dfree(s->QP); dfree(s->QH);
     void* p = s->ctrl; dfree(p);
     p = s->partials; dfree(p);

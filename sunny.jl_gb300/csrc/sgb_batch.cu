@@ -108,10 +108,11 @@ __device__ __forceinline__ void batch_noise(uint64_t seed, int r, uint64_t step,
 
 // Heun over every replica (Integrators.jl:313-332); each replica uses its own kT.
 template <class R, bool GEN>
-__global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_heun(BatchArgs<R> A, const double* kT, int nsteps, double dt,
-                                                            double lam, uint64_t seed, unsigned long long* counters) {
+__global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_heun(BatchArgs<R> A, const R* kTR, int nsteps, R dt,
+                                                            R lam, uint64_t seed, unsigned long long* counters) {
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(A.M, smem);
+    const R two_dt_lam = 2 * dt * lam;   // noise variance per unit kT (fill_noise!, Integrators.jl:288-298)
     const uint64_t step0 = *((volatile unsigned long long*)counters);
     const int NS = A.NS;
     for (int step = 0; step < nsteps; ++step) {
@@ -122,14 +123,14 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_heun
             const R* Y = A.S + NS + c.off;
             const R* Z = A.S + 2 * NS + c.off;
             R sx = X[c.s], sy = Y[c.s], sz = Z[c.s];
-            const double kt = kT[c.r];
-            R scale = (lam == 0.0 || kt == 0.0) ? (R)0 : (R)sqrt(2 * dt * lam * kt);
+            const R kt = kTR[c.r];
+            R scale = (lam == (R)0 || kt == (R)0) ? (R)0 : sgb_sqrt<R>(two_dt_lam * kt);
             R xx, xy, xz;
             batch_noise<R>(seed, c.r, step0 + step, c.s, scale, xx, xy, xz);
             R hx, hy, hz, gx, gy, gz, d0, d1, d2;
             site_field(A, c.a, hx, hy, hz);
             grad_table<R, GEN>(A.M, T, c.a, c.s, A.nbr + c.nbo, c.nsr, hx, hy, hz, sx, sy, sz, X, Y, Z, gx, gy, gz);
-            rhs_dipole<R>(sx, sy, sz, xx, xy, xz, gx, gy, gz, (R)dt, (R)lam, d0, d1, d2);
+            rhs_dipole<R>(sx, sy, sz, xx, xy, xz, gx, gy, gz, dt, lam, d0, d1, d2);
             const int g = c.off + c.s;
             A.D1[g] = d0; A.D1[NS + g] = d1; A.D1[2 * NS + g] = d2;
             R px = sx + d0, py = sy + d1, pz = sz + d2;
@@ -145,14 +146,14 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_heun
             const R* Y = A.P + NS + c.off;
             const R* Z = A.P + 2 * NS + c.off;
             R px = X[c.s], py = Y[c.s], pz = Z[c.s];
-            const double kt = kT[c.r];
-            R scale = (lam == 0.0 || kt == 0.0) ? (R)0 : (R)sqrt(2 * dt * lam * kt);
+            const R kt = kTR[c.r];
+            R scale = (lam == (R)0 || kt == (R)0) ? (R)0 : sgb_sqrt<R>(two_dt_lam * kt);
             R xx, xy, xz;
             batch_noise<R>(seed, c.r, step0 + step, c.s, scale, xx, xy, xz);
             R hx, hy, hz, gx, gy, gz, e0, e1, e2;
             site_field(A, c.a, hx, hy, hz);
             grad_table<R, GEN>(A.M, T, c.a, c.s, A.nbr + c.nbo, c.nsr, hx, hy, hz, px, py, pz, X, Y, Z, gx, gy, gz);
-            rhs_dipole<R>(px, py, pz, xx, xy, xz, gx, gy, gz, (R)dt, (R)lam, e0, e1, e2);
+            rhs_dipole<R>(px, py, pz, xx, xy, xz, gx, gy, gz, dt, lam, e0, e1, e2);
             R nx = A.S[g] + (A.D1[g] + e0) / 2;
             R ny = A.S[NS + g] + (A.D1[NS + g] + e1) / 2;
             R nz = A.S[2 * NS + g] + (A.D1[2 * NS + g] + e2) / 2;
@@ -237,8 +238,9 @@ __global__ void k_batch_reduce(const double* Epart, const int* tfirst, const int
 // (group-major); ladder[p] is the replica currently at slot p, which holds kT[ladder[p]].
 // exch_start <= 0 takes the round from counters[1] (step_ensemble! alternation).
 __global__ void k_batch_exchange(int ngroups, const int* gstart, const int* gcount, int* ladder, double* kT,
-                                 const double* E, int exch_start, uint64_t seed, uint64_t round_arg,
-                                 unsigned long long* counters, const double* uniforms, long long* n_accept) {
+                                 void* kTR, int rbytes, const double* E, int exch_start, uint64_t seed,
+                                 uint64_t round_arg, unsigned long long* counters, const double* uniforms,
+                                 long long* n_accept) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     uint64_t round = round_arg;
     int start = exch_start;
@@ -269,6 +271,8 @@ __global__ void k_batch_exchange(int ngroups, const int* gstart, const int* gcou
             if (lnP >= 0 || u < exp(lnP)) {
                 kT[r1] = kT2;
                 kT[r2] = kT1;
+                if (rbytes == 4) { ((float*)kTR)[r1] = (float)kT2; ((float*)kTR)[r2] = (float)kT1; }
+                else { ((double*)kTR)[r1] = kT2; ((double*)kTR)[r2] = kT1; }
                 ladder[p] = r2;
                 ladder[p + 1] = r1;
                 n_accept[p] += 1;
@@ -324,11 +328,12 @@ __device__ __forceinline__ void snap_write(const BSnap<R>& sn, int r, int t, int
 #define SGB_MAXREP_CORR 64
 
 template <class R, bool GEN>
-__global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midpoint(BatchArgs<R> A, MidArgs<R> X, int nsteps, double dt,
-                                                                double lam, BSnap<R> sn) {
+__global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midpoint(BatchArgs<R> A, MidArgs<R> X, int nsteps, R dt,
+                                                                R lam, BSnap<R> sn) {
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(A.M, smem);
     __shared__ double sacc[SGB_MAXREP_CORR];
+    __shared__ unsigned long long conv_mask;   // bit q: replica q met the tolerance this iteration
     const int NS = A.NS;
     const bool leader = (blockIdx.x == 0 && threadIdx.x == 0);
     bool act[SGB_MAXT];
@@ -387,7 +392,7 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                         site_field(A, c.a, fx, fy, fz);
                         grad_table<R, GEN>(A.M, T, c.a, c.s, A.nbr + c.nbo, c.nsr, fx, fy, fz, hx, hy, hz, Hc + c.off,
                                            Hc + NS + c.off, Hc + 2 * NS + c.off, gx, gy, gz);
-                        rhs_dipole<R>(hx, hy, hz, (R)0, (R)0, (R)0, gx, gy, gz, (R)dt, (R)lam, dx, dy, dz);
+                        rhs_dipole<R>(hx, hy, hz, (R)0, (R)0, (R)0, gx, gy, gz, dt, lam, dx, dy, dz);
                         R nx = sx + dx, ny = sy + dy, nz = sz + dz;
                         R ex = qx - nx, ey = qy - ny, ez = qz - nz;
                         acc = ex * ex + ey * ey + ez * ez;
@@ -422,14 +427,21 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
             }
             if (!sgb_grid_barrier(A.ctrl, gridDim.x)) return;
             itg++;
-            all_done = true;
-            for (int q = 0; q < X.nrep; q++)
-                if (!(X.racc[slot * X.nrep + q] <= X.atol2)) { all_done = false; break; }
+            // one thread per block compares the FP64 sums with the tolerance
+            if (threadIdx.x == 0) {
+                unsigned long long m = 0;
+                for (int q = 0; q < X.nrep; q++)
+                    if (X.racc[slot * X.nrep + q] <= X.atol2) m |= 1ull << q;
+                conv_mask = m;
+            }
+            __syncthreads();
+            const unsigned long long mask = conv_mask;
+            all_done = (X.nrep == 64) ? (mask == ~0ull) : (mask == ((1ull << X.nrep) - 1));
             for (int k = 0; k < SGB_MAXT; k++) {
                 const int t = blockIdx.x + k * gridDim.x;
                 if (t >= A.ntiles) break;
                 const int r = A.tiles[t].x;
-                if (act[k] && X.racc[slot * X.nrep + r] <= X.atol2) {
+                if (act[k] && ((mask >> r) & 1ull)) {
                     act[k] = false;
                     if (tile_has(A.tiles, t)) {
                         const int g = A.roff[r] + A.tiles[t].y + threadIdx.x;
@@ -559,9 +571,10 @@ int enqueue_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, int
     BatchArgs<R> A = bargs<R>(b);
     int grid = 0;
     size_t smem = (size_t)b->tables_bytes;
-    double* kT = b->kT;
+    const R* kTR = reinterpret_cast<const R*>(b->kTR);
     unsigned long long* ctr = b->counters;
-    void* args[] = {&A, &kT, &nsteps, &dt, &damping, &seed, &ctr};
+    R rdt = (R)dt, rlam = (R)damping;
+    void* args[] = {&A, &kTR, &nsteps, &rdt, &rlam, &seed, &ctr};
     if (A.M.general) {
         int rc = bgrid(b, k_batch_heun<R, true>, smem, 0, &grid);
         return rc ? rc : bcoop(b, k_batch_heun<R, true>, grid, smem, args);
@@ -585,8 +598,9 @@ int enqueue_energy(sgb_batch* b) {
 }
 
 int enqueue_exchange(sgb_batch* b, int exch_start, uint64_t seed, uint64_t round, const double* uniforms_dev) {
-    k_batch_exchange<<<1, 32, 0, b->stream>>>(b->ngroups, b->gstart, b->gcount, b->ladder, b->kT, b->E, exch_start, seed,
-                                              round, b->counters, uniforms_dev, b->n_accept);
+    k_batch_exchange<<<1, 32, 0, b->stream>>>(b->ngroups, b->gstart, b->gcount, b->ladder, b->kT, b->kTR,
+                                              (int)bsize(b), b->E, exch_start, seed, round, b->counters, uniforms_dev,
+                                              b->n_accept);
     b->launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? SGB_OK : bfail(b, SGB_ERR_CUDA, std::string("exchange launch: ") + cudaGetErrorString(e));
@@ -663,7 +677,7 @@ static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
     size_t smem = (size_t)b->tables_bytes;
     if (b->nrep > SGB_MAXREP_CORR) return bfail(b, SGB_ERR_ARG, "batched sampling supports at most 64 replicas");
     BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
-    double dt = c->dt, lam = c->damping;
+    R dt = (R)c->dt, lam = (R)c->damping;
     void* args[] = {&A, &X, &nsteps, &dt, &lam, &sn};
     int rc;
     if (A.M.general) {
@@ -703,7 +717,7 @@ void sgb_batch_destroy(sgb_batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     bfree(b->tables); bfree(b->kap); bfree(b->h);
     void* p;
-    p = b->rd; bfree(p); p = b->roff; bfree(p); p = b->kT; bfree(p); p = b->ladder; bfree(p);
+    p = b->rd; bfree(p); p = b->roff; bfree(p); p = b->kT; bfree(p); bfree(b->kTR); p = b->ladder; bfree(p);
     p = b->gstart; bfree(p); p = b->gcount; bfree(p); p = b->tiles; bfree(p); p = b->tfirst_d; bfree(p);
     p = b->tcount_d; bfree(p);
     p = b->pc; bfree(p);
@@ -770,6 +784,7 @@ int sgb_batch_create(const sgb_desc* d, int32_t nrep, const int32_t* dims, sgb_b
     rc |= bmalloc(b, (void**)&b->rd, sizeof(int4) * nrep);
     rc |= bmalloc(b, (void**)&b->roff, sizeof(int) * (nrep + 1));
     rc |= bmalloc(b, (void**)&b->kT, sizeof(double) * nrep);
+    rc |= bmalloc(b, (void**)&b->kTR, sizeof(double) * nrep);
     rc |= bmalloc(b, (void**)&b->ladder, sizeof(int) * nrep);
     rc |= bmalloc(b, (void**)&b->gstart, sizeof(int) * nrep);
     rc |= bmalloc(b, (void**)&b->gcount, sizeof(int) * nrep);
@@ -809,6 +824,7 @@ int sgb_batch_create(const sgb_desc* d, int32_t nrep, const int32_t* dims, sgb_b
     cudaMemset(b->n_accept, 0, sizeof(long long) * nrep);
     b->kT_h.assign(nrep, 0.0);
     cudaMemset(b->kT, 0, sizeof(double) * nrep);
+    cudaMemset(b->kTR, 0, sizeof(double) * nrep);
     if (rebuild_groups(b)) return bad(SGB_ERR_CUDA);
     *out = b;
     return SGB_OK;
@@ -980,6 +996,12 @@ int sgb_batch_set_kT(sgb_batch* b, const double* kT) {
         if (!(kT[r] >= 0)) return bfail(b, SGB_ERR_ARG, "Select nonnegative kT");
     b->kT_h.assign(kT, kT + b->nrep);
     BCK(cudaMemcpy(b->kT, kT, sizeof(double) * b->nrep, cudaMemcpyHostToDevice));
+    if (b->fp32) {
+        std::vector<float> f(kT, kT + b->nrep);
+        BCK(cudaMemcpy(b->kTR, f.data(), sizeof(float) * b->nrep, cudaMemcpyHostToDevice));
+    } else {
+        BCK(cudaMemcpy(b->kTR, kT, sizeof(double) * b->nrep, cudaMemcpyHostToDevice));
+    }
     return rebuild_groups(b);
 }
 

@@ -336,6 +336,21 @@ __device__ inline void grad_table(const Model<R>& M, const Tab<R>& T, int a, int
     }
 }
 
+// Single-system table form: per-site Zeeman field from M.h and the neighbour table M.nbr.
+template <class R>
+__device__ inline void grad_single(const Model<R>& M, const Tab<R>& T, int site, R sx, R sy, R sz, const R* X,
+                                   const R* Y, const R* Zc, R& gx, R& gy, R& gz) {
+    R hx = 0, hy = 0, hz = 0;
+    if (M.h) {
+        hx = __ldg(M.h + site);
+        hy = __ldg(M.h + M.ns + site);
+        hz = __ldg(M.h + 2 * M.ns + site);
+    }
+    const int a = site / M.ncell;
+    if (M.general) grad_table<R, true>(M, T, a, site, M.nbr, M.ns, hx, hy, hz, sx, sy, sz, X, Y, Zc, gx, gy, gz);
+    else grad_table<R, false>(M, T, a, site, M.nbr, M.ns, hx, hy, hz, sx, sy, sz, X, Y, Zc, gx, gy, gz);
+}
+
 // Single-system form: per-site Zeeman field from M.h, offsets pre-reduced mod dims.
 template <class R>
 __device__ inline void grad_site(const Model<R>& M, const Tab<R>& T, int site, const SiteIdx& ix,

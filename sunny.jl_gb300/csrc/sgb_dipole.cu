@@ -53,9 +53,8 @@ k_dip_heun(Model<R> M, R* S, R* P, Ctrl* ctrl, int nsteps, R dt, R lam, R nscale
                 sgb_normals4<R>(seed, 0u, step0 + step, (uint32_t)site, 0u, g4);
                 xi[k][0] = g4[0] * nscale; xi[k][1] = g4[1] * nscale; xi[k][2] = g4[2] * nscale;
             }
-            SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
             R gx, gy, gz;
-            grad_site<R>(M, T, site, ix, s[k][0], s[k][1], s[k][2], Sx, Sy, Sz, gx, gy, gz);
+            grad_single<R>(M, T, site, s[k][0], s[k][1], s[k][2], Sx, Sy, Sz, gx, gy, gz);
             rhs_dipole<R>(s[k][0], s[k][1], s[k][2], xi[k][0], xi[k][1], xi[k][2], gx, gy, gz, dt, lam,
                           d1[k][0], d1[k][1], d1[k][2]);
             R px = s[k][0] + d1[k][0], py = s[k][1] + d1[k][1], pz = s[k][2] + d1[k][2];
@@ -68,9 +67,8 @@ k_dip_heun(Model<R> M, R* S, R* P, Ctrl* ctrl, int nsteps, R dt, R lam, R nscale
             int site = tid + k * nthr;
             if (site >= ns) continue;
             R px = Px[site], py = Py[site], pz = Pz[site];
-            SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
             R gx, gy, gz, e0, e1, e2;
-            grad_site<R>(M, T, site, ix, px, py, pz, Px, Py, Pz, gx, gy, gz);
+            grad_single<R>(M, T, site, px, py, pz, Px, Py, Pz, gx, gy, gz);
             rhs_dipole<R>(px, py, pz, xi[k][0], xi[k][1], xi[k][2], gx, gy, gz, dt, lam, e0, e1, e2);
             R nx = s[k][0] + (d1[k][0] + e0) / 2, ny = s[k][1] + (d1[k][1] + e1) / 2,
               nz = s[k][2] + (d1[k][2] + e2) / 2;
@@ -145,9 +143,8 @@ k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, doub
                 const R kap = __ldg(M.kappa + site);
                 R hx = (s[k][0] + sp[k][0]) / 2, hy = (s[k][1] + sp[k][1]) / 2, hz = (s[k][2] + sp[k][2]) / 2;
                 normalize_dip<R>(hx, hy, hz, kap);
-                SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
                 R gx, gy, gz, dx, dy, dz;
-                grad_site<R>(M, T, site, ix, hx, hy, hz, Hc, Hc + ns, Hc + 2 * ns, gx, gy, gz);
+                grad_single<R>(M, T, site, hx, hy, hz, Hc, Hc + ns, Hc + 2 * ns, gx, gy, gz);
                 rhs_dipole<R>(hx, hy, hz, (R)0, (R)0, (R)0, gx, gy, gz, dt, lam, dx, dy, dz);
                 R qx = s[k][0] + dx, qy = s[k][1] + dy, qz = s[k][2] + dz;
                 R ex = sp[k][0] - qx, ey = sp[k][1] - qy, ez = sp[k][2] - qz;

@@ -28,6 +28,7 @@ struct sgb_system {
     void* h = nullptr;       // [3][ns]
     void* tables = nullptr;
     int tables_bytes = 0;
+    int* nbr = nullptr;             // neighbour table of the single system
     Model<float> mf{};
     Model<double> md{};
     // state buffers
@@ -104,6 +105,7 @@ struct sgb_batch {
     int4* rd = nullptr;             // (L1, L2, L3, ncell)
     int* roff = nullptr;
     double* kT = nullptr;
+    void* kTR = nullptr;            // kT in the working precision (noise amplitudes)
     std::vector<double> kT_h;
     int* ladder = nullptr;          // replica at each ladder position (group-major)
     int* gstart = nullptr;          // first ladder position of each group
