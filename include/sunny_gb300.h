@@ -118,6 +118,16 @@ int sgb_get_state(sgb_system* sys, double* dipoles, double* coherents);
  * current state. grad: double[ns][3] (dipole) or double[ns][N][2] (SU(N)). */
 int sgb_energy_grad(sgb_system* sys, double* grad);
 
+/* sgb_energy_grad without any device allocation (no counterpart in the reference).
+ * For callers that may not allocate device memory: a host recording a CUDA graph, a host
+ * whose device memory is owned by its own pool, a loop that must stay out of the
+ * allocator. The gradient goes through one 8 MiB static device array (2^20 doubles) per
+ * device, shared by every call: systems needing more (3 doubles per dipole site, 2N per
+ * SU(N) site) get SGB_ERR_ARG; calls must not overlap (issue them one after another).
+ * The state must be set after the last coupling change (else SGB_ERR_STATE). The first
+ * call on a device resolves the array's address; make it before any stream capture. */
+int sgb_energy_grad_static(sgb_system* sys, double* grad);
+
 /* energy(sys) (Interactions.jl:401-432) in FP64, and the magnetisation sum(sys.dipoles)
  * (ParallelTempering.jl:31). Either output may be NULL. */
 int sgb_energy(sgb_system* sys, double* energy, double* magnetization3);

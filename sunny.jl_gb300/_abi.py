@@ -63,6 +63,7 @@ SIGNATURES = {
     "sgb_set_state": (C.c_int, [_P, _D, _D]),
     "sgb_get_state": (C.c_int, [_P, _D, _D]),
     "sgb_energy_grad": (C.c_int, [_P, _D]),
+    "sgb_energy_grad_static": (C.c_int, [_P, _D]),
     "sgb_energy": (C.c_int, [_P, _D, _D]),
     "sgb_langevin": (C.c_int, [_P, C.c_double, C.c_double, C.c_double, _U64, _U64, _I32, _D]),
     "sgb_langevin_noise": (C.c_int, [_P, _U64, _U64, _D]),
