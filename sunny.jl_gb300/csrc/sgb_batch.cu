@@ -23,6 +23,7 @@
 #include <cstring>
 #include <numeric>
 #include <string>
+#include <type_traits>
 #include <vector>
 #include "sgb_device.cuh"
 #include "sgb_tables.h"
@@ -327,28 +328,69 @@ __device__ __forceinline__ void snap_write(const BSnap<R>& sn, int r, int t, int
 
 #define SGB_MAXREP_CORR 64
 
-template <class R, bool GEN>
+// Batched implicit midpoint (Integrators.jl:379-413 per replica) recording snapshots.
+// Each CTA owns at most SGB_MAXT tiles for the whole launch. Their descriptors, the
+// sublattice of every site, kappa and the Zeeman field per sublattice, and (IDX != 0)
+// the neighbour index of every bond of every site are copied to shared memory once, so
+// the iteration loop issues no dependent index loads: the only global loads left are the
+// site's own spins and its neighbours' midpoint spins, fetched G bonds at a time.
+// IDX 2 keeps indices as uint16 (replicas of at most 65,536 sites), IDX 4 as int32,
+// IDX 0 reads them from the global table.
+template <class R, bool GEN, int IDX>
 __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midpoint(BatchArgs<R> A, MidArgs<R> X, int nsteps, R dt,
-                                                                R lam, BSnap<R> sn) {
+                                                                R lam, BSnap<R> sn, int kb) {
+    using IT = typename std::conditional<IDX == 2, unsigned short, int>::type;
+    constexpr int G = IDX != 0 ? 9 : 6;
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(A.M, smem);
+    IT* sidx = reinterpret_cast<IT*>(smem + A.M.tables_bytes);   // [tile][bond][SGB_TILE]
     __shared__ double sacc[SGB_MAXREP_CORR];
     __shared__ unsigned long long conv_mask;   // bit q: replica q met the tolerance this iteration
-    const int NS = A.NS;
-    const bool leader = (blockIdx.x == 0 && threadIdx.x == 0);
-    bool act[SGB_MAXT];
+    __shared__ int4 st_a[SGB_MAXT];            // (replica, first site, count, replica offset)
+    __shared__ int2 st_b[SGB_MAXT];            // (replica sites, neighbour-table offset)
+    __shared__ unsigned char st_atom[SGB_MAXT][SGB_TILE];
+    __shared__ R s_kap[SGB_MAX_SUBLAT];
+    __shared__ R s_h[3 * SGB_MAX_SUBLAT];
+    const int NS = A.NS, na = A.M.na;
+    const int tid = threadIdx.x;
+    const bool leader = (blockIdx.x == 0 && tid == 0);
+    const int ntb = (int)blockIdx.x < A.ntiles
+                        ? min(SGB_MAXT, (A.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x)
+                        : 0;
+    for (int q = tid; q < na; q += blockDim.x) {
+        s_kap[q] = A.kap[q];
+        s_h[q] = A.h ? A.h[q] : (R)0;
+        s_h[na + q] = A.h ? A.h[na + q] : (R)0;
+        s_h[2 * na + q] = A.h ? A.h[2 * na + q] : (R)0;
+    }
+    for (int k = 0; k < ntb; k++) {
+        const int t = blockIdx.x + k * gridDim.x;
+        TileD c = tile_d(A.td, A.pc, t);
+        if (tid == 0) {
+            st_a[k] = make_int4(c.r, c.s, c.cnt, c.off);
+            st_b[k] = make_int2(c.nsr, c.nbo);
+        }
+        if (tid < c.cnt) {
+            st_atom[k][tid] = (unsigned char)c.a;
+            if (IDX != 0) {
+                const int nb = T.boff[c.a + 1] - T.boff[c.a];
+                for (int b = 0; b < nb; b++)
+                    sidx[((size_t)k * kb + b) * SGB_TILE + tid] = (IT)__ldg(A.nbr + c.nbo + (size_t)b * c.nsr + c.s);
+            }
+        }
+    }
+    __syncthreads();
     int cur = 0;
     // first midpoint spins normalize((S + S)/2) and the first snapshot
-    for (int k = 0; k < SGB_MAXT; k++) {
-        const int t = blockIdx.x + k * gridDim.x;
-        if (t >= A.ntiles || !tile_has(A.tiles, t)) continue;
-        TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
-        const int g = c.off + c.s;
+    for (int k = 0; k < ntb; k++) {
+        const int4 ti = st_a[k];
+        if (tid >= ti.z) continue;
+        const int s = ti.y + tid, g = ti.w + s;
         R sx = A.S[g], sy = A.S[NS + g], sz = A.S[2 * NS + g];
         R hx = (sx + sx) / 2, hy = (sy + sy) / 2, hz = (sz + sz) / 2;
-        normalize_dip<R>(hx, hy, hz, A.kap[c.ix.a]);
+        normalize_dip<R>(hx, hy, hz, s_kap[st_atom[k][tid]]);
         X.H[g] = hx; X.H[NS + g] = hy; X.H[2 * NS + g] = hz;
-        if (sn.enabled) snap_write<R>(sn, c.r, sn.t0, c.s, c.d.w * A.M.na, sx, sy, sz);
+        if (sn.enabled) snap_write<R>(sn, ti.x, sn.t0, s, st_b[k].x, sx, sy, sz);
     }
     if (leader) {
         for (int q = 0; q < 3 * X.nrep; q++) X.racc[q] = 0.0;
@@ -357,12 +399,11 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
     long long itg = 0;
     int done = 0;
     for (int step = 0; step < nsteps; ++step) {
-        for (int k = 0; k < SGB_MAXT; k++) {
-            act[k] = true;
-            const int t = blockIdx.x + k * gridDim.x;
-            if (t >= A.ntiles || !tile_has(A.tiles, t)) continue;
-            TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
-            const int g = c.off + c.s;
+        unsigned actm = (1u << ntb) - 1u;   // bit k: tile k's replica is still iterating
+        for (int k = 0; k < ntb; k++) {
+            const int4 ti = st_a[k];
+            if (tid >= ti.z) continue;
+            const int g = ti.w + ti.y + tid;
             X.Sp[g] = A.S[g]; X.Sp[NS + g] = A.S[NS + g]; X.Sp[2 * NS + g] = A.S[2 * NS + g];
         }
         bool all_done = false;
@@ -372,26 +413,33 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
             R* Hn = X.H + (size_t)nxt * 3 * NS;
             R* Hs = X.H + (size_t)nst * 3 * NS;
             const int slot = (int)(itg % 3);
-            for (int q = threadIdx.x; q < X.nrep; q += blockDim.x) sacc[q] = 0.0;
+            for (int q = tid; q < X.nrep; q += blockDim.x) sacc[q] = 0.0;
             __syncthreads();
-            for (int k = 0; k < SGB_MAXT; k++) {
-                const int t = blockIdx.x + k * gridDim.x;
-                if (t >= A.ntiles) break;
+            for (int k = 0; k < ntb; k++) {
+                const int4 ti = st_a[k];
+                const bool on = (actm >> k) & 1u;
                 R acc = 0;   // per-site terms in R; the warp, block and grid sums are FP64
-                TileD c = tile_d(A.td, A.pc, t);
-                const int r = c.r;
-                if ((int)threadIdx.x < c.cnt) {
-                    const int g = c.off + c.s;
-                    if (act[k]) {
-                        const R kap = A.kap[c.a];
+                if (tid < ti.z) {
+                    const int s = ti.y + tid, g = ti.w + s;
+                    if (on) {
+                        const int a = st_atom[k][tid];
+                        const R kap = s_kap[a];
                         R sx = A.S[g], sy = A.S[NS + g], sz = A.S[2 * NS + g];
                         R qx = X.Sp[g], qy = X.Sp[NS + g], qz = X.Sp[2 * NS + g];
                         R hx = (sx + qx) / 2, hy = (sy + qy) / 2, hz = (sz + qz) / 2;
                         normalize_dip<R>(hx, hy, hz, kap);
-                        R fx, fy, fz, gx, gy, gz, dx, dy, dz;
-                        site_field(A, c.a, fx, fy, fz);
-                        grad_table<R, GEN>(A.M, T, c.a, c.s, A.nbr + c.nbo, c.nsr, fx, fy, fz, hx, hy, hz, Hc + c.off,
-                                           Hc + NS + c.off, Hc + 2 * NS + c.off, gx, gy, gz);
+                        R gx, gy, gz, dx, dy, dz;
+                        const R* HX = Hc + ti.w;
+                        const R* HY = Hc + NS + ti.w;
+                        const R* HZ = Hc + 2 * NS + ti.w;
+                        if (IDX != 0) {
+                            const IT* ip = sidx + (size_t)k * kb * SGB_TILE + tid;
+                            grad_nbi<R, GEN, G>(A.M, T, a, [ip](int b) { return (int)ip[b * SGB_TILE]; }, s_h[a],
+                                                s_h[na + a], s_h[2 * na + a], hx, hy, hz, HX, HY, HZ, gx, gy, gz);
+                        } else {
+                            grad_table<R, GEN>(A.M, T, a, s, A.nbr + st_b[k].y, st_b[k].x, s_h[a], s_h[na + a],
+                                               s_h[2 * na + a], hx, hy, hz, HX, HY, HZ, gx, gy, gz);
+                        }
                         rhs_dipole<R>(hx, hy, hz, (R)0, (R)0, (R)0, gx, gy, gz, dt, lam, dx, dy, dz);
                         R nx = sx + dx, ny = sy + dy, nz = sz + dz;
                         R ex = qx - nx, ey = qy - ny, ez = qz - nz;
@@ -411,15 +459,15 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                         Hs[g] = Hn[g]; Hs[NS + g] = Hn[NS + g]; Hs[2 * NS + g] = Hn[2 * NS + g];
                     }
                 }
-                if (act[k]) {
+                if (on) {
                     // warp sum, then one shared-memory FP64 atomic per warp (tiles never straddle replicas)
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-                    if ((threadIdx.x & 31) == 0) atomicAdd(&sacc[r], (double)acc);
+                    if ((tid & 31) == 0) atomicAdd(&sacc[ti.x], (double)acc);
                 }
             }
             __syncthreads();
-            for (int q = threadIdx.x; q < X.nrep; q += blockDim.x)
+            for (int q = tid; q < X.nrep; q += blockDim.x)
                 if (sacc[q] != 0.0) atomicAdd(&X.racc[slot * X.nrep + q], sacc[q]);
             if (leader) {
                 for (int q = 0; q < X.nrep; q++) X.racc[((slot + 1) % 3) * X.nrep + q] = 0.0;
@@ -428,7 +476,7 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
             if (!sgb_grid_barrier(A.ctrl, gridDim.x)) return;
             itg++;
             // one thread per block compares the FP64 sums with the tolerance
-            if (threadIdx.x == 0) {
+            if (tid == 0) {
                 unsigned long long m = 0;
                 for (int q = 0; q < X.nrep; q++)
                     if (X.racc[slot * X.nrep + q] <= X.atol2) m |= 1ull << q;
@@ -437,14 +485,12 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
             __syncthreads();
             const unsigned long long mask = conv_mask;
             all_done = (X.nrep == 64) ? (mask == ~0ull) : (mask == ((1ull << X.nrep) - 1));
-            for (int k = 0; k < SGB_MAXT; k++) {
-                const int t = blockIdx.x + k * gridDim.x;
-                if (t >= A.ntiles) break;
-                const int r = A.tiles[t].x;
-                if (act[k] && ((mask >> r) & 1ull)) {
-                    act[k] = false;
-                    if (tile_has(A.tiles, t)) {
-                        const int g = A.roff[r] + A.tiles[t].y + threadIdx.x;
+            for (int k = 0; k < ntb; k++) {
+                const int4 ti = st_a[k];
+                if (((actm >> k) & 1u) && ((mask >> ti.x) & 1ull)) {
+                    actm &= ~(1u << k);
+                    if (tid < ti.z) {
+                        const int g = ti.w + ti.y + tid;
                         A.S[g] = X.Sc[g]; A.S[NS + g] = X.Sc[NS + g]; A.S[2 * NS + g] = X.Sc[2 * NS + g];
                     }
                 }
@@ -461,13 +507,11 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
         }
         done = step + 1;
         if (sn.enabled && (done % sn.measperiod) == 0) {
-            for (int k = 0; k < SGB_MAXT; k++) {
-                const int t = blockIdx.x + k * gridDim.x;
-                if (t >= A.ntiles || !tile_has(A.tiles, t)) continue;
-                TileCtx c = tile_ctx(A.tiles, A.rd, A.roff, A.pc, t);
-                const int g = c.off + c.s;
-                snap_write<R>(sn, c.r, sn.t0 + done / sn.measperiod, c.s, c.d.w * A.M.na, A.S[g], A.S[NS + g],
-                              A.S[2 * NS + g]);
+            for (int k = 0; k < ntb; k++) {
+                const int4 ti = st_a[k];
+                if (tid >= ti.z) continue;
+                const int s = ti.y + tid, g = ti.w + s;
+                snap_write<R>(sn, ti.x, sn.t0 + done / sn.measperiod, s, st_b[k].x, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
             }
         }
     }
@@ -649,6 +693,38 @@ int rebuild_groups(sgb_batch* b) {
 }  // namespace
 
 // ---- batched add_sample! (called from sgb_corr_add_sample) ----------------------------------
+// Launch shape of the batched midpoint kernel: the most co-resident CTAs (up to the
+// register-bound limit) whose shared memory also holds their tiles' neighbour indices;
+// the global-index variant when no such shape exists.
+template <class R, bool GEN>
+static int launch_midpoint(sgb_batch* b, void** args) {
+    const size_t tab = (size_t)b->tables_bytes;
+    const size_t isz = b->nsr_max <= 65536 ? 2 : 4;
+    const int maxbps = sizeof(R) == 4 ? 3 : 2;
+    for (int bps = maxbps; bps >= 1 && b->kb > 0; bps--) {
+        const long long g = std::min<long long>((long long)bps * b->nsm, b->ntiles);
+        const long long ntb = (b->ntiles + g - 1) / g;
+        if (ntb > SGB_MAXT) break;
+        const size_t smem = tab + (size_t)ntb * b->kb * SGB_TILE * isz;
+        auto kern = isz == 2 ? k_batch_midpoint<R, GEN, 2> : k_batch_midpoint<R, GEN, 4>;
+        if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        int fit = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, SGB_TILE, smem) != cudaSuccess)
+            return bfail(b, SGB_ERR_CUDA, "occupancy query failed");
+        if (fit < bps) continue;
+        b->mid_idx = (int)isz;
+        return bcoop(b, kern, (int)g, smem, args);
+    }
+    int grid = 0;
+    int rc = bgrid(b, k_batch_midpoint<R, GEN, 0>, tab, SGB_MAXT, &grid);
+    if (rc) return rc;
+    b->mid_idx = 0;
+    return bcoop(b, k_batch_midpoint<R, GEN, 0>, grid, tab, args);
+}
+
 template <class R>
 static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
     BatchArgs<R> A = bargs<R>(b);
@@ -673,20 +749,12 @@ static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
     sn.rep_stride = (size_t)c->nomega * c->nobs * c->npos * c->ncell;
     sn.scale = (R)(1.0 / std::sqrt((double)c->ncell));
     int nsteps = c->measperiod * (c->nsnaps - 1);
-    int grid = 0;
-    size_t smem = (size_t)b->tables_bytes;
     if (b->nrep > SGB_MAXREP_CORR) return bfail(b, SGB_ERR_ARG, "batched sampling supports at most 64 replicas");
     BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
     R dt = (R)c->dt, lam = (R)c->damping;
-    void* args[] = {&A, &X, &nsteps, &dt, &lam, &sn};
-    int rc;
-    if (A.M.general) {
-        rc = bgrid(b, k_batch_midpoint<R, true>, smem, SGB_MAXT, &grid);
-        if (!rc) rc = bcoop(b, k_batch_midpoint<R, true>, grid, smem, args);
-    } else {
-        rc = bgrid(b, k_batch_midpoint<R, false>, smem, SGB_MAXT, &grid);
-        if (!rc) rc = bcoop(b, k_batch_midpoint<R, false>, grid, smem, args);
-    }
+    int kb = b->kb;
+    void* args[] = {&A, &X, &nsteps, &dt, &lam, &sn, &kb};
+    int rc = A.M.general ? launch_midpoint<R, true>(b, args) : launch_midpoint<R, false>(b, args);
     if (rc) return rc;
     Ctrl st;
     if ((rc = read_status(b, &st))) return rc;
@@ -759,6 +827,7 @@ int sgb_batch_create(const sgb_desc* d, int32_t nrep, const int32_t* dims, sgb_b
     }
     b->off[nrep] = (int)tot;
     b->NS = (int)tot;
+    for (int r = 0; r < nrep; r++) b->nsr_max = std::max(b->nsr_max, b->off[r + 1] - b->off[r]);
     auto bad = [&](int code) { std::string m = b->err; sgb_batch_destroy(b); g_batch_error = m; return code; };
     if (cudaSetDevice(d->device) != cudaSuccess) { bfail(b, SGB_ERR_CUDA, "cudaSetDevice failed"); return bad(SGB_ERR_CUDA); }
     cudaDeviceProp prop;
@@ -900,6 +969,7 @@ int sgb_batch_set_couplings(sgb_batch* b, const double* kappa, const double* g, 
         const int* boff = reinterpret_cast<const int*>(buf.data() + off_boff);
         int kb = 0;
         for (int a = 0; a < na; a++) kb = std::max(kb, boff[a + 1] - boff[a]);
+        b->kb = kb;
         std::vector<int> table, nbo(b->nrep, 0);
         std::vector<std::array<int, 4>> seen;   // (L1, L2, L3, offset)
         for (int r = 0; r < b->nrep; r++) {

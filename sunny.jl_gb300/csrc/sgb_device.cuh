@@ -279,19 +279,26 @@ __device__ inline void grad_batch(const Model<R>& M, const Tab<R>& T, int c1, in
 template <class R, bool GEN>
 __device__ inline void grad_table(const Model<R>& M, const Tab<R>& T, int a, int s, const int* nb, int nsr,
                                   R hx, R hy, R hz, R sx, R sy, R sz, const R* X, const R* Y, const R* Zc,
-                                  R& gx, R& gy, R& gz) {
+                                  R& gx, R& gy, R& gz);
+
+// Gradient of one site from a neighbour-index source: nbi(k) is the site index (within
+// the replica) of the k-th bond of sublattice a. Neighbour spins are fetched G bonds at a
+// time so that their loads are in flight together.
+template <class R, bool GEN, int G, class NBI>
+__device__ __forceinline__ void grad_nbi(const Model<R>& M, const Tab<R>& T, int a, NBI nbi, R hx, R hy, R hz,
+                                         R sx, R sy, R sz, const R* X, const R* Y, const R* Zc, R& gx, R& gy,
+                                         R& gz) {
     gx = hx; gy = hy; gz = hz;
     {
         int km = T.kmax[a];
         if (km > 0) classical_aniso<R>(T.stev + 28 * a, km, sx, sy, sz, gx, gy, gz);
     }
     const int b0 = T.boff[a], b1 = T.boff[a + 1];
-    constexpr int G = 6;
     for (int b = b0; b < b1; b += G) {
         int js[G];
 #pragma unroll
         for (int k = 0; k < G; k++)
-            if (b + k < b1) js[k] = __ldg(nb + (size_t)(b + k - b0) * nsr + s);
+            if (b + k < b1) js[k] = nbi(b + k - b0);
         R tx[G], ty[G], tz[G];
 #pragma unroll
         for (int k = 0; k < G; k++) {
@@ -334,6 +341,15 @@ __device__ inline void grad_table(const Model<R>& M, const Tab<R>& T, int a, int
             }
         }
     }
+}
+
+template <class R, bool GEN>
+__device__ inline void grad_table(const Model<R>& M, const Tab<R>& T, int a, int s, const int* nb, int nsr,
+                                  R hx, R hy, R hz, R sx, R sy, R sz, const R* X, const R* Y, const R* Zc,
+                                  R& gx, R& gy, R& gz) {
+    const int* p = nb + s;
+    grad_nbi<R, GEN, 6>(M, T, a, [p, nsr](int k) { return __ldg(p + (size_t)k * nsr); }, hx, hy, hz, sx, sy, sz,
+                        X, Y, Zc, gx, gy, gz);
 }
 
 // Single-system table form: per-site Zeeman field from M.h and the neighbour table M.nbr.

@@ -121,6 +121,9 @@ struct sgb_batch {
     int* nbr = nullptr;             // neighbour tables, one per distinct replica size
     int* nbo = nullptr;             // [nrep] offset of each replica's table in nbr
     int4* td = nullptr;             // [ntiles][2] tile descriptors
+    int kb = 0;                     // most bonds of any sublattice (neighbour-table rows)
+    int nsr_max = 0;                // sites of the largest replica
+    int mid_idx = -1;               // neighbour-index staging of the last midpoint launch (0, 2 or 4 bytes)
     // state
     void* S = nullptr;
     void* P = nullptr;
