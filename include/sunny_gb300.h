@@ -119,9 +119,9 @@ int sgb_get_state(sgb_system* sys, double* dipoles, double* coherents);
 int sgb_energy_grad(sgb_system* sys, double* grad);
 
 /* sgb_energy_grad without any device allocation (no counterpart in the reference).
- * For callers that may not allocate device memory: a host recording a CUDA graph, a host
- * whose device memory is owned by its own pool, a loop that must stay out of the
- * allocator. The gradient goes through one 8 MiB static device array (2^20 doubles) per
+ * For callers that may not allocate device memory: a host whose device memory is owned
+ * by its own pool allocator or capped by a fixed budget, or a loop that must stay out of
+ * the allocator. The gradient goes through one 8 MiB static device array (2^20 doubles) per
  * device, shared by every call: systems needing more (3 doubles per dipole site, 2N per
  * SU(N) site) get SGB_ERR_ARG; calls must not overlap (issue them one after another).
  * The state must be set after the last coupling change (else SGB_ERR_STATE). The first
@@ -250,6 +250,14 @@ int sgb_batch_langevin_noise(sgb_batch* b, int32_t rep, uint64_t seed, uint64_t 
  * (the parallel add_sample! pattern of Sunny's docs/src/parallelism.md:82-125, merged
  * on device). The accumulator is then used with sgb_corr_data / merge / destroy. */
 int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* desc, sgb_corr** out);
+/* Launch shapes of the batched midpoint kernel (no counterpart in the reference). The
+ * first batched add_sample after the couplings are set times every shape that fits on a
+ * 3-step run and keeps the fastest. Writes up to `cap` rows of (neighbour-index bytes in
+ * shared memory or 0 for the global table, bonds gathered together, CTAs per SM, grid,
+ * dynamic shared bytes) into shapes[cap][5] and their tuning times into ms[cap] (either
+ * may be NULL); *chosen = the row in use. Returns the number of shapes (0 before the
+ * first batched add_sample). */
+int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, float* ms, int32_t* chosen);
 
 /* ---- measurement helpers ---------------------------------------------------- */
 
