@@ -175,6 +175,15 @@ def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000):
     res = {"ms": ms.value, "phase_ms": (ph / max(1, n.value)).tolist(), "launches": lib.sgb_batch_kernel_launches(b.handle) - launches0,
            "clocks": clk, "nrep": nrep, "ns": proto.nsites, "nsteps_per_sample": nsteps_sample,
            "iters_per_step": its.value / max(1, n.value) / nsteps_sample, "n_all_omega": sc.n_all_omega}
+    shapes = (C.c_int32 * 40)()
+    tms = (C.c_float * 8)()
+    chosen = C.c_int32(-1)
+    nsh = lib.sgb_batch_midpoint_shapes(b.handle, 8, shapes, tms, C.byref(chosen))
+    res["midpoint_shapes"] = {
+        "chosen": chosen.value,
+        "shapes": [{"nbr_index_bytes_smem": shapes[5 * k], "bonds_gathered": shapes[5 * k + 1],
+                    "ctas_per_sm": shapes[5 * k + 2], "grid": shapes[5 * k + 3], "smem": shapes[5 * k + 4],
+                    "tune_ms_3_steps": round(tms[k], 4)} for k in range(max(0, min(nsh, 8)))]}
     # end to end: every replica's state in from host memory, add_sample, every state out
     states = [b.get_state(r) for r in range(nrep)]
     t0 = time.perf_counter()
@@ -457,6 +466,7 @@ def main():
             "midpoint_iters_per_step": {"fp32_batched": rb["iters_per_step"], "fp32": r32["iters_per_step"],
                                         "fp64": None if r64 is None else r64["iters_per_step"]},
             "us_per_midpoint_iteration": 1000.0 * ph[0] / (rb["iters_per_step"] * nsteps_sample),
+            "midpoint_autotune": rb["midpoint_shapes"],
             "kernels": kernels,
             "langevin_site_steps": {"simple_cubic_16^3_dipole": extra.get("sc"), "triangular_48x48x4_SU3": extra.get("tri"),
                                     "tempering_256_replicas": pt},

@@ -91,6 +91,7 @@ SIGNATURES = {
     "sgb_batch_graph_active": (C.c_int, [_P]),
     "sgb_batch_langevin_noise": (C.c_int, [_P, _I32, _U64, _U64, _D]),
     "sgb_batch_corr_create": (C.c_int, [_P, C.POINTER(CorrDesc), C.POINTER(_P)]),
+    "sgb_batch_midpoint_shapes": (C.c_int, [_P, _I32, C.POINTER(_I32), C.POINTER(C.c_float), C.POINTER(_I32)]),
     "sgb_event_record": (C.c_int, [_P, _I32]),
     "sgb_event_elapsed": (C.c_int, [_P, _I32, _I32, C.POINTER(C.c_float)]),
     "sgb_batch_event_record": (C.c_int, [_P, _I32]),

@@ -138,11 +138,11 @@ class SampledCorrelations:
                 raise ValueError("batched sampling needs replicas with the prototype's dims")
             self._batch = sys
             sys._check(sys._lib.sgb_batch_corr_create(sys.handle, C.byref(d), C.byref(h)))
-            self._lib, self._errh = sys._lib, None
+            self._lib = sys._lib
         else:
             sys._sync_to_device()
             _abi.check(sys._lib.sgb_corr_create(sys.handle, C.byref(d), C.byref(h)), sys._lib, sys.handle)
-            self._lib, self._errh = sys._lib, sys.handle
+            self._lib = sys._lib
         self._h = h
 
     def close(self):
@@ -152,9 +152,11 @@ class SampledCorrelations:
 
     def _check(self, rc):
         if rc != _abi.SGB_OK:
-            if self._batch is not None:
+            if self._batch is not None and self._batch.handle is not None:
                 self._batch._check(rc)
-            _abi.check(rc, self._lib, self._errh)
+            # errors of an accumulator whose owner was closed are in the process-wide message
+            owner = None if self._batch is not None else self.sys.handle
+            _abi.check(rc, self._lib, owner)
 
     def __del__(self):
         try:

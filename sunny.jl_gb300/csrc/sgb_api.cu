@@ -341,6 +341,7 @@ int sgb_create(const sgb_desc* d, sgb_system** out) {
 void sgb_destroy(sgb_system* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    sgb_detach_corrs(s->corrs);
     dfree(s->kappa); dfree(s->h); dfree(s->tables);
     { void* p = s->nbr; dfree(p); } dfree(s->S); dfree(s->P); dfree(s->H);
     dfree(s->Z); dfree(s->Q); dfree(s->QP); dfree(s->QH);
@@ -628,6 +629,9 @@ static int cfail(sgb_corr* c, int code, const std::string& msg) {
 void sgb_corr_destroy(sgb_corr* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    auto unlink = [c](std::vector<sgb_corr*>& v) { v.erase(std::remove(v.begin(), v.end(), c), v.end()); };
+    if (c->sys) unlink(c->sys->corrs);
+    if (c->batch) unlink(c->batch->corrs);
     dfree(c->ops);
     void* p = c->pairs; dfree(p);
     dfree(c->A); dfree(c->Ahat);
@@ -718,6 +722,7 @@ int sgb_corr_create(sgb_system* s, const sgb_corr_desc* d, sgb_corr** out) {
     c->launches = &s->launches;
     rc = corr_setup(c, d, s->fp32, s->sun, s->N, s->ns, s->d.natoms, s->d.dims, 1);
     if (rc) { sgb_corr_destroy(c); return rc; }
+    s->corrs.push_back(c);
     *out = c;
     return SGB_OK;
 }
@@ -737,7 +742,8 @@ int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* d, sgb_corr** out) 
         if (cudaMalloc(p, bytes) != cudaSuccess) { *p = nullptr; b->err = "device allocation failed"; return SGB_ERR_NOMEM; }
         return SGB_OK;
     };
-    if ((rc = lazy(&b->Sp, R * 3 * b->NS)) || (rc = lazy(&b->H, R * 9 * b->NS)) || (rc = lazy(&b->Sc, R * 3 * b->NS)) ||
+    // midpoint-private buffers: room for one 4-element vector per site (FP32 float4 layout)
+    if ((rc = lazy(&b->Sp, R * 4 * b->NS)) || (rc = lazy(&b->H, R * 12 * b->NS)) || (rc = lazy(&b->Sc, R * 4 * b->NS)) ||
         (rc = lazy((void**)&b->racc, sizeof(double) * 3 * b->nrep)))
         return rc;
     sgb_corr* c = new sgb_corr();
@@ -747,6 +753,7 @@ int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* d, sgb_corr** out) 
     const int ns = b->off[1] - b->off[0];
     rc = corr_setup(c, d, b->fp32, false, 0, ns, b->na, b->dims.data(), b->nrep);
     if (rc) { b->err = c->err; sgb_corr_destroy(c); return rc; }
+    b->corrs.push_back(c);
     *out = c;
     return SGB_OK;
 }
@@ -772,6 +779,7 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
     if (!c) return fail(nullptr, SGB_ERR_ARG, "null handle");
     sgb_system* s = c->sys;
     sgb_batch* b = c->batch;
+    if (!s && !b) return cfail(c, SGB_ERR_STATE, "the System (or replica batch) of this accumulator was destroyed");
     if (window != 0 && window != 1) return cfail(c, SGB_ERR_ARG, "window must be 0 (:cosine) or 1 (:rectangular)");
     if (c->window >= 0 && c->window != window)
         return cfail(c, SGB_ERR_ARG, "all samples of one accumulator must use the same window");

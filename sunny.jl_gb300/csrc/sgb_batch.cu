@@ -295,9 +295,9 @@ __global__ void k_batch_noise(int ns, int rep, uint64_t seed, uint64_t step, dou
 
 template <class R>
 struct MidArgs {
-    R* Sp;          // current iterate S'
-    R* H;           // 3 rotating buffers of midpoint spins, [3][3][NS]
-    R* Sc;          // candidate new state
+    R* Sp;          // current iterate S' (MV layout)
+    R* H;           // 3 rotating buffers of midpoint spins, MV<R>::W * NS elements each
+    R* Sc;          // candidate new state (MV layout)
     double* racc;   // [3][nrep] FP64 convergence sums
     int nrep;
     double atol2;
@@ -328,6 +328,33 @@ __device__ __forceinline__ void snap_write(const BSnap<R>& sn, int r, int t, int
 
 #define SGB_MAXREP_CORR 64
 
+// Midpoint-private 3-vector buffers (iterate, candidate, rotating midpoint spins). FP32
+// keeps one float4 per site so that a neighbour costs one 16-byte load; FP64 keeps SoA
+// [3][NS]. K: elements from one site to the next; W * NS: elements of one buffer.
+template <class R>
+struct MV;
+template <>
+struct MV<float> {
+    static constexpr int K = 4, W = 4;
+    __device__ static __forceinline__ void ld(const float* b, int, int i, float& x, float& y, float& z) {
+        const float4 v = reinterpret_cast<const float4*>(b)[i];
+        x = v.x; y = v.y; z = v.z;
+    }
+    __device__ static __forceinline__ void st(float* b, int, int i, float x, float y, float z) {
+        reinterpret_cast<float4*>(b)[i] = make_float4(x, y, z, 0.f);
+    }
+};
+template <>
+struct MV<double> {
+    static constexpr int K = 1, W = 3;
+    __device__ static __forceinline__ void ld(const double* b, int n, int i, double& x, double& y, double& z) {
+        x = b[i]; y = b[n + i]; z = b[2 * n + i];
+    }
+    __device__ static __forceinline__ void st(double* b, int n, int i, double x, double y, double z) {
+        b[i] = x; b[n + i] = y; b[2 * n + i] = z;
+    }
+};
+
 // Batched implicit midpoint (Integrators.jl:379-413 per replica) recording snapshots.
 // Each CTA owns at most SGB_MAXT tiles for the whole launch. Their descriptors, the
 // sublattice of every site, kappa and the Zeeman field per sublattice, and (IDX != 0)
@@ -335,12 +362,11 @@ __device__ __forceinline__ void snap_write(const BSnap<R>& sn, int r, int t, int
 // the iteration loop issues no dependent index loads: the only global loads left are the
 // site's own spins and its neighbours' midpoint spins, fetched G bonds at a time.
 // IDX 2 keeps indices as uint16 (replicas of at most 65,536 sites), IDX 4 as int32,
-// IDX 0 reads them from the global table.
-template <class R, bool GEN, int IDX>
+// IDX 0 reads them from the global table. G is the number of bonds gathered together.
+template <class R, bool GEN, int IDX, int G>
 __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midpoint(BatchArgs<R> A, MidArgs<R> X, int nsteps, R dt,
                                                                 R lam, BSnap<R> sn, int kb) {
     using IT = typename std::conditional<IDX == 2, unsigned short, int>::type;
-    constexpr int G = IDX != 0 ? 9 : 6;
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(A.M, smem);
     IT* sidx = reinterpret_cast<IT*>(smem + A.M.tables_bytes);   // [tile][bond][SGB_TILE]
@@ -389,7 +415,7 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
         R sx = A.S[g], sy = A.S[NS + g], sz = A.S[2 * NS + g];
         R hx = (sx + sx) / 2, hy = (sy + sy) / 2, hz = (sz + sz) / 2;
         normalize_dip<R>(hx, hy, hz, s_kap[st_atom[k][tid]]);
-        X.H[g] = hx; X.H[NS + g] = hy; X.H[2 * NS + g] = hz;
+        MV<R>::st(X.H, NS, g, hx, hy, hz);
         if (sn.enabled) snap_write<R>(sn, ti.x, sn.t0, s, st_b[k].x, sx, sy, sz);
     }
     if (leader) {
@@ -404,14 +430,14 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
             const int4 ti = st_a[k];
             if (tid >= ti.z) continue;
             const int g = ti.w + ti.y + tid;
-            X.Sp[g] = A.S[g]; X.Sp[NS + g] = A.S[NS + g]; X.Sp[2 * NS + g] = A.S[2 * NS + g];
+            MV<R>::st(X.Sp, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
         }
         bool all_done = false;
         for (int it = 0; it < X.max_iters; ++it) {
             const int nxt = (cur + 1) % 3, nst = (cur + 2) % 3;
-            const R* Hc = X.H + (size_t)cur * 3 * NS;
-            R* Hn = X.H + (size_t)nxt * 3 * NS;
-            R* Hs = X.H + (size_t)nst * 3 * NS;
+            const R* Hc = X.H + (size_t)cur * MV<R>::W * NS;
+            R* Hn = X.H + (size_t)nxt * MV<R>::W * NS;
+            R* Hs = X.H + (size_t)nst * MV<R>::W * NS;
             const int slot = (int)(itg % 3);
             for (int q = tid; q < X.nrep; q += blockDim.x) sacc[q] = 0.0;
             __syncthreads();
@@ -425,38 +451,43 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                         const int a = st_atom[k][tid];
                         const R kap = s_kap[a];
                         R sx = A.S[g], sy = A.S[NS + g], sz = A.S[2 * NS + g];
-                        R qx = X.Sp[g], qy = X.Sp[NS + g], qz = X.Sp[2 * NS + g];
-                        R hx = (sx + qx) / 2, hy = (sy + qy) / 2, hz = (sz + qz) / 2;
-                        normalize_dip<R>(hx, hy, hz, kap);
+                        R qx, qy, qz, hx, hy, hz;
+                        MV<R>::ld(X.Sp, NS, g, qx, qy, qz);
+                        // own midpoint spin normalize((S + S')/2): stored by the previous
+                        // iteration (or step) with exactly this arithmetic
+                        MV<R>::ld(Hc, NS, g, hx, hy, hz);
                         R gx, gy, gz, dx, dy, dz;
-                        const R* HX = Hc + ti.w;
-                        const R* HY = Hc + NS + ti.w;
-                        const R* HZ = Hc + 2 * NS + ti.w;
+                        const R* HB = Hc + (size_t)MV<R>::K * ti.w;
+                        auto nld = [HB, NS](int j, R& x, R& y, R& z) { MV<R>::ld(HB, NS, j, x, y, z); };
                         if (IDX != 0) {
                             const IT* ip = sidx + (size_t)k * kb * SGB_TILE + tid;
-                            grad_nbi<R, GEN, G>(A.M, T, a, [ip](int b) { return (int)ip[b * SGB_TILE]; }, s_h[a],
-                                                s_h[na + a], s_h[2 * na + a], hx, hy, hz, HX, HY, HZ, gx, gy, gz);
+                            grad_nbi_ld<R, GEN, G>(A.M, T, a, [ip](int b) { return (int)ip[b * SGB_TILE]; }, nld,
+                                                   s_h[a], s_h[na + a], s_h[2 * na + a], hx, hy, hz, gx, gy, gz);
                         } else {
-                            grad_table<R, GEN>(A.M, T, a, s, A.nbr + st_b[k].y, st_b[k].x, s_h[a], s_h[na + a],
-                                               s_h[2 * na + a], hx, hy, hz, HX, HY, HZ, gx, gy, gz);
+                            const int* ip = A.nbr + st_b[k].y + s;
+                            const int nsr = st_b[k].x;
+                            grad_nbi_ld<R, GEN, G>(A.M, T, a, [ip, nsr](int b) { return __ldg(ip + (size_t)b * nsr); },
+                                                   nld, s_h[a], s_h[na + a], s_h[2 * na + a], hx, hy, hz, gx, gy, gz);
                         }
                         rhs_dipole<R>(hx, hy, hz, (R)0, (R)0, (R)0, gx, gy, gz, dt, lam, dx, dy, dz);
                         R nx = sx + dx, ny = sy + dy, nz = sz + dz;
                         R ex = qx - nx, ey = qy - ny, ez = qz - nz;
                         acc = ex * ex + ey * ey + ez * ez;
-                        X.Sp[g] = nx; X.Sp[NS + g] = ny; X.Sp[2 * NS + g] = nz;
+                        MV<R>::st(X.Sp, NS, g, nx, ny, nz);
                         R mx = (sx + nx) / 2, my = (sy + ny) / 2, mz = (sz + nz) / 2;
                         normalize_dip<R>(mx, my, mz, kap);
-                        Hn[g] = mx; Hn[NS + g] = my; Hn[2 * NS + g] = mz;
+                        MV<R>::st(Hn, NS, g, mx, my, mz);
                         R cx = nx, cy = ny, cz = nz;
                         normalize_dip<R>(cx, cy, cz, kap);
-                        X.Sc[g] = cx; X.Sc[NS + g] = cy; X.Sc[2 * NS + g] = cz;
+                        MV<R>::st(X.Sc, NS, g, cx, cy, cz);
                         R wx = (cx + cx) / 2, wy = (cy + cy) / 2, wz = (cz + cz) / 2;
                         normalize_dip<R>(wx, wy, wz, kap);
-                        Hs[g] = wx; Hs[NS + g] = wy; Hs[2 * NS + g] = wz;
+                        MV<R>::st(Hs, NS, g, wx, wy, wz);
                     } else {
                         // converged replica: carry its next-step midpoint spins forward
-                        Hs[g] = Hn[g]; Hs[NS + g] = Hn[NS + g]; Hs[2 * NS + g] = Hn[2 * NS + g];
+                        R x, y, z;
+                        MV<R>::ld(Hn, NS, g, x, y, z);
+                        MV<R>::st(Hs, NS, g, x, y, z);
                     }
                 }
                 if (on) {
@@ -491,7 +522,9 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                     actm &= ~(1u << k);
                     if (tid < ti.z) {
                         const int g = ti.w + ti.y + tid;
-                        A.S[g] = X.Sc[g]; A.S[NS + g] = X.Sc[NS + g]; A.S[2 * NS + g] = X.Sc[2 * NS + g];
+                        R x, y, z;
+                        MV<R>::ld(X.Sc, NS, g, x, y, z);
+                        A.S[g] = x; A.S[NS + g] = y; A.S[2 * NS + g] = z;
                     }
                 }
             }
@@ -693,36 +726,107 @@ int rebuild_groups(sgb_batch* b) {
 }  // namespace
 
 // ---- batched add_sample! (called from sgb_corr_add_sample) ----------------------------------
-// Launch shape of the batched midpoint kernel: the most co-resident CTAs (up to the
-// register-bound limit) whose shared memory also holds their tiles' neighbour indices;
-// the global-index variant when no such shape exists.
+// ---- launch shapes of the batched midpoint kernel and their autotuner ----------------------
+//
+// A shape is (neighbour-index staging, bonds gathered together, CTAs per SM). The staged
+// shapes need their tiles' indices to fit in shared memory next to the coupling tables;
+// the global-index shapes always fit. The first trajectory after the couplings are set
+// times every shape that fits on a short run (3 steps without snapshots, the replicas'
+// state saved and restored around it) and keeps the fastest for this batch.
+template <class R>
+using MidKernel = void (*)(BatchArgs<R>, MidArgs<R>, int, R, R, BSnap<R>, int);
+
 template <class R, bool GEN>
-static int launch_midpoint(sgb_batch* b, void** args) {
+static MidKernel<R> mid_kernel(int idx, int G) {
+    if (idx == 2) return G == 9 ? k_batch_midpoint<R, GEN, 2, 9> : k_batch_midpoint<R, GEN, 2, 6>;
+    if (idx == 4) return G == 9 ? k_batch_midpoint<R, GEN, 4, 9> : k_batch_midpoint<R, GEN, 4, 6>;
+    return G == 9 ? k_batch_midpoint<R, GEN, 0, 9> : k_batch_midpoint<R, GEN, 0, 6>;
+}
+
+template <class R, bool GEN>
+static int mid_shapes(sgb_batch* b, std::vector<MidShape>& out) {
+    out.clear();
     const size_t tab = (size_t)b->tables_bytes;
-    const size_t isz = b->nsr_max <= 65536 ? 2 : 4;
+    const int isz = b->nsr_max <= 65536 ? 2 : 4;
     const int maxbps = sizeof(R) == 4 ? 3 : 2;
-    for (int bps = maxbps; bps >= 1 && b->kb > 0; bps--) {
-        const long long g = std::min<long long>((long long)bps * b->nsm, b->ntiles);
-        const long long ntb = (b->ntiles + g - 1) / g;
-        if (ntb > SGB_MAXT) break;
-        const size_t smem = tab + (size_t)ntb * b->kb * SGB_TILE * isz;
-        auto kern = isz == 2 ? k_batch_midpoint<R, GEN, 2> : k_batch_midpoint<R, GEN, 4>;
-        if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-            cudaGetLastError();
-            continue;
+    for (int idx : {isz, 0}) {
+        if (idx != 0 && b->kb == 0) continue;
+        for (int G : {6, 9}) {
+            for (int bps = maxbps; bps >= std::max(1, maxbps - 1); bps--) {
+                const long long g = std::min<long long>((long long)bps * b->nsm, b->ntiles);
+                const long long ntb = (b->ntiles + g - 1) / g;
+                if (ntb > SGB_MAXT) continue;
+                const size_t smem = tab + (idx ? (size_t)ntb * b->kb * SGB_TILE * idx : 0);
+                MidKernel<R> kern = mid_kernel<R, GEN>(idx, G);
+                if (smem > 48 * 1024 &&
+                    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+                    cudaGetLastError();
+                    continue;
+                }
+                int fit = 0;
+                if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, SGB_TILE, smem) != cudaSuccess)
+                    return bfail(b, SGB_ERR_CUDA, "occupancy query failed");
+                if (fit < bps) continue;
+                out.push_back(MidShape{idx, G, bps, (int)g, smem, 0.f});
+            }
         }
-        int fit = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, SGB_TILE, smem) != cudaSuccess)
-            return bfail(b, SGB_ERR_CUDA, "occupancy query failed");
-        if (fit < bps) continue;
-        b->mid_idx = (int)isz;
-        return bcoop(b, kern, (int)g, smem, args);
     }
-    int grid = 0;
-    int rc = bgrid(b, k_batch_midpoint<R, GEN, 0>, tab, SGB_MAXT, &grid);
+    if (out.empty()) return bfail(b, SGB_ERR_ARG, "replica batch too large for one persistent launch of the midpoint kernel");
+    return SGB_OK;
+}
+
+template <class R, bool GEN>
+static int mid_launch(sgb_batch* b, const MidShape& sh, BatchArgs<R>& A, MidArgs<R>& X, int nsteps, R dt, R lam,
+                      BSnap<R>& sn) {
+    int kb = b->kb;
+    void* args[] = {&A, &X, &nsteps, &dt, &lam, &sn, &kb};
+    return bcoop(b, mid_kernel<R, GEN>(sh.idx, sh.G), sh.grid, sh.smem, args);
+}
+
+template <class R, bool GEN>
+static int mid_tune(sgb_batch* b, BatchArgs<R>& A, MidArgs<R>& X, R dt, R lam, BSnap<R> sn) {
+    std::vector<MidShape> shapes;
+    int rc = mid_shapes<R, GEN>(b, shapes);
     if (rc) return rc;
-    b->mid_idx = 0;
-    return bcoop(b, k_batch_midpoint<R, GEN, 0>, grid, tab, args);
+    b->mid_shapes = shapes;
+    if (shapes.size() == 1) {
+        b->mid_choice = 0;
+        return SGB_OK;
+    }
+    const size_t bytes = bsize(b) * 3 * (size_t)b->NS;
+    BCK(cudaMemcpyAsync(b->P, b->S, bytes, cudaMemcpyDeviceToDevice, b->stream));   // P is free outside Langevin
+    sn.enabled = 0;
+    const int tsteps = 3;
+    int best = 0;
+    for (size_t k = 0; k < shapes.size(); k++) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; rep++) {
+            BCK(cudaMemcpyAsync(b->S, b->P, bytes, cudaMemcpyDeviceToDevice, b->stream));
+            BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
+            BCK(cudaEventRecord(b->ev[6], b->stream));
+            if ((rc = mid_launch<R, GEN>(b, shapes[k], A, X, tsteps, dt, lam, sn))) return rc;
+            BCK(cudaEventRecord(b->ev[7], b->stream));
+            BCK(cudaEventSynchronize(b->ev[7]));
+            BCK(cudaEventElapsedTime(&ms, b->ev[6], b->ev[7]));
+        }
+        Ctrl st;
+        if ((rc = read_status(b, &st))) return rc;
+        b->mid_shapes[k].ms = st.status == 0 ? ms : 1e30f;
+        if (b->mid_shapes[k].ms < b->mid_shapes[best].ms) best = (int)k;
+    }
+    BCK(cudaMemcpyAsync(b->S, b->P, bytes, cudaMemcpyDeviceToDevice, b->stream));
+    b->mid_choice = best;
+    return SGB_OK;
+}
+
+template <class R, bool GEN>
+static int launch_midpoint(sgb_batch* b, BatchArgs<R>& A, MidArgs<R>& X, int nsteps, R dt, R lam, BSnap<R>& sn) {
+    if (b->mid_choice < 0) {
+        int rc = mid_tune<R, GEN>(b, A, X, dt, lam, sn);
+        if (rc) return rc;
+    }
+    BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
+    return mid_launch<R, GEN>(b, b->mid_shapes[b->mid_choice], A, X, nsteps, dt, lam, sn);
 }
 
 template <class R>
@@ -750,11 +854,9 @@ static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
     sn.scale = (R)(1.0 / std::sqrt((double)c->ncell));
     int nsteps = c->measperiod * (c->nsnaps - 1);
     if (b->nrep > SGB_MAXREP_CORR) return bfail(b, SGB_ERR_ARG, "batched sampling supports at most 64 replicas");
-    BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
     R dt = (R)c->dt, lam = (R)c->damping;
-    int kb = b->kb;
-    void* args[] = {&A, &X, &nsteps, &dt, &lam, &sn, &kb};
-    int rc = A.M.general ? launch_midpoint<R, true>(b, args) : launch_midpoint<R, false>(b, args);
+    int rc = A.M.general ? launch_midpoint<R, true>(b, A, X, nsteps, dt, lam, sn)
+                         : launch_midpoint<R, false>(b, A, X, nsteps, dt, lam, sn);
     if (rc) return rc;
     Ctrl st;
     if ((rc = read_status(b, &st))) return rc;
@@ -782,6 +884,7 @@ const char* sgb_batch_last_error(const sgb_batch* b) { return b ? b->err.c_str()
 void sgb_batch_destroy(sgb_batch* b) {
     if (!b) return;
     if (b->stream) cudaStreamSynchronize(b->stream);
+    sgb_detach_corrs(b->corrs);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     bfree(b->tables); bfree(b->kap); bfree(b->h);
     void* p;
@@ -1023,6 +1126,7 @@ int sgb_batch_set_couplings(sgb_batch* b, const double* kappa, const double* g, 
     for (Model<float>* m : {&b->mf}) { m->tables = (const unsigned char*)b->tables; m->dipole_mode = 1; m->na = na; }
     for (Model<double>* m : {&b->md}) { m->tables = (const unsigned char*)b->tables; m->dipole_mode = 1; m->na = na; }
     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+    b->mid_choice = -1;
     b->coup_set = true;
     return SGB_OK;
 }
@@ -1205,6 +1309,21 @@ int sgb_batch_step_ensemble(sgb_batch* b, double dt, double damping, uint64_t se
 }
 
 int sgb_batch_graph_active(const sgb_batch* b) { return b && b->graph ? 1 : 0; }
+
+int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, float* ms, int32_t* chosen) {
+    if (!b) return SGB_ERR_ARG;
+    const int n = (int)b->mid_shapes.size();
+    for (int k = 0; k < n && k < cap; k++) {
+        const MidShape& m = b->mid_shapes[k];
+        if (shapes) {
+            int32_t* r = shapes + 5 * k;
+            r[0] = m.idx; r[1] = m.G; r[2] = m.bps; r[3] = m.grid; r[4] = (int32_t)m.smem;
+        }
+        if (ms) ms[k] = m.ms;
+    }
+    if (chosen) *chosen = b->mid_choice;
+    return n;
+}
 
 int sgb_batch_event_record(sgb_batch* b, int32_t slot) {
     if (!b || slot < 0 || slot >= 8) return bfail(b, SGB_ERR_ARG, "bad event slot");

@@ -282,12 +282,12 @@ __device__ inline void grad_table(const Model<R>& M, const Tab<R>& T, int a, int
                                   R& gx, R& gy, R& gz);
 
 // Gradient of one site from a neighbour-index source: nbi(k) is the site index (within
-// the replica) of the k-th bond of sublattice a. Neighbour spins are fetched G bonds at a
-// time so that their loads are in flight together.
-template <class R, bool GEN, int G, class NBI>
-__device__ __forceinline__ void grad_nbi(const Model<R>& M, const Tab<R>& T, int a, NBI nbi, R hx, R hy, R hz,
-                                         R sx, R sy, R sz, const R* X, const R* Y, const R* Zc, R& gx, R& gy,
-                                         R& gz) {
+// the replica) of the k-th bond of sublattice a, and nld(j, x, y, z) loads the spin of
+// site j. Neighbour spins are fetched G bonds at a time so that their loads are in
+// flight together.
+template <class R, bool GEN, int G, class NBI, class NLD>
+__device__ __forceinline__ void grad_nbi_ld(const Model<R>& M, const Tab<R>& T, int a, NBI nbi, NLD nld, R hx, R hy,
+                                            R hz, R sx, R sy, R sz, R& gx, R& gy, R& gz) {
     gx = hx; gy = hy; gz = hz;
     {
         int km = T.kmax[a];
@@ -302,7 +302,7 @@ __device__ __forceinline__ void grad_nbi(const Model<R>& M, const Tab<R>& T, int
         R tx[G], ty[G], tz[G];
 #pragma unroll
         for (int k = 0; k < G; k++) {
-            if (b + k < b1) { tx[k] = sgb_ld(X + js[k]); ty[k] = sgb_ld(Y + js[k]); tz[k] = sgb_ld(Zc + js[k]); }
+            if (b + k < b1) nld(js[k], tx[k], ty[k], tz[k]);
         }
 #pragma unroll
         for (int k = 0; k < G; k++) {
@@ -341,6 +341,19 @@ __device__ __forceinline__ void grad_nbi(const Model<R>& M, const Tab<R>& T, int
             }
         }
     }
+}
+
+// Spins in SoA form: X[j], Y[j], Zc[j].
+template <class R, bool GEN, int G, class NBI>
+__device__ __forceinline__ void grad_nbi(const Model<R>& M, const Tab<R>& T, int a, NBI nbi, R hx, R hy, R hz,
+                                         R sx, R sy, R sz, const R* X, const R* Y, const R* Zc, R& gx, R& gy,
+                                         R& gz) {
+    grad_nbi_ld<R, GEN, G>(
+        M, T, a, nbi,
+        [X, Y, Zc](int j, R& x, R& y, R& z) {
+            x = sgb_ld(X + j); y = sgb_ld(Y + j); z = sgb_ld(Zc + j);
+        },
+        hx, hy, hz, sx, sy, sz, gx, gy, gz);
 }
 
 template <class R, bool GEN>

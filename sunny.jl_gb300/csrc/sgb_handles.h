@@ -47,6 +47,7 @@ struct sgb_system {
     void* flush = nullptr;
     char* stage = nullptr;      // pinned host staging
     size_t stage_cap = 0;
+    std::vector<sgb_corr*> corrs;   // accumulators created on this system (detached on destroy)
 };
 
 struct sgb_corr {
@@ -74,10 +75,21 @@ struct sgb_corr {
     sgb_batch* batch = nullptr;   // set when the accumulator samples a replica batch
     int nrep = 1;                 // replicas sampled per add_sample call
     int64_t prof_iters_last = 0;
-    cudaStream_t stream = nullptr;
-    long long* launches = nullptr;
+    cudaStream_t stream = nullptr;  // the owner's stream; null (default stream) once the owner is destroyed
+    long long* launches = nullptr;  // the owner's launch counter, else own_launches
+    long long own_launches = 0;
 };
 
+
+// One launch shape of the batched midpoint kernel and its autotuning time.
+struct MidShape {
+    int idx;        // neighbour indices: 2 = uint16 in shared memory, 4 = int32 in shared memory, 0 = global
+    int G;          // bonds whose neighbour spins are gathered together
+    int bps;        // CTAs per SM
+    int grid;
+    size_t smem;
+    float ms;       // time of the tuning run (0 if not timed)
+};
 
 struct sgb_batch {
     sgb_desc proto{};
@@ -123,7 +135,8 @@ struct sgb_batch {
     int4* td = nullptr;             // [ntiles][2] tile descriptors
     int kb = 0;                     // most bonds of any sublattice (neighbour-table rows)
     int nsr_max = 0;                // sites of the largest replica
-    int mid_idx = -1;               // neighbour-index staging of the last midpoint launch (0, 2 or 4 bytes)
+    std::vector<MidShape> mid_shapes;   // launch shapes of the batched midpoint kernel that fit
+    int mid_choice = -1;            // shape picked by the autotuner (-1: not tuned for these couplings)
     // state
     void* S = nullptr;
     void* P = nullptr;
@@ -144,7 +157,20 @@ struct sgb_batch {
     int graph_interval = -1;
     double graph_dt = 0, graph_damping = 0;
     uint64_t graph_seed = 0;
+    std::vector<sgb_corr*> corrs;   // accumulators created on this batch (detached on destroy)
 };
+
+// Detach every accumulator of a system or batch that is being destroyed: they keep their
+// data (read-out and merge run on the default stream) but can no longer add samples.
+inline void sgb_detach_corrs(std::vector<sgb_corr*>& corrs) {
+    for (sgb_corr* c : corrs) {
+        c->sys = nullptr;
+        c->batch = nullptr;
+        c->stream = nullptr;
+        c->launches = &c->own_launches;
+    }
+    corrs.clear();
+}
 
 // batched add_sample! trajectory (sgb_batch.cu)
 int batch_corr_trajectory(sgb_corr* c);

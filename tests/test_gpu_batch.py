@@ -117,3 +117,38 @@ def test_batched_sampling_equals_single_samples(gpu, sg):
         assert rel(b.get_state(r), single.dipoles_flat()) < 1e-12
     assert scs.nsamples == 3
     assert rel(scb.data, scs.data) < 1e-11
+
+
+def test_midpoint_autotune_shapes(gpu, sg):
+    # the first batched add_sample times every launch shape that fits and keeps the fastest;
+    # the tuning runs must leave the replicas' state as it was
+    import ctypes as C
+    proto = sg.System(sg.pyrochlore_crystal(), [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(4, 4, 4), seed=5,
+                      precision="fp32", device=None)
+    proto.set_exchange(1.0, proto.crystal.bonds_at_distance(np.sqrt(2) / 4)[0])
+    kw = dict(energies=np.linspace(0, 6, 8), dt=0.025, tol=1e-6)
+    finals = []
+    for tuned_first in (False, True):
+        b = sg.ReplicaBatch(proto, [(4, 4, 4)] * 4, kT=[0.2] * 4, precision="fp32", seed=9)
+        b.randomize_spins()
+        sc = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), **kw)
+        if tuned_first:
+            # tune on a different state, then run from the same initial state as the first batch
+            saved = [b.get_state(r) for r in range(4)]
+            b.randomize_spins()
+            sg.add_sample(sc, b)
+            for r in range(4):
+                b.set_state(r, saved[r])
+        sg.add_sample(sc, b)
+        finals.append([b.get_state(r) for r in range(4)])
+        shapes = (C.c_int32 * 40)()
+        ms = (C.c_float * 8)()
+        chosen = C.c_int32(-1)
+        n = b._lib.sgb_batch_midpoint_shapes(b.handle, 8, shapes, ms, C.byref(chosen))
+        assert n >= 2 and 0 <= chosen.value < n
+        rows = [tuple(shapes[5 * k:5 * k + 5]) for k in range(n)]
+        assert any(r[0] == 2 for r in rows) and any(r[0] == 0 for r in rows)
+        assert all(ms[k] > 0 for k in range(n))
+        b.close()
+    for r in range(4):
+        assert np.array_equal(finals[0][r], finals[1][r])

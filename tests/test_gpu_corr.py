@@ -128,3 +128,18 @@ def test_sqw_sun_parity(gpu, sg, orc):
     sg.add_sample(sc, sys_)
     oc.add_sample(S, Z)
     assert np.max(np.abs(sc.data - oc.data)) < 1e-10 * np.max(np.abs(oc.data))
+
+
+def test_accumulator_outlives_its_system(gpu, sg):
+    # destroying the System first detaches its accumulators: data can still be read,
+    # adding samples raises instead of touching freed memory
+    sys_ = diamond_reference_model(sg)
+    sc = sg.SampledCorrelations(sys_, measure=sg.ssf_perp(sys_), energies=np.linspace(0.0, 5.5, 10), dt=0.12)
+    sg.add_sample(sc, sys_)
+    before = sc.data
+    sys_.close()
+    assert sc.nsamples == 1
+    assert np.array_equal(sc.data, before)
+    with pytest.raises(sg.SunnyGPUError, match="destroyed"):
+        sc._check(sc._lib.sgb_corr_add_sample(sc._h, 0))
+    sc.close()
