@@ -39,6 +39,13 @@ WMAX = 6.0
 DT = 0.025
 
 
+# DRAM bytes (dram__bytes read + write, ncu) per full-size launch of the dominant kernel:
+# k_batch_midpoint measured 1.547e9 bytes on the 399-step, 20-snapshot launch of the
+# nw=20 case (8 replicas, L=16) and is scaled by steps to the 4,179-step, 200-snapshot
+# launch (its traffic is the snapshot stream plus L2 write-backs, both per step).
+DRAM_BYTES_PER_LAUNCH = {"k_batch_midpoint": 1.547e9 * 4179 / 399}
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -439,10 +446,7 @@ def main():
          "achieved_gbs": bytes_accum / (ph[3] * 1e6) if ph[3] else None},
     ]
     dom = max((k for k in kernels if "alg_bytes" in k), key=lambda k: k["ms_per_launch"])
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        traffic = json.loads(tf.read_text()).get(dom["kernel"].split()[0])
+    traffic = DRAM_BYTES_PER_LAUNCH.get(dom["kernel"].split()[0]) if (L, NOMEGA, R) == (16, 200, 8) else None
     roof = {"bound": "hbm", "kernel": dom["kernel"], "achieved": dom["achieved_gbs"], "peak": hbm, "unit": "GB/s",
             "frac": dom["achieved_gbs"] / hbm, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs"}
     line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
