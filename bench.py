@@ -277,6 +277,53 @@ def dynamics_rate(sg, kind, precision, device, nsteps):
             "nsites": ns, "steps": nsteps, "energy_per_site": E}
 
 
+def run_adjoint(sg, device, L_=24, nw=64, checkpoint=64):
+    """Differentiation workload: simple cubic 24^3 dipole lattice (13,824 spins, s=1) from a
+    state thermalised by Langevin at kT=0.3; parameters J1 (1.0), J2 (0.1), D (0.05, onsite
+    -D Sz^2); loss = mean squared difference of one sample's S(q,w) (nw=64 up to 16 meV:
+    dt 0.025 -> 0.02454, measurement period 8, 504 midpoint steps) against the sample at
+    J1=1.1, J2=0.08, D=0.07 from the same state; adjoint with a checkpoint every 64 steps,
+    checked by central differences (h=1e-4) of the same loss."""
+    params = [lambda s_, v: s_.set_exchange(v, sg.Bond(1, 1, [1, 0, 0])),
+              lambda s_, v: s_.set_exchange(v, sg.Bond(1, 1, [1, 1, 0])),
+              lambda s_, v: s_.set_onsite_coupling(lambda Sx, Sy, Sz: -v * Sz @ Sz, 1)]
+    theta0, theta_t = np.array([1.0, 0.1, 0.05]), np.array([1.1, 0.08, 0.07])
+    s = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=(L_, L_, L_), seed=5, device=device)
+    for f, v in zip(params, theta0):
+        f(s, float(v))
+    s.randomize_spins()
+    sg.step(s, sg.Langevin(0.02, damping=0.1, kT=0.3), nsteps=1000)
+    S0 = s.dipoles_flat()
+    adj = sg.SampledCorrelationsAdjoint(s, params, measure=sg.ssf_trace(s), energies=np.linspace(0.0, 16.0, nw),
+                                        dt=0.025)
+    adj.set_params(theta_t)
+    _, target = adj.loss(S0, return_data=True)
+    adj.set_target(target)
+    adj.set_params(theta0)
+    adj.loss_and_grad(S0, checkpoint=checkpoint)          # warm-up (plans, buffers)
+    t0 = time.perf_counter()
+    loss, g = adj.loss_and_grad(S0, checkpoint=checkpoint)
+    t_adj = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    adj.loss(S0)
+    t_fwd = time.perf_counter() - t0
+    fd = np.zeros(3)
+    for k in range(3):
+        e = np.zeros(3)
+        e[k] = 1e-4
+        adj.set_params(theta0 + e)
+        lp = adj.loss(S0)
+        adj.set_params(theta0 - e)
+        lm = adj.loss(S0)
+        fd[k] = (lp - lm) / 2e-4
+    adj.close()
+    s.close()
+    return {"workload": f"simple cubic {L_}^3 (13,824 spins) dipole, J1/J2/D, nw={nw}, {adj.nsteps} midpoint steps, "
+                        f"checkpoint every {checkpoint}", "loss": loss, "grad": g.tolist(), "fd_grad": fd.tolist(),
+            "fd_rel_err": float(np.linalg.norm(g - fd) / np.linalg.norm(fd)), "ms_loss_and_grad": 1000 * t_adj,
+            "ms_forward_only": 1000 * t_fwd, "dtype": "f64"}
+
+
 # ---- CPU restatement (oracle) timing ----------------------------------------------------------
 
 def _cpu_sample_worker(args):
@@ -421,6 +468,7 @@ def main():
             bb = dynamics_rate(sg, kind, "fp64", local, n // 4)
             extra[kind] = {"fp32": a, "fp64": bb, "speedup": a["site_steps_per_s"] / bb["site_steps_per_s"]}
         pt = run_tempering(sg, local)
+        extra["adjoint"] = run_adjoint(sg, local)
     barrier()
     ms = maxall(rb["ms"])
     value = world * args.steps * rb["nrep"] / (ms / 1000.0)
@@ -474,6 +522,7 @@ def main():
             "kernels": kernels,
             "langevin_site_steps": {"simple_cubic_16^3_dipole": extra.get("sc"), "triangular_48x48x4_SU3": extra.get("tri"),
                                     "tempering_256_replicas": pt},
+            "adjoint_c5": extra.get("adjoint"),
             "roofline": roof,
             "gpu_launches": rb["launches"],
             "clocks": rb["clocks"],

@@ -259,6 +259,39 @@ int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* desc, sgb_corr** ou
  * first batched add_sample). */
 int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, float* ms, int32_t* chosen);
 
+/* ---- adjoint: S(q,ω) loss gradient through a midpoint trajectory ------------ */
+/* No reverse rule exists in the reference; parameters follow the labelled-parameter
+ * convention of its fitting code (src/Fitting.jl:123-152, src/ModelParams.jl:140-150):
+ * the energy is linear in them, E(θ) = E_rest + Σ_k θ_k E_k, and parameter k is given by
+ * its unit coupling set E_k = (bonds of parameter k, onsite coefficients of parameter k).
+ * The caller keeps the system's own couplings equal to the current θ (sgb_set_bonds /
+ * sgb_set_onsite as usual). Supported: FP64 dipole-mode systems with bilinear pair
+ * couplings and onsite anisotropy of rank <= 2, damping 0, one cosine-window sample.
+ *
+ * typedef of the handle: */
+typedef struct sgb_adjoint sgb_adjoint;
+
+/* `desc` as for sgb_corr_create (dt, measperiod, tol; damping must be 0). `bonds` holds
+ * the unit bonds of every parameter back to back, nbonds[k] of parameter k; `onsite`
+ * is [nparams][natoms][28] Stevens coefficients (or NULL). 1 <= nparams <= 8. */
+int sgb_adjoint_create(sgb_system* sys, const sgb_corr_desc* desc, int32_t nparams, const sgb_bond* bonds,
+                       const int32_t* nbonds, const double* onsite, sgb_adjoint** out);
+void sgb_adjoint_destroy(sgb_adjoint* a);
+const char* sgb_adjoint_last_error(const sgb_adjoint* a);
+/* Target data in the layout of sgb_corr_data (complex [c,i,j,q1,q2,q3,ω], column-major). */
+int sgb_adjoint_set_target(sgb_adjoint* a, const double* target);
+/* From S0 (double[ns][3]): integrate measperiod*(nsnaps-1) midpoint steps recording
+ * snapshots (add_sample!, CorrelationSampling.jl:1-139), form the sample's S(q,ω) and
+ * loss = mean over all complex bins of |data - target|^2; then the discrete adjoint gives
+ * grad[k] = dloss/dθ_k and (if not NULL) grad_S0[ns][3] = dloss/dS0. The trajectory is
+ * checkpointed every `checkpoint` steps (rounded to whole measurement periods) and
+ * recomputed segment by segment. data_out (may be NULL) receives the sample's S(q,ω).
+ * Leaves the system in the final state of the trajectory. */
+int sgb_adjoint_loss_grad(sgb_adjoint* a, const double* S0, int32_t checkpoint, double* loss, double* grad,
+                          double* grad_S0, double* data_out);
+/* The forward half only: loss (and data_out) of the sample from S0. */
+int sgb_adjoint_loss(sgb_adjoint* a, const double* S0, double* loss, double* data_out);
+
 /* ---- measurement helpers ---------------------------------------------------- */
 
 /* CUDA-event timing on the handle's own stream: slot in [0, 8). */

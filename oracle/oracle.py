@@ -274,3 +274,14 @@ def replica_exchange(E, kT, system_ids, exch_start, uniforms):
             ids[i1], ids[i2] = ids[i2], ids[i1]
             acc[i1] = True
     return ids, acc
+
+
+# ---- S(q,w) loss of one sample, for finite-difference reference gradients -----------------
+
+def sqw_loss(osys: OracleSystem, obs_flat, nobs, corr_pairs, n_all_omega, measperiod, dt, tol, S0, target):
+    """mean over all complex bins of |data - target|^2, data = one add_sample! from S0
+    (CorrelationSampling.jl:1-139, cosine window), in FP64. Returns (loss, data)."""
+    oc = OracleCorrelations(osys, obs_flat, nobs, corr_pairs, n_all_omega, measperiod, dt, tol)
+    oc.add_sample(np.asarray(S0, dtype=float), None)
+    d = oc.data
+    return float(np.mean(np.abs(d - target) ** 2)), d

@@ -15,6 +15,7 @@ from .correlations import (SampledCorrelations, MeasureSpec, ssf_trace, ssf_perp
                            merge_correlations, available_energies, available_wave_vectors,
                            adjusted_dt_and_downsampling_factor, all_dipole_observables)
 from .tempering import ReplicaBatch, ParallelTempering
+from .adjoint import SampledCorrelationsAdjoint
 from ._abi import SunnyGPUError, load as load_library
 
 __all__ = [n for n in dir() if not n.startswith("_")]

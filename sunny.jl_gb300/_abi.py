@@ -92,6 +92,12 @@ SIGNATURES = {
     "sgb_batch_langevin_noise": (C.c_int, [_P, _I32, _U64, _U64, _D]),
     "sgb_batch_corr_create": (C.c_int, [_P, C.POINTER(CorrDesc), C.POINTER(_P)]),
     "sgb_batch_midpoint_shapes": (C.c_int, [_P, _I32, C.POINTER(_I32), C.POINTER(C.c_float), C.POINTER(_I32)]),
+    "sgb_adjoint_create": (C.c_int, [_P, C.POINTER(CorrDesc), _I32, _P, C.POINTER(_I32), _D, C.POINTER(_P)]),
+    "sgb_adjoint_destroy": (None, [_P]),
+    "sgb_adjoint_last_error": (C.c_char_p, [_P]),
+    "sgb_adjoint_set_target": (C.c_int, [_P, _D]),
+    "sgb_adjoint_loss_grad": (C.c_int, [_P, _D, _I32, _D, _D, _D, _D]),
+    "sgb_adjoint_loss": (C.c_int, [_P, _D, _D, _D]),
     "sgb_event_record": (C.c_int, [_P, _I32]),
     "sgb_event_elapsed": (C.c_int, [_P, _I32, _I32, C.POINTER(C.c_float)]),
     "sgb_batch_event_record": (C.c_int, [_P, _I32]),

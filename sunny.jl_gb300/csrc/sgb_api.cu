@@ -955,3 +955,12 @@ int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src) {
 }
 
 }  // extern "C"
+
+// ---- internal entry points used by the adjoint (sgb_adjoint.cu) -------------------------------
+int sgb_int_midpoint_snap(sgb_system* s, double dt, double tol, int max_iters, int nsteps, const SnapArgs<double>& sn,
+                          int64_t* iters) {
+    return run_midpoint<double>(s, dt, 0.0, tol, max_iters, nsteps, iters, sn);
+}
+void sgb_int_window_weights(int n, int window, std::vector<double>& g) { window_weights(n, window, g); }
+int sgb_int_ensure_tables(sgb_system* s) { return ensure_tables(s); }
+void sgb_int_set_error(const std::string& msg) { g_last_error = msg; }

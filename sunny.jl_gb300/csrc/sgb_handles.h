@@ -175,3 +175,10 @@ inline void sgb_detach_corrs(std::vector<sgb_corr*>& corrs) {
 // batched add_sample! trajectory (sgb_batch.cu)
 int batch_corr_trajectory(sgb_corr* c);
 const char* batch_error(sgb_batch* b);
+
+// internal entry points of sgb_api.cu used by the adjoint (sgb_adjoint.cu)
+int sgb_int_midpoint_snap(sgb_system* s, double dt, double tol, int max_iters, int nsteps, const SnapArgs<double>& sn,
+                          int64_t* iters);
+void sgb_int_window_weights(int n, int window, std::vector<double>& g);
+int sgb_int_ensure_tables(sgb_system* s);
+void sgb_int_set_error(const std::string& msg);
