@@ -170,7 +170,9 @@ typedef struct {
     double  damping;       /* ImplicitMidpoint damping (0 by default)                        */
     double  tol;           /* ImplicitMidpoint tol                                           */
     int32_t max_iters;     /* 100 in Sunny                                                   */
-    int32_t calculate_errors; /* keep the Welford M array (SampledCorrelations.jl:244)       */
+    int32_t calculate_errors; /* keep the Welford M array (SampledCorrelations.jl:244): each
+                                 sample is transformed and folded into the running mean and
+                                 M (CorrelationSampling.jl:117-134) instead of summed        */
 } sgb_corr_desc;
 
 /* SampledCorrelations(sys; measure, energies, dt, integrator=ImplicitMidpoint)
@@ -191,7 +193,8 @@ int sgb_corr_add_sample(sgb_corr* sc, int32_t window);
  * nsamples may be NULL. Either array pointer may be NULL. */
 int sgb_corr_data(sgb_corr* sc, double* data, double* M, int64_t* nsamples);
 
-/* merge_correlations([dst, src]) into dst (SampledCorrelations.jl:128-142). */
+/* merge_correlations([dst, src]) into dst (SampledCorrelations.jl:128-142), with M when
+ * both were created with calculate_errors (mixing the two kinds is SGB_ERR_ARG). */
 int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src);
 
 /* Per-phase device time of add_sample!, summed over the samples taken while profiling is
@@ -257,6 +260,13 @@ int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* desc, sgb_corr** ou
  * dynamic shared bytes) into shapes[cap][5] and their tuning times into ms[cap] (either
  * may be NULL); *chosen = the row in use. Returns the number of shapes (0 before the
  * first batched add_sample). */
+/* First fixed-point iterate of each batched midpoint step (no counterpart in the
+ * reference, which starts from S' = S, Integrators.jl:389): order 0 does the same; 1 and 2
+ * start from the linear / quadratic extrapolation of the last states, which reaches the
+ * same convergence test (sum |S'-S''|^2 <= (tol sqrt(ns))^2) in fewer iterations, so the
+ * result differs from order 0 only within the tolerance. Default: 2 for FP32 batches,
+ * 0 for FP64 batches. */
+int sgb_batch_set_midpoint_predictor(sgb_batch* b, int32_t order);
 int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, float* ms, int32_t* chosen);
 
 /* ---- adjoint: S(q,ω) loss gradient through a midpoint trajectory ------------ */

@@ -182,7 +182,7 @@ class OracleCorrelations:
     correlations). Layout of `data`: [c, i, j, q1, q2, q3, ω] like Sunny."""
 
     def __init__(self, osys: OracleSystem, obs_flat, nobs, corr_pairs, n_all_omega, measperiod, dt, tol,
-                 damping=0.0, max_iters=100):
+                 damping=0.0, max_iters=100, calculate_errors=False):
         self.o = osys
         self.obs_flat = obs_flat
         self.nobs = nobs
@@ -192,6 +192,7 @@ class OracleCorrelations:
         self.dt, self.tol, self.damping, self.max_iters = dt, tol, damping, max_iters
         L1, L2, L3 = osys.dims
         self.data = np.zeros((len(self.pairs), osys.na, osys.na, L1, L2, L3, n_all_omega), dtype=complex)
+        self.M = np.zeros(self.data.shape) if calculate_errors else None
         self.nsamples = 0
 
     def trajectory(self, S, Z):
@@ -238,12 +239,29 @@ class OracleCorrelations:
                         corr = corr * win
                     corr = np.fft.fft(corr, axis=3)
                     d = self.data[c, i, j]
-                    d += (corr - d) * (1.0 / count)
+                    if self.M is None:
+                        d += (corr - d) * (1.0 / count)
+                    else:
+                        # Welford update (CorrelationSampling.jl:117-134)
+                        mu_old = d.copy()
+                        d += (corr - d) / count
+                        self.M[c, i, j] += np.real((corr - mu_old) * np.conj(corr - d))
 
     def add_sample(self, S, Z, window="cosine"):
         buf, S, Z = self.trajectory(S, Z)
         self.accum(buf, window)
         return S, Z
+
+
+def merge_with_errors(datas, Ms, counts):
+    """merge_correlations with M (SampledCorrelations.jl:128-142)."""
+    d, M, n = datas[0].copy(), Ms[0].copy(), counts[0]
+    for d2, M2, m in zip(datas[1:], Ms[1:], counts[1:]):
+        mu = (n / (n + m)) * d + (m / (n + m)) * d2
+        M = (M + n * np.abs(mu - d) ** 2) + (M2 + m * np.abs(mu - d2) ** 2)
+        d = mu
+        n += m
+    return d, M, n
 
 
 def merge_means(datas, counts):

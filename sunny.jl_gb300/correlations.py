@@ -178,6 +178,16 @@ class SampledCorrelations:
         return (ncorr, na, na, *proto.dims, self.n_all_omega)
 
     @property
+    def M(self):
+        """sc.M: Welford sums of squared deviations [c, i, j, q1, q2, q3, ω] (calculate_errors=true), else None."""
+        if not self.calculate_errors:
+            return None
+        shp = self.shape
+        flat = np.zeros(int(np.prod(shp)))
+        self._check(self._lib.sgb_corr_data(self._h, None, _abi.dptr(flat), None))
+        return flat.reshape(shp[::-1]).transpose(tuple(range(len(shp) - 1, -1, -1)))
+
+    @property
     def data(self) -> np.ndarray:
         """sc.data: complex array indexed [c, i, j, q1, q2, q3, ω] (0-based)."""
         shp = self.shape
@@ -219,7 +229,7 @@ def merge_correlations(scs):
     d.damping = first.integrator.damping
     d.tol = first.integrator.tol
     d.max_iters = 100
-    d.calculate_errors = 0
+    d.calculate_errors = 1 if first.calculate_errors else 0
     lib = first._lib
     h = C.c_void_p()
     if first._batch is not None:

@@ -639,6 +639,9 @@ void sgb_corr_destroy(sgb_corr* c) {
     p = c->g; dfree(p);
     if (c->have_space) cufftDestroy(c->plan_space);
     if (c->have_time) cufftDestroy(c->plan_time);
+    if (c->have_chunk) cufftDestroy(c->plan_chunk);
+    p = c->M; dfree(p);
+    p = c->ctmp; dfree(p);
     for (int i = 0; i < 5; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     delete c;
 }
@@ -681,6 +684,11 @@ static int corr_setup(sgb_corr* c, const sgb_corr_desc* d, bool fp32, bool sun, 
     if ((rc = alloc((void**)&c->P, 16 * c->plen))) return rc;
     cudaMemset(c->P, 0, 16 * c->plen);
     if ((rc = alloc((void**)&c->g, sizeof(double) * c->nomega))) return rc;
+    if (d->calculate_errors) {
+        c->welford = true;
+        if ((rc = alloc((void**)&c->M, 8 * c->plen))) return rc;
+        cudaMemset(c->M, 0, 8 * c->plen);
+    }
     // cuFFT plans: space FFT over (L3, L2, L1) for every snapshot row; time FFT along ω
     const cufftType ty = fp32 ? CUFFT_C2C : CUFFT_Z2Z;
     int n3[3] = {dims[2], dims[1], dims[0]};
@@ -704,7 +712,6 @@ static int corr_check_desc(const sgb_corr_desc* d) {
     if (d->nobs < 1 || d->ncorr < 1 || !d->obs || !d->pairs) return fail(nullptr, SGB_ERR_ARG, "observables and correlation pairs are required");
     if (d->n_all_omega < 1 || d->measperiod < 1) return fail(nullptr, SGB_ERR_ARG, "n_all_omega and measperiod must be positive");
     if (d->n_all_omega > 1 && !(d->dt > 0)) return fail(nullptr, SGB_ERR_ARG, "Select positive dt");
-    if (d->calculate_errors) return fail(nullptr, SGB_ERR_ARG, "calculate_errors is not supported by this build of the accumulator");
     for (int k = 0; k < 2 * d->ncorr; k++)
         if (d->pairs[k] < 0 || d->pairs[k] >= d->nobs) return fail(nullptr, SGB_ERR_ARG, "correlation pair index out of range");
     return SGB_OK;
@@ -744,6 +751,7 @@ int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* d, sgb_corr** out) 
     };
     // midpoint-private buffers: room for one 4-element vector per site (FP32 float4 layout)
     if ((rc = lazy(&b->Sp, R * 4 * b->NS)) || (rc = lazy(&b->H, R * 12 * b->NS)) || (rc = lazy(&b->Sc, R * 4 * b->NS)) ||
+        (rc = lazy(&b->P1, R * 4 * b->NS)) || (rc = lazy(&b->H1, R * 4 * b->NS)) ||
         (rc = lazy((void**)&b->racc, sizeof(double) * 3 * b->nrep)))
         return rc;
     sgb_corr* c = new sgb_corr();
@@ -773,6 +781,53 @@ static void window_weights(int n, int window, std::vector<double>& g) {
         }
         g[k] = contrib <= 0 ? 0.0 : w / contrib / n;
     }
+}
+
+// calculate_errors path of add_sample!: for every replica's sample, in order, form the
+// products column chunk by column chunk, apply IFFT -> window/n_contrib/n -> FFT
+// (CorrelationSampling.jl:71-109) and update the running mean and M (:117-134).
+static int welford_samples(sgb_corr* c, const void* spec, bool fp32, size_t rep_stride) {
+    const int n = c->nomega;
+    const size_t ld = c->plen / n;
+    if (!c->ctmp) {
+        size_t chunk = std::max<size_t>(1, ((size_t)64 << 20) / ((size_t)16 * n));
+        c->chunk = std::min(chunk, ld);
+        if (cudaMalloc((void**)&c->ctmp, 16 * c->chunk * n) != cudaSuccess) {
+            c->ctmp = nullptr;
+            return cfail(c, SGB_ERR_NOMEM, "device allocation failed");
+        }
+        if (n > 1) {
+            int n1[1] = {n};
+            if (cufftPlanMany(&c->plan_chunk, 1, n1, nullptr, 1, n, nullptr, 1, n, CUFFT_Z2Z, (int)c->chunk) != CUFFT_SUCCESS)
+                return cfail(c, SGB_ERR_CUDA, "cufftPlanMany (per-sample transform) failed");
+            c->have_chunk = true;
+        }
+    }
+    if (c->have_chunk) cufftSetStream(c->plan_chunk, c->stream);
+    const size_t esz = fp32 ? 8 : 16;
+    for (int r = 0; r < c->nrep; r++) {
+        const void* Ar = (const char*)spec + esz * rep_stride * r;
+        const double count = (double)(c->nsamples + r + 1);
+        for (size_t col0 = 0; col0 < ld; col0 += c->chunk) {
+            const int ncol = (int)std::min(c->chunk, ld - col0);
+            int rc = fp32 ? corr_launch_product<float>((const float*)Ar, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, n,
+                                                       col0, ncol, c->ctmp, c->stream)
+                          : corr_launch_product<double>((const double*)Ar, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, n,
+                                                        col0, ncol, c->ctmp, c->stream);
+            if (rc) return cfail(c, SGB_ERR_CUDA, "product launch");
+            if (c->have_chunk &&
+                cufftExecZ2Z(c->plan_chunk, (cufftDoubleComplex*)c->ctmp, (cufftDoubleComplex*)c->ctmp, CUFFT_INVERSE) != CUFFT_SUCCESS)
+                return cfail(c, SGB_ERR_CUDA, "per-sample transform failed");
+            if (corr_launch_window(c->ctmp, ncol, n, c->g, c->stream)) return cfail(c, SGB_ERR_CUDA, "window launch");
+            if (c->have_chunk &&
+                cufftExecZ2Z(c->plan_chunk, (cufftDoubleComplex*)c->ctmp, (cufftDoubleComplex*)c->ctmp, CUFFT_FORWARD) != CUFFT_SUCCESS)
+                return cfail(c, SGB_ERR_CUDA, "per-sample transform failed");
+            if (corr_launch_welford(c->ctmp, ncol, n, col0, ld, count, c->P, c->M, c->stream))
+                return cfail(c, SGB_ERR_CUDA, "Welford launch");
+            (*c->launches) += 3;
+        }
+    }
+    return SGB_OK;
 }
 
 int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
@@ -841,13 +896,18 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
         spec = c->Ahat;
     }
     if (c->profile) cudaEventRecord(c->ev[3], c->stream);
-    // 4. accumulate sum_r conj(A_alpha,i) A_beta,j into the FP64 sum
-    rc = fp32 ? corr_launch_accum<float>((const float*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, c->nomega,
-                                         c->nrep, rep_stride, c->stream)
-              : corr_launch_accum<double>((const double*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell, c->nomega,
-                                          c->nrep, rep_stride, c->stream);
-    (*c->launches)++;
-    if (rc) return cfail(c, SGB_ERR_CUDA, std::string("accumulate launch: ") + cudaGetErrorString(cudaGetLastError()));
+    // 4. accumulate sum_r conj(A_alpha,i) A_beta,j into the FP64 sum, or (calculate_errors)
+    //    transform every sample and fold it into the running mean and M
+    if (c->welford) {
+        if ((rc = welford_samples(c, spec, fp32, rep_stride))) return rc;
+    } else {
+        rc = fp32 ? corr_launch_accum<float>((const float*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell,
+                                             c->nomega, c->nrep, rep_stride, c->stream)
+                  : corr_launch_accum<double>((const double*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell,
+                                              c->nomega, c->nrep, rep_stride, c->stream);
+        (*c->launches)++;
+        if (rc) return cfail(c, SGB_ERR_CUDA, std::string("accumulate launch: ") + cudaGetErrorString(cudaGetLastError()));
+    }
     c->nsamples += c->nrep;
     if (c->profile) {
         cudaEventRecord(c->ev[4], c->stream);
@@ -887,7 +947,16 @@ int sgb_corr_data(sgb_corr* c, double* data, double* M, int64_t* nsamples) {
     if (!c) return fail(nullptr, SGB_ERR_ARG, "null handle");
     cudaStream_t stream = c->stream;
     if (nsamples) *nsamples = c->nsamples;
-    if (M) return cfail(c, SGB_ERR_ARG, "calculate_errors is not supported by this build of the accumulator");
+    if (M && !c->welford) return cfail(c, SGB_ERR_ARG, "M is kept only with calculate_errors");
+    if (c->welford) {
+        // running mean and M are kept transformed, in Sunny's layout
+        cudaError_t e = cudaSuccess;
+        if (data) e = cudaMemcpyAsync(data, c->P, 16 * c->plen, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess && M) e = cudaMemcpyAsync(M, c->M, 8 * c->plen, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return cfail(c, SGB_ERR_CUDA, std::string("copy data: ") + cudaGetErrorString(e));
+        return SGB_OK;
+    }
     if (!data) return SGB_OK;
     const int n = c->nomega;
     const size_t ld = c->plen / n;  // columns
@@ -942,8 +1011,17 @@ int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src) {
         return cfail(dst, SGB_ERR_ARG, "accumulators have different shapes");
     if (src->nsamples > 0 && dst->window >= 0 && src->window >= 0 && dst->window != src->window)
         return cfail(dst, SGB_ERR_ARG, "accumulators used different windows");
+    if (dst->welford != src->welford)
+        return cfail(dst, SGB_ERR_ARG, "accumulators with and without calculate_errors cannot be merged");
     if (src->stream != dst->stream) cudaStreamSynchronize(src->stream);
-    if (corr_launch_add(dst->P, src->P, 2 * dst->plen, dst->stream) != SGB_OK) return cfail(dst, SGB_ERR_CUDA, "merge launch");
+    if (dst->welford) {
+        if (src->nsamples > 0 &&
+            corr_launch_merge_welford(dst->P, dst->M, src->P, src->M, (double)dst->nsamples, (double)src->nsamples,
+                                      dst->plen, dst->stream) != SGB_OK)
+            return cfail(dst, SGB_ERR_CUDA, "merge launch");
+    } else if (corr_launch_add(dst->P, src->P, 2 * dst->plen, dst->stream) != SGB_OK) {
+        return cfail(dst, SGB_ERR_CUDA, "merge launch");
+    }
     (*dst->launches)++;
     if (dst->window < 0 && src->window >= 0) {
         dst->window = src->window;

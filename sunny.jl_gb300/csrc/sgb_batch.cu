@@ -299,6 +299,9 @@ struct MidArgs {
     R* H;           // 3 rotating buffers of midpoint spins, MV<R>::W * NS elements each
     R* Sc;          // candidate new state (MV layout)
     double* racc;   // [3][nrep] FP64 convergence sums
+    R* P1;          // first iterate of the next step (MV layout), ord > 0
+    R* H1;          // state of the previous step (MV layout), ord == 2
+    int ord;        // initial iterate of each step: 0 S' = S (as the reference), 1 linear, 2 quadratic extrapolation
     int nrep;
     double atol2;
     int max_iters;
@@ -426,12 +429,17 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
     int done = 0;
     for (int step = 0; step < nsteps; ++step) {
         unsigned actm = (1u << ntb) - 1u;   // bit k: tile k's replica is still iterating
-        for (int k = 0; k < ntb; k++) {
-            const int4 ti = st_a[k];
-            if (tid >= ti.z) continue;
-            const int g = ti.w + ti.y + tid;
-            MV<R>::st(X.Sp, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
+        // first iterate S' = S; with extrapolation (ord > 0) the converging iteration of the
+        // previous step already stored it
+        if (step == 0 || X.ord == 0) {
+            for (int k = 0; k < ntb; k++) {
+                const int4 ti = st_a[k];
+                if (tid >= ti.z) continue;
+                const int g = ti.w + ti.y + tid;
+                MV<R>::st(X.Sp, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
+            }
         }
+        const int ord = min(X.ord, step + 1);   // extrapolation order available for the next step
         bool all_done = false;
         for (int it = 0; it < X.max_iters; ++it) {
             const int nxt = (cur + 1) % 3, nst = (cur + 2) % 3;
@@ -480,7 +488,17 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                         R cx = nx, cy = ny, cz = nz;
                         normalize_dip<R>(cx, cy, cz, kap);
                         MV<R>::st(X.Sc, NS, g, cx, cy, cz);
-                        R wx = (cx + cx) / 2, wy = (cy + cy) / 2, wz = (cz + cz) / 2;
+                        // next step's first iterate p and midpoint spin normalize((c + p)/2)
+                        R px = cx, py = cy, pz = cz;
+                        if (ord == 1) {
+                            px = 2 * cx - sx; py = 2 * cy - sy; pz = 2 * cz - sz;
+                        } else if (ord == 2) {
+                            R ux, uy, uz;
+                            MV<R>::ld(X.H1, NS, g, ux, uy, uz);
+                            px = 3 * (cx - sx) + ux; py = 3 * (cy - sy) + uy; pz = 3 * (cz - sz) + uz;
+                        }
+                        if (ord > 0) MV<R>::st(X.P1, NS, g, px, py, pz);
+                        R wx = (cx + px) / 2, wy = (cy + py) / 2, wz = (cz + pz) / 2;
                         normalize_dip<R>(wx, wy, wz, kap);
                         MV<R>::st(Hs, NS, g, wx, wy, wz);
                     } else {
@@ -524,6 +542,12 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                         const int g = ti.w + ti.y + tid;
                         R x, y, z;
                         MV<R>::ld(X.Sc, NS, g, x, y, z);
+                        if (X.ord > 0) {
+                            if (X.ord == 2) MV<R>::st(X.H1, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
+                            R px, py, pz;
+                            MV<R>::ld(X.P1, NS, g, px, py, pz);
+                            MV<R>::st(X.Sp, NS, g, px, py, pz);
+                        }
                         A.S[g] = x; A.S[NS + g] = y; A.S[2 * NS + g] = z;
                     }
                 }
@@ -738,9 +762,10 @@ using MidKernel = void (*)(BatchArgs<R>, MidArgs<R>, int, R, R, BSnap<R>, int);
 
 template <class R, bool GEN>
 static MidKernel<R> mid_kernel(int idx, int G) {
-    if (idx == 2) return G == 9 ? k_batch_midpoint<R, GEN, 2, 9> : k_batch_midpoint<R, GEN, 2, 6>;
-    if (idx == 4) return G == 9 ? k_batch_midpoint<R, GEN, 4, 9> : k_batch_midpoint<R, GEN, 4, 6>;
-    return G == 9 ? k_batch_midpoint<R, GEN, 0, 9> : k_batch_midpoint<R, GEN, 0, 6>;
+    (void)G;   // 6 bonds gathered together: 9 spilled registers and was slower in every tuning run
+    if (idx == 2) return k_batch_midpoint<R, GEN, 2, 6>;
+    if (idx == 4) return k_batch_midpoint<R, GEN, 4, 6>;
+    return k_batch_midpoint<R, GEN, 0, 6>;
 }
 
 template <class R, bool GEN>
@@ -751,7 +776,7 @@ static int mid_shapes(sgb_batch* b, std::vector<MidShape>& out) {
     const int maxbps = sizeof(R) == 4 ? 3 : 2;
     for (int idx : {isz, 0}) {
         if (idx != 0 && b->kb == 0) continue;
-        for (int G : {6, 9}) {
+        for (int G : {6}) {
             for (int bps = maxbps; bps >= std::max(1, maxbps - 1); bps--) {
                 const long long g = std::min<long long>((long long)bps * b->nsm, b->ntiles);
                 const long long ntb = (b->ntiles + g - 1) / g;
@@ -837,6 +862,9 @@ static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
     X.H = (R*)b->H;
     X.Sc = (R*)b->Sc;
     X.racc = b->racc;
+    X.P1 = (R*)b->P1;
+    X.H1 = (R*)b->H1;
+    X.ord = b->mid_order;
     X.nrep = b->nrep;
     double atol = c->tol * std::sqrt((double)(b->off[1] - b->off[0]));
     X.atol2 = atol * atol;
@@ -895,7 +923,7 @@ void sgb_batch_destroy(sgb_batch* b) {
     p = b->nbr; bfree(p);
     p = b->nbo; bfree(p);
     p = b->td; bfree(p);
-    bfree(b->S); bfree(b->P); bfree(b->D1); bfree(b->Sp); bfree(b->H); bfree(b->Sc);
+    bfree(b->S); bfree(b->P); bfree(b->D1); bfree(b->Sp); bfree(b->H); bfree(b->Sc); bfree(b->P1); bfree(b->H1);
     p = b->racc; bfree(p); p = b->ctrl; bfree(p); p = b->Epart; bfree(p); p = b->E; bfree(p);
     p = b->counters; bfree(p); p = b->n_accept; bfree(p);
     if (b->stage) cudaFreeHost(b->stage);
@@ -915,6 +943,7 @@ int sgb_batch_create(const sgb_desc* d, int32_t nrep, const int32_t* dims, sgb_b
     b->nrep = nrep;
     b->na = d->natoms;
     b->fp32 = d->precision == SGB_FP32;
+    b->mid_order = b->fp32 ? 2 : 0;
     b->dims.assign(dims, dims + 3 * nrep);
     b->off.assign(nrep + 1, 0);
     long long tot = 0;
@@ -1309,6 +1338,13 @@ int sgb_batch_step_ensemble(sgb_batch* b, double dt, double damping, uint64_t se
 }
 
 int sgb_batch_graph_active(const sgb_batch* b) { return b && b->graph ? 1 : 0; }
+
+int sgb_batch_set_midpoint_predictor(sgb_batch* b, int32_t order) {
+    if (!b) return bfail(nullptr, SGB_ERR_ARG, "null handle");
+    if (order < 0 || order > 2) return bfail(b, SGB_ERR_ARG, "predictor order must be 0, 1 or 2");
+    b->mid_order = order;
+    return SGB_OK;
+}
 
 int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, float* ms, int32_t* chosen) {
     if (!b) return SGB_ERR_ARG;

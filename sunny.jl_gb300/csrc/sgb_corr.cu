@@ -139,6 +139,63 @@ __global__ void k_add_inplace(double* __restrict__ dst, const double* __restrict
         dst[e] += src[e];
 }
 
+// Per-sample products of columns [col0, col0 + ncol) of one replica's spectra, in the
+// read-out layout tmp[col - col0][ω] (col = c + ncorr (i + npos (j + npos q))):
+//     conj(A_{α,i}(q, ω)) A_{β,j}(q, ω).
+template <class R>
+__global__ void k_product_cols(const R* __restrict__ A, const int* __restrict__ pairs, int ncorr, int nobs, int npos,
+                               int ncell, int n, size_t col0, int ncol, double2* __restrict__ tmp) {
+    const size_t total = (size_t)ncol * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int w = (int)(e % n);
+        const size_t col = col0 + e / n;
+        const int c = (int)(col % ncorr);
+        size_t t = col / ncorr;
+        const int i = (int)(t % npos);
+        t /= npos;
+        const int j = (int)(t % npos);
+        const int q = (int)(t / npos);
+        const size_t ia = (((size_t)w * nobs + pairs[2 * c]) * npos + i) * ncell + q;
+        const size_t ib = (((size_t)w * nobs + pairs[2 * c + 1]) * npos + j) * ncell + q;
+        const double ax = A[2 * ia], ay = A[2 * ia + 1], bx = A[2 * ib], by = A[2 * ib + 1];
+        tmp[e] = make_double2(ax * bx + ay * by, ax * by - ay * bx);
+    }
+}
+
+// Welford update of the running mean and M with one transformed sample x (read-out
+// layout, columns [col0, col0 + ncol)), CorrelationSampling.jl:117-134:
+//   μ_old = mean; mean += (x - mean) / count; M += Re((x - μ_old) conj(x - mean)).
+// mean and M use Sunny's layout, index ω * ld + col.
+__global__ void k_welford_cols(const double2* __restrict__ tmp, int ncol, int n, size_t col0, size_t ld, double count,
+                               double2* __restrict__ mean, double* __restrict__ M) {
+    const size_t total = (size_t)ncol * n;
+    const double inv = 1.0 / count;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int w = (int)(e / ncol), cl = (int)(e % ncol);
+        const double2 x = tmp[(size_t)cl * n + w];
+        const size_t idx = (size_t)w * ld + col0 + cl;
+        const double2 m0 = mean[idx];
+        const double2 m1 = make_double2(m0.x + (x.x - m0.x) * inv, m0.y + (x.y - m0.y) * inv);
+        mean[idx] = m1;
+        const double dx0 = x.x - m0.x, dy0 = x.y - m0.y, dx1 = x.x - m1.x, dy1 = x.y - m1.y;
+        M[idx] += dx0 * dx1 + dy0 * dy1;
+    }
+}
+
+// merge_correlations with errors (SampledCorrelations.jl:128-142):
+//   μ = n/(n+m) d1 + m/(n+m) d2; M1 = (M1 + n|μ - d1|²) + (M2 + m|μ - d2|²); d1 = μ.
+__global__ void k_merge_welford(double2* __restrict__ d1, double* __restrict__ M1, const double2* __restrict__ d2,
+                                const double* __restrict__ M2, double n, double m, size_t len) {
+    const double a = n / (n + m), b = m / (n + m);
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < len; e += (size_t)gridDim.x * blockDim.x) {
+        const double2 x = d1[e], y = d2[e];
+        const double2 mu = make_double2(a * x.x + b * y.x, a * x.y + b * y.y);
+        const double ex = mu.x - x.x, ey = mu.y - x.y, fx = mu.x - y.x, fy = mu.y - y.y;
+        M1[e] = (M1[e] + n * (ex * ex + ey * ey)) + (M2[e] + m * (fx * fx + fy * fy));
+        d1[e] = mu;
+    }
+}
+
 int grid_for(size_t n) {
     size_t g = (n + 255) / 256;
     if (g > 65535) g = 65535;
@@ -147,6 +204,30 @@ int grid_for(size_t n) {
 }
 
 }  // namespace
+
+template <class R>
+int corr_launch_product(const R* A, const int* pairs, int ncorr, int nobs, int npos, int ncell, int n, size_t col0,
+                        int ncol, double* tmp, cudaStream_t st) {
+    k_product_cols<R><<<grid_for((size_t)ncol * n), 256, 0, st>>>(A, pairs, ncorr, nobs, npos, ncell, n, col0, ncol,
+                                                                   reinterpret_cast<double2*>(tmp));
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+template int corr_launch_product<float>(const float*, const int*, int, int, int, int, int, size_t, int, double*, cudaStream_t);
+template int corr_launch_product<double>(const double*, const int*, int, int, int, int, int, size_t, int, double*, cudaStream_t);
+
+int corr_launch_welford(const double* tmp, int ncol, int n, size_t col0, size_t ld, double count, double* mean, double* M,
+                        cudaStream_t st) {
+    k_welford_cols<<<grid_for((size_t)ncol * n), 256, 0, st>>>(reinterpret_cast<const double2*>(tmp), ncol, n, col0, ld,
+                                                                count, reinterpret_cast<double2*>(mean), M);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+int corr_launch_merge_welford(double* d1, double* M1, const double* d2, const double* M2, double n, double m, size_t len,
+                              cudaStream_t st) {
+    k_merge_welford<<<grid_for(len), 256, 0, st>>>(reinterpret_cast<double2*>(d1), M1, reinterpret_cast<const double2*>(d2),
+                                                   M2, n, m, len);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
 
 template <class R>
 int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,

@@ -11,3 +11,11 @@ int corr_launch_gather(const double* P, size_t ld, size_t col0, int ncol, int n,
 int corr_launch_window(double* tmp, int ncol, int n, const double* g, cudaStream_t st);
 int corr_launch_scatter(const double* tmp, int ncol, int n, double* out, cudaStream_t st);
 int corr_launch_add(double* dst, const double* src, size_t n, cudaStream_t st);
+// calculate_errors: per-sample products of a column range, Welford update, merge with M
+template <class R>
+int corr_launch_product(const R* A, const int* pairs, int ncorr, int nobs, int npos, int ncell, int n, size_t col0,
+                        int ncol, double* tmp, cudaStream_t st);
+int corr_launch_welford(const double* tmp, int ncol, int n, size_t col0, size_t ld, double count, double* mean, double* M,
+                        cudaStream_t st);
+int corr_launch_merge_welford(double* d1, double* M1, const double* d2, const double* M2, double n, double m, size_t len,
+                              cudaStream_t st);

@@ -78,6 +78,14 @@ struct sgb_corr {
     cudaStream_t stream = nullptr;  // the owner's stream; null (default stream) once the owner is destroyed
     long long* launches = nullptr;  // the owner's launch counter, else own_launches
     long long own_launches = 0;
+    // calculate_errors: P holds the running mean of the transformed samples (not their
+    // sum) and M the Welford sums of squared deviations, both in Sunny's layout
+    bool welford = false;
+    double* M = nullptr;
+    double* ctmp = nullptr;         // [chunk][n] complex work buffer of the per-sample transform
+    size_t chunk = 0;
+    cufftHandle plan_chunk = 0;
+    bool have_chunk = false;
 };
 
 
@@ -144,6 +152,9 @@ struct sgb_batch {
     void* Sp = nullptr;             // midpoint iterate
     void* H = nullptr;              // midpoint rotating buffers [3][3][NS]
     void* Sc = nullptr;             // midpoint candidate
+    void* P1 = nullptr;             // next step's first midpoint iterate (extrapolated)
+    void* H1 = nullptr;             // previous step's state (quadratic extrapolation)
+    int mid_order = 0;              // initial-iterate extrapolation order of the batched midpoint
     double* racc = nullptr;         // [3][nrep] convergence sums
     Ctrl* ctrl = nullptr;
     double* Epart = nullptr;        // [ntiles]

@@ -121,6 +121,12 @@ class ReplicaBatch:
         self._check(self._lib.sgb_batch_langevin_noise(self._h, r, self.seed, step, _abi.dptr(out)))
         return out
 
+    def set_midpoint_predictor(self, order: int):
+        """First iterate of each batched midpoint step: 0 S' = S (the reference's choice),
+        1 / 2 linear / quadratic extrapolation of the last states (fewer iterations, same
+        convergence test). Default 2 for FP32, 0 for FP64."""
+        self._check(self._lib.sgb_batch_set_midpoint_predictor(self._h, int(order)))
+
     def energies(self) -> np.ndarray:
         out = np.zeros(self.nrep)
         self._check(self._lib.sgb_batch_energy(self._h, _abi.dptr(out)))

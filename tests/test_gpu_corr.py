@@ -9,6 +9,10 @@ from models import oracle_of, rich_sun
 pytestmark = pytest.mark.gpu
 
 
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
 def diamond_reference_model(sg, precision="fp64"):
     # the configuration of test_correlation_sampling.jl:156-169 (diamond 2x3x4, s=3/2, J=0.6498)
     sys_ = sg.System(sg.diamond_crystal(), [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(2, 3, 4), seed=101,
@@ -147,12 +151,15 @@ def test_accumulator_outlives_its_system(gpu, sg):
     sc.close()
 
 
-def test_batched_fp32_sqw_per_bin_error(gpu, sg, orc):
+@pytest.mark.parametrize("order", [0, 2])
+def test_batched_fp32_sqw_per_bin_error(gpu, sg, orc, order):
     # the headline path: FP32 replicas sampled in one batched add_sample (tol 1e-6)
-    # against the FP64 oracle's running mean over the same initial states
+    # against the FP64 oracle's running mean over the same initial states, with the
+    # reference's first iterate (order 0) and with the extrapolated one (order 2, default)
     proto = diamond_reference_model(sg, "fp64")
     kw = dict(energies=np.linspace(0.0, 5.5, 10), dt=0.12)
     b = sg.ReplicaBatch(proto, [proto.dims] * 3, kT=[0.2] * 3, precision="fp32", seed=4)
+    b.set_midpoint_predictor(order)
     b.randomize_spins()
     states = [b.get_state(r) for r in range(3)]
     sc = sg.SampledCorrelations(b, measure=sg.ssf_perp(proto), tol=1e-6, **kw)
@@ -165,4 +172,84 @@ def test_batched_fp32_sqw_per_bin_error(gpu, sg, orc):
     err = np.abs(sc.data - ref)
     assert np.all(err <= 0.01 * np.abs(ref) + 1e-4 * np.max(np.abs(ref)))
     sc.close()
+    b.close()
+
+
+def test_calculate_errors_parity_and_merge(gpu, sg, orc):
+    # calculate_errors=true: running mean and Welford M against the oracle
+    # (CorrelationSampling.jl:117-134), and merge with M (SampledCorrelations.jl:128-142)
+    sys_ = diamond_reference_model(sg)
+    kw = dict(measure=sg.ssf_perp(sys_), energies=np.linspace(0.0, 5.5, 10), dt=0.12, calculate_errors=True)
+    sc0, sc1, sc2 = (sg.SampledCorrelations(sys_, **kw) for _ in range(3))
+    o, oc = oracle_corr(orc, sys_, sc0)
+    oc.M = np.zeros(oc.data.shape)
+    rng = np.random.default_rng(23)
+    states = []
+    for _ in range(3):
+        S = rng.standard_normal((sys_.nsites, 3))
+        states.append(1.5 * S / np.linalg.norm(S, axis=1)[:, None])
+    for k, S in enumerate(states):
+        sys_.set_state_flat(dipoles=S)
+        sg.add_sample(sc0, sys_)
+        sys_.set_state_flat(dipoles=S)
+        sg.add_sample(sc1 if k == 0 else sc2, sys_)
+        oc.add_sample(S, None)
+    scale = np.max(np.abs(oc.data))
+    assert np.max(np.abs(sc0.data - oc.data)) < 1e-10 * scale
+    assert np.max(np.abs(sc0.M - oc.M)) < 1e-10 * np.max(np.abs(oc.M))
+    merged = sg.merge_correlations([sc1, sc2])
+    assert merged.nsamples == 3
+    assert np.max(np.abs(merged.data - sc0.data)) < 1e-12 * scale
+    assert np.max(np.abs(merged.M - sc0.M)) < 1e-10 * np.max(np.abs(sc0.M))
+    # accumulators with and without errors do not merge
+    plain = sg.SampledCorrelations(sys_, measure=sg.ssf_perp(sys_), energies=np.linspace(0.0, 5.5, 10), dt=0.12)
+    with pytest.raises(sg.SunnyGPUError, match="calculate_errors"):
+        sg.merge_correlations([sc0, plain])
+
+
+def test_batched_calculate_errors_equals_single(gpu, sg):
+    # one batched add_sample over 3 replicas == 3 single add_samples, mean and M
+    cr = sg.diamond_crystal()
+    proto = sg.System(cr, [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(2, 3, 2), seed=101, device=None)
+    proto.set_exchange(0.6498, sg.Bond(1, 3, [0, 0, 0]))
+    b = sg.ReplicaBatch(proto, [(2, 3, 2)] * 3, kT=[0.2] * 3, seed=2)
+    b.randomize_spins()
+    states = [b.get_state(r) for r in range(3)]
+    kw = dict(energies=np.linspace(0, 5.5, 10), dt=0.12, calculate_errors=True)
+    scb = sg.SampledCorrelations(b, measure=sg.ssf_perp(proto), **kw)
+    sg.add_sample(scb, b)
+    single = sg.System(cr, [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(2, 3, 2), seed=101)
+    single.set_exchange(0.6498, sg.Bond(1, 3, [0, 0, 0]))
+    scs = sg.SampledCorrelations(single, measure=sg.ssf_perp(single), **kw)
+    for r in range(3):
+        single.set_state_flat(dipoles=states[r])
+        sg.add_sample(scs, single)
+    assert np.max(np.abs(scb.data - scs.data)) < 1e-11 * np.max(np.abs(scs.data))
+    assert np.max(np.abs(scb.M - scs.M)) < 1e-10 * np.max(np.abs(scs.M))
+    scb.close()
+    b.close()
+
+
+def test_batched_predictor_reaches_the_same_fixed_point(gpu, sg):
+    # FP64 batch with the quadratic first iterate against the single-system path (which
+    # starts from S' = S as the reference does): equal within the midpoint tolerance
+    cr = sg.diamond_crystal()
+    proto = sg.System(cr, [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(2, 3, 2), seed=101, device=None)
+    proto.set_exchange(0.6498, sg.Bond(1, 3, [0, 0, 0]))
+    b = sg.ReplicaBatch(proto, [(2, 3, 2)] * 2, kT=[0.2] * 2, seed=2)
+    b.set_midpoint_predictor(2)
+    b.randomize_spins()
+    states = [b.get_state(r) for r in range(2)]
+    kw = dict(energies=np.linspace(0, 5.5, 10), dt=0.12)
+    scb = sg.SampledCorrelations(b, measure=sg.ssf_perp(proto), **kw)
+    sg.add_sample(scb, b)
+    single = sg.System(cr, [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(2, 3, 2), seed=101)
+    single.set_exchange(0.6498, sg.Bond(1, 3, [0, 0, 0]))
+    scs = sg.SampledCorrelations(single, measure=sg.ssf_perp(single), **kw)
+    for r in range(2):
+        single.set_state_flat(dipoles=states[r])
+        sg.add_sample(scs, single)
+        assert rel(b.get_state(r), single.dipoles_flat()) < 1e-9
+    assert rel(scb.data, scs.data) < 1e-9
+    scb.close()
     b.close()

@@ -265,3 +265,33 @@ def test_replica_exchange_detailed_balance(orc):
     assert acc[0] == (lnP01 >= 0)
     lnP23 = (E[2] - E[3]) * (1 / kT[2] - 1 / kT[3])
     assert acc[2] == (lnP23 >= 0 or 0.999 < np.exp(lnP23))
+
+
+def test_welford_errors_merge_oracle(sg, orc, host):
+    # test_correlation_sampling.jl:104-136 with calculate_errors=true: merging 1 + 2
+    # samples gives the data and M of the 3-sample running accumulation
+    cryst = sg.fcc_primitive_crystal()
+    h = host(cryst, 1, "dipole", dims=(3, 3, 3))
+    h.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    o = _osys(orc, h)
+    rng = np.random.default_rng(17)
+    from sunny_gb300.correlations import adjusted_dt_and_downsampling_factor, CORR_PAIRS
+    energies = np.linspace(0, 10.0, 8)
+    dt, mp = adjusted_dt_and_downsampling_factor(0.08, len(energies), energies[-1])
+    n = 2 * (len(energies) - 1)
+    obs = np.tile(np.eye(3)[:, None, :], (1, h.nsites, 1)).reshape(-1)
+    mk = lambda: orc.OracleCorrelations(o, obs, 3, CORR_PAIRS, n, mp, dt, 1e-12, calculate_errors=True)
+    sc0, sc1, sc2 = mk(), mk(), mk()
+    states = []
+    for _ in range(3):
+        S = rng.standard_normal((h.nsites, 3))
+        states.append(S / np.linalg.norm(S, axis=1)[:, None])
+    for k, S in enumerate(states):
+        sc0.add_sample(S, None)
+        (sc1 if k == 0 else sc2).add_sample(S, None)
+    d, M, nn = orc.merge_with_errors([sc1.data, sc2.data], [sc1.M, sc2.M], [1, 2])
+    assert nn == 3
+    assert np.allclose(d, sc0.data, rtol=1e-12, atol=1e-13 * np.max(np.abs(sc0.data)))
+    assert np.allclose(M, sc0.M, rtol=1e-10, atol=1e-12 * np.max(np.abs(sc0.M)))
+    # M is the sum of squared deviations from the final mean
+    assert np.max(sc0.M) > 0 and np.min(sc0.M) > -1e-12 * np.max(sc0.M)
