@@ -152,13 +152,15 @@ def run_arm(sg, precision, device, warmup, steps, tol, thermal_steps=2000, e2e_s
     return res
 
 
-def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000):
+def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000, predictor=None):
     """Batched FP32 sampling: `nrep` replicas of the pyrochlore model advance in one
     persistent launch; each add_sample adds nrep samples with a rank-nrep accumulator pass."""
     import ctypes as C
     lib = sg.load_library()
     proto = build_system(sg, "fp32", None)
     b = sg.ReplicaBatch(proto, [proto.dims] * nrep, kT=[0.2] * nrep, precision="fp32", device=device, seed=7)
+    if predictor is not None:
+        b.set_midpoint_predictor(predictor)
     b.randomize_spins()
     b.langevin(DT, 0.1, thermal_steps)
     sc = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), energies=np.linspace(0, WMAX, NOMEGA), dt=DT, tol=tol)
@@ -418,6 +420,8 @@ def main():
     ap.add_argument("--nrep", type=int, default=8, help="replicas sampled per batched add_sample")
     ap.add_argument("--nomega", type=int, default=200, help="energy bins (200 is the benchmark; fewer for profiling)")
     ap.add_argument("--no-extra", action="store_true", help="skip the tempering and Langevin site-step arms")
+    ap.add_argument("--predictor", type=int, default=None,
+                    help="first-iterate extrapolation order of the batched midpoint (library default if omitted)")
     args = ap.parse_args()
     global L, NOMEGA
     L = args.L
@@ -454,7 +458,7 @@ def main():
         return float(t.item())
 
     barrier()
-    rb = run_batched(sg, local, args.nrep, args.warmup, args.steps, tol=1e-6)
+    rb = run_batched(sg, local, args.nrep, args.warmup, args.steps, tol=1e-6, predictor=args.predictor)
     barrier()
     r32 = run_arm(sg, "fp32", local, args.warmup, max(2, args.steps // 2), tol=1e-6)
     # (single-system FP32 path: one replica per add_sample)

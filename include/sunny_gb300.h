@@ -261,11 +261,11 @@ int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* desc, sgb_corr** ou
  * may be NULL); *chosen = the row in use. Returns the number of shapes (0 before the
  * first batched add_sample). */
 /* First fixed-point iterate of each batched midpoint step (no counterpart in the
- * reference, which starts from S' = S, Integrators.jl:389): order 0 does the same; 1 and 2
- * start from the linear / quadratic extrapolation of the last states, which reaches the
- * same convergence test (sum |S'-S''|^2 <= (tol sqrt(ns))^2) in fewer iterations, so the
- * result differs from order 0 only within the tolerance. Default: 2 for FP32 batches,
- * 0 for FP64 batches. */
+ * reference, which starts from S' = S, Integrators.jl:389): order 0 does the same; order
+ * k in 1..4 starts from the degree-k polynomial extrapolation of the last k+1 states,
+ * which reaches the same convergence test (sum |S'-S''|^2 <= (tol sqrt(ns))^2) in fewer
+ * iterations, so the result differs from order 0 only within the tolerance. Default:
+ * 4 for FP32 batches, 0 for FP64 batches. */
 int sgb_batch_set_midpoint_predictor(sgb_batch* b, int32_t order);
 int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, float* ms, int32_t* chosen);
 

@@ -300,8 +300,10 @@ struct MidArgs {
     R* Sc;          // candidate new state (MV layout)
     double* racc;   // [3][nrep] FP64 convergence sums
     R* P1;          // first iterate of the next step (MV layout), ord > 0
-    R* H1;          // state of the previous step (MV layout), ord == 2
-    int ord;        // initial iterate of each step: 0 S' = S (as the reference), 1 linear, 2 quadratic extrapolation
+    R* H1;          // states of the 1st, 2nd and 3rd previous steps (MV layout), ord >= 2, 3, 4
+    R* H2;
+    R* H3;
+    int ord;        // initial iterate of each step: 0 S' = S (as the reference), k > 0 polynomial extrapolation of order k
     int nrep;
     double atol2;
     int max_iters;
@@ -492,10 +494,26 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                         R px = cx, py = cy, pz = cz;
                         if (ord == 1) {
                             px = 2 * cx - sx; py = 2 * cy - sy; pz = 2 * cz - sz;
-                        } else if (ord == 2) {
+                        } else if (ord >= 2) {
+                            // Newton backward differences through c = S_{n+1}, s = S_n, S_{n-1}, ...
                             R ux, uy, uz;
                             MV<R>::ld(X.H1, NS, g, ux, uy, uz);
-                            px = 3 * (cx - sx) + ux; py = 3 * (cy - sy) + uy; pz = 3 * (cz - sz) + uz;
+                            if (ord == 2) {
+                                px = 3 * (cx - sx) + ux; py = 3 * (cy - sy) + uy; pz = 3 * (cz - sz) + uz;
+                            } else {
+                                R vx, vy, vz;
+                                MV<R>::ld(X.H2, NS, g, vx, vy, vz);
+                                if (ord == 3) {
+                                    px = 4 * (cx + ux) - 6 * sx - vx; py = 4 * (cy + uy) - 6 * sy - vy;
+                                    pz = 4 * (cz + uz) - 6 * sz - vz;
+                                } else {
+                                    R wx0, wy0, wz0;
+                                    MV<R>::ld(X.H3, NS, g, wx0, wy0, wz0);
+                                    px = 5 * (cx - vx) + 10 * (ux - sx) + wx0;
+                                    py = 5 * (cy - vy) + 10 * (uy - sy) + wy0;
+                                    pz = 5 * (cz - vz) + 10 * (uz - sz) + wz0;
+                                }
+                            }
                         }
                         if (ord > 0) MV<R>::st(X.P1, NS, g, px, py, pz);
                         R wx = (cx + px) / 2, wy = (cy + py) / 2, wz = (cz + pz) / 2;
@@ -543,7 +561,18 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                         R x, y, z;
                         MV<R>::ld(X.Sc, NS, g, x, y, z);
                         if (X.ord > 0) {
-                            if (X.ord == 2) MV<R>::st(X.H1, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
+                            // shift the history: S_{n-2} -> H3, S_{n-1} -> H2, S_n -> H1
+                            if (X.ord >= 4) {
+                                R hx, hy, hz;
+                                MV<R>::ld(X.H2, NS, g, hx, hy, hz);
+                                MV<R>::st(X.H3, NS, g, hx, hy, hz);
+                            }
+                            if (X.ord >= 3) {
+                                R hx, hy, hz;
+                                MV<R>::ld(X.H1, NS, g, hx, hy, hz);
+                                MV<R>::st(X.H2, NS, g, hx, hy, hz);
+                            }
+                            if (X.ord >= 2) MV<R>::st(X.H1, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
                             R px, py, pz;
                             MV<R>::ld(X.P1, NS, g, px, py, pz);
                             MV<R>::st(X.Sp, NS, g, px, py, pz);
@@ -864,6 +893,8 @@ static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
     X.racc = b->racc;
     X.P1 = (R*)b->P1;
     X.H1 = (R*)b->H1;
+    X.H2 = (R*)b->H2;
+    X.H3 = (R*)b->H3;
     X.ord = b->mid_order;
     X.nrep = b->nrep;
     double atol = c->tol * std::sqrt((double)(b->off[1] - b->off[0]));
@@ -923,7 +954,7 @@ void sgb_batch_destroy(sgb_batch* b) {
     p = b->nbr; bfree(p);
     p = b->nbo; bfree(p);
     p = b->td; bfree(p);
-    bfree(b->S); bfree(b->P); bfree(b->D1); bfree(b->Sp); bfree(b->H); bfree(b->Sc); bfree(b->P1); bfree(b->H1);
+    bfree(b->S); bfree(b->P); bfree(b->D1); bfree(b->Sp); bfree(b->H); bfree(b->Sc); bfree(b->P1); bfree(b->H1); bfree(b->H2); bfree(b->H3);
     p = b->racc; bfree(p); p = b->ctrl; bfree(p); p = b->Epart; bfree(p); p = b->E; bfree(p);
     p = b->counters; bfree(p); p = b->n_accept; bfree(p);
     if (b->stage) cudaFreeHost(b->stage);
@@ -943,7 +974,7 @@ int sgb_batch_create(const sgb_desc* d, int32_t nrep, const int32_t* dims, sgb_b
     b->nrep = nrep;
     b->na = d->natoms;
     b->fp32 = d->precision == SGB_FP32;
-    b->mid_order = b->fp32 ? 2 : 0;
+    b->mid_order = b->fp32 ? 4 : 0;
     b->dims.assign(dims, dims + 3 * nrep);
     b->off.assign(nrep + 1, 0);
     long long tot = 0;
@@ -1341,7 +1372,7 @@ int sgb_batch_graph_active(const sgb_batch* b) { return b && b->graph ? 1 : 0; }
 
 int sgb_batch_set_midpoint_predictor(sgb_batch* b, int32_t order) {
     if (!b) return bfail(nullptr, SGB_ERR_ARG, "null handle");
-    if (order < 0 || order > 2) return bfail(b, SGB_ERR_ARG, "predictor order must be 0, 1 or 2");
+    if (order < 0 || order > 4) return bfail(b, SGB_ERR_ARG, "predictor order must be in 0..4");
     b->mid_order = order;
     return SGB_OK;
 }

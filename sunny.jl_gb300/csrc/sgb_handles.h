@@ -153,7 +153,9 @@ struct sgb_batch {
     void* H = nullptr;              // midpoint rotating buffers [3][3][NS]
     void* Sc = nullptr;             // midpoint candidate
     void* P1 = nullptr;             // next step's first midpoint iterate (extrapolated)
-    void* H1 = nullptr;             // previous step's state (quadratic extrapolation)
+    void* H1 = nullptr;             // states of the three previous steps (extrapolation history)
+    void* H2 = nullptr;
+    void* H3 = nullptr;
     int mid_order = 0;              // initial-iterate extrapolation order of the batched midpoint
     double* racc = nullptr;         // [3][nrep] convergence sums
     Ctrl* ctrl = nullptr;

@@ -123,8 +123,8 @@ class ReplicaBatch:
 
     def set_midpoint_predictor(self, order: int):
         """First iterate of each batched midpoint step: 0 S' = S (the reference's choice),
-        1 / 2 linear / quadratic extrapolation of the last states (fewer iterations, same
-        convergence test). Default 2 for FP32, 0 for FP64."""
+        k in 1..4 the degree-k extrapolation of the last k+1 states (fewer iterations, same
+        convergence test). Default 4 for FP32, 0 for FP64."""
         self._check(self._lib.sgb_batch_set_midpoint_predictor(self._h, int(order)))
 
     def energies(self) -> np.ndarray:

@@ -151,7 +151,7 @@ def test_accumulator_outlives_its_system(gpu, sg):
     sc.close()
 
 
-@pytest.mark.parametrize("order", [0, 2])
+@pytest.mark.parametrize("order", [0, 2, 4])
 def test_batched_fp32_sqw_per_bin_error(gpu, sg, orc, order):
     # the headline path: FP32 replicas sampled in one batched add_sample (tol 1e-6)
     # against the FP64 oracle's running mean over the same initial states, with the
@@ -231,13 +231,13 @@ def test_batched_calculate_errors_equals_single(gpu, sg):
 
 
 def test_batched_predictor_reaches_the_same_fixed_point(gpu, sg):
-    # FP64 batch with the quadratic first iterate against the single-system path (which
+    # FP64 batch with the order-4 first iterate against the single-system path (which
     # starts from S' = S as the reference does): equal within the midpoint tolerance
     cr = sg.diamond_crystal()
     proto = sg.System(cr, [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(2, 3, 2), seed=101, device=None)
     proto.set_exchange(0.6498, sg.Bond(1, 3, [0, 0, 0]))
     b = sg.ReplicaBatch(proto, [(2, 3, 2)] * 2, kT=[0.2] * 2, seed=2)
-    b.set_midpoint_predictor(2)
+    b.set_midpoint_predictor(4)
     b.randomize_spins()
     states = [b.get_state(r) for r in range(2)]
     kw = dict(energies=np.linspace(0, 5.5, 10), dt=0.12)
