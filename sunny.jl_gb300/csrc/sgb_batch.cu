@@ -487,6 +487,10 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                         R mx = (sx + nx) / 2, my = (sy + ny) / 2, mz = (sz + nz) / 2;
                         normalize_dip<R>(mx, my, mz, kap);
                         MV<R>::st(Hn, NS, g, mx, my, mz);
+                        // With an extrapolated first iterate the step is never accepted at its
+                        // first iteration (see the convergence mask below), so the next-step data
+                        // are only prepared from the second iteration on.
+                        if (X.ord == 0 || it > 0) {
                         R cx = nx, cy = ny, cz = nz;
                         normalize_dip<R>(cx, cy, cz, kap);
                         MV<R>::st(X.Sc, NS, g, cx, cy, cz);
@@ -519,6 +523,7 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
                         R wx = (cx + px) / 2, wy = (cy + py) / 2, wz = (cz + pz) / 2;
                         normalize_dip<R>(wx, wy, wz, kap);
                         MV<R>::st(Hs, NS, g, wx, wy, wz);
+                        }
                     } else {
                         // converged replica: carry its next-step midpoint spins forward
                         R x, y, z;
@@ -545,8 +550,11 @@ __global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midp
             // one thread per block compares the FP64 sums with the tolerance
             if (tid == 0) {
                 unsigned long long m = 0;
-                for (int q = 0; q < X.nrep; q++)
-                    if (X.racc[slot * X.nrep + q] <= X.atol2) m |= 1ull << q;
+                // the convergence test of the reference, Σ|S' - S''|² <= atol²; with an
+                // extrapolated first iterate it is applied from the second iteration on
+                if (X.ord == 0 || it > 0)
+                    for (int q = 0; q < X.nrep; q++)
+                        if (X.racc[slot * X.nrep + q] <= X.atol2) m |= 1ull << q;
                 conv_mask = m;
             }
             __syncthreads();

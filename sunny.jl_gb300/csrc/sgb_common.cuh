@@ -41,14 +41,20 @@ __host__ __device__ inline double biquad_metric(int q) {
 // %globaltimer; on expiry the kernel records SGB_ERR_TIMEOUT and returns, so that a
 // stuck barrier never hangs the GPU.
 // ---------------------------------------------------------------------------------
-// Control words of one persistent launch. The barrier words, the convergence sums and
+// Control words of one persistent launch. The barrier word, the convergence sums and
 // the status live on separate 128-byte lines so that spinning, atomics and flag reads
 // do not contend for one L2 line.
+//
+// The barrier word packs the arrival count (bits 0-31), the generation (bits 32-62) and
+// an abort flag (bit 63) that sgb_set_status raises, so that an arrival returns the
+// generation it waits on and a waiter sees an error in the word it polls: no extra
+// loads on the barrier's critical path.
+#define SGB_BAR_GEN 0x100000000ull
+#define SGB_BAR_ABORT 0x8000000000000000ull
 struct alignas(128) Ctrl {
-    unsigned int bar_count;
-    unsigned int pad0[31];
-    unsigned int bar_gen;
-    unsigned int pad1[31];
+    unsigned long long bar;
+    unsigned int pad0[30];
+    unsigned int pad1[32];
     double acc[3];       // rotating FP64 convergence accumulators
     double pad2[13];
     int status;
@@ -66,6 +72,8 @@ __device__ __forceinline__ uint64_t sgb_globaltimer() {
 
 __device__ __forceinline__ void sgb_set_status(Ctrl* c, int code) {
     atomicCAS(&c->status, 0, code);
+    __threadfence();
+    atomicOr(&c->bar, SGB_BAR_ABORT);   // waiters at a barrier leave at once
 }
 
 __device__ __forceinline__ int sgb_read_status(Ctrl* c) {
@@ -77,25 +85,31 @@ __device__ __forceinline__ int sgb_read_status(Ctrl* c) {
 // Barrier across `nblocks` co-resident CTAs (cooperative launch guarantees residency).
 // Memory written before the barrier by any CTA is visible to plain loads of every CTA
 // after it (fences around the arrival, as cooperative-groups grid sync does).
-// Returns false if the wait timed out or another CTA flagged an error.
+// Returns false if the wait timed out or some CTA raised an error (sgb_set_status).
 __device__ __forceinline__ bool sgb_grid_barrier(Ctrl* c, unsigned int nblocks) {
     __shared__ int ok_s;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
         if (nblocks > 1) {
-            cuda::atomic_ref<unsigned int, cuda::thread_scope_device> cnt(c->bar_count);
-            cuda::atomic_ref<unsigned int, cuda::thread_scope_device> gen(c->bar_gen);
+            cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> bar(c->bar);
             __threadfence();
-            unsigned int g = gen.load(cuda::memory_order_acquire);
-            unsigned int prev = cnt.fetch_add(1u, cuda::memory_order_acq_rel);
-            if (prev == nblocks - 1) {
-                cnt.store(0u, cuda::memory_order_relaxed);
-                gen.fetch_add(1u, cuda::memory_order_release);
+            const unsigned long long prev = bar.fetch_add(1ull, cuda::memory_order_acq_rel);
+            const unsigned long long gen = prev >> 32;   // generation and abort flag
+            if (prev & SGB_BAR_ABORT) {
+                ok = 0;
+            } else if ((unsigned int)prev == nblocks - 1) {
+                // last arrival: count back to 0 and the next generation, in one release
+                bar.fetch_add(SGB_BAR_GEN - nblocks, cuda::memory_order_release);
             } else {
                 uint64_t t0 = 0;
                 unsigned int spins = 0;
-                while (gen.load(cuda::memory_order_acquire) == g) {
+                for (;;) {
+                    const unsigned long long now = bar.load(cuda::memory_order_acquire);
+                    if ((now >> 32) != gen) {
+                        if (now & SGB_BAR_ABORT) ok = 0;
+                        break;
+                    }
                     if ((++spins & 255u) == 0) {
                         uint64_t t = sgb_globaltimer();
                         if (t0 == 0) t0 = t;
@@ -108,8 +122,10 @@ __device__ __forceinline__ bool sgb_grid_barrier(Ctrl* c, unsigned int nblocks) 
                 }
             }
             __threadfence();
+        } else if (cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>(c->bar).load(
+                       cuda::memory_order_relaxed) & SGB_BAR_ABORT) {
+            ok = 0;
         }
-        if (ok && sgb_read_status(c) != 0) ok = 0;
         ok_s = ok;
     }
     __syncthreads();
