@@ -229,13 +229,9 @@ int corr_launch_merge_welford(double* d1, double* M1, const double* d2, const do
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
-template <class R>
-int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
-                      int nrep, size_t rep_stride, cudaStream_t st) {
-    constexpr int QT = 32;
-    size_t smem = (size_t)nrep * nobs * (npos + 1) * QT * sizeof(C2<R>) + 2 * ncorr * sizeof(int) + 16;
-    if (smem > 200 * 1024) return SGB_ERR_ARG;
-    if (ncorr * npos * npos > 8 * 256) return SGB_ERR_ARG;   // at most 8 accumulator entries per thread and row
+template <class R, int QT>
+static int accum_qt(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
+                    int nrep, size_t rep_stride, size_t smem, cudaStream_t st) {
     if (smem > 48 * 1024) {
         if (cudaFuncSetAttribute(k_corr_accum<R, QT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return SGB_ERR_CUDA;
@@ -243,6 +239,20 @@ int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int no
     dim3 grid((ncell + QT - 1) / QT, nomega);
     k_corr_accum<R, QT><<<grid, 256, smem, st>>>(A, P, pairs, ncorr, nobs, npos, ncell, nomega, nrep, rep_stride);
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+// The q tile shrinks (32 -> 16 -> 8 wave vectors per CTA) when many replicas' spectra
+// would not fit in shared memory.
+template <class R>
+int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
+                      int nrep, size_t rep_stride, cudaStream_t st) {
+    if (ncorr * npos * npos > 8 * 256) return SGB_ERR_ARG;   // at most 8 accumulator entries per thread and row
+    auto bytes = [&](int qt) { return (size_t)nrep * nobs * (npos + 1) * qt * sizeof(C2<R>) + 2 * ncorr * sizeof(int) + 16; };
+    const size_t lim = 200 * 1024;
+    if (bytes(32) <= lim) return accum_qt<R, 32>(A, P, pairs, ncorr, nobs, npos, ncell, nomega, nrep, rep_stride, bytes(32), st);
+    if (bytes(16) <= lim) return accum_qt<R, 16>(A, P, pairs, ncorr, nobs, npos, ncell, nomega, nrep, rep_stride, bytes(16), st);
+    if (bytes(8) <= lim) return accum_qt<R, 8>(A, P, pairs, ncorr, nobs, npos, ncell, nomega, nrep, rep_stride, bytes(8), st);
+    return SGB_ERR_ARG;
 }
 
 int corr_launch_gather(const double* P, size_t ld, size_t col0, int ncol, int n, double scale, double* tmp, cudaStream_t st) {
