@@ -369,7 +369,7 @@ struct MV<double> {
 // IDX 2 keeps indices as uint16 (replicas of at most 65,536 sites), IDX 4 as int32,
 // IDX 0 reads them from the global table. G is the number of bonds gathered together.
 template <class R, bool GEN, int IDX, int G>
-__global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_midpoint(BatchArgs<R> A, MidArgs<R> X, int nsteps, R dt,
+__global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) k_batch_midpoint(BatchArgs<R> A, MidArgs<R> X, int nsteps, R dt,
                                                                 R lam, BSnap<R> sn, int kb) {
     using IT = typename std::conditional<IDX == 2, unsigned short, int>::type;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -799,10 +799,11 @@ using MidKernel = void (*)(BatchArgs<R>, MidArgs<R>, int, R, R, BSnap<R>, int);
 
 template <class R, bool GEN>
 static MidKernel<R> mid_kernel(int idx, int G) {
-    (void)G;   // 6 bonds gathered together: 9 spilled registers and was slower in every tuning run
-    if (idx == 2) return k_batch_midpoint<R, GEN, 2, 6>;
-    if (idx == 4) return k_batch_midpoint<R, GEN, 4, 6>;
-    return k_batch_midpoint<R, GEN, 0, 6>;
+    // G = 6 runs 3 CTAs per SM within 80 registers; G = 12 keeps twice as many neighbour
+    // loads in flight per thread and runs 2 CTAs per SM within 128 registers (no spills)
+    if (idx == 2) return G == 12 ? k_batch_midpoint<R, GEN, 2, 12> : k_batch_midpoint<R, GEN, 2, 6>;
+    if (idx == 4) return G == 12 ? k_batch_midpoint<R, GEN, 4, 12> : k_batch_midpoint<R, GEN, 4, 6>;
+    return G == 12 ? k_batch_midpoint<R, GEN, 0, 12> : k_batch_midpoint<R, GEN, 0, 6>;
 }
 
 template <class R, bool GEN>
@@ -813,8 +814,9 @@ static int mid_shapes(sgb_batch* b, std::vector<MidShape>& out) {
     const int maxbps = sizeof(R) == 4 ? 3 : 2;
     for (int idx : {isz, 0}) {
         if (idx != 0 && b->kb == 0) continue;
-        for (int G : {6}) {
-            for (int bps = maxbps; bps >= std::max(1, maxbps - 1); bps--) {
+        for (int G : {6, 12}) {
+            const int top = G == 12 ? 2 : maxbps;
+            for (int bps = top; bps >= std::max(1, top - 1); bps--) {
                 const long long g = std::min<long long>((long long)bps * b->nsm, b->ntiles);
                 const long long ntb = (b->ntiles + g - 1) / g;
                 if (ntb > SGB_MAXT) continue;
