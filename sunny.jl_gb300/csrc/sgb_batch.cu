@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) 
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(A.M, smem);
     IT* sidx = reinterpret_cast<IT*>(smem + A.M.tables_bytes);   // [tile][bond][SGB_TILE]
-    __shared__ double sacc[SGB_MAXREP_CORR];
+    __shared__ R wpart[SGB_MAXT][SGB_TILE / 32];   // per-warp convergence partials of each tile
     __shared__ unsigned long long conv_mask;   // bit q: replica q met the tolerance this iteration
     __shared__ int4 st_a[SGB_MAXT];            // (replica, first site, count, replica offset)
     __shared__ int2 st_b[SGB_MAXT];            // (replica sites, neighbour-table offset)
@@ -449,8 +449,6 @@ __global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) 
             R* Hn = X.H + (size_t)nxt * MV<R>::W * NS;
             R* Hs = X.H + (size_t)nst * MV<R>::W * NS;
             const int slot = (int)(itg % 3);
-            for (int q = tid; q < X.nrep; q += blockDim.x) sacc[q] = 0.0;
-            __syncthreads();
             for (int k = 0; k < ntb; k++) {
                 const int4 ti = st_a[k];
                 const bool on = (actm >> k) & 1u;
@@ -532,15 +530,21 @@ __global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) 
                     }
                 }
                 if (on) {
-                    // warp sum, then one shared-memory FP64 atomic per warp (tiles never straddle replicas)
+                    // warp sum in R, kept per warp (no shared-memory FP64 atomics)
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-                    if ((tid & 31) == 0) atomicAdd(&sacc[ti.x], (double)acc);
+                    if ((tid & 31) == 0) wpart[k][tid >> 5] = acc;
                 }
             }
             __syncthreads();
-            for (int q = tid; q < X.nrep; q += blockDim.x)
-                if (sacc[q] != 0.0) atomicAdd(&X.racc[slot * X.nrep + q], sacc[q]);
+            // one thread per active tile: the tile's sum of its warps' partials, added in FP64
+            // to its replica's grid sum (tiles never straddle replicas)
+            if (tid < ntb && ((actm >> tid) & 1u)) {
+                R t = 0;
+#pragma unroll
+                for (int w = 0; w < SGB_TILE / 32; w++) t += wpart[tid][w];
+                atomicAdd(&X.racc[slot * X.nrep + st_a[tid].x], (double)t);
+            }
             if (leader) {
                 for (int q = 0; q < X.nrep; q++) X.racc[((slot + 1) % 3) * X.nrep + q] = 0.0;
                 A.ctrl->iters += 1;
