@@ -193,6 +193,20 @@ int sgb_corr_add_sample(sgb_corr* sc, int32_t window);
  * nsamples may be NULL. Either array pointer may be NULL. */
 int sgb_corr_data(sgb_corr* sc, double* data, double* M, int64_t* nsamples);
 
+/* The phase-averaged, combined part of intensities(sc, qpts; energies, kT)
+ * (DataRetrieval.jl:77-171, PhaseAveraging.jl), on the device. For nq wave vectors given
+ * by their index in the accumulator's q grid, qidx[k] = m1 + L1 (m2 + L2 m3) with the
+ * caller's rounding and wrapping (DataRetrieval.jl pruned_wave_vector_info), their
+ * per-atom prefactors pref[k][npos][2] = form factor × exp(-2πi q·r_atom) (complex), and
+ * nw energy indices widx into the n_all_omega axis, writes
+ *   combiner 0: out[k][t] = tr Re S(q, ω)                        (ssf_trace)
+ *   combiner 1: out[k][t] = tr Re S - q·Re S·q / |q|², 2/3 tr at q = 0 (ssf_perp, qcart[k][3])
+ *   combiner 2: out[k][t][ncorr][2] = the phase-averaged correlation elements
+ * Combiners 0 and 1 need the six ssf_* correlation pairs. The conversion to a density
+ * (1/(n_all_omega Δω)) and the classical-to-quantum factor are left to the caller. */
+int sgb_corr_intensities(sgb_corr* sc, int32_t nq, const int32_t* qidx, const double* pref, const double* qcart,
+                         int32_t nw, const int32_t* widx, int32_t combiner, double* out);
+
 /* merge_correlations([dst, src]) into dst (SampledCorrelations.jl:128-142), with M when
  * both were created with calculate_errors (mixing the two kinds is SGB_ERR_ARG). */
 int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src);

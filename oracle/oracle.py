@@ -303,3 +303,33 @@ def sqw_loss(osys: OracleSystem, obs_flat, nobs, corr_pairs, n_all_omega, measpe
     oc.add_sample(np.asarray(S0, dtype=float), None)
     d = oc.data
     return float(np.mean(np.abs(d - target) ** 2)), d
+
+
+# ---- intensities (DataRetrieval.jl:1-181, PhaseAveraging.jl) -------------------------------
+
+def intensities(data, recipvecs, positions, dims, qs, widx, combiner, n_all_omega, dw, kT=None, ws=None,
+                formfactors=None):
+    """intensities_aux! and the density / classical-to-quantum post-processing, on the raw
+    data [c, i, j, q1, q2, q3, w]. qs in RLU; widx are energy indices; combiner(q_abs,
+    elems) is the MeasureSpec combiner. Returns [w, q]."""
+    Ls = np.asarray(dims)
+    npos = data.shape[1]
+    out = np.zeros((len(widx), len(qs)))
+    for k, q in enumerate(qs):
+        m = np.rint(np.asarray(q) * Ls).astype(int)
+        i1, i2, i3 = np.mod(m, Ls)
+        qabs = recipvecs @ (m / Ls)
+        ff = np.ones(npos) if formfactors is None else np.array([f(qabs @ qabs) for f in formfactors])
+        pref = ff * np.exp(-2j * np.pi * ((m / Ls) @ np.asarray(positions).T))
+        for t, w in enumerate(widx):
+            elems = np.zeros(data.shape[0], dtype=complex)
+            for j in range(npos):
+                for i in range(npos):
+                    elems += (pref[i] * np.conj(pref[j])) * data[:, i, j, i1, i2, i3, w]
+            out[t, k] = combiner(qabs, elems)
+    if dw is not None and not np.isnan(dw):
+        out /= n_all_omega * dw
+        if kT is not None:
+            c2q = np.array([1.0 if w == 0 else abs((w / kT) / (1 - np.exp(-w / kT))) for w in ws])
+            out *= c2q[:, None]
+    return out

@@ -13,7 +13,8 @@ from .system import (System, Moment, Langevin, ImplicitMidpoint, step, energy, e
                      randomize_spins, polarize_spins, langevin_noise)
 from .correlations import (SampledCorrelations, MeasureSpec, ssf_trace, ssf_perp, ssf_custom, add_sample,
                            merge_correlations, available_energies, available_wave_vectors,
-                           adjusted_dt_and_downsampling_factor, all_dipole_observables)
+                           adjusted_dt_and_downsampling_factor, all_dipole_observables, intensities,
+                           intensities_static, Intensities)
 from .tempering import ReplicaBatch, ParallelTempering
 from .adjoint import SampledCorrelationsAdjoint
 from ._abi import SunnyGPUError, load as load_library

@@ -72,6 +72,7 @@ SIGNATURES = {
     "sgb_corr_destroy": (None, [_P]),
     "sgb_corr_add_sample": (C.c_int, [_P, _I32]),
     "sgb_corr_data": (C.c_int, [_P, _D, _D, C.POINTER(_I64)]),
+    "sgb_corr_intensities": (C.c_int, [_P, _I32, C.POINTER(_I32), _D, _D, _I32, C.POINTER(_I32), _I32, _D]),
     "sgb_corr_merge": (C.c_int, [_P, _P]),
     "sgb_corr_profile": (C.c_int, [_P, _I32]),
     "sgb_corr_phase_times": (C.c_int, [_P, _D, C.POINTER(_I64), C.POINTER(_I64)]),

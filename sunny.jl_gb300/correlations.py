@@ -21,10 +21,12 @@ CORR_PAIRS = [(3, 3), (2, 3), (1, 3), (2, 2), (1, 2), (1, 1)]  # MeasureSpec.jl:
 class MeasureSpec:
     """Observables (nobs per site) and 1-based correlation pairs (MeasureSpec.jl:5-27)."""
 
-    def __init__(self, observables: np.ndarray, corr_pairs, combiner=None):
+    def __init__(self, observables: np.ndarray, corr_pairs, combiner=None, kind: str = "custom", formfactors=None):
         self.observables = observables      # dipole: (nobs, ns, 3); SU(N): (nobs, ns, N, N) complex
         self.corr_pairs = list(corr_pairs)
         self.combiner = combiner
+        self.kind = kind                    # "trace" / "perp" run the combiner on the device
+        self.formfactors = formfactors      # per atom: callable of |q|^2, or None for 1
 
     @property
     def nobs(self):
@@ -53,16 +55,20 @@ def ssf_custom(f, sys: System, apply_g: bool = True) -> MeasureSpec:
     return MeasureSpec(all_dipole_observables(sys, apply_g), CORR_PAIRS, combiner)
 
 
-def ssf_trace(sys: System, apply_g: bool = True) -> MeasureSpec:
-    return ssf_custom(lambda q, ssf: np.trace(ssf.real), sys, apply_g)
+def ssf_trace(sys: System, apply_g: bool = True, formfactors=None) -> MeasureSpec:
+    m = ssf_custom(lambda q, ssf: np.trace(ssf.real), sys, apply_g)
+    m.kind, m.formfactors = "trace", formfactors
+    return m
 
 
-def ssf_perp(sys: System, apply_g: bool = True) -> MeasureSpec:
+def ssf_perp(sys: System, apply_g: bool = True, formfactors=None) -> MeasureSpec:
     def f(q, ssf):
         q2 = float(np.dot(q, q))
         ssf = ssf.real
         return (2 / 3) * np.trace(ssf) if q2 == 0 else np.trace(ssf) - q @ ssf @ q / q2
-    return ssf_custom(f, sys, apply_g)
+    m = ssf_custom(f, sys, apply_g)
+    m.kind, m.formfactors = "perp", formfactors
+    return m
 
 
 def adjusted_dt_and_downsampling_factor(dt: float, nw: int, wmax: float):
@@ -261,3 +267,113 @@ def available_wave_vectors(sc: SampledCorrelations):
     lo = [1 - L // 2 - o for L, o in zip(Ls, offs)]
     grids = [np.arange(l, h + 1) / L for l, h, L in zip(lo, hi, Ls)]
     return np.stack(np.meshgrid(*grids, indexing="ij"), -1)
+
+
+# ---- intensities (DataRetrieval.jl:1-181, PhaseAveraging.jl) ---------------------------------
+
+class Intensities:
+    """Intensities(crystal, qpts, energies, data): data[ω, q] (static: data[q])."""
+
+    def __init__(self, crystal, qpts, energies, data):
+        self.crystal, self.qpts, self.energies, self.data = crystal, qpts, energies, data
+
+
+def _energy_indices(sc: SampledCorrelations, energies):
+    """Energy axis indices (DataRetrieval.jl:64-71, 85-95)."""
+    n = sc.n_all_omega
+    if math.isnan(sc.dw):
+        return np.array([math.nan]), np.array([0], dtype=np.int32)
+    if isinstance(energies, str) and energies == "available":
+        w = available_energies(sc)
+        return w, np.arange(len(w), dtype=np.int32)
+    if isinstance(energies, str) and energies == "available_with_negative":
+        w = available_energies(sc, negative_energies=True)
+        return w, np.arange(n, dtype=np.int32)
+    ref = available_energies(sc, negative_energies=True)
+    energies = np.asarray(energies, dtype=float)
+    if np.any(np.diff(energies) < 0):
+        raise ValueError("Specified energies must be an ordered list.")
+    if energies.min() < ref.min() or energies.max() > ref.max():
+        raise ValueError("Specified energies includes values for which there is no available data.")
+    idx = []
+    for val in energies:
+        # find_idx_of_nearest_fft_energy (DataRetrieval.jl:37-58)
+        found = None
+        for i in range(len(ref) - 1):
+            x1, x2 = ref[i], ref[i + 1]
+            if x1 <= val <= x2:
+                found = i if abs(x1 - val) < abs(x2 - val) else i + 1
+                break
+        if found is None and ref[-1] <= val <= 0.0:
+            found = len(ref) - 1 if abs(ref[-1] - val) <= abs(val) else 0
+        if found is None:
+            raise ValueError("Value does not lie in bounds of reference list.")
+        idx.append(found)
+    idx = np.array(idx, dtype=np.int32)
+    return ref[idx], idx
+
+
+def intensities(sc: SampledCorrelations, qpts, *, energies="available", kT=None):
+    """intensities(sc, qpts; energies, kT) (DataRetrieval.jl:77-143): wave vectors in RLU
+    are rounded to the accumulator's grid (pruned_wave_vector_info), phase-averaged with
+    form factors and combined on the device; returns data[ω, q]."""
+    if kT is not None and kT <= 0:
+        raise ValueError("Positive `kT` required for classical-to-quantum corrections, or set `kT=nothing` to disable.")
+    proto = sc._batch.proto if sc._batch is not None else sc.sys
+    cr = proto.crystal
+    Ls = np.array(proto.dims)
+    qs = np.atleast_2d(np.asarray(qpts, dtype=float))
+    ms = np.rint(qs * Ls[None, :]).astype(np.int64)           # round to nearest (ties to even)
+    wrapped = np.mod(ms, Ls[None, :])
+    qidx = np.ascontiguousarray(wrapped[:, 0] + Ls[0] * (wrapped[:, 1] + Ls[1] * wrapped[:, 2]), dtype=np.int32)
+    qrlu = ms / Ls[None, :]
+    qabs = qrlu @ cr.recipvecs.T                                # recipvecs * (m ./ dims)
+    pos = np.array([cr._pos[a] for a in range(proto.natoms)])
+    ffs = sc.measure.formfactors
+    q2 = np.sum(qabs * qabs, axis=1)
+    ff = np.ones((len(qs), proto.natoms))
+    if ffs is not None:
+        for a, f in enumerate(ffs):
+            if f is not None:
+                ff[:, a] = [f(x) for x in q2]
+    pref = ff * np.exp(-2j * np.pi * (qrlu @ pos.T))           # prefactors_for_phase_averaging
+    pbuf = np.ascontiguousarray(np.stack([pref.real, pref.imag], -1).reshape(-1))
+    ws, widx = _energy_indices(sc, energies)
+    widx = np.ascontiguousarray(widx, dtype=np.int32)
+    kind = sc.measure.kind
+    comb = {"trace": 0, "perp": 1}.get(kind, 2)
+    if comb < 2 and [tuple(p) for p in sc.measure.corr_pairs] != CORR_PAIRS:
+        comb = 2
+    nq, nw = len(qs), len(widx)
+    ncorr = len(sc.measure.corr_pairs)
+    out = np.zeros(nq * nw * (2 * ncorr if comb == 2 else 1))
+    qc = np.ascontiguousarray(qabs, dtype=float).reshape(-1)
+    sc._check(sc._lib.sgb_corr_intensities(sc._h, nq, qidx.ctypes.data_as(C.POINTER(C.c_int32)), _abi.dptr(pbuf),
+                                           _abi.dptr(qc), nw, widx.ctypes.data_as(C.POINTER(C.c_int32)), comb,
+                                           _abi.dptr(out)))
+    if comb == 2:
+        el = out.reshape(nq, nw, ncorr, 2)
+        el = el[..., 0] + 1j * el[..., 1]
+        vals = np.array([[sc.measure.combiner(qabs[k], el[k, t]) for t in range(nw)] for k in range(nq)], dtype=float)
+    else:
+        vals = out.reshape(nq, nw)
+    data = vals.T.copy()                                       # [ω, q]
+    if not math.isnan(sc.dw):
+        data /= sc.n_all_omega * sc.dw
+        if kT is not None:
+            c2q = np.array([1.0 if w == 0 else abs((w / kT) / (1 - math.exp(-w / kT))) for w in ws])
+            data *= c2q[:, None]
+        return Intensities(cr, qs, ws, data)
+    return Intensities(cr, qs, None, data[0])
+
+
+def intensities_static(sc: SampledCorrelations, qpts, *, bounds=(-math.inf, math.inf), kT=None):
+    """intensities_static (DataRetrieval.jl:159-177): energy-integrated intensities."""
+    if math.isnan(sc.dw):
+        return intensities(sc, qpts, energies="available", kT=None)
+    ws = available_energies(sc, negative_energies=True)
+    sel = [w for w in ws if bounds[0] <= w < bounds[1]]
+    if not sel:
+        raise ValueError("No information available within specified energy `bounds`. Try a larger interval.")
+    res = intensities(sc, qpts, kT=kT, energies=sorted(sel))
+    return Intensities(res.crystal, res.qpts, None, res.data.sum(axis=0) * sc.dw)

@@ -1006,6 +1006,90 @@ int sgb_corr_data(sgb_corr* c, double* data, double* M, int64_t* nsamples) {
     return SGB_OK;
 }
 
+int sgb_corr_intensities(sgb_corr* c, int32_t nq, const int32_t* qidx, const double* pref, const double* qcart,
+                         int32_t nw, const int32_t* widx, int32_t combiner, double* out) {
+    if (!c || nq < 0 || nw < 1 || (nq > 0 && (!qidx || !pref || !out)) || !widx) return cfail(c, SGB_ERR_ARG, "invalid arguments");
+    if (combiner < 0 || combiner > 2) return cfail(c, SGB_ERR_ARG, "combiner must be 0 (trace), 1 (perp) or 2 (raw)");
+    if (combiner == 1 && !qcart) return cfail(c, SGB_ERR_ARG, "the perpendicular combiner needs the absolute wave vectors");
+    if (combiner < 2 && c->ncorr != 6) return cfail(c, SGB_ERR_ARG, "trace and perp combiners need the six ssf correlation pairs");
+    if (c->ncorr > 8) return cfail(c, SGB_ERR_ARG, "at most 8 correlation pairs");
+    const int n = c->nomega;
+    for (int t = 0; t < nw; t++)
+        if (widx[t] < 0 || widx[t] >= n) return cfail(c, SGB_ERR_ARG, "energy index out of range");
+    for (int k = 0; k < nq; k++)
+        if (qidx[k] < 0 || qidx[k] >= c->ncell) return cfail(c, SGB_ERR_ARG, "wave vector index out of range");
+    const size_t per_out = combiner == 2 ? (size_t)2 * c->ncorr : 1;
+    if (nq == 0) return SGB_OK;
+    if (c->nsamples == 0) {
+        std::memset(out, 0, sizeof(double) * per_out * nw * nq);
+        return SGB_OK;
+    }
+    cudaStream_t st = c->stream;
+    const int B = c->ncorr * c->npos * c->npos;
+    const size_t ld = c->plen / n;
+    const size_t per_q = (size_t)B * n * 16;
+    const int qc = (int)std::max<size_t>(1, std::min<size_t>((size_t)nq, ((size_t)256 << 20) / per_q));
+    double *tmp = nullptr, *pref_d = nullptr, *qcart_d = nullptr, *out_d = nullptr;
+    int *qidx_d = nullptr, *widx_d = nullptr;
+    int status = SGB_OK;
+    std::string what;
+    auto al = [&](void** p, size_t bytes) { if (status == SGB_OK && cudaMalloc(p, bytes) != cudaSuccess) { *p = nullptr; status = SGB_ERR_NOMEM; what = "device allocation failed"; } };
+    al((void**)&tmp, per_q * qc);
+    al((void**)&pref_d, 16 * (size_t)c->npos * qc);
+    al((void**)&qcart_d, 24 * (size_t)qc);
+    al((void**)&out_d, sizeof(double) * per_out * nw * qc);
+    al((void**)&qidx_d, sizeof(int) * qc);
+    al((void**)&widx_d, sizeof(int) * nw);
+    cufftHandle plan = 0;
+    int plan_batch = 0;
+    const bool transform = !c->welford && n > 1;
+    if (status == SGB_OK && cudaMemcpyAsync(widx_d, widx, sizeof(int) * nw, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        status = SGB_ERR_CUDA; what = "copy energy indices";
+    }
+    for (int q0 = 0; q0 < nq && status == SGB_OK; q0 += qc) {
+        const int m = std::min(qc, nq - q0);
+        if (transform && plan_batch != m * B) {
+            if (plan) cufftDestroy(plan);
+            plan = 0;
+            int n1[1] = {n};
+            if (cufftPlanMany(&plan, 1, n1, nullptr, 1, n, nullptr, 1, n, CUFFT_Z2Z, m * B) != CUFFT_SUCCESS) {
+                status = SGB_ERR_CUDA; what = "cufftPlanMany (intensities) failed"; break;
+            }
+            cufftSetStream(plan, st);
+            plan_batch = m * B;
+        }
+        if (cudaMemcpyAsync(qidx_d, qidx + q0, sizeof(int) * m, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(pref_d, pref + (size_t)2 * c->npos * q0, 16 * (size_t)c->npos * m, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            (qcart && cudaMemcpyAsync(qcart_d, qcart + 3 * (size_t)q0, 24 * (size_t)m, cudaMemcpyHostToDevice, st) != cudaSuccess)) {
+            status = SGB_ERR_CUDA; what = "copy wave vectors"; break;
+        }
+        const double scale = c->welford ? 1.0 : 1.0 / (double)c->nsamples;
+        if (corr_launch_gather_q(c->P, ld, qidx_d, m, B, n, scale, tmp, st)) { status = SGB_ERR_CUDA; what = "gather launch"; break; }
+        if (transform) {
+            if (cufftExecZ2Z(plan, (cufftDoubleComplex*)tmp, (cufftDoubleComplex*)tmp, CUFFT_INVERSE) != CUFFT_SUCCESS ||
+                corr_launch_window(tmp, m * B, n, c->g, st) ||
+                cufftExecZ2Z(plan, (cufftDoubleComplex*)tmp, (cufftDoubleComplex*)tmp, CUFFT_FORWARD) != CUFFT_SUCCESS) {
+                status = SGB_ERR_CUDA; what = "read-out transform failed"; break;
+            }
+        }
+        if (corr_launch_intensity(tmp, c->ncorr, c->npos, n, pref_d, qcart ? qcart_d : nullptr, widx_d, nw, combiner, m,
+                                  out_d, st)) {
+            status = SGB_ERR_CUDA; what = "intensity launch"; break;
+        }
+        (*c->launches) += transform ? 3 : 2;
+        if (cudaMemcpyAsync(out + per_out * nw * (size_t)q0, out_d, sizeof(double) * per_out * nw * m, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            status = SGB_ERR_CUDA; what = "copy intensities"; break;
+        }
+    }
+    cudaStreamSynchronize(st);
+    if (plan) cufftDestroy(plan);
+    void* bufs[] = {tmp, pref_d, qcart_d, out_d, qidx_d, widx_d};
+    for (void* p : bufs) if (p) cudaFree(p);
+    if (status != SGB_OK) return cfail(c, status, std::string("intensities: ") + what);
+    return SGB_OK;
+}
+
 int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src) {
     if (!dst || !src) return fail(nullptr, SGB_ERR_ARG, "null handle");
     if (dst->plen != src->plen || dst->nomega != src->nomega || dst->ncorr != src->ncorr)

@@ -196,6 +196,76 @@ __global__ void k_merge_welford(double2* __restrict__ d1, double* __restrict__ M
     }
 }
 
+// Columns of the accumulator belonging to the wave vectors qidx[0..nq): the B = ncorr*npos^2
+// columns of wave vector q are [q*B, (q+1)*B). tmp[k*B + b][ω] = scale * P[ω][qidx[k]*B + b].
+__global__ void k_gather_qcols(const double2* __restrict__ P, size_t ld, const int* __restrict__ qidx, int nq, int B,
+                               int n, double scale, double2* __restrict__ tmp) {
+    const size_t total = (size_t)nq * B * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int w = (int)(e % n);
+        const size_t col = e / n;
+        const int k = (int)(col / B), b = (int)(col % B);
+        double2 v = P[(size_t)w * ld + (size_t)qidx[k] * B + b];
+        v.x *= scale; v.y *= scale;
+        tmp[e] = v;
+    }
+}
+
+// Phase averaging and the S(q,ω) combiner (DataRetrieval.jl:147-171, PhaseAveraging.jl):
+// elems[c] = Σ_{i,j} p_i conj(p_j) data[c,i,j,q,ω] with p_i = ff_i(|q|) exp(-2πi q·r_i);
+// combiner 0 = trace of the 3x3 correlation matrix, 1 = its component perpendicular to q
+// (ssf_trace / ssf_perp, MeasureSpec.jl:115-224, corr_pairs (3,3),(2,3),(1,3),(2,2),(1,2),(1,1)),
+// 2 = the ncorr raw elements. One CTA per wave vector, threads over the requested ω.
+__global__ void k_intensity(const double2* __restrict__ tmp, int ncorr, int npos, int n, const double2* __restrict__ pref,
+                            const double* __restrict__ qcart, const int* __restrict__ widx, int nw, int combiner,
+                            double* __restrict__ out) {
+    const int k = blockIdx.x;
+    const int B = ncorr * npos * npos;
+    const double2* col0 = tmp + (size_t)k * B * n;
+    const double2* p = pref + (size_t)k * npos;
+    for (int t = threadIdx.x; t < nw; t += blockDim.x) {
+        const int w = widx[t];
+        double er[8], ei[8];
+        for (int c = 0; c < ncorr && c < 8; c++) { er[c] = 0; ei[c] = 0; }
+        for (int j = 0; j < npos; j++) {
+            const double2 pj = p[j];
+            for (int i = 0; i < npos; i++) {
+                const double2 pi = p[i];
+                // f = p_i conj(p_j)
+                const double fr = pi.x * pj.x + pi.y * pj.y, fi = pi.y * pj.x - pi.x * pj.y;
+                for (int c = 0; c < ncorr && c < 8; c++) {
+                    const double2 d = col0[(size_t)(c + ncorr * (i + npos * j)) * n + w];
+                    er[c] += fr * d.x - fi * d.y;
+                    ei[c] += fr * d.y + fi * d.x;
+                }
+            }
+        }
+        if (combiner == 2) {
+            for (int c = 0; c < ncorr; c++) {
+                out[(((size_t)k * nw + t) * ncorr + c) * 2] = er[c];
+                out[(((size_t)k * nw + t) * ncorr + c) * 2 + 1] = ei[c];
+            }
+            continue;
+        }
+        // real 3x3 matrix from (3,3),(2,3),(1,3),(2,2),(1,2),(1,1): m11 = e5, m12 = e4, m13 = e2,
+        // m22 = e3, m23 = e1, m33 = e0 (real parts; the matrix is Hermitian)
+        const double tr = er[5] + er[3] + er[0];
+        double v = tr;
+        if (combiner == 1) {
+            const double qx = qcart[3 * k], qy = qcart[3 * k + 1], qz = qcart[3 * k + 2];
+            const double q2 = qx * qx + qy * qy + qz * qz;
+            if (q2 == 0.0) {
+                v = (2.0 / 3.0) * tr;
+            } else {
+                const double qmq = qx * qx * er[5] + qy * qy * er[3] + qz * qz * er[0] + 2 * qx * qy * er[4] +
+                                   2 * qx * qz * er[2] + 2 * qy * qz * er[1];
+                v = tr - qmq / q2;
+            }
+        }
+        out[(size_t)k * nw + t] = v;
+    }
+}
+
 int grid_for(size_t n) {
     size_t g = (n + 255) / 256;
     if (g > 65535) g = 65535;
@@ -204,6 +274,21 @@ int grid_for(size_t n) {
 }
 
 }  // namespace
+
+int corr_launch_gather_q(const double* P, size_t ld, const int* qidx, int nq, int B, int n, double scale, double* tmp,
+                         cudaStream_t st) {
+    k_gather_qcols<<<grid_for((size_t)nq * B * n), 256, 0, st>>>(reinterpret_cast<const double2*>(P), ld, qidx, nq, B, n,
+                                                                  scale, reinterpret_cast<double2*>(tmp));
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+int corr_launch_intensity(const double* tmp, int ncorr, int npos, int n, const double* pref, const double* qcart,
+                          const int* widx, int nw, int combiner, int nq, double* out, cudaStream_t st) {
+    if (ncorr > 8) return SGB_ERR_ARG;
+    k_intensity<<<nq, 128, 0, st>>>(reinterpret_cast<const double2*>(tmp), ncorr, npos, n,
+                                     reinterpret_cast<const double2*>(pref), qcart, widx, nw, combiner, out);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
 
 template <class R>
 int corr_launch_product(const R* A, const int* pairs, int ncorr, int nobs, int npos, int ncell, int n, size_t col0,

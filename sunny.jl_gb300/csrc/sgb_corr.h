@@ -19,3 +19,8 @@ int corr_launch_welford(const double* tmp, int ncol, int n, size_t col0, size_t 
                         cudaStream_t st);
 int corr_launch_merge_welford(double* d1, double* M1, const double* d2, const double* M2, double n, double m, size_t len,
                               cudaStream_t st);
+// intensities: gather the columns of a list of wave vectors; phase averaging + combiner
+int corr_launch_gather_q(const double* P, size_t ld, const int* qidx, int nq, int B, int n, double scale, double* tmp,
+                         cudaStream_t st);
+int corr_launch_intensity(const double* tmp, int ncorr, int npos, int n, const double* pref, const double* qcart,
+                          const int* widx, int nw, int combiner, int nq, double* out, cudaStream_t st);

@@ -253,3 +253,62 @@ def test_batched_predictor_reaches_the_same_fixed_point(gpu, sg):
     assert rel(scb.data, scs.data) < 1e-9
     scb.close()
     b.close()
+
+
+def test_intensities_parity(gpu, sg, orc):
+    # intensities(sc, qpts; energies, kT) (DataRetrieval.jl:77-171) against the oracle's
+    # restatement on its own data: on-grid, off-grid (rounded), negative and zero q,
+    # nonnegative / all / listed energies, with and without the classical-to-quantum factor
+    sys_ = diamond_reference_model(sg)
+    kw = dict(energies=np.linspace(0.0, 5.5, 10), dt=0.12)
+    sc = sg.SampledCorrelations(sys_, measure=sg.ssf_perp(sys_), **kw)
+    o, oc = oracle_corr(orc, sys_, sc)
+    S = sys_.dipoles_flat()
+    sg.add_sample(sc, sys_)
+    oc.add_sample(S, None)
+    cr = sys_.crystal
+    pos = np.array([cr._pos[a] for a in range(sys_.natoms)])
+    qs = np.array([[0.0, 0.0, 0.0], [-0.2, 0.4, -0.1], [0.5, 1 / 3, 0.25], [1.26, -0.74, 0.49], [-0.5, 0.0, 0.75]])
+    comb = sc.measure.combiner
+    for energies, kT in (("available", None), ("available_with_negative", 0.4), ([-1.0, 0.0, 0.61, 2.0], None)):
+        res = sg.intensities(sc, qs, energies=energies, kT=kT)
+        ws, widx = sg.correlations._energy_indices(sc, energies)
+        ref = orc.intensities(oc.data, cr.recipvecs, pos, sys_.dims, qs, widx, comb, sc.n_all_omega, sc.dw, kT, ws)
+        assert res.data.shape == ref.shape
+        assert np.max(np.abs(res.data - ref)) < 1e-9 * np.max(np.abs(ref))
+    # the reference golden vector's q = 0 column: the cosine window's spectrum of the
+    # conserved total moment, I(0, Δω) = I(0, 0) / 2 and ~0 above (test_correlation_sampling.jl:167)
+    col = sg.intensities(sc, qs[:1], energies="available", kT=None).data[:, 0]
+    assert col[1] == pytest.approx(0.5 * col[0], rel=1e-10)
+    assert np.max(np.abs(col[2:])) < 1e-10 * col[0]
+    # the device trace combiner and the host path for a custom combiner agree
+    sct = sg.SampledCorrelations(sys_, measure=sg.ssf_trace(sys_), **kw)
+    scc = sg.SampledCorrelations(sys_, measure=sg.ssf_custom(lambda q, m: np.trace(m.real), sys_), **kw)
+    for x in (sct, scc):
+        sys_.set_state_flat(dipoles=S)
+        sg.add_sample(x, sys_)
+    a = sg.intensities(sct, qs, energies="available").data
+    b = sg.intensities(scc, qs, energies="available").data
+    assert np.max(np.abs(a - b)) < 1e-12 * np.max(np.abs(a))
+    st = sg.intensities_static(sct, qs)
+    assert np.allclose(st.data, sg.intensities(sct, qs, energies="available_with_negative").data.sum(axis=0) * sct.dw,
+                       rtol=1e-12)
+
+
+def test_intensities_with_errors_mode_equal_deferred(gpu, sg):
+    # the Welford accumulator holds the transformed mean: same intensities as the deferred sum
+    sys_ = diamond_reference_model(sg)
+    kw = dict(measure=sg.ssf_perp(sys_), energies=np.linspace(0.0, 5.5, 10), dt=0.12)
+    a = sg.SampledCorrelations(sys_, **kw)
+    b = sg.SampledCorrelations(sys_, calculate_errors=True, **kw)
+    rng = np.random.default_rng(5)
+    for _ in range(2):
+        S = rng.standard_normal((sys_.nsites, 3))
+        S = 1.5 * S / np.linalg.norm(S, axis=1)[:, None]
+        for x in (a, b):
+            sys_.set_state_flat(dipoles=S)
+            sg.add_sample(x, sys_)
+    qs = np.array([[0.0, 0.0, 0.0], [0.5, 1 / 3, 0.25], [-0.5, 0.0, 0.75]])
+    ia = sg.intensities(a, qs, energies="available_with_negative", kT=0.3).data
+    ib = sg.intensities(b, qs, energies="available_with_negative", kT=0.3).data
+    assert np.max(np.abs(ia - ib)) < 1e-10 * np.max(np.abs(ia))
