@@ -326,6 +326,40 @@ def run_adjoint(sg, device, L_=24, nw=64, checkpoint=64):
             "ms_forward_only": 1000 * t_fwd, "dtype": "f64"}
 
 
+def run_c3_sqw(sg, device, precision, nsamples):
+    """S(q,w) samples/s of the SU(3) workload: layered triangular 48x48x4 (9,216 sites), spin-1
+    coherent states, anisotropic J1, J2, J3, Jc, -2.2 Sz^2; Langevin at kT=0.3 (damping 0.1),
+    then SampledCorrelations with nw=150 up to 7.5 meV (dt 0.025 -> measurement period 17,
+    2,533 midpoint steps per sample), ssf_perp."""
+    import ctypes as C
+    lib = sg.load_library()
+    cr = sg.triangular_crystal(a=4.05, c=6.75)
+    s = sg.System(cr, [(1, sg.Moment(s=1, g=2))], "SUN", dims=(48, 48, 4), seed=1, precision=precision, device=device)
+    J1 = np.array([[-0.24, 0, 0], [0, -0.24, 0.1], [0, 0.1, -0.24]])
+    s.set_exchange(J1, sg.Bond(1, 1, [1, 0, 0]))
+    s.set_exchange(0.05, sg.Bond(1, 1, [1, 2, 0]))
+    s.set_exchange(0.32, sg.Bond(1, 1, [2, 0, 0]))
+    s.set_exchange(-0.05, sg.Bond(1, 1, [0, 0, 1]))
+    s.set_onsite_coupling(lambda Sx, Sy, Sz: -2.2 * Sz @ Sz, 1)
+    s.randomize_spins()
+    sg.step(s, sg.Langevin(0.025, damping=0.1, kT=0.3), nsteps=1000)
+    sc = sg.SampledCorrelations(s, measure=sg.ssf_perp(s), energies=np.linspace(0, 7.5, 150), dt=0.025,
+                                tol=1e-6 if precision == "fp32" else 1e-12)
+    sg.add_sample(sc, s)                                   # warm-up (plans)
+    lib.sgb_synchronize(s.handle)
+    lib.sgb_event_record(s.handle, 0)
+    for _ in range(nsamples):
+        sg.add_sample(sc, s)
+    lib.sgb_event_record(s.handle, 1)
+    ms = C.c_float()
+    lib.sgb_event_elapsed(s.handle, 0, 1, C.byref(ms))
+    out = {"samples_per_s": nsamples / (ms.value / 1000.0), "ms_per_sample": ms.value / nsamples,
+           "steps_per_sample": sc.measperiod * (sc.n_all_omega // 2), "nsites": s.nsites}
+    sc.close()
+    s.close()
+    return out
+
+
 # ---- CPU restatement (oracle) timing ----------------------------------------------------------
 
 def _cpu_sample_worker(args):
@@ -473,6 +507,9 @@ def main():
             extra[kind] = {"fp32": a, "fp64": bb, "speedup": a["site_steps_per_s"] / bb["site_steps_per_s"]}
         pt = run_tempering(sg, local)
         extra["adjoint"] = run_adjoint(sg, local)
+        c3 = {"fp32": run_c3_sqw(sg, local, "fp32", 2), "fp64": run_c3_sqw(sg, local, "fp64", 1)}
+        c3["speedup"] = c3["fp32"]["samples_per_s"] / c3["fp64"]["samples_per_s"]
+        extra["c3_sqw"] = c3
     barrier()
     ms = maxall(rb["ms"])
     value = world * args.steps * rb["nrep"] / (ms / 1000.0)
@@ -527,6 +564,7 @@ def main():
             "langevin_site_steps": {"simple_cubic_16^3_dipole": extra.get("sc"), "triangular_48x48x4_SU3": extra.get("tri"),
                                     "tempering_256_replicas": pt},
             "adjoint_c5": extra.get("adjoint"),
+            "sqw_su3_triangular_48x48x4": extra.get("c3_sqw"),
             "roofline": roof,
             "gpu_launches": rb["launches"],
             "clocks": rb["clocks"],
