@@ -128,6 +128,14 @@ int sgb_energy_grad(sgb_system* sys, double* grad);
  * call on a device resolves the array's address; make it before any stream capture. */
 int sgb_energy_grad_static(sgb_system* sys, double* grad);
 
+/* First fixed-point iterate of each dipole-mode midpoint step within one sgb_midpoint /
+ * sgb_corr_add_sample call (no counterpart in the reference, which starts from S' = S,
+ * Integrators.jl:389): order 0 does the same; order k in 1..4 starts from the degree-k
+ * extrapolation of the last states and accepts a step from its second iteration on (same
+ * convergence test, fewer iterations; used when a thread holds 1 or 2 sites). Default 4
+ * for FP32 dipole systems, 0 otherwise; SU(N) mode always starts from Z' = Z. */
+int sgb_set_midpoint_predictor(sgb_system* sys, int32_t order);
+
 /* energy(sys) (Interactions.jl:401-432) in FP64, and the magnetisation sum(sys.dipoles)
  * (ParallelTempering.jl:31). Either output may be NULL. */
 int sgb_energy(sgb_system* sys, double* energy, double* magnetization3);

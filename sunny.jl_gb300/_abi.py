@@ -62,6 +62,7 @@ SIGNATURES = {
     "sgb_set_bonds": (C.c_int, [_P, C.POINTER(BondC), _I32]),
     "sgb_set_state": (C.c_int, [_P, _D, _D]),
     "sgb_get_state": (C.c_int, [_P, _D, _D]),
+    "sgb_set_midpoint_predictor": (C.c_int, [_P, _I32]),
     "sgb_energy_grad": (C.c_int, [_P, _D]),
     "sgb_energy_grad_static": (C.c_int, [_P, _D]),
     "sgb_energy": (C.c_int, [_P, _D, _D]),

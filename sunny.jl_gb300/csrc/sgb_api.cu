@@ -227,7 +227,7 @@ int run_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t s
 
 template <class R>
 int run_midpoint(sgb_system* s, double dt, double damping, double tol, int max_iters, int nsteps, int64_t* iters,
-                 const SnapArgs<R>& snap, bool sync_status = true) {
+                 const SnapArgs<R>& snap, bool sync_status = true, int order = 0) {
     LaunchInfo li;
     int rc = plan_launch<R>(s, li);
     if (rc) return rc;
@@ -236,7 +236,8 @@ int run_midpoint(sgb_system* s, double dt, double damping, double tol, int max_i
     Model<R>& M = model<R>(s);
     if ((rc = reset_ctrl(s))) return rc;
     if (!s->sun)
-        rc = dip_launch_midpoint<R>(M, (R*)s->S, (R*)s->H, s->ctrl, nsteps, dt, damping, atol2, max_iters, snap, li, s->stream);
+        rc = dip_launch_midpoint<R>(M, (R*)s->S, (R*)s->H, s->ctrl, nsteps, dt, damping, atol2, max_iters, snap, li, s->stream,
+                                    order);
     else
         rc = sun_launch_midpoint<R>(M, (R*)s->Z, (R*)s->S, (R*)s->Q, (R*)s->H, (R*)s->QH, s->ctrl, nsteps, dt, damping, atol2,
                                     max_iters, snap, li, s->stream);
@@ -298,6 +299,7 @@ int sgb_create(const sgb_desc* d, sgb_system** out) {
     s->sun = d->mode == SGB_MODE_SUN;
     s->N = s->sun ? d->N : 0;
     s->fp32 = d->precision == SGB_FP32;
+    s->mid_order = (s->fp32 && d->mode != SGB_MODE_SUN) ? 4 : 0;
     auto bad = [&](int code) { sgb_destroy(s); return code; };
     cudaError_t e = cudaSetDevice(d->device);
     if (e != cudaSuccess) { fail(nullptr, SGB_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e)); return bad(SGB_ERR_CUDA); }
@@ -491,6 +493,13 @@ int sgb_get_state(sgb_system* s, double* dipoles, double* coherents) {
     return SGB_OK;
 }
 
+int sgb_set_midpoint_predictor(sgb_system* s, int32_t order) {
+    if (!s) return fail(nullptr, SGB_ERR_ARG, "null handle");
+    if (order < 0 || order > 4) return fail(s, SGB_ERR_ARG, "predictor order must be in 0..4");
+    s->mid_order = order;
+    return SGB_OK;
+}
+
 int sgb_energy_grad(sgb_system* s, double* grad) {
     if (!s || !grad) return fail(s, SGB_ERR_ARG, "null argument");
     int rc = ensure_tables(s);
@@ -579,10 +588,10 @@ int sgb_midpoint(sgb_system* s, double dt, double damping, double tol, int32_t m
     if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called before stepping");
     if (s->fp32) {
         SnapArgs<float> sn{};
-        return run_midpoint<float>(s, dt, damping, tol, max_iters, nsteps, iters_out, sn);
+        return run_midpoint<float>(s, dt, damping, tol, max_iters, nsteps, iters_out, sn, true, s->mid_order);
     }
     SnapArgs<double> sn{};
-    return run_midpoint<double>(s, dt, damping, tol, max_iters, nsteps, iters_out, sn);
+    return run_midpoint<double>(s, dt, damping, tol, max_iters, nsteps, iters_out, sn, true, s->mid_order);
 }
 
 int sgb_event_record(sgb_system* s, int32_t slot) {
@@ -865,11 +874,11 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
         if (rc) return cfail(c, rc, batch_error(b));
     } else if (fp32) {
         SnapArgs<float> sn{1, c->nobs, c->measperiod, 0, (const float*)c->ops, (float*)c->A, (float)scale};
-        if (nsteps > 0) rc = run_midpoint<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true);
+        if (nsteps > 0) rc = run_midpoint<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true, s->mid_order);
         else rc = run_midpoint<float>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
     } else {
         SnapArgs<double> sn{1, c->nobs, c->measperiod, 0, (const double*)c->ops, (double*)c->A, scale};
-        if (nsteps > 0) rc = run_midpoint<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true);
+        if (nsteps > 0) rc = run_midpoint<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true, s->mid_order);
         else rc = run_midpoint<double>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
     }
     if (rc) return rc;

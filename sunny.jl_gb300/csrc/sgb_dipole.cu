@@ -97,12 +97,27 @@ __device__ __forceinline__ void write_snapshot_dip(const Model<R>& M, const Snap
     }
 }
 
+// Degree-k polynomial extrapolation of the next state from c = S_{n+1}, s = S_n and the
+// history h1 = S_{n-1}, h2 = S_{n-2}, h3 = S_{n-3} (Newton backward differences).
+template <class R>
+__device__ __forceinline__ R extrap(int k, R c, R s, R h1, R h2, R h3) {
+    switch (k) {
+        case 1: return 2 * c - s;
+        case 2: return 3 * (c - s) + h1;
+        case 3: return 4 * (c + h1) - 6 * s - h2;
+        case 4: return 5 * (c - h2) + 10 * (h1 - s) + h3;
+    }
+    return c;
+}
+
 // Spherical midpoint, Integrators.jl:379-413. H holds 3 rotating SoA buffers of
-// midpoint spins S-hat (3*3*ns reals).
-template <class R, int SPT>
+// midpoint spins S-hat (3*3*ns reals). With PRED, each step after the first starts its
+// fixed-point iteration from the degree-`ord` extrapolation of the last states (kept in
+// registers) instead of S' = S, and a step is accepted from its second iteration on.
+template <class R, int SPT, bool PRED>
 __global__ void __launch_bounds__(sgb_maxblock(sizeof(R) == 8, false, SPT))
 k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, double atol2,
-               int max_iters, SnapArgs<R> snap) {
+               int max_iters, SnapArgs<R> snap, int ord) {
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(M, smem);
     const int ns = M.ns;
@@ -110,6 +125,8 @@ k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, doub
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const bool leader = (blockIdx.x == 0 && threadIdx.x == 0);
     R s[SPT][3], sp[SPT][3], sc[SPT][3];
+    constexpr int PH = PRED ? SPT : 1;
+    R h1[PH][3], h2[PH][3], h3[PH][3], pn[PH][3];   // history and next first iterate (PRED)
     int cur = 0;
 #pragma unroll
     for (int k = 0; k < SPT; k++) {
@@ -127,8 +144,12 @@ k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, doub
     long long itg = 0;
     int done = 0;
     for (int step = 0; step < nsteps; ++step) {
+        const int oe = PRED ? min(ord, step + 1) : 0;   // extrapolation order for the next step
 #pragma unroll
-        for (int k = 0; k < SPT; k++) { sp[k][0] = s[k][0]; sp[k][1] = s[k][1]; sp[k][2] = s[k][2]; }
+        for (int k = 0; k < SPT; k++) {
+            if (PRED && step > 0) { sp[k][0] = pn[k % PH][0]; sp[k][1] = pn[k % PH][1]; sp[k][2] = pn[k % PH][2]; }
+            else { sp[k][0] = s[k][0]; sp[k][1] = s[k][1]; sp[k][2] = s[k][2]; }
+        }
         bool conv = false;
         for (int it = 0; it < max_iters; ++it) {
             const int nxt = (cur + 1) % 3, nst = (cur + 2) % 3;
@@ -155,12 +176,22 @@ k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, doub
                 normalize_dip<R>(nx, ny, nz, kap);
                 Hn[site] = nx; Hn[ns + site] = ny; Hn[2 * ns + site] = nz;
                 // candidate new state and the next step's first midpoint
-                R cx = qx, cy = qy, cz = qz;
-                normalize_dip<R>(cx, cy, cz, kap);
-                sc[k][0] = cx; sc[k][1] = cy; sc[k][2] = cz;
-                R mx = (cx + cx) / 2, my = (cy + cy) / 2, mz = (cz + cz) / 2;
-                normalize_dip<R>(mx, my, mz, kap);
-                Hs[site] = mx; Hs[ns + site] = my; Hs[2 * ns + site] = mz;
+                if (!PRED || it > 0) {
+                    R cx = qx, cy = qy, cz = qz;
+                    normalize_dip<R>(cx, cy, cz, kap);
+                    sc[k][0] = cx; sc[k][1] = cy; sc[k][2] = cz;
+                    R px = cx, py = cy, pz = cz;
+                    if (PRED) {
+                        const int j = k % PH;
+                        px = extrap<R>(oe, cx, s[k][0], h1[j][0], h2[j][0], h3[j][0]);
+                        py = extrap<R>(oe, cy, s[k][1], h1[j][1], h2[j][1], h3[j][1]);
+                        pz = extrap<R>(oe, cz, s[k][2], h1[j][2], h2[j][2], h3[j][2]);
+                        pn[j][0] = px; pn[j][1] = py; pn[j][2] = pz;
+                    }
+                    R mx = (cx + px) / 2, my = (cy + py) / 2, mz = (cz + pz) / 2;
+                    normalize_dip<R>(mx, my, mz, kap);
+                    Hs[site] = mx; Hs[ns + site] = my; Hs[2 * ns + site] = mz;
+                }
             }
             double bsum = sgb_block_sum_r<R>(acc);
             const int slot = (int)(itg % 3);
@@ -169,10 +200,16 @@ k_dip_midpoint(Model<R> M, R* S, R* H, Ctrl* ctrl, int nsteps, R dt, R lam, doub
             if (!sgb_grid_barrier(ctrl, gridDim.x)) return;
             double tot = __ldcg(&ctrl->acc[slot]);
             itg++;
-            if (tot <= atol2) {  // false for NaN, as fast_isapprox
+            if (tot <= atol2 && (!PRED || it > 0)) {  // false for NaN, as fast_isapprox
                 conv = true;
 #pragma unroll
-                for (int k = 0; k < SPT; k++) { s[k][0] = sc[k][0]; s[k][1] = sc[k][1]; s[k][2] = sc[k][2]; }
+                for (int k = 0; k < SPT; k++) {
+                    if (PRED) {
+                        const int j = k % PH;
+                        for (int q = 0; q < 3; q++) { h3[j][q] = h2[j][q]; h2[j][q] = h1[j][q]; h1[j][q] = s[k][q]; }
+                    }
+                    s[k][0] = sc[k][0]; s[k][1] = sc[k][1]; s[k][2] = sc[k][2];
+                }
                 cur = nst;
                 break;
             }
@@ -363,16 +400,21 @@ int dip_launch_heun(const Model<R>& M, R* S, R* P, Ctrl* ctrl, int nsteps, doubl
 template <class R>
 int dip_launch_midpoint(const Model<R>& M, R* S, R* H, Ctrl* ctrl, int nsteps, double dt, double lam,
                         double atol2, int max_iters, const SnapArgs<R>& snap, const LaunchInfo& li,
-                        cudaStream_t st) {
+                        cudaStream_t st, int order) {
     Model<R> m = M;
     SnapArgs<R> sn = snap;
     R rdt = (R)dt, rlam = (R)lam;
-    void* args[] = {&m, &S, &H, &ctrl, &nsteps, &rdt, &rlam, &atol2, &max_iters, &sn};
+    int ord = order;
+    void* args[] = {&m, &S, &H, &ctrl, &nsteps, &rdt, &rlam, &atol2, &max_iters, &sn, &ord};
+    // extrapolated first iterates keep their history in registers: 1 or 2 sites per thread
+    const bool pred = order > 0 && li.spt <= 2;
     switch (li.spt) {
-        case 1: return coop_launch(k_dip_midpoint<R, 1>, li, args, st);
-        case 2: return coop_launch(k_dip_midpoint<R, 2>, li, args, st);
-        case 4: return coop_launch(k_dip_midpoint<R, 4>, li, args, st);
-        case 8: return coop_launch(k_dip_midpoint<R, 8>, li, args, st);
+        case 1: return pred ? coop_launch(k_dip_midpoint<R, 1, true>, li, args, st)
+                            : coop_launch(k_dip_midpoint<R, 1, false>, li, args, st);
+        case 2: return pred ? coop_launch(k_dip_midpoint<R, 2, true>, li, args, st)
+                            : coop_launch(k_dip_midpoint<R, 2, false>, li, args, st);
+        case 4: return coop_launch(k_dip_midpoint<R, 4, false>, li, args, st);
+        case 8: return coop_launch(k_dip_midpoint<R, 8, false>, li, args, st);
     }
     return SGB_ERR_ARG;
 }
@@ -388,10 +430,12 @@ int dip_max_blocks(int spt, int block, size_t smem, int* bps) {
     };
     int rc = SGB_OK;
     switch (spt) {
-        case 1: rc |= one(k_dip_heun<R, 1, false>); rc |= one(k_dip_heun<R, 1, true>); rc |= one(k_dip_midpoint<R, 1>); break;
-        case 2: rc |= one(k_dip_heun<R, 2, false>); rc |= one(k_dip_heun<R, 2, true>); rc |= one(k_dip_midpoint<R, 2>); break;
-        case 4: rc |= one(k_dip_heun<R, 4, false>); rc |= one(k_dip_heun<R, 4, true>); rc |= one(k_dip_midpoint<R, 4>); break;
-        case 8: rc |= one(k_dip_heun<R, 8, false>); rc |= one(k_dip_heun<R, 8, true>); rc |= one(k_dip_midpoint<R, 8>); break;
+        case 1: rc |= one(k_dip_heun<R, 1, false>); rc |= one(k_dip_heun<R, 1, true>); rc |= one(k_dip_midpoint<R, 1, false>);
+                rc |= one(k_dip_midpoint<R, 1, true>); break;
+        case 2: rc |= one(k_dip_heun<R, 2, false>); rc |= one(k_dip_heun<R, 2, true>); rc |= one(k_dip_midpoint<R, 2, false>);
+                rc |= one(k_dip_midpoint<R, 2, true>); break;
+        case 4: rc |= one(k_dip_heun<R, 4, false>); rc |= one(k_dip_heun<R, 4, true>); rc |= one(k_dip_midpoint<R, 4, false>); break;
+        case 8: rc |= one(k_dip_heun<R, 8, false>); rc |= one(k_dip_heun<R, 8, true>); rc |= one(k_dip_midpoint<R, 8, false>); break;
         default: return SGB_ERR_ARG;
     }
     if (rc != SGB_OK) return SGB_ERR_CUDA;
@@ -439,7 +483,7 @@ int util_launch_fill(double* p, size_t n, double v, cudaStream_t st) {
     template int dip_launch_heun<R>(const Model<R>&, R*, R*, Ctrl*, int, double, double, double, uint64_t, \
                                     uint64_t, const double*, const LaunchInfo&, cudaStream_t);          \
     template int dip_launch_midpoint<R>(const Model<R>&, R*, R*, Ctrl*, int, double, double, double, int,  \
-                                        const SnapArgs<R>&, const LaunchInfo&, cudaStream_t);           \
+                                        const SnapArgs<R>&, const LaunchInfo&, cudaStream_t, int);      \
     template int dip_launch_grad<R>(const Model<R>&, const R*, double*, cudaStream_t);                    \
     template int dip_launch_energy<R>(const Model<R>&, const R*, double*, int, cudaStream_t);             \
     template int dip_max_blocks<R>(int, int, size_t, int*);                                                    \

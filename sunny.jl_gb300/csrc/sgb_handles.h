@@ -12,6 +12,7 @@ struct sgb_system {
     int ns = 0, ncell = 0, N = 0;
     bool fp32 = false;
     bool sun = false;
+    int mid_order = 0;          // first-iterate extrapolation of the dipole midpoint (0: S' = S)
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
     std::string err;

@@ -58,7 +58,7 @@ int dip_launch_heun(const Model<R>& M, R* S, R* P, Ctrl* ctrl, int nsteps, doubl
 template <class R>
 int dip_launch_midpoint(const Model<R>& M, R* S, R* H, Ctrl* ctrl, int nsteps, double dt, double lam,
                         double atol2, int max_iters, const SnapArgs<R>& snap, const LaunchInfo& li,
-                        cudaStream_t st);
+                        cudaStream_t st, int order = 0);
 template <class R>
 int dip_launch_grad(const Model<R>& M, const R* S, double* grad, cudaStream_t st);
 template <class R>

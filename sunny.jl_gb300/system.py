@@ -408,6 +408,12 @@ class System:
             flatd[:] = self._kappa[:, None] * (d / np.linalg.norm(d))[None, :]
         self._host_newer = True
 
+    def set_midpoint_predictor(self, order: int):
+        """First iterate of each dipole midpoint step within one call: 0 S' = S (the
+        reference's choice), k in 1..4 the degree-k extrapolation of the last states.
+        Default 4 for FP32 dipole systems, 0 otherwise."""
+        _abi.check(self._lib.sgb_set_midpoint_predictor(self._h, int(order)), self._lib, self._h)
+
     def randomize_spins(self):
         """randomize_spins!(sys) (System.jl:444-452, 513-517)."""
         self._sync_to_host()

@@ -107,11 +107,13 @@ def test_static_correlations(gpu, sg, orc):
     assert tot.real == pytest.approx(64.0, rel=1e-12)
 
 
-@pytest.mark.parametrize("tol", [1e-7, 1e-6])
-def test_sqw_fp32_per_bin_error(gpu, sg, orc, tol):
-    # 1e-6 is the FP32 midpoint tolerance the benchmark runs with
+@pytest.mark.parametrize("tol,order", [(1e-7, 4), (1e-6, 4), (1e-6, 0)])
+def test_sqw_fp32_per_bin_error(gpu, sg, orc, tol, order):
+    # 1e-6 is the FP32 midpoint tolerance the benchmark runs with; order 4 is the default
+    # extrapolated first iterate, 0 the reference's S' = S
     sys64 = diamond_reference_model(sg, "fp64")
     sys32 = diamond_reference_model(sg, "fp32")
+    sys32.set_midpoint_predictor(order)
     sys32.set_state_flat(dipoles=sys64.dipoles_flat())
     kw = dict(energies=np.linspace(0.0, 5.5, 10), dt=0.12)
     sc = sg.SampledCorrelations(sys32, measure=sg.ssf_perp(sys32), tol=tol, **kw)
