@@ -248,6 +248,47 @@ def merge_correlations(scs):
     return out
 
 
+def merge_host(datas, counts, Ms=None):
+    """merge_correlations' arithmetic on host arrays (SampledCorrelations.jl:128-142): the
+    count-weighted mean of the data and, with Ms, the combined Welford M. Used to merge
+    accumulators read back from several processes (one GPU each)."""
+    d = np.array(datas[0], dtype=complex)
+    n = int(counts[0])
+    M = None if Ms is None else np.array(Ms[0], dtype=float)
+    for k in range(1, len(datas)):
+        m = int(counts[k])
+        if n + m == 0:
+            continue
+        mu = (n / (n + m)) * d + (m / (n + m)) * datas[k]
+        if M is not None:
+            M = (M + n * np.abs(mu - d) ** 2) + (Ms[k] + m * np.abs(mu - datas[k]) ** 2)
+        d, n = mu, n + m
+    return d, n, M
+
+
+def allreduce_correlations(data, count, M=None, group=None):
+    """Merge one accumulator per process (replicas on several GPUs) with torch.distributed:
+    every rank returns the merged (data, count, M), identical to merge_host over the
+    ranks' accumulators. The reductions are two sums over ranks, so any backend works
+    (gloo on CPU, NCCL on GPU tensors)."""
+    import torch
+    import torch.distributed as dist
+    c = torch.tensor([float(count)], dtype=torch.float64)
+    dist.all_reduce(c, group=group)
+    total = c.item()
+    d = np.asarray(data, dtype=complex)
+    w = torch.from_numpy(np.ascontiguousarray(np.stack([d.real, d.imag]) * float(count)))
+    dist.all_reduce(w, group=group)
+    mu = (w[0].numpy() + 1j * w[1].numpy()) / total if total > 0 else np.zeros_like(d)
+    Mt = None
+    if M is not None:
+        # M = Σ_r [M_r + n_r |d_r - μ|²]: the per-rank Welford sums about the common mean
+        part = torch.from_numpy(np.ascontiguousarray(np.asarray(M, dtype=float) + count * np.abs(d - mu) ** 2))
+        dist.all_reduce(part, group=group)
+        Mt = part.numpy()
+    return mu, int(round(total)), Mt
+
+
 def available_energies(sc: SampledCorrelations, negative_energies: bool = False):
     """CorrelationUtils.jl:29-37."""
     if math.isnan(sc.dw):
