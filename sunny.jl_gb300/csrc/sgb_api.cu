@@ -11,6 +11,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -651,6 +652,7 @@ void sgb_corr_destroy(sgb_corr* c) {
     if (c->have_chunk) cufftDestroy(c->plan_chunk);
     p = c->M; dfree(p);
     p = c->ctmp; dfree(p);
+    p = c->err_d; dfree(p);
     for (int i = 0; i < 5; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     delete c;
 }
@@ -693,6 +695,8 @@ static int corr_setup(sgb_corr* c, const sgb_corr_desc* d, bool fp32, bool sun, 
     if ((rc = alloc((void**)&c->P, 16 * c->plen))) return rc;
     cudaMemset(c->P, 0, 16 * c->plen);
     if ((rc = alloc((void**)&c->g, sizeof(double) * c->nomega))) return rc;
+    if ((rc = alloc((void**)&c->err_d, sizeof(int)))) return rc;
+    cudaMemset(c->err_d, 0, sizeof(int));
     if (d->calculate_errors) {
         c->welford = true;
         if ((rc = alloc((void**)&c->M, 8 * c->plen))) return rc;
@@ -912,9 +916,9 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
         if ((rc = welford_samples(c, spec, fp32, rep_stride))) return rc;
     } else {
         rc = fp32 ? corr_launch_accum<float>((const float*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell,
-                                             c->nomega, c->nrep, rep_stride, c->stream)
+                                             c->nomega, c->nrep, rep_stride, c->stream, c->accum_variant, c->err_d)
                   : corr_launch_accum<double>((const double*)spec, c->P, c->pairs, c->ncorr, c->nobs, c->npos, c->ncell,
-                                              c->nomega, c->nrep, rep_stride, c->stream);
+                                              c->nomega, c->nrep, rep_stride, c->stream, c->accum_variant, c->err_d);
         (*c->launches)++;
         if (rc) return cfail(c, SGB_ERR_CUDA, std::string("accumulate launch: ") + cudaGetErrorString(cudaGetLastError()));
     }
@@ -958,6 +962,13 @@ int sgb_corr_data(sgb_corr* c, double* data, double* M, int64_t* nsamples) {
     cudaStream_t stream = c->stream;
     if (nsamples) *nsamples = c->nsamples;
     if (M && !c->welford) return cfail(c, SGB_ERR_ARG, "M is kept only with calculate_errors");
+    {
+        int flag = 0;
+        if (cudaMemcpyAsync(&flag, c->err_d, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess)
+            return cfail(c, SGB_ERR_CUDA, "reading the accumulation status failed");
+        if (flag) return cfail(c, SGB_ERR_TIMEOUT, "a bounded wait of the accumulation kernel gave up; the data are incomplete");
+    }
     if (c->welford) {
         // running mean and M are kept transformed, in Sunny's layout
         cudaError_t e = cudaSuccess;

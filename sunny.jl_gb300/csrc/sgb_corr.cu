@@ -18,8 +18,59 @@
 //                   (identical to Sunny's column-major data[c, i, j, q1, q2, q3, ω])
 #include "sgb_corr.h"
 #include <cufft.h>
+#include <stdint.h>
 
 namespace {
+
+// ---- bulk-copy (TMA) primitives: 1-D cp.async.bulk with mbarrier completion ---------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* m) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(m)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// wait for phase `parity` of m to complete; false after a 2 s limit
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* m, uint32_t parity) {
+    if (mbar_try_wait(m, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    while (!mbar_try_wait(m, parity))
+        if (globaltimer_ns() - t0 > 2000000000ull) return false;
+    return true;
+}
+// global -> shared, completion counted on mbarrier m (bytes: multiple of 16, 16-byte aligned)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* m) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(m))
+                 : "memory");
+}
+// shared -> global, tracked by bulk groups
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 template <class R> struct C2 { R x, y; };
 
@@ -99,6 +150,119 @@ __global__ void __launch_bounds__(256) k_corr_accum(const R* __restrict__ A, dou
             acc[k].y += (double)sim;
             __stcs(row + threadIdx.x + k * blockDim.x, acc[k]);
         }
+    }
+}
+
+// The same accumulation with the accumulator rows moved by bulk copies, warp-specialised.
+// A CTA owns one ω and QT consecutive wave vectors: one contiguous block of QT rows of B
+// complex doubles. Warp NCW (the producer) streams the rows through a ring of NST
+// shared-memory buffers with bulk loads (mbarrier `full`) and writes each finished row
+// back with a bulk store once the NCW compute warps have released it (mbarrier `done`);
+// the compute warps add the replicas' products in shared memory and never wait for a
+// store. Every wait is bounded (2 s): on expiry the CTA records err = 1 and stops.
+template <class R, int QT, int NST>
+__global__ void __launch_bounds__(288) k_corr_accum_bulk(const R* __restrict__ A, double* __restrict__ P,
+                                                       const int* __restrict__ pairs, int ncorr, int nobs, int npos,
+                                                       int ncell, int nomega, int nrep, size_t rep_stride,
+                                                       int* __restrict__ err) {
+    constexpr int NCW = 8;   // compute warps
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int B = ncorr * npos * npos;
+    const uint32_t rowbytes = (uint32_t)B * 16u;
+    double2* rows = reinterpret_cast<double2*>(smem_raw);                       // [NST][B]
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NST * rowbytes);
+    uint64_t* done = full + NST;
+    constexpr int MBYTES = (16 * NST + 15) / 16 * 16;
+    const int nrow = nobs * npos;
+    const int rowpad = nobs * (npos + 1);
+    C2<R>* As = reinterpret_cast<C2<R>*>(smem_raw + (size_t)NST * rowbytes + MBYTES);   // [nrep][QT][rowpad]
+    int* pr = reinterpret_cast<int*>(As + (size_t)nrep * QT * rowpad);
+    __shared__ int bad;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.y;
+    const int q0 = blockIdx.x * QT;
+    const int nq = min(QT, ncell - q0);
+    double2* out = reinterpret_cast<double2*>(P) + ((size_t)w * ncell + q0) * B;
+    if (warp == NCW && lane == 0) {
+        bad = 0;
+        for (int s = 0; s < NST; s++) { mbar_init(&full[s], 1); mbar_init(&done[s], NCW); }
+        mbar_fence_init();
+        for (int s = 0; s < NST && s < nq; s++) {
+            mbar_expect_tx(&full[s], rowbytes);
+            bulk_load(rows + (size_t)s * B, out + (size_t)s * B, rowbytes, &full[s]);
+        }
+    }
+    for (int e = threadIdx.x; e < nrep * nrow * QT; e += blockDim.x) {
+        int r = e / (nrow * QT), rem = e - r * nrow * QT;
+        int row = rem / QT, ql = rem % QT;
+        C2<R> v = {0, 0};
+        if (ql < nq) {
+            size_t idx = (size_t)r * rep_stride + ((size_t)w * nrow + row) * ncell + q0 + ql;
+            v.x = A[2 * idx];
+            v.y = A[2 * idx + 1];
+        }
+        const int o = row / npos, p = row - o * npos;
+        As[((size_t)r * QT + ql) * rowpad + o * (npos + 1) + p] = v;
+    }
+    for (int e = threadIdx.x; e < 2 * ncorr; e += blockDim.x) pr[e] = pairs[e];
+    __syncthreads();
+    if (warp == NCW) {
+        // producer: store finished rows, refill their buffers
+        if (lane == 0) {
+            for (int ql = 0; ql < nq; ql++) {
+                const int s = ql % NST;
+                if (!mbar_wait_bounded(&done[s], (uint32_t)((ql / NST) & 1))) { bad = 1; break; }
+                bulk_store(out + (size_t)ql * B, rows + (size_t)s * B, rowbytes);
+                if (ql + NST < nq) {
+                    bulk_wait_read_all();   // the store has read the buffer
+                    mbar_expect_tx(&full[s], rowbytes);
+                    bulk_load(rows + (size_t)s * B, out + (size_t)(ql + NST) * B, rowbytes, &full[s]);
+                }
+            }
+            bulk_wait_all();
+            if (bad) atomicExch(err, 1);
+        }
+        return;
+    }
+    constexpr int KMAX = 8;
+    int ia[KMAX], ib[KMAX];
+    const int nthr = NCW * 32;
+    const int nk = (B + nthr - 1) / nthr;
+#pragma unroll
+    for (int k = 0; k < KMAX; k++) {
+        int r = threadIdx.x + k * nthr;
+        ia[k] = -1; ib[k] = -1;
+        if (k < nk && r < B) {
+            int c = r % ncorr, t = r / ncorr;
+            int i = t % npos, j = t / npos;
+            ia[k] = pr[2 * c] * (npos + 1) + i;
+            ib[k] = pr[2 * c + 1] * (npos + 1) + j;
+        }
+    }
+    for (int ql = 0; ql < nq; ql++) {
+        const int s = ql % NST;
+        if (!mbar_wait_bounded(&full[s], (uint32_t)((ql / NST) & 1))) { bad = 1; break; }
+        if (bad) break;
+        double2* row = rows + (size_t)s * B;
+#pragma unroll
+        for (int k = 0; k < KMAX; k++) {
+            if (ia[k] < 0) continue;
+            R sre = 0, sim = 0;
+            for (int rr = 0; rr < nrep; rr++) {
+                const C2<R>* Ar = As + ((size_t)rr * QT + ql) * rowpad;
+                C2<R> a = Ar[ia[k]];
+                C2<R> b = Ar[ib[k]];
+                sre += a.x * b.x + a.y * b.y;
+                sim += a.x * b.y - a.y * b.x;
+            }
+            double2 acc = row[threadIdx.x + k * nthr];
+            acc.x += (double)sre;
+            acc.y += (double)sim;
+            row[threadIdx.x + k * nthr] = acc;
+        }
+        fence_proxy_async();   // the generic-proxy writes become visible to the bulk store
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&done[s]);
     }
 }
 
@@ -314,6 +478,20 @@ int corr_launch_merge_welford(double* d1, double* M1, const double* d2, const do
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
+template <class R, int QT, int NST>
+static int accum_bulk(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
+                      int nrep, size_t rep_stride, int* err, cudaStream_t st) {
+    const size_t B = (size_t)ncorr * npos * npos;
+    const size_t smem = (size_t)NST * B * 16 + (16 * NST + 15) / 16 * 16 +
+                        (size_t)nrep * nobs * (npos + 1) * QT * sizeof(C2<R>) + 2 * ncorr * sizeof(int) + 16;
+    if (smem > 220 * 1024) return SGB_ERR_ARG;
+    if (cudaFuncSetAttribute(k_corr_accum_bulk<R, QT, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return SGB_ERR_CUDA;
+    dim3 grid((ncell + QT - 1) / QT, nomega);
+    k_corr_accum_bulk<R, QT, NST><<<grid, 288, smem, st>>>(A, P, pairs, ncorr, nobs, npos, ncell, nomega, nrep, rep_stride, err);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
 template <class R, int QT>
 static int accum_qt(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
                     int nrep, size_t rep_stride, size_t smem, cudaStream_t st) {
@@ -330,8 +508,14 @@ static int accum_qt(const R* A, double* P, const int* pairs, int ncorr, int nobs
 // would not fit in shared memory.
 template <class R>
 int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
-                      int nrep, size_t rep_stride, cudaStream_t st) {
+                      int nrep, size_t rep_stride, cudaStream_t st, int variant, int* err) {
     if (ncorr * npos * npos > 8 * 256) return SGB_ERR_ARG;   // at most 8 accumulator entries per thread and row
+    if (variant > 0 && err) {
+        // 8 wave vectors per CTA and a 2-row ring: 2-3 CTAs per SM (measured fastest of
+        // tiles 4/8/16 x rings 2/3/4 on the 16^3 x 16 pyrochlore with 8 replicas)
+        const int rc = accum_bulk<R, 8, 2>(A, P, pairs, ncorr, nobs, npos, ncell, nomega, nrep, rep_stride, err, st);
+        if (rc != SGB_ERR_ARG) return rc;
+    }
     auto bytes = [&](int qt) { return (size_t)nrep * nobs * (npos + 1) * qt * sizeof(C2<R>) + 2 * ncorr * sizeof(int) + 16; };
     const size_t lim = 200 * 1024;
     if (bytes(32) <= lim) return accum_qt<R, 32>(A, P, pairs, ncorr, nobs, npos, ncell, nomega, nrep, rep_stride, bytes(32), st);
@@ -362,5 +546,7 @@ int corr_launch_add(double* dst, const double* src, size_t n, cudaStream_t st) {
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
-template int corr_launch_accum<float>(const float*, double*, const int*, int, int, int, int, int, int, size_t, cudaStream_t);
-template int corr_launch_accum<double>(const double*, double*, const int*, int, int, int, int, int, int, size_t, cudaStream_t);
+template int corr_launch_accum<float>(const float*, double*, const int*, int, int, int, int, int, int, size_t, cudaStream_t,
+                                      int, int*);
+template int corr_launch_accum<double>(const double*, double*, const int*, int, int, int, int, int, int, size_t,
+                                       cudaStream_t, int, int*);

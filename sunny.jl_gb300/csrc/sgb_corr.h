@@ -4,9 +4,12 @@
 #include <stddef.h>
 #include "../../include/sunny_gb300.h"
 
+// variant 0: loads/stores through registers; 1: rows moved by warp-specialised bulk
+// copies (falls back to 0 when the staging does not fit); err (device int, needed for
+// variant 1) is set to 1 if a bounded wait of the bulk variant gave up.
 template <class R>
 int corr_launch_accum(const R* A, double* P, const int* pairs, int ncorr, int nobs, int npos, int ncell, int nomega,
-                      int nrep, size_t rep_stride, cudaStream_t st);
+                      int nrep, size_t rep_stride, cudaStream_t st, int variant = 0, int* err = nullptr);
 int corr_launch_gather(const double* P, size_t ld, size_t col0, int ncol, int n, double scale, double* tmp, cudaStream_t st);
 int corr_launch_window(double* tmp, int ncol, int n, const double* g, cudaStream_t st);
 int corr_launch_scatter(const double* tmp, int ncol, int n, double* out, cudaStream_t st);

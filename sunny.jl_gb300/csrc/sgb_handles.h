@@ -81,6 +81,8 @@ struct sgb_corr {
     long long own_launches = 0;
     // calculate_errors: P holds the running mean of the transformed samples (not their
     // sum) and M the Welford sums of squared deviations, both in Sunny's layout
+    int* err_d = nullptr;           // device flag: a bounded wait of the accumulation gave up
+    int accum_variant = 1;          // 0 register streaming, 1 bulk-copy rows
     bool welford = false;
     double* M = nullptr;
     double* ctmp = nullptr;         // [chunk][n] complex work buffer of the per-sample transform
