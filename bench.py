@@ -531,7 +531,7 @@ def main():
          "alg_bytes": bytes_traj, "achieved_gbs": bytes_traj / (ph[0] * 1e6) if ph[0] else None},
         {"kernel": f"cuFFT space (3-D, {R} x 200 x 48 transforms)", "ms_per_launch": ph[1]},
         {"kernel": f"cuFFT time (1-D n=398, {R} x 196,608 transforms)", "ms_per_launch": ph[2]},
-        {"kernel": f"k_corr_accum (rank-{R} FP64 accumulator stream)", "ms_per_launch": ph[3], "alg_bytes": bytes_accum,
+        {"kernel": f"k_corr_accum_bulk (rank-{R} FP64 accumulator stream, bulk-copy rows)", "ms_per_launch": ph[3], "alg_bytes": bytes_accum,
          "achieved_gbs": bytes_accum / (ph[3] * 1e6) if ph[3] else None},
     ]
     dom = max((k for k in kernels if "alg_bytes" in k), key=lambda k: k["ms_per_launch"])
