@@ -160,6 +160,13 @@ __global__ void __launch_bounds__(256) k_corr_accum(const R* __restrict__ A, dou
 // back with a bulk store once the NCW compute warps have released it (mbarrier `done`);
 // the compute warps add the replicas' products in shared memory and never wait for a
 // store. Every wait is bounded (2 s): on expiry the CTA records err = 1 and stops.
+// conj(a) b added to (re, im)
+template <class R>
+__device__ __forceinline__ void cmul_conj_acc(const C2<R>& a, const C2<R>& b, R& re, R& im) {
+    re += a.x * b.x + a.y * b.y;
+    im += a.x * b.y - a.y * b.x;
+}
+
 template <class R, int QT, int NST>
 __global__ void __launch_bounds__(288) k_corr_accum_bulk(const R* __restrict__ A, double* __restrict__ P,
                                                        const int* __restrict__ pairs, int ncorr, int nobs, int npos,
@@ -239,11 +246,48 @@ __global__ void __launch_bounds__(288) k_corr_accum_bulk(const R* __restrict__ A
             ib[k] = pr[2 * c + 1] * (npos + 1) + j;
         }
     }
+    // Three observables with the canonical six pairs (every ssf_* measure): a thread owns
+    // whole (i, j) sublattice pairs, loads the 3 + 3 spectra of a replica once and forms
+    // the six products from them, half the shared-memory loads of one entry per thread.
+    const bool canon = nobs == 3 && ncorr == 6 && pr[0] == 2 && pr[1] == 2 && pr[2] == 1 && pr[3] == 2 &&
+                       pr[4] == 0 && pr[5] == 2 && pr[6] == 1 && pr[7] == 1 && pr[8] == 0 && pr[9] == 1 &&
+                       pr[10] == 0 && pr[11] == 0;
     for (int ql = 0; ql < nq; ql++) {
         const int s = ql % NST;
         if (!mbar_wait_bounded(&full[s], (uint32_t)((ql / NST) & 1))) { bad = 1; break; }
         if (bad) break;
         double2* row = rows + (size_t)s * B;
+        if (canon) {
+            for (int pidx = threadIdx.x; pidx < npos * npos; pidx += nthr) {
+                const int i = pidx % npos, j = pidx / npos;
+                R tr[6], ti[6];
+#pragma unroll
+                for (int c = 0; c < 6; c++) { tr[c] = 0; ti[c] = 0; }
+                for (int rr = 0; rr < nrep; rr++) {
+                    const C2<R>* Ar = As + ((size_t)rr * QT + ql) * rowpad;
+                    const C2<R> a0 = Ar[i], a1 = Ar[(npos + 1) + i], a2 = Ar[2 * (npos + 1) + i];
+                    const C2<R> b0 = Ar[j], b1 = Ar[(npos + 1) + j], b2 = Ar[2 * (npos + 1) + j];
+                    cmul_conj_acc(a2, b2, tr[0], ti[0]);
+                    cmul_conj_acc(a1, b2, tr[1], ti[1]);
+                    cmul_conj_acc(a0, b2, tr[2], ti[2]);
+                    cmul_conj_acc(a1, b1, tr[3], ti[3]);
+                    cmul_conj_acc(a0, b1, tr[4], ti[4]);
+                    cmul_conj_acc(a0, b0, tr[5], ti[5]);
+                }
+                double2* e = row + (size_t)6 * pidx;
+#pragma unroll
+                for (int c = 0; c < 6; c++) {
+                    double2 acc = e[c];
+                    acc.x += (double)tr[c];
+                    acc.y += (double)ti[c];
+                    e[c] = acc;
+                }
+            }
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&done[s]);
+            continue;
+        }
 #pragma unroll
         for (int k = 0; k < KMAX; k++) {
             if (ia[k] < 0) continue;
