@@ -164,6 +164,45 @@ int sgb_langevin_noise(sgb_system* sys, uint64_t seed, uint64_t step, double* ou
 int sgb_midpoint(sgb_system* sys, double dt, double damping, double tol, int32_t max_iters,
                  int32_t nsteps, int64_t* iters_out);
 
+/* ---- LocalSampler (MonteCarlo/Samplers.jl) ----------------------------------- */
+
+#define SGB_PROPOSE_UNIFORM 0   /* propose_uniform = randspin (Samplers.jl:14, System.jl:444-447)   */
+#define SGB_PROPOSE_FLIP    1   /* propose_flip: S -> -S (Samplers.jl:23, System.jl:440-442)        */
+#define SGB_PROPOSE_DELTA   2   /* propose_delta(magnitude) (Samplers.jl:46-48, System.jl:454-460)  */
+
+/* A proposal function, or a @mix_proposals of up to 4 (Samplers.jl:64-98): kind i is
+ * chosen with probability weight[i] / sum(weight). magnitude[i] is used by
+ * SGB_PROPOSE_DELTA (INFINITY selects propose_uniform, as perturbed_spin does). */
+typedef struct {
+    int32_t n;
+    int32_t kind[4];
+    double  weight[4];
+    double  magnitude[4];
+} sgb_proposal;
+
+/* step!(sys, LocalSampler(; kT, nsweeps, propose)) (Samplers.jl:139-158), dipole modes.
+ * Sunny proposes ceil(nsweeps*ns) updates at uniformly drawn sites; here one sweep
+ * visits every site once, colour class by colour class of a greedy colouring of the
+ * bond graph (sites of one class share no coupling and are updated in parallel), so
+ * each sweep is a sequence of exact single-spin Metropolis updates and the chain has
+ * the same stationary distribution. A fractional nsweeps adds one sweep in which every
+ * site takes part with probability nsweeps - floor(nsweeps). Acceptance: ΔE <= 0 at
+ * kT = 0, else u <= exp(-ΔE/kT) with ΔE = local_energy_change.
+ * rand == NULL: random numbers from a counter-based generator keyed by
+ *   (seed, sweep0 + k, site); rand != NULL: caller-supplied, [nsweeps_total][ns][6]
+ *   = (3 standard normals, mixture uniform, acceptance uniform, participation uniform).
+ * dE (nullable) receives the summed energy change of the accepted updates and dS3
+ * (nullable) the summed dipole change: the sampler's ΔE and ΔS (Samplers.jl:153-156). */
+int sgb_local_sweeps(sgb_system* sys, double kT, double nsweeps, const sgb_proposal* propose,
+                     uint64_t seed, uint64_t sweep0, const double* rand, double* dE, double* dS3);
+
+/* The colouring used by sgb_local_sweeps: *ncolors classes, color (nullable) [ns]. */
+int sgb_local_colors(sgb_system* sys, int32_t* ncolors, int32_t* color);
+
+/* local_energy_change(sys, site, state) (Interactions.jl:311-373), dipole modes: the
+ * energy change if the dipole at `site` (0-based, Sunny's linear order) became S_new. */
+int sgb_local_energy_change(sgb_system* sys, int64_t site, const double* S_new, double* dE);
+
 /* ---- SampledCorrelations --------------------------------------------------- */
 
 typedef struct {

@@ -62,6 +62,9 @@ def load() -> C.CDLL:
             "or_observables": (None, [P, _D, _D, C.c_int, _D, _D]),
             "or_langevin_replicas": (C.c_int, [P, C.c_int, _D, _D, C.c_double, C.c_double, C.c_int, C.c_uint64]),
             "or_expected_spin": (None, [C.c_int, _D, _D]),
+            "or_local_energy_change": (C.c_double, [P, _D, C.c_int64, _D]),
+            "or_local_sweeps": (None, [P, _D, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_int), C.c_int,
+                                       C.POINTER(C.c_int), _D, _D, _D, _D, _D]),
         }
         for k, (res, args) in sig.items():
             f = getattr(lib, k)
@@ -137,6 +140,30 @@ class OracleSystem:
         out = np.zeros((self.ns, 3))
         self.lib.or_grad_dipoles(C.byref(self.s), _p(S), _p(out))
         return out
+
+    def local_energy_change(self, S, site, S_new):
+        """local_energy_change (Interactions.jl:311-373), dipole modes."""
+        S = np.ascontiguousarray(S, dtype=float)
+        Sn = np.ascontiguousarray(S_new, dtype=float)
+        return self.lib.or_local_energy_change(C.byref(self.s), _p(S), int(site), _p(Sn))
+
+    def local_sweeps(self, S, kT, nsweeps, frac, order, proposal, rand):
+        """LocalSampler updates in the site order `order` (each sweep), with caller randoms
+        rand [nsweeps][ns][6]; proposal: list of (kind, weight, magnitude). Returns
+        (S, dE, dS)."""
+        S = np.ascontiguousarray(S, dtype=float).copy()
+        perm = np.ascontiguousarray(order, dtype=np.int32)
+        w = np.array([p[1] for p in proposal], dtype=float)
+        cum = np.cumsum(w / w.sum())
+        kind = np.array([p[0] for p in proposal], dtype=np.int32)
+        mag = np.array([p[2] for p in proposal], dtype=float)
+        rnd = np.ascontiguousarray(rand, dtype=float).reshape(-1)
+        dE = C.c_double()
+        dS = np.zeros(3)
+        IP = C.POINTER(C.c_int)
+        self.lib.or_local_sweeps(C.byref(self.s), _p(S), float(kT), int(nsweeps), float(frac), perm.ctypes.data_as(IP),
+                                 len(proposal), kind.ctypes.data_as(IP), _p(cum), _p(mag), _p(rnd), C.byref(dE), _p(dS))
+        return S, dE.value, dS
 
     def energy(self, S, Z=None):
         S = np.ascontiguousarray(S, dtype=float)

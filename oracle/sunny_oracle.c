@@ -506,6 +506,101 @@ double or_energy(const or_sys* s, const double* S, const double* Z) {
     return E;
 }
 
+/* ---- local_energy_change (Interactions.jl:311-373), dipole modes ------------------ */
+static double biquad_pair(const sgb_bond* pc, const double* Qa, const double* Qb) {
+    /* Qa' B Qb (kind 2) or biquad * sum_q Qa_q metric_q Qb_q (kind 1) */
+    double acc = 0;
+    if (pc->biquad_kind == 1) {
+        for (int q = 0; q < 5; q++) acc += Qa[q] * (METRIC[q] * Qb[q]);
+        return pc->biquad[0] * acc;
+    }
+    for (int q = 0; q < 5; q++)
+        for (int p = 0; p < 5; p++) acc += Qa[q] * pc->biquad[q + 5 * p] * Qb[p];
+    return acc;
+}
+
+double or_local_energy_change(const or_sys* s, const double* S, int64_t site, const double* Snew) {
+    int L1 = s->L[0], L2 = s->L[1], L3 = s->L[2];
+    int64_t ncell = (int64_t)L1 * L2 * L3;
+    int a = (int)(site / ncell);
+    int64_t cell = site % ncell;
+    int c1 = (int)(cell % L1), c2 = (int)((cell / L1) % L2), c3 = (int)(cell / ((int64_t)L1 * L2));
+    const double* S0 = S + 3 * site;
+    double dS[3] = {Snew[0] - S0[0], Snew[1] - S0[1], Snew[2] - S0[2]};
+    double dE = 0.0;
+    if (s->field) {
+        const double* g = s->g + 9 * site;
+        const double* B = s->field + 3 * site;
+        for (int r = 0; r < 3; r++) dE += B[r] * (g[r] * dS[0] + g[r + 3] * dS[1] + g[r + 6] * dS[2]);
+    }
+    if (s->onsite) {
+        double g3[3];
+        dE += or_classical_anisotropy(s->onsite + 28 * a, Snew, g3) - or_classical_anisotropy(s->onsite + 28 * a, S0, g3);
+    }
+    double Qn[5], Qo[5], dQ[5];
+    quadrupole(Snew, Qn);
+    quadrupole(S0, Qo);
+    for (int q = 0; q < 5; q++) dQ[q] = Qn[q] - Qo[q];
+    for (int b = 0; b < s->nbonds; b++) {
+        const sgb_bond* pc = &s->bonds[b];
+        const double* J = pc->bilin;
+        if (pc->i == a) {   /* site is the first end: partner at c + n */
+            int64_t j = site_index(s, wrap(c1 + pc->n[0], L1), wrap(c2 + pc->n[1], L2), wrap(c3 + pc->n[2], L3), pc->j);
+            if (j == site) return NAN;
+            const double* Sj = S + 3 * j;
+            for (int r = 0; r < 3; r++) dE += dS[r] * (J[r] * Sj[0] + J[r + 3] * Sj[1] + J[r + 6] * Sj[2]);
+            if (pc->biquad_kind != 0) { double Qj[5]; quadrupole(Sj, Qj); dE += biquad_pair(pc, dQ, Qj); }
+        }
+        if (pc->j == a) {   /* site is the second end: partner at c - n */
+            int64_t k = site_index(s, wrap(c1 - pc->n[0], L1), wrap(c2 - pc->n[1], L2), wrap(c3 - pc->n[2], L3), pc->i);
+            if (k == site) return NAN;
+            const double* Sk = S + 3 * k;
+            for (int r = 0; r < 3; r++) dE += Sk[r] * (J[r] * dS[0] + J[r + 3] * dS[1] + J[r + 6] * dS[2]);
+            if (pc->biquad_kind != 0) { double Qk[5]; quadrupole(Sk, Qk); dE += biquad_pair(pc, Qk, dQ); }
+        }
+    }
+    return dE;
+}
+
+void or_local_sweeps(const or_sys* s, double* S, double kT, int nsweeps, double frac, const int* perm,
+                     int nkind, const int* kind, const double* cum, const double* mag, const double* rand,
+                     double* dE, double* dS3) {
+    int64_t ns = or_nsites(s);
+    double aE = 0, aS[3] = {0, 0, 0};
+    for (int k = 0; k < nsweeps; k++) {
+        int partial = (k == nsweeps - 1) && frac < 1.0;
+        for (int64_t idx = 0; idx < ns; idx++) {
+            int64_t site = perm[idx];
+            const double* r = rand + ((size_t)k * ns + site) * 6;
+            if (partial && !(r[5] < frac)) continue;
+            int kd = kind[nkind - 1];
+            double m = mag[nkind - 1];
+            for (int i = 0; i < nkind - 1; i++)
+                if (r[3] < cum[i]) { kd = kind[i]; m = mag[i]; break; }
+            if (kd == SGB_PROPOSE_DELTA && isinf(m)) kd = SGB_PROPOSE_UNIFORM;
+            const double kap = s->kappa[site];
+            const double* S0 = S + 3 * site;
+            double Sn[3];
+            if (kd == SGB_PROPOSE_FLIP) {
+                Sn[0] = -S0[0]; Sn[1] = -S0[1]; Sn[2] = -S0[2];
+            } else {
+                double v[3];
+                if (kd == SGB_PROPOSE_UNIFORM) { v[0] = r[0]; v[1] = r[1]; v[2] = r[2]; }   /* randspin */
+                else for (int c = 0; c < 3; c++) v[c] = S0[c] + m * kap * r[c];             /* perturbed_spin */
+                normalize_dipole(v, kap, Sn);
+            }
+            double e = or_local_energy_change(s, S, site, Sn);
+            int accept = kT == 0.0 ? (e <= 0.0) : (r[4] <= exp(-e / kT));
+            if (accept) {
+                aE += e;
+                for (int c = 0; c < 3; c++) { aS[c] += Sn[c] - S0[c]; S[3 * site + c] = Sn[c]; }
+            }
+        }
+    }
+    if (dE) *dE = aE;
+    if (dS3) { dS3[0] = aS[0]; dS3[1] = aS[1]; dS3[2] = aS[2]; }
+}
+
 /* ---- Integrators.jl:266-275 rhs_dipole! for one site ------------------------------- */
 static inline void rhs_dipole(const double* S, const double* xi, const double* g, double dt, double lam, double* dS) {
     double v[3];

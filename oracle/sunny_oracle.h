@@ -71,6 +71,23 @@ int or_midpoint_steps(const or_sys* s, double* S, double* Z, double dt, double d
 void or_observables(const or_sys* s, const double* S, const double* Z, int nobs,
                     const double* obs, double* out);
 
+/* local_energy_change (Interactions.jl:311-373), dipole modes: energy change if the dipole
+ * at `site` became Snew. Pair terms of both bond directions: ΔS·J·S_j where the site is
+ * the bond's first end, S_k·J·ΔS where it is the second. Returns NAN for a bond that
+ * maps a site onto itself (the reference raises an error there). */
+double or_local_energy_change(const or_sys* s, const double* S, int64_t site, const double* Snew);
+
+/* LocalSampler updates (Samplers.jl:139-158, proposals System.jl:440-460, mixture
+ * Samplers.jl:64-98) applied in a fixed order: for each of `nsweeps` sweeps, the sites
+ * perm[0..ns) in turn; in the last sweep a site takes part only if its participation
+ * uniform is below `frac` (frac >= 1: all). rand: [nsweeps][ns][6] = 3 standard normals,
+ * mixture uniform, acceptance uniform, participation uniform, indexed by site. kind/cum/
+ * mag: the mixture (cum = cumulative probabilities). dE, dS3 receive the sums of the
+ * accepted changes. */
+void or_local_sweeps(const or_sys* s, double* S, double kT, int nsweeps, double frac, const int* perm,
+                     int nkind, const int* kind, const double* cum, const double* mag, const double* rand,
+                     double* dE, double* dS3);
+
 /* Independent replicas stepped on a thread pool (OpenMP when compiled with it):
  * replica r has state S + r*ns*3 and temperature kT[r]; noise from the caller per
  * replica is not supported, the CPU path uses its own Gaussian source seeded by

@@ -10,7 +10,8 @@ from .operators import (spin_matrices, spin_matrices_of_dim, stevens_matrices_of
                         matrix_to_stevens_coefficients, expected_spin, ket_from_dipole)
 from .system import (System, Moment, Langevin, ImplicitMidpoint, step, energy, energy_per_site,
                      magnetization, energy_grad, set_exchange, set_onsite_coupling, set_field,
-                     randomize_spins, polarize_spins, langevin_noise)
+                     randomize_spins, polarize_spins, langevin_noise, LocalSampler, propose_uniform,
+                     propose_flip, propose_delta, mix_proposals, local_energy_change, local_colors)
 from .correlations import (SampledCorrelations, MeasureSpec, ssf_trace, ssf_perp, ssf_custom, add_sample,
                            merge_correlations, available_energies, available_wave_vectors,
                            adjusted_dt_and_downsampling_factor, all_dipole_observables, intensities,

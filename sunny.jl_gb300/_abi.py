@@ -38,6 +38,13 @@ class BondC(C.Structure):
                 ("bilin", C.c_double * 9), ("biquad_kind", C.c_int32), ("biquad", C.c_double * 25)]
 
 
+class Proposal(C.Structure):
+    _fields_ = [("n", C.c_int32), ("kind", C.c_int32 * 4), ("weight", C.c_double * 4), ("magnitude", C.c_double * 4)]
+
+
+PROPOSE_UNIFORM, PROPOSE_FLIP, PROPOSE_DELTA = 0, 1, 2
+
+
 class CorrDesc(C.Structure):
     _fields_ = [("nobs", C.c_int32), ("obs", C.POINTER(C.c_double)), ("ncorr", C.c_int32),
                 ("pairs", C.POINTER(C.c_int32)), ("n_all_omega", C.c_int32), ("measperiod", C.c_int32),
@@ -69,6 +76,9 @@ SIGNATURES = {
     "sgb_langevin": (C.c_int, [_P, C.c_double, C.c_double, C.c_double, _U64, _U64, _I32, _D]),
     "sgb_langevin_noise": (C.c_int, [_P, _U64, _U64, _D]),
     "sgb_midpoint": (C.c_int, [_P, C.c_double, C.c_double, C.c_double, _I32, _I32, C.POINTER(_I64)]),
+    "sgb_local_sweeps": (C.c_int, [_P, C.c_double, C.c_double, C.POINTER(Proposal), _U64, _U64, _D, _D, _D]),
+    "sgb_local_colors": (C.c_int, [_P, C.POINTER(_I32), C.POINTER(_I32)]),
+    "sgb_local_energy_change": (C.c_int, [_P, _I64, _D, _D]),
     "sgb_corr_create": (C.c_int, [_P, C.POINTER(CorrDesc), C.POINTER(_P)]),
     "sgb_corr_destroy": (None, [_P]),
     "sgb_corr_add_sample": (C.c_int, [_P, _I32]),

@@ -113,6 +113,9 @@ int build_tables(sgb_system* s, Model<R>& M) {
                             tab[(size_t)k * s->ns + site] = x1 + L1 * (x2 + L2 * (x3 + L3 * B.j));
                         }
                     }
+        s->boff_h.assign(boff, boff + na + 1);
+        s->nbr_h = tab;
+        s->colors_dirty = true;
         void* p = s->nbr;
         dfree(p);
         s->nbr = nullptr;
@@ -267,6 +270,103 @@ int do_refresh(sgb_system* s) {
     return rc ? cuda_fail(s, cudaGetLastError(), "refresh launch") : SGB_OK;
 }
 
+// Greedy colouring of the bond graph in site order (every bond is listed from both
+// ends, so a site's own list holds all its neighbours): class of a site = the smallest
+// class none of its already coloured neighbours has. Sites of one class share no
+// coupling and can be updated together by the LocalSampler sweep.
+int ensure_colors(sgb_system* s) {
+    int rc = ensure_tables(s);
+    if (rc) return rc;
+    if (!s->colors_dirty) return SGB_OK;
+    const int ns = s->ns, ncell = s->ncell;
+    std::vector<int> col(ns, -1);
+    int ncol = 0;
+    for (int i = 0; i < ns; i++) {
+        const int a = i / ncell;
+        uint64_t used = 0;
+        for (int k = 0; k < s->boff_h[a + 1] - s->boff_h[a]; k++) {
+            const int j = s->nbr_h[(size_t)k * ns + i];
+            // local_energy_change (Interactions.jl:345)
+            if (j == i) return fail(s, SGB_ERR_ARG, "Energy delta for self-interaction not supported");
+            if (col[j] >= 0 && col[j] < 64) used |= 1ull << col[j];
+        }
+        int c = 0;
+        while (c < 64 && ((used >> c) & 1ull)) c++;
+        if (c >= SGB_MC_MAXCOL) return fail(s, SGB_ERR_ARG, "bond graph needs more than 64 colour classes");
+        col[i] = c;
+        ncol = std::max(ncol, c + 1);
+    }
+    s->coff_h.assign(ncol + 1, 0);
+    for (int i = 0; i < ns; i++) s->coff_h[col[i] + 1]++;
+    for (int c = 0; c < ncol; c++) s->coff_h[c + 1] += s->coff_h[c];
+    s->perm_h.assign(ns, 0);
+    std::vector<int> pos(s->coff_h.begin(), s->coff_h.end() - 1);
+    for (int i = 0; i < ns; i++) s->perm_h[pos[col[i]]++] = i;   // ascending within a class
+    s->color_h = col;
+    void* p = s->mc_perm;
+    dfree(p);
+    s->mc_perm = nullptr;
+    if ((rc = dmalloc(s, (void**)&s->mc_perm, sizeof(int) * (size_t)ns))) return rc;
+    CK(cudaMemcpy(s->mc_perm, s->perm_h.data(), sizeof(int) * (size_t)ns, cudaMemcpyHostToDevice));
+    s->colors_dirty = false;
+    return SGB_OK;
+}
+
+template <class R>
+int run_local_sweeps(sgb_system* s, McArgs& A, const double* rnd_host, double* out4) {
+    int bps = 0;
+    if (mc_max_blocks<R>((size_t)s->tables_bytes, &bps) != SGB_OK || bps < 1)
+        return fail(s, SGB_ERR_CUDA, "occupancy query failed");
+    int maxclass = 1;
+    for (int c = 0; c < A.ncol; c++) maxclass = std::max(maxclass, A.coff[c + 1] - A.coff[c]);
+    const int grid = std::max(1, std::min(bps * s->nsm, (maxclass + SGB_BLOCK - 1) / SGB_BLOCK));
+    int rc;
+    if (s->mc_part_cap < grid) {
+        void* p = s->mc_part;
+        dfree(p);
+        s->mc_part = nullptr;
+        s->mc_part_cap = 0;
+        if ((rc = dmalloc(s, (void**)&s->mc_part, sizeof(double) * 4 * (size_t)grid))) return rc;
+        s->mc_part_cap = grid;
+    }
+    const int total = A.nsweeps;
+    const size_t per = (size_t)6 * s->ns;
+    int chunk = total;
+    if (rnd_host) {
+        chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)total, ((size_t)1 << 24) / per));
+        if ((rc = ensure_dbuf(s, per * chunk))) return rc;
+    }
+    double acc[4] = {0, 0, 0, 0};
+    const double frac = A.frac;
+    for (int k0 = 0; k0 < total; k0 += chunk) {
+        const int nk = std::min(chunk, total - k0);
+        McArgs a = A;
+        a.nsweeps = nk;
+        a.sweep0 = A.sweep0 + (uint64_t)k0;
+        a.frac = (k0 + nk == total) ? frac : 1.0;
+        a.rnd = nullptr;
+        if (rnd_host) {
+            CK(cudaMemcpyAsync(s->dbuf, rnd_host + per * k0, per * nk * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+            a.rnd = s->dbuf;
+        }
+        if ((rc = reset_ctrl(s))) return rc;
+        rc = mc_launch_sweeps<R>(model<R>(s), (R*)s->S, s->ctrl, a, grid, s->mc_part, s->stream);
+        s->launches++;
+        if (rc) return cuda_fail(s, cudaGetLastError(), "LocalSampler launch");
+        if ((rc = util_launch_reduce(s->mc_part, grid, 4, s->red, s->stream))) return cuda_fail(s, cudaGetLastError(), "reduce launch");
+        s->launches++;
+        double part[4];
+        CK(cudaMemcpyAsync(part, s->red, sizeof(part), cudaMemcpyDeviceToHost, s->stream));
+        Ctrl c;
+        if ((rc = read_ctrl(s, &c))) return rc;
+        if (c.status == SGB_ERR_TIMEOUT) return fail(s, SGB_ERR_TIMEOUT, "a device-side barrier timed out");
+        if (c.status != 0) return fail(s, c.status, "LocalSampler kernel reported an error");
+        for (int q = 0; q < 4; q++) acc[q] += part[q];
+    }
+    for (int q = 0; q < 4; q++) out4[q] = acc[q];
+    return SGB_OK;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------------
@@ -352,6 +452,8 @@ void sgb_destroy(sgb_system* s) {
     p = s->partials; dfree(p);
     p = s->red; dfree(p);
     p = s->dbuf; dfree(p);
+    p = s->mc_perm; dfree(p);
+    p = s->mc_part; dfree(p);
     dfree(s->flush);
     if (s->stage) cudaFreeHost(s->stage);
     for (int i = 0; i < 8; i++) if (s->ev[i]) cudaEventDestroy(s->ev[i]);
@@ -593,6 +695,85 @@ int sgb_midpoint(sgb_system* s, double dt, double damping, double tol, int32_t m
     }
     SnapArgs<double> sn{};
     return run_midpoint<double>(s, dt, damping, tol, max_iters, nsteps, iters_out, sn, true, s->mid_order);
+}
+
+int sgb_local_sweeps(sgb_system* s, double kT, double nsweeps, const sgb_proposal* prop, uint64_t seed, uint64_t sweep0,
+                     const double* rand, double* dE, double* dS3) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    if (s->sun) return fail(s, SGB_ERR_ARG, "LocalSampler on the GPU supports the dipole modes");
+    if (!(kT >= 0)) return fail(s, SGB_ERR_ARG, "Select nonnegative kT");
+    if (!(nsweeps >= 0) || nsweeps > 1e9) return fail(s, SGB_ERR_ARG, "nsweeps must be nonnegative");
+    if (!prop || prop->n < 1 || prop->n > 4) return fail(s, SGB_ERR_ARG, "a proposal mixture has 1 to 4 functions");
+    McArgs A{};
+    double wsum = 0;
+    for (int i = 0; i < prop->n; i++) {
+        const int k = prop->kind[i];
+        if (k != SGB_PROPOSE_UNIFORM && k != SGB_PROPOSE_FLIP && k != SGB_PROPOSE_DELTA)
+            return fail(s, SGB_ERR_ARG, "unknown proposal kind");
+        if (!(prop->weight[i] >= 0)) return fail(s, SGB_ERR_ARG, "proposal weights must be nonnegative");
+        if (k == SGB_PROPOSE_DELTA && !(prop->magnitude[i] >= 0)) return fail(s, SGB_ERR_ARG, "propose_delta magnitude must be nonnegative");
+        wsum += prop->weight[i];
+    }
+    if (!(wsum > 0)) return fail(s, SGB_ERR_ARG, "proposal weights must not all be zero");
+    // cumulative probabilities (Samplers.jl:77-81)
+    double run = 0;
+    for (int i = 0; i < prop->n; i++) {
+        run += prop->weight[i] / wsum;
+        A.kind[i] = prop->kind[i];
+        A.cum[i] = run;
+        A.mag[i] = prop->magnitude[i];
+    }
+    A.nkind = prop->n;
+    if (dE) *dE = 0;
+    if (dS3) dS3[0] = dS3[1] = dS3[2] = 0;
+    const double nfull = std::floor(nsweeps);
+    const double frac = nsweeps - nfull;
+    const int total = (int)nfull + (frac > 0 ? 1 : 0);
+    if (total == 0) return SGB_OK;
+    int rc = ensure_colors(s);
+    if (rc) return rc;
+    if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called before stepping");
+    A.perm = s->mc_perm;
+    A.ncol = (int)s->coff_h.size() - 1;
+    for (int c = 0; c <= A.ncol; c++) A.coff[c] = s->coff_h[c];
+    A.nsweeps = total;
+    A.frac = frac > 0 ? frac : 1.0;
+    A.kT = kT;
+    A.seed = seed;
+    A.sweep0 = sweep0;
+    double out[4];
+    rc = s->fp32 ? run_local_sweeps<float>(s, A, rand, out) : run_local_sweeps<double>(s, A, rand, out);
+    if (rc) return rc;
+    if (dE) *dE = out[0];
+    if (dS3) { dS3[0] = out[1]; dS3[1] = out[2]; dS3[2] = out[3]; }
+    return SGB_OK;
+}
+
+int sgb_local_colors(sgb_system* s, int32_t* ncolors, int32_t* color) {
+    if (!s || !ncolors) return fail(s, SGB_ERR_ARG, "null argument");
+    int rc = ensure_colors(s);
+    if (rc) return rc;
+    *ncolors = (int32_t)s->coff_h.size() - 1;
+    if (color)
+        for (int i = 0; i < s->ns; i++) color[i] = s->color_h[i];
+    return SGB_OK;
+}
+
+int sgb_local_energy_change(sgb_system* s, int64_t site, const double* S_new, double* dE) {
+    if (!s || !S_new || !dE) return fail(s, SGB_ERR_ARG, "null argument");
+    if (s->sun) return fail(s, SGB_ERR_ARG, "LocalSampler on the GPU supports the dipole modes");
+    if (site < 0 || site >= s->ns) return fail(s, SGB_ERR_ARG, "site out of range");
+    int rc = ensure_colors(s);   // also rejects self-interaction
+    if (rc) return rc;
+    if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called first");
+    if ((rc = ensure_dbuf(s, 1))) return rc;
+    rc = s->fp32 ? mc_launch_local_dE<float>(s->mf, (const float*)s->S, (int)site, S_new[0], S_new[1], S_new[2], s->dbuf, s->stream)
+                 : mc_launch_local_dE<double>(s->md, (const double*)s->S, (int)site, S_new[0], S_new[1], S_new[2], s->dbuf, s->stream);
+    s->launches++;
+    if (rc) return cuda_fail(s, cudaGetLastError(), "local energy launch");
+    CK(cudaMemcpyAsync(dE, s->dbuf, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return SGB_OK;
 }
 
 int sgb_event_record(sgb_system* s, int32_t slot) {

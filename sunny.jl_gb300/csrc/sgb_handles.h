@@ -49,6 +49,13 @@ struct sgb_system {
     char* stage = nullptr;      // pinned host staging
     size_t stage_cap = 0;
     std::vector<sgb_corr*> corrs;   // accumulators created on this system (detached on destroy)
+    // LocalSampler: neighbour table on the host, the bond-graph colouring and its device copy
+    std::vector<int> nbr_h, boff_h;   // [kb][ns] as nbr; bonds per sublattice offsets [na+1]
+    std::vector<int> color_h, perm_h, coff_h;
+    bool colors_dirty = true;
+    int* mc_perm = nullptr;
+    double* mc_part = nullptr;       // [grid][4] per-block ΔE, ΔS partials
+    int mc_part_cap = 0;
 };
 
 struct sgb_corr {

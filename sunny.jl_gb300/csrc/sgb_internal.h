@@ -85,6 +85,31 @@ int sun_launch_energy(const Model<R>& M, const R* Z, const R* D, const R* Q, dou
 template <class R>
 int sun_max_blocks(int N, int spt, int block, size_t smem, int* blocks_per_sm);
 
+// ---- LocalSampler (sgb_mc.cu) ----
+#define SGB_MC_MAXCOL 64       // colour classes of the bond-graph colouring
+struct McArgs {
+    const int* perm;             // [ns] sites ordered by colour class, ascending within a class
+    int coff[SGB_MC_MAXCOL + 1]; // class c is perm[coff[c] .. coff[c+1])
+    int ncol;
+    int nsweeps;                 // sweeps, the last one partial when frac < 1
+    double frac;                 // participation probability of the last sweep
+    double kT;
+    int nkind;                   // proposal mixture (sgb_proposal)
+    int kind[4];
+    double cum[4];               // cumulative probabilities
+    double mag[4];
+    uint64_t seed, sweep0;
+    const double* rnd;           // injected randoms [nsweeps][ns][6] or nullptr
+};
+template <class R>
+int mc_launch_sweeps(const Model<R>& M, R* S, Ctrl* ctrl, const McArgs& A, int grid, double* partials,
+                     cudaStream_t st);
+template <class R>
+int mc_max_blocks(size_t smem, int* blocks_per_sm);
+template <class R>
+int mc_launch_local_dE(const Model<R>& M, const R* S, int site, double nx, double ny, double nz, double* out,
+                       cudaStream_t st);
+
 // ---- shared utilities (sgb_dipole.cu) ----
 int util_launch_reduce(const double* partials, int n, int ncomp, double* out, cudaStream_t st);
 template <class R>

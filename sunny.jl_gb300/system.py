@@ -76,6 +76,62 @@ class ImplicitMidpoint:
         return ImplicitMidpoint(self.dt, damping=self.damping, kT=self.kT, tol=self.tol)
 
 
+class Proposal:
+    """A LocalSampler proposal function, or a mixture of them (Samplers.jl:1-98):
+    `terms` holds (kind, weight, magnitude) with kind one of _abi.PROPOSE_*."""
+
+    def __init__(self, terms):
+        self.terms = [(int(k), float(w), float(m)) for k, w, m in terms]
+
+    def cstruct(self) -> _abi.Proposal:
+        p = _abi.Proposal()
+        p.n = len(self.terms)
+        for i, (k, w, m) in enumerate(self.terms):
+            p.kind[i], p.weight[i], p.magnitude[i] = k, w, m
+        return p
+
+
+propose_uniform = Proposal([(_abi.PROPOSE_UNIFORM, 1.0, 0.0)])   # Samplers.jl:14 (randspin)
+propose_flip = Proposal([(_abi.PROPOSE_FLIP, 1.0, 0.0)])         # Samplers.jl:23
+
+
+def propose_delta(magnitude) -> Proposal:
+    """propose_delta(magnitude) (Samplers.jl:46-48): S + |S| ξ with ξ ~ N(0, magnitude²),
+    renormalised; an infinite magnitude is propose_uniform (System.jl:455)."""
+    return Proposal([(_abi.PROPOSE_DELTA, 1.0, float(magnitude))])
+
+
+def mix_proposals(*terms) -> Proposal:
+    """@mix_proposals weight1 propose1 weight2 propose2 ... (Samplers.jl:64-98)."""
+    if len(terms) % 2:
+        raise ValueError("Alternate weights and proposal functions.")
+    out = []
+    for w, p in zip(terms[0::2], terms[1::2]):
+        if len(p.terms) != 1:
+            raise ValueError("mix_proposals takes single proposal functions")
+        k, _, m = p.terms[0]
+        out.append((k, float(w), m))
+    if not 1 <= len(out) <= 4:
+        raise ValueError("a proposal mixture has 1 to 4 functions")
+    return Proposal(out)
+
+
+class LocalSampler:
+    """LocalSampler(; kT, nsweeps=1.0, propose=propose_uniform) (Samplers.jl:101-137).
+
+    `ΔE` and `ΔS` accumulate the energy and net dipole changes of accepted updates."""
+
+    def __init__(self, *, kT, nsweeps=1.0, propose=None):
+        self.kT = float(kT)
+        self.nsweeps = float(nsweeps)
+        self.propose = propose if propose is not None else propose_uniform
+        self.ΔE = 0.0
+        self.ΔS = np.zeros(3)
+
+    def copy(self):
+        return LocalSampler(kT=self.kT, nsweeps=self.nsweeps, propose=self.propose)
+
+
 @dataclass
 class PairCoupling:
     scalar: float
@@ -129,6 +185,7 @@ class System:
         self.rng = np.random.default_rng(seed)
         self.seed = int(seed) if seed is not None else int(self.rng.integers(0, 2**62))
         self.noise_step = 0
+        self.mc_sweep = 0
         self._couplings_dirty = True
         self._host_newer = True
         self._dev_newer = False
@@ -490,6 +547,8 @@ def step(sys: System, integrator, nsteps: int = 1, noise: np.ndarray | None = No
     Langevin noise comes from the device generator keyed by (sys.seed, step counter),
     or from `noise` (standard normals, [nsteps][ns][3] or complex [nsteps][ns][N]).
     Returns the number of midpoint iterations (0 for Langevin)."""
+    if isinstance(integrator, LocalSampler):
+        return _local_sampler_steps(sys, integrator, nsteps, noise)
     if math.isnan(integrator.dt):
         raise ValueError("Set integration timestep `dt`.")
     sys._sync_to_device()
@@ -517,6 +576,54 @@ def step(sys: System, integrator, nsteps: int = 1, noise: np.ndarray | None = No
         _abi.check(rc, lib, h)
         return iters.value
     raise TypeError(f"unsupported integrator {type(integrator).__name__}")
+
+
+def _local_sampler_steps(sys: System, sampler: LocalSampler, nsteps: int, rand) -> int:
+    """`nsteps` x step!(sys, sampler) (Samplers.jl:139-158). Random numbers come from the
+    device generator keyed by (sys.seed, sweep counter), or from `rand`
+    ([sweeps][ns][6]: 3 normals, mixture, acceptance and participation uniforms)."""
+    sys._sync_to_device()
+    lib, h = sys._lib, sys._h
+    per_step = math.ceil(sampler.nsweeps)
+    if rand is not None:
+        rand = np.ascontiguousarray(rand, dtype=float).reshape(-1)
+        if rand.size != per_step * nsteps * sys.nsites * 6:
+            raise ValueError("rand must hold sweeps x nsites x 6 numbers")
+    prop = sampler.propose.cstruct()
+    # integer sweeps fuse into one launch; a fractional sweep ends every step
+    calls = [(sampler.nsweeps * nsteps, 0)] if sampler.nsweeps == per_step else \
+        [(sampler.nsweeps, k * per_step) for k in range(nsteps)]
+    dE, dS = C.c_double(), np.zeros(3)
+    for nsw, k0 in calls:
+        r = None if rand is None else rand[k0 * sys.nsites * 6:]
+        rc = lib.sgb_local_sweeps(h, sampler.kT, nsw, C.byref(prop), sys.seed, sys.mc_sweep, _abi.dptr(r), C.byref(dE),
+                                  _abi.dptr(dS))
+        sys._dev_newer = True
+        _abi.check(rc, lib, h)
+        sys.mc_sweep += math.ceil(nsw)
+        sampler.ΔE += dE.value
+        sampler.ΔS = sampler.ΔS + dS
+    return 0
+
+
+def local_energy_change(sys: System, site: int, S_new) -> float:
+    """local_energy_change(sys, site, state) (Interactions.jl:311-373), dipole modes;
+    `site` is the 0-based linear index."""
+    sys._sync_to_device()
+    out = C.c_double()
+    Sn = np.ascontiguousarray(S_new, dtype=float).reshape(3)
+    _abi.check(sys._lib.sgb_local_energy_change(sys._h, int(site), _abi.dptr(Sn), C.byref(out)), sys._lib, sys._h)
+    return out.value
+
+
+def local_colors(sys: System):
+    """(ncolors, color per site) of the bond-graph colouring the LocalSampler sweeps use."""
+    sys._sync_to_device()
+    n = C.c_int32()
+    col = np.zeros(sys.nsites, dtype=np.int32)
+    _abi.check(sys._lib.sgb_local_colors(sys._h, C.byref(n), col.ctypes.data_as(C.POINTER(C.c_int32))), sys._lib,
+               sys._h)
+    return n.value, col
 
 
 def langevin_noise(sys: System, step_index: int) -> np.ndarray:

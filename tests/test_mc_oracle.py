@@ -1,0 +1,62 @@
+"""LocalSampler on the CPU: the oracle's local_energy_change against total-energy
+differences (test_energy_consistency.jl:58-76 does the same check at atol 1e-12), the
+sampler's ΔE/ΔS bookkeeping, and the host-side proposal mixture rules."""
+import numpy as np
+import pytest
+
+from models import rich_dipole, sc_c1
+
+
+def _systems(sg):
+    yield rich_dipole(sg, device=None)
+    yield sc_c1(sg, L=4, device=None)
+    # an axis of length 2: a site meets the same neighbour through two bonds
+    s = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=2, g=2))], "dipole", dims=(2, 3, 4), seed=5, device=None)
+    s.set_bond_coupling(sg.Bond(1, 1, [1, 0, 0]), 0.2, np.array([[0.1, 0.2, 0.3], [0.0, -0.4, 0.5], [0.6, 0.0, 0.7]]),
+                        0.3)
+    s.set_exchange(-0.5, sg.Bond(1, 1, [0, 1, 1]))
+    s.randomize_spins()
+    yield s
+
+
+def test_oracle_local_energy_change_is_energy_difference(sg, orc):
+    rng = np.random.default_rng(0)
+    for sys_ in _systems(sg):
+        o = orc.OracleSystem.from_system(sys_)
+        S = sys_.dipoles_flat()
+        kap = sys_.kappas.reshape(-1) if hasattr(sys_.kappas, "reshape") else np.asarray(sys_.kappas)
+        E0 = o.energy(S)
+        for _ in range(5):
+            i = int(rng.integers(0, sys_.nsites))
+            v = rng.standard_normal(3)
+            Sn = kap[i] * v / np.linalg.norm(v)
+            dE = o.local_energy_change(S, i, Sn)
+            S1 = S.copy()
+            S1[i] = Sn
+            assert dE == pytest.approx(o.energy(S1) - E0, abs=1e-12 * max(1.0, abs(E0)))
+
+
+def test_oracle_local_sweeps_bookkeeping(sg, orc):
+    sys_ = rich_dipole(sg, device=None)
+    o = orc.OracleSystem.from_system(sys_)
+    S0 = sys_.dipoles_flat()
+    rng = np.random.default_rng(1)
+    rand = np.concatenate([rng.standard_normal((3, sys_.nsites, 3)), rng.random((3, sys_.nsites, 3))], axis=2)
+    prop = [(0, 0.3, 0.0), (1, 0.2, 0.0), (2, 0.5, 0.4)]
+    S1, dE, dS = o.local_sweeps(S0, 0.7, 3, 0.5, np.arange(sys_.nsites), prop, rand)
+    assert not np.allclose(S1, S0)
+    assert dE == pytest.approx(o.energy(S1) - o.energy(S0), abs=1e-10)
+    assert np.allclose(dS, S1.sum(0) - S0.sum(0), atol=1e-10)
+    kap = np.asarray(sys_.kappas).reshape(-1)
+    assert np.allclose(np.linalg.norm(S1, axis=1), kap, rtol=1e-13)
+
+
+def test_proposal_mixture_rules(sg):
+    m = sg.mix_proposals(0.4, sg.propose_flip, 0.6, sg.propose_delta(0.2))
+    assert m.terms == [(1, 0.4, 0.0), (2, 0.6, 0.2)]
+    with pytest.raises(ValueError, match="Alternate weights"):
+        sg.mix_proposals(0.4, sg.propose_flip, 0.6)
+    s = sg.LocalSampler(kT=0.2)
+    assert s.nsweeps == 1.0 and s.propose is sg.propose_uniform and s.ΔE == 0.0
+    c = s.copy()
+    assert c.kT == 0.2 and c is not s
