@@ -11,12 +11,13 @@ from .operators import (spin_matrices, spin_matrices_of_dim, stevens_matrices_of
 from .system import (System, Moment, Langevin, ImplicitMidpoint, step, energy, energy_per_site,
                      magnetization, energy_grad, set_exchange, set_onsite_coupling, set_field,
                      randomize_spins, polarize_spins, langevin_noise, LocalSampler, propose_uniform,
-                     propose_flip, propose_delta, mix_proposals, local_energy_change, local_colors)
+                     propose_flip, propose_delta, mix_proposals, local_energy_change, local_colors,
+                     clone_system)
 from .correlations import (SampledCorrelations, MeasureSpec, ssf_trace, ssf_perp, ssf_custom, add_sample,
                            merge_correlations, available_energies, available_wave_vectors,
                            adjusted_dt_and_downsampling_factor, all_dipole_observables, intensities,
                            intensities_static, Intensities)
-from .tempering import ReplicaBatch, ParallelTempering
+from .tempering import ReplicaBatch, ParallelTempering, SystemParallelTempering, exchange_round
 from .adjoint import SampledCorrelationsAdjoint
 from ._abi import SunnyGPUError, load as load_library
 

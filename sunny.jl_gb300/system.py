@@ -191,6 +191,7 @@ class System:
         self._dev_newer = False
         self._h = None
         self._lib = None
+        self.device = device
         if device is None:
             self.polarize_spins((0, 0, 1))
             return
@@ -576,6 +577,31 @@ def step(sys: System, integrator, nsteps: int = 1, noise: np.ndarray | None = No
         _abi.check(rc, lib, h)
         return iters.value
     raise TypeError(f"unsupported integrator {type(integrator).__name__}")
+
+
+def clone_system(sys: System, seed=None) -> System:
+    """clone_system(sys) (System.jl:144-175): a new System with copies of the couplings,
+    κ, g, field and state, on the same device. Sunny copies the RNG; the clone keeps
+    sys.seed and its counters unless `seed` is given."""
+    if sys._h is not None:
+        sys._sync_to_host()
+    mom =[(i + 1, m) for i, m in enumerate(sys.moments)]
+    c = System(sys.crystal, mom, sys.mode, sys.dims, seed=sys.seed if seed is None else seed,
+               precision=sys.precision, device=sys.device)
+    c._kappa[:] = sys._kappa
+    c._g[:] = sys._g
+    c._field[:] = sys._field
+    c._pairs = {b: PairCoupling(pc.scalar, np.array(pc.bilin, dtype=float),
+                                pc.biquad.copy() if isinstance(pc.biquad, np.ndarray) else pc.biquad)
+                for b, pc in sys._pairs.items()}
+    c._onsite = [None if o is None else np.array(o) for o in sys._onsite]
+    c._base_dip[:] = sys._base_dip
+    c._base_coh[:] = sys._base_coh
+    if seed is None:
+        c.noise_step, c.mc_sweep = sys.noise_step, sys.mc_sweep
+    c._couplings_dirty = True
+    c._host_newer = True
+    return c
 
 
 def _local_sampler_steps(sys: System, sampler: LocalSampler, nsteps: int, rand) -> int:

@@ -10,11 +10,12 @@ CUDA graph.
 from __future__ import annotations
 
 import ctypes as C
+import math
 
 import numpy as np
 
 from . import _abi
-from .system import System
+from .system import System, LocalSampler, clone_system, energy, magnetization, step
 
 
 class ReplicaBatch:
@@ -133,9 +134,39 @@ class ReplicaBatch:
         return out
 
 
+def exchange_round(E, kT, system_ids, exch_start, uniform):
+    """The swap decisions of replica_exchange! (ParallelTempering.jl:40-73) on one ladder.
+    E[k]: energy at ladder position k; exch_start is 1-based (1 or 2); uniform(k) draws
+    the acceptance uniform of pair (k, k+1). Returns the new ids and, per position, whether
+    an exchange was attempted and accepted."""
+    n = len(kT)
+    ids = list(system_ids)
+    E = list(E)
+    tried = np.zeros(n, dtype=bool)
+    acc = np.zeros(n, dtype=bool)
+    for k in range(exch_start - 1, n - 1, 2):
+        E1, E2 = E[k], E[k + 1]
+        lnP = (E1 / kT[k] - E2 / kT[k]) + (E2 / kT[k + 1] - E1 / kT[k + 1])
+        tried[k] = True
+        if lnP >= 0 or uniform(k) < math.exp(lnP):
+            ids[k], ids[k + 1] = ids[k + 1], ids[k]
+            E[k], E[k + 1] = E[k + 1], E[k]
+            acc[k] = True
+    return ids, tried, acc
+
+
 class ParallelTempering:
     """ParallelTempering(system, Langevin, kT_sched) over replicas of (possibly) several
-    sizes (ParallelTempering.jl:18-37). Each group of equal dims has its own ladder."""
+    sizes (ParallelTempering.jl:18-37). Each group of equal dims has its own ladder.
+
+    ParallelTempering(system, sampler, kT_sched) with a `System` builds the reference's
+    own form instead: clones of one system, one sampler per temperature
+    (SystemParallelTempering)."""
+
+    def __new__(cls, *args, **kw):
+        if cls is ParallelTempering and args and isinstance(args[0], System):
+            return super().__new__(SystemParallelTempering)
+        return super().__new__(cls)
 
     def __init__(self, batch: ReplicaBatch, dt: float, damping: float):
         self.batch = batch
@@ -167,3 +198,66 @@ class ParallelTempering:
     @property
     def graph_active(self) -> bool:
         return bool(self.batch._lib.sgb_batch_graph_active(self.batch._h))
+
+
+class SystemParallelTempering(ParallelTempering):
+    """ParallelTempering(system, sampler, kT_sched) (ParallelTempering.jl:2-95) over device
+    clones of one System.
+
+    - Each ladder position has its own copy of `sampler` at its temperature; with a
+      LocalSampler its ΔE/ΔS start at the clone's energy and net dipole and are swapped
+      with the systems, so exchanges need no energy evaluation (ParallelTempering.jl:28-34,
+      45-46, 64-66); other samplers (Langevin) use energy(system).
+    - Clone r uses seed system.seed + r for its device random streams (Sunny copies the
+      RNG); the exchange uniforms come from a host generator seeded by system.seed.
+    """
+
+    def __init__(self, system: System, sampler, kT_sched):
+        self.n_replicas = len(kT_sched)
+        self.kT_sched = [float(k) for k in kT_sched]
+        self.samplers = []
+        for kT in self.kT_sched:
+            smp = sampler.copy()
+            smp.kT = kT
+            self.samplers.append(smp)
+        self.systems = [clone_system(system, seed=system.seed + r) for r in range(self.n_replicas)]
+        self.system_ids = list(range(self.n_replicas))
+        self.n_accept = np.zeros(self.n_replicas, dtype=np.int64)
+        self.n_exch = np.zeros(self.n_replicas, dtype=np.int64)
+        self.rng = np.random.default_rng(system.seed)
+        self.local = isinstance(sampler, LocalSampler)
+        if self.local:
+            for rank in range(self.n_replicas):
+                self.samplers[rank].ΔE = energy(self.systems[rank])
+                self.samplers[rank].ΔS = magnetization(self.systems[rank])
+                self.samplers[rank].nsweeps = 1.0
+
+    def energies(self):
+        """Energy at each ladder position, as the exchange sees it."""
+        if self.local:
+            return [s.ΔE for s in self.samplers]
+        return [energy(self.systems[i]) for i in self.system_ids]
+
+    def replica_exchange(self, exch_start: int):
+        """replica_exchange!(PT, exch_start) (ParallelTempering.jl:40-73)."""
+        ids, tried, acc = exchange_round(self.energies(), self.kT_sched, self.system_ids, exch_start,
+                                         lambda k: self.rng.random())
+        if self.local:
+            for k in np.nonzero(acc)[0]:
+                a, b = self.samplers[k], self.samplers[k + 1]
+                a.ΔE, b.ΔE = b.ΔE, a.ΔE
+                a.ΔS, b.ΔS = b.ΔS, a.ΔS
+        self.system_ids = ids
+        self.n_accept += acc
+        self.n_exch += tried
+
+    def step_ensemble(self, nsteps: int, exch_interval: int):
+        """step_ensemble!(PT, nsteps, exch_interval) (ParallelTempering.jl:80-95)."""
+        for i in range(1, -(-nsteps // exch_interval) + 1):
+            for rank in range(self.n_replicas):
+                step(self.systems[self.system_ids[rank]], self.samplers[rank], exch_interval)
+            self.replica_exchange((i % 2) + 1)
+
+    def close(self):
+        for s in self.systems:
+            s.close()

@@ -163,3 +163,27 @@ def test_rejects_sun_and_self_bonds(gpu, sg):
     d.randomize_spins()
     with pytest.raises(sg.SunnyGPUError, match="self-interaction"):
         sg.step(d, sg.LocalSampler(kT=0.1))
+
+
+@pytest.mark.parametrize("kind", ["local", "langevin"])
+def test_parallel_tempering_over_clones(gpu, sg, kind):
+    sys_ = sc_c1(sg, L=4, J=-1.0, D=0.3)
+    kT = [1.0, 1.04, 1.08, 1.12]   # close enough for swaps of 64-spin replicas to be accepted
+    smp = sg.LocalSampler(kT=1.0, propose=sg.propose_delta(0.5)) if kind == "local" else \
+        sg.Langevin(0.02, damping=0.2, kT=1.0)
+    pt = sg.ParallelTempering(sys_, smp, kT)
+    assert isinstance(pt, sg.SystemParallelTempering)
+    if kind == "local":
+        for r in range(4):
+            assert pt.samplers[r].ΔE == pytest.approx(sg.energy(pt.systems[r]), rel=1e-12)
+    pt.step_ensemble(40, 5)
+    assert pt.n_exch.sum() == 4 * 1 + 4 * 2   # 8 rounds alternating between 1 and 2 pairs
+    assert sorted(pt.system_ids) == [0, 1, 2, 3]
+    if kind == "local":
+        # sampler bookkeeping follows the system now at its temperature (ParallelTempering.jl:64-66)
+        for rank in range(4):
+            s = pt.systems[pt.system_ids[rank]]
+            assert pt.samplers[rank].ΔE == pytest.approx(sg.energy(s), abs=1e-9 * s.nsites)
+            assert np.allclose(pt.samplers[rank].ΔS, sg.magnetization(s), atol=1e-9 * s.nsites)
+    assert pt.n_accept.sum() > 0
+    pt.close()

@@ -60,3 +60,30 @@ def test_proposal_mixture_rules(sg):
     assert s.nsweeps == 1.0 and s.propose is sg.propose_uniform and s.ΔE == 0.0
     c = s.copy()
     assert c.kT == 0.2 and c is not s
+
+
+def test_exchange_round_matches_oracle(sg, orc):
+    rng = np.random.default_rng(4)
+    for trial in range(20):
+        n = int(rng.integers(2, 9))
+        E_sys = rng.normal(-10.0, 3.0, n)
+        kT = np.sort(rng.uniform(0.1, 2.0, n))
+        ids = list(rng.permutation(n))
+        u = rng.random(n)
+        for start in (1, 2):
+            ref_ids, ref_acc = orc.replica_exchange(E_sys, kT, ids, start, u)
+            got_ids, tried, acc = sg.exchange_round([E_sys[i] for i in ids], kT, ids, start, lambda k: u[k])
+            assert got_ids == list(ref_ids)
+            assert np.array_equal(acc, ref_acc)
+            assert np.array_equal(tried, [(k >= start - 1 and (k - start + 1) % 2 == 0 and k < n - 1) for k in range(n)])
+
+
+def test_clone_system_copies_couplings_and_state(sg, orc):
+    s = rich_dipole(sg, device=None)
+    c = sg.clone_system(s, seed=99)
+    assert c.seed == 99 and c.dims == s.dims
+    S = s.dipoles_flat()
+    assert np.array_equal(c.dipoles_flat(), S)
+    assert orc.OracleSystem.from_system(c).energy(S) == orc.OracleSystem.from_system(s).energy(S)
+    c.set_state_flat(dipoles=-S)
+    assert np.array_equal(s.dipoles_flat(), S)
