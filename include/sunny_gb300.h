@@ -203,6 +203,15 @@ int sgb_local_colors(sgb_system* sys, int32_t* ncolors, int32_t* color);
  * energy change if the dipole at `site` (0-based, Sunny's linear order) became S_new. */
 int sgb_local_energy_change(sgb_system* sys, int64_t site, const double* S_new, double* dE);
 
+/* minimize_energy!(sys; maxiters, jitter) (Optimization.jl:102-166), dipole modes, FP64
+ * systems: perturb every spin by `jitter` (perturbed_spin with normals keyed by seed),
+ * then conjugate-gradient descent on the unit spheres until the largest gradient
+ * component is <= 1e-12 * characteristic_energy_scale or the largest step component is
+ * <= 1e-12. The state is left at the minimiser; converged/niters/energy_out (nullable)
+ * receive the MinimizationResult fields. */
+int sgb_minimize_energy(sgb_system* sys, int32_t maxiters, double jitter, uint64_t seed, int32_t* converged,
+                        int32_t* niters, double* energy_out);
+
 /* ---- SampledCorrelations --------------------------------------------------- */
 
 typedef struct {

@@ -749,6 +749,172 @@ int sgb_local_sweeps(sgb_system* s, double kT, double nsweeps, const sgb_proposa
     return SGB_OK;
 }
 
+// minimize_energy! (Optimization.jl:102-166), dipole modes, FP64 systems. Riemannian
+// nonlinear conjugate gradient on the unit spheres: Hager-Zhang β with the η = 0.4 lower
+// bound (Optim.jl ConjugateGradient defaults), a bracketing line search (secant on φ',
+// else bisection) on φ(α) = E(κ·normalize(x + α d)) that accepts the strong Wolfe
+// conditions, first step ψ0/|g|∞ (Hager & Zhang's I0 with |x|∞ = 1), then
+// α_prev·φ'_prev(0)/φ'(0), capped at αmax = 10. Converged when the largest projected-gradient component is at most
+// 1e-12·characteristic_energy_scale or the largest step component at most 1e-12
+// (Optimization.jl:149-156); on a failed line search the direction restarts from -g
+// once, as optimize_with_restarts does (Optimization.jl:59-70).
+int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t seed, int32_t* converged,
+                        int32_t* niters, double* energy_out) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    if (s->sun) return fail(s, SGB_ERR_ARG, "minimize_energy on the GPU supports the dipole modes");
+    if (s->fp32) return fail(s, SGB_ERR_ARG, "minimize_energy needs an FP64 system (its tolerances are 1e-12)");
+    if (maxiters < 0 || !(jitter >= 0)) return fail(s, SGB_ERR_ARG, "invalid maxiters or jitter");
+    int rc = ensure_tables(s);
+    if (rc) return rc;
+    if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called first");
+    const int ns = s->ns;
+    const int grid = opt_grid(ns);
+    double *x = nullptr, *g = nullptr, *d = nullptr, *grad = nullptr, *part = nullptr;
+    struct Guard {
+        double** p[5];
+        ~Guard() { for (auto q : p) if (*q) { cudaFree(*q); *q = nullptr; } }
+    } guard{{&x, &g, &d, &grad, &part}};
+    const size_t vb = sizeof(double) * 3 * (size_t)ns;
+    if ((rc = dmalloc(s, (void**)&x, vb)) || (rc = dmalloc(s, (void**)&g, vb)) || (rc = dmalloc(s, (void**)&d, vb)) ||
+        (rc = dmalloc(s, (void**)&grad, vb)) || (rc = dmalloc(s, (void**)&part, sizeof(double) * 10 * grid)))
+        return rc;
+    double* S = (double*)s->S;
+    const double* kap = (const double*)s->kappa;
+    cudaStream_t st = s->stream;
+    CK(cudaMemsetAsync(g, 0, vb, st));
+    CK(cudaMemsetAsync(d, 0, vb, st));
+    if (opt_launch_init(S, kap, ns, jitter, seed, x, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
+    const int nbE = std::min(SGB_ENERGY_BLOCKS, (ns + SGB_BLOCK - 1) / SGB_BLOCK);
+    std::vector<double> hp(10 * (size_t)grid);
+    auto pull = [&](int K, double* out, const bool* is_max) -> int {
+        CK(cudaMemcpyAsync(hp.data(), part, sizeof(double) * K * grid, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int k = 0; k < K; k++) {
+            double a = 0;
+            for (int b = 0; b < grid; b++) a = is_max[k] ? std::max(a, hp[(size_t)b * K + k]) : a + hp[(size_t)b * K + k];
+            out[k] = a;
+        }
+        return SGB_OK;
+    };
+    int nevals = 0;
+    // E and φ'(α) at κ·normalize(x + α d); the gradient stays in `grad`
+    auto eval = [&](double alpha, double* f, double* dphi) -> int {
+        nevals++;
+        if (opt_launch_point(x, d, alpha, kap, ns, S, st) || dip_launch_grad<double>(s->md, S, grad, st) ||
+            dip_launch_energy<double>(s->md, S, s->partials, nbE, st) || util_launch_reduce(s->partials, nbE, 4, s->red, st))
+            return cuda_fail(s, cudaGetLastError(), "optimizer evaluation");
+        s->launches += 4;
+        if (dphi) {
+            if (opt_launch_dphi(x, d, alpha, grad, kap, ns, part, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
+            s->launches++;
+        }
+        CK(cudaMemcpyAsync(f, s->red, sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (dphi) {
+            const bool mx[1] = {false};
+            return pull(1, dphi, mx);
+        }
+        CK(cudaStreamSynchronize(st));
+        return SGB_OK;
+    };
+    const bool acc_max[10] = {false, false, false, false, false, false, false, true, true, false};
+    auto accept = [&](double alpha, double* v) -> int {
+        if (opt_launch_accept(x, d, alpha, grad, kap, ns, g, part, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
+        s->launches++;
+        return pull(10, v, acc_max);
+    };
+    const bool dir_max[2] = {false, true};
+    auto direction = [&](double beta, double* v) -> int {
+        if (opt_launch_dir(g, d, beta, ns, part, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
+        s->launches++;
+        return pull(2, v, dir_max);
+    };
+    double f = 0, v[10], w[2];
+    if ((rc = eval(0.0, &f, nullptr)) || (rc = accept(0.0, v))) return rc;
+    const double g_abstol = 1e-12 * std::sqrt(v[9]) / std::sqrt((double)ns);   // characteristic_energy_scale
+    const double x_abstol = 1e-12;
+    bool conv = v[7] <= g_abstol;
+    int iters = 0;
+    if (!conv && (rc = direction(0.0, w))) return rc;
+    double alpha_prev = 0, dphi_prev = 0, gmax = v[7];
+    bool restarted = false;
+    while (!conv && iters < maxiters) {
+        const double phi0 = f, dphi0 = w[0];
+        // strong Wolfe with σ = 0.1 (near-exact steps, which CG needs); sufficient decrease
+        // is relaxed to the FP64 noise level of E once E no longer changes measurably
+        const double eps = 1e-12 * std::fabs(phi0), sig = 0.1, del = 1e-4, amax = 10.0;
+        auto wolfe = [&](double a, double fa, double da) {
+            return std::fabs(da) <= -sig * dphi0 && (fa <= phi0 + del * a * dphi0 || fa <= phi0 + eps);
+        };
+        double a = alpha_prev == 0 ? 0.01 / gmax : alpha_prev * dphi_prev / dphi0;   // N&W (3.60)
+        a = std::min(a, amax);
+        double lo = 0, flo = phi0, dlo = dphi0, hi = -1, fhi = 0, dhi = 0;
+        double acc_a = -1, acc_f = 0;
+        for (int k = 0; k < 60 && acc_a < 0; k++) {
+            double fa, da;
+            if ((rc = eval(a, &fa, &da))) return rc;
+            if (!std::isfinite(fa) || !std::isfinite(da)) {
+                hi = a; fhi = INFINITY; dhi = INFINITY;
+            } else if (wolfe(a, fa, da)) {
+                acc_a = a; acc_f = fa;
+                break;
+            } else if (da >= 0 || (fa > phi0 + eps && fa > phi0 + del * a * dphi0) || (hi < 0 && fa > flo + eps)) {
+                hi = a; fhi = fa; dhi = da;
+            } else {
+                lo = a; flo = fa; dlo = da;
+            }
+            if (hi < 0) {                       // still descending: expand
+                if (a >= amax) break;
+                a = std::min(5.0 * a, amax);
+                continue;
+            }
+            // next trial inside (lo, hi): secant on φ', else bisection
+            const double wdt = hi - lo;
+            if (std::fabs(wdt) <= 1e-15 * std::max(1.0, std::fabs(lo))) break;
+            double t = 0.5 * (lo + hi);
+            if (std::isfinite(dhi) && dhi > dlo) {
+                const double sec = lo - dlo * (hi - lo) / (dhi - dlo);
+                if (sec > lo + 0.05 * wdt && sec < hi - 0.05 * wdt) t = sec;
+            }
+            a = t;
+        }
+        (void)fhi;
+        if (acc_a < 0) {
+            if (restarted) break;                // second failure in a row: give up
+            restarted = true;
+            if ((rc = eval(0.0, &f, nullptr)) || (rc = accept(0.0, v)) || (rc = direction(0.0, w))) return rc;
+            alpha_prev = 0;
+            continue;
+        }
+        restarted = false;
+        if (acc_a != a) { double fa, da; if ((rc = eval(acc_a, &fa, &da))) return rc; }
+        if ((rc = accept(acc_a, v))) return rc;
+        iters++;
+        f = acc_f;
+        gmax = v[7];
+        if (v[7] <= g_abstol || v[8] <= x_abstol) { conv = true; break; }
+        // Hager-Zhang β with the η lower bound (vectors already transported)
+        double beta = 0;
+        if (v[0] != 0) {
+            beta = (v[2] - 2.0 * v[1] * v[3] / v[0]) / v[0];
+            const double eta = -1.0 / (std::sqrt(v[4]) * std::min(0.4, std::sqrt(v[5])));
+            beta = std::max(beta, eta);
+        }
+        if ((rc = direction(beta, w))) return rc;
+        if (!(w[0] < 0) && (rc = direction(0.0, w))) return rc;   // not a descent direction: restart
+        alpha_prev = acc_a;
+        dphi_prev = dphi0;
+    }
+    if (opt_launch_point(x, d, 0.0, kap, ns, S, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
+    s->launches++;
+    double E = f;
+    if ((rc = eval(0.0, &E, nullptr))) return rc;
+    CK(cudaStreamSynchronize(st));
+    if (converged) *converged = conv ? 1 : 0;
+    if (niters) *niters = iters;
+    if (energy_out) *energy_out = E;
+    return SGB_OK;
+}
+
 int sgb_local_colors(sgb_system* s, int32_t* ncolors, int32_t* color) {
     if (!s || !ncolors) return fail(s, SGB_ERR_ARG, "null argument");
     int rc = ensure_colors(s);

@@ -110,6 +110,17 @@ template <class R>
 int mc_launch_local_dE(const Model<R>& M, const R* S, int site, double nx, double ny, double nz, double* out,
                        cudaStream_t st);
 
+// ---- minimize_energy! vector kernels (sgb_opt.cu), FP64 dipole state ----
+int opt_grid(int ns);   // blocks of every partial-writing kernel below
+int opt_launch_init(double* S, const double* kappa, int ns, double jitter, uint64_t seed, double* x, cudaStream_t st);
+int opt_launch_point(const double* x, const double* d, double alpha, const double* kappa, int ns, double* S,
+                     cudaStream_t st);
+int opt_launch_dphi(const double* x, const double* d, double alpha, const double* grad, const double* kappa, int ns,
+                    double* part, cudaStream_t st);
+int opt_launch_accept(double* x, double* d, double alpha, const double* grad, const double* kappa, int ns, double* g,
+                      double* part, cudaStream_t st);
+int opt_launch_dir(const double* g, double* d, double beta, int ns, double* part, cudaStream_t st);
+
 // ---- shared utilities (sgb_dipole.cu) ----
 int util_launch_reduce(const double* partials, int n, int ncomp, double* out, cudaStream_t st);
 template <class R>

@@ -632,6 +632,33 @@ def _local_sampler_steps(sys: System, sampler: LocalSampler, nsteps: int, rand) 
     return 0
 
 
+@dataclass
+class MinimizationResult:
+    """MinimizationResult (Optimization.jl:1-10): converged, niters, energy."""
+    converged: bool
+    niters: int
+    energy: float
+
+
+def minimize_energy(sys: System, maxiters: int = 1000, jitter: float = 1e-8) -> MinimizationResult:
+    """minimize_energy!(sys; maxiters=1000, jitter=1e-8) (Optimization.jl:102-166), dipole
+    modes, FP64 systems: conjugate-gradient descent on the unit spheres on the device.
+    Warns when it does not converge, as the reference does."""
+    sys._sync_to_device()
+    conv, nit, E = C.c_int32(), C.c_int32(), C.c_double()
+    seed = (sys.seed * 1000003 + sys.mc_sweep + 17) % (1 << 63)
+    rc = sys._lib.sgb_minimize_energy(sys._h, int(maxiters), float(jitter), seed, C.byref(conv), C.byref(nit),
+                                      C.byref(E))
+    sys._dev_newer = True
+    _abi.check(rc, sys._lib, sys._h)
+    sys.mc_sweep += 1
+    res = MinimizationResult(bool(conv.value), int(nit.value), float(E.value))
+    if not res.converged:
+        import warnings
+        warnings.warn(f"Non-converged after {res.niters} iterations")
+    return res
+
+
 def local_energy_change(sys: System, site: int, S_new) -> float:
     """local_energy_change(sys, site, state) (Interactions.jl:311-373), dipole modes;
     `site` is the 0-based linear index."""
