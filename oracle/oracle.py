@@ -63,6 +63,7 @@ def load() -> C.CDLL:
             "or_langevin_replicas": (C.c_int, [P, C.c_int, _D, _D, C.c_double, C.c_double, C.c_int, C.c_uint64]),
             "or_expected_spin": (None, [C.c_int, _D, _D]),
             "or_local_energy_change": (C.c_double, [P, _D, C.c_int64, _D]),
+            "or_ewald_matrices": (None, [C.c_int, C.c_int, C.c_int, C.c_int, _D, _D, _D, C.c_double, _D]),
             "or_local_sweeps": (None, [P, _D, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_int), C.c_int,
                                        C.POINTER(C.c_int), _D, _D, _D, _D, _D]),
         }
@@ -319,6 +320,41 @@ def replica_exchange(E, kT, system_ids, exch_start, uniforms):
             ids[i1], ids[i2] = ids[i2], ids[i1]
             acc[i1] = True
     return ids, acc
+
+
+# ---- dipole-dipole (Ewald.jl) in pairwise form ------------------------------------------
+
+def ewald_matrices(dims, latvecs, positions, demag, mu0_muB2):
+    """A[cell, i, j] (3x3, [row, col]) of precompute_dipole_ewald (Ewald.jl:40-146), from the
+    C restatement; cell = c1 + L1*(c2 + L2*c3) is the offset of atom j's cell."""
+    lib = load()
+    L1, L2, L3 = dims
+    na = len(positions)
+    out = np.zeros(L1 * L2 * L3 * na * na * 9)
+    lat = np.ascontiguousarray(np.asarray(latvecs, dtype=float).T.reshape(-1))
+    pos = np.ascontiguousarray(np.asarray(positions, dtype=float).reshape(-1))
+    dm = np.ascontiguousarray(np.asarray(demag, dtype=float).T.reshape(-1))
+    lib.or_ewald_matrices(L1, L2, L3, na, _p(lat), _p(pos), _p(dm), float(mu0_muB2), _p(out))
+    return out.reshape(L1 * L2 * L3, na, na, 3, 3).transpose(0, 1, 2, 4, 3)
+
+
+def ewald_pairwise_grad(A, dims, na, S, g):
+    """dE/dS of the dipole-dipole energy as a sum over pairs (Ewald.jl:210-228):
+    ∇E_1 = Σ_2 g_1ᵀ A[cell_2 - cell_1, i_1, i_2] g_2 S_2. S: [ns][3]; g: [ns][3][3]."""
+    L1, L2, L3 = dims
+    ncell = L1 * L2 * L3
+    ns = ncell * na
+    cells = np.arange(ns) % ncell
+    atoms = np.arange(ns) // ncell
+    c = np.stack([cells % L1, (cells // L1) % L2, cells // (L1 * L2)], 1)
+    mu = np.einsum("sab,sb->sa", g, S)
+    grad = np.zeros((ns, 3))
+    for s1 in range(ns):
+        off = (c - c[s1]) % np.array(dims)
+        oi = off[:, 0] + L1 * (off[:, 1] + L2 * off[:, 2])
+        phi = np.einsum("sab,sb->a", A[oi, atoms[s1], atoms], mu)
+        grad[s1] = g[s1].T @ phi
+    return grad
 
 
 # ---- S(q,w) loss of one sample, for finite-difference reference gradients -----------------

@@ -601,6 +601,91 @@ void or_local_sweeps(const or_sys* s, double* S, double kT, int nsweeps, double 
     if (dS3) { dS3[0] = aS[0]; dS3[1] = aS[1]; dS3[2] = aS[2]; }
 }
 
+/* ---- Ewald.jl:40-146: real-space and reciprocal sums of the dipole kernel ---------- */
+static const double OR_PI = 3.14159265358979323846;
+
+static void mat3_mul_vec(const double* M, const double* v, double* out) {   /* M column-major */
+    for (int r = 0; r < 3; r++) out[r] = M[r] * v[0] + M[r + 3] * v[1] + M[r + 6] * v[2];
+}
+
+void or_ewald_matrices(int L1, int L2, int L3, int na, const double* latvecs, const double* positions,
+                       const double* demag, double mu0_muB2, double* out) {
+    const int L[3] = {L1, L2, L3};
+    double sup[9], rec[9];   /* supercell vectors and their reciprocals (columns) */
+    for (int c = 0; c < 3; c++)
+        for (int r = 0; r < 3; r++) sup[r + 3 * c] = latvecs[r + 3 * c] * L[c];
+    const double* a = sup;
+    double det = a[0] * (a[4] * a[8] - a[7] * a[5]) - a[3] * (a[1] * a[8] - a[7] * a[2]) + a[6] * (a[1] * a[5] - a[4] * a[2]);
+    /* rec = 2π (sup^-1)^T: columns b_k with a_i·b_k = 2π δ_ik */
+    double inv[9];
+    inv[0] = (a[4] * a[8] - a[7] * a[5]) / det; inv[3] = (a[6] * a[5] - a[3] * a[8]) / det; inv[6] = (a[3] * a[7] - a[6] * a[4]) / det;
+    inv[1] = (a[7] * a[2] - a[1] * a[8]) / det; inv[4] = (a[0] * a[8] - a[6] * a[2]) / det; inv[7] = (a[6] * a[1] - a[0] * a[7]) / det;
+    inv[2] = (a[1] * a[5] - a[4] * a[2]) / det; inv[5] = (a[3] * a[2] - a[0] * a[5]) / det; inv[8] = (a[0] * a[4] - a[3] * a[1]) / det;
+    for (int c = 0; c < 3; c++)
+        for (int r = 0; r < 3; r++) rec[r + 3 * c] = 2 * OR_PI * inv[c + 3 * r];
+    const double V = fabs(det), Lc = cbrt(V);
+    const double sig = Lc / 3, sig2 = sig * sig, sig3 = sig2 * sig;
+    const double rmax = 6 * sqrt(2.0) * sig, kmax = 6 * sqrt(2.0) / sig;
+    int nmax[3], mmax[3];
+    for (int k = 0; k < 3; k++) {
+        const double* ak = sup + 3 * k;
+        const double* bk = rec + 3 * k;
+        double nb = sqrt(bk[0] * bk[0] + bk[1] * bk[1] + bk[2] * bk[2]);
+        double na_ = sqrt(ak[0] * ak[0] + ak[1] * ak[1] + ak[2] * ak[2]);
+        double ab = (ak[0] * bk[0] + ak[1] * bk[1] + ak[2] * bk[2]);
+        nmax[k] = (int)lround(rmax / (ab / nb) + 1e-6) + 1;
+        mmax[k] = (int)lround(kmax / (ab / na_) + 1e-6);
+    }
+    const int ncell = L1 * L2 * L3;
+    for (int i = 0; i < na; i++)
+        for (int j = 0; j < na; j++)
+            for (int c3 = 0; c3 < L3; c3++)
+                for (int c2 = 0; c2 < L2; c2++)
+                    for (int c1 = 0; c1 < L1; c1++) {
+                        double acc[9] = {0};
+                        double fr[3] = {c1 + positions[3 * j] - positions[3 * i], c2 + positions[3 * j + 1] - positions[3 * i + 1],
+                                        c3 + positions[3 * j + 2] - positions[3 * i + 2]};
+                        double dr[3];
+                        mat3_mul_vec(latvecs, fr, dr);
+                        for (int n1 = -nmax[0]; n1 <= nmax[0]; n1++)
+                            for (int n2 = -nmax[1]; n2 <= nmax[1]; n2++)
+                                for (int n3 = -nmax[2]; n3 <= nmax[2]; n3++) {
+                                    double nn[3] = {n1, n2, n3}, sh[3];
+                                    mat3_mul_vec(sup, nn, sh);
+                                    double rv[3] = {dr[0] + sh[0], dr[1] + sh[1], dr[2] + sh[2]};
+                                    double r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+                                    if (!(r2 > 0 && r2 <= rmax * rmax)) continue;
+                                    double r = sqrt(r2), r3 = r2 * r;
+                                    double ec = erfc(r / (sqrt(2.0) * sig));
+                                    double ga = sqrt(2 / OR_PI) * (r / sig) * exp(-r2 / (2 * sig2));
+                                    double c_iso = (ec + ga) / r3 / (4 * OR_PI);
+                                    double c_rr = 3 * (ec + (1 + r2 / (3 * sig2)) * ga) / r3 / (4 * OR_PI) / r2;
+                                    for (int q = 0; q < 3; q++)
+                                        for (int p = 0; p < 3; p++) acc[p + 3 * q] += (p == q ? c_iso : 0) - c_rr * rv[p] * rv[q];
+                                }
+                        for (int m1 = -mmax[0]; m1 <= mmax[0]; m1++)
+                            for (int m2 = -mmax[1]; m2 <= mmax[1]; m2++)
+                                for (int m3 = -mmax[2]; m3 <= mmax[2]; m3++) {
+                                    double mm[3] = {m1, m2, m3}, k[3];
+                                    mat3_mul_vec(rec, mm, k);
+                                    double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+                                    if (k2 <= 1e-16) {
+                                        for (int q = 0; q < 9; q++) acc[q] += demag[q] / V;   /* surface term */
+                                    } else if (k2 <= kmax * kmax) {
+                                        double w = cos(k[0] * dr[0] + k[1] * dr[1] + k[2] * dr[2]) * exp(-sig2 * k2 / 2) / k2 / V;
+                                        for (int q = 0; q < 3; q++)
+                                            for (int p = 0; p < 3; p++) acc[p + 3 * q] += w * k[p] * k[q];
+                                    }
+                                }
+                        if (dr[0] == 0 && dr[1] == 0 && dr[2] == 0)
+                            for (int q = 0; q < 3; q++) acc[q + 3 * q] -= 1.0 / (3 * pow(2 * OR_PI, 1.5) * sig3);
+                        int cell = c1 + L1 * (c2 + L2 * c3);
+                        double* o = out + (((size_t)cell * na + i) * na + j) * 9;
+                        for (int q = 0; q < 9; q++) o[q] = acc[q] * mu0_muB2;
+                    }
+    (void)ncell;
+}
+
 /* ---- Integrators.jl:266-275 rhs_dipole! for one site ------------------------------- */
 static inline void rhs_dipole(const double* S, const double* xi, const double* g, double dt, double lam, double* dS) {
     double v[3];

@@ -88,6 +88,13 @@ void or_local_sweeps(const or_sys* s, double* S, double kT, int nsweeps, double 
                      int nkind, const int* kind, const double* cum, const double* mag, const double* rand,
                      double* dE, double* dS3);
 
+/* Dipole-dipole Ewald matrices (Ewald.jl:40-146 precompute_dipole_ewald at q = 0):
+ * A[cell][i][j] (3x3 column-major, cell = c1 + L1*(c2 + L2*c3) is the offset of atom j's
+ * cell from atom i's), times mu0_muB2. latvecs: 3x3 column-major lattice vectors of the
+ * unit cell; positions: [na][3] fractional; demag: 3x3 column-major. out: ncell*na*na*9. */
+void or_ewald_matrices(int L1, int L2, int L3, int na, const double* latvecs, const double* positions,
+                       const double* demag, double mu0_muB2, double* out);
+
 /* Independent replicas stepped on a thread pool (OpenMP when compiled with it):
  * replica r has state S + r*ns*3 and temperature kT[r]; noise from the caller per
  * replica is not supported, the CPU path uses its own Gaussian source seeded by

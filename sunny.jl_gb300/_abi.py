@@ -79,6 +79,7 @@ SIGNATURES = {
     "sgb_local_sweeps": (C.c_int, [_P, C.c_double, C.c_double, C.POINTER(Proposal), _U64, _U64, _D, _D, _D]),
     "sgb_local_colors": (C.c_int, [_P, C.POINTER(_I32), C.POINTER(_I32)]),
     "sgb_local_energy_change": (C.c_int, [_P, _I64, _D, _D]),
+    "sgb_set_dipole_dipole": (C.c_int, [_P, C.c_double, _D, _D, _D]),
     "sgb_minimize_energy": (C.c_int, [_P, _I32, C.c_double, _U64, C.POINTER(_I32), C.POINTER(_I32), _D]),
     "sgb_corr_create": (C.c_int, [_P, C.POINTER(CorrDesc), C.POINTER(_P)]),
     "sgb_corr_destroy": (None, [_P]),

@@ -17,7 +17,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libsunnygb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["sgb_api.cu", "sgb_dipole.cu", "sgb_sun.cu", "sgb_corr.cu", "sgb_batch.cu", "sgb_static.cu", "sgb_adjoint.cu", "sgb_mc.cu", "sgb_opt.cu"]
+SOURCES = ["sgb_api.cu", "sgb_dipole.cu", "sgb_sun.cu", "sgb_corr.cu", "sgb_batch.cu", "sgb_static.cu", "sgb_adjoint.cu", "sgb_mc.cu", "sgb_opt.cu", "sgb_ewald.cu"]
 
 
 def nvcc() -> str:

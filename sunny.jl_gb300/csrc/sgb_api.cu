@@ -270,6 +270,144 @@ int do_refresh(sgb_system* s) {
     return rc ? cuda_fail(s, cudaGetLastError(), "refresh launch") : SGB_OK;
 }
 
+void ewald_free(sgb_system* s) {
+    EwaldDev& E = s->ew;
+    void* p;
+    p = E.g; dfree(p); p = E.mu; dfree(p); p = E.phi; dfree(p);
+    p = E.FA; dfree(p); p = E.Fmu; dfree(p); p = E.Fphi; dfree(p);
+    p = s->ew_part; dfree(p);
+    if (E.have_f) cufftDestroy(E.plan_f);
+    if (E.have_b) cufftDestroy(E.plan_b);
+    E = EwaldDev{};
+    s->ew_part = nullptr;
+    s->ewald_on = false;
+}
+
+// Adds the dipole-dipole gradient at state S (device, R) into grad ([ns][3] FP64 on the
+// device, may be null); *E (nullable) receives the dipole-dipole energy.
+template <class R>
+int ewald_add(sgb_system* s, const R* S, double* grad, double* E) {
+    if (!s->ewald_on) {
+        if (E) *E = 0;
+        return SGB_OK;
+    }
+    if (ewald_apply<R>(s->ew, S, grad, E ? s->ew_part : nullptr, s->stream)) return cuda_fail(s, cudaGetLastError(), "dipole-dipole launch");
+    s->launches += 4;
+    if (E) {
+        double hp[EWALD_PART_BLOCKS];
+        CK(cudaMemcpyAsync(hp, s->ew_part, sizeof(hp), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        double t = 0;
+        for (int b = 0; b < EWALD_PART_BLOCKS; b++) t += hp[b];
+        *E = t;
+    }
+    return SGB_OK;
+}
+
+int ewald_upload_g(sgb_system* s) {
+    if (!s->ewald_on) return SGB_OK;
+    CK(cudaMemcpy(s->ew.g, s->g_h.data(), sizeof(double) * 9 * (size_t)s->ns, cudaMemcpyHostToDevice));
+    return SGB_OK;
+}
+
+// Step loops for systems with dipole-dipole interactions: every gradient needs the
+// transform over the whole lattice, so each integrator stage is its own launch (local
+// gradient, Ewald gradient, stage update) instead of one persistent launch.
+int ensure_lr_grad(sgb_system* s, double** grad) {
+    if ((size_t)s->lr_grad_cap < 3 * (size_t)s->ns) {
+        void* p = s->lr_grad;
+        dfree(p);
+        s->lr_grad = nullptr;
+        s->lr_grad_cap = 0;
+        int rc = dmalloc(s, (void**)&s->lr_grad, sizeof(double) * 3 * (size_t)s->ns);
+        if (rc) return rc;
+        s->lr_grad_cap = 3 * s->ns;
+    }
+    *grad = s->lr_grad;
+    return SGB_OK;
+}
+
+template <class R>
+int lr_gradient(sgb_system* s, const R* X, double* grad) {
+    if (dip_launch_grad<R>(model<R>(s), X, grad, s->stream)) return cuda_fail(s, cudaGetLastError(), "gradient launch");
+    s->launches++;
+    return ewald_add<R>(s, X, grad, nullptr);
+}
+
+template <class R>
+int run_langevin_lr(sgb_system* s, double dt, double damping, double kT, uint64_t seed, uint64_t step0, int nsteps,
+                    const double* noise) {
+    double* grad;
+    int rc = ensure_lr_grad(s, &grad);
+    if (rc) return rc;
+    const int ns = s->ns;
+    const double nscale = (damping == 0.0 || kT == 0.0) ? 0.0 : std::sqrt(2 * dt * damping * kT);
+    if (noise && (rc = ensure_dbuf(s, 3 * (size_t)ns))) return rc;
+    R* S = (R*)s->S;
+    R* P = (R*)s->P;
+    R* D1 = (R*)s->H;
+    R* XI = D1 + 3 * (size_t)ns;
+    const R* kap = (const R*)s->kappa;
+    for (int k = 0; k < nsteps; k++) {
+        const double* dn = nullptr;
+        if (noise) {
+            CK(cudaMemcpyAsync(s->dbuf, noise + 3 * (size_t)ns * k, sizeof(double) * 3 * ns, cudaMemcpyHostToDevice, s->stream));
+            dn = s->dbuf;
+        }
+        if ((rc = lr_gradient<R>(s, S, grad))) return rc;
+        if (lr_heun_a<R>(S, grad, P, D1, XI, kap, ns, dt, damping, nscale, seed, step0 + k, dn, s->stream))
+            return cuda_fail(s, cudaGetLastError(), "Langevin stage launch");
+        if ((rc = lr_gradient<R>(s, P, grad))) return rc;
+        if (lr_heun_b<R>(S, P, grad, D1, XI, kap, ns, dt, damping, s->stream)) return cuda_fail(s, cudaGetLastError(), "Langevin stage launch");
+        s->launches += 2;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return SGB_OK;
+}
+
+template <class R>
+int run_midpoint_lr(sgb_system* s, double dt, double damping, double tol, int max_iters, int nsteps, int64_t* iters) {
+    double* grad;
+    int rc = ensure_lr_grad(s, &grad);
+    if (rc) return rc;
+    const int ns = s->ns;
+    const double atol = tol * std::sqrt((double)ns);
+    R* S = (R*)s->S;
+    R* H = (R*)s->H;
+    R* Sp = H + 3 * (size_t)ns;
+    const R* kap = (const R*)s->kappa;
+    int64_t total = 0;
+    double hp[EWALD_PART_BLOCKS];
+    for (int k = 0; k < nsteps; k++) {
+        CK(cudaMemcpyAsync(Sp, S, sizeof(R) * 3 * ns, cudaMemcpyDeviceToDevice, s->stream));   // S' = S
+        bool conv = false;
+        for (int it = 0; it < max_iters; it++) {
+            total++;
+            if (lr_mid_half<R>(S, Sp, H, kap, ns, s->stream)) return cuda_fail(s, cudaGetLastError(), "midpoint stage launch");
+            if ((rc = lr_gradient<R>(s, H, grad))) return rc;
+            if (lr_mid_update<R>(S, H, grad, Sp, ns, dt, damping, s->partials, s->stream))
+                return cuda_fail(s, cudaGetLastError(), "midpoint stage launch");
+            s->launches += 2;
+            CK(cudaMemcpyAsync(hp, s->partials, sizeof(hp), cudaMemcpyDeviceToHost, s->stream));
+            CK(cudaStreamSynchronize(s->stream));
+            double acc = 0;
+            for (int b = 0; b < EWALD_PART_BLOCKS; b++) acc += hp[b];
+            if (acc <= atol * atol) {   // fast_isapprox (Integrators.jl:361-371)
+                if (lr_mid_accept<R>(S, Sp, kap, ns, s->stream)) return cuda_fail(s, cudaGetLastError(), "midpoint stage launch");
+                s->launches++;
+                conv = true;
+                break;
+            }
+        }
+        if (iters) *iters = total;
+        if (!conv)
+            return fail(s, SGB_ERR_NOCONVERGE, "Spherical midpoint method failed to converge to tolerance " + fmt_g(tol) +
+                                                   " after " + std::to_string(max_iters) + " iterations.");
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return SGB_OK;
+}
+
 // Greedy colouring of the bond graph in site order (every bond is listed from both
 // ends, so a site's own list holds all its neighbours): class of a site = the smallest
 // class none of its already coloured neighbours has. Sites of one class share no
@@ -454,6 +592,8 @@ void sgb_destroy(sgb_system* s) {
     p = s->dbuf; dfree(p);
     p = s->mc_perm; dfree(p);
     p = s->mc_part; dfree(p);
+    ewald_free(s);
+    p = s->lr_grad; dfree(p);
     dfree(s->flush);
     if (s->stage) cudaFreeHost(s->stage);
     for (int i = 0; i < 8; i++) if (s->ev[i]) cudaEventDestroy(s->ev[i]);
@@ -494,7 +634,7 @@ int sgb_set_sites(sgb_system* s, const double* kappa, const double* g, const dou
     }
     s->sites_set = true;
     s->tables_dirty = true;
-    return SGB_OK;
+    return ewald_upload_g(s);
 }
 
 int sgb_set_onsite(sgb_system* s, int32_t atom, const double* coeffs) {
@@ -532,6 +672,93 @@ int sgb_set_bonds(sgb_system* s, const sgb_bond* bonds, int32_t nbonds) {
     s->bonds_h.assign(bonds, bonds + nbonds);
     s->bonds_set = true;
     s->tables_dirty = true;
+    return SGB_OK;
+}
+
+int sgb_set_dipole_dipole(sgb_system* s, double mu0_muB2, const double* demag, const double* latvecs,
+                          const double* positions) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    ewald_free(s);
+    if (mu0_muB2 == 0.0) return SGB_OK;
+    if (!demag || !latvecs || !positions) return fail(s, SGB_ERR_ARG, "demag, latvecs and positions are required");
+    if (s->sun) return fail(s, SGB_ERR_ARG, "dipole-dipole interactions on the GPU support the dipole modes");
+    if (!s->sites_set) return fail(s, SGB_ERR_STATE, "sgb_set_sites must be called before sgb_set_dipole_dipole");
+    EwaldGeom G{};
+    const int* L = s->d.dims;
+    G.L[0] = L[0]; G.L[1] = L[1]; G.L[2] = L[2];
+    G.na = s->d.natoms;
+    G.mu0 = mu0_muB2;
+    for (int q = 0; q < 9; q++) { G.lat[q] = latvecs[q]; G.demag[q] = demag[q]; }
+    // supercell vectors and reciprocals (Ewald.jl:65-67), σ = V^(1/3)/3, cut-offs 6√2σ and
+    // 6√2/σ, image ranges (Ewald.jl:70-89)
+    for (int c = 0; c < 3; c++)
+        for (int r = 0; r < 3; r++) G.sup[r + 3 * c] = latvecs[r + 3 * c] * L[c];
+    const double* a = G.sup;
+    const double det = a[0] * (a[4] * a[8] - a[7] * a[5]) - a[3] * (a[1] * a[8] - a[7] * a[2]) + a[6] * (a[1] * a[5] - a[4] * a[2]);
+    if (!(std::fabs(det) > 0)) return fail(s, SGB_ERR_ARG, "lattice vectors are degenerate");
+    double inv[9];
+    inv[0] = (a[4] * a[8] - a[7] * a[5]) / det; inv[3] = (a[6] * a[5] - a[3] * a[8]) / det; inv[6] = (a[3] * a[7] - a[6] * a[4]) / det;
+    inv[1] = (a[7] * a[2] - a[1] * a[8]) / det; inv[4] = (a[0] * a[8] - a[6] * a[2]) / det; inv[7] = (a[6] * a[1] - a[0] * a[7]) / det;
+    inv[2] = (a[1] * a[5] - a[4] * a[2]) / det; inv[5] = (a[3] * a[2] - a[0] * a[5]) / det; inv[8] = (a[0] * a[4] - a[3] * a[1]) / det;
+    const double twopi = 6.283185307179586476925;
+    for (int c = 0; c < 3; c++)
+        for (int r = 0; r < 3; r++) G.rec[r + 3 * c] = twopi * inv[c + 3 * r];
+    G.V = std::fabs(det);
+    G.sig = std::cbrt(G.V) / 3;
+    G.rmax = 6 * std::sqrt(2.0) * G.sig;
+    G.kmax = 6 * std::sqrt(2.0) / G.sig;
+    for (int k = 0; k < 3; k++) {
+        const double* ak = G.sup + 3 * k;
+        const double* bk = G.rec + 3 * k;
+        const double nb = std::sqrt(bk[0] * bk[0] + bk[1] * bk[1] + bk[2] * bk[2]);
+        const double nak = std::sqrt(ak[0] * ak[0] + ak[1] * ak[1] + ak[2] * ak[2]);
+        const double ab = ak[0] * bk[0] + ak[1] * bk[1] + ak[2] * bk[2];
+        G.nmax[k] = (int)std::lround(G.rmax / (ab / nb) + 1e-6) + 1;
+        G.mmax[k] = (int)std::lround(G.kmax / (ab / nak) + 1e-6);
+    }
+    EwaldDev& E = s->ew;
+    E.L[0] = L[0]; E.L[1] = L[1]; E.L[2] = L[2];
+    E.na = G.na;
+    const int ncell = s->ncell, na = G.na;
+    E.nm = L[2] * L[1] * (L[0] / 2 + 1);
+    const size_t ncomp = (size_t)9 * na * na;
+    double* A = nullptr;
+    double* pos_d = nullptr;
+    int rc;
+    if ((rc = dmalloc(s, (void**)&E.g, sizeof(double) * 9 * (size_t)s->ns)) || (rc = dmalloc(s, (void**)&E.mu, sizeof(double) * 3 * (size_t)s->ns)) ||
+        (rc = dmalloc(s, (void**)&E.phi, sizeof(double) * 3 * (size_t)s->ns)) ||
+        (rc = dmalloc(s, (void**)&E.FA, sizeof(cufftDoubleComplex) * ncomp * E.nm)) ||
+        (rc = dmalloc(s, (void**)&E.Fmu, sizeof(cufftDoubleComplex) * 3 * na * (size_t)E.nm)) ||
+        (rc = dmalloc(s, (void**)&E.Fphi, sizeof(cufftDoubleComplex) * 3 * na * (size_t)E.nm)) ||
+        (rc = dmalloc(s, (void**)&s->ew_part, sizeof(double) * EWALD_PART_BLOCKS)) ||
+        (rc = dmalloc(s, (void**)&A, sizeof(double) * ncomp * ncell)) || (rc = dmalloc(s, (void**)&pos_d, sizeof(double) * 3 * na))) {
+        void* p = A; dfree(p); p = pos_d; dfree(p);
+        ewald_free(s);
+        return rc;
+    }
+    s->ewald_on = true;
+    auto bail = [&](const char* what) {
+        void* p = A; dfree(p); p = pos_d; dfree(p);
+        ewald_free(s);
+        return fail(s, SGB_ERR_CUDA, what);
+    };
+    if (cudaMemcpy(pos_d, positions, sizeof(double) * 3 * na, cudaMemcpyHostToDevice) != cudaSuccess) return bail("position upload failed");
+    if (ewald_upload_g(s)) return bail("g upload failed");
+    if (ewald_precompute(G, pos_d, A, s->stream)) return bail("Ewald matrix launch failed");
+    s->launches++;
+    int n[3] = {L[2], L[1], L[0]};
+    cufftHandle pa;
+    if (cufftPlanMany(&pa, 3, n, nullptr, 1, ncell, nullptr, 1, E.nm, CUFFT_D2Z, (int)ncomp) != CUFFT_SUCCESS) return bail("cuFFT plan failed");
+    cufftSetStream(pa, s->stream);
+    const bool ok = cufftExecD2Z(pa, A, E.FA) == CUFFT_SUCCESS;
+    cudaStreamSynchronize(s->stream);
+    cufftDestroy(pa);
+    if (!ok) return bail("cuFFT transform failed");
+    if (cufftPlanMany(&E.plan_f, 3, n, nullptr, 1, ncell, nullptr, 1, E.nm, CUFFT_D2Z, 3 * na) != CUFFT_SUCCESS) return bail("cuFFT plan failed");
+    E.have_f = true;
+    if (cufftPlanMany(&E.plan_b, 3, n, nullptr, 1, E.nm, nullptr, 1, ncell, CUFFT_Z2D, 3 * na) != CUFFT_SUCCESS) return bail("cuFFT plan failed");
+    E.have_b = true;
+    void* p = A; dfree(p); p = pos_d; dfree(p);
     return SGB_OK;
 }
 
@@ -612,6 +839,12 @@ int sgb_energy_grad(sgb_system* s, double* grad) {
     if (!s->sun) {
         rc = s->fp32 ? dip_launch_grad<float>(s->mf, (const float*)s->S, s->dbuf, s->stream)
                      : dip_launch_grad<double>(s->md, (const double*)s->S, s->dbuf, s->stream);
+        if (rc == SGB_OK && s->ewald_on) {
+            s->launches++;
+            rc = s->fp32 ? ewald_add<float>(s, (const float*)s->S, s->dbuf, nullptr)
+                         : ewald_add<double>(s, (const double*)s->S, s->dbuf, nullptr);
+            if (rc) return rc;
+        }
     } else {
         rc = s->fp32 ? sun_launch_grad<float>(s->mf, (const float*)s->Z, (const float*)s->S, (const float*)s->Q, s->dbuf, s->stream)
                      : sun_launch_grad<double>(s->md, (const double*)s->Z, (const double*)s->S, (const double*)s->Q, s->dbuf, s->stream);
@@ -642,6 +875,12 @@ int sgb_energy(sgb_system* s, double* E, double* M3) {
     double out[4];
     CK(cudaMemcpyAsync(out, s->red, sizeof(out), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    if (s->ewald_on && !s->sun) {
+        double Ed = 0;
+        rc = s->fp32 ? ewald_add<float>(s, (const float*)s->S, nullptr, &Ed) : ewald_add<double>(s, (const double*)s->S, nullptr, &Ed);
+        if (rc) return rc;
+        out[0] += Ed;
+    }
     if (E) *E = out[0];
     if (M3) { M3[0] = out[1]; M3[1] = out[2]; M3[2] = out[3]; }
     return SGB_OK;
@@ -660,6 +899,9 @@ int sgb_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t s
     int rc = ensure_tables(s);
     if (rc) return rc;
     if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called before stepping");
+    if (s->ewald_on)
+        return s->fp32 ? run_langevin_lr<float>(s, dt, damping, kT, seed, step0, nsteps, noise)
+                       : run_langevin_lr<double>(s, dt, damping, kT, seed, step0, nsteps, noise);
     return s->fp32 ? run_langevin<float>(s, dt, damping, kT, seed, step0, nsteps, noise)
                    : run_langevin<double>(s, dt, damping, kT, seed, step0, nsteps, noise);
 }
@@ -689,6 +931,9 @@ int sgb_midpoint(sgb_system* s, double dt, double damping, double tol, int32_t m
     int rc = ensure_tables(s);
     if (rc) return rc;
     if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called before stepping");
+    if (s->ewald_on)
+        return s->fp32 ? run_midpoint_lr<float>(s, dt, damping, tol, max_iters, nsteps, iters_out)
+                       : run_midpoint_lr<double>(s, dt, damping, tol, max_iters, nsteps, iters_out);
     if (s->fp32) {
         SnapArgs<float> sn{};
         return run_midpoint<float>(s, dt, damping, tol, max_iters, nsteps, iters_out, sn, true, s->mid_order);
@@ -701,6 +946,7 @@ int sgb_local_sweeps(sgb_system* s, double kT, double nsweeps, const sgb_proposa
                      const double* rand, double* dE, double* dS3) {
     if (!s) return fail(s, SGB_ERR_ARG, "null handle");
     if (s->sun) return fail(s, SGB_ERR_ARG, "LocalSampler on the GPU supports the dipole modes");
+    if (s->ewald_on) return fail(s, SGB_ERR_ARG, "LocalSampler with dipole-dipole interactions is not supported on the GPU");
     if (!(kT >= 0)) return fail(s, SGB_ERR_ARG, "Select nonnegative kT");
     if (!(nsweeps >= 0) || nsweeps > 1e9) return fail(s, SGB_ERR_ARG, "nsweeps must be nonnegative");
     if (!prop || prop->n < 1 || prop->n > 4) return fail(s, SGB_ERR_ARG, "a proposal mixture has 1 to 4 functions");
@@ -754,7 +1000,8 @@ int sgb_local_sweeps(sgb_system* s, double kT, double nsweeps, const sgb_proposa
 // bound (Optim.jl ConjugateGradient defaults), a bracketing line search (secant on φ',
 // else bisection) on φ(α) = E(κ·normalize(x + α d)) that accepts the strong Wolfe
 // conditions, first step ψ0/|g|∞ (Hager & Zhang's I0 with |x|∞ = 1), then
-// α_prev·φ'_prev(0)/φ'(0), capped at αmax = 10. Converged when the largest projected-gradient component is at most
+// α_prev·φ'_prev(0)/φ'(0), capped at αmax = 10 (the bracketing phase may expand past
+// it, which lets a jittered start leave a saddle). Converged when the largest projected-gradient component is at most
 // 1e-12·characteristic_energy_scale or the largest step component at most 1e-12
 // (Optimization.jl:149-156); on a failed line search the direction restarts from -g
 // once, as optimize_with_restarts does (Optimization.jl:59-70).
@@ -804,6 +1051,9 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
             dip_launch_energy<double>(s->md, S, s->partials, nbE, st) || util_launch_reduce(s->partials, nbE, 4, s->red, st))
             return cuda_fail(s, cudaGetLastError(), "optimizer evaluation");
         s->launches += 4;
+        double Ed = 0;
+        int erc = ewald_add<double>(s, S, grad, s->ewald_on ? &Ed : nullptr);
+        if (erc) return erc;
         if (dphi) {
             if (opt_launch_dphi(x, d, alpha, grad, kap, ns, part, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
             s->launches++;
@@ -811,9 +1061,12 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
         CK(cudaMemcpyAsync(f, s->red, sizeof(double), cudaMemcpyDeviceToHost, st));
         if (dphi) {
             const bool mx[1] = {false};
-            return pull(1, dphi, mx);
+            int prc = pull(1, dphi, mx);
+            *f += Ed;
+            return prc;
         }
         CK(cudaStreamSynchronize(st));
+        *f += Ed;
         return SGB_OK;
     };
     const bool acc_max[10] = {false, false, false, false, false, false, false, true, true, false};
@@ -830,7 +1083,8 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
     };
     double f = 0, v[10], w[2];
     if ((rc = eval(0.0, &f, nullptr)) || (rc = accept(0.0, v))) return rc;
-    const double g_abstol = 1e-12 * std::sqrt(v[9]) / std::sqrt((double)ns);   // characteristic_energy_scale
+    const double v9_0 = v[9];
+    const double g_abstol = 1e-12 * std::sqrt(v9_0) / std::sqrt((double)ns);   // characteristic_energy_scale
     const double x_abstol = 1e-12;
     bool conv = v[7] <= g_abstol;
     int iters = 0;
@@ -862,9 +1116,9 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
             } else {
                 lo = a; flo = fa; dlo = da;
             }
-            if (hi < 0) {                       // still descending: expand
-                if (a >= amax) break;
-                a = std::min(5.0 * a, amax);
+            if (hi < 0) {                       // still descending: expand (past the cap of the
+                if (a * w[1] >= 10.0) break;     // initial guess, as Hager-Zhang does) until a
+                a = 5.0 * a;                     // component would turn by 10 radians
                 continue;
             }
             // next trial inside (lo, hi): secant on φ', else bisection
@@ -879,9 +1133,16 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
         }
         (void)fhi;
         if (acc_a < 0) {
-            if (restarted) break;                // second failure in a row: give up
+            if (restarted) {
+                // second failure in a row: no step decreases E at FP64 resolution, so x no
+                // longer moves (Optim then reports x_abschange = 0 <= x_abstol). Accept that
+                // as convergence only near a stationary point.
+                conv = gmax <= 1e-6 * std::sqrt(v9_0) / std::sqrt((double)ns);
+                break;
+            }
             restarted = true;
             if ((rc = eval(0.0, &f, nullptr)) || (rc = accept(0.0, v)) || (rc = direction(0.0, w))) return rc;
+            gmax = v[7];
             alpha_prev = 0;
             continue;
         }
@@ -928,6 +1189,7 @@ int sgb_local_colors(sgb_system* s, int32_t* ncolors, int32_t* color) {
 int sgb_local_energy_change(sgb_system* s, int64_t site, const double* S_new, double* dE) {
     if (!s || !S_new || !dE) return fail(s, SGB_ERR_ARG, "null argument");
     if (s->sun) return fail(s, SGB_ERR_ARG, "LocalSampler on the GPU supports the dipole modes");
+    if (s->ewald_on) return fail(s, SGB_ERR_ARG, "LocalSampler with dipole-dipole interactions is not supported on the GPU");
     if (site < 0 || site >= s->ns) return fail(s, SGB_ERR_ARG, "site out of range");
     int rc = ensure_colors(s);   // also rejects self-interaction
     if (rc) return rc;
@@ -1196,6 +1458,8 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
     sgb_system* s = c->sys;
     sgb_batch* b = c->batch;
     if (!s && !b) return cfail(c, SGB_ERR_STATE, "the System (or replica batch) of this accumulator was destroyed");
+    if (s && s->ewald_on)
+        return cfail(c, SGB_ERR_ARG, "SampledCorrelations trajectories with dipole-dipole interactions are not supported on the GPU");
     if (window != 0 && window != 1) return cfail(c, SGB_ERR_ARG, "window must be 0 (:cosine) or 1 (:rectangular)");
     if (c->window >= 0 && c->window != window)
         return cfail(c, SGB_ERR_ARG, "all samples of one accumulator must use the same window");

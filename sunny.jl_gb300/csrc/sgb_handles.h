@@ -56,6 +56,12 @@ struct sgb_system {
     int* mc_perm = nullptr;
     double* mc_part = nullptr;       // [grid][4] per-block ΔE, ΔS partials
     int mc_part_cap = 0;
+    // dipole-dipole (Ewald) interactions, when enabled
+    bool ewald_on = false;
+    EwaldDev ew{};
+    double* ew_part = nullptr;       // [EWALD_PART_BLOCKS] energy partials
+    double* lr_grad = nullptr;       // [ns][3] gradient of the per-stage integrator path
+    int lr_grad_cap = 0;
 };
 
 struct sgb_corr {

@@ -121,6 +121,48 @@ int opt_launch_accept(double* x, double* d, double alpha, const double* grad, co
                       double* part, cudaStream_t st);
 int opt_launch_dir(const double* g, double* d, double beta, int ns, double* part, cudaStream_t st);
 
+// ---- dipole-dipole Ewald summation (sgb_ewald.cu) ----
+#include <cufft.h>
+struct EwaldGeom {
+    int L[3], na;
+    double lat[9], sup[9], rec[9];   // column-major: unit cell, supercell, supercell reciprocals
+    double demag[9];
+    double V, sig, rmax, kmax, mu0;
+    int nmax[3], mmax[3];
+};
+struct EwaldDev {
+    int L[3], na, nm;                // nm = L3*L2*(L1/2+1) complex cells
+    double* g = nullptr;             // [ns][9] column-major g tensors
+    double* mu = nullptr;            // [na][3][ncell]
+    double* phi = nullptr;           // [na][3][ncell]
+    cufftDoubleComplex* FA = nullptr;    // [na*na*9][nm]
+    cufftDoubleComplex* Fmu = nullptr;   // [na*3][nm]
+    cufftDoubleComplex* Fphi = nullptr;  // [na*3][nm]
+    cufftHandle plan_f = 0, plan_b = 0;
+    bool have_f = false, have_b = false;
+};
+#define EWALD_PART_BLOCKS 256
+int ewald_precompute(const EwaldGeom& G, const double* pos_d, double* A, cudaStream_t st);
+// adds the Ewald gradient into grad_aos ([ns][3], may be null) and writes EWALD_PART_BLOCKS
+// energy partials into part (may be null)
+template <class R>
+int ewald_apply(const EwaldDev& E, const R* S, double* grad_aos, double* part, cudaStream_t st);
+
+// integrator stages used when long-range terms need a global transform per gradient
+template <class R>
+int lr_heun_a(const R* S, const double* grad, R* P, R* D1, R* XI, const R* kappa, int ns, double dt, double lam,
+              double nscale, uint64_t seed, uint64_t step, const double* noise, cudaStream_t st);
+template <class R>
+int lr_heun_b(R* S, const R* P, const double* grad, const R* D1, const R* XI, const R* kappa, int ns, double dt,
+              double lam, cudaStream_t st);
+template <class R>
+int lr_mid_half(const R* S, const R* Sp, R* H, const R* kappa, int ns, cudaStream_t st);
+template <class R>
+int lr_mid_update(const R* S, const R* H, const double* grad, R* Sp, int ns, double dt, double lam, double* part,
+                  cudaStream_t st);
+template <class R>
+int lr_mid_accept(R* S, const R* Sp, const R* kappa, int ns, cudaStream_t st);
+
 // ---- shared utilities (sgb_dipole.cu) ----
 int util_launch_reduce(const double* partials, int n, int ncomp, double* out, cudaStream_t st);
 template <class R>

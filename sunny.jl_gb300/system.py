@@ -186,6 +186,8 @@ class System:
         self.seed = int(seed) if seed is not None else int(self.rng.integers(0, 2**62))
         self.noise_step = 0
         self.mc_sweep = 0
+        self._ewald = None            # (μ0 μB², demag 3x3) when dipole-dipole is enabled
+        self._ewald_dirty = False
         self._couplings_dirty = True
         self._host_newer = True
         self._dev_newer = False
@@ -316,6 +318,17 @@ class System:
         lib, h = self._lib, self._h
         _abi.check(lib.sgb_set_sites(h, _abi.dptr(self._kappa), _abi.dptr(np.ascontiguousarray(self._g.transpose(0, 2, 1)).reshape(-1)),
                                      _abi.dptr(np.ascontiguousarray(self._field.reshape(-1)))), lib, h)
+        if self._ewald_dirty:
+            if self._ewald is None:
+                _abi.check(lib.sgb_set_dipole_dipole(h, 0.0, None, None, None), lib, h)
+            else:
+                mu0, demag = self._ewald
+                lat = np.ascontiguousarray(np.asarray(self.crystal.latvecs, dtype=float).T.reshape(-1))   # column-major
+                pos = np.ascontiguousarray(np.array([self.crystal.position(i) for i in range(1, self.natoms + 1)],
+                                                    dtype=float).reshape(-1))
+                dm = np.ascontiguousarray(np.asarray(demag, dtype=float).T.reshape(-1))
+                _abi.check(lib.sgb_set_dipole_dipole(h, float(mu0), _abi.dptr(dm), _abi.dptr(lat), _abi.dptr(pos)), lib, h)
+            self._ewald_dirty = False
         for a in range(self.natoms):
             oc = self._onsite[a]
             if self.N:
@@ -441,6 +454,19 @@ class System:
             self._onsite[a - 1] = c.copy()
         self._couplings_dirty = True
 
+    def enable_dipole_dipole(self, mu0_muB2=None, demag=1 / 3):
+        """enable_dipole_dipole!(sys, μ0_μB²; demag=1/3) (Interactions.jl:180-188): Ewald-summed
+        dipole-dipole interactions over the periodic supercell; `demag` is a scalar (times
+        the identity) or a 3x3 tensor."""
+        if mu0_muB2 is None:
+            import warnings
+            warnings.warn("Deprecated syntax! Consider `enable_dipole_dipole(sys, units.vacuum_permeability)`")
+            mu0_muB2 = 0.6745817653   # μ0 μB² in meV Å³ (Units.jl:57)
+        dm = np.asarray(demag, dtype=float)
+        self._ewald = (float(mu0_muB2), dm * np.eye(3) if dm.ndim == 0 else dm.reshape(3, 3))
+        self._ewald_dirty = True
+        self._couplings_dirty = True
+
     def set_field(self, B):
         """set_field!(sys, B) (Interactions.jl:210-214); B already scaled by μB."""
         self._field[:] = np.asarray(B, dtype=float).reshape(3)
@@ -508,6 +534,10 @@ def randomize_spins(sys: System):
 
 def polarize_spins(sys: System, direction):
     sys.polarize_spins(direction)
+
+
+def enable_dipole_dipole(sys: System, mu0_muB2=None, demag=1 / 3):
+    sys.enable_dipole_dipole(mu0_muB2, demag)
 
 
 def energy(sys: System) -> float:
@@ -595,6 +625,9 @@ def clone_system(sys: System, seed=None) -> System:
                                 pc.biquad.copy() if isinstance(pc.biquad, np.ndarray) else pc.biquad)
                 for b, pc in sys._pairs.items()}
     c._onsite = [None if o is None else np.array(o) for o in sys._onsite]
+    if sys._ewald is not None:
+        c._ewald = (sys._ewald[0], np.array(sys._ewald[1]))
+        c._ewald_dirty = True
     c._base_dip[:] = sys._base_dip
     c._base_coh[:] = sys._base_coh
     if seed is None:

@@ -1,0 +1,149 @@
+"""Dipole-dipole interactions (Ewald summation) on the GPU against the reference's known
+answers (test_ewald.jl, test_optimization.jl:31-52) and the oracle's pairwise sums."""
+import math
+
+import numpy as np
+import pytest
+
+from models import oracle_of
+
+pytestmark = pytest.mark.gpu
+
+
+def _triclinic(sg, precision="fp64", dims=(1, 1, 1), seed=0):
+    # a random box with three atoms of different spins and random g tensors (test_ewald.jl:29-47)
+    rng = np.random.default_rng(seed)
+    cr = sg.Crystal(sg.lattice_vectors(1.1, 0.9, 0.8, 92, 85, 95), [[0, 0.01, 0.01], [0.1, 0.01, 0.01], [0.6, 0.4, 0.5]])
+    mom = [(1, sg.Moment(s=1, g=rng.random((3, 3)))), (2, sg.Moment(s=1.5, g=rng.random((3, 3)))),
+           (3, sg.Moment(s=2, g=rng.random((3, 3))))]
+    s = sg.System(cr, mom, "dipole", dims=dims, seed=seed + 1, precision=precision)
+    s.randomize_spins()
+    R = rng.standard_normal((3, 3))
+    demag = R.T @ R
+    s.enable_dipole_dipole(1.0, demag)
+    return s, demag
+
+
+def _reference_grad(orc, sys_, demag, mu0=1.0):
+    o = oracle_of(orc, sys_)
+    S = sys_.dipoles_flat()
+    cr = sys_.crystal
+    pos = [cr.position(i) for i in range(1, sys_.natoms + 1)]
+    A = orc.ewald_matrices(sys_.dims, cr.latvecs, pos, demag, mu0)
+    g = sys_._g
+    gd = orc.ewald_pairwise_grad(A, sys_.dims, sys_.natoms, S, g)
+    return o, S, gd, o.grad(S) + gd
+
+
+def test_single_dipole_energy(gpu, sg):
+    cr = sg.Crystal(sg.lattice_vectors(1, 1, 1, 90, 90, 90), [[0, 0, 0]])
+    s = sg.System(cr, [(1, sg.Moment(s=1, g=1))], "dipole")
+    s.enable_dipole_dipole(1.0, demag=0)
+    assert sg.energy(s) == pytest.approx(-1 / 6, abs=1e-13)
+    s2 = sg.System(cr, [(1, sg.Moment(s=1, g=1))], "dipole", dims=(2, 3, 4))
+    s2.enable_dipole_dipole(1.0, demag=0)
+    assert sg.energy_per_site(s2) == pytest.approx(-1 / 6, abs=1e-13)
+
+
+@pytest.mark.parametrize("dims", [(1, 1, 1), (2, 3, 1)])
+def test_energy_and_gradient_match_pairwise_sums(gpu, sg, orc, dims):
+    sys_, demag = _triclinic(sg, dims=dims)
+    o, S, gd, gtot = _reference_grad(orc, sys_, demag)
+    g_gpu = sg.energy_grad(sys_)
+    assert np.max(np.abs(g_gpu - gtot)) <= 1e-12 * np.max(np.abs(gtot))
+    E_ref = o.energy(S) + 0.5 * np.sum(S * gd)
+    assert sg.energy(sys_) == pytest.approx(E_ref, abs=1e-12 * max(1.0, abs(E_ref)))
+
+
+def test_energy_per_site_independent_of_supercell(gpu, sg):
+    a, _ = _triclinic(sg, dims=(1, 1, 1))
+    b, _ = _triclinic(sg, dims=(2, 3, 1))
+    Sa = a.dipoles_flat()
+    b.set_state_flat(dipoles=np.repeat(Sa, 6, axis=0).reshape(3, 6, 3).reshape(-1, 3))   # same spin per atom
+    assert sg.energy_per_site(a) == pytest.approx(sg.energy_per_site(b), abs=1e-12)
+
+
+def _rhs(S, xi, g, dt, lam):
+    # Integrators.jl:266-275
+    return -np.cross(S, xi + dt * g - dt * lam * np.cross(S, g))
+
+
+def _norm(S, kap):
+    return S / np.linalg.norm(S, axis=1)[:, None] * kap[:, None]
+
+
+def test_langevin_with_dipole_dipole_matches_restatement(gpu, sg, orc):
+    sys_, demag = _triclinic(sg, dims=(2, 1, 1))
+    kap = np.asarray(sys_.kappas, dtype=float)
+    o = oracle_of(orc, sys_)
+    cr = sys_.crystal
+    A = orc.ewald_matrices(sys_.dims, cr.latvecs, [cr.position(i) for i in range(1, 4)], demag, 1.0)
+
+    def grad(S):
+        return o.grad(S) + orc.ewald_pairwise_grad(A, sys_.dims, sys_.natoms, S, sys_._g)
+
+    dt, lam, kT = 0.01, 0.2, 0.3
+    noise = np.random.default_rng(9).standard_normal((2, sys_.nsites, 3))
+    S = sys_.dipoles_flat()
+    for k in range(2):   # stochastic Heun (Integrators.jl:313-332) in FP64
+        xi = noise[k] * math.sqrt(2 * dt * lam * kT)
+        d1 = _rhs(S, xi, grad(S), dt, lam)
+        P = _norm(S + d1, kap)
+        d2 = _rhs(P, xi, grad(P), dt, lam)
+        S = _norm(S + (d1 + d2) / 2, kap)
+    sg.step(sys_, sg.Langevin(dt, damping=lam, kT=kT), 2, noise)
+    assert np.max(np.abs(sys_.dipoles_flat() - S)) < 1e-12 * np.max(np.abs(S))
+
+
+def test_midpoint_with_dipole_dipole(gpu, sg, orc):
+    # exchange plus dipole-dipole on a cubic lattice (the random box's 0.1 Å pairs are too
+    # stiff for the fixed-point iteration at a useful dt)
+    cr = sg.Crystal(sg.lattice_vectors(2, 2, 2, 90, 90, 90), [[0, 0, 0]])
+    sys_ = sg.System(cr, [(1, sg.Moment(s=1, g=2))], "dipole", dims=(3, 3, 2), seed=4)
+    sys_.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    sys_.enable_dipole_dipole(0.5)
+    sys_.randomize_spins()
+    o = oracle_of(orc, sys_)
+    A = orc.ewald_matrices(sys_.dims, cr.latvecs, [cr.position(1)], np.eye(3) / 3, 0.5)
+    kap = np.asarray(sys_.kappas, dtype=float)
+
+    def grad(S):
+        return o.grad(S) + orc.ewald_pairwise_grad(A, sys_.dims, 1, S, sys_._g)
+
+    dt, tol = 0.01, 1e-12
+    atol2 = tol * tol * sys_.nsites
+    S = sys_.dipoles_flat()
+    E0 = sg.energy(sys_)
+    for _ in range(3):   # spherical midpoint (Integrators.jl:379-413) in FP64
+        Sp = S.copy()
+        for _ in range(100):
+            H = _norm((S + Sp) / 2, kap)
+            Spp = S + _rhs(H, 0.0, grad(H), dt, 0.0)
+            done = np.sum((Sp - Spp) ** 2) <= atol2
+            Sp = Spp
+            if done:
+                break
+        S = _norm(Sp, kap)
+    sg.step(sys_, sg.ImplicitMidpoint(dt, tol=tol), 3)
+    assert np.max(np.abs(sys_.dipoles_flat() - S)) < 1e-10
+    sg.step(sys_, sg.ImplicitMidpoint(dt, tol=tol), 200)
+    assert abs(sg.energy(sys_) - E0) <= 1e-3 * abs(E0)
+
+
+@pytest.mark.parametrize("jitter,ref", [(0.0, 0.6327349993784377), (1e-8, -5.7060439873282)])
+def test_canted_afm_optimization(gpu, sg, jitter, ref):
+    cr = sg.Crystal(sg.lattice_vectors(1, 1, 2, 90, 90, 90), [[0, 0, 0]])
+    s = sg.System(cr, [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(4, 4, 1), seed=3)
+    s.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    s.set_field([1.0, 0, 0])
+    s.enable_dipole_dipole(1.0)
+    s.polarize_spins([0, 0, 1])
+    r = sg.minimize_energy(s, jitter=jitter)
+    assert r.converged
+    assert sg.energy_per_site(s) == pytest.approx(ref, rel=1e-9)
+
+
+def test_unsupported_paths_reject_dipole_dipole(gpu, sg):
+    sys_, _ = _triclinic(sg)
+    with pytest.raises(sg.SunnyGPUError, match="dipole-dipole"):
+        sg.step(sys_, sg.LocalSampler(kT=0.1))
