@@ -279,6 +279,33 @@ def dynamics_rate(sg, kind, precision, device, nsteps):
             "nsites": ns, "steps": nsteps, "energy_per_site": E}
 
 
+def local_sampler_rate(sg, precision, device, nsweeps=200):
+    """Single-spin Metropolis proposals/s of the LocalSampler on the simple cubic 16^3
+    model (s=1, J=1, -0.1 Sz^2) at kT=0.5 with propose_delta(0.3): colour-class parallel
+    sweeps in one persistent launch."""
+    import ctypes as C
+    lib = sg.load_library()
+    sys_ = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=(16, 16, 16), seed=1,
+                     precision=precision, device=device)
+    sys_.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    sys_.set_onsite_coupling(lambda Sx, Sy, Sz: -0.1 * Sz @ Sz, 1)
+    sys_.randomize_spins()
+    smp = sg.LocalSampler(kT=0.5, propose=sg.propose_delta(0.3))
+    sg.step(sys_, smp, 20)
+    lib.sgb_synchronize(sys_.handle)
+    lib.sgb_event_record(sys_.handle, 0)
+    sg.step(sys_, smp, nsweeps)
+    lib.sgb_event_record(sys_.handle, 1)
+    ms = C.c_float()
+    lib.sgb_event_elapsed(sys_.handle, 0, 1, C.byref(ms))
+    ns = sys_.nsites
+    ncol, _ = sg.local_colors(sys_)
+    E = sg.energy_per_site(sys_)
+    sys_.close()
+    return {"proposals_per_s": ns * nsweeps / (ms.value / 1000.0), "us_per_sweep": 1000.0 * ms.value / nsweeps,
+            "nsites": ns, "sweeps": nsweeps, "colour_classes": ncol, "energy_per_site": E}
+
+
 def run_adjoint(sg, device, L_=24, nw=64, checkpoint=64):
     """Differentiation workload: simple cubic 24^3 dipole lattice (13,824 spins, s=1) from a
     state thermalised by Langevin at kT=0.3; parameters J1 (1.0), J2 (0.1), D (0.05, onsite
@@ -505,6 +532,7 @@ def main():
             a = dynamics_rate(sg, kind, "fp32", local, n)
             bb = dynamics_rate(sg, kind, "fp64", local, n // 4)
             extra[kind] = {"fp32": a, "fp64": bb, "speedup": a["site_steps_per_s"] / bb["site_steps_per_s"]}
+        extra["local_sampler_sc"] = {p: local_sampler_rate(sg, p, local) for p in ("fp32", "fp64")}
         pt = run_tempering(sg, local)
         extra["adjoint"] = run_adjoint(sg, local)
         c3 = {"fp32": run_c3_sqw(sg, local, "fp32", 2), "fp64": run_c3_sqw(sg, local, "fp64", 1)}
@@ -565,6 +593,7 @@ def main():
                                     "tempering_256_replicas": pt},
             "adjoint_c5": extra.get("adjoint"),
             "sqw_su3_triangular_48x48x4": extra.get("c3_sqw"),
+            "local_sampler_simple_cubic_16^3": extra.get("local_sampler_sc"),
             "roofline": roof,
             "gpu_launches": rb["launches"],
             "clocks": rb["clocks"],
