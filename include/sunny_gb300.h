@@ -192,7 +192,8 @@ typedef struct {
     double  magnitude[4];
 } sgb_proposal;
 
-/* step!(sys, LocalSampler(; kT, nsweeps, propose)) (Samplers.jl:139-158), dipole modes.
+/* step!(sys, LocalSampler(; kT, nsweeps, propose)) (Samplers.jl:139-158), dipole and SU(N)
+ * modes.
  * Sunny proposes ceil(nsweeps*ns) updates at uniformly drawn sites; here one sweep
  * visits every site once, colour class by colour class of a greedy colouring of the
  * bond graph (sites of one class share no coupling and are updated in parallel), so
@@ -202,7 +203,10 @@ typedef struct {
  * kT = 0, else u <= exp(-ΔE/kT) with ΔE = local_energy_change.
  * rand == NULL: random numbers from a counter-based generator keyed by
  *   (seed, sweep0 + k, site); rand != NULL: caller-supplied, [nsweeps_total][ns][6]
- *   = (3 standard normals, mixture uniform, acceptance uniform, participation uniform).
+ *   = (3 standard normals, mixture uniform, acceptance uniform, participation uniform);
+ *   in SU(N) mode [nsweeps_total][ns][2N+3] = (N complex normals with E|z|^2 = 1 as
+ *   (re, im), then the three uniforms). SU(N) proposals: randspin (System.jl:448-452),
+ *   flip_ket (Spin.jl:121-128), perturbed_spin (System.jl:461-468).
  * dE (nullable) receives the summed energy change of the accepted updates and dS3
  * (nullable) the summed dipole change: the sampler's ΔE and ΔS (Samplers.jl:153-156). */
 int sgb_local_sweeps(sgb_system* sys, double kT, double nsweeps, const sgb_proposal* propose,
@@ -211,8 +215,9 @@ int sgb_local_sweeps(sgb_system* sys, double kT, double nsweeps, const sgb_propo
 /* The colouring used by sgb_local_sweeps: *ncolors classes, color (nullable) [ns]. */
 int sgb_local_colors(sgb_system* sys, int32_t* ncolors, int32_t* color);
 
-/* local_energy_change(sys, site, state) (Interactions.jl:311-373), dipole modes: the
- * energy change if the dipole at `site` (0-based, Sunny's linear order) became S_new. */
+/* local_energy_change(sys, site, state) (Interactions.jl:311-373): the energy change if
+ * the state at `site` (0-based, Sunny's linear order) became S_new: a dipole [3] in dipole
+ * modes, a coherent state [N][2] in SU(N) mode. */
 int sgb_local_energy_change(sgb_system* sys, int64_t site, const double* S_new, double* dE);
 
 /* minimize_energy!(sys; maxiters, jitter) (Optimization.jl:102-166), dipole modes, FP64

@@ -63,6 +63,9 @@ def load() -> C.CDLL:
             "or_langevin_replicas": (C.c_int, [P, C.c_int, _D, _D, C.c_double, C.c_double, C.c_int, C.c_uint64]),
             "or_expected_spin": (None, [C.c_int, _D, _D]),
             "or_local_energy_change": (C.c_double, [P, _D, C.c_int64, _D]),
+            "or_local_energy_change_sun": (C.c_double, [P, _D, _D, C.c_int64, _D]),
+            "or_local_sweeps_sun": (None, [P, _D, _D, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_int), C.c_int,
+                                           C.POINTER(C.c_int), _D, _D, _D, _D, _D]),
             "or_ewald_matrices": (None, [C.c_int, C.c_int, C.c_int, C.c_int, _D, _D, _D, C.c_double, _D]),
             "or_local_sweeps": (None, [P, _D, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_int), C.c_int,
                                        C.POINTER(C.c_int), _D, _D, _D, _D, _D]),
@@ -142,9 +145,13 @@ class OracleSystem:
         self.lib.or_grad_dipoles(C.byref(self.s), _p(S), _p(out))
         return out
 
-    def local_energy_change(self, S, site, S_new):
-        """local_energy_change (Interactions.jl:311-373), dipole modes."""
+    def local_energy_change(self, S, site, S_new, Z=None):
+        """local_energy_change (Interactions.jl:311-373). SU(N) mode: Z (ns, N) complex kets,
+        S their expected dipoles, S_new the new ket (N,) complex."""
         S = np.ascontiguousarray(S, dtype=float)
+        if self.N:
+            zn = np.ascontiguousarray(np.stack([np.real(S_new), np.imag(S_new)], -1), dtype=float).reshape(-1)
+            return self.lib.or_local_energy_change_sun(C.byref(self.s), _p(S), _p(self._zbuf(Z)), int(site), _p(zn))
         Sn = np.ascontiguousarray(S_new, dtype=float)
         return self.lib.or_local_energy_change(C.byref(self.s), _p(S), int(site), _p(Sn))
 
@@ -165,6 +172,25 @@ class OracleSystem:
         self.lib.or_local_sweeps(C.byref(self.s), _p(S), float(kT), int(nsweeps), float(frac), perm.ctypes.data_as(IP),
                                  len(proposal), kind.ctypes.data_as(IP), _p(cum), _p(mag), _p(rnd), C.byref(dE), _p(dS))
         return S, dE.value, dS
+
+    def local_sweeps_sun(self, S, Z, kT, nsweeps, frac, order, proposal, rand):
+        """SU(N) LocalSampler updates (see local_sweeps); rand [nsweeps][ns][2N+3].
+        Returns (S, Z, dE, dS)."""
+        S = np.ascontiguousarray(S, dtype=float).copy()
+        zb = self._zbuf(Z).copy()
+        perm = np.ascontiguousarray(order, dtype=np.int32)
+        w = np.array([p[1] for p in proposal], dtype=float)
+        cum = np.cumsum(w / w.sum())
+        kind = np.array([p[0] for p in proposal], dtype=np.int32)
+        mag = np.array([p[2] for p in proposal], dtype=float)
+        rnd = np.ascontiguousarray(rand, dtype=float).reshape(-1)
+        dE = C.c_double()
+        dS = np.zeros(3)
+        IP = C.POINTER(C.c_int)
+        self.lib.or_local_sweeps_sun(C.byref(self.s), _p(S), _p(zb), float(kT), int(nsweeps), float(frac),
+                                     perm.ctypes.data_as(IP), len(proposal), kind.ctypes.data_as(IP), _p(cum), _p(mag),
+                                     _p(rnd), C.byref(dE), _p(dS))
+        return S, self._unz(zb), dE.value, dS
 
     def energy(self, S, Z=None):
         S = np.ascontiguousarray(S, dtype=float)

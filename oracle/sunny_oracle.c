@@ -562,6 +562,112 @@ double or_local_energy_change(const or_sys* s, const double* S, int64_t site, co
     return dE;
 }
 
+/* SU(N) mode: Z [ns][N][2] and S [ns][3] (expected dipoles); the ket at `site` becomes
+ * Znew [N][2]. Neighbours enter through expected dipoles and quadrupoles. */
+static double onsite_e(int N, const double* lam, const cplx* z) {
+    cplx acc = 0;
+    for (int c = 0; c < N; c++)
+        for (int r = 0; r < N; r++) acc += conj(z[r]) * (lam[2 * (r + N * c)] + I * lam[2 * (r + N * c) + 1]) * z[c];
+    return creal(acc);
+}
+
+double or_local_energy_change_sun(const or_sys* s, const double* S, const double* Z, int64_t site, const double* Znew) {
+    const int N = s->N, L1 = s->L[0], L2 = s->L[1], L3 = s->L[2];
+    or_ops ops;
+    build_ops(N, &ops);
+    int64_t ncell = (int64_t)L1 * L2 * L3;
+    int a = (int)(site / ncell);
+    int64_t cell = site % ncell;
+    int c1 = (int)(cell % L1), c2 = (int)((cell / L1) % L2), c3 = (int)(cell / ((int64_t)L1 * L2));
+    cplx z0[8], zn[8];
+    for (int k = 0; k < N; k++) { z0[k] = zget(Z, site, N, k); zn[k] = Znew[2 * k] + I * Znew[2 * k + 1]; }
+    double s0[3], sn[3], q0[5], qn[5], dS[3], dQ[5];
+    or_expected_spin(N, Z + 2 * (size_t)N * site, s0);
+    or_expected_spin(N, Znew, sn);
+    expected_quadrupole(&ops, z0, q0);
+    expected_quadrupole(&ops, zn, qn);
+    for (int r = 0; r < 3; r++) dS[r] = sn[r] - s0[r];
+    for (int q = 0; q < 5; q++) dQ[q] = qn[q] - q0[q];
+    double dE = 0;
+    if (s->field) {
+        const double* g = s->g + 9 * site;
+        const double* B = s->field + 3 * site;
+        for (int r = 0; r < 3; r++) dE += B[r] * (g[r] * dS[0] + g[r + 3] * dS[1] + g[r + 6] * dS[2]);
+    }
+    if (s->onsite) dE += onsite_e(N, s->onsite + 2 * N * N * a, zn) - onsite_e(N, s->onsite + 2 * N * N * a, z0);
+    for (int b = 0; b < s->nbonds; b++) {
+        const sgb_bond* pc = &s->bonds[b];
+        const double* J = pc->bilin;
+        for (int end = 0; end < 2; end++) {
+            if ((end == 0 ? pc->i : pc->j) != a) continue;
+            int sg_ = end == 0 ? 1 : -1;
+            int64_t j = site_index(s, wrap(c1 + sg_ * pc->n[0], L1), wrap(c2 + sg_ * pc->n[1], L2), wrap(c3 + sg_ * pc->n[2], L3),
+                                   end == 0 ? pc->j : pc->i);
+            if (j == site) return NAN;
+            const double* Sj = S + 3 * j;
+            if (end == 0) for (int r = 0; r < 3; r++) dE += dS[r] * (J[r] * Sj[0] + J[r + 3] * Sj[1] + J[r + 6] * Sj[2]);
+            else for (int r = 0; r < 3; r++) dE += Sj[r] * (J[r] * dS[0] + J[r + 3] * dS[1] + J[r + 6] * dS[2]);
+            if (pc->biquad_kind != 0) {
+                cplx zj[8];
+                double Qj[5];
+                for (int k = 0; k < N; k++) zj[k] = zget(Z, j, N, k);
+                expected_quadrupole(&ops, zj, Qj);
+                dE += end == 0 ? biquad_pair(pc, dQ, Qj) : biquad_pair(pc, Qj, dQ);
+            }
+        }
+    }
+    return dE;
+}
+
+void or_local_sweeps_sun(const or_sys* s, double* S, double* Z, double kT, int nsweeps, double frac, const int* perm,
+                         int nkind, const int* kind, const double* cum, const double* mag, const double* rand,
+                         double* dE, double* dS3) {
+    const int N = s->N, per = 2 * N + 3;
+    int64_t ns = or_nsites(s);
+    double aE = 0, aS[3] = {0, 0, 0};
+    for (int k = 0; k < nsweeps; k++) {
+        int partial = (k == nsweeps - 1) && frac < 1.0;
+        for (int64_t idx = 0; idx < ns; idx++) {
+            int64_t site = perm[idx];
+            const double* r = rand + ((size_t)k * ns + site) * per;
+            if (partial && !(r[2 * N + 2] < frac)) continue;
+            int kd = kind[nkind - 1];
+            double m = mag[nkind - 1];
+            for (int i = 0; i < nkind - 1; i++)
+                if (r[2 * N] < cum[i]) { kd = kind[i]; m = mag[i]; break; }
+            if (kd == SGB_PROPOSE_DELTA && isinf(m)) kd = SGB_PROPOSE_UNIFORM;
+            const double kap = s->kappa[site];
+            double zn[16];
+            const double* z0 = Z + 2 * (size_t)N * site;
+            if (kd == SGB_PROPOSE_FLIP) {       /* flip_ket: reverse(parity .* conj(z)) */
+                for (int q = 0; q < N; q++) {
+                    int src = N - 1 - q;
+                    double par = (src % 2) ? -1.0 : 1.0;
+                    zn[2 * q] = par * z0[2 * src];
+                    zn[2 * q + 1] = -par * z0[2 * src + 1];
+                }
+            } else {
+                for (int q = 0; q < 2 * N; q++) zn[q] = kd == SGB_PROPOSE_UNIFORM ? r[q] : z0[q] + m * sqrt(kap) * r[q];
+                double n2 = 0;
+                for (int q = 0; q < 2 * N; q++) n2 += zn[q] * zn[q];
+                double d = sqrt(n2 / kap);   /* normalize_ket */
+                for (int q = 0; q < 2 * N; q++) zn[q] = kap == 0 ? 0 : zn[q] / d;
+            }
+            double e = or_local_energy_change_sun(s, S, Z, site, zn);
+            int accept = kT == 0.0 ? (e <= 0.0) : (r[2 * N + 1] <= exp(-e / kT));
+            if (accept) {
+                double sn[3];
+                or_expected_spin(N, zn, sn);
+                aE += e;
+                for (int c = 0; c < 3; c++) { aS[c] += sn[c] - S[3 * site + c]; S[3 * site + c] = sn[c]; }
+                for (int q = 0; q < 2 * N; q++) Z[2 * (size_t)N * site + q] = zn[q];
+            }
+        }
+    }
+    if (dE) *dE = aE;
+    if (dS3) { dS3[0] = aS[0]; dS3[1] = aS[1]; dS3[2] = aS[2]; }
+}
+
 void or_local_sweeps(const or_sys* s, double* S, double kT, int nsweeps, double frac, const int* perm,
                      int nkind, const int* kind, const double* cum, const double* mag, const double* rand,
                      double* dE, double* dS3) {

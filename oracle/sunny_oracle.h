@@ -88,6 +88,14 @@ void or_local_sweeps(const or_sys* s, double* S, double kT, int nsweeps, double 
                      int nkind, const int* kind, const double* cum, const double* mag, const double* rand,
                      double* dE, double* dS3);
 
+/* The same for SU(N) mode: Z [ns][N][2] kets, S [ns][3] their expected dipoles; Znew
+ * [N][2]; rand [nsweeps][ns][2N+3] (N complex normals as (re, im), then the mixture,
+ * acceptance and participation uniforms). Updates Z and S. */
+double or_local_energy_change_sun(const or_sys* s, const double* S, const double* Z, int64_t site, const double* Znew);
+void or_local_sweeps_sun(const or_sys* s, double* S, double* Z, double kT, int nsweeps, double frac, const int* perm,
+                         int nkind, const int* kind, const double* cum, const double* mag, const double* rand,
+                         double* dE, double* dS3);
+
 /* Dipole-dipole Ewald matrices (Ewald.jl:40-146 precompute_dipole_ewald at q = 0):
  * A[cell][i][j] (3x3 column-major, cell = c1 + L1*(c2 + L2*c3) is the offset of atom j's
  * cell from atom i's), times mu0_muB2. latvecs: 3x3 column-major lattice vectors of the

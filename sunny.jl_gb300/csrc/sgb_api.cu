@@ -453,7 +453,7 @@ int ensure_colors(sgb_system* s) {
 template <class R>
 int run_local_sweeps(sgb_system* s, McArgs& A, const double* rnd_host, double* out4) {
     int bps = 0;
-    if (mc_max_blocks<R>((size_t)s->tables_bytes, &bps) != SGB_OK || bps < 1)
+    if ((s->sun ? sun_mc_max_blocks<R>(model<R>(s), &bps) : mc_max_blocks<R>((size_t)s->tables_bytes, &bps)) != SGB_OK || bps < 1)
         return fail(s, SGB_ERR_CUDA, "occupancy query failed");
     int maxclass = 1;
     for (int c = 0; c < A.ncol; c++) maxclass = std::max(maxclass, A.coff[c + 1] - A.coff[c]);
@@ -468,7 +468,7 @@ int run_local_sweeps(sgb_system* s, McArgs& A, const double* rnd_host, double* o
         s->mc_part_cap = grid;
     }
     const int total = A.nsweeps;
-    const size_t per = (size_t)6 * s->ns;
+    const size_t per = (size_t)(s->sun ? 2 * s->N + 3 : 6) * s->ns;
     int chunk = total;
     if (rnd_host) {
         chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)total, ((size_t)1 << 24) / per));
@@ -488,7 +488,8 @@ int run_local_sweeps(sgb_system* s, McArgs& A, const double* rnd_host, double* o
             a.rnd = s->dbuf;
         }
         if ((rc = reset_ctrl(s))) return rc;
-        rc = mc_launch_sweeps<R>(model<R>(s), (R*)s->S, s->ctrl, a, grid, s->mc_part, s->stream);
+        rc = s->sun ? sun_launch_local_sweeps<R>(model<R>(s), (R*)s->Z, (R*)s->S, (R*)s->Q, s->ctrl, a, grid, s->mc_part, s->stream)
+                    : mc_launch_sweeps<R>(model<R>(s), (R*)s->S, s->ctrl, a, grid, s->mc_part, s->stream);
         s->launches++;
         if (rc) return cuda_fail(s, cudaGetLastError(), "LocalSampler launch");
         if ((rc = util_launch_reduce(s->mc_part, grid, 4, s->red, s->stream))) return cuda_fail(s, cudaGetLastError(), "reduce launch");
@@ -945,7 +946,6 @@ int sgb_midpoint(sgb_system* s, double dt, double damping, double tol, int32_t m
 int sgb_local_sweeps(sgb_system* s, double kT, double nsweeps, const sgb_proposal* prop, uint64_t seed, uint64_t sweep0,
                      const double* rand, double* dE, double* dS3) {
     if (!s) return fail(s, SGB_ERR_ARG, "null handle");
-    if (s->sun) return fail(s, SGB_ERR_ARG, "LocalSampler on the GPU supports the dipole modes");
     if (s->ewald_on) return fail(s, SGB_ERR_ARG, "LocalSampler with dipole-dipole interactions is not supported on the GPU");
     if (!(kT >= 0)) return fail(s, SGB_ERR_ARG, "Select nonnegative kT");
     if (!(nsweeps >= 0) || nsweeps > 1e9) return fail(s, SGB_ERR_ARG, "nsweeps must be nonnegative");
@@ -1188,15 +1188,21 @@ int sgb_local_colors(sgb_system* s, int32_t* ncolors, int32_t* color) {
 
 int sgb_local_energy_change(sgb_system* s, int64_t site, const double* S_new, double* dE) {
     if (!s || !S_new || !dE) return fail(s, SGB_ERR_ARG, "null argument");
-    if (s->sun) return fail(s, SGB_ERR_ARG, "LocalSampler on the GPU supports the dipole modes");
     if (s->ewald_on) return fail(s, SGB_ERR_ARG, "LocalSampler with dipole-dipole interactions is not supported on the GPU");
     if (site < 0 || site >= s->ns) return fail(s, SGB_ERR_ARG, "site out of range");
     int rc = ensure_colors(s);   // also rejects self-interaction
     if (rc) return rc;
     if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called first");
     if ((rc = ensure_dbuf(s, 1))) return rc;
-    rc = s->fp32 ? mc_launch_local_dE<float>(s->mf, (const float*)s->S, (int)site, S_new[0], S_new[1], S_new[2], s->dbuf, s->stream)
-                 : mc_launch_local_dE<double>(s->md, (const double*)s->S, (int)site, S_new[0], S_new[1], S_new[2], s->dbuf, s->stream);
+    if (s->sun) {
+        SunKet zk{};
+        for (int q = 0; q < 2 * s->N; q++) zk.v[q] = S_new[q];
+        rc = s->fp32 ? sun_launch_local_dE<float>(s->mf, (const float*)s->Z, (const float*)s->S, (const float*)s->Q, (int)site, zk, s->dbuf, s->stream)
+                     : sun_launch_local_dE<double>(s->md, (const double*)s->Z, (const double*)s->S, (const double*)s->Q, (int)site, zk, s->dbuf, s->stream);
+    } else {
+        rc = s->fp32 ? mc_launch_local_dE<float>(s->mf, (const float*)s->S, (int)site, S_new[0], S_new[1], S_new[2], s->dbuf, s->stream)
+                     : mc_launch_local_dE<double>(s->md, (const double*)s->S, (int)site, S_new[0], S_new[1], S_new[2], s->dbuf, s->stream);
+    }
     s->launches++;
     if (rc) return cuda_fail(s, cudaGetLastError(), "local energy launch");
     CK(cudaMemcpyAsync(dE, s->dbuf, sizeof(double), cudaMemcpyDeviceToHost, s->stream));

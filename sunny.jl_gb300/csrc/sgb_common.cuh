@@ -194,6 +194,23 @@ __device__ inline void sgb_normals4(uint64_t seed, uint32_t stream, uint64_t ste
     }
 }
 
+// Four uniforms in (0, 1) for the LocalSampler's Metropolis draws of (seed, sweep, site),
+// on a Philox stream of their own.
+#define SGB_MC_STREAM 0x80000001u
+__device__ inline void sgb_mc_uniforms4(uint64_t seed, uint64_t sweep, uint32_t site, double u[4]) {
+    Philox4 c;
+    c.x = site;
+    c.y = (uint32_t)sweep;
+    c.z = (uint32_t)(sweep >> 32) ^ (1u << 24);
+    c.w = SGB_MC_STREAM;
+    Philox4 r = sgb_philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const double s = 2.3283064365386963e-10;   // 2^-32
+    u[0] = ((double)r.x + 0.5) * s;
+    u[1] = ((double)r.y + 0.5) * s;
+    u[2] = ((double)r.z + 0.5) * s;
+    u[3] = ((double)r.w + 0.5) * s;
+}
+
 // ---------------------------------------------------------------------------------
 // Small helpers
 // ---------------------------------------------------------------------------------

@@ -109,6 +109,15 @@ int mc_max_blocks(size_t smem, int* blocks_per_sm);
 template <class R>
 int mc_launch_local_dE(const Model<R>& M, const R* S, int site, double nx, double ny, double nz, double* out,
                        cudaStream_t st);
+struct SunKet { double v[10]; };   // one coherent state, (re, im) per component, N <= 5
+template <class R>
+int sun_launch_local_sweeps(const Model<R>& M, R* Z, R* D, R* Q, Ctrl* ctrl, const McArgs& A, int grid, double* part,
+                            cudaStream_t st);
+template <class R>
+int sun_mc_max_blocks(const Model<R>& M, int* bps);
+template <class R>
+int sun_launch_local_dE(const Model<R>& M, const R* Z, const R* D, const R* Q, int site, const SunKet& zk, double* out,
+                        cudaStream_t st);
 
 // ---- minimize_energy! vector kernels (sgb_opt.cu), FP64 dipole state ----
 int opt_grid(int ns);   // blocks of every partial-writing kernel below

@@ -21,23 +21,6 @@
 namespace {
 using namespace sgbdev;
 
-constexpr uint32_t kMcStream = 0x80000001u;   // Philox stream tag of the Metropolis draws
-
-// Four uniforms in (0, 1) for (seed, sweep, site).
-__device__ inline void mc_uniforms4(uint64_t seed, uint64_t sweep, uint32_t site, double u[4]) {
-    Philox4 c;
-    c.x = site;
-    c.y = (uint32_t)sweep;
-    c.z = (uint32_t)(sweep >> 32) ^ (1u << 24);
-    c.w = kMcStream;
-    Philox4 r = sgb_philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-    const double s = 2.3283064365386963e-10;   // 2^-32
-    u[0] = ((double)r.x + 0.5) * s;
-    u[1] = ((double)r.y + 0.5) * s;
-    u[2] = ((double)r.z + 0.5) * s;
-    u[3] = ((double)r.w + 0.5) * s;
-}
-
 // local_energy_change (Interactions.jl:311-373) for a dipole: S at `site` goes from o to
 // n. Every bond of the site's sublattice is visited (the reversed copies carry J^T and
 // the transposed biquadratic matrix), as Sunny's per-site pair list is.
@@ -122,7 +105,7 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_local_sweeps(Model<R> M, R* S, Ct
                     rr = A.rnd + ((size_t)k * ns + site) * 6;
                     u[0] = rr[3]; u[1] = rr[4]; u[2] = rr[5];
                 } else {
-                    mc_uniforms4(A.seed, sweep, (uint32_t)site, u);
+                    sgb_mc_uniforms4(A.seed, sweep, (uint32_t)site, u);
                 }
                 if (partial && !(u[2] < A.frac)) continue;
                 int kind = A.kind[A.nkind - 1];
@@ -138,7 +121,7 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_local_sweeps(Model<R> M, R* S, Ct
                 } else {
                     R g[4];
                     if (INJECT) { g[0] = (R)rr[0]; g[1] = (R)rr[1]; g[2] = (R)rr[2]; }
-                    else sgb_normals4<R>(A.seed, kMcStream, sweep, (uint32_t)site, 0u, g);
+                    else sgb_normals4<R>(A.seed, SGB_MC_STREAM, sweep, (uint32_t)site, 0u, g);
                     if (kind == SGB_PROPOSE_UNIFORM) {
                         nx = g[0]; ny = g[1]; nz = g[2];
                     } else {

@@ -655,6 +655,239 @@ int grid1d(const Model<R>& M) {
     return grid > 4096 ? 4096 : grid;
 }
 
+// ---- LocalSampler in SU(N) mode (Samplers.jl:139-158, Interactions.jl:311-373) --------
+// <z|Λ|z> of one ket (the onsite energy, Interactions.jl:331-332)
+template <class R, int N>
+__device__ __forceinline__ R onsite_energy(const R* lam, const R* z) {
+    R acc = 0;
+#pragma unroll
+    for (int c = 0; c < N; c++)
+#pragma unroll
+        for (int r = 0; r < N; r++) {
+            const R lr = lam[2 * (r + N * c)], li = lam[2 * (r + N * c) + 1];
+            const R tr = lr * z[2 * c] - li * z[2 * c + 1], ti = lr * z[2 * c + 1] + li * z[2 * c];
+            acc += z[2 * r] * tr + z[2 * r + 1] * ti;
+        }
+    return acc;
+}
+
+// local_energy_change for a coherent state: ket z0 (dipole s0, quadrupole q0) at `site`
+// becomes zn (sn, qn); neighbours enter through their expected dipoles and quadrupoles.
+template <class R, int N, bool BQ>
+__device__ inline R sun_local_dE(const Model<R>& M, const SunTab<R, N>& S, int site, const R* D, const R* Qb,
+                                 const R* z0, const R* s0, const R* q0, const R* zn, const R* sn, const R* qn) {
+    const int ns = M.ns, a = site / M.ncell;
+    const R dx = sn[0] - s0[0], dy = sn[1] - s0[1], dz = sn[2] - s0[2];
+    R dE = 0;
+    if (M.h) dE += M.h[site] * dx + M.h[ns + site] * dy + M.h[2 * ns + site] * dz;
+    const R* lam = S.lam + a * 2 * N * N;
+    dE += onsite_energy<R, N>(lam, zn) - onsite_energy<R, N>(lam, z0);
+    for (int b = S.t.boff[a], k = 0; b < S.t.boff[a + 1]; b++, k++) {
+        const DBond<R>& B = S.t.bonds[b];
+        const int j = M.nbr[(size_t)k * ns + site];
+        const R tx = sgb_ld(D + j), ty = sgb_ld(D + ns + j), tz = sgb_ld(D + 2 * ns + j);
+        if (B.jkind == 0) {
+            dE += B.J[0] * (dx * tx + dy * ty + dz * tz);
+        } else {
+            dE += dx * (B.J[0] * tx + B.J[3] * ty + B.J[6] * tz) + dy * (B.J[1] * tx + B.J[4] * ty + B.J[7] * tz) +
+                  dz * (B.J[2] * tx + B.J[5] * ty + B.J[8] * tz);
+        }
+        if (BQ && B.bqkind != 0) {
+            R Qj[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) Qj[q] = sgb_ld(Qb + (size_t)q * ns + j);
+            R acc = 0;
+            if (B.bqkind == 1) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) acc += (qn[q] - q0[q]) * ((R)biquad_metric(q) * Qj[q]);
+                acc *= B.bq;
+            } else {
+                const R* Bm = S.t.bq + 25 * B.bqidx;
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    R r = 0;
+#pragma unroll
+                    for (int p = 0; p < 5; p++) r += Bm[q + 5 * p] * Qj[p];
+                    acc += (qn[q] - q0[q]) * r;
+                }
+            }
+            dE += acc;
+        }
+    }
+    return dE;
+}
+
+// Colour-class sweeps as the dipole LocalSampler. Proposals: randspin (normalize_ket of a
+// complex normal vector, System.jl:448-452), flip_ket (Spin.jl:121-128), perturbed_spin
+// (Z + magnitude·√κ·ξ, System.jl:461-468); complex normals have E|ξ_k|² = 1 (Julia's
+// randn(ComplexF64)). Injected randoms: [sweep][ns][2N + 3].
+template <class R, int N, bool BQ, bool INJECT>
+__global__ void __launch_bounds__(SGB_BLOCK) k_sun_local_sweeps(Model<R> M, R* Z, R* D, R* Qb, Ctrl* ctrl, McArgs A,
+                                                               double* partials) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SunTab<R, N> S = stage_sun<R, N>(M, smem);
+    __syncthreads();
+    SpinConst<R, N> sc;
+    const int ns = M.ns;
+    const int nthr = gridDim.x * blockDim.x;
+    constexpr int PER = 2 * N + 3;
+    double aE = 0, ax = 0, ay = 0, az = 0;
+    bool ok = true;
+    for (int k = 0; k < A.nsweeps && ok; k++) {
+        const bool partial = (k == A.nsweeps - 1) && A.frac < 1.0;
+        const uint64_t sweep = A.sweep0 + (uint64_t)k;
+        for (int c = 0; c < A.ncol; c++) {
+            for (int idx = A.coff[c] + blockIdx.x * blockDim.x + threadIdx.x; idx < A.coff[c + 1]; idx += nthr) {
+                const int site = A.perm[idx];
+                double u[4];
+                const double* rr = nullptr;
+                if (INJECT) {
+                    rr = A.rnd + ((size_t)k * ns + site) * PER;
+                    u[0] = rr[2 * N]; u[1] = rr[2 * N + 1]; u[2] = rr[2 * N + 2];
+                } else {
+                    sgb_mc_uniforms4(A.seed, sweep, (uint32_t)site, u);
+                }
+                if (partial && !(u[2] < A.frac)) continue;
+                int kind = A.kind[A.nkind - 1];
+                double mag = A.mag[A.nkind - 1];
+                for (int i = 0; i < A.nkind - 1; i++)
+                    if (u[0] < A.cum[i]) { kind = A.kind[i]; mag = A.mag[i]; break; }
+                if (kind == SGB_PROPOSE_DELTA && isinf(mag)) kind = SGB_PROPOSE_UNIFORM;
+                const R kap = M.kappa[site];
+                R z0[2 * N], zn[2 * N];
+#pragma unroll
+                for (int q = 0; q < 2 * N; q++) z0[q] = Z[(size_t)q * ns + site];
+                if (kind == SGB_PROPOSE_FLIP) {
+#pragma unroll
+                    for (int q = 0; q < N; q++) {   // reverse(parity .* conj(z))
+                        const R par = ((N - 1 - q) % 2) ? (R)-1 : (R)1;
+                        zn[2 * q] = par * z0[2 * (N - 1 - q)];
+                        zn[2 * q + 1] = -par * z0[2 * (N - 1 - q) + 1];
+                    }
+                } else {
+                    R g[12];
+                    if (INJECT) {
+#pragma unroll
+                        for (int q = 0; q < 2 * N; q++) g[q] = (R)rr[q];
+                    } else {
+#pragma unroll
+                        for (int blk = 0; blk < (2 * N + 3) / 4; blk++) sgb_normals4<R>(A.seed, SGB_MC_STREAM, sweep, (uint32_t)site, (uint32_t)blk, g + 4 * blk);
+#pragma unroll
+                        for (int q = 0; q < 2 * N; q++) g[q] *= (R)0.70710678118654752;
+                    }
+                    if (kind == SGB_PROPOSE_UNIFORM) {
+#pragma unroll
+                        for (int q = 0; q < 2 * N; q++) zn[q] = g[q];
+                    } else {
+                        const R m = (R)mag * sgb_sqrt<R>(kap);
+#pragma unroll
+                        for (int q = 0; q < 2 * N; q++) zn[q] = z0[q] + m * g[q];
+                    }
+                    normalize_ket<R, N>(zn, kap);
+                }
+                R s0[3], sn[3], q0[5], qn[5];
+                s0[0] = D[site]; s0[1] = D[ns + site]; s0[2] = D[2 * ns + site];
+                expected_spin<R, N>(sc, zn, sn[0], sn[1], sn[2]);
+                if (BQ) {
+#pragma unroll
+                    for (int q = 0; q < 5; q++) q0[q] = Qb[(size_t)q * ns + site];
+                    expected_quad<R, N>(S.qm, zn, qn);
+                }
+                const R dE = sun_local_dE<R, N, BQ>(M, S, site, D, Qb, z0, s0, q0, zn, sn, qn);
+                const double e = (double)dE;
+                const bool accept = A.kT == 0.0 ? (e <= 0.0) : (u[1] <= exp(-e / A.kT));
+                if (accept) {
+#pragma unroll
+                    for (int q = 0; q < 2 * N; q++) Z[(size_t)q * ns + site] = zn[q];
+                    D[site] = sn[0]; D[ns + site] = sn[1]; D[2 * ns + site] = sn[2];
+                    if (BQ) {
+#pragma unroll
+                        for (int q = 0; q < 5; q++) Qb[(size_t)q * ns + site] = qn[q];
+                    }
+                    aE += e;
+                    ax += (double)sn[0] - (double)s0[0];
+                    ay += (double)sn[1] - (double)s0[1];
+                    az += (double)sn[2] - (double)s0[2];
+                }
+            }
+            if (!sgb_grid_barrier(ctrl, gridDim.x)) { ok = false; break; }
+        }
+    }
+    const double e = sgb_block_sum(aE);
+    const double s0 = sgb_block_sum(ax);
+    const double s1 = sgb_block_sum(ay);
+    const double s2 = sgb_block_sum(az);
+    if (threadIdx.x == 0) {
+        partials[4 * blockIdx.x + 0] = e;
+        partials[4 * blockIdx.x + 1] = s0;
+        partials[4 * blockIdx.x + 2] = s1;
+        partials[4 * blockIdx.x + 3] = s2;
+    }
+}
+
+template <class R, int N, bool BQ>
+__global__ void k_sun_local_dE(Model<R> M, const R* Z, const R* D, const R* Qb, int site, SunKet zk, double* out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SunTab<R, N> S = stage_sun<R, N>(M, smem);
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    SpinConst<R, N> sc;
+    const int ns = M.ns;
+    R z0[2 * N], zn[2 * N], s0[3], sn[3], q0[5], qn[5];
+#pragma unroll
+    for (int q = 0; q < 2 * N; q++) { z0[q] = Z[(size_t)q * ns + site]; zn[q] = (R)zk.v[q]; }
+    s0[0] = D[site]; s0[1] = D[ns + site]; s0[2] = D[2 * ns + site];
+    expected_spin<R, N>(sc, zn, sn[0], sn[1], sn[2]);
+    if (BQ) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) q0[q] = Qb[(size_t)q * ns + site];
+        expected_quad<R, N>(S.qm, zn, qn);
+    }
+    *out = (double)sun_local_dE<R, N, BQ>(M, S, site, D, Qb, z0, s0, q0, zn, sn, qn);
+}
+
+template <class R, int N>
+int sun_sweeps_n(const Model<R>& M, R* Z, R* D, R* Q, Ctrl* ctrl, const McArgs& A, int grid, double* part,
+                 cudaStream_t st) {
+    Model<R> m = M;
+    McArgs a = A;
+    void* args[] = {&m, &Z, &D, &Q, &ctrl, &a, &part};
+    const size_t smem = (size_t)M.tables_bytes;
+    const bool bq = M.has_biquad != 0, inj = A.rnd != nullptr;
+    const void* k = bq ? (inj ? (const void*)k_sun_local_sweeps<R, N, true, true> : (const void*)k_sun_local_sweeps<R, N, true, false>)
+                       : (inj ? (const void*)k_sun_local_sweeps<R, N, false, true> : (const void*)k_sun_local_sweeps<R, N, false, false>);
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return SGB_ERR_CUDA;
+    return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(SGB_BLOCK), args, smem, st) == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+template <class R, int N>
+int sun_mc_occ_n(size_t smem, int* bps) {
+    int best = 1 << 30, a = 0;
+    const void* ks[4] = {(const void*)k_sun_local_sweeps<R, N, true, true>, (const void*)k_sun_local_sweeps<R, N, true, false>,
+                         (const void*)k_sun_local_sweeps<R, N, false, true>, (const void*)k_sun_local_sweeps<R, N, false, false>};
+    for (const void* k : ks) {
+        if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return SGB_ERR_CUDA;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k, SGB_BLOCK, smem) != cudaSuccess) return SGB_ERR_CUDA;
+        best = a < best ? a : best;
+    }
+    *bps = best;
+    return SGB_OK;
+}
+
+template <class R, int N>
+int sun_dE_n(const Model<R>& M, const R* Z, const R* D, const R* Q, int site, const SunKet& zk, double* out, cudaStream_t st) {
+    const size_t smem = (size_t)M.tables_bytes;
+    const void* k = M.has_biquad ? (const void*)k_sun_local_dE<R, N, true> : (const void*)k_sun_local_dE<R, N, false>;
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return SGB_ERR_CUDA;
+    Model<R> m = M;
+    SunKet z = zk;
+    void* args[] = {&m, &Z, &D, &Q, &site, &z, &out};
+    return cudaLaunchKernel(k, dim3(1), dim3(32), args, smem, st) == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
 }  // namespace
 
 #define SGB_SUN_DISPATCH(EXPR2, EXPR3, EXPR4, EXPR5) \
@@ -737,6 +970,27 @@ int sun_launch_energy(const Model<R>& M, const R* Z, const R* D, const R* Q, dou
                      (energy_n<R, 4>(M, Z, D, Q, partials, nblocks, st)), (energy_n<R, 5>(M, Z, D, Q, partials, nblocks, st)))
 }
 
+template <class R>
+int sun_launch_local_sweeps(const Model<R>& M, R* Z, R* D, R* Q, Ctrl* ctrl, const McArgs& A, int grid, double* part,
+                            cudaStream_t st) {
+    SGB_SUN_DISPATCH((sun_sweeps_n<R, 2>(M, Z, D, Q, ctrl, A, grid, part, st)), (sun_sweeps_n<R, 3>(M, Z, D, Q, ctrl, A, grid, part, st)),
+                     (sun_sweeps_n<R, 4>(M, Z, D, Q, ctrl, A, grid, part, st)), (sun_sweeps_n<R, 5>(M, Z, D, Q, ctrl, A, grid, part, st)))
+}
+
+template <class R>
+int sun_mc_max_blocks(const Model<R>& M, int* bps) {
+    const size_t smem = (size_t)M.tables_bytes;
+    SGB_SUN_DISPATCH((sun_mc_occ_n<R, 2>(smem, bps)), (sun_mc_occ_n<R, 3>(smem, bps)), (sun_mc_occ_n<R, 4>(smem, bps)),
+                     (sun_mc_occ_n<R, 5>(smem, bps)))
+}
+
+template <class R>
+int sun_launch_local_dE(const Model<R>& M, const R* Z, const R* D, const R* Q, int site, const SunKet& zk, double* out,
+                        cudaStream_t st) {
+    SGB_SUN_DISPATCH((sun_dE_n<R, 2>(M, Z, D, Q, site, zk, out, st)), (sun_dE_n<R, 3>(M, Z, D, Q, site, zk, out, st)),
+                     (sun_dE_n<R, 4>(M, Z, D, Q, site, zk, out, st)), (sun_dE_n<R, 5>(M, Z, D, Q, site, zk, out, st)))
+}
+
 #define SGB_SUN_INST(R)                                                                                         \
     template int sun_launch_heun<R>(const Model<R>&, R*, R*, R*, R*, R*, Ctrl*, int, double, double, double,    \
                                     uint64_t, uint64_t, const double*, const LaunchInfo&, cudaStream_t);        \
@@ -745,6 +999,9 @@ int sun_launch_energy(const Model<R>& M, const R* Z, const R* D, const R* Q, dou
     template int sun_max_blocks<R>(int, int, int, size_t, int*);                                                     \
     template int sun_launch_refresh<R>(const Model<R>&, const R*, R*, R*, cudaStream_t);                        \
     template int sun_launch_grad<R>(const Model<R>&, const R*, const R*, const R*, double*, cudaStream_t);      \
-    template int sun_launch_energy<R>(const Model<R>&, const R*, const R*, const R*, double*, int, cudaStream_t);
+    template int sun_launch_energy<R>(const Model<R>&, const R*, const R*, const R*, double*, int, cudaStream_t); \
+    template int sun_launch_local_sweeps<R>(const Model<R>&, R*, R*, R*, Ctrl*, const McArgs&, int, double*, cudaStream_t); \
+    template int sun_mc_max_blocks<R>(const Model<R>&, int*);                                                    \
+    template int sun_launch_local_dE<R>(const Model<R>&, const R*, const R*, const R*, int, const SunKet&, double*, cudaStream_t);
 SGB_SUN_INST(float)
 SGB_SUN_INST(double)

@@ -640,21 +640,23 @@ def clone_system(sys: System, seed=None) -> System:
 def _local_sampler_steps(sys: System, sampler: LocalSampler, nsteps: int, rand) -> int:
     """`nsteps` x step!(sys, sampler) (Samplers.jl:139-158). Random numbers come from the
     device generator keyed by (sys.seed, sweep counter), or from `rand`
-    ([sweeps][ns][6]: 3 normals, mixture, acceptance and participation uniforms)."""
+    ([sweeps][ns][6]: 3 normals, mixture, acceptance and participation uniforms; in SU(N)
+    mode [sweeps][ns][2N+3], N complex normals as (re, im) first)."""
     sys._sync_to_device()
     lib, h = sys._lib, sys._h
     per_step = math.ceil(sampler.nsweeps)
+    per_site = 2 * sys.N + 3 if sys.N else 6
     if rand is not None:
         rand = np.ascontiguousarray(rand, dtype=float).reshape(-1)
-        if rand.size != per_step * nsteps * sys.nsites * 6:
-            raise ValueError("rand must hold sweeps x nsites x 6 numbers")
+        if rand.size != per_step * nsteps * sys.nsites * per_site:
+            raise ValueError(f"rand must hold sweeps x nsites x {per_site} numbers")
     prop = sampler.propose.cstruct()
     # integer sweeps fuse into one launch; a fractional sweep ends every step
     calls = [(sampler.nsweeps * nsteps, 0)] if sampler.nsweeps == per_step else \
         [(sampler.nsweeps, k * per_step) for k in range(nsteps)]
     dE, dS = C.c_double(), np.zeros(3)
     for nsw, k0 in calls:
-        r = None if rand is None else rand[k0 * sys.nsites * 6:]
+        r = None if rand is None else rand[k0 * sys.nsites * per_site:]
         rc = lib.sgb_local_sweeps(h, sampler.kT, nsw, C.byref(prop), sys.seed, sys.mc_sweep, _abi.dptr(r), C.byref(dE),
                                   _abi.dptr(dS))
         sys._dev_newer = True
@@ -693,11 +695,15 @@ def minimize_energy(sys: System, maxiters: int = 1000, jitter: float = 1e-8) -> 
 
 
 def local_energy_change(sys: System, site: int, S_new) -> float:
-    """local_energy_change(sys, site, state) (Interactions.jl:311-373), dipole modes;
-    `site` is the 0-based linear index."""
+    """local_energy_change(sys, site, state) (Interactions.jl:311-373); `site` is the
+    0-based linear index; S_new is a dipole, or a coherent state (N complex) in SU(N) mode."""
     sys._sync_to_device()
     out = C.c_double()
-    Sn = np.ascontiguousarray(S_new, dtype=float).reshape(3)
+    if sys.N:
+        z = np.asarray(S_new, dtype=complex).reshape(sys.N)
+        Sn = np.ascontiguousarray(np.stack([z.real, z.imag], -1).reshape(-1))
+    else:
+        Sn = np.ascontiguousarray(S_new, dtype=float).reshape(3)
     _abi.check(sys._lib.sgb_local_energy_change(sys._h, int(site), _abi.dptr(Sn), C.byref(out)), sys._lib, sys._h)
     return out.value
 

@@ -152,12 +152,64 @@ def test_single_ion_energy(gpu, sg):
     assert np.mean(sz2) == pytest.approx(exact, rel=0.02)
 
 
-def test_rejects_sun_and_self_bonds(gpu, sg):
-    s = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "SUN", dims=(2, 2, 2), seed=1, device=0)
-    s.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
-    s.randomize_spins()
-    with pytest.raises(sg.SunnyGPUError, match="dipole modes"):
-        sg.step(s, sg.LocalSampler(kT=0.1))
+def test_sun_local_energy_change(gpu, sg, orc):
+    from models import rich_sun
+    sys_ = rich_sun(sg, N=3)
+    o = oracle_of(orc, sys_)
+    Z = sys_.coherents_flat()
+    S = o.expected_spin(Z)
+    E0 = sg.energy(sys_)
+    rng = np.random.default_rng(12)
+    for _ in range(5):
+        i = int(rng.integers(0, sys_.nsites))
+        z = rng.standard_normal(3) + 1j * rng.standard_normal(3)
+        z /= np.linalg.norm(z)
+        dE = sg.local_energy_change(sys_, i, z)
+        assert dE == pytest.approx(o.local_energy_change(S, i, z, Z), abs=1e-12 * max(1.0, abs(E0)))
+
+
+@pytest.mark.parametrize("N", [3, 4])
+def test_sun_sweeps_match_oracle_injected(gpu, sg, orc, N):
+    from models import rich_sun
+    sys_ = rich_sun(sg, N=N)
+    o = oracle_of(orc, sys_)
+    Z0 = sys_.coherents_flat()
+    S0 = o.expected_spin(Z0)
+    ncol, col = sg.local_colors(sys_)
+    order = np.lexsort((np.arange(sys_.nsites), col))
+    rng = np.random.default_rng(13)
+    rand = np.concatenate([rng.standard_normal((2, sys_.nsites, 2 * N)) / np.sqrt(2), rng.random((2, sys_.nsites, 3))], axis=2)
+    prop = sg.mix_proposals(0.3, sg.propose_uniform, 0.3, sg.propose_flip, 0.4, sg.propose_delta(0.5))
+    smp = sg.LocalSampler(kT=0.7, nsweeps=2, propose=prop)
+    sg.step(sys_, smp, 1, rand)
+    S_ref, Z_ref, dE_ref, dS_ref = o.local_sweeps_sun(S0, Z0, 0.7, 2, 1.0, order, prop.terms, rand)
+    Z_gpu = sys_.coherents_flat()
+    assert np.max(np.abs(Z_gpu - Z_ref)) < 1e-12
+    assert not np.allclose(Z_gpu, Z0)
+    assert smp.ΔE == pytest.approx(dE_ref, abs=1e-10)
+    assert np.allclose(smp.ΔS, dS_ref, atol=1e-10)
+    assert np.allclose(sys_.dipoles_flat(), S_ref, atol=1e-12)
+
+
+def test_sun_anisotropy_energy(gpu, sg):
+    # SU(3) spins with Λ = D Sz², no couplings (test_samplers.jl:5-10, 61-80): the exact
+    # thermal mean energy, here sampled by the LocalSampler
+    D, kT = 1.0, 0.5
+    sys_ = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "SUN", dims=(16, 16, 16), seed=14)
+    sys_.set_onsite_coupling(lambda Sx, Sy, Sz: D * Sz @ Sz, 1)
+    sys_.randomize_spins()
+    smp = sg.LocalSampler(kT=kT)
+    sg.step(sys_, smp, 50)
+    Es = []
+    for _ in range(100):
+        sg.step(sys_, smp, 1)
+        Es.append(sg.energy_per_site(sys_))
+    a = D / kT
+    exact = D * (2 - (2 + 2 * a + a * a) * math.exp(-a)) / (a * (1 - (1 + a) * math.exp(-a)))
+    assert np.mean(Es) == pytest.approx(exact, rel=0.02)
+
+
+def test_rejects_self_bonds(gpu, sg):
     d = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=(1, 2, 2), seed=1, device=0)
     d.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
     d.randomize_spins()

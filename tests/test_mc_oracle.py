@@ -87,3 +87,39 @@ def test_clone_system_copies_couplings_and_state(sg, orc):
     assert orc.OracleSystem.from_system(c).energy(S) == orc.OracleSystem.from_system(s).energy(S)
     c.set_state_flat(dipoles=-S)
     assert np.array_equal(s.dipoles_flat(), S)
+
+
+def test_oracle_sun_local_energy_change_is_energy_difference(sg, orc):
+    from models import rich_sun
+    rng = np.random.default_rng(5)
+    for N in (3, 4):   # rich_sun sets an onsite term, which spin 1/2 rejects
+        sys_ = rich_sun(sg, N=N, device=None)
+        o = orc.OracleSystem.from_system(sys_)
+        Z = sys_.coherents_flat()
+        S = o.expected_spin(Z)
+        E0 = o.energy(S, Z)
+        for _ in range(4):
+            i = int(rng.integers(0, sys_.nsites))
+            z = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+            z /= np.linalg.norm(z)
+            dE = o.local_energy_change(S, i, z, Z)
+            Z1 = Z.copy()
+            Z1[i] = z
+            assert dE == pytest.approx(o.energy(o.expected_spin(Z1), Z1) - E0, abs=1e-12 * max(1.0, abs(E0)))
+
+
+def test_oracle_sun_local_sweeps_bookkeeping(sg, orc):
+    from models import rich_sun
+    sys_ = rich_sun(sg, N=3, device=None)
+    o = orc.OracleSystem.from_system(sys_)
+    Z0 = sys_.coherents_flat()
+    S0 = o.expected_spin(Z0)
+    rng = np.random.default_rng(6)
+    ns, N = sys_.nsites, 3
+    rand = np.concatenate([rng.standard_normal((2, ns, 2 * N)) / np.sqrt(2), rng.random((2, ns, 3))], axis=2)
+    prop = [(0, 0.3, 0.0), (1, 0.3, 0.0), (2, 0.4, 0.5)]
+    S1, Z1, dE, dS = o.local_sweeps_sun(S0, Z0, 0.8, 2, 1.0, np.arange(ns), prop, rand)
+    assert not np.allclose(Z1, Z0)
+    assert np.allclose(S1, o.expected_spin(Z1), atol=1e-13)
+    assert dE == pytest.approx(o.energy(S1, Z1) - o.energy(S0, Z0), abs=1e-10)
+    assert np.allclose(dS, S1.sum(0) - S0.sum(0), atol=1e-10)
