@@ -220,8 +220,8 @@ int sgb_local_colors(sgb_system* sys, int32_t* ncolors, int32_t* color);
  * modes, a coherent state [N][2] in SU(N) mode. */
 int sgb_local_energy_change(sgb_system* sys, int64_t site, const double* S_new, double* dE);
 
-/* minimize_energy!(sys; maxiters, jitter) (Optimization.jl:102-166), dipole modes, FP64
- * systems: perturb every spin by `jitter` (perturbed_spin with normals keyed by seed),
+/* minimize_energy!(sys; maxiters, jitter) (Optimization.jl:102-166), dipole and SU(N)
+ * modes, FP64 systems: perturb every spin by `jitter` (perturbed_spin with normals keyed by seed),
  * then conjugate-gradient descent on the unit spheres until the largest gradient
  * component is <= 1e-12 * characteristic_energy_scale or the largest step component is
  * <= 1e-12. The state is left at the minimiser; converged/niters/energy_out (nullable)

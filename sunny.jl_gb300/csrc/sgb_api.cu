@@ -995,7 +995,9 @@ int sgb_local_sweeps(sgb_system* s, double kT, double nsweeps, const sgb_proposa
     return SGB_OK;
 }
 
-// minimize_energy! (Optimization.jl:102-166), dipole modes, FP64 systems. Riemannian
+// minimize_energy! (Optimization.jl:102-166), FP64 systems: dipoles, or coherent states
+// (gradient HZ, complex tangent projection; the dipoles and quadrupoles are refreshed
+// from the kets before every evaluation). Riemannian
 // nonlinear conjugate gradient on the unit spheres: Hager-Zhang β with the η = 0.4 lower
 // bound (Optim.jl ConjugateGradient defaults), a bracketing line search (secant on φ',
 // else bisection) on φ(α) = E(κ·normalize(x + α d)) that accepts the strong Wolfe
@@ -1008,7 +1010,6 @@ int sgb_local_sweeps(sgb_system* s, double kT, double nsweeps, const sgb_proposa
 int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t seed, int32_t* converged,
                         int32_t* niters, double* energy_out) {
     if (!s) return fail(s, SGB_ERR_ARG, "null handle");
-    if (s->sun) return fail(s, SGB_ERR_ARG, "minimize_energy on the GPU supports the dipole modes");
     if (s->fp32) return fail(s, SGB_ERR_ARG, "minimize_energy needs an FP64 system (its tolerances are 1e-12)");
     if (maxiters < 0 || !(jitter >= 0)) return fail(s, SGB_ERR_ARG, "invalid maxiters or jitter");
     int rc = ensure_tables(s);
@@ -1016,21 +1017,23 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
     if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called first");
     const int ns = s->ns;
     const int grid = opt_grid(ns);
+    const int K = s->sun ? 2 * s->N : 3;            // reals per site
+    const double gdiv = s->sun ? 2.0 : 1.0;          // the kernels' ket gradient is 2·√κ·HZ
     double *x = nullptr, *g = nullptr, *d = nullptr, *grad = nullptr, *part = nullptr;
     struct Guard {
         double** p[5];
         ~Guard() { for (auto q : p) if (*q) { cudaFree(*q); *q = nullptr; } }
     } guard{{&x, &g, &d, &grad, &part}};
-    const size_t vb = sizeof(double) * 3 * (size_t)ns;
+    const size_t vb = sizeof(double) * K * (size_t)ns;
     if ((rc = dmalloc(s, (void**)&x, vb)) || (rc = dmalloc(s, (void**)&g, vb)) || (rc = dmalloc(s, (void**)&d, vb)) ||
         (rc = dmalloc(s, (void**)&grad, vb)) || (rc = dmalloc(s, (void**)&part, sizeof(double) * 10 * grid)))
         return rc;
-    double* S = (double*)s->S;
+    double* S = (double*)(s->sun ? s->Z : s->S);   // the optimised state: dipoles or kets
     const double* kap = (const double*)s->kappa;
     cudaStream_t st = s->stream;
     CK(cudaMemsetAsync(g, 0, vb, st));
     CK(cudaMemsetAsync(d, 0, vb, st));
-    if (opt_launch_init(S, kap, ns, jitter, seed, x, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
+    if (opt_launch_init(K, S, kap, ns, jitter, seed, x, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
     const int nbE = std::min(SGB_ENERGY_BLOCKS, (ns + SGB_BLOCK - 1) / SGB_BLOCK);
     std::vector<double> hp(10 * (size_t)grid);
     auto pull = [&](int K, double* out, const bool* is_max) -> int {
@@ -1047,15 +1050,23 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
     // E and φ'(α) at κ·normalize(x + α d); the gradient stays in `grad`
     auto eval = [&](double alpha, double* f, double* dphi) -> int {
         nevals++;
-        if (opt_launch_point(x, d, alpha, kap, ns, S, st) || dip_launch_grad<double>(s->md, S, grad, st) ||
-            dip_launch_energy<double>(s->md, S, s->partials, nbE, st) || util_launch_reduce(s->partials, nbE, 4, s->red, st))
-            return cuda_fail(s, cudaGetLastError(), "optimizer evaluation");
+        int lrc;
+        if (!s->sun) {
+            lrc = opt_launch_point(K, x, d, alpha, kap, ns, S, st) || dip_launch_grad<double>(s->md, S, grad, st) ||
+                  dip_launch_energy<double>(s->md, S, s->partials, nbE, st);
+        } else {
+            double* D = (double*)s->S;
+            double* Q = (double*)s->Q;
+            lrc = opt_launch_point(K, x, d, alpha, kap, ns, S, st) || sun_launch_refresh<double>(s->md, S, D, Q, st) ||
+                  sun_launch_grad<double>(s->md, S, D, Q, grad, st) || sun_launch_energy<double>(s->md, S, D, Q, s->partials, nbE, st);
+        }
+        if (lrc || util_launch_reduce(s->partials, nbE, 4, s->red, st)) return cuda_fail(s, cudaGetLastError(), "optimizer evaluation");
         s->launches += 4;
         double Ed = 0;
         int erc = ewald_add<double>(s, S, grad, s->ewald_on ? &Ed : nullptr);
         if (erc) return erc;
         if (dphi) {
-            if (opt_launch_dphi(x, d, alpha, grad, kap, ns, part, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
+            if (opt_launch_dphi(K, x, d, alpha, grad, kap, ns, part, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
             s->launches++;
         }
         CK(cudaMemcpyAsync(f, s->red, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1071,20 +1082,20 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
     };
     const bool acc_max[10] = {false, false, false, false, false, false, false, true, true, false};
     auto accept = [&](double alpha, double* v) -> int {
-        if (opt_launch_accept(x, d, alpha, grad, kap, ns, g, part, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
+        if (opt_launch_accept(K, x, d, alpha, grad, kap, ns, g, part, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
         s->launches++;
         return pull(10, v, acc_max);
     };
     const bool dir_max[2] = {false, true};
     auto direction = [&](double beta, double* v) -> int {
-        if (opt_launch_dir(g, d, beta, ns, part, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
+        if (opt_launch_dir(K, g, d, beta, ns, part, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
         s->launches++;
         return pull(2, v, dir_max);
     };
     double f = 0, v[10], w[2];
     if ((rc = eval(0.0, &f, nullptr)) || (rc = accept(0.0, v))) return rc;
-    const double v9_0 = v[9];
-    const double g_abstol = 1e-12 * std::sqrt(v9_0) / std::sqrt((double)ns);   // characteristic_energy_scale
+    const double v9_0 = v[9] / (gdiv * gdiv);
+    const double g_abstol = gdiv * 1e-12 * std::sqrt(v9_0) / std::sqrt((double)ns);   // characteristic_energy_scale, in the kernels' units
     const double x_abstol = 1e-12;
     bool conv = v[7] <= g_abstol;
     int iters = 0;
@@ -1137,7 +1148,7 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
                 // second failure in a row: no step decreases E at FP64 resolution, so x no
                 // longer moves (Optim then reports x_abschange = 0 <= x_abstol). Accept that
                 // as convergence only near a stationary point.
-                conv = gmax <= 1e-6 * std::sqrt(v9_0) / std::sqrt((double)ns);
+                conv = gmax <= gdiv * 1e-6 * std::sqrt(v9_0) / std::sqrt((double)ns);
                 break;
             }
             restarted = true;
@@ -1165,7 +1176,7 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
         alpha_prev = acc_a;
         dphi_prev = dphi0;
     }
-    if (opt_launch_point(x, d, 0.0, kap, ns, S, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
+    if (opt_launch_point(K, x, d, 0.0, kap, ns, S, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
     s->launches++;
     double E = f;
     if ((rc = eval(0.0, &E, nullptr))) return rc;

@@ -119,16 +119,18 @@ template <class R>
 int sun_launch_local_dE(const Model<R>& M, const R* Z, const R* D, const R* Q, int site, const SunKet& zk, double* out,
                         cudaStream_t st);
 
-// ---- minimize_energy! vector kernels (sgb_opt.cu), FP64 dipole state ----
+// ---- minimize_energy! vector kernels (sgb_opt.cu), FP64 state ----
+// K reals per site: 3 (dipoles) or 2N (coherent states as (re, im)); vectors SoA [K][ns],
+// gradients AoS [ns][K]
 int opt_grid(int ns);   // blocks of every partial-writing kernel below
-int opt_launch_init(double* S, const double* kappa, int ns, double jitter, uint64_t seed, double* x, cudaStream_t st);
-int opt_launch_point(const double* x, const double* d, double alpha, const double* kappa, int ns, double* S,
+int opt_launch_init(int K, double* S, const double* kappa, int ns, double jitter, uint64_t seed, double* x, cudaStream_t st);
+int opt_launch_point(int K, const double* x, const double* d, double alpha, const double* kappa, int ns, double* S,
                      cudaStream_t st);
-int opt_launch_dphi(const double* x, const double* d, double alpha, const double* grad, const double* kappa, int ns,
+int opt_launch_dphi(int K, const double* x, const double* d, double alpha, const double* grad, const double* kappa, int ns,
                     double* part, cudaStream_t st);
-int opt_launch_accept(double* x, double* d, double alpha, const double* grad, const double* kappa, int ns, double* g,
+int opt_launch_accept(int K, double* x, double* d, double alpha, const double* grad, const double* kappa, int ns, double* g,
                       double* part, cudaStream_t st);
-int opt_launch_dir(const double* g, double* d, double beta, int ns, double* part, cudaStream_t st);
+int opt_launch_dir(int K, const double* g, double* d, double beta, int ns, double* part, cudaStream_t st);
 
 // ---- dipole-dipole Ewald summation (sgb_ewald.cu) ----
 #include <cufft.h>
