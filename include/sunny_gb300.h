@@ -162,6 +162,14 @@ int sgb_energy(sgb_system* sys, double* energy, double* magnetization3);
 int sgb_langevin(sgb_system* sys, double dt, double damping, double kT,
                  uint64_t seed, uint64_t step0, int32_t nsteps, const double* noise);
 
+/* Kernel choice of sgb_langevin on dipole lattices (no counterpart in the reference).
+ * Small lattices can be held whole by one thread-block cluster in distributed shared
+ * memory, where a Heun stage ends at the cluster's hardware barrier instead of a grid
+ * barrier. mode -1 (default): time both kernels on the first call and keep the faster;
+ * 0: the persistent grid kernel; 1: the cluster kernel (SGB_ERR_ARG if the lattice does
+ * not fit one cluster). Both give the same results. */
+int sgb_set_langevin_cluster(sgb_system* sys, int32_t mode);
+
 /* Writes the standard normals that sgb_langevin(noise=NULL) uses for step `step`
  * into out ([ns][3] or [ns][N][2]), so that an FP64 CPU restatement can replay a
  * device-noise trajectory exactly. */

@@ -116,6 +116,7 @@ int build_tables(sgb_system* s, Model<R>& M) {
         s->boff_h.assign(boff, boff + na + 1);
         s->nbr_h = tab;
         s->colors_dirty = true;
+        if (!s->heun_forced) s->heun_cluster = -1;
         void* p = s->nbr;
         dfree(p);
         s->nbr = nullptr;
@@ -192,12 +193,70 @@ std::string fmt_g(double x) {
     return b;
 }
 
+// Cluster size for a dipole lattice held in distributed shared memory: one site per thread
+// where possible, at most 16 CTAs, the slices within 160 KB of shared memory each; 0 when
+// the lattice is too large for one cluster.
+template <class R>
+int cluster_size(sgb_system* s) {
+    if (s->sun) return 0;
+    int cs = 1;
+    while (cs < SGB_CLUSTER_MAX && (long long)cs * SGB_CLUSTER_BLOCK < s->ns) cs *= 2;
+    const int nsl = (s->ns + cs - 1) / cs;
+    if (nsl > 8 * SGB_CLUSTER_BLOCK || dip_cluster_smem<R>(model<R>(s), nsl) > 160 * 1024) return 0;
+    return cs;
+}
+
+// Chooses, once per handle, between the persistent grid kernel and the cluster kernel
+// (at the largest cluster size and at 1/2 and 1/4 of it) for Langevin on small dipole
+// lattices, by timing 20 steps of each on a copy of the state (restored afterwards).
+template <class R>
+int tune_heun(sgb_system* s, const LaunchInfo& li, double dt, double damping, double nscale, uint64_t seed) {
+    if (s->heun_cluster >= 0) return SGB_OK;
+    s->heun_cluster = 0;
+    const int csmax = cluster_size<R>(s);
+    if (csmax == 0) return SGB_OK;
+    const size_t bytes = sizeof(R) * 3 * (size_t)s->ns;
+    void* save = nullptr;
+    int rc = dmalloc(s, &save, bytes);
+    if (rc) return rc;
+    Model<R>& M = model<R>(s);
+    const int nt = 20;
+    const int cand[4] = {0, csmax, csmax / 2, csmax / 4};
+    float best = 0;
+    for (int v = 0; v < 4; v++) {
+        const int cs = cand[v];
+        if (v > 0 && (cs < 1 || (long long)cs * 8 * SGB_CLUSTER_BLOCK < s->ns ||
+                      dip_cluster_smem<R>(M, (s->ns + cs - 1) / cs) > 160 * 1024))
+            continue;
+        float t = 0;
+        bool ok = true;
+        for (int rep = 0; rep < 2 && ok; rep++) {   // the first repetition warms up
+            ok = cudaMemcpyAsync(save, s->S, bytes, cudaMemcpyDeviceToDevice, s->stream) == cudaSuccess &&
+                 reset_ctrl(s) == SGB_OK && cudaEventRecord(s->ev[6], s->stream) == cudaSuccess;
+            if (!ok) break;
+            int lrc = cs == 0 ? dip_launch_heun<R>(M, (R*)s->S, (R*)s->P, s->ctrl, nt, dt, damping, nscale, seed, 0, nullptr, li, s->stream)
+                              : dip_launch_heun_cluster<R>(M, (R*)s->S, cs, nt, dt, damping, nscale, seed, 0, nullptr, s->stream);
+            s->launches++;
+            if (lrc != SGB_OK) cudaGetLastError();
+            ok = lrc == SGB_OK && cudaEventRecord(s->ev[7], s->stream) == cudaSuccess &&
+                 cudaMemcpyAsync(s->S, save, bytes, cudaMemcpyDeviceToDevice, s->stream) == cudaSuccess &&
+                 cudaStreamSynchronize(s->stream) == cudaSuccess;
+            if (ok) cudaEventElapsedTime(&t, s->ev[6], s->ev[7]);
+        }
+        if (!ok) continue;
+        if (v == 0 || t < best) { best = t; s->heun_cluster = cs; }
+    }
+    dfree(save);
+    return SGB_OK;
+}
+
 template <class R>
 int run_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t seed, uint64_t step0, int nsteps, const double* noise) {
     LaunchInfo li;
     int rc = plan_launch<R>(s, li);
     if (rc) return rc;
     double nscale = (damping == 0.0 || kT == 0.0) ? 0.0 : std::sqrt(2 * dt * damping * kT);
+    if (!s->sun && (rc = tune_heun<R>(s, li, dt, damping, nscale, seed))) return rc;
     const size_t per = s->sun ? (size_t)2 * s->N * s->ns : (size_t)3 * s->ns;
     int chunk = nsteps;
     if (noise) {
@@ -214,7 +273,9 @@ int run_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t s
             dn = s->dbuf;
         }
         if ((rc = reset_ctrl(s))) return rc;
-        if (!s->sun)
+        if (!s->sun && s->heun_cluster > 0)
+            rc = dip_launch_heun_cluster<R>(M, (R*)s->S, s->heun_cluster, nk, dt, damping, nscale, seed, step0 + k0, dn, s->stream);
+        else if (!s->sun)
             rc = dip_launch_heun<R>(M, (R*)s->S, (R*)s->P, s->ctrl, nk, dt, damping, nscale, seed, step0 + k0, dn, li, s->stream);
         else
             rc = sun_launch_heun<R>(M, (R*)s->Z, (R*)s->S, (R*)s->Q, (R*)s->P, (R*)s->QP, s->ctrl, nk, dt, damping, nscale,
@@ -821,6 +882,22 @@ int sgb_get_state(sgb_system* s, double* dipoles, double* coherents) {
                 coherents[(size_t)2 * N * i + c] = s->fp32 ? (double)reinterpret_cast<float*>(s->stage)[(size_t)c * ns + i]
                                                            : reinterpret_cast<double*>(s->stage)[(size_t)c * ns + i];
     }
+    return SGB_OK;
+}
+
+int sgb_set_langevin_cluster(sgb_system* s, int32_t mode) {
+    if (!s) return fail(nullptr, SGB_ERR_ARG, "null handle");
+    if (mode < -1 || mode > 1) return fail(s, SGB_ERR_ARG, "mode must be -1 (timed choice), 0 (grid) or 1 (cluster)");
+    if (mode == 1) {
+        int rc = ensure_tables(s);
+        if (rc) return rc;
+        const int cs = s->fp32 ? cluster_size<float>(s) : cluster_size<double>(s);
+        if (cs == 0) return fail(s, SGB_ERR_ARG, "the lattice is too large for one thread-block cluster");
+        s->heun_cluster = cs;
+    } else {
+        s->heun_cluster = mode;
+    }
+    s->heun_forced = mode >= 0;
     return SGB_OK;
 }
 

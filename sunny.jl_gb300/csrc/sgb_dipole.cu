@@ -14,9 +14,12 @@
 // spins and the next step's starting midpoint spins, so each fixed-point iteration costs
 // exactly one barrier; the FP64 convergence sum rotates through three accumulators.
 #include "sgb_internal.h"
+#include <cooperative_groups.h>
 #include <stdio.h>
 
 #include "sgb_device.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 using namespace sgbdev;
@@ -364,6 +367,96 @@ int set_smem_attr(K kernel, size_t smem) {
     return SGB_OK;
 }
 
+// Small lattices: one thread-block cluster holds the whole state in distributed shared
+// memory, CTA r owning sites [r*nsl, (r+1)*nsl) as [3][nsl] slices of S, the predictor
+// P, the first increment and the noise. Neighbour spins are read from the owning CTA's
+// shared memory, and the two Heun stages of a step are separated by the cluster's
+// hardware barrier instead of a grid barrier through L2. Same per-site arithmetic and
+// noise stream as k_dip_heun.
+template <class R, bool INJECT, bool GEN>
+__global__ void __launch_bounds__(SGB_CLUSTER_BLOCK) k_dip_heun_cluster(Model<R> M, R* S, int nsl, int nsteps, R dt, R lam,
+                                                                       R nscale, uint64_t seed, uint64_t step0,
+                                                                       const double* noise) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    cg::cluster_group cl = cg::this_cluster();
+    Tab<R> T = stage_tables<R>(M, smem);
+    const int rank = (int)cl.block_rank();
+    const int ns = M.ns;
+    R* lS = reinterpret_cast<R*>(smem + ((M.tables_bytes + 15) / 16) * 16);   // [3][nsl]
+    R* lP = lS + 3 * nsl;
+    R* lD = lP + 3 * nsl;
+    R* lX = lD + 3 * nsl;
+    __shared__ const R* rS[SGB_CLUSTER_MAX];
+    __shared__ const R* rP[SGB_CLUSTER_MAX];
+    if (threadIdx.x < cl.num_blocks()) {
+        rS[threadIdx.x] = cl.map_shared_rank(lS, threadIdx.x);
+        rP[threadIdx.x] = cl.map_shared_rank(lP, threadIdx.x);
+    }
+    const int s0 = rank * nsl, n = max(0, min(ns, s0 + nsl) - s0);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        lS[i] = S[s0 + i]; lS[nsl + i] = S[ns + s0 + i]; lS[2 * nsl + i] = S[2 * ns + s0 + i];
+    }
+    cl.sync();
+    auto ldS = [&](int j, R& x, R& y, R& z) {
+        const int q = j / nsl, l = j - q * nsl;
+        const R* b = rS[q];
+        x = b[l]; y = b[nsl + l]; z = b[2 * nsl + l];
+    };
+    auto ldP = [&](int j, R& x, R& y, R& z) {
+        const int q = j / nsl, l = j - q * nsl;
+        const R* b = rP[q];
+        x = b[l]; y = b[nsl + l]; z = b[2 * nsl + l];
+    };
+    for (int step = 0; step < nsteps; ++step) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int site = s0 + i, a = site / M.ncell;
+            R x0 = 0, x1 = 0, x2 = 0;
+            if (nscale != (R)0) {
+                if (INJECT) {
+                    const double* nz = noise + ((size_t)step * ns + site) * 3;
+                    x0 = (R)nz[0] * nscale; x1 = (R)nz[1] * nscale; x2 = (R)nz[2] * nscale;
+                } else {
+                    R g4[4];
+                    sgb_normals4<R>(seed, 0u, step0 + step, (uint32_t)site, 0u, g4);
+                    x0 = g4[0] * nscale; x1 = g4[1] * nscale; x2 = g4[2] * nscale;
+                }
+            }
+            const R sx = lS[i], sy = lS[nsl + i], sz = lS[2 * nsl + i];
+            R hx = 0, hy = 0, hz = 0;
+            if (M.h) { hx = __ldg(M.h + site); hy = __ldg(M.h + ns + site); hz = __ldg(M.h + 2 * ns + site); }
+            const int* ip = M.nbr + site;
+            R gx, gy, gz, d0, d1, d2;
+            grad_nbi_ld<R, GEN, 6>(M, T, a, [ip, ns](int b) { return __ldg(ip + (size_t)b * ns); }, ldS, hx, hy, hz, sx, sy, sz,
+                                   gx, gy, gz);
+            rhs_dipole<R>(sx, sy, sz, x0, x1, x2, gx, gy, gz, dt, lam, d0, d1, d2);
+            R px = sx + d0, py = sy + d1, pz = sz + d2;
+            normalize_dip<R>(px, py, pz, __ldg(M.kappa + site));
+            lP[i] = px; lP[nsl + i] = py; lP[2 * nsl + i] = pz;
+            lD[i] = d0; lD[nsl + i] = d1; lD[2 * nsl + i] = d2;
+            lX[i] = x0; lX[nsl + i] = x1; lX[2 * nsl + i] = x2;
+        }
+        cl.sync();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int site = s0 + i, a = site / M.ncell;
+            const R px = lP[i], py = lP[nsl + i], pz = lP[2 * nsl + i];
+            R hx = 0, hy = 0, hz = 0;
+            if (M.h) { hx = __ldg(M.h + site); hy = __ldg(M.h + ns + site); hz = __ldg(M.h + 2 * ns + site); }
+            const int* ip = M.nbr + site;
+            R gx, gy, gz, e0, e1, e2;
+            grad_nbi_ld<R, GEN, 6>(M, T, a, [ip, ns](int b) { return __ldg(ip + (size_t)b * ns); }, ldP, hx, hy, hz, px, py, pz,
+                                   gx, gy, gz);
+            rhs_dipole<R>(px, py, pz, lX[i], lX[nsl + i], lX[2 * nsl + i], gx, gy, gz, dt, lam, e0, e1, e2);
+            R nx = lS[i] + (lD[i] + e0) / 2, ny = lS[nsl + i] + (lD[nsl + i] + e1) / 2, nz = lS[2 * nsl + i] + (lD[2 * nsl + i] + e2) / 2;
+            normalize_dip<R>(nx, ny, nz, __ldg(M.kappa + site));
+            lS[i] = nx; lS[nsl + i] = ny; lS[2 * nsl + i] = nz;
+        }
+        cl.sync();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        S[s0 + i] = lS[i]; S[ns + s0 + i] = lS[nsl + i]; S[2 * ns + s0 + i] = lS[2 * nsl + i];
+    }
+}
+
 template <class K>
 int coop_launch(K kernel, const LaunchInfo& li, void** args, cudaStream_t st) {
     if (set_smem_attr(kernel, li.smem) != SGB_OK) return SGB_ERR_CUDA;
@@ -395,6 +488,41 @@ int dip_launch_heun(const Model<R>& M, R* S, R* P, Ctrl* ctrl, int nsteps, doubl
     }
 #undef SGB_HEUN_CASE
     return SGB_ERR_ARG;
+}
+
+template <class R>
+size_t dip_cluster_smem(const Model<R>& M, int nsl) {
+    return (size_t)((M.tables_bytes + 15) / 16) * 16 + (size_t)12 * nsl * sizeof(R);
+}
+
+template <class R>
+int dip_launch_heun_cluster(const Model<R>& M, R* S, int cs, int nsteps, double dt, double lam, double noise_scale,
+                            uint64_t seed, uint64_t step0, const double* noise, cudaStream_t st) {
+    const int nsl = (M.ns + cs - 1) / cs;
+    const size_t smem = dip_cluster_smem<R>(M, nsl);
+    const void* k = noise ? (M.general ? (const void*)k_dip_heun_cluster<R, true, true> : (const void*)k_dip_heun_cluster<R, true, false>)
+                          : (M.general ? (const void*)k_dip_heun_cluster<R, false, true> : (const void*)k_dip_heun_cluster<R, false, false>);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return SGB_ERR_CUDA;
+    if (cs > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return SGB_ERR_CUDA;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(SGB_CLUSTER_BLOCK);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, k, &cfg) != cudaSuccess || clusters < 1) return SGB_ERR_ARG;
+    Model<R> m = M;
+    R rdt = (R)dt, rlam = (R)lam, rns = (R)noise_scale;
+    int ns_ = nsl, nst = nsteps;
+    void* args[] = {&m, &S, &ns_, &nst, &rdt, &rlam, &rns, &seed, &step0, &noise};
+    return cudaLaunchKernelExC(&cfg, k, args) == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
 template <class R>
@@ -487,6 +615,9 @@ int util_launch_fill(double* p, size_t n, double v, cudaStream_t st) {
     template int dip_launch_grad<R>(const Model<R>&, const R*, double*, cudaStream_t);                    \
     template int dip_launch_energy<R>(const Model<R>&, const R*, double*, int, cudaStream_t);             \
     template int dip_max_blocks<R>(int, int, size_t, int*);                                                    \
+    template int dip_launch_heun_cluster<R>(const Model<R>&, R*, int, int, double, double, double, uint64_t, uint64_t, \
+                                            const double*, cudaStream_t);                                      \
+    template size_t dip_cluster_smem<R>(const Model<R>&, int);                                                 \
     template int util_launch_noise_export<R>(int, int, int, uint64_t, uint64_t, double*, cudaStream_t);
 SGB_INST(float)
 SGB_INST(double)

@@ -62,6 +62,10 @@ struct sgb_system {
     double* ew_part = nullptr;       // [EWALD_PART_BLOCKS] energy partials
     double* lr_grad = nullptr;       // [ns][3] gradient of the per-stage integrator path
     int lr_grad_cap = 0;
+    // Langevin on small dipole lattices: -1 not yet timed, 0 persistent grid, cs > 0 a
+    // cluster of cs CTAs holding the lattice in distributed shared memory
+    int heun_cluster = -1;
+    bool heun_forced = false;        // set by sgb_set_langevin_cluster
 };
 
 struct sgb_corr {

@@ -65,6 +65,15 @@ template <class R>
 int dip_launch_energy(const Model<R>& M, const R* S, double* partials, int nblocks, cudaStream_t st);
 template <class R>
 int dip_max_blocks(int spt, int block, size_t smem, int* blocks_per_sm);
+// Langevin for small dipole lattices held by one thread-block cluster (cs CTAs); returns
+// SGB_ERR_ARG when the cluster cannot be scheduled
+#define SGB_CLUSTER_BLOCK 256
+#define SGB_CLUSTER_MAX 16
+template <class R>
+int dip_launch_heun_cluster(const Model<R>& M, R* S, int cs, int nsteps, double dt, double lam, double noise_scale,
+                            uint64_t seed, uint64_t step0, const double* noise, cudaStream_t st);
+template <class R>
+size_t dip_cluster_smem(const Model<R>& M, int nsl);
 
 // ---- SU(N) kernels (sgb_sun.cu) ----
 template <class R>

@@ -492,6 +492,12 @@ class System:
             flatd[:] = self._kappa[:, None] * (d / np.linalg.norm(d))[None, :]
         self._host_newer = True
 
+    def set_langevin_cluster(self, mode: int):
+        """Kernel choice of Langevin steps on dipole lattices: -1 timed choice (default),
+        0 persistent grid kernel, 1 one thread-block cluster holding the lattice."""
+        self._sync_to_device()
+        _abi.check(self._lib.sgb_set_langevin_cluster(self._h, int(mode)), self._lib, self._h)
+
     def set_midpoint_predictor(self, order: int):
         """First iterate of each dipole midpoint step within one call: 0 S' = S (the
         reference's choice), k in 1..4 the degree-k extrapolation of the last states.

@@ -181,3 +181,33 @@ def test_pyrochlore_fp64_langevin_parity(gpu, sg, orc):
     sg.step(sys_, sg.Langevin(0.025, damping=0.1, kT=0.2), nsteps=20, noise=noise)
     S_ref, _ = o.langevin(S0, None, 0.025, 0.1, 0.2, 20, noise)
     assert rel(sys_.dipoles_flat(), S_ref) < 1e-11
+
+
+@pytest.mark.parametrize("builder", ["rich", "sc"])
+def test_langevin_cluster_kernel_matches_grid_and_oracle(gpu, sg, orc, builder):
+    # the cluster-resident Heun kernel (small lattices in distributed shared memory) and
+    # the persistent grid kernel give the same FP64 trajectory as the oracle
+    def make():
+        return rich_dipole(sg) if builder == "rich" else sc_c1(sg, L=8)
+    a, b = make(), make()
+    o = oracle_of(orc, a)
+    S0 = a.dipoles_flat()
+    noise = np.random.default_rng(21).standard_normal((20, a.nsites, 3))
+    a.set_langevin_cluster(0)
+    b.set_langevin_cluster(1)
+    integ = sg.Langevin(0.02, damping=0.1, kT=0.5)
+    sg.step(a, integ, 20, noise)
+    sg.step(b, integ, 20, noise)
+    ref, _ = o.langevin(S0, None, 0.02, 0.1, 0.5, 20, noise)
+    assert rel(b.dipoles_flat(), a.dipoles_flat()) < 1e-12
+    assert rel(b.dipoles_flat(), ref) < 1e-12
+
+
+def test_langevin_cluster_kernel_fp32_device_noise(gpu, sg):
+    a, b = sc_c1(sg, L=16, precision="fp32"), sc_c1(sg, L=16, precision="fp32")
+    a.set_langevin_cluster(0)
+    b.set_langevin_cluster(1)
+    integ = sg.Langevin(0.02, damping=0.1, kT=0.5)
+    sg.step(a, integ, 50)
+    sg.step(b, integ, 50)
+    assert rel(b.dipoles_flat(), a.dipoles_flat()) < 1e-5
