@@ -197,13 +197,30 @@ std::string fmt_g(double x) {
 // where possible, at most 16 CTAs, the slices within 160 KB of shared memory each; 0 when
 // the lattice is too large for one cluster.
 template <class R>
+int do_refresh(sgb_system* s);
+
+template <class R>
+size_t cluster_smem(sgb_system* s, int nsl) {
+    return s->sun ? sun_cluster_smem<R>(model<R>(s), nsl) : dip_cluster_smem<R>(model<R>(s), nsl);
+}
+
+template <class R>
 int cluster_size(sgb_system* s) {
-    if (s->sun) return 0;
     int cs = 1;
     while (cs < SGB_CLUSTER_MAX && (long long)cs * SGB_CLUSTER_BLOCK < s->ns) cs *= 2;
     const int nsl = (s->ns + cs - 1) / cs;
-    if (nsl > 8 * SGB_CLUSTER_BLOCK || dip_cluster_smem<R>(model<R>(s), nsl) > 160 * 1024) return 0;
+    if (nsl > 8 * SGB_CLUSTER_BLOCK || cluster_smem<R>(s, nsl) > 160 * 1024) return 0;
     return cs;
+}
+
+template <class R>
+int launch_heun_cluster(sgb_system* s, int cs, int nsteps, double dt, double damping, double nscale, uint64_t seed,
+                        uint64_t step0, const double* noise) {
+    Model<R>& M = model<R>(s);
+    if (s->sun)
+        return sun_launch_heun_cluster<R>(M, (R*)s->Z, (R*)s->S, (R*)s->Q, cs, nsteps, dt, damping, nscale, seed, step0, noise,
+                                          s->stream);
+    return dip_launch_heun_cluster<R>(M, (R*)s->S, cs, nsteps, dt, damping, nscale, seed, step0, noise, s->stream);
 }
 
 // Chooses, once per handle, between the persistent grid kernel and the cluster kernel
@@ -215,7 +232,10 @@ int tune_heun(sgb_system* s, const LaunchInfo& li, double dt, double damping, do
     s->heun_cluster = 0;
     const int csmax = cluster_size<R>(s);
     if (csmax == 0) return SGB_OK;
-    const size_t bytes = sizeof(R) * 3 * (size_t)s->ns;
+    // the state that a trial run changes: dipoles, or kets (dipoles and quadrupoles are
+    // refreshed from them afterwards)
+    R* X = (R*)(s->sun ? s->Z : s->S);
+    const size_t bytes = sizeof(R) * (s->sun ? 2 * s->N : 3) * (size_t)s->ns;
     void* save = nullptr;
     int rc = dmalloc(s, &save, bytes);
     if (rc) return rc;
@@ -225,22 +245,25 @@ int tune_heun(sgb_system* s, const LaunchInfo& li, double dt, double damping, do
     float best = 0;
     for (int v = 0; v < 4; v++) {
         const int cs = cand[v];
-        if (v > 0 && (cs < 1 || (long long)cs * 8 * SGB_CLUSTER_BLOCK < s->ns ||
-                      dip_cluster_smem<R>(M, (s->ns + cs - 1) / cs) > 160 * 1024))
+        if (v > 0 && (cs < 1 || (long long)cs * 8 * SGB_CLUSTER_BLOCK < s->ns || cluster_smem<R>(s, (s->ns + cs - 1) / cs) > 160 * 1024))
             continue;
         float t = 0;
         bool ok = true;
         for (int rep = 0; rep < 2 && ok; rep++) {   // the first repetition warms up
-            ok = cudaMemcpyAsync(save, s->S, bytes, cudaMemcpyDeviceToDevice, s->stream) == cudaSuccess &&
-                 reset_ctrl(s) == SGB_OK && cudaEventRecord(s->ev[6], s->stream) == cudaSuccess;
+            ok = cudaMemcpyAsync(save, X, bytes, cudaMemcpyDeviceToDevice, s->stream) == cudaSuccess && reset_ctrl(s) == SGB_OK &&
+                 cudaEventRecord(s->ev[6], s->stream) == cudaSuccess;
             if (!ok) break;
-            int lrc = cs == 0 ? dip_launch_heun<R>(M, (R*)s->S, (R*)s->P, s->ctrl, nt, dt, damping, nscale, seed, 0, nullptr, li, s->stream)
-                              : dip_launch_heun_cluster<R>(M, (R*)s->S, cs, nt, dt, damping, nscale, seed, 0, nullptr, s->stream);
+            int lrc;
+            if (cs > 0) lrc = launch_heun_cluster<R>(s, cs, nt, dt, damping, nscale, seed, 0, nullptr);
+            else if (!s->sun) lrc = dip_launch_heun<R>(M, (R*)s->S, (R*)s->P, s->ctrl, nt, dt, damping, nscale, seed, 0, nullptr, li, s->stream);
+            else lrc = sun_launch_heun<R>(M, (R*)s->Z, (R*)s->S, (R*)s->Q, (R*)s->P, (R*)s->QP, s->ctrl, nt, dt, damping, nscale, seed, 0,
+                                          nullptr, li, s->stream);
             s->launches++;
             if (lrc != SGB_OK) cudaGetLastError();
             ok = lrc == SGB_OK && cudaEventRecord(s->ev[7], s->stream) == cudaSuccess &&
-                 cudaMemcpyAsync(s->S, save, bytes, cudaMemcpyDeviceToDevice, s->stream) == cudaSuccess &&
-                 cudaStreamSynchronize(s->stream) == cudaSuccess;
+                 cudaMemcpyAsync(X, save, bytes, cudaMemcpyDeviceToDevice, s->stream) == cudaSuccess;
+            if (ok && s->sun) ok = do_refresh<R>(s) == SGB_OK;
+            ok = ok && cudaStreamSynchronize(s->stream) == cudaSuccess;
             if (ok) cudaEventElapsedTime(&t, s->ev[6], s->ev[7]);
         }
         if (!ok) continue;
@@ -256,7 +279,7 @@ int run_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t s
     int rc = plan_launch<R>(s, li);
     if (rc) return rc;
     double nscale = (damping == 0.0 || kT == 0.0) ? 0.0 : std::sqrt(2 * dt * damping * kT);
-    if (!s->sun && (rc = tune_heun<R>(s, li, dt, damping, nscale, seed))) return rc;
+    if ((rc = tune_heun<R>(s, li, dt, damping, nscale, seed))) return rc;
     const size_t per = s->sun ? (size_t)2 * s->N * s->ns : (size_t)3 * s->ns;
     int chunk = nsteps;
     if (noise) {
@@ -273,8 +296,8 @@ int run_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t s
             dn = s->dbuf;
         }
         if ((rc = reset_ctrl(s))) return rc;
-        if (!s->sun && s->heun_cluster > 0)
-            rc = dip_launch_heun_cluster<R>(M, (R*)s->S, s->heun_cluster, nk, dt, damping, nscale, seed, step0 + k0, dn, s->stream);
+        if (s->heun_cluster > 0)
+            rc = launch_heun_cluster<R>(s, s->heun_cluster, nk, dt, damping, nscale, seed, step0 + k0, dn);
         else if (!s->sun)
             rc = dip_launch_heun<R>(M, (R*)s->S, (R*)s->P, s->ctrl, nk, dt, damping, nscale, seed, step0 + k0, dn, li, s->stream);
         else

@@ -74,6 +74,11 @@ int dip_launch_heun_cluster(const Model<R>& M, R* S, int cs, int nsteps, double 
                             uint64_t seed, uint64_t step0, const double* noise, cudaStream_t st);
 template <class R>
 size_t dip_cluster_smem(const Model<R>& M, int nsl);
+template <class R>
+size_t sun_cluster_smem(const Model<R>& M, int nsl);
+template <class R>
+int sun_launch_heun_cluster(const Model<R>& M, R* Z, R* D, R* Q, int cs, int nsteps, double dt, double lam, double nscale,
+                            uint64_t seed, uint64_t step0, const double* noise, cudaStream_t st);
 
 // ---- SU(N) kernels (sgb_sun.cu) ----
 template <class R>

@@ -12,7 +12,11 @@
 // keeps its sites' coherent states Z in registers for the whole persistent launch and
 // publishes only <Z|S|Z> (3 reals) and, when biquadratic couplings exist, <Z|O2q|Z>
 // (5 reals) per site through L2-resident SoA buffers.
+#include <cooperative_groups.h>
+
 #include "sgb_device.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 using namespace sgbdev;
@@ -655,6 +659,217 @@ int grid1d(const Model<R>& M) {
     return grid > 4096 ? 4096 : grid;
 }
 
+// ---- Langevin for small SU(N) lattices held by one thread-block cluster ---------------
+// HZ of one site with the neighbours' expected dipoles (and quadrupoles) fetched through
+// loaders, bonds in table order (the same sums as sun_field).
+template <class R, int N, bool BQ, class LDD, class LDQ>
+__device__ __forceinline__ void local_HZ_ld(const Model<R>& M, const SunTab<R, N>& S, const SpinConst<R, N>& sc, int site,
+                                            LDD ldD, LDQ ldQ, const R* z, R* hz) {
+    const int ns = M.ns, a = site / M.ncell;
+    R d[3] = {0, 0, 0}, v[5] = {0, 0, 0, 0, 0};
+    if (M.h) { d[0] = __ldg(M.h + site); d[1] = __ldg(M.h + ns + site); d[2] = __ldg(M.h + 2 * ns + site); }
+    const int b0 = S.t.boff[a], b1 = S.t.boff[a + 1];
+    for (int b = b0; b < b1; b++) {
+        const DBond<R>& B = S.t.bonds[b];
+        const int j = __ldg(M.nbr + (size_t)(b - b0) * ns + site);
+        R t[3];
+        ldD(j, t);
+        if (B.jkind == 0) {
+            const R jj = B.J[0];
+            d[0] += jj * t[0]; d[1] += jj * t[1]; d[2] += jj * t[2];
+        } else {
+            d[0] += B.J[0] * t[0] + B.J[3] * t[1] + B.J[6] * t[2];
+            d[1] += B.J[1] * t[0] + B.J[4] * t[1] + B.J[7] * t[2];
+            d[2] += B.J[2] * t[0] + B.J[5] * t[1] + B.J[8] * t[2];
+        }
+        if (BQ && B.bqkind != 0) {
+            R Qj[5];
+            ldQ(j, Qj);
+            if (B.bqkind == 1) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) v[q] += B.bq * ((R)biquad_metric(q) * Qj[q]);
+            } else {
+                const R* Bm = S.t.bq + 25 * B.bqidx;
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    R acc = 0;
+#pragma unroll
+                    for (int p = 0; p < 5; p++) acc += Bm[q + 5 * p] * Qj[p];
+                    v[q] += acc;
+                }
+            }
+        }
+    }
+    apply_H<R, N, BQ>(sc, S.lam + a * 2 * N * N, S.qm, d, v, z, hz);
+}
+
+// CTA r of the cluster holds sites [r*nsl, (r+1)*nsl): their kets, predictor kets, first
+// increments and noise, and the expected dipoles (quadrupoles) of the state and of the
+// predictor that neighbours read. Stages end at the cluster barrier. Same per-site
+// arithmetic and noise stream as k_sun_heun.
+template <class R, int N, bool INJECT, bool BQ>
+__global__ void __launch_bounds__(SGB_CLUSTER_BLOCK) k_sun_heun_cluster(Model<R> M, R* Z, R* D, R* Qb, int nsl, int nsteps,
+                                                                       R dt, R lam, R nscale, uint64_t seed, uint64_t step0,
+                                                                       const double* noise) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    cg::cluster_group cl = cg::this_cluster();
+    SunTab<R, N> S = stage_sun<R, N>(M, smem);
+    SpinConst<R, N> sc;
+    const int rank = (int)cl.block_rank();
+    const int ns = M.ns;
+    constexpr int K = 2 * N;
+    R* lZ = reinterpret_cast<R*>(smem + ((M.tables_bytes + 15) / 16) * 16);   // [K][nsl]
+    R* lZP = lZ + K * nsl;
+    R* lD1 = lZP + K * nsl;
+    R* lZE = lD1 + K * nsl;
+    R* lD = lZE + K * nsl;     // [3][nsl]
+    R* lDP = lD + 3 * nsl;
+    R* lQ = lDP + 3 * nsl;     // [5][nsl] (BQ)
+    R* lQP = lQ + 5 * nsl;
+    __shared__ const R* rD[SGB_CLUSTER_MAX];
+    __shared__ const R* rDP[SGB_CLUSTER_MAX];
+    __shared__ const R* rQ[SGB_CLUSTER_MAX];
+    __shared__ const R* rQP[SGB_CLUSTER_MAX];
+    if (threadIdx.x < cl.num_blocks()) {
+        rD[threadIdx.x] = cl.map_shared_rank(lD, threadIdx.x);
+        rDP[threadIdx.x] = cl.map_shared_rank(lDP, threadIdx.x);
+        if (BQ) {
+            rQ[threadIdx.x] = cl.map_shared_rank(lQ, threadIdx.x);
+            rQP[threadIdx.x] = cl.map_shared_rank(lQP, threadIdx.x);
+        }
+    }
+    const int s0 = rank * nsl, n = max(0, min(ns, s0 + nsl) - s0);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+#pragma unroll
+        for (int c = 0; c < K; c++) lZ[c * nsl + i] = Z[(size_t)c * ns + s0 + i];
+#pragma unroll
+        for (int c = 0; c < 3; c++) lD[c * nsl + i] = D[(size_t)c * ns + s0 + i];
+        if (BQ) {
+#pragma unroll
+            for (int c = 0; c < 5; c++) lQ[c * nsl + i] = Qb[(size_t)c * ns + s0 + i];
+        }
+    }
+    cl.sync();
+    auto mkld = [&](const R* const* base, int ncomp) {
+        return [base, ncomp, nsl](int j, R* out) {
+            const int q = j / nsl, l = j - q * nsl;
+            const R* b = base[q];
+            for (int c = 0; c < ncomp; c++) out[c] = b[c * nsl + l];
+        };
+    };
+    auto ldD = mkld(rD, 3);
+    auto ldDP = mkld(rDP, 3);
+    auto ldQ = mkld(rQ, 5);
+    auto ldQP = mkld(rQP, 5);
+    for (int step = 0; step < nsteps; ++step) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int site = s0 + i;
+            R z[K], ze[K], hz[K], d1[K], zp[K];
+#pragma unroll
+            for (int c = 0; c < K; c++) z[c] = lZ[c * nsl + i];
+            if (nscale == (R)0) {
+#pragma unroll
+                for (int c = 0; c < K; c++) ze[c] = 0;
+            } else if (INJECT) {
+                const double* nz = noise + ((size_t)step * ns + site) * K;
+#pragma unroll
+                for (int c = 0; c < K; c++) ze[c] = (R)nz[c] * nscale;
+            } else {
+                const R r2 = (R)0.70710678118654752440;
+#pragma unroll
+                for (int c = 0; c < K; c += 4) {
+                    R g4[4];
+                    sgb_normals4<R>(seed, 0u, step0 + step, (uint32_t)site, (uint32_t)(c / 4), g4);
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (c + q < K) ze[c + q] = g4[q] * r2 * nscale;
+                }
+            }
+            local_HZ_ld<R, N, BQ>(M, S, sc, site, ldD, ldQ, z, hz);
+            rhs_sun<R, N>(z, ze, hz, dt, lam, d1);
+#pragma unroll
+            for (int c = 0; c < K; c++) zp[c] = z[c] + d1[c];
+            normalize_ket<R, N>(zp, __ldg(M.kappa + site));
+#pragma unroll
+            for (int c = 0; c < K; c++) { lZP[c * nsl + i] = zp[c]; lD1[c * nsl + i] = d1[c]; lZE[c * nsl + i] = ze[c]; }
+            R nx, ny, nz_;
+            expected_spin<R, N>(sc, zp, nx, ny, nz_);
+            lDP[i] = nx; lDP[nsl + i] = ny; lDP[2 * nsl + i] = nz_;
+            if (BQ) {
+                R q[5];
+                expected_quad<R, N>(S.qm, zp, q);
+#pragma unroll
+                for (int c = 0; c < 5; c++) lQP[c * nsl + i] = q[c];
+            }
+        }
+        cl.sync();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int site = s0 + i;
+            R zp[K], ze[K], hz[K], d2[K], z[K];
+#pragma unroll
+            for (int c = 0; c < K; c++) { zp[c] = lZP[c * nsl + i]; ze[c] = lZE[c * nsl + i]; }
+            local_HZ_ld<R, N, BQ>(M, S, sc, site, ldDP, ldQP, zp, hz);
+            rhs_sun<R, N>(zp, ze, hz, dt, lam, d2);
+#pragma unroll
+            for (int c = 0; c < K; c++) z[c] = lZ[c * nsl + i] + (lD1[c * nsl + i] + d2[c]) / 2;
+            normalize_ket<R, N>(z, __ldg(M.kappa + site));
+#pragma unroll
+            for (int c = 0; c < K; c++) lZ[c * nsl + i] = z[c];
+            R nx, ny, nz_;
+            expected_spin<R, N>(sc, z, nx, ny, nz_);
+            lD[i] = nx; lD[nsl + i] = ny; lD[2 * nsl + i] = nz_;
+            if (BQ) {
+                R q[5];
+                expected_quad<R, N>(S.qm, z, q);
+#pragma unroll
+                for (int c = 0; c < 5; c++) lQ[c * nsl + i] = q[c];
+            }
+        }
+        cl.sync();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+#pragma unroll
+        for (int c = 0; c < K; c++) Z[(size_t)c * ns + s0 + i] = lZ[c * nsl + i];
+#pragma unroll
+        for (int c = 0; c < 3; c++) D[(size_t)c * ns + s0 + i] = lD[c * nsl + i];
+        if (BQ) {
+#pragma unroll
+            for (int c = 0; c < 5; c++) Qb[(size_t)c * ns + s0 + i] = lQ[c * nsl + i];
+        }
+    }
+}
+
+template <class R, int N>
+int sun_heun_cluster_n(const Model<R>& M, R* Z, R* D, R* Q, int cs, int nsteps, double dt, double lam, double nscale,
+                       uint64_t seed, uint64_t step0, const double* noise, cudaStream_t st) {
+    const int nsl = (M.ns + cs - 1) / cs;
+    const size_t smem = sun_cluster_smem<R>(M, nsl);
+    const bool bq = M.has_biquad != 0;
+    const void* k = noise ? (bq ? (const void*)k_sun_heun_cluster<R, N, true, true> : (const void*)k_sun_heun_cluster<R, N, true, false>)
+                          : (bq ? (const void*)k_sun_heun_cluster<R, N, false, true> : (const void*)k_sun_heun_cluster<R, N, false, false>);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return SGB_ERR_CUDA;
+    if (cs > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return SGB_ERR_CUDA;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(SGB_CLUSTER_BLOCK);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, k, &cfg) != cudaSuccess || clusters < 1) return SGB_ERR_ARG;
+    Model<R> m = M;
+    R rdt = (R)dt, rlam = (R)lam, rns = (R)nscale;
+    int nsl_ = nsl, nst = nsteps;
+    void* args[] = {&m, &Z, &D, &Q, &nsl_, &nst, &rdt, &rlam, &rns, &seed, &step0, &noise};
+    return cudaLaunchKernelExC(&cfg, k, args) == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
 // ---- LocalSampler in SU(N) mode (Samplers.jl:139-158, Interactions.jl:311-373) --------
 // <z|Λ|z> of one ket (the onsite energy, Interactions.jl:331-332)
 template <class R, int N>
@@ -971,6 +1186,20 @@ int sun_launch_energy(const Model<R>& M, const R* Z, const R* D, const R* Q, dou
 }
 
 template <class R>
+size_t sun_cluster_smem(const Model<R>& M, int nsl) {
+    return (size_t)((M.tables_bytes + 15) / 16) * 16 + (size_t)(8 * M.N + 6 + (M.has_biquad ? 10 : 0)) * nsl * sizeof(R);
+}
+
+template <class R>
+int sun_launch_heun_cluster(const Model<R>& M, R* Z, R* D, R* Q, int cs, int nsteps, double dt, double lam, double nscale,
+                            uint64_t seed, uint64_t step0, const double* noise, cudaStream_t st) {
+    SGB_SUN_DISPATCH((sun_heun_cluster_n<R, 2>(M, Z, D, Q, cs, nsteps, dt, lam, nscale, seed, step0, noise, st)),
+                     (sun_heun_cluster_n<R, 3>(M, Z, D, Q, cs, nsteps, dt, lam, nscale, seed, step0, noise, st)),
+                     (sun_heun_cluster_n<R, 4>(M, Z, D, Q, cs, nsteps, dt, lam, nscale, seed, step0, noise, st)),
+                     (sun_heun_cluster_n<R, 5>(M, Z, D, Q, cs, nsteps, dt, lam, nscale, seed, step0, noise, st)))
+}
+
+template <class R>
 int sun_launch_local_sweeps(const Model<R>& M, R* Z, R* D, R* Q, Ctrl* ctrl, const McArgs& A, int grid, double* part,
                             cudaStream_t st) {
     SGB_SUN_DISPATCH((sun_sweeps_n<R, 2>(M, Z, D, Q, ctrl, A, grid, part, st)), (sun_sweeps_n<R, 3>(M, Z, D, Q, ctrl, A, grid, part, st)),
@@ -1002,6 +1231,9 @@ int sun_launch_local_dE(const Model<R>& M, const R* Z, const R* D, const R* Q, i
     template int sun_launch_energy<R>(const Model<R>&, const R*, const R*, const R*, double*, int, cudaStream_t); \
     template int sun_launch_local_sweeps<R>(const Model<R>&, R*, R*, R*, Ctrl*, const McArgs&, int, double*, cudaStream_t); \
     template int sun_mc_max_blocks<R>(const Model<R>&, int*);                                                    \
+    template size_t sun_cluster_smem<R>(const Model<R>&, int);                                                  \
+    template int sun_launch_heun_cluster<R>(const Model<R>&, R*, R*, R*, int, int, double, double, double, uint64_t, \
+                                            uint64_t, const double*, cudaStream_t);                            \
     template int sun_launch_local_dE<R>(const Model<R>&, const R*, const R*, const R*, int, const SunKet&, double*, cudaStream_t);
 SGB_SUN_INST(float)
 SGB_SUN_INST(double)

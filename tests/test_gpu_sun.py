@@ -80,3 +80,33 @@ def test_triangular_fp32_vs_fp64(gpu, sg, orc):
     S_ref, Z_ref = o.langevin(S0, Z0, 0.02, 0.1, 0.3, 1, noise)
     assert rel(s32.coherents_flat(), Z_ref) < 1e-5
     assert sg.energy(s32) == pytest.approx(o.energy(s32.dipoles_flat(), s32.coherents_flat()), rel=1e-5)
+
+
+@pytest.mark.parametrize("N", [3, 4])
+def test_heun_cluster_kernel_matches_grid_and_oracle(gpu, sg, orc, N):
+    # SU(N) Langevin with the lattice held by one thread-block cluster: same trajectory as
+    # the persistent grid kernel and the FP64 oracle, biquadratic couplings included
+    a, b = rich_sun(sg, N=N, biquad=N == 3), rich_sun(sg, N=N, biquad=N == 3)
+    o = oracle_of(orc, a)
+    Z0 = a.coherents_flat()
+    rng = np.random.default_rng(31)
+    noise = (rng.standard_normal((10, a.nsites, N)) + 1j * rng.standard_normal((10, a.nsites, N))) / np.sqrt(2)
+    a.set_langevin_cluster(0)
+    b.set_langevin_cluster(1)
+    integ = sg.Langevin(0.01, damping=0.1, kT=0.3)
+    sg.step(a, integ, 10, noise)
+    sg.step(b, integ, 10, noise)
+    _, Zref = o.langevin(o.expected_spin(Z0), Z0, 0.01, 0.1, 0.3, 10, noise)
+    assert rel(b.coherents_flat(), a.coherents_flat()) < 1e-12
+    assert rel(b.coherents_flat(), Zref) < 1e-11
+    assert rel(b.dipoles_flat(), o.expected_spin(Zref)) < 1e-11
+
+
+def test_heun_cluster_kernel_fp32_triangular(gpu, sg):
+    a, b = triangular_c3(sg, L=(12, 12, 4)), triangular_c3(sg, L=(12, 12, 4))
+    a.set_langevin_cluster(0)
+    b.set_langevin_cluster(1)
+    integ = sg.Langevin(0.02, damping=0.1, kT=0.3)
+    sg.step(a, integ, 30)
+    sg.step(b, integ, 30)
+    assert rel(b.coherents_flat(), a.coherents_flat()) < 1e-4
