@@ -236,6 +236,8 @@ int tune_heun(sgb_system* s, const LaunchInfo& li, double dt, double damping, do
     // refreshed from them afterwards)
     R* X = (R*)(s->sun ? s->Z : s->S);
     const size_t bytes = sizeof(R) * (s->sun ? 2 * s->N : 3) * (size_t)s->ns;
+    for (int e = 0; e < 2; e++)
+        if (!s->tev[e] && cudaEventCreate(&s->tev[e]) != cudaSuccess) return cuda_fail(s, cudaGetLastError(), "event creation");
     void* save = nullptr;
     int rc = dmalloc(s, &save, bytes);
     if (rc) return rc;
@@ -251,7 +253,7 @@ int tune_heun(sgb_system* s, const LaunchInfo& li, double dt, double damping, do
         bool ok = true;
         for (int rep = 0; rep < 2 && ok; rep++) {   // the first repetition warms up
             ok = cudaMemcpyAsync(save, X, bytes, cudaMemcpyDeviceToDevice, s->stream) == cudaSuccess && reset_ctrl(s) == SGB_OK &&
-                 cudaEventRecord(s->ev[6], s->stream) == cudaSuccess;
+                 cudaEventRecord(s->tev[0], s->stream) == cudaSuccess;
             if (!ok) break;
             int lrc;
             if (cs > 0) lrc = launch_heun_cluster<R>(s, cs, nt, dt, damping, nscale, seed, 0, nullptr);
@@ -260,11 +262,11 @@ int tune_heun(sgb_system* s, const LaunchInfo& li, double dt, double damping, do
                                           nullptr, li, s->stream);
             s->launches++;
             if (lrc != SGB_OK) cudaGetLastError();
-            ok = lrc == SGB_OK && cudaEventRecord(s->ev[7], s->stream) == cudaSuccess &&
+            ok = lrc == SGB_OK && cudaEventRecord(s->tev[1], s->stream) == cudaSuccess &&
                  cudaMemcpyAsync(X, save, bytes, cudaMemcpyDeviceToDevice, s->stream) == cudaSuccess;
             if (ok && s->sun) ok = do_refresh<R>(s) == SGB_OK;
             ok = ok && cudaStreamSynchronize(s->stream) == cudaSuccess;
-            if (ok) cudaEventElapsedTime(&t, s->ev[6], s->ev[7]);
+            if (ok) cudaEventElapsedTime(&t, s->tev[0], s->tev[1]);
         }
         if (!ok) continue;
         if (v == 0 || t < best) { best = t; s->heun_cluster = cs; }
@@ -682,6 +684,7 @@ void sgb_destroy(sgb_system* s) {
     dfree(s->flush);
     if (s->stage) cudaFreeHost(s->stage);
     for (int i = 0; i < 8; i++) if (s->ev[i]) cudaEventDestroy(s->ev[i]);
+    for (int i = 0; i < 2; i++) if (s->tev[i]) cudaEventDestroy(s->tev[i]);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }

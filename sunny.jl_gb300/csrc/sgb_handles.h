@@ -66,6 +66,7 @@ struct sgb_system {
     // cluster of cs CTAs holding the lattice in distributed shared memory
     int heun_cluster = -1;
     bool heun_forced = false;        // set by sgb_set_langevin_cluster
+    cudaEvent_t tev[2] = {};         // events of the kernel-choice timing (not the user's slots)
 };
 
 struct sgb_corr {
