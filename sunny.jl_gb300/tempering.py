@@ -24,6 +24,8 @@ class ReplicaBatch:
     def __init__(self, proto: System, dims_list, kT=None, precision: str | None = None, device: int = 0, seed: int = 0):
         if proto.N:
             raise ValueError("replica batches support the dipole modes")
+        if getattr(proto, "_ewald", None) is not None:
+            raise ValueError("replica batches do not support dipole-dipole interactions")
         self.proto = proto
         self.dims_list = [tuple(int(x) for x in d) for d in dims_list]
         self.nrep = len(self.dims_list)

@@ -123,3 +123,10 @@ def test_oracle_sun_local_sweeps_bookkeeping(sg, orc):
     assert np.allclose(S1, o.expected_spin(Z1), atol=1e-13)
     assert dE == pytest.approx(o.energy(S1, Z1) - o.energy(S0, Z0), abs=1e-10)
     assert np.allclose(dS, S1.sum(0) - S0.sum(0), atol=1e-10)
+
+
+def test_replica_batch_rejects_dipole_dipole(sg):
+    s = sc_c1(sg, L=4, device=None)
+    s.enable_dipole_dipole(1.0)
+    with pytest.raises(ValueError, match="dipole-dipole"):
+        sg.ReplicaBatch(s, [s.dims] * 2, kT=[0.1, 0.2])
