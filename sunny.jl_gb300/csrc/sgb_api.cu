@@ -452,7 +452,8 @@ int run_langevin_lr(sgb_system* s, double dt, double damping, double kT, uint64_
 }
 
 template <class R>
-int run_midpoint_lr(sgb_system* s, double dt, double damping, double tol, int max_iters, int nsteps, int64_t* iters) {
+int run_midpoint_lr(sgb_system* s, double dt, double damping, double tol, int max_iters, int nsteps, int64_t* iters,
+                    const SnapArgs<R>* snap = nullptr) {
     double* grad;
     int rc = ensure_lr_grad(s, &grad);
     if (rc) return rc;
@@ -464,6 +465,12 @@ int run_midpoint_lr(sgb_system* s, double dt, double damping, double tol, int ma
     const R* kap = (const R*)s->kappa;
     int64_t total = 0;
     double hp[EWALD_PART_BLOCKS];
+    // snapshots every measperiod steps (CorrelationSampling.jl:21-46), the first one of the
+    // initial state
+    if (snap && snap->enabled) {
+        if (dip_launch_snapshot<R>(model<R>(s), S, *snap, snap->t0, s->stream)) return cuda_fail(s, cudaGetLastError(), "snapshot launch");
+        s->launches++;
+    }
     for (int k = 0; k < nsteps; k++) {
         CK(cudaMemcpyAsync(Sp, S, sizeof(R) * 3 * ns, cudaMemcpyDeviceToDevice, s->stream));   // S' = S
         bool conv = false;
@@ -489,6 +496,11 @@ int run_midpoint_lr(sgb_system* s, double dt, double damping, double tol, int ma
         if (!conv)
             return fail(s, SGB_ERR_NOCONVERGE, "Spherical midpoint method failed to converge to tolerance " + fmt_g(tol) +
                                                    " after " + std::to_string(max_iters) + " iterations.");
+        if (snap && snap->enabled && (k + 1) % snap->measperiod == 0) {
+            if (dip_launch_snapshot<R>(model<R>(s), S, *snap, snap->t0 + (k + 1) / snap->measperiod, s->stream))
+                return cuda_fail(s, cudaGetLastError(), "snapshot launch");
+            s->launches++;
+        }
     }
     CK(cudaStreamSynchronize(s->stream));
     return SGB_OK;
@@ -1578,8 +1590,6 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
     sgb_system* s = c->sys;
     sgb_batch* b = c->batch;
     if (!s && !b) return cfail(c, SGB_ERR_STATE, "the System (or replica batch) of this accumulator was destroyed");
-    if (s && s->ewald_on)
-        return cfail(c, SGB_ERR_ARG, "SampledCorrelations trajectories with dipole-dipole interactions are not supported on the GPU");
     if (window != 0 && window != 1) return cfail(c, SGB_ERR_ARG, "window must be 0 (:cosine) or 1 (:rectangular)");
     if (c->window >= 0 && c->window != window)
         return cfail(c, SGB_ERR_ARG, "all samples of one accumulator must use the same window");
@@ -1609,11 +1619,13 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
         if (rc) return cfail(c, rc, batch_error(b));
     } else if (fp32) {
         SnapArgs<float> sn{1, c->nobs, c->measperiod, 0, (const float*)c->ops, (float*)c->A, (float)scale};
-        if (nsteps > 0) rc = run_midpoint<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true, s->mid_order);
+        if (s->ewald_on) rc = run_midpoint_lr<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, &sn);
+        else if (nsteps > 0) rc = run_midpoint<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true, s->mid_order);
         else rc = run_midpoint<float>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
     } else {
         SnapArgs<double> sn{1, c->nobs, c->measperiod, 0, (const double*)c->ops, (double*)c->A, scale};
-        if (nsteps > 0) rc = run_midpoint<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true, s->mid_order);
+        if (s->ewald_on) rc = run_midpoint_lr<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, &sn);
+        else if (nsteps > 0) rc = run_midpoint<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true, s->mid_order);
         else rc = run_midpoint<double>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
     }
     if (rc) return rc;

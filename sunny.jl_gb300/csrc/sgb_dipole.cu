@@ -457,6 +457,13 @@ __global__ void __launch_bounds__(SGB_CLUSTER_BLOCK) k_dip_heun_cluster(Model<R>
     }
 }
 
+// One snapshot row t of every site's observables (the snapshot of the fused kernels).
+template <class R>
+__global__ void k_dip_snapshot(Model<R> M, const R* S, SnapArgs<R> sn, int t) {
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < M.ns; site += gridDim.x * blockDim.x)
+        write_snapshot_dip<R>(M, sn, t, site, S[site], S[M.ns + site], S[2 * M.ns + site]);
+}
+
 template <class K>
 int coop_launch(K kernel, const LaunchInfo& li, void** args, cudaStream_t st) {
     if (set_smem_attr(kernel, li.smem) != SGB_OK) return SGB_ERR_CUDA;
@@ -488,6 +495,14 @@ int dip_launch_heun(const Model<R>& M, R* S, R* P, Ctrl* ctrl, int nsteps, doubl
     }
 #undef SGB_HEUN_CASE
     return SGB_ERR_ARG;
+}
+
+template <class R>
+int dip_launch_snapshot(const Model<R>& M, const R* S, const SnapArgs<R>& sn, int t, cudaStream_t st) {
+    int grid = (M.ns + SGB_BLOCK - 1) / SGB_BLOCK;
+    if (grid > 4096) grid = 4096;
+    k_dip_snapshot<R><<<grid, SGB_BLOCK, 0, st>>>(M, S, sn, t);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
 template <class R>
@@ -618,6 +633,7 @@ int util_launch_fill(double* p, size_t n, double v, cudaStream_t st) {
     template int dip_launch_heun_cluster<R>(const Model<R>&, R*, int, int, double, double, double, uint64_t, uint64_t, \
                                             const double*, cudaStream_t);                                      \
     template size_t dip_cluster_smem<R>(const Model<R>&, int);                                                 \
+    template int dip_launch_snapshot<R>(const Model<R>&, const R*, const SnapArgs<R>&, int, cudaStream_t);     \
     template int util_launch_noise_export<R>(int, int, int, uint64_t, uint64_t, double*, cudaStream_t);
 SGB_INST(float)
 SGB_INST(double)

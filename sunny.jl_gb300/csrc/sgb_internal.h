@@ -74,6 +74,10 @@ int dip_launch_heun_cluster(const Model<R>& M, R* S, int cs, int nsteps, double 
                             uint64_t seed, uint64_t step0, const double* noise, cudaStream_t st);
 template <class R>
 size_t dip_cluster_smem(const Model<R>& M, int nsl);
+// one snapshot row t of the observables of dipoles S (SampledCorrelations trajectories
+// outside the fused midpoint kernels)
+template <class R>
+int dip_launch_snapshot(const Model<R>& M, const R* S, const SnapArgs<R>& sn, int t, cudaStream_t st);
 template <class R>
 size_t sun_cluster_smem(const Model<R>& M, int nsl);
 template <class R>

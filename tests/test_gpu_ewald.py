@@ -147,3 +147,39 @@ def test_unsupported_paths_reject_dipole_dipole(gpu, sg):
     sys_, _ = _triclinic(sg)
     with pytest.raises(sg.SunnyGPUError, match="dipole-dipole"):
         sg.step(sys_, sg.LocalSampler(kT=0.1))
+
+
+def test_sqw_trajectory_with_dipole_dipole(gpu, sg, orc):
+    # S(q,ω) sampling runs the per-stage midpoint path with snapshots when dipole-dipole is
+    # on. With a negligible μ0 μB² the trajectory is the plain one: same data as the oracle.
+    sys_ = sg.System(sg.diamond_crystal(), [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(2, 3, 4), seed=101)
+    sys_.set_exchange(0.6498, sg.Bond(1, 3, [0, 0, 0]))
+    sys_.randomize_spins()
+    sys_.enable_dipole_dipole(1e-14)
+    sc = sg.SampledCorrelations(sys_, measure=sg.ssf_perp(sys_), energies=np.linspace(0.0, 5.5, 10), dt=0.12)
+    o = oracle_of(orc, sys_)
+    obs = sc.measure.observables.reshape(-1)
+    oc = orc.OracleCorrelations(o, obs, sc.measure.nobs, sc.measure.corr_pairs, sc.n_all_omega, sc.measperiod, sc.dt,
+                                sc.integrator.tol)
+    S = sys_.dipoles_flat()
+    for _ in range(2):
+        sg.add_sample(sc, sys_)
+        S, _ = oc.add_sample(S, None)
+    assert np.max(np.abs(sc.data - oc.data)) < 1e-8 * np.max(np.abs(oc.data))
+    assert np.max(np.abs(sys_.dipoles_flat() - S)) < 1e-8
+
+
+def test_sum_rule_with_dipole_dipole(gpu, sg):
+    # test_correlation_sampling.jl:29-50 holds for any trajectory, here one driven by
+    # dipole-dipole interactions as well
+    cr = sg.fcc_primitive_crystal()
+    sys_ = sg.System(cr, [(1, sg.Moment(s=1, g=2))], "dipole", dims=(4, 4, 4), seed=111)
+    sys_.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    sys_.enable_dipole_dipole(0.3)
+    sys_.randomize_spins()
+    sc = sg.SampledCorrelations(sys_, measure=sg.ssf_trace(sys_, apply_g=False), energies=np.linspace(0, 10.0, 40), dt=0.08)
+    sg.add_sample(sc, sys_)
+    d = sc.data
+    diag = [c for c, (a, b) in enumerate(sc.measure.corr_pairs) if a == b]
+    tot = sum(d[c, 0, 0].sum() for c in diag)
+    assert tot.real == pytest.approx(sc.n_all_omega * 64 * 1.0, rel=1e-12)
