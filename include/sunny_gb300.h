@@ -107,9 +107,9 @@ int sgb_set_bonds(sgb_system* sys, const sgb_bond* bonds, int32_t nbonds);
  * periodic supercell. latvecs: unit-cell lattice vectors as the columns of a 3x3
  * column-major matrix; positions: [natoms][3] fractional; demag: 3x3 column-major
  * demagnetisation tensor. mu0_muB2 = 0 disables. Call after sgb_set_sites. Energy,
- * gradient, Langevin, implicit midpoint and minimize_energy then include the term (the
- * integrators run one launch per stage, since each gradient needs a transform over the
- * whole lattice); LocalSampler, SampledCorrelations trajectories, batches and the
+ * gradient, Langevin, implicit midpoint, SampledCorrelations trajectories and
+ * minimize_energy then include the term (the integrators run one launch per stage, since
+ * each gradient needs a transform over the whole lattice); LocalSampler, batches and the
  * adjoint return SGB_ERR_ARG. */
 int sgb_set_dipole_dipole(sgb_system* sys, double mu0_muB2, const double* demag, const double* latvecs,
                           const double* positions);
