@@ -4,7 +4,7 @@
 // sgb_energy_grad evaluates the gradient into a device scratch buffer that the handle
 // grows with cudaMalloc on first use. Some callers cannot allow that: a host that runs
 // under a fixed device-memory budget owned by its own pool allocator, or a real-time loop
-// that must not enter the driver's allocator. This variant writes the gradient into a
+// that must not enter the CUDA allocator. This variant writes the gradient into a
 // file-scope static device array instead, so a call performs no allocation of any kind.
 //
 // Limits and sharing rules:
