@@ -369,6 +369,8 @@ void ewald_free(sgb_system* s) {
     s->ewald_on = false;
 }
 
+int ensure_lr_grad(sgb_system* s, double** grad);
+
 // Adds the dipole-dipole gradient at state S (device, R) into grad ([ns][3] FP64 on the
 // device, may be null); *E (nullable) receives the dipole-dipole energy.
 template <class R>
@@ -387,6 +389,25 @@ int ewald_add(sgb_system* s, const R* S, double* grad, double* E) {
         for (int b = 0; b < EWALD_PART_BLOCKS; b++) t += hp[b];
         *E = t;
     }
+    return SGB_OK;
+}
+
+// SU(N) mode: adds the dipole-dipole term to HZ ([ns][N][2] on the device) through dE/dS
+// at the expected dipoles; *E (nullable) receives the dipole-dipole energy.
+template <class R>
+int ewald_add_sun(sgb_system* s, double* hz, double* E) {
+    if (!s->ewald_on) {
+        if (E) *E = 0;
+        return SGB_OK;
+    }
+    double* f;
+    int rc = ensure_lr_grad(s, &f);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(f, 0, sizeof(double) * 3 * (size_t)s->ns, s->stream));
+    if ((rc = ewald_add<R>(s, (const R*)s->S, f, E))) return rc;
+    if (hz && sun_launch_add_dipole_field<R>(model<R>(s), (const R*)s->Z, f, hz, s->stream))
+        return cuda_fail(s, cudaGetLastError(), "dipole field launch");
+    s->launches++;
     return SGB_OK;
 }
 
@@ -781,7 +802,6 @@ int sgb_set_dipole_dipole(sgb_system* s, double mu0_muB2, const double* demag, c
     ewald_free(s);
     if (mu0_muB2 == 0.0) return SGB_OK;
     if (!demag || !latvecs || !positions) return fail(s, SGB_ERR_ARG, "demag, latvecs and positions are required");
-    if (s->sun) return fail(s, SGB_ERR_ARG, "dipole-dipole interactions on the GPU support the dipole modes");
     if (!s->sites_set) return fail(s, SGB_ERR_STATE, "sgb_set_sites must be called before sgb_set_dipole_dipole");
     EwaldGeom G{};
     const int* L = s->d.dims;
@@ -964,6 +984,10 @@ int sgb_energy_grad(sgb_system* s, double* grad) {
     } else {
         rc = s->fp32 ? sun_launch_grad<float>(s->mf, (const float*)s->Z, (const float*)s->S, (const float*)s->Q, s->dbuf, s->stream)
                      : sun_launch_grad<double>(s->md, (const double*)s->Z, (const double*)s->S, (const double*)s->Q, s->dbuf, s->stream);
+        if (rc == SGB_OK && s->ewald_on) {
+            s->launches++;
+            if ((rc = s->fp32 ? ewald_add_sun<float>(s, s->dbuf, nullptr) : ewald_add_sun<double>(s, s->dbuf, nullptr))) return rc;
+        }
     }
     s->launches++;
     if (rc) return cuda_fail(s, cudaGetLastError(), "gradient launch");
@@ -991,7 +1015,7 @@ int sgb_energy(sgb_system* s, double* E, double* M3) {
     double out[4];
     CK(cudaMemcpyAsync(out, s->red, sizeof(out), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    if (s->ewald_on && !s->sun) {
+    if (s->ewald_on) {
         double Ed = 0;
         rc = s->fp32 ? ewald_add<float>(s, (const float*)s->S, nullptr, &Ed) : ewald_add<double>(s, (const double*)s->S, nullptr, &Ed);
         if (rc) return rc;
@@ -1015,6 +1039,7 @@ int sgb_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t s
     int rc = ensure_tables(s);
     if (rc) return rc;
     if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called before stepping");
+    if (s->ewald_on && s->sun) return fail(s, SGB_ERR_ARG, "SU(N) dynamics with dipole-dipole interactions is not supported on the GPU");
     if (s->ewald_on)
         return s->fp32 ? run_langevin_lr<float>(s, dt, damping, kT, seed, step0, nsteps, noise)
                        : run_langevin_lr<double>(s, dt, damping, kT, seed, step0, nsteps, noise);
@@ -1047,6 +1072,7 @@ int sgb_midpoint(sgb_system* s, double dt, double damping, double tol, int32_t m
     int rc = ensure_tables(s);
     if (rc) return rc;
     if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called before stepping");
+    if (s->ewald_on && s->sun) return fail(s, SGB_ERR_ARG, "SU(N) dynamics with dipole-dipole interactions is not supported on the GPU");
     if (s->ewald_on)
         return s->fp32 ? run_midpoint_lr<float>(s, dt, damping, tol, max_iters, nsteps, iters_out)
                        : run_midpoint_lr<double>(s, dt, damping, tol, max_iters, nsteps, iters_out);
@@ -1178,7 +1204,8 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
         if (lrc || util_launch_reduce(s->partials, nbE, 4, s->red, st)) return cuda_fail(s, cudaGetLastError(), "optimizer evaluation");
         s->launches += 4;
         double Ed = 0;
-        int erc = ewald_add<double>(s, S, grad, s->ewald_on ? &Ed : nullptr);
+        int erc = s->sun ? ewald_add_sun<double>(s, grad, s->ewald_on ? &Ed : nullptr)
+                         : ewald_add<double>(s, S, grad, s->ewald_on ? &Ed : nullptr);
         if (erc) return erc;
         if (dphi) {
             if (opt_launch_dphi(K, x, d, alpha, grad, kap, ns, part, st)) return cuda_fail(s, cudaGetLastError(), "optimizer launch");
@@ -1590,6 +1617,8 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
     sgb_system* s = c->sys;
     sgb_batch* b = c->batch;
     if (!s && !b) return cfail(c, SGB_ERR_STATE, "the System (or replica batch) of this accumulator was destroyed");
+    if (s && s->sun && s->ewald_on)
+        return cfail(c, SGB_ERR_ARG, "SU(N) dynamics with dipole-dipole interactions is not supported on the GPU");
     if (window != 0 && window != 1) return cfail(c, SGB_ERR_ARG, "window must be 0 (:cosine) or 1 (:rectangular)");
     if (c->window >= 0 && c->window != window)
         return cfail(c, SGB_ERR_ARG, "all samples of one accumulator must use the same window");

@@ -80,6 +80,9 @@ template <class R>
 int dip_launch_snapshot(const Model<R>& M, const R* S, const SnapArgs<R>& sn, int t, cudaStream_t st);
 template <class R>
 size_t sun_cluster_smem(const Model<R>& M, int nsl);
+// hz ([ns][N][2]) += (f · S) Z for a per-site dipole field f ([ns][3], dE/dS)
+template <class R>
+int sun_launch_add_dipole_field(const Model<R>& M, const R* Z, const double* f, double* hz, cudaStream_t st);
 template <class R>
 int sun_launch_heun_cluster(const Model<R>& M, R* Z, R* D, R* Q, int cs, int nsteps, double dt, double lam, double nscale,
                             uint64_t seed, uint64_t step0, const double* noise, cudaStream_t st);

@@ -659,6 +659,43 @@ int grid1d(const Model<R>& M) {
     return grid > 4096 ? 4096 : grid;
 }
 
+// HZ += (f · S) Z for an external dipole field f = dE/dS per site (the dipole-dipole term
+// of set_energy_grad_coherents!, Interactions.jl:596-669, which enters through dE/dS).
+template <class R, int N>
+__global__ void k_sun_add_dipole_field(const R* Z, const double* f, double* hz, int ns) {
+    SpinConst<R, N> sc;
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < ns; site += gridDim.x * blockDim.x) {
+        const double dx = f[3 * (size_t)site], dy = f[3 * (size_t)site + 1], dz = f[3 * (size_t)site + 2];
+        double z[2 * N];
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) z[c] = (double)Z[(size_t)c * ns + site];
+#pragma unroll
+        for (int r = 0; r < N; r++) {
+            double ar = dz * (double)sc.sz[r] * z[2 * r], ai = dz * (double)sc.sz[r] * z[2 * r + 1];
+            if (r + 1 < N) {   // (dx - i dy) off_r z_{r+1}
+                const double o = (double)sc.off[r], pr = o * dx, pi = -o * dy;
+                ar += pr * z[2 * r + 2] - pi * z[2 * r + 3];
+                ai += pr * z[2 * r + 3] + pi * z[2 * r + 2];
+            }
+            if (r > 0) {       // (dx + i dy) off_{r-1} z_{r-1}
+                const double o = (double)sc.off[r - 1], pr = o * dx, pi = o * dy;
+                ar += pr * z[2 * r - 2] - pi * z[2 * r - 1];
+                ai += pr * z[2 * r - 1] + pi * z[2 * r - 2];
+            }
+            hz[(size_t)site * 2 * N + 2 * r] += ar;
+            hz[(size_t)site * 2 * N + 2 * r + 1] += ai;
+        }
+    }
+}
+
+template <class R, int N>
+int add_field_n(const R* Z, const double* f, double* hz, int ns, cudaStream_t st) {
+    int grid = (ns + SGB_BLOCK - 1) / SGB_BLOCK;
+    if (grid > 4096) grid = 4096;
+    k_sun_add_dipole_field<R, N><<<grid, SGB_BLOCK, 0, st>>>(Z, f, hz, ns);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
 // ---- Langevin for small SU(N) lattices held by one thread-block cluster ---------------
 // HZ of one site with the neighbours' expected dipoles (and quadrupoles) fetched through
 // loaders, bonds in table order (the same sums as sun_field).
@@ -1186,6 +1223,12 @@ int sun_launch_energy(const Model<R>& M, const R* Z, const R* D, const R* Q, dou
 }
 
 template <class R>
+int sun_launch_add_dipole_field(const Model<R>& M, const R* Z, const double* f, double* hz, cudaStream_t st) {
+    SGB_SUN_DISPATCH((add_field_n<R, 2>(Z, f, hz, M.ns, st)), (add_field_n<R, 3>(Z, f, hz, M.ns, st)),
+                     (add_field_n<R, 4>(Z, f, hz, M.ns, st)), (add_field_n<R, 5>(Z, f, hz, M.ns, st)))
+}
+
+template <class R>
 size_t sun_cluster_smem(const Model<R>& M, int nsl) {
     return (size_t)((M.tables_bytes + 15) / 16) * 16 + (size_t)(8 * M.N + 6 + (M.has_biquad ? 10 : 0)) * nsl * sizeof(R);
 }
@@ -1232,6 +1275,7 @@ int sun_launch_local_dE(const Model<R>& M, const R* Z, const R* D, const R* Q, i
     template int sun_launch_local_sweeps<R>(const Model<R>&, R*, R*, R*, Ctrl*, const McArgs&, int, double*, cudaStream_t); \
     template int sun_mc_max_blocks<R>(const Model<R>&, int*);                                                    \
     template size_t sun_cluster_smem<R>(const Model<R>&, int);                                                  \
+    template int sun_launch_add_dipole_field<R>(const Model<R>&, const R*, const double*, double*, cudaStream_t); \
     template int sun_launch_heun_cluster<R>(const Model<R>&, R*, R*, R*, int, int, double, double, double, uint64_t, \
                                             uint64_t, const double*, cudaStream_t);                            \
     template int sun_launch_local_dE<R>(const Model<R>&, const R*, const R*, const R*, int, const SunKet&, double*, cudaStream_t);

@@ -130,10 +130,12 @@ def test_midpoint_with_dipole_dipole(gpu, sg, orc):
     assert abs(sg.energy(sys_) - E0) <= 1e-3 * abs(E0)
 
 
-@pytest.mark.parametrize("jitter,ref", [(0.0, 0.6327349993784377), (1e-8, -5.7060439873282)])
-def test_canted_afm_optimization(gpu, sg, jitter, ref):
+@pytest.mark.parametrize("mode,jitter,ref", [("dipole", 0.0, 0.6327349993784377), ("dipole", 1e-8, -5.7060439873282),
+                                             ("SUN", 0.0, -0.619368052000758), ("SUN", 1e-8, -5.7060439873282)])
+def test_canted_afm_optimization(gpu, sg, mode, jitter, ref):
+    # test_optimization.jl:31-52, both modes
     cr = sg.Crystal(sg.lattice_vectors(1, 1, 2, 90, 90, 90), [[0, 0, 0]])
-    s = sg.System(cr, [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(4, 4, 1), seed=3)
+    s = sg.System(cr, [(1, sg.Moment(s=1.5, g=2))], mode, dims=(4, 4, 1), seed=3)
     s.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
     s.set_field([1.0, 0, 0])
     s.enable_dipole_dipole(1.0)
@@ -183,3 +185,28 @@ def test_sum_rule_with_dipole_dipole(gpu, sg):
     diag = [c for c, (a, b) in enumerate(sc.measure.corr_pairs) if a == b]
     tot = sum(d[c, 0, 0].sum() for c in diag)
     assert tot.real == pytest.approx(sc.n_all_omega * 64 * 1.0, rel=1e-12)
+
+
+def test_sun_gradient_with_dipole_dipole(gpu, sg, orc):
+    # HZ gains (dE/dS · S) Z with dE/dS the dipole-dipole field at the expected dipoles
+    cr = sg.Crystal(sg.lattice_vectors(1.1, 0.9, 1.3, 90, 90, 90), [[0, 0, 0], [0.5, 0.4, 0.3]])
+    s = sg.System(cr, [(1, sg.Moment(s=1, g=2))], "SUN", dims=(2, 2, 1), seed=7)
+    s.set_exchange(0.3, sg.Bond(1, 2, [0, 0, 0]))
+    s.set_onsite_coupling(lambda Sx, Sy, Sz: -0.4 * Sz @ Sz, 1)
+    s.set_onsite_coupling(lambda Sx, Sy, Sz: -0.4 * Sz @ Sz, 2)
+    s.randomize_spins()
+    demag = np.eye(3) / 3
+    s.enable_dipole_dipole(0.7, demag)
+    o = oracle_of(orc, s)
+    Z = s.coherents_flat()
+    S = o.expected_spin(Z)
+    A = orc.ewald_matrices(s.dims, cr.latvecs, [cr.position(i) for i in (1, 2)], demag, 0.7)
+    f = orc.ewald_pairwise_grad(A, s.dims, s.natoms, S, s._g)
+    Sx, Sy, Sz = sg.spin_matrices_of_dim(3)
+    hz_ref = o.grad(None, Z) + np.einsum("sa,abc,sc->sb", f, np.stack([Sx, Sy, Sz]), Z)
+    hz = sg.energy_grad(s)
+    assert np.max(np.abs(hz - hz_ref)) < 1e-12 * np.max(np.abs(hz_ref))
+    E_ref = o.energy(S, Z) + 0.5 * np.sum(S * f)
+    assert sg.energy(s) == pytest.approx(E_ref, abs=1e-12 * abs(E_ref))
+    with pytest.raises(sg.SunnyGPUError, match="SU\\(N\\) dynamics"):
+        sg.step(s, sg.Langevin(0.01, damping=0.1, kT=0.1))
