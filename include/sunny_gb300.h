@@ -102,15 +102,16 @@ int sgb_set_onsite(sgb_system* sys, int32_t atom, const double* coeffs);
 /* Replaces the whole pair-coupling table (Interactions.jl:1-42 `repopulate_couplings…`). */
 int sgb_set_bonds(sgb_system* sys, const sgb_bond* bonds, int32_t nbonds);
 
-/* enable_dipole_dipole!(sys, μ0_μB²; demag) (Interactions.jl:180-188, Ewald.jl:1-207),
- * dipole modes: Ewald-summed dipole-dipole energy E = μ (A ⋆ μ)/2 with μ = -g S over the
+/* enable_dipole_dipole!(sys, μ0_μB²; demag) (Interactions.jl:180-188, Ewald.jl:1-207):
+ * Ewald-summed dipole-dipole energy E = μ (A ⋆ μ)/2 with μ = -g S over the
  * periodic supercell. latvecs: unit-cell lattice vectors as the columns of a 3x3
  * column-major matrix; positions: [natoms][3] fractional; demag: 3x3 column-major
  * demagnetisation tensor. mu0_muB2 = 0 disables. Call after sgb_set_sites. Energy,
  * gradient, Langevin, implicit midpoint, SampledCorrelations trajectories and
  * minimize_energy then include the term (the integrators run one launch per stage, since
  * each gradient needs a transform over the whole lattice); LocalSampler, batches and the
- * adjoint return SGB_ERR_ARG. */
+ * adjoint return SGB_ERR_ARG. In SU(N) mode (S = expected dipoles) energy, gradient and
+ * minimize_energy include it and the integrators return SGB_ERR_ARG. */
 int sgb_set_dipole_dipole(sgb_system* sys, double mu0_muB2, const double* demag, const double* latvecs,
                           const double* positions);
 
