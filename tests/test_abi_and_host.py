@@ -37,6 +37,8 @@ def test_struct_layouts_match_header(sg):
     assert ctypes.sizeof(_abi.BondC) == 4 * 5 + 4 + 8 + 72 + 4 + 4 + 200  # i,j,n[3], pad, scalar, bilin, kind, pad, biquad
     assert ctypes.sizeof(_abi.Desc) == 8 * 4
     assert _abi.CorrDesc.dt.offset == 40
+    # sgb_proposal: int32 n, int32 kind[4], (pad), double weight[4], double magnitude[4]
+    assert ctypes.sizeof(_abi.Proposal) == 88 and _abi.Proposal.weight.offset == 24
 
 
 def test_create_without_gpu_fails_cleanly(sg):
