@@ -43,40 +43,56 @@ __device__ inline R mc_local_dE(const Model<R>& M, const Tab<R>& T, int site, in
     }
     R Qn[5], Qo[5];
     bool haveQ = false;
-    for (int b = T.boff[a], k = 0; b < T.boff[a + 1]; b++, k++) {
-        const DBond<R>& B = T.bonds[b];
-        const int j = M.nbr[(size_t)k * ns + site];
-        const R tx = sgb_ld(S + j), ty = sgb_ld(S + ns + j), tz = sgb_ld(S + 2 * ns + j);
-        if (B.jkind == 0) {
-            dE += B.J[0] * (dx * tx + dy * ty + dz * tz);
-        } else {
-            dE += dx * (B.J[0] * tx + B.J[3] * ty + B.J[6] * tz) + dy * (B.J[1] * tx + B.J[4] * ty + B.J[7] * tz) +
-                  dz * (B.J[2] * tx + B.J[5] * ty + B.J[8] * tz);
-        }
-        if (M.dipole_mode && B.bqkind != 0) {
-            if (!haveQ) {
-                quad5<R>(nx, ny, nz, Qn);
-                quad5<R>(ox, oy, oz, Qo);
-                haveQ = true;
-            }
-            R Qj[5];
-            quad5<R>(tx, ty, tz, Qj);
-            R acc = 0;
-            if (B.bqkind == 1) {
+    // neighbour indices and spins are fetched MC_GATHER bonds at a time, so that their
+    // loads are in flight together instead of one dependent pair of loads per bond
+    constexpr int MC_GATHER = 8;
+    const int b0 = T.boff[a], b1 = T.boff[a + 1];
+    for (int bb = b0; bb < b1; bb += MC_GATHER) {
+        int js[MC_GATHER];
+        R txs[MC_GATHER], tys[MC_GATHER], tzs[MC_GATHER];
 #pragma unroll
-                for (int q = 0; q < 5; q++) acc += (Qn[q] - Qo[q]) * ((R)biquad_metric(q) * Qj[q]);
-                acc *= B.bq;
+        for (int g = 0; g < MC_GATHER; g++)
+            if (bb + g < b1) js[g] = __ldg(M.nbr + (size_t)(bb + g - b0) * ns + site);
+#pragma unroll
+        for (int g = 0; g < MC_GATHER; g++)
+            if (bb + g < b1) { txs[g] = sgb_ld(S + js[g]); tys[g] = sgb_ld(S + ns + js[g]); tzs[g] = sgb_ld(S + 2 * ns + js[g]); }
+#pragma unroll
+        for (int g = 0; g < MC_GATHER; g++) {
+            if (bb + g >= b1) break;
+            const int b = bb + g;
+            const DBond<R>& B = T.bonds[b];
+            const R tx = txs[g], ty = tys[g], tz = tzs[g];
+            if (B.jkind == 0) {
+                dE += B.J[0] * (dx * tx + dy * ty + dz * tz);
             } else {
-                const R* Bm = T.bq + 25 * B.bqidx;
-#pragma unroll
-                for (int q = 0; q < 5; q++) {
-                    R r = 0;
-#pragma unroll
-                    for (int p = 0; p < 5; p++) r += Bm[q + 5 * p] * Qj[p];
-                    acc += (Qn[q] - Qo[q]) * r;
-                }
+                dE += dx * (B.J[0] * tx + B.J[3] * ty + B.J[6] * tz) + dy * (B.J[1] * tx + B.J[4] * ty + B.J[7] * tz) +
+                      dz * (B.J[2] * tx + B.J[5] * ty + B.J[8] * tz);
             }
-            dE += acc;
+            if (M.dipole_mode && B.bqkind != 0) {
+                if (!haveQ) {
+                    quad5<R>(nx, ny, nz, Qn);
+                    quad5<R>(ox, oy, oz, Qo);
+                    haveQ = true;
+                }
+                R Qj[5];
+                quad5<R>(tx, ty, tz, Qj);
+                R acc = 0;
+                if (B.bqkind == 1) {
+#pragma unroll
+                    for (int q = 0; q < 5; q++) acc += (Qn[q] - Qo[q]) * ((R)biquad_metric(q) * Qj[q]);
+                    acc *= B.bq;
+                } else {
+                    const R* Bm = T.bq + 25 * B.bqidx;
+#pragma unroll
+                    for (int q = 0; q < 5; q++) {
+                        R r = 0;
+#pragma unroll
+                        for (int p = 0; p < 5; p++) r += Bm[q + 5 * p] * Qj[p];
+                        acc += (Qn[q] - Qo[q]) * r;
+                    }
+                }
+                dE += acc;
+            }
         }
     }
     return dE;

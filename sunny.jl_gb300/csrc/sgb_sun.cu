@@ -934,36 +934,51 @@ __device__ inline R sun_local_dE(const Model<R>& M, const SunTab<R, N>& S, int s
     if (M.h) dE += M.h[site] * dx + M.h[ns + site] * dy + M.h[2 * ns + site] * dz;
     const R* lam = S.lam + a * 2 * N * N;
     dE += onsite_energy<R, N>(lam, zn) - onsite_energy<R, N>(lam, z0);
-    for (int b = S.t.boff[a], k = 0; b < S.t.boff[a + 1]; b++, k++) {
-        const DBond<R>& B = S.t.bonds[b];
-        const int j = M.nbr[(size_t)k * ns + site];
-        const R tx = sgb_ld(D + j), ty = sgb_ld(D + ns + j), tz = sgb_ld(D + 2 * ns + j);
-        if (B.jkind == 0) {
-            dE += B.J[0] * (dx * tx + dy * ty + dz * tz);
-        } else {
-            dE += dx * (B.J[0] * tx + B.J[3] * ty + B.J[6] * tz) + dy * (B.J[1] * tx + B.J[4] * ty + B.J[7] * tz) +
-                  dz * (B.J[2] * tx + B.J[5] * ty + B.J[8] * tz);
-        }
-        if (BQ && B.bqkind != 0) {
-            R Qj[5];
+    // neighbour indices and dipoles are fetched 8 bonds at a time (loads in flight together)
+    constexpr int GATHER = 8;
+    const int b0 = S.t.boff[a], b1 = S.t.boff[a + 1];
+    for (int bb = b0; bb < b1; bb += GATHER) {
+        int js[GATHER];
+        R txs[GATHER], tys[GATHER], tzs[GATHER];
 #pragma unroll
-            for (int q = 0; q < 5; q++) Qj[q] = sgb_ld(Qb + (size_t)q * ns + j);
-            R acc = 0;
-            if (B.bqkind == 1) {
+        for (int g = 0; g < GATHER; g++)
+            if (bb + g < b1) js[g] = __ldg(M.nbr + (size_t)(bb + g - b0) * ns + site);
 #pragma unroll
-                for (int q = 0; q < 5; q++) acc += (qn[q] - q0[q]) * ((R)biquad_metric(q) * Qj[q]);
-                acc *= B.bq;
+        for (int g = 0; g < GATHER; g++)
+            if (bb + g < b1) { txs[g] = sgb_ld(D + js[g]); tys[g] = sgb_ld(D + ns + js[g]); tzs[g] = sgb_ld(D + 2 * ns + js[g]); }
+#pragma unroll
+        for (int g = 0; g < GATHER; g++) {
+            if (bb + g >= b1) break;
+            const DBond<R>& B = S.t.bonds[bb + g];
+            const int j = js[g];
+            const R tx = txs[g], ty = tys[g], tz = tzs[g];
+            if (B.jkind == 0) {
+                dE += B.J[0] * (dx * tx + dy * ty + dz * tz);
             } else {
-                const R* Bm = S.t.bq + 25 * B.bqidx;
-#pragma unroll
-                for (int q = 0; q < 5; q++) {
-                    R r = 0;
-#pragma unroll
-                    for (int p = 0; p < 5; p++) r += Bm[q + 5 * p] * Qj[p];
-                    acc += (qn[q] - q0[q]) * r;
-                }
+                dE += dx * (B.J[0] * tx + B.J[3] * ty + B.J[6] * tz) + dy * (B.J[1] * tx + B.J[4] * ty + B.J[7] * tz) +
+                      dz * (B.J[2] * tx + B.J[5] * ty + B.J[8] * tz);
             }
-            dE += acc;
+            if (BQ && B.bqkind != 0) {
+                R Qj[5];
+#pragma unroll
+                for (int q = 0; q < 5; q++) Qj[q] = sgb_ld(Qb + (size_t)q * ns + j);
+                R acc = 0;
+                if (B.bqkind == 1) {
+#pragma unroll
+                    for (int q = 0; q < 5; q++) acc += (qn[q] - q0[q]) * ((R)biquad_metric(q) * Qj[q]);
+                    acc *= B.bq;
+                } else {
+                    const R* Bm = S.t.bq + 25 * B.bqidx;
+#pragma unroll
+                    for (int q = 0; q < 5; q++) {
+                        R r = 0;
+#pragma unroll
+                        for (int p = 0; p < 5; p++) r += Bm[q + 5 * p] * Qj[p];
+                        acc += (qn[q] - q0[q]) * r;
+                    }
+                }
+                dE += acc;
+            }
         }
     }
     return dE;
