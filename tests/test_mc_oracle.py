@@ -130,3 +130,26 @@ def test_replica_batch_rejects_dipole_dipole(sg):
     s.enable_dipole_dipole(1.0)
     with pytest.raises(ValueError, match="dipole-dipole"):
         sg.ReplicaBatch(s, [s.dims] * 2, kT=[0.1, 0.2])
+
+
+def test_enable_dipole_dipole_host_settings(sg):
+    s = sc_c1(sg, L=2, device=None)
+    with pytest.warns(UserWarning, match="Deprecated"):
+        s.enable_dipole_dipole()
+    mu0, demag = s._ewald
+    assert mu0 == pytest.approx(0.6745817653)
+    assert np.allclose(demag, np.eye(3) / 3)
+    s.enable_dipole_dipole(0.5, demag=np.diag([0.1, 0.2, 0.7]))
+    c = sg.clone_system(s, seed=3)
+    assert c._ewald[0] == 0.5 and np.allclose(c._ewald[1], np.diag([0.1, 0.2, 0.7]))
+    assert c._ewald_dirty
+
+
+def test_oracle_ewald_single_dipole_known_answer(orc):
+    # test_ewald.jl:18-30: one dipole (g = 1, |S| = 1) in a unit cubic box, demag 0: E = -1/6
+    A = orc.ewald_matrices((1, 1, 1), np.eye(3), [[0, 0, 0]], np.zeros((3, 3)), 1.0)
+    mu = np.array([0.0, 0.0, -1.0])
+    assert 0.5 * mu @ A[0, 0, 0] @ mu == pytest.approx(-1 / 6, abs=1e-13)
+    A = orc.ewald_matrices((2, 3, 4), np.eye(3), [[0, 0, 0]], np.zeros((3, 3)), 1.0)
+    E = 0.5 * sum(mu @ A[c, 0, 0] @ mu for c in range(24))
+    assert E == pytest.approx(-1 / 6, abs=1e-13)
