@@ -680,6 +680,12 @@ class MinimizationResult:
     niters: int
     energy: float
 
+    def __str__(self):
+        # Optimization.jl:12-20
+        if self.converged:
+            return f"Converged in {self.niters} iterations"
+        return f"Non-converged after {self.niters} iterations"
+
 
 def minimize_energy(sys: System, maxiters: int = 1000, jitter: float = 1e-8) -> MinimizationResult:
     """minimize_energy!(sys; maxiters=1000, jitter=1e-8) (Optimization.jl:102-166), dipole
@@ -696,7 +702,7 @@ def minimize_energy(sys: System, maxiters: int = 1000, jitter: float = 1e-8) -> 
     res = MinimizationResult(bool(conv.value), int(nit.value), float(E.value))
     if not res.converged:
         import warnings
-        warnings.warn(f"Non-converged after {res.niters} iterations")
+        warnings.warn(str(res))
     return res
 
 

@@ -153,3 +153,8 @@ def test_oracle_ewald_single_dipole_known_answer(orc):
     A = orc.ewald_matrices((2, 3, 4), np.eye(3), [[0, 0, 0]], np.zeros((3, 3)), 1.0)
     E = 0.5 * sum(mu @ A[c, 0, 0] @ mu for c in range(24))
     assert E == pytest.approx(-1 / 6, abs=1e-13)
+
+
+def test_minimization_result_text(sg):
+    assert str(sg.MinimizationResult(True, 12, -1.0)) == "Converged in 12 iterations"
+    assert str(sg.MinimizationResult(False, 1000, -1.0)) == "Non-converged after 1000 iterations"
