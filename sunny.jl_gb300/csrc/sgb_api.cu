@@ -1254,18 +1254,18 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
         };
         double a = alpha_prev == 0 ? 0.01 / gmax : alpha_prev * dphi_prev / dphi0;   // N&W (3.60)
         a = std::min(a, amax);
-        double lo = 0, flo = phi0, dlo = dphi0, hi = -1, fhi = 0, dhi = 0;
+        double lo = 0, flo = phi0, dlo = dphi0, hi = -1, dhi = 0;
         double acc_a = -1, acc_f = 0;
         for (int k = 0; k < 60 && acc_a < 0; k++) {
             double fa, da;
             if ((rc = eval(a, &fa, &da))) return rc;
             if (!std::isfinite(fa) || !std::isfinite(da)) {
-                hi = a; fhi = INFINITY; dhi = INFINITY;
+                hi = a; dhi = INFINITY;
             } else if (wolfe(a, fa, da)) {
                 acc_a = a; acc_f = fa;
                 break;
             } else if (da >= 0 || (fa > phi0 + eps && fa > phi0 + del * a * dphi0) || (hi < 0 && fa > flo + eps)) {
-                hi = a; fhi = fa; dhi = da;
+                hi = a; dhi = da;
             } else {
                 lo = a; flo = fa; dlo = da;
             }
@@ -1284,7 +1284,6 @@ int sgb_minimize_energy(sgb_system* s, int32_t maxiters, double jitter, uint64_t
             }
             a = t;
         }
-        (void)fhi;
         if (acc_a < 0) {
             if (restarted) {
                 // second failure in a row: no step decreases E at FP64 resolution, so x no
