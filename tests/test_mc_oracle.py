@@ -158,3 +158,28 @@ def test_oracle_ewald_single_dipole_known_answer(orc):
 def test_minimization_result_text(sg):
     assert str(sg.MinimizationResult(True, 12, -1.0)) == "Converged in 12 iterations"
     assert str(sg.MinimizationResult(False, 1000, -1.0)) == "Non-converged after 1000 iterations"
+
+
+def test_oracle_local_sweeps_heisenberg_ring(sg, orc):
+    # the oracle's Metropolis restatement samples the classical Heisenberg ring:
+    # <S_i · S_i+1> = coth(βJ) - 1/(βJ) for unit spins (Fisher 1964)
+    import math
+    J, kT = -1.0, 0.5
+    cr = sg.Crystal(sg.lattice_vectors(1, 1.3, 1.7, 90, 90, 90), [[0, 0, 0]])
+    n = 512
+    s = sg.System(cr, [(1, sg.Moment(s=1, g=2))], "dipole_uncorrected", dims=(n, 1, 1), seed=3, device=None)
+    s.set_exchange(J, sg.Bond(1, 1, [1, 0, 0]))
+    s.randomize_spins()
+    o = orc.OracleSystem.from_system(s)
+    rng = np.random.default_rng(8)
+    S = s.dipoles_flat()
+    order = np.arange(n)
+    prop = [(2, 1.0, 0.8)]
+    Es = []
+    for block in range(300):
+        rand = np.concatenate([rng.standard_normal((10, n, 3)), rng.random((10, n, 3))], axis=2)
+        S, _, _ = o.local_sweeps(S, kT, 10, 1.0, order, prop, rand)
+        if block >= 50:
+            Es.append(o.energy(S) / n)
+    exact = J * (1 / math.tanh(abs(J) / kT) - kT / abs(J))
+    assert np.mean(Es) == pytest.approx(exact, rel=0.02)
