@@ -183,3 +183,26 @@ def test_oracle_local_sweeps_heisenberg_ring(sg, orc):
             Es.append(o.energy(S) / n)
     exact = J * (1 / math.tanh(abs(J) / kT) - kT / abs(J))
     assert np.mean(Es) == pytest.approx(exact, rel=0.02)
+
+
+def test_oracle_sun_local_sweeps_anisotropy_energy(sg, orc):
+    # SU(3) spins with Λ = D Sz², no couplings (test_samplers.jl:5-10): the oracle's
+    # Metropolis sweeps reproduce the exact thermal mean energy
+    import math
+    D, kT, n = 1.0, 0.5, 512
+    s = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "SUN", dims=(8, 8, 8), seed=4, device=None)
+    s.set_onsite_coupling(lambda Sx, Sy, Sz: D * Sz @ Sz, 1)
+    s.randomize_spins()
+    o = orc.OracleSystem.from_system(s)
+    rng = np.random.default_rng(12)
+    Z = s.coherents_flat()
+    S = o.expected_spin(Z)
+    Es = []
+    for block in range(120):
+        rand = np.concatenate([rng.standard_normal((5, n, 6)) / np.sqrt(2), rng.random((5, n, 3))], axis=2)
+        S, Z, _, _ = o.local_sweeps_sun(S, Z, kT, 5, 1.0, np.arange(n), [(0, 1.0, 0.0)], rand)
+        if block >= 20:
+            Es.append(o.energy(S, Z) / n)
+    a = D / kT
+    exact = D * (2 - (2 + 2 * a + a * a) * math.exp(-a)) / (a * (1 - (1 + a) * math.exp(-a)))
+    assert np.mean(Es) == pytest.approx(exact, rel=0.02)
