@@ -152,6 +152,83 @@ def run_arm(sg, precision, device, warmup, steps, tol, thermal_steps=2000, e2e_s
     return res
 
 
+def stated_error(sg, device, L_=16, nomega=200, nrep=8, nsamples=32, decorr=1000, thermal_steps=2000, seed=11):
+    """Error of the FP32 batched S(q,w) path against the plain FP64 path on the pyrochlore
+    model with L_^3 conventional cells (L_=16, nomega=200 is the benchmark workload).
+
+    Energy: every FP32 batched add_sample integrates nrep 4,179-step (at nomega=200)
+    implicit-midpoint trajectories at tol 1e-6 with the degree-4 first iterate; the
+    relative change of each replica's FP64-reduced energy over its trajectory is its
+    energy error (the exact dynamics conserve energy). The FP64 path (tol 1e-12) runs the
+    same trajectory from replica 0's start for comparison.
+    S(q,w): nsamples samples on each path (calculate_errors=true), every sample after a
+    decorrelating Langevin run (kT 0.2, damping 0.1, `decorr` steps), compared bin by bin
+    with compare_correlations against the combined Welford error bars."""
+    cr = sg.pyrochlore_crystal()
+
+    def model(precision, dev):
+        s_ = sg.System(cr, [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(L_, L_, L_), seed=seed, precision=precision,
+                       device=dev)
+        s_.set_exchange(1.0, cr.bonds_at_distance(math.sqrt(2) / 4)[0])
+        s_.set_exchange(0.05, cr.bonds_at_distance(math.sqrt(6) / 4)[0])
+        s_.randomize_spins()
+        return s_
+
+    energies = np.linspace(0, WMAX, nomega)
+    proto = model("fp32", None)
+    b = sg.ReplicaBatch(proto, [proto.dims] * nrep, kT=[0.2] * nrep, precision="fp32", device=device, seed=seed)
+    b.randomize_spins()
+    b.langevin(DT, 0.1, thermal_steps)
+    s64 = model("fp64", device)
+    s64.set_state_flat(dipoles=b.get_state(0))
+    sc32 = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), energies=energies, dt=DT, tol=1e-6,
+                                  calculate_errors=True)
+    sc64 = sg.SampledCorrelations(s64, measure=sg.ssf_trace(s64), energies=energies, dt=DT, tol=1e-12,
+                                  calculate_errors=True)
+    nsteps = sc32.measperiod * (sc32.n_all_omega // 2)
+    lang = sg.Langevin(DT, damping=0.1, kT=0.2)
+    e32, e64 = [], []
+    E64_first = None
+    t0 = time.perf_counter()
+    for p in range(nsamples // nrep):
+        if p:
+            b.langevin(DT, 0.1, decorr)
+        Ea = b.energies()
+        sg.add_sample(sc32, b)
+        Eb = b.energies()
+        e32.extend(np.abs(Eb - Ea) / np.abs(Ea))
+        if p == 0:
+            E32_first = Eb[0]
+    for k in range(nsamples):
+        if k:
+            sg.step(s64, lang, nsteps=decorr)
+        Ea = sg.energy(s64)
+        sg.add_sample(sc64, s64)
+        Eb = sg.energy(s64)
+        e64.append(abs(Eb - Ea) / abs(Ea))
+        if k == 0:
+            E64_first = Eb
+    cmp = sg.compare_correlations(sc32, sc64)
+    wall = time.perf_counter() - t0
+    sc32.close()
+    sc64.close()
+    b.close()
+    s64.close()
+    e32 = np.array(e32)
+    return {"workload": f"pyrochlore {L_}^3 x 16 ({16 * L_**3} spins), nw={nomega}, {nsteps} midpoint steps per sample, "
+                        f"{nsamples} samples per path ({nrep} replicas x {nsamples // nrep} on FP32), "
+                        f"{decorr} Langevin steps between samples",
+            "energy_rel_err_per_sample_max": float(e32.max()),
+            "energy_rel_err_per_sample_median": float(np.median(e32)),
+            "energy_rel_err_per_step": float(e32.max()) / nsteps,
+            "energy_rel_err_vs_fp64_same_start": float(abs(E32_first - E64_first) / abs(E64_first)),
+            "fp64_energy_rel_err_per_sample_max": float(max(e64)),
+            "sqw_vs_fp64": cmp,
+            "sqw_systematic_rel_rms_bound": cmp["bias_rel_bound"],
+            "steps_per_sample": nsteps, "wall_s": wall,
+            "limits": {"energy_rel_err": 1e-5, "sqw_per_bin_rel": 1e-2}}
+
+
 def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000, predictor=None):
     """Batched FP32 sampling: `nrep` replicas of the pyrochlore model advance in one
     persistent launch; each add_sample adds nrep samples with a rank-nrep accumulator pass."""
@@ -481,6 +558,8 @@ def main():
     ap.add_argument("--nrep", type=int, default=8, help="replicas sampled per batched add_sample")
     ap.add_argument("--nomega", type=int, default=200, help="energy bins (200 is the benchmark; fewer for profiling)")
     ap.add_argument("--no-extra", action="store_true", help="skip the tempering and Langevin site-step arms")
+    ap.add_argument("--no-error", action="store_true", help="skip the stated-error measurement (FP32 vs FP64)")
+    ap.add_argument("--error-samples", type=int, default=32, help="samples per path of the stated-error measurement")
     ap.add_argument("--predictor", type=int, default=None,
                     help="first-iterate extrapolation order of the batched midpoint (library default if omitted)")
     args = ap.parse_args()
@@ -538,6 +617,9 @@ def main():
         c3 = {"fp32": run_c3_sqw(sg, local, "fp32", 2), "fp64": run_c3_sqw(sg, local, "fp64", 1)}
         c3["speedup"] = c3["fp32"]["samples_per_s"] / c3["fp64"]["samples_per_s"]
         extra["c3_sqw"] = c3
+    err = None
+    if not args.no_error:
+        err = stated_error(sg, local, L_=L, nomega=NOMEGA, nrep=args.nrep, nsamples=args.error_samples)
     barrier()
     ms = maxall(rb["ms"])
     value = world * args.steps * rb["nrep"] / (ms / 1000.0)
@@ -582,7 +664,6 @@ def main():
             "fp64_plain": None if r64 is None else
             {"value": v64, "unit": "samples/s", "site_steps_per_s": v64 * r32["ns"] * nsteps_sample,
              "ms_per_step": r64["ms"] / args.fp64_steps, "phase_ms": r64["phase_ms"]},
-            "speedup_vs_fp64_plain": None if r64 is None else value / v64,
             "phase_ms": {"trajectory": ph[0], "space_fft": ph[1], "time_fft": ph[2], "accumulate": ph[3]},
             "midpoint_iters_per_step": {"fp32_batched": rb["iters_per_step"], "fp32": r32["iters_per_step"],
                                         "fp64": None if r64 is None else r64["iters_per_step"]},
@@ -594,11 +675,19 @@ def main():
             "adjoint_c5": extra.get("adjoint"),
             "sqw_su3_triangular_48x48x4": extra.get("c3_sqw"),
             "local_sampler_simple_cubic_16^3": extra.get("local_sampler_sc"),
+            "error_detail": err,
             "roofline": roof,
             "gpu_launches": rb["launches"],
             "clocks": rb["clocks"],
             "e2e": {"value": e2e_val, "unit": "samples/s", "h2d_bytes_per_step": rb["h2d"],
-                    "d2h_bytes_per_step": rb["d2h"]}}
+                    "d2h_bytes_per_step": rb["d2h"]},
+            "speedup_vs_fp64_plain": None if r64 is None else value / v64,
+            "error": None if err is None else
+            {"energy_rel_err_per_sample_max": err["energy_rel_err_per_sample_max"],
+             "energy_rel_err_per_step": err["energy_rel_err_per_step"],
+             "sqw_chi2_ratio_vs_fp64": err["sqw_vs_fp64"]["chi2_ratio"],
+             "sqw_systematic_rel_rms_bound": err["sqw_systematic_rel_rms_bound"],
+             "limits": err["limits"]}}
     if L != 16 or NOMEGA != 200:
         line["config"]["workload"] = (f"REDUCED SIZE L={L}, nw={NOMEGA} (profiling case, not the benchmark): "
                                       + line["config"]["workload"])
@@ -609,6 +698,8 @@ def main():
                                           "the 1,536 (c,i,j) correlation blocks plus the sample FFTs on one core, "
                                           "extrapolated to one full add_sample",
                                 "midpoint_step_s": t_step}
+    for k in ("speedup_vs_fp64_plain", "error"):      # the summary keys last, where a tail shows them
+        line[k] = line.pop(k)
     barrier()
     if rank == 0:
         print(json.dumps(line), flush=True)

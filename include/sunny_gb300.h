@@ -78,6 +78,17 @@ typedef struct {
     double  biquad[25];   /* kind 1: biquad[0]; kind 2: 5x5 column-major               */
 } sgb_bond;
 
+/* One pair coupling of an inhomogeneous system (to_inhomogeneous,
+ * src/System/Interactions.jl:81-100): the non-culled PairCoupling held in the coupling
+ * list of site (cell, bond.i). Couplings set with set_exchange_at! / set_pair_coupling_at!
+ * (src/System/PairExchange.jl:447-534) are stored from both sites like every other bond,
+ * so pass only the non-culled copy; the library adds the reversed copy itself. */
+typedef struct {
+    int32_t  cell[3];     /* 0-based cell of the bond's first site; its atom is bond.i  */
+    int32_t  pad;
+    sgb_bond bond;        /* the coupling as seen from that site (raw cell offset n)    */
+} sgb_site_bond;
+
 /* ---- system lifetime ------------------------------------------------------- */
 
 /* Replaces System(...) construction of buffers (src/System/System.jl:33-93). */
@@ -99,8 +110,26 @@ int sgb_set_sites(sgb_system* sys, const double* kappa, const double* g, const d
  * column-major, interleaved (re,im). */
 int sgb_set_onsite(sgb_system* sys, int32_t atom, const double* coeffs);
 
-/* Replaces the whole pair-coupling table (Interactions.jl:1-42 `repopulate_couplings…`). */
+/* Replaces the whole pair-coupling table (Interactions.jl:1-42 `repopulate_couplings…`).
+ * The per-sublattice table replaces any per-site table of sgb_set_bonds_at. */
 int sgb_set_bonds(sgb_system* sys, const sgb_bond* bonds, int32_t nbonds);
+
+/* Inhomogeneous pair couplings: every site's own list, as Sunny keeps it after
+ * to_inhomogeneous (Interactions.jl:81-100) and edits it with set_exchange_at!,
+ * set_pair_coupling_at! (PairExchange.jl:447-534), set_vacancy_at! (Interactions.jl:237-257)
+ * and remove_periodicity!. `bonds` lists the non-culled couplings of all sites in any
+ * order; neighbours are bonded_site(site, bond) with the periodic wrap (System.jl:204-212).
+ * Replaces the per-sublattice table until the next sgb_set_bonds. Energy, gradient,
+ * Langevin, the implicit midpoint, SampledCorrelations, LocalSampler and
+ * minimize_energy use the per-site lists; replica batches and the adjoint return
+ * SGB_ERR_ARG for such a system. */
+int sgb_set_bonds_at(sgb_system* sys, const sgb_site_bond* bonds, int64_t nbonds);
+
+/* Per-site onsite couplings (set_onsite_coupling_at!, OnsiteCoupling.jl:222-231):
+ * coeffs[ns][28] renormalised Stevens coefficients (dipole modes) or [ns][N*N][2] Λ
+ * (SU(N) mode), in site order. Replaces the per-sublattice onsite couplings until the
+ * next sgb_set_onsite. */
+int sgb_set_onsite_at(sgb_system* sys, const double* coeffs);
 
 /* enable_dipole_dipole!(sys, μ0_μB²; demag) (Interactions.jl:180-188, Ewald.jl:1-207):
  * Ewald-summed dipole-dipole energy E = μ (A ⋆ μ)/2 with μ = -g S over the
@@ -136,7 +165,9 @@ int sgb_energy_grad(sgb_system* sys, double* grad);
  * by its own pool allocator or capped by a fixed budget, or a loop that must stay out of
  * the allocator. The gradient goes through one 8 MiB static device array (2^20 doubles) per
  * device, shared by every call: systems needing more (3 doubles per dipole site, 2N per
- * SU(N) site) get SGB_ERR_ARG; calls must not overlap (issue them one after another).
+ * SU(N) site, plus 3 per SU(N) site with dipole-dipole interactions) get SGB_ERR_ARG;
+ * calls must not overlap (issue them one after another). Dipole-dipole interactions are
+ * included as in sgb_energy_grad. The caller's current device is left unchanged.
  * The state must be set after the last coupling change (else SGB_ERR_STATE). The first
  * call on a device resolves the array's address; make it before any stream capture. */
 int sgb_energy_grad_static(sgb_system* sys, double* grad);
@@ -292,6 +323,14 @@ int sgb_corr_intensities(sgb_corr* sc, int32_t nq, const int32_t* qidx, const do
 /* merge_correlations([dst, src]) into dst (SampledCorrelations.jl:128-142), with M when
  * both were created with calculate_errors (mixing the two kinds is SGB_ERR_ARG). */
 int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src);
+/* Statistical comparison of two accumulators of the same shape, both made with
+ * calculate_errors and holding >= 2 samples (no counterpart in the reference; it states
+ * the error of one sampling path against another). Per bin, Δ = mean_a − mean_b and
+ * s = M_a/(n_a(n_a−1)) + M_b/(n_b(n_b−1)), the variance of Δ when both means estimate
+ * one S(q,ω). out[9]: Σ|Δ|², Σs, Σs², Σ|mean_b|², Σ|mean_a|², the number of bins with
+ * |Δ|² > 9s, the number with s > 0, the number of bins, and the variance of Σ(|Δ|² − s)
+ * estimated from the spread of 1024 partial sums over interleaved bin sets. */
+int sgb_corr_compare(const sgb_corr* a, const sgb_corr* b, double* out);
 
 /* Per-phase device time of add_sample!, summed over the samples taken while profiling is
  * on (CUDA events between phases; no Julia analogue): ms4[0] trajectory with snapshots,
@@ -410,6 +449,17 @@ int sgb_synchronize(sgb_system* sys);
 /* Number of this library's own kernels launched on the handle so far (cuFFT excluded). */
 int64_t sgb_kernel_launches(const sgb_system* sys);
 int64_t sgb_batch_kernel_launches(const sgb_batch* b);
+/* Wall-clock limit of the bounded waits (grid barriers) of this handle's persistent
+ * kernels (no counterpart in the reference, which has no device waits). A wait that runs
+ * past it makes the kernel record SGB_ERR_TIMEOUT and return, so the call fails with
+ * SGB_ERR_TIMEOUT and the handle stays usable. seconds = 0 restores the default, 4 s. */
+int sgb_set_wait_limit(sgb_system* sys, double seconds);
+int sgb_batch_set_wait_limit(sgb_batch* b, double seconds);
+/* Runs a grid barrier that expects one more CTA than it launches, so that it can only end
+ * at the wait limit (no counterpart in the reference). Returns SGB_ERR_TIMEOUT with the
+ * message of a timed-out barrier; lets callers check how their handle reports a wait that
+ * gave up. */
+int sgb_wait_probe(sgb_system* sys);
 /* Writes a 256 MiB device buffer on the handle's stream to evict L2. */
 int sgb_flush_l2(sgb_system* sys);
 /* Library version string. */

@@ -28,10 +28,16 @@ class BondC(C.Structure):
                 ("bilin", C.c_double * 9), ("biquad_kind", C.c_int32), ("biquad", C.c_double * 25)]
 
 
+class SiteBondC(C.Structure):
+    _fields_ = [("cell", C.c_int32 * 3), ("pad", C.c_int32), ("bond", BondC)]
+
+
 class OrSys(C.Structure):
     _fields_ = [("L", C.c_int * 3), ("na", C.c_int), ("N", C.c_int), ("mode", C.c_int),
                 ("kappa", C.POINTER(C.c_double)), ("g", C.POINTER(C.c_double)), ("field", C.POINTER(C.c_double)),
-                ("onsite", C.POINTER(C.c_double)), ("bonds", C.POINTER(BondC)), ("nbonds", C.c_int)]
+                ("onsite", C.POINTER(C.c_double)), ("bonds", C.POINTER(BondC)), ("nbonds", C.c_int),
+                ("onsite_site", C.POINTER(C.c_double)), ("site_bonds", C.POINTER(SiteBondC)),
+                ("nsite_bonds", C.c_int64)]
 
 
 _D = C.POINTER(C.c_double)
@@ -84,7 +90,10 @@ def _p(a):
 class OracleSystem:
     """FP64 CPU model built from the same host tables the GPU library receives."""
 
-    def __init__(self, dims, natoms, N, mode, kappa, g_colmajor, field, onsite, bonds):
+    def __init__(self, dims, natoms, N, mode, kappa, g_colmajor, field, onsite, bonds, onsite_site=None,
+                 site_bonds=None):
+        """onsite_site / site_bonds: the per-site onsite couplings and the non-culled per-site
+        pair couplings (SiteBondC) of an inhomogeneous system, else None."""
         self.lib = load()
         self.dims, self.na, self.N, self.mode = tuple(dims), natoms, N, mode
         self.ns = int(np.prod(dims)) * natoms
@@ -103,6 +112,16 @@ class OracleSystem:
         s.onsite = _p(self._keep[3])
         s.bonds = arr
         s.nbonds = len(bonds)
+        if onsite_site is not None:
+            self._onsite_site = np.ascontiguousarray(onsite_site, dtype=float).reshape(-1)
+            s.onsite_site = _p(self._onsite_site)
+        if site_bonds is not None:
+            sb = (SiteBondC * max(1, len(site_bonds)))()
+            for k, b in enumerate(site_bonds):
+                C.memmove(C.byref(sb[k]), C.byref(b), C.sizeof(SiteBondC))
+            self._site_bonds = sb
+            s.site_bonds = sb
+            s.nsite_bonds = len(site_bonds)
         self.s = s
 
     @classmethod
@@ -120,7 +139,10 @@ class OracleSystem:
         gcm = np.ascontiguousarray(sys._g.transpose(0, 2, 1)).reshape(-1)
         field = sys._field.reshape(-1) if np.any(sys._field) else None
         mode = {"dipole": MODE_DIPOLE, "dipole_uncorrected": MODE_DIPOLE_UNCORRECTED, "SUN": MODE_SUN}[sys.mode]
-        return cls(sys.dims, na, sys.N, mode, sys._kappa, gcm, field, onsite, sys.bond_table())
+        if sys.is_homogeneous():
+            return cls(sys.dims, na, sys.N, mode, sys._kappa, gcm, field, onsite, sys.bond_table())
+        return cls(sys.dims, na, sys.N, mode, sys._kappa, gcm, field, onsite, [], onsite_site=sys.onsite_site_table(),
+                   site_bonds=[SiteBondC.from_buffer_copy(bytes(b)) for b in sys.site_bond_table()])
 
     # ---- state helpers: S (ns, 3) float; Z (ns, N) complex --------------------------------
     def _zbuf(self, Z):

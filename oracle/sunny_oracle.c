@@ -37,6 +37,24 @@ static inline void cross3(const double* a, const double* b, double* out) {
     out[2] = a[0] * b[1] - a[1] * b[0];
 }
 
+/* Onsite coupling of site i: its own (inhomogeneous systems) or its sublattice's. */
+static const double* onsite_at(const or_sys* s, int64_t i) {
+    const int64_t ncell = (int64_t)s->L[0] * s->L[1] * s->L[2];
+    const int64_t per = s->mode == SGB_MODE_SUN ? 2 * (int64_t)s->N * s->N : 28;
+    if (s->onsite_site) return s->onsite_site + per * i;
+    if (s->onsite) return s->onsite + per * (i / ncell);
+    return NULL;
+}
+
+/* The two sites of an inhomogeneous coupling: (cell, bond.i) and
+ * bonded_site((cell, bond.i), bond) (System.jl:204-212). */
+static void site_bond_ends(const or_sys* s, const sgb_site_bond* e, int64_t* i, int64_t* j) {
+    const sgb_bond* b = &e->bond;
+    *i = site_index(s, e->cell[0], e->cell[1], e->cell[2], b->i);
+    *j = site_index(s, wrap(e->cell[0] + b->n[0], s->L[0]), wrap(e->cell[1] + b->n[1], s->L[1]),
+                    wrap(e->cell[2] + b->n[2], s->L[2]), b->j);
+}
+
 /* System.jl:421-423 normalize_dipole: κ*normalize(s) */
 static inline void normalize_dipole(const double* v, double kappa, double* out) {
     if (kappa == 0.0) { out[0] = out[1] = out[2] = 0.0; return; }
@@ -261,6 +279,48 @@ double or_classical_anisotropy(const double* cc, const double* S, double* grad3)
 }
 
 /* ---- Interactions.jl:516-592 set_energy_grad_dipoles! ------------------------------ */
+/* One non-culled coupling pc between sites i and j = bonded_site(i, pc.bond), scattered
+ * into both ends (Interactions.jl:554-591). */
+static void pair_grad_dipoles(const sgb_bond* pc, int64_t i, int64_t j, const double* S, double* grad, int dipole_mode) {
+    const double* J = pc->bilin;
+    const double* Si = S + 3 * i;
+    const double* Sj = S + 3 * j;
+    for (int r = 0; r < 3; r++) {
+        grad[3 * i + r] += J[r + 0] * Sj[0] + J[r + 3] * Sj[1] + J[r + 6] * Sj[2];
+    }
+    for (int r = 0; r < 3; r++) {
+        grad[3 * j + r] += J[0 + 3 * r] * Si[0] + J[1 + 3 * r] * Si[1] + J[2 + 3 * r] * Si[2];
+    }
+    if (dipole_mode && pc->biquad_kind != 0) {
+        double Qi[5], Qj[5], dQi[5][3], dQj[5][3];
+        quadrupole(Si, Qi);
+        quadrupole(Sj, Qj);
+        grad_quadrupole(Si, dQi);
+        grad_quadrupole(Sj, dQj);
+        double vi[5], vj[5];
+        if (pc->biquad_kind == 1) {
+            double Jb = pc->biquad[0];
+            for (int q = 0; q < 5; q++) { vi[q] = Jb * (Qj[q] * METRIC[q]); vj[q] = Jb * (Qi[q] * METRIC[q]); }
+        } else {
+            const double* B = pc->biquad;
+            for (int q = 0; q < 5; q++) {
+                double acc_i = 0, acc_j = 0;
+                for (int p = 0; p < 5; p++) {
+                    acc_i += B[q + 5 * p] * Qj[p];   /* (J Qj)_q */
+                    acc_j += Qi[p] * B[p + 5 * q];   /* (Qi' J)_q */
+                }
+                vi[q] = acc_i; vj[q] = acc_j;
+            }
+        }
+        for (int r = 0; r < 3; r++) {
+            double ai = 0, aj = 0;
+            for (int q = 0; q < 5; q++) { ai += vi[q] * dQi[q][r]; aj += vj[q] * dQj[q][r]; }
+            grad[3 * i + r] += ai;
+            grad[3 * j + r] += aj;
+        }
+    }
+}
+
 void or_grad_dipoles(const or_sys* s, const double* S, double* grad) {
     int64_t ns = or_nsites(s);
     int L1 = s->L[0], L2 = s->L[1], L3 = s->L[2];
@@ -275,9 +335,29 @@ void or_grad_dipoles(const or_sys* s, const double* S, double* grad) {
         }
     }
     int dipole_mode = (s->mode != SGB_MODE_SUN);
+    if (s->site_bonds || s->onsite_site) {
+        /* inhomogeneous: per site, its onsite term then its own non-culled couplings
+         * (Interactions.jl:535-540 with sites = (site,)) */
+        if (dipole_mode)
+            for (int64_t i = 0; i < ns; i++) {
+                const double* c = onsite_at(s, i);
+                if (!c) continue;
+                double g3[3];
+                or_classical_anisotropy(c, S + 3 * i, g3);
+                grad[3 * i] += g3[0]; grad[3 * i + 1] += g3[1]; grad[3 * i + 2] += g3[2];
+            }
+        if (s->site_bonds) {
+            for (int64_t e = 0; e < s->nsite_bonds; e++) {
+                int64_t i, j;
+                site_bond_ends(s, &s->site_bonds[e], &i, &j);
+                pair_grad_dipoles(&s->site_bonds[e].bond, i, j, S, grad, dipole_mode);
+            }
+            return;
+        }
+    }
     for (int a = 0; a < s->na; a++) {
         /* onsite (dipole modes only), Interactions.jl:546-552 */
-        if (dipole_mode && s->onsite) {
+        if (dipole_mode && s->onsite && !s->onsite_site) {
             for (int c3 = 0; c3 < L3; c3++)
                 for (int c2 = 0; c2 < L2; c2++)
                     for (int c1 = 0; c1 < L1; c1++) {
@@ -291,49 +371,13 @@ void or_grad_dipoles(const or_sys* s, const double* S, double* grad) {
         for (int b = 0; b < s->nbonds; b++) {
             const sgb_bond* pc = &s->bonds[b];
             if (pc->i != a) continue;
-            const double* J = pc->bilin;
             for (int c3 = 0; c3 < L3; c3++)
                 for (int c2 = 0; c2 < L2; c2++)
                     for (int c1 = 0; c1 < L1; c1++) {
                         int64_t i = site_index(s, c1, c2, c3, a);
                         int64_t j = site_index(s, wrap(c1 + pc->n[0], L1), wrap(c2 + pc->n[1], L2),
                                                wrap(c3 + pc->n[2], L3), pc->j);
-                        const double* Si = S + 3 * i;
-                        const double* Sj = S + 3 * j;
-                        for (int r = 0; r < 3; r++) {
-                            grad[3 * i + r] += J[r + 0] * Sj[0] + J[r + 3] * Sj[1] + J[r + 6] * Sj[2];
-                        }
-                        for (int r = 0; r < 3; r++) {
-                            grad[3 * j + r] += J[0 + 3 * r] * Si[0] + J[1 + 3 * r] * Si[1] + J[2 + 3 * r] * Si[2];
-                        }
-                        if (dipole_mode && pc->biquad_kind != 0) {
-                            double Qi[5], Qj[5], dQi[5][3], dQj[5][3];
-                            quadrupole(Si, Qi);
-                            quadrupole(Sj, Qj);
-                            grad_quadrupole(Si, dQi);
-                            grad_quadrupole(Sj, dQj);
-                            double vi[5], vj[5];
-                            if (pc->biquad_kind == 1) {
-                                double Jb = pc->biquad[0];
-                                for (int q = 0; q < 5; q++) { vi[q] = Jb * (Qj[q] * METRIC[q]); vj[q] = Jb * (Qi[q] * METRIC[q]); }
-                            } else {
-                                const double* B = pc->biquad;
-                                for (int q = 0; q < 5; q++) {
-                                    double acc_i = 0, acc_j = 0;
-                                    for (int p = 0; p < 5; p++) {
-                                        acc_i += B[q + 5 * p] * Qj[p];   /* (J Qj)_q */
-                                        acc_j += Qi[p] * B[p + 5 * q];   /* (Qi' J)_q */
-                                    }
-                                    vi[q] = acc_i; vj[q] = acc_j;
-                                }
-                            }
-                            for (int r = 0; r < 3; r++) {
-                                double ai = 0, aj = 0;
-                                for (int q = 0; q < 5; q++) { ai += vi[q] * dQi[q][r]; aj += vj[q] * dQj[q][r]; }
-                                grad[3 * i + r] += ai;
-                                grad[3 * j + r] += aj;
-                            }
-                        }
+                        pair_grad_dipoles(pc, i, j, S, grad, dipole_mode);
                     }
         }
     }
@@ -367,6 +411,32 @@ static void mul_quadrupole_matrices(const or_ops* ops, const double* dEdQ, const
 }
 
 /* ---- Interactions.jl:596-669 set_energy_grad_coherents! ----------------------------- */
+/* Biquadratic coupling pc between sites i and j in SU(N) mode (Interactions.jl:643-658). */
+static void pair_grad_coherents(const or_ops* ops, const sgb_bond* pc, int64_t i, int64_t j, const double* Z, double* HZ) {
+    const int N = ops->N;
+    cplx zi[8], zj[8], oi[8], oj[8];
+    for (int k = 0; k < N; k++) { zi[k] = zget(Z, i, N, k); zj[k] = zget(Z, j, N, k); }
+    double Qi[5], Qj[5], dQi[5], dQj[5];
+    expected_quadrupole(ops, zi, Qi);
+    expected_quadrupole(ops, zj, Qj);
+    if (pc->biquad_kind == 1) {
+        for (int q = 0; q < 5; q++) { dQi[q] = pc->biquad[0] * (METRIC[q] * Qj[q]); dQj[q] = pc->biquad[0] * (METRIC[q] * Qi[q]); }
+    } else {
+        const double* B = pc->biquad;
+        for (int q = 0; q < 5; q++) {
+            double ai = 0, aj = 0;
+            for (int p = 0; p < 5; p++) { ai += B[q + 5 * p] * Qj[p]; aj += B[p + 5 * q] * Qi[p]; }
+            dQi[q] = ai; dQj[q] = aj;
+        }
+    }
+    mul_quadrupole_matrices(ops, dQi, zi, oi);
+    mul_quadrupole_matrices(ops, dQj, zj, oj);
+    for (int k = 0; k < N; k++) {
+        zset(HZ, i, N, k, zget(HZ, i, N, k) + oi[k]);
+        zset(HZ, j, N, k, zget(HZ, j, N, k) + oj[k]);
+    }
+}
+
 void or_grad_coherents(const or_sys* s, const double* Z, double* HZ) {
     int N = s->N;
     int64_t ns = or_nsites(s);
@@ -378,55 +448,92 @@ void or_grad_coherents(const or_sys* s, const double* Z, double* HZ) {
     for (int64_t i = 0; i < ns; i++) or_expected_spin(N, Z + 2 * N * i, dip + 3 * i);
     or_grad_dipoles(s, dip, dEdS); /* SU(N) mode: Zeeman + bilinear only */
     memset(HZ, 0, sizeof(double) * 2 * N * ns);
-    for (int a = 0; a < s->na; a++) {
-        const double* lam = s->onsite ? s->onsite + 2 * N * N * a : NULL;
-        for (int c3 = 0; c3 < L3; c3++)
-            for (int c2 = 0; c2 < L2; c2++)
-                for (int c1 = 0; c1 < L1; c1++) {
-                    int64_t i = site_index(s, c1, c2, c3, a);
-                    cplx z[8], out[8];
-                    for (int k = 0; k < N; k++) z[k] = zget(Z, i, N, k);
-                    mul_spin_matrices(&ops, lam, dEdS + 3 * i, z, out);
-                    for (int k = 0; k < N; k++) zset(HZ, i, N, k, zget(HZ, i, N, k) + out[k]);
-                }
-        for (int b = 0; b < s->nbonds; b++) {
-            const sgb_bond* pc = &s->bonds[b];
-            if (pc->i != a || pc->biquad_kind == 0) continue;
-            for (int c3 = 0; c3 < L3; c3++)
-                for (int c2 = 0; c2 < L2; c2++)
-                    for (int c1 = 0; c1 < L1; c1++) {
-                        int64_t i = site_index(s, c1, c2, c3, a);
-                        int64_t j = site_index(s, wrap(c1 + pc->n[0], L1), wrap(c2 + pc->n[1], L2),
-                                               wrap(c3 + pc->n[2], L3), pc->j);
-                        cplx zi[8], zj[8], oi[8], oj[8];
-                        for (int k = 0; k < N; k++) { zi[k] = zget(Z, i, N, k); zj[k] = zget(Z, j, N, k); }
-                        double Qi[5], Qj[5], dQi[5], dQj[5];
-                        expected_quadrupole(&ops, zi, Qi);
-                        expected_quadrupole(&ops, zj, Qj);
-                        if (pc->biquad_kind == 1) {
-                            for (int q = 0; q < 5; q++) { dQi[q] = pc->biquad[0] * (METRIC[q] * Qj[q]); dQj[q] = pc->biquad[0] * (METRIC[q] * Qi[q]); }
-                        } else {
-                            const double* B = pc->biquad;
-                            for (int q = 0; q < 5; q++) {
-                                double ai = 0, aj = 0;
-                                for (int p = 0; p < 5; p++) { ai += B[q + 5 * p] * Qj[p]; aj += B[p + 5 * q] * Qi[p]; }
-                                dQi[q] = ai; dQj[q] = aj;
-                            }
-                        }
-                        mul_quadrupole_matrices(&ops, dQi, zi, oi);
-                        mul_quadrupole_matrices(&ops, dQj, zj, oj);
-                        for (int k = 0; k < N; k++) {
-                            zset(HZ, i, N, k, zget(HZ, i, N, k) + oi[k]);
-                            zset(HZ, j, N, k, zget(HZ, j, N, k) + oj[k]);
-                        }
-                    }
+    /* (Λ + dE/dS·S) Z per site (Interactions.jl:605-630) */
+    for (int64_t i = 0; i < ns; i++) {
+        cplx z[8], out[8];
+        for (int k = 0; k < N; k++) z[k] = zget(Z, i, N, k);
+        mul_spin_matrices(&ops, onsite_at(s, i), dEdS + 3 * i, z, out);
+        for (int k = 0; k < N; k++) zset(HZ, i, N, k, zget(HZ, i, N, k) + out[k]);
+    }
+    if (s->site_bonds) {
+        for (int64_t e = 0; e < s->nsite_bonds; e++) {
+            const sgb_bond* pc = &s->site_bonds[e].bond;
+            if (pc->biquad_kind == 0) continue;
+            int64_t i, j;
+            site_bond_ends(s, &s->site_bonds[e], &i, &j);
+            pair_grad_coherents(&ops, pc, i, j, Z, HZ);
         }
+    } else {
+        for (int a = 0; a < s->na; a++)
+            for (int b = 0; b < s->nbonds; b++) {
+                const sgb_bond* pc = &s->bonds[b];
+                if (pc->i != a || pc->biquad_kind == 0) continue;
+                for (int c3 = 0; c3 < L3; c3++)
+                    for (int c2 = 0; c2 < L2; c2++)
+                        for (int c1 = 0; c1 < L1; c1++) {
+                            int64_t i = site_index(s, c1, c2, c3, a);
+                            int64_t j = site_index(s, wrap(c1 + pc->n[0], L1), wrap(c2 + pc->n[1], L2),
+                                                   wrap(c3 + pc->n[2], L3), pc->j);
+                            pair_grad_coherents(&ops, pc, i, j, Z, HZ);
+                        }
+            }
     }
     free(dip);
     free(dEdS);
 }
 
 /* ---- Interactions.jl:401-508 energy ------------------------------------------------- */
+/* Energy of one non-culled coupling between sites i and j (Interactions.jl:466-505). */
+static double pair_energy(const or_sys* s, const or_ops* ops, const sgb_bond* pc, int64_t i, int64_t j, const double* S,
+                          const double* Z, int sun) {
+    const int N = s->N;
+    const double* J = pc->bilin;
+    const double* Si = S + 3 * i;
+    const double* Sj = S + 3 * j;
+    double Ea = 0;
+    if (sun) Ea += pc->scalar * s->kappa[i] * s->kappa[j];
+    else Ea += pc->scalar;
+    double JS[3];
+    for (int r = 0; r < 3; r++) JS[r] = J[r] * Sj[0] + J[r + 3] * Sj[1] + J[r + 6] * Sj[2];
+    Ea += Si[0] * JS[0] + Si[1] * JS[1] + Si[2] * JS[2];
+    if (pc->biquad_kind != 0) {
+        double Qi[5], Qj[5];
+        if (!sun) { quadrupole(Si, Qi); quadrupole(Sj, Qj); }
+        else {
+            cplx zi[8], zj[8];
+            for (int k = 0; k < N; k++) { zi[k] = zget(Z, i, N, k); zj[k] = zget(Z, j, N, k); }
+            expected_quadrupole(ops, zi, Qi);
+            expected_quadrupole(ops, zj, Qj);
+        }
+        if (pc->biquad_kind == 1) {
+            double acc = 0;
+            for (int q = 0; q < 5; q++) acc += Qi[q] * (METRIC[q] * Qj[q]);
+            Ea += pc->biquad[0] * acc;
+        } else {
+            double acc = 0;
+            for (int q = 0; q < 5; q++)
+                for (int p = 0; p < 5; p++) acc += Qi[q] * pc->biquad[q + 5 * p] * Qj[p];
+            Ea += acc;
+        }
+    }
+    return Ea;
+}
+
+/* Onsite energy of site i (Interactions.jl:449-462). */
+static double onsite_energy(const or_sys* s, int64_t i, const double* S, const double* Z, int sun) {
+    const double* c = onsite_at(s, i);
+    if (!c) return 0;
+    if (!sun) {
+        double g3[3];
+        return or_classical_anisotropy(c, S + 3 * i, g3);
+    }
+    const int N = s->N;
+    cplx acc = 0;
+    for (int cc = 0; cc < N; cc++)
+        for (int r = 0; r < N; r++) acc += conj(zget(Z, i, N, r)) * (c[2 * (r + N * cc)] + I * c[2 * (r + N * cc) + 1]) * zget(Z, i, N, cc);
+    return creal(acc);
+}
+
 double or_energy(const or_sys* s, const double* S, const double* Z) {
     int64_t ns = or_nsites(s);
     int L1 = s->L[0], L2 = s->L[1], L3 = s->L[2];
@@ -445,60 +552,31 @@ double or_energy(const or_sys* s, const double* S, const double* Z) {
             E += B[0] * gS[0] + B[1] * gS[1] + B[2] * gS[2];
         }
     }
+    if (s->site_bonds) {
+        /* inhomogeneous: per site, Interactions.jl:433-440 */
+        for (int64_t i = 0; i < ns; i++) E += onsite_energy(s, i, S, Z, sun);
+        for (int64_t e = 0; e < s->nsite_bonds; e++) {
+            int64_t i, j;
+            site_bond_ends(s, &s->site_bonds[e], &i, &j);
+            E += pair_energy(s, &ops, &s->site_bonds[e].bond, i, j, S, Z, sun);
+        }
+        return E;
+    }
     for (int a = 0; a < s->na; a++) {
         double Ea = 0.0;
         for (int c3 = 0; c3 < L3; c3++)
             for (int c2 = 0; c2 < L2; c2++)
-                for (int c1 = 0; c1 < L1; c1++) {
-                    int64_t i = site_index(s, c1, c2, c3, a);
-                    if (!sun) {
-                        if (s->onsite) { double g3[3]; Ea += or_classical_anisotropy(s->onsite + 28 * a, S + 3 * i, g3); }
-                    } else if (s->onsite) {
-                        const double* lam = s->onsite + 2 * N * N * a;
-                        cplx acc = 0;
-                        for (int c = 0; c < N; c++)
-                            for (int r = 0; r < N; r++)
-                                acc += conj(zget(Z, i, N, r)) * (lam[2 * (r + N * c)] + I * lam[2 * (r + N * c) + 1]) * zget(Z, i, N, c);
-                        Ea += creal(acc);
-                    }
-                }
+                for (int c1 = 0; c1 < L1; c1++) Ea += onsite_energy(s, site_index(s, c1, c2, c3, a), S, Z, sun);
         for (int b = 0; b < s->nbonds; b++) {
             const sgb_bond* pc = &s->bonds[b];
             if (pc->i != a) continue;
-            const double* J = pc->bilin;
             for (int c3 = 0; c3 < L3; c3++)
                 for (int c2 = 0; c2 < L2; c2++)
                     for (int c1 = 0; c1 < L1; c1++) {
                         int64_t i = site_index(s, c1, c2, c3, a);
                         int64_t j = site_index(s, wrap(c1 + pc->n[0], L1), wrap(c2 + pc->n[1], L2),
                                                wrap(c3 + pc->n[2], L3), pc->j);
-                        const double* Si = S + 3 * i;
-                        const double* Sj = S + 3 * j;
-                        if (sun) Ea += pc->scalar * s->kappa[i] * s->kappa[j];
-                        else Ea += pc->scalar;
-                        double JS[3];
-                        for (int r = 0; r < 3; r++) JS[r] = J[r] * Sj[0] + J[r + 3] * Sj[1] + J[r + 6] * Sj[2];
-                        Ea += Si[0] * JS[0] + Si[1] * JS[1] + Si[2] * JS[2];
-                        if (pc->biquad_kind != 0) {
-                            double Qi[5], Qj[5];
-                            if (!sun) { quadrupole(Si, Qi); quadrupole(Sj, Qj); }
-                            else {
-                                cplx zi[8], zj[8];
-                                for (int k = 0; k < N; k++) { zi[k] = zget(Z, i, N, k); zj[k] = zget(Z, j, N, k); }
-                                expected_quadrupole(&ops, zi, Qi);
-                                expected_quadrupole(&ops, zj, Qj);
-                            }
-                            if (pc->biquad_kind == 1) {
-                                double acc = 0;
-                                for (int q = 0; q < 5; q++) acc += Qi[q] * (METRIC[q] * Qj[q]);
-                                Ea += pc->biquad[0] * acc;
-                            } else {
-                                double acc = 0;
-                                for (int q = 0; q < 5; q++)
-                                    for (int p = 0; p < 5; p++) acc += Qi[q] * pc->biquad[q + 5 * p] * Qj[p];
-                                Ea += acc;
-                            }
-                        }
+                        Ea += pair_energy(s, &ops, pc, i, j, S, Z, sun);
                     }
         }
         E += Ea;
@@ -533,14 +611,36 @@ double or_local_energy_change(const or_sys* s, const double* S, int64_t site, co
         const double* B = s->field + 3 * site;
         for (int r = 0; r < 3; r++) dE += B[r] * (g[r] * dS[0] + g[r + 3] * dS[1] + g[r + 6] * dS[2]);
     }
-    if (s->onsite) {
+    const double* c28 = onsite_at(s, site);
+    if (c28) {
         double g3[3];
-        dE += or_classical_anisotropy(s->onsite + 28 * a, Snew, g3) - or_classical_anisotropy(s->onsite + 28 * a, S0, g3);
+        dE += or_classical_anisotropy(c28, Snew, g3) - or_classical_anisotropy(c28, S0, g3);
     }
     double Qn[5], Qo[5], dQ[5];
     quadrupole(Snew, Qn);
     quadrupole(S0, Qo);
     for (int q = 0; q < 5; q++) dQ[q] = Qn[q] - Qo[q];
+    if (s->site_bonds) {
+        /* inhomogeneous: the site's own list holds its non-culled couplings and the
+         * reversed copies of its neighbours' (Interactions.jl:344-372) */
+        for (int64_t e = 0; e < s->nsite_bonds; e++) {
+            const sgb_bond* pc = &s->site_bonds[e].bond;
+            const double* J = pc->bilin;
+            int64_t i, j;
+            site_bond_ends(s, &s->site_bonds[e], &i, &j);
+            if (i == site && j == site) return NAN;
+            if (i == site) {
+                const double* Sj = S + 3 * j;
+                for (int r = 0; r < 3; r++) dE += dS[r] * (J[r] * Sj[0] + J[r + 3] * Sj[1] + J[r + 6] * Sj[2]);
+                if (pc->biquad_kind != 0) { double Qj[5]; quadrupole(Sj, Qj); dE += biquad_pair(pc, dQ, Qj); }
+            } else if (j == site) {
+                const double* Sk = S + 3 * i;
+                for (int r = 0; r < 3; r++) dE += Sk[r] * (J[r] * dS[0] + J[r + 3] * dS[1] + J[r + 6] * dS[2]);
+                if (pc->biquad_kind != 0) { double Qk[5]; quadrupole(Sk, Qk); dE += biquad_pair(pc, Qk, dQ); }
+            }
+        }
+        return dE;
+    }
     for (int b = 0; b < s->nbonds; b++) {
         const sgb_bond* pc = &s->bonds[b];
         const double* J = pc->bilin;
@@ -594,7 +694,31 @@ double or_local_energy_change_sun(const or_sys* s, const double* S, const double
         const double* B = s->field + 3 * site;
         for (int r = 0; r < 3; r++) dE += B[r] * (g[r] * dS[0] + g[r + 3] * dS[1] + g[r + 6] * dS[2]);
     }
-    if (s->onsite) dE += onsite_e(N, s->onsite + 2 * N * N * a, zn) - onsite_e(N, s->onsite + 2 * N * N * a, z0);
+    const double* lam = onsite_at(s, site);
+    if (lam) dE += onsite_e(N, lam, zn) - onsite_e(N, lam, z0);
+    if (s->site_bonds) {
+        for (int64_t e = 0; e < s->nsite_bonds; e++) {
+            const sgb_bond* pc = &s->site_bonds[e].bond;
+            const double* J = pc->bilin;
+            int64_t i, j;
+            site_bond_ends(s, &s->site_bonds[e], &i, &j);
+            if (i == site && j == site) return NAN;
+            if (i != site && j != site) continue;
+            const int end = i == site ? 0 : 1;
+            const int64_t o = end == 0 ? j : i;
+            const double* So = S + 3 * o;
+            if (end == 0) for (int r = 0; r < 3; r++) dE += dS[r] * (J[r] * So[0] + J[r + 3] * So[1] + J[r + 6] * So[2]);
+            else for (int r = 0; r < 3; r++) dE += So[r] * (J[r] * dS[0] + J[r + 3] * dS[1] + J[r + 6] * dS[2]);
+            if (pc->biquad_kind != 0) {
+                cplx zo[8];
+                double Qo[5];
+                for (int k = 0; k < N; k++) zo[k] = zget(Z, o, N, k);
+                expected_quadrupole(&ops, zo, Qo);
+                dE += end == 0 ? biquad_pair(pc, dQ, Qo) : biquad_pair(pc, Qo, dQ);
+            }
+        }
+        return dE;
+    }
     for (int b = 0; b < s->nbonds; b++) {
         const sgb_bond* pc = &s->bonds[b];
         const double* J = pc->bilin;

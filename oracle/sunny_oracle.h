@@ -31,6 +31,12 @@ typedef struct {
     const double* onsite;  /* dipole: [na][28]; SU(N): [na][N*N][2] col-major */
     const sgb_bond* bonds; /* non-culled bonds  */
     int nbonds;
+    /* Inhomogeneous systems (to_inhomogeneous, Interactions.jl:81-100), else NULL:
+     * onsite couplings per site ([ns][28] or [ns][N*N][2]) and every site's non-culled
+     * pair couplings, in the reference's site order (they replace `bonds`). */
+    const double* onsite_site;
+    const sgb_site_bond* site_bonds;
+    int64_t nsite_bonds;
 } or_sys;
 
 int64_t or_nsites(const or_sys* s);

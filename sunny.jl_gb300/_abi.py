@@ -38,6 +38,10 @@ class BondC(C.Structure):
                 ("bilin", C.c_double * 9), ("biquad_kind", C.c_int32), ("biquad", C.c_double * 25)]
 
 
+class SiteBondC(C.Structure):
+    _fields_ = [("cell", C.c_int32 * 3), ("pad", C.c_int32), ("bond", BondC)]
+
+
 class Proposal(C.Structure):
     _fields_ = [("n", C.c_int32), ("kind", C.c_int32 * 4), ("weight", C.c_double * 4), ("magnitude", C.c_double * 4)]
 
@@ -67,6 +71,8 @@ SIGNATURES = {
     "sgb_set_sites": (C.c_int, [_P, _D, _D, _D]),
     "sgb_set_onsite": (C.c_int, [_P, _I32, _D]),
     "sgb_set_bonds": (C.c_int, [_P, C.POINTER(BondC), _I32]),
+    "sgb_set_bonds_at": (C.c_int, [_P, C.POINTER(SiteBondC), _I64]),
+    "sgb_set_onsite_at": (C.c_int, [_P, _D]),
     "sgb_set_state": (C.c_int, [_P, _D, _D]),
     "sgb_get_state": (C.c_int, [_P, _D, _D]),
     "sgb_set_midpoint_predictor": (C.c_int, [_P, _I32]),
@@ -88,6 +94,7 @@ SIGNATURES = {
     "sgb_corr_data": (C.c_int, [_P, _D, _D, C.POINTER(_I64)]),
     "sgb_corr_intensities": (C.c_int, [_P, _I32, C.POINTER(_I32), _D, _D, _I32, C.POINTER(_I32), _I32, _D]),
     "sgb_corr_merge": (C.c_int, [_P, _P]),
+    "sgb_corr_compare": (C.c_int, [_P, _P, _D]),
     "sgb_corr_profile": (C.c_int, [_P, _I32]),
     "sgb_corr_phase_times": (C.c_int, [_P, _D, C.POINTER(_I64), C.POINTER(_I64)]),
     "sgb_batch_create": (C.c_int, [C.POINTER(Desc), _I32, C.POINTER(_I32), C.POINTER(_P)]),
@@ -122,6 +129,9 @@ SIGNATURES = {
     "sgb_kernel_launches": (_I64, [_P]),
     "sgb_batch_kernel_launches": (_I64, [_P]),
     "sgb_flush_l2": (C.c_int, [_P]),
+    "sgb_set_wait_limit": (C.c_int, [_P, C.c_double]),
+    "sgb_batch_set_wait_limit": (C.c_int, [_P, C.c_double]),
+    "sgb_wait_probe": (C.c_int, [_P]),
     "sgb_version": (C.c_char_p, []),
 }
 

@@ -326,6 +326,7 @@ int sgb_adjoint_create(sgb_system* s, const sgb_corr_desc* d, int32_t nparams, c
     *out = nullptr;
     if (s->sun || s->fp32) return afail(nullptr, SGB_ERR_ARG, "the adjoint supports FP64 dipole-mode systems");
     if (s->ewald_on) return afail(nullptr, SGB_ERR_ARG, "the adjoint does not support dipole-dipole interactions");
+    if (s->inh_bonds || s->inh_onsite) return afail(nullptr, SGB_ERR_ARG, "the adjoint supports homogeneous systems only");
     if (d->damping != 0.0) return afail(nullptr, SGB_ERR_ARG, "the adjoint differentiates the undamped midpoint method (damping = 0)");
     if (d->n_all_omega < 2) return afail(nullptr, SGB_ERR_ARG, "the adjoint needs a dynamical S(q,ω) (n_all_omega > 1)");
     int rc = sgb_int_ensure_tables(s);

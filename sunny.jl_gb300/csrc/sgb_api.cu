@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <map>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -83,6 +84,9 @@ int ensure_dbuf(sgb_system* s, size_t n) {
 }
 
 template <class R>
+int build_inh_tables(sgb_system* s, Model<R>& M);
+
+template <class R>
 int build_tables(sgb_system* s, Model<R>& M) {
     std::vector<unsigned char> buf;
     bool any_bq = false;
@@ -129,6 +133,153 @@ int build_tables(sgb_system* s, Model<R>& M) {
     M.kappa = reinterpret_cast<const R*>(s->kappa);
     M.h = s->has_field ? reinterpret_cast<const R*>(s->h) : nullptr;
     M.tables = reinterpret_cast<const unsigned char*>(s->tables);
+    return build_inh_tables<R>(s, M);
+}
+
+// Per-site coupling rows of an inhomogeneous system (to_inhomogeneous,
+// Interactions.jl:81-100): each non-culled coupling of a site's list becomes the forward
+// row at that site and the reversed row (J^T, transposed biquadratic matrix, fwd = 0) at
+// bonded_site (System.jl:204-212), as set_pair_coupling_at_aux! stores both
+// (PairExchange.jl:447-468). Equal rows are stored once.
+template <class R>
+int build_inh_tables(sgb_system* s, Model<R>& M) {
+    M.ioff = nullptr; M.ient = nullptr; M.ctab = nullptr; M.cbq = nullptr;
+    M.oidx = nullptr; M.otab = nullptr; M.okmax = nullptr;
+    dfree(s->inh_dev);
+    s->inh_off_h.clear();
+    s->inh_nbr_h.clear();
+    if (!s->inh_bonds && !s->inh_onsite) return SGB_OK;
+    const int ns = s->ns;
+    const int L1 = s->d.dims[0], L2 = s->d.dims[1], L3 = s->d.dims[2];
+    std::vector<int> off(ns + 1, 0);
+    std::vector<int2> ent;
+    std::vector<DBond<R>> rows;
+    std::vector<R> bqrows;
+    bool any_bq = false, general = false;
+    if (s->inh_bonds) {
+        std::map<std::string, int> row_of;
+        auto row = [&](const sgb_bond& b, bool fwd) {
+            DBond<R> e{};
+            bool iso = b.bilin[0] == b.bilin[4] && b.bilin[0] == b.bilin[8];
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) {
+                    const double v = fwd ? b.bilin[r + 3 * c] : b.bilin[c + 3 * r];
+                    e.J[r + 3 * c] = (R)v;
+                    if (r != c && v != 0.0) iso = false;
+                }
+            e.jkind = iso ? 0 : 1;
+            e.scalar = (R)b.scalar;
+            e.bqkind = b.biquad_kind;
+            std::vector<R> m;
+            if (b.biquad_kind == 1) {
+                e.bq = (R)b.biquad[0];
+                if (b.biquad[0] == 0.0) e.bqkind = 0;
+            } else if (b.biquad_kind == 2) {
+                for (int c = 0; c < 5; c++)
+                    for (int r = 0; r < 5; r++) m.push_back((R)(fwd ? b.biquad[r + 5 * c] : b.biquad[c + 5 * r]));
+            }
+            e.fwd = fwd ? 1 : 0;
+            std::string key(reinterpret_cast<const char*>(&e), sizeof(e));
+            key.append(reinterpret_cast<const char*>(m.data()), m.size() * sizeof(R));
+            auto it = row_of.find(key);
+            if (it != row_of.end()) return it->second;
+            if (e.bqkind == 2) {
+                e.bqidx = (int)(bqrows.size() / 25);
+                bqrows.insert(bqrows.end(), m.begin(), m.end());
+            }
+            any_bq |= e.bqkind != 0;
+            general |= e.jkind != 0 || e.bqkind != 0;
+            const int k = (int)rows.size();
+            rows.push_back(e);
+            row_of.emplace(std::move(key), k);
+            return k;
+        };
+        struct Dir { int from, to, row; };
+        std::vector<Dir> dirs;
+        dirs.reserve(2 * s->site_bonds_h.size());
+        for (const sgb_site_bond& sb : s->site_bonds_h) {
+            const sgb_bond& b = sb.bond;
+            const int i = sb.cell[0] + L1 * (sb.cell[1] + L2 * (sb.cell[2] + L3 * b.i));
+            const int j = sgbhost::imod(sb.cell[0] + b.n[0], L1) +
+                          L1 * (sgbhost::imod(sb.cell[1] + b.n[1], L2) + L2 * (sgbhost::imod(sb.cell[2] + b.n[2], L3) + L3 * b.j));
+            dirs.push_back({i, j, row(b, true)});
+            dirs.push_back({j, i, row(b, false)});
+        }
+        for (const Dir& d : dirs) off[d.from + 1]++;
+        for (int i = 0; i < ns; i++) off[i + 1] += off[i];
+        ent.resize(dirs.size());
+        std::vector<int> fill(off.begin(), off.end() - 1);
+        for (const Dir& d : dirs) ent[fill[d.from]++] = make_int2(d.to, d.row);
+        s->inh_off_h = off;
+        s->inh_nbr_h.resize(ent.size());
+        for (size_t k = 0; k < ent.size(); k++) s->inh_nbr_h[k] = ent[k].x;
+    }
+    std::vector<int> oidx, okmax;
+    std::vector<R> otab;
+    if (s->inh_onsite) {
+        const int per = s->sun ? 2 * s->N * s->N : 28;
+        std::map<std::vector<double>, int> row_of;
+        oidx.resize(ns);
+        for (int i = 0; i < ns; i++) {
+            std::vector<double> c(s->onsite_site_h.begin() + (size_t)per * i, s->onsite_site_h.begin() + (size_t)per * (i + 1));
+            int km = 0;
+            if (!s->sun) {
+                // StevensExpansion drops k-blocks of norm < 1e-12 (Types.jl:12-16)
+                const int start[4] = {0, 1, 6, 15}, len[4] = {1, 5, 9, 13};
+                for (int g = 0; g < 4; g++) {
+                    double nrm = 0;
+                    for (int q = 0; q < len[g]; q++) nrm += c[start[g] + q] * c[start[g] + q];
+                    const bool zero = std::sqrt(nrm) < 1e-12;
+                    if (zero) for (int q = 0; q < len[g]; q++) c[start[g] + q] = 0;
+                    if (!zero && g > 0) km = 2 * g;
+                }
+            }
+            auto it = row_of.find(c);
+            if (it == row_of.end()) {
+                const int k = (int)okmax.size();
+                for (double v : c) otab.push_back((R)v);
+                okmax.push_back(km);
+                it = row_of.emplace(c, k).first;
+            }
+            oidx[i] = it->second;
+        }
+    }
+    // one device allocation, 16-byte aligned parts
+    size_t o_off = 0, o_ent, o_ctab, o_cbq, o_oidx, o_otab, o_okmax, total;
+    o_ent = sgbhost::align16(o_off + sizeof(int) * (s->inh_bonds ? ns + 1 : 0));
+    o_ctab = sgbhost::align16(o_ent + sizeof(int2) * ent.size());
+    o_cbq = sgbhost::align16(o_ctab + sizeof(DBond<R>) * rows.size());
+    o_oidx = sgbhost::align16(o_cbq + sizeof(R) * bqrows.size());
+    o_otab = sgbhost::align16(o_oidx + sizeof(int) * oidx.size());
+    o_okmax = sgbhost::align16(o_otab + sizeof(R) * otab.size());
+    total = sgbhost::align16(o_okmax + sizeof(int) * okmax.size());
+    std::vector<unsigned char> buf(total, 0);
+    auto put = [&](size_t at, const void* src, size_t bytes) { if (bytes) std::memcpy(buf.data() + at, src, bytes); };
+    if (s->inh_bonds) put(o_off, off.data(), sizeof(int) * (ns + 1));
+    put(o_ent, ent.data(), sizeof(int2) * ent.size());
+    put(o_ctab, rows.data(), sizeof(DBond<R>) * rows.size());
+    put(o_cbq, bqrows.data(), sizeof(R) * bqrows.size());
+    put(o_oidx, oidx.data(), sizeof(int) * oidx.size());
+    put(o_otab, otab.data(), sizeof(R) * otab.size());
+    put(o_okmax, okmax.data(), sizeof(int) * okmax.size());
+    int rc = dmalloc(s, &s->inh_dev, total);
+    if (rc) return rc;
+    CK(cudaMemcpy(s->inh_dev, buf.data(), total, cudaMemcpyHostToDevice));
+    unsigned char* d = reinterpret_cast<unsigned char*>(s->inh_dev);
+    if (s->inh_bonds) {
+        M.ioff = reinterpret_cast<const int*>(d + o_off);
+        M.ient = reinterpret_cast<const int2*>(d + o_ent);
+        M.ctab = reinterpret_cast<const DBond<R>*>(d + o_ctab);
+        M.cbq = reinterpret_cast<const R*>(d + o_cbq);
+        s->has_biquad = any_bq;
+        M.has_biquad = any_bq ? 1 : 0;
+        M.general = general ? 1 : 0;
+    }
+    if (s->inh_onsite) {
+        M.oidx = reinterpret_cast<const int*>(d + o_oidx);
+        M.otab = reinterpret_cast<const R*>(d + o_otab);
+        M.okmax = reinterpret_cast<const int*>(d + o_okmax);
+    }
     return SGB_OK;
 }
 
@@ -170,7 +321,7 @@ int plan_launch(sgb_system* s, LaunchInfo& li) {
 }
 
 int reset_ctrl(sgb_system* s) {
-    CK(cudaMemsetAsync(s->ctrl, 0, sizeof(Ctrl), s->stream));
+    CK(cudaMemsetAsync(s->ctrl, 0, sgb_ctrl_clear_bytes(), s->stream));
     return SGB_OK;
 }
 
@@ -206,6 +357,8 @@ size_t cluster_smem(sgb_system* s, int nsl) {
 
 template <class R>
 int cluster_size(sgb_system* s) {
+    // the cluster kernels read the per-sublattice tables only
+    if (s->inh_bonds || s->inh_onsite) return 0;
     int cs = 1;
     while (cs < SGB_CLUSTER_MAX && (long long)cs * SGB_CLUSTER_BLOCK < s->ns) cs *= 2;
     const int nsl = (s->ns + cs - 1) / cs;
@@ -538,11 +691,13 @@ int ensure_colors(sgb_system* s) {
     const int ns = s->ns, ncell = s->ncell;
     std::vector<int> col(ns, -1);
     int ncol = 0;
+    const bool inh = s->inh_bonds;
     for (int i = 0; i < ns; i++) {
         const int a = i / ncell;
         uint64_t used = 0;
-        for (int k = 0; k < s->boff_h[a + 1] - s->boff_h[a]; k++) {
-            const int j = s->nbr_h[(size_t)k * ns + i];
+        const int nk = inh ? s->inh_off_h[i + 1] - s->inh_off_h[i] : s->boff_h[a + 1] - s->boff_h[a];
+        for (int k = 0; k < nk; k++) {
+            const int j = inh ? s->inh_nbr_h[(size_t)s->inh_off_h[i] + k] : s->nbr_h[(size_t)k * ns + i];
             // local_energy_change (Interactions.jl:345)
             if (j == i) return fail(s, SGB_ERR_ARG, "Energy delta for self-interaction not supported");
             if (col[j] >= 0 && col[j] < 64) used |= 1ull << col[j];
@@ -712,6 +867,7 @@ void sgb_destroy(sgb_system* s) {
     p = s->dbuf; dfree(p);
     p = s->mc_perm; dfree(p);
     p = s->mc_part; dfree(p);
+    dfree(s->inh_dev);
     ewald_free(s);
     p = s->lr_grad; dfree(p);
     dfree(s->flush);
@@ -776,6 +932,7 @@ int sgb_set_onsite(sgb_system* s, int32_t atom, const double* coeffs) {
             }
         std::copy(coeffs, coeffs + 2 * N * N, s->onsite_h.begin() + (size_t)2 * N * N * atom);
     }
+    s->inh_onsite = false;
     s->tables_dirty = true;
     return SGB_OK;
 }
@@ -791,7 +948,53 @@ int sgb_set_bonds(sgb_system* s, const sgb_bond* bonds, int32_t nbonds) {
         if (b.biquad_kind < 0 || b.biquad_kind > 2) return fail(s, SGB_ERR_ARG, "biquad_kind must be 0, 1 or 2");
     }
     s->bonds_h.assign(bonds, bonds + nbonds);
+    s->inh_bonds = false;
+    s->site_bonds_h.clear();
     s->bonds_set = true;
+    s->tables_dirty = true;
+    return SGB_OK;
+}
+
+int sgb_set_bonds_at(sgb_system* s, const sgb_site_bond* bonds, int64_t nbonds) {
+    if (!s || (nbonds > 0 && !bonds) || nbonds < 0) return fail(s, SGB_ERR_ARG, "invalid bond list");
+    if (2 * nbonds > (int64_t)INT32_MAX) return fail(s, SGB_ERR_ARG, "too many couplings");
+    const int* L = s->d.dims;
+    for (int64_t k = 0; k < nbonds; k++) {
+        const sgb_bond& b = bonds[k].bond;
+        const int32_t* c = bonds[k].cell;
+        if (b.i < 0 || b.i >= s->d.natoms) return fail(s, SGB_ERR_ARG, "Atom index " + std::to_string(b.i + 1) + " is out of range.");
+        if (b.j < 0 || b.j >= s->d.natoms) return fail(s, SGB_ERR_ARG, "Atom index " + std::to_string(b.j + 1) + " is out of range.");
+        if (b.biquad_kind < 0 || b.biquad_kind > 2) return fail(s, SGB_ERR_ARG, "biquad_kind must be 0, 1 or 2");
+        for (int d = 0; d < 3; d++)
+            if (c[d] < 0 || c[d] >= L[d]) return fail(s, SGB_ERR_ARG, "cell index out of range");
+    }
+    s->site_bonds_h.assign(bonds, bonds + nbonds);
+    s->inh_bonds = true;
+    s->bonds_set = true;
+    s->tables_dirty = true;
+    return SGB_OK;
+}
+
+int sgb_set_onsite_at(sgb_system* s, const double* coeffs) {
+    if (!s || !coeffs) return fail(s, SGB_ERR_ARG, "null argument");
+    const int ns = s->ns;
+    if (s->sun) {
+        const int N = s->N;
+        for (int i = 0; i < ns; i++) {
+            const double* m = coeffs + (size_t)2 * N * N * i;
+            for (int r = 0; r < N; r++)
+                for (int c = 0; c < N; c++) {
+                    double ar = m[2 * (r + N * c)], ai = m[2 * (r + N * c) + 1];
+                    double br = m[2 * (c + N * r)], bi = m[2 * (c + N * r) + 1];
+                    if (std::fabs(ar - br) > 1e-10 * (1 + std::fabs(ar)) || std::fabs(ai + bi) > 1e-10 * (1 + std::fabs(ai)))
+                        return fail(s, SGB_ERR_ARG, "Operator is not Hermitian");
+                }
+        }
+        s->onsite_site_h.assign(coeffs, coeffs + (size_t)2 * N * N * ns);
+    } else {
+        s->onsite_site_h.assign(coeffs, coeffs + (size_t)28 * ns);
+    }
+    s->inh_onsite = true;
     s->tables_dirty = true;
     return SGB_OK;
 }
@@ -1375,6 +1578,28 @@ int sgb_event_elapsed(sgb_system* s, int32_t a, int32_t b, float* ms) {
     return SGB_OK;
 }
 
+int sgb_set_wait_limit(sgb_system* s, double seconds) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    if (!(seconds >= 0) || seconds > 3600) return fail(s, SGB_ERR_ARG, "wait limit must be in [0, 3600] s (0: the 4 s default)");
+    const unsigned long long ns = (unsigned long long)(seconds * 1e9);
+    CK(cudaMemcpyAsync(&s->ctrl->wait_ns, &ns, sizeof(ns), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return SGB_OK;
+}
+
+int sgb_wait_probe(sgb_system* s) {
+    if (!s) return fail(s, SGB_ERR_ARG, "null handle");
+    int rc = reset_ctrl(s);
+    if (rc) return rc;
+    if (util_launch_wait_probe(s->ctrl, 2, s->stream)) return cuda_fail(s, cudaGetLastError(), "wait probe launch");
+    s->launches++;
+    Ctrl c;
+    if ((rc = read_ctrl(s, &c))) return rc;
+    if (c.status == SGB_ERR_TIMEOUT) return fail(s, SGB_ERR_TIMEOUT, "a device-side barrier timed out");
+    if (c.status) return fail(s, c.status, "the wait probe ended with an unexpected status");
+    return fail(s, SGB_ERR_STATE, "the wait probe's barrier completed, which it cannot");
+}
+
 int sgb_synchronize(sgb_system* s) {
     if (!s) return fail(s, SGB_ERR_ARG, "null handle");
     CK(cudaStreamSynchronize(s->stream));
@@ -1905,6 +2130,45 @@ int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src) {
     }
     dst->nsamples += src->nsamples;
     cudaStreamSynchronize(dst->stream);
+    return SGB_OK;
+}
+
+int sgb_corr_compare(const sgb_corr* a, const sgb_corr* b, double* out) {
+    if (!a || !b || !out) return fail(nullptr, SGB_ERR_ARG, "null argument");
+    sgb_corr* ca = const_cast<sgb_corr*>(a);
+    if (!a->welford || !b->welford) return cfail(ca, SGB_ERR_ARG, "both accumulators need calculate_errors");
+    if (a->plen != b->plen || a->nomega != b->nomega || a->ncorr != b->ncorr || a->npos != b->npos)
+        return cfail(ca, SGB_ERR_ARG, "accumulators have different shapes");
+    if (a->nsamples < 2 || b->nsamples < 2) return cfail(ca, SGB_ERR_ARG, "each accumulator needs at least 2 samples");
+    if (b->stream != a->stream) cudaStreamSynchronize(b->stream);
+    double* part = nullptr;
+    if (cudaMalloc((void**)&part, sizeof(double) * 7 * SGB_CMP_BLOCKS) != cudaSuccess)
+        return cfail(ca, SGB_ERR_NOMEM, "device allocation failed");
+    const double na = (double)a->nsamples, nb = (double)b->nsamples;
+    int rc = corr_launch_compare_welford(a->P, a->M, b->P, b->M, 1.0 / (na * (na - 1)), 1.0 / (nb * (nb - 1)), a->plen,
+                                         part, a->stream);
+    (*ca->launches)++;
+    std::vector<double> h(7 * SGB_CMP_BLOCKS);
+    cudaError_t e = rc == SGB_OK ? cudaMemcpyAsync(h.data(), part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, a->stream)
+                                 : cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(a->stream);
+    cudaFree(part);
+    if (rc != SGB_OK || e != cudaSuccess) return cfail(ca, SGB_ERR_CUDA, std::string("compare: ") + cudaGetErrorString(e));
+    for (int k = 0; k < 7; k++) {
+        double t = 0;
+        for (int q = 0; q < SGB_CMP_BLOCKS; q++) t += h[(size_t)q * 7 + k];
+        out[k] = t;
+    }
+    out[7] = (double)a->plen;
+    // variance of Σ(|Δ|² − s) estimated from the spread of the per-block partial sums
+    // (blocks own interleaved bin sets, so correlated neighbouring bins stay in one block)
+    const double G = SGB_CMP_BLOCKS, mean = (out[0] - out[1]) / G;
+    double v = 0;
+    for (int q = 0; q < SGB_CMP_BLOCKS; q++) {
+        const double d = (h[(size_t)q * 7] - h[(size_t)q * 7 + 1]) - mean;
+        v += d * d;
+    }
+    out[8] = G * v / (G - 1);
     return SGB_OK;
 }
 

@@ -870,7 +870,7 @@ static int mid_tune(sgb_batch* b, BatchArgs<R>& A, MidArgs<R>& X, R dt, R lam, B
         float ms = 0.f;
         for (int rep = 0; rep < 2; rep++) {
             BCK(cudaMemcpyAsync(b->S, b->P, bytes, cudaMemcpyDeviceToDevice, b->stream));
-            BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
+            BCK(cudaMemsetAsync(b->ctrl, 0, sgb_ctrl_clear_bytes(), b->stream));
             BCK(cudaEventRecord(b->ev[6], b->stream));
             if ((rc = mid_launch<R, GEN>(b, shapes[k], A, X, tsteps, dt, lam, sn))) return rc;
             BCK(cudaEventRecord(b->ev[7], b->stream));
@@ -893,7 +893,7 @@ static int launch_midpoint(sgb_batch* b, BatchArgs<R>& A, MidArgs<R>& X, int nst
         int rc = mid_tune<R, GEN>(b, A, X, dt, lam, sn);
         if (rc) return rc;
     }
-    BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
+    BCK(cudaMemsetAsync(b->ctrl, 0, sgb_ctrl_clear_bytes(), b->stream));
     return mid_launch<R, GEN>(b, b->mid_shapes[b->mid_choice], A, X, nsteps, dt, lam, sn);
 }
 
@@ -1269,7 +1269,7 @@ int sgb_batch_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, u
     if (nsteps <= 0) return nsteps == 0 ? SGB_OK : bfail(b, SGB_ERR_ARG, "nsteps must be nonnegative");
     unsigned long long s0 = step0;
     BCK(cudaMemcpyAsync(b->counters, &s0, sizeof(s0), cudaMemcpyHostToDevice, b->stream));
-    BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
+    BCK(cudaMemsetAsync(b->ctrl, 0, sgb_ctrl_clear_bytes(), b->stream));
     int rc = b->fp32 ? enqueue_langevin<float>(b, dt, damping, seed, nsteps) : enqueue_langevin<double>(b, dt, damping, seed, nsteps);
     if (rc) return rc;
     Ctrl st;
@@ -1333,7 +1333,7 @@ int sgb_batch_step_ensemble(sgb_batch* b, double dt, double damping, uint64_t se
     if (!b->coup_set || !b->state_set) return bfail(b, SGB_ERR_STATE, "couplings and states must be set first");
     const int n_exch = (nsteps + exch_interval - 1) / exch_interval;
     int rc = SGB_OK;
-    BCK(cudaMemsetAsync(b->ctrl, 0, sizeof(Ctrl), b->stream));
+    BCK(cudaMemsetAsync(b->ctrl, 0, sgb_ctrl_clear_bytes(), b->stream));
     BCK(cudaMemsetAsync(b->counters + 1, 0, sizeof(unsigned long long), b->stream));
     const bool reuse = b->graph && b->graph_interval == exch_interval && b->graph_dt == dt && b->graph_damping == damping &&
                        b->graph_seed == seed;
@@ -1404,6 +1404,18 @@ int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, 
     }
     if (chosen) *chosen = b->mid_choice;
     return n;
+}
+
+int sgb_batch_set_wait_limit(sgb_batch* b, double seconds) {
+    if (!b) return SGB_ERR_ARG;
+    if (!(seconds >= 0) || seconds > 3600) {
+        b->err = "wait limit must be in [0, 3600] s (0: the 4 s default)";
+        return SGB_ERR_ARG;
+    }
+    const unsigned long long ns = (unsigned long long)(seconds * 1e9);
+    BCK(cudaMemcpyAsync(&b->ctrl->wait_ns, &ns, sizeof(ns), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    return SGB_OK;
 }
 
 int sgb_batch_event_record(sgb_batch* b, int32_t slot) {

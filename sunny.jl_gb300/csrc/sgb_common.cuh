@@ -5,6 +5,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stddef.h>
 #include <cuda/atomic>
 #include "../../include/sunny_gb300.h"
 
@@ -62,7 +63,15 @@ struct alignas(128) Ctrl {
     long long iters;
     int final_buf;
     int pad3[27];
+    // Wall-clock limit of every bounded wait of the launch, in ns (0: SGB_BARRIER_TIMEOUT_NS).
+    // It sits after the words that each launch clears (sgb_ctrl_clear_bytes), so a limit set
+    // on a handle (sgb_set_wait_limit) holds for all of its later launches.
+    unsigned long long wait_ns;
+    unsigned long long pad4[15];
 };
+
+// Bytes of Ctrl that are zeroed before a launch: everything up to the wait limit.
+constexpr size_t sgb_ctrl_clear_bytes() { return offsetof(Ctrl, wait_ns); }
 
 __device__ __forceinline__ uint64_t sgb_globaltimer() {
     uint64_t t;
@@ -80,7 +89,13 @@ __device__ __forceinline__ int sgb_read_status(Ctrl* c) {
     return cuda::atomic_ref<int, cuda::thread_scope_device>(c->status).load(cuda::memory_order_relaxed);
 }
 
+// Default limit of a bounded wait (4 s).
 #define SGB_BARRIER_TIMEOUT_NS 4000000000ull
+
+__device__ __forceinline__ uint64_t sgb_wait_limit(const Ctrl* c) {
+    const unsigned long long w = *(volatile const unsigned long long*)&c->wait_ns;
+    return w ? w : SGB_BARRIER_TIMEOUT_NS;
+}
 
 // Barrier across `nblocks` co-resident CTAs (cooperative launch guarantees residency).
 // Memory written before the barrier by any CTA is visible to plain loads of every CTA
@@ -102,7 +117,7 @@ __device__ __forceinline__ bool sgb_grid_barrier(Ctrl* c, unsigned int nblocks) 
                 // last arrival: count back to 0 and the next generation, in one release
                 bar.fetch_add(SGB_BAR_GEN - nblocks, cuda::memory_order_release);
             } else {
-                uint64_t t0 = 0;
+                uint64_t t0 = 0, lim = 0;
                 unsigned int spins = 0;
                 for (;;) {
                     const unsigned long long now = bar.load(cuda::memory_order_acquire);
@@ -112,8 +127,10 @@ __device__ __forceinline__ bool sgb_grid_barrier(Ctrl* c, unsigned int nblocks) 
                     }
                     if ((++spins & 255u) == 0) {
                         uint64_t t = sgb_globaltimer();
-                        if (t0 == 0) t0 = t;
-                        else if (t - t0 > SGB_BARRIER_TIMEOUT_NS) {
+                        if (t0 == 0) {
+                            t0 = t;
+                            lim = sgb_wait_limit(c);
+                        } else if (t - t0 > lim) {
                             sgb_set_status(c, SGB_ERR_TIMEOUT);
                             ok = 0;
                             break;

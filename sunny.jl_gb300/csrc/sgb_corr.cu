@@ -404,6 +404,44 @@ __global__ void k_merge_welford(double2* __restrict__ d1, double* __restrict__ M
     }
 }
 
+// Statistical comparison of two calculate_errors accumulators of one layout. Per bin k,
+// Δ = μa − μb and s = Ma/(na(na−1)) + Mb/(nb(nb−1)), the variance of Δ if both means
+// estimate one S(q,ω). Each block writes 7 FP64 partial sums: Σ|Δ|², Σs, Σs², Σ|μb|²,
+// Σ|μa|², #(|Δ|² > 9s), #(s > 0). Launched with 256 threads.
+__global__ void k_compare_welford(const double2* __restrict__ ma, const double* __restrict__ Ma,
+                                  const double2* __restrict__ mb, const double* __restrict__ Mb, double fa, double fb,
+                                  size_t len, double* __restrict__ part) {
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < len; e += (size_t)gridDim.x * blockDim.x) {
+        const double2 x = ma[e], y = mb[e];
+        const double dx = x.x - y.x, dy = x.y - y.y;
+        const double d2 = dx * dx + dy * dy;
+        const double sv = fa * Ma[e] + fb * Mb[e];
+        acc[0] += d2;
+        acc[1] += sv;
+        acc[2] += sv * sv;
+        acc[3] += y.x * y.x + y.y * y.y;
+        acc[4] += x.x * x.x + x.y * x.y;
+        acc[5] += d2 > 9.0 * sv ? 1.0 : 0.0;
+        acc[6] += sv > 0.0 ? 1.0 : 0.0;
+    }
+    __shared__ double red[8][7];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        double v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (l == 0) red[w][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 7) {
+        double t = 0;
+        for (int q = 0; q < 8; q++) t += red[q][threadIdx.x];
+        part[(size_t)blockIdx.x * 7 + threadIdx.x] = t;
+    }
+}
+
 // Columns of the accumulator belonging to the wave vectors qidx[0..nq): the B = ncorr*npos^2
 // columns of wave vector q are [q*B, (q+1)*B). tmp[k*B + b][ω] = scale * P[ω][qidx[k]*B + b].
 __global__ void k_gather_qcols(const double2* __restrict__ P, size_t ld, const int* __restrict__ qidx, int nq, int B,
@@ -482,6 +520,13 @@ int grid_for(size_t n) {
 }
 
 }  // namespace
+
+int corr_launch_compare_welford(const double* ma, const double* Ma, const double* mb, const double* Mb, double fa, double fb,
+                                size_t len, double* part, cudaStream_t st) {
+    k_compare_welford<<<SGB_CMP_BLOCKS, 256, 0, st>>>(reinterpret_cast<const double2*>(ma), Ma,
+                                                       reinterpret_cast<const double2*>(mb), Mb, fa, fb, len, part);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
 
 int corr_launch_gather_q(const double* P, size_t ld, const int* qidx, int nq, int B, int n, double scale, double* tmp,
                          cudaStream_t st) {

@@ -22,6 +22,10 @@ int corr_launch_welford(const double* tmp, int ncol, int n, size_t col0, size_t 
                         cudaStream_t st);
 int corr_launch_merge_welford(double* d1, double* M1, const double* d2, const double* M2, double n, double m, size_t len,
                               cudaStream_t st);
+// 7 partial sums per block of SGB_CMP_BLOCKS blocks (sgb_corr_compare)
+#define SGB_CMP_BLOCKS 1024
+int corr_launch_compare_welford(const double* ma, const double* Ma, const double* mb, const double* Mb, double fa, double fb,
+                                size_t len, double* part, cudaStream_t st);
 // intensities: gather the columns of a list of wave vectors; phase averaging + combiner
 int corr_launch_gather_q(const double* P, size_t ld, const int* qidx, int nq, int B, int n, double scale, double* tmp,
                          cudaStream_t st);

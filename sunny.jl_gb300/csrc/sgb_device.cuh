@@ -365,10 +365,20 @@ __device__ inline void grad_table(const Model<R>& M, const Tab<R>& T, int a, int
                         X, Y, Zc, gx, gy, gz);
 }
 
+template <class R, class NLD>
+__device__ inline void grad_inh(const Model<R>& M, const Tab<R>& T, int site, NLD nld, R sx, R sy, R sz, R& gx, R& gy,
+                                R& gz);
+
 // Single-system table form: per-site Zeeman field from M.h and the neighbour table M.nbr.
 template <class R>
 __device__ inline void grad_single(const Model<R>& M, const Tab<R>& T, int site, R sx, R sy, R sz, const R* X,
                                    const R* Y, const R* Zc, R& gx, R& gy, R& gz) {
+    if (M.ioff || M.oidx) {
+        grad_inh<R>(M, T, site, [X, Y, Zc](int j, R& x, R& y, R& z) {
+            x = sgb_ld(X + j); y = sgb_ld(Y + j); z = sgb_ld(Zc + j);
+        }, sx, sy, sz, gx, gy, gz);
+        return;
+    }
     R hx = 0, hy = 0, hz = 0;
     if (M.h) {
         hx = __ldg(M.h + site);
@@ -392,6 +402,92 @@ __device__ inline void grad_site(const Model<R>& M, const Tab<R>& T, int site, c
         hz = __ldg(M.h + 2 * M.ns + site);
     }
     grad_site_L<R, false>(M, T, ix, M.L1, M.L2, M.L3, hx, hy, hz, sx, sy, sz, X, Y, Zc, gx, gy, gz);
+}
+
+// ---- inhomogeneous systems: per-site coupling rows ------------------------------------
+// Visits the couplings of `site`: its own CSR entries when the system is inhomogeneous,
+// else the rows of its sublattice with neighbours from the table M.nbr. f(B, bq, j) gets
+// the coupling row, the base of its biquadratic matrices and the neighbour site.
+template <class R, class F>
+__device__ __forceinline__ void for_site_bonds(const Model<R>& M, const Tab<R>& T, int site, int a, F f) {
+    if (M.ioff) {
+        const int e1 = __ldg(M.ioff + site + 1);
+        for (int e = __ldg(M.ioff + site); e < e1; e++) {
+            const int2 en = __ldg(M.ient + e);
+            f(M.ctab[en.y], M.cbq, en.x);
+        }
+    } else {
+        const int b0 = T.boff[a], b1 = T.boff[a + 1];
+        for (int b = b0; b < b1; b++) f(T.bonds[b], T.bq, __ldg(M.nbr + (size_t)(b - b0) * M.ns + site));
+    }
+}
+
+// Stevens coefficients (and highest rank) of the onsite coupling at `site`.
+template <class R>
+__device__ __forceinline__ const R* stevens_at(const Model<R>& M, const Tab<R>& T, int site, int a, int& kmax) {
+    if (M.oidx) {
+        const int o = __ldg(M.oidx + site);
+        kmax = __ldg(M.okmax + o);
+        return M.otab + 28 * (size_t)o;
+    }
+    kmax = T.kmax[a];
+    return T.stev + 28 * a;
+}
+
+// J·t (+ biquadratic dE/dS at s) of one coupling row on neighbour spin t.
+template <class R>
+__device__ __forceinline__ void bond_grad(const Model<R>& M, const DBond<R>& B, const R* bqtab, R sx, R sy, R sz, R tx,
+                                          R ty, R tz, R& gx, R& gy, R& gz) {
+    if (B.jkind == 0) {
+        const R j = B.J[0];
+        gx += j * tx; gy += j * ty; gz += j * tz;
+    } else {
+        gx += B.J[0] * tx + B.J[3] * ty + B.J[6] * tz;
+        gy += B.J[1] * tx + B.J[4] * ty + B.J[7] * tz;
+        gz += B.J[2] * tx + B.J[5] * ty + B.J[8] * tz;
+    }
+    if (M.dipole_mode && B.bqkind != 0) {
+        R Qj[5], v[5];
+        quad5<R>(tx, ty, tz, Qj);
+        if (B.bqkind == 1) {
+#pragma unroll
+            for (int q = 0; q < 5; q++) v[q] = B.bq * ((R)biquad_metric(q) * Qj[q]);
+        } else {
+            const R* Bm = bqtab + 25 * B.bqidx;
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                R acc = 0;
+#pragma unroll
+                for (int p = 0; p < 5; p++) acc += Bm[q + 5 * p] * Qj[p];
+                v[q] = acc;
+            }
+        }
+        add_quad_grad<R>(sx, sy, sz, v, gx, gy, gz);
+    }
+}
+
+// dE/dS at `site` of a system with per-site couplings (set_energy_grad_dipoles! with
+// interactions_union[site], Interactions.jl:535-540); nld(j, x, y, z) loads spin j.
+template <class R, class NLD>
+__device__ inline void grad_inh(const Model<R>& M, const Tab<R>& T, int site, NLD nld, R sx, R sy, R sz, R& gx, R& gy,
+                                R& gz) {
+    gx = 0; gy = 0; gz = 0;
+    if (M.h) {
+        gx = __ldg(M.h + site);
+        gy = __ldg(M.h + M.ns + site);
+        gz = __ldg(M.h + 2 * M.ns + site);
+    }
+    const int a = site / M.ncell;
+    if (M.dipole_mode) {
+        int km;
+        const R* c = stevens_at<R>(M, T, site, a, km);
+        if (km > 0) classical_aniso<R>(c, km, sx, sy, sz, gx, gy, gz);
+    }
+    for_site_bonds<R>(M, T, site, a, [&](const DBond<R>& B, const R* bq, int j) {
+        R tx, ty, tz;
+        nld(j, tx, ty, tz);
+        bond_grad<R>(M, B, bq, sx, sy, sz, tx, ty, tz, gx, gy, gz);
+    });
 }
 
 // Integrators.jl:266-275 rhs_dipole!

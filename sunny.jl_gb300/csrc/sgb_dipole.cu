@@ -246,12 +246,47 @@ k_dip_grad(Model<R> M, const R* S, double* out) {
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(M, smem);
     const int ns = M.ns;
+    const bool inh = M.ioff || M.oidx;
     for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < ns; site += gridDim.x * blockDim.x) {
-        SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
         R gx, gy, gz;
-        grad_site<R>(M, T, site, ix, S[site], S[ns + site], S[2 * ns + site], S, S + ns, S + 2 * ns, gx, gy, gz);
+        if (inh) {
+            grad_single<R>(M, T, site, S[site], S[ns + site], S[2 * ns + site], S, S + ns, S + 2 * ns, gx, gy, gz);
+        } else {
+            SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
+            grad_site<R>(M, T, site, ix, S[site], S[ns + site], S[2 * ns + site], S, S + ns, S + 2 * ns, gx, gy, gz);
+        }
         out[3 * site] = gx; out[3 * site + 1] = gy; out[3 * site + 2] = gz;
     }
+}
+
+// Energy of one non-culled coupling row between spins s (this site) and t (Interactions.jl:466-505).
+template <class R>
+__device__ __forceinline__ double pair_energy_dip(const Model<R>& M, const DBond<R>& B, const R* bqtab, double sx,
+                                                  double sy, double sz, double tx, double ty, double tz) {
+    double E = (double)B.scalar;
+    if (B.jkind == 0) E += (double)B.J[0] * (sx * tx + sy * ty + sz * tz);
+    else {
+        double jx = (double)B.J[0] * tx + (double)B.J[3] * ty + (double)B.J[6] * tz;
+        double jy = (double)B.J[1] * tx + (double)B.J[4] * ty + (double)B.J[7] * tz;
+        double jz = (double)B.J[2] * tx + (double)B.J[5] * ty + (double)B.J[8] * tz;
+        E += sx * jx + sy * jy + sz * jz;
+    }
+    if (M.dipole_mode && B.bqkind != 0) {
+        double Qi[5], Qj[5];
+        quad5<double>(sx, sy, sz, Qi);
+        quad5<double>(tx, ty, tz, Qj);
+        double acc = 0;
+        if (B.bqkind == 1) {
+            for (int q = 0; q < 5; q++) acc += Qi[q] * (biquad_metric(q) * Qj[q]);
+            acc *= (double)B.bq;
+        } else {
+            const R* Bm = bqtab + 25 * B.bqidx;
+            for (int q = 0; q < 5; q++)
+                for (int p = 0; p < 5; p++) acc += Qi[q] * (double)Bm[q + 5 * p] * Qj[p];
+        }
+        E += acc;
+    }
+    return E;
 }
 
 // FP64 energy and magnetisation (Interactions.jl:401-508): partials[block][4].
@@ -269,11 +304,19 @@ k_dip_energy(Model<R> M, const R* S, double* partials) {
         if (M.h) E += (double)M.h[site] * sx + (double)M.h[ns + site] * sy + (double)M.h[2 * ns + site] * sz;
         const int a = ix.a;
         if (M.dipole_mode) {
-            int km = T.kmax[a];
+            int km;
+            const R* cr = stevens_at<R>(M, T, site, a, km);
             double c[28];
-            for (int q = 0; q < 28; q++) c[q] = (double)T.stev[28 * a + q];
+            for (int q = 0; q < 28; q++) c[q] = (double)cr[q];
             double gx = 0, gy = 0, gz = 0;
             E += classical_aniso<double>(c, km, sx, sy, sz, gx, gy, gz);
+        }
+        if (M.ioff) {
+            // per-site couplings: the non-culled rows of this site's own list
+            for_site_bonds<R>(M, T, site, a, [&](const DBond<R>& B, const R* bq, int js) {
+                if (B.fwd) E += pair_energy_dip<R>(M, B, bq, sx, sy, sz, S[js], S[ns + js], S[2 * ns + js]);
+            });
+            continue;
         }
         for (int b = T.boff[a]; b < T.boff[a + 1]; b++) {
             const DBond<R>& B = T.bonds[b];
@@ -619,6 +662,18 @@ int util_launch_noise_export(int sun, int N, int ns, uint64_t seed, uint64_t ste
 
 int util_launch_fill(double* p, size_t n, double v, cudaStream_t st) {
     k_fill<<<1024, SGB_BLOCK, 0, st>>>(p, n, v);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+// A grid barrier that expects one more CTA than the launch has, so it can only end by the
+// handle's wait limit: every CTA records SGB_ERR_TIMEOUT (or sees the abort flag) and
+// returns. Used to show callers that a bounded wait ends and the handle stays usable.
+__global__ void k_wait_probe(Ctrl* ctrl) {
+    sgb_grid_barrier(ctrl, gridDim.x + 1);
+}
+
+int util_launch_wait_probe(Ctrl* ctrl, int grid, cudaStream_t st) {
+    k_wait_probe<<<grid, 32, 0, st>>>(ctrl);
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 

@@ -62,6 +62,12 @@ struct sgb_system {
     double* ew_part = nullptr;       // [EWALD_PART_BLOCKS] energy partials
     double* lr_grad = nullptr;       // [ns][3] gradient of the per-stage integrator path
     int lr_grad_cap = 0;
+    // inhomogeneous couplings (sgb_set_bonds_at / sgb_set_onsite_at) and their device rows
+    bool inh_bonds = false, inh_onsite = false;
+    std::vector<sgb_site_bond> site_bonds_h;
+    std::vector<double> onsite_site_h;
+    void* inh_dev = nullptr;         // one allocation: ioff, ient, ctab, cbq, oidx, otab, okmax
+    std::vector<int> inh_off_h, inh_nbr_h;   // host copies of the per-site lists (LocalSampler colouring)
     // Langevin on small dipole lattices: -1 not yet timed, 0 persistent grid, cs > 0 a
     // cluster of cs CTAs holding the lattice in distributed shared memory
     int heun_cluster = -1;

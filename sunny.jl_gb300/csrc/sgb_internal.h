@@ -31,6 +31,18 @@ struct Model {
     int off_lam;        // R[na][N*N][2]        (SU(N): Λ, column-major)
     int off_qmat;       // R[5][N*N][2]         (SU(N): Stevens quadrupoles)
     int nb, nbq;
+    // Inhomogeneous systems (per-site couplings); nullptr where the per-sublattice tables
+    // above apply. Bonds: site s owns entries ioff[s] .. ioff[s+1] of ient, each (neighbour
+    // site, row of ctab); ctab rows hold both directions (the reversed copy has J^T and
+    // fwd = 0) and cbq their 5x5 biquadratic matrices. Onsite: oidx[s] is a row of otab
+    // (dipole: 28 Stevens coefficients, with highest rank okmax[row]; SU(N): N*N*2 Λ).
+    const int* ioff;
+    const int2* ient;
+    const DBond<R>* ctab;
+    const R* cbq;
+    const int* oidx;
+    const R* otab;
+    const int* okmax;
 };
 
 // Observable recording for SampledCorrelations trajectories.
@@ -201,6 +213,7 @@ template <class R>
 int util_launch_noise_export(int mode_sun, int N, int ns, uint64_t seed, uint64_t step, double* out,
                              cudaStream_t st);
 int util_launch_fill(double* p, size_t n, double v, cudaStream_t st);
+int util_launch_wait_probe(Ctrl* ctrl, int grid, cudaStream_t st);
 
 #define SGB_ENERGY_BLOCKS 256
 #define SGB_BLOCK 256          // block size of the non-persistent kernels

@@ -32,17 +32,56 @@ __device__ inline R mc_local_dE(const Model<R>& M, const Tab<R>& T, int site, in
     R dE = 0;
     if (M.h) dE += M.h[site] * dx + M.h[ns + site] * dy + M.h[2 * ns + site] * dz;
     if (M.dipole_mode) {
-        const int km = T.kmax[a];
+        int km;
+        const R* cs = stevens_at<R>(M, T, site, a, km);
         if (km > 0) {
             R c[28];
 #pragma unroll
-            for (int q = 0; q < 28; q++) c[q] = T.stev[28 * a + q];
+            for (int q = 0; q < 28; q++) c[q] = cs[q];
             R g0 = 0, g1 = 0, g2 = 0;
             dE += classical_aniso<R>(c, km, nx, ny, nz, g0, g1, g2) - classical_aniso<R>(c, km, ox, oy, oz, g0, g1, g2);
         }
     }
     R Qn[5], Qo[5];
     bool haveQ = false;
+    if (M.ioff) {
+        // per-site couplings: every row of the site's own list (reversed copies carry J^T)
+        for_site_bonds<R>(M, T, site, a, [&](const DBond<R>& B, const R* bq, int j) {
+            const R tx = sgb_ld(S + j), ty = sgb_ld(S + ns + j), tz = sgb_ld(S + 2 * ns + j);
+            if (B.jkind == 0) {
+                dE += B.J[0] * (dx * tx + dy * ty + dz * tz);
+            } else {
+                dE += dx * (B.J[0] * tx + B.J[3] * ty + B.J[6] * tz) + dy * (B.J[1] * tx + B.J[4] * ty + B.J[7] * tz) +
+                      dz * (B.J[2] * tx + B.J[5] * ty + B.J[8] * tz);
+            }
+            if (M.dipole_mode && B.bqkind != 0) {
+                if (!haveQ) {
+                    quad5<R>(nx, ny, nz, Qn);
+                    quad5<R>(ox, oy, oz, Qo);
+                    haveQ = true;
+                }
+                R Qj[5];
+                quad5<R>(tx, ty, tz, Qj);
+                R acc = 0;
+                if (B.bqkind == 1) {
+#pragma unroll
+                    for (int q = 0; q < 5; q++) acc += (Qn[q] - Qo[q]) * ((R)biquad_metric(q) * Qj[q]);
+                    acc *= B.bq;
+                } else {
+                    const R* Bm = bq + 25 * B.bqidx;
+#pragma unroll
+                    for (int q = 0; q < 5; q++) {
+                        R r = 0;
+#pragma unroll
+                        for (int p = 0; p < 5; p++) r += Bm[q + 5 * p] * Qj[p];
+                        acc += (Qn[q] - Qo[q]) * r;
+                    }
+                }
+                dE += acc;
+            }
+        });
+        return dE;
+    }
     // neighbour indices and spins are fetched MC_GATHER bonds at a time, so that their
     // loads are in flight together instead of one dependent pair of loads per bond
     constexpr int MC_GATHER = 8;

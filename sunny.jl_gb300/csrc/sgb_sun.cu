@@ -263,13 +263,62 @@ __device__ __forceinline__ void publish(const SpinConst<R, N>& sc, const R* qm, 
     }
 }
 
+// Λ of the onsite coupling at `site`: its own row (inhomogeneous systems) or its sublattice's.
+template <class R, int N>
+__device__ __forceinline__ const R* lam_at(const Model<R>& M, const SunTab<R, N>& S, int site, int a) {
+    return M.oidx ? M.otab + (size_t)2 * N * N * __ldg(M.oidx + site) : S.lam + a * 2 * N * N;
+}
+
+// sun_field over the site's own coupling rows (inhomogeneous systems).
+template <class R, bool BQ>
+__device__ __forceinline__ void sun_field_inh(const Model<R>& M, const Tab<R>& T, int site, int a, const R* D,
+                                              const R* Qb, R* d, R* v) {
+    const int ns = M.ns;
+    d[0] = 0; d[1] = 0; d[2] = 0;
+    if (M.h) { d[0] = __ldg(M.h + site); d[1] = __ldg(M.h + ns + site); d[2] = __ldg(M.h + 2 * ns + site); }
+    if (BQ) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) v[q] = 0;
+    }
+    for_site_bonds<R>(M, T, site, a, [&](const DBond<R>& B, const R* bq, int js) {
+        const R tx = sgb_ld(D + js), ty = sgb_ld(D + ns + js), tz = sgb_ld(D + 2 * ns + js);
+        if (B.jkind == 0) {
+            const R j = B.J[0];
+            d[0] += j * tx; d[1] += j * ty; d[2] += j * tz;
+        } else {
+            d[0] += B.J[0] * tx + B.J[3] * ty + B.J[6] * tz;
+            d[1] += B.J[1] * tx + B.J[4] * ty + B.J[7] * tz;
+            d[2] += B.J[2] * tx + B.J[5] * ty + B.J[8] * tz;
+        }
+        if (BQ && B.bqkind != 0) {
+            R Qj[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) Qj[q] = sgb_ld(Qb + (size_t)q * ns + js);
+            if (B.bqkind == 1) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) v[q] += B.bq * ((R)biquad_metric(q) * Qj[q]);
+            } else {
+                const R* Bm = bq + 25 * B.bqidx;
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    R acc = 0;
+#pragma unroll
+                    for (int p = 0; p < 5; p++) acc += Bm[q + 5 * p] * Qj[p];
+                    v[q] += acc;
+                }
+            }
+        }
+    });
+}
+
 template <class R, int N, bool BQ>
 __device__ __forceinline__ void local_HZ(const Model<R>& M, const SunTab<R, N>& S, const SpinConst<R, N>& sc, int site,
                                          const R* D, const R* Qb, const R* z, R* hz) {
     SiteIdx ix = decompose(site, M.L1, M.L2, M.L3);
     R d[3], v[5];
-    sun_field<R, BQ>(M, S.t, site, ix, D, Qb, d, v);
-    apply_H<R, N, BQ>(sc, S.lam + ix.a * 2 * N * N, S.qm, d, v, z, hz);
+    if (M.ioff) sun_field_inh<R, BQ>(M, S.t, site, ix.a, D, Qb, d, v);
+    else sun_field<R, BQ>(M, S.t, site, ix, D, Qb, d, v);
+    apply_H<R, N, BQ>(sc, lam_at<R, N>(M, S, site, ix.a), S.qm, d, v, z, hz);
 }
 
 template <class R, int N, int SPT, bool INJECT, bool BQ>
@@ -527,7 +576,7 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_sun_energy(Model<R> M, const R* Z
         double z[2 * N];
 #pragma unroll
         for (int c = 0; c < 2 * N; c++) z[c] = Z[(size_t)c * ns + site];
-        const R* lam = S.lam + ix.a * 2 * N * N;
+        const R* lam = lam_at<R, N>(M, S, site, ix.a);
         double eo = 0;
 #pragma unroll
         for (int c = 0; c < N; c++)
@@ -545,13 +594,7 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_sun_energy(Model<R> M, const R* Z
             expected_quad<double, N>(qmd, z, qi);
         }
         const double ki = (double)M.kappa[site];
-        for (int b = S.t.boff[ix.a]; b < S.t.boff[ix.a + 1]; b++) {
-            const DBond<R>& B = S.t.bonds[b];
-            if (!B.fwd) continue;
-            int x1 = sgb_wrap_pos(ix.c1 + B.n[0], M.L1);
-            int x2 = sgb_wrap_pos(ix.c2 + B.n[1], M.L2);
-            int x3 = sgb_wrap_pos(ix.c3 + B.n[2], M.L3);
-            int js = x1 + M.L1 * (x2 + M.L2 * (x3 + M.L3 * B.j));
+        auto bond_E = [&](const DBond<R>& B, const R* bqtab, int js) {
             double tx = D[js], ty = D[ns + js], tz = D[2 * ns + js];
             E += (double)B.scalar * ki * (double)M.kappa[js];
             if (B.jkind == 0) E += (double)B.J[0] * (sx * tx + sy * ty + sz * tz);
@@ -572,11 +615,25 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_sun_energy(Model<R> M, const R* Z
                     for (int q = 0; q < 5; q++) acc += qi[q] * (biquad_metric(q) * qj[q]);
                     acc *= (double)B.bq;
                 } else {
-                    const R* Bm = S.t.bq + 25 * B.bqidx;
+                    const R* Bm = bqtab + 25 * B.bqidx;
                     for (int q = 0; q < 5; q++)
                         for (int p = 0; p < 5; p++) acc += qi[q] * (double)Bm[q + 5 * p] * qj[p];
                 }
                 E += acc;
+            }
+        };
+        if (M.ioff) {
+            for_site_bonds<R>(M, S.t, site, ix.a, [&](const DBond<R>& B, const R* bq, int js) {
+                if (B.fwd) bond_E(B, bq, js);
+            });
+        } else {
+            for (int b = S.t.boff[ix.a]; b < S.t.boff[ix.a + 1]; b++) {
+                const DBond<R>& B = S.t.bonds[b];
+                if (!B.fwd) continue;
+                int x1 = sgb_wrap_pos(ix.c1 + B.n[0], M.L1);
+                int x2 = sgb_wrap_pos(ix.c2 + B.n[1], M.L2);
+                int x3 = sgb_wrap_pos(ix.c3 + B.n[2], M.L3);
+                bond_E(B, S.t.bq, x1 + M.L1 * (x2 + M.L2 * (x3 + M.L3 * B.j)));
             }
         }
     }
@@ -932,8 +989,42 @@ __device__ inline R sun_local_dE(const Model<R>& M, const SunTab<R, N>& S, int s
     const R dx = sn[0] - s0[0], dy = sn[1] - s0[1], dz = sn[2] - s0[2];
     R dE = 0;
     if (M.h) dE += M.h[site] * dx + M.h[ns + site] * dy + M.h[2 * ns + site] * dz;
-    const R* lam = S.lam + a * 2 * N * N;
+    const R* lam = lam_at<R, N>(M, S, site, a);
     dE += onsite_energy<R, N>(lam, zn) - onsite_energy<R, N>(lam, z0);
+    if (M.ioff) {
+        // per-site couplings: every row of the site's own list (reversed copies carry J^T)
+        for_site_bonds<R>(M, S.t, site, a, [&](const DBond<R>& B, const R* bq, int j) {
+            const R tx = sgb_ld(D + j), ty = sgb_ld(D + ns + j), tz = sgb_ld(D + 2 * ns + j);
+            if (B.jkind == 0) {
+                dE += B.J[0] * (dx * tx + dy * ty + dz * tz);
+            } else {
+                dE += dx * (B.J[0] * tx + B.J[3] * ty + B.J[6] * tz) + dy * (B.J[1] * tx + B.J[4] * ty + B.J[7] * tz) +
+                      dz * (B.J[2] * tx + B.J[5] * ty + B.J[8] * tz);
+            }
+            if (BQ && B.bqkind != 0) {
+                R Qj[5];
+#pragma unroll
+                for (int q = 0; q < 5; q++) Qj[q] = sgb_ld(Qb + (size_t)q * ns + j);
+                R acc = 0;
+                if (B.bqkind == 1) {
+#pragma unroll
+                    for (int q = 0; q < 5; q++) acc += (qn[q] - q0[q]) * ((R)biquad_metric(q) * Qj[q]);
+                    acc *= B.bq;
+                } else {
+                    const R* Bm = bq + 25 * B.bqidx;
+#pragma unroll
+                    for (int q = 0; q < 5; q++) {
+                        R r = 0;
+#pragma unroll
+                        for (int p = 0; p < 5; p++) r += Bm[q + 5 * p] * Qj[p];
+                        acc += (qn[q] - q0[q]) * r;
+                    }
+                }
+                dE += acc;
+            }
+        });
+        return dE;
+    }
     // neighbour indices and dipoles are fetched 8 bonds at a time (loads in flight together)
     constexpr int GATHER = 8;
     const int b0 = S.t.boff[a], b1 = S.t.boff[a + 1];

@@ -180,6 +180,10 @@ class System:
         self._field = np.zeros((ns, 3))
         self._pairs: dict[Bond, PairCoupling] = {}
         self._onsite = [None] * na
+        # inhomogeneous systems: per site, Sunny's pair list [Bond, PairCoupling, isculled]
+        # and its onsite coupling (None while the system is homogeneous)
+        self._site_pairs: list | None = None
+        self._site_onsite: list | None = None
         self._base_dip = np.zeros((na, L3, L2, L1, 3))
         self._base_coh = np.zeros((na, L3, L2, L1, max(self.N, 1)), dtype=complex)
         self.rng = np.random.default_rng(seed)
@@ -329,14 +333,17 @@ class System:
                 dm = np.ascontiguousarray(np.asarray(demag, dtype=float).T.reshape(-1))
                 _abi.check(lib.sgb_set_dipole_dipole(h, float(mu0), _abi.dptr(dm), _abi.dptr(lat), _abi.dptr(pos)), lib, h)
             self._ewald_dirty = False
+        if self._site_pairs is not None:
+            _abi.check(lib.sgb_set_onsite_at(h, _abi.dptr(self.onsite_site_table())), lib, h)
+            sb = self.site_bond_table()
+            arr = (_abi.SiteBondC * max(1, len(sb)))()
+            for k, b in enumerate(sb):
+                arr[k] = b
+            _abi.check(lib.sgb_set_bonds_at(h, arr, len(sb)), lib, h)
+            self._couplings_dirty = False
+            return
         for a in range(self.natoms):
-            oc = self._onsite[a]
-            if self.N:
-                M = np.zeros((self.N, self.N), dtype=complex) if oc is None else oc
-                arr = np.ascontiguousarray(np.stack([M.T.real, M.T.imag], -1).reshape(-1))  # column-major
-            else:
-                arr = np.zeros(28) if oc is None else np.ascontiguousarray(oc, dtype=float)
-            _abi.check(lib.sgb_set_onsite(h, a, _abi.dptr(arr)), lib, h)
+            _abi.check(lib.sgb_set_onsite(h, a, _abi.dptr(self._onsite_row(self._onsite[a]))), lib, h)
         bonds = self.bond_table()
         arr = (_abi.BondC * max(1, len(bonds)))()
         for k, b in enumerate(bonds):
@@ -344,23 +351,214 @@ class System:
         _abi.check(lib.sgb_set_bonds(h, arr, len(bonds)), lib, h)
         self._couplings_dirty = False
 
+    def _onsite_row(self, oc) -> np.ndarray:
+        """One onsite coupling in the C layout: 28 Stevens coefficients (dipole modes) or
+        the N x N matrix column-major as (re, im) (SU(N) mode)."""
+        if self.N:
+            M = np.zeros((self.N, self.N), dtype=complex) if oc is None else oc
+            return np.ascontiguousarray(np.stack([M.T.real, M.T.imag], -1).reshape(-1))
+        return np.zeros(28) if oc is None else np.ascontiguousarray(oc, dtype=float)
+
+    @staticmethod
+    def _bond_c(b: Bond, pc: PairCoupling):
+        e = _abi.BondC()
+        e.i, e.j = b.i - 1, b.j - 1
+        e.n[:] = b.n
+        e.scalar = pc.scalar
+        e.bilin[:] = list(np.asarray(pc.bilin, dtype=float).T.reshape(-1))
+        if isinstance(pc.biquad, np.ndarray):
+            e.biquad_kind = 2
+            e.biquad[:] = list(pc.biquad.T.reshape(-1))
+        elif pc.biquad != 0:
+            e.biquad_kind = 1
+            e.biquad[0] = float(pc.biquad)
+        return e
+
     def bond_table(self):
         """Non-culled pair couplings in the C layout (0-based atoms, column-major J)."""
-        out = []
+        return [self._bond_c(b, pc) for b, pc in self._pairs.items()]
+
+    # ---- inhomogeneous systems (Interactions.jl:81-100, 237-257; PairExchange.jl:431-605) ----
+    def is_homogeneous(self) -> bool:
+        return self._site_pairs is None
+
+    def _site_of(self, site) -> int:
+        """0-based linear site of a Sunny Site (c1, c2, c3, atom), all 1-based, or of an int."""
+        if isinstance(site, (int, np.integer)):
+            return int(site)
+        c1, c2, c3, a = (int(x) for x in site)
+        return self.site_index(c1, c2, c3, a)
+
+    def _cell_atom(self, i: int):
+        L1, L2, L3 = self.dims
+        return (i % L1, (i // L1) % L2, (i // (L1 * L2)) % L3), i // self.ncell
+
+    def bonded_site(self, i: int, b: Bond) -> int:
+        """bonded_site (System.jl:204-212), 0-based linear sites."""
+        (c1, c2, c3), _ = self._cell_atom(i)
+        L1, L2, L3 = self.dims
+        return self.site_index((c1 + b.n[0]) % L1 + 1, (c2 + b.n[1]) % L2 + 1, (c3 + b.n[2]) % L3 + 1, b.j)
+
+    def _make_inhomogeneous(self):
+        from .crystal import bond_parity
+        per_atom = [[] for _ in range(self.natoms)]
         for b, pc in self._pairs.items():
-            e = _abi.BondC()
-            e.i, e.j = b.i - 1, b.j - 1
-            e.n[:] = b.n
-            e.scalar = pc.scalar
-            e.bilin[:] = list(np.asarray(pc.bilin, dtype=float).T.reshape(-1))
-            if isinstance(pc.biquad, np.ndarray):
-                e.biquad_kind = 2
-                e.biquad[:] = list(pc.biquad.T.reshape(-1))
-            elif pc.biquad != 0:
-                e.biquad_kind = 1
-                e.biquad[0] = float(pc.biquad)
-            out.append(e)
+            per_atom[b.i - 1].append([b, pc, not bond_parity(b)])
+            rb = b.reverse()
+            rq = pc.biquad.T if isinstance(pc.biquad, np.ndarray) else pc.biquad
+            per_atom[b.j - 1].append([rb, PairCoupling(pc.scalar, np.asarray(pc.bilin, dtype=float).T, rq),
+                                      not bond_parity(rb)])
+        for lst in per_atom:
+            lst.sort(key=lambda e: e[2])          # non-culled first (Interactions.jl:38-41)
+        ns = self.nsites
+        self._site_pairs = [[list(e) for e in per_atom[i // self.ncell]] for i in range(ns)]
+        self._site_onsite = [self._onsite[i // self.ncell] for i in range(ns)]
+        self._couplings_dirty = True
+
+    def _require_inhomogeneous(self):
+        if self._site_pairs is None:
+            raise ValueError("Use `to_inhomogeneous` first.")
+
+    def _site_bond(self, i: int, k: int, offset):
+        """sites_to_internal_bond (PairExchange.jl:390-430), 0-based linear sites."""
+        (ca, a), (cb, b) = self._cell_atom(i), self._cell_atom(k)
+        n0 = np.array(cb) - np.array(ca)
+        dims = np.array(self.dims)
+        if offset is not None:
+            n = np.array(offset, dtype=int)
+            if np.all(np.mod(n - n0, dims) == 0):
+                return Bond(a + 1, b + 1, tuple(int(x) for x in n))
+            raise ValueError(f"Cells {tuple(int(x) + 1 for x in ca)} and {tuple(int(x) + 1 for x in cb)} are not "
+                             f"compatible with the offset {tuple(int(x) for x in n)} for a system with dimensions "
+                             f"{self.dims}.")
+        cands = [Bond(a + 1, b + 1, tuple(int(x) for x in n0 + dims * np.array((w1, w2, w3))))
+                 for w3 in (-1, 0, 1) for w2 in (-1, 0, 1) for w1 in (-1, 0, 1)]
+        d = np.array([self.crystal.distance(c) for c in cands])
+        perm = np.argsort(d, kind="stable")
+        if 4 * d[perm[0]] < d[perm[1]] - 1e-12:
+            return cands[perm[0]]
+        raise ValueError(f"Ambiguous offset vector. Possibilities include {cands[perm[0]].n} and {cands[perm[1]].n}. "
+                         "Try using a bigger system size, or pass an explicit offset.")
+
+    @staticmethod
+    def _replace_in_list(lst, b: Bond, pc: PairCoupling | None):
+        """replace_coupling_in_list! (PairExchange.jl:431-445)."""
+        from .crystal import bond_parity
+        lst[:] = [e for e in lst if e[0] != b]
+        if pc is None:
+            return
+        lst.append([b, pc, not bond_parity(b)])
+        lst.sort(key=lambda e: e[2])
+
+    def set_pair_coupling_at(self, scalar: float, bilin, biquad, site1, site2, offset=None):
+        """set_pair_coupling_at_aux! (PairExchange.jl:447-468): one coupling on the single
+        bond from site1 to site2, stored from both ends, ignoring crystal symmetry."""
+        self._require_inhomogeneous()
+        i, k = self._site_of(site1), self._site_of(site2)
+        if self._kappa[i] == 0 or self._kappa[k] == 0:
+            raise ValueError("Cannot couple vacant site")
+        J = np.asarray(bilin, dtype=float)
+        J = J * np.eye(3) if J.ndim == 0 else J.reshape(3, 3)
+        if self.mode == "dipole":
+            (_, a), (_, b) = self._cell_atom(i), self._cell_atom(k)
+            biquad = biquad * rcs_factors(self.spin_label(a + 1))[2] * rcs_factors(self.spin_label(b + 1))[2]
+        bond = self._site_bond(i, k, offset)
+        zero = scalar == 0 and not np.any(J) and (np.all(biquad == 0) if isinstance(biquad, np.ndarray) else biquad == 0)
+        rq = biquad.T if isinstance(biquad, np.ndarray) else biquad
+        self._replace_in_list(self._site_pairs[i], bond, None if zero else PairCoupling(float(scalar), J, biquad))
+        self._replace_in_list(self._site_pairs[k], bond.reverse(), None if zero else PairCoupling(float(scalar), J.T, rq))
+        self._couplings_dirty = True
+
+    def set_exchange_at(self, J, site1, site2, biquad: float = 0.0, offset=None):
+        """set_exchange_at!(sys, J, site1, site2; biquad, offset) (PairExchange.jl:470-490),
+        with adapt_for_biquad's scalar and bilinear shifts (PairExchange.jl:300-330)."""
+        J = np.asarray(J, dtype=float)
+        J = J * np.eye(3) if J.ndim == 0 else J.reshape(3, 3)
+        scalar = 0.0
+        biquad = float(biquad)
+        if biquad != 0:
+            (_, a), (_, b) = self._cell_atom(self._site_of(site1)), self._cell_atom(self._site_of(site2))
+            s1, s2 = self.spin_label(a + 1), self.spin_label(b + 1)
+            if self.mode in ("SUN", "dipole"):
+                J = J - (biquad / 2) * np.eye(3)
+                scalar += biquad * s1 * (s1 + 1) * s2 * (s2 + 1) / 3
+            else:
+                scalar += biquad * s1**2 * s2**2 / 3
+        self.set_pair_coupling_at(scalar, J, biquad, site1, site2, offset)
+
+    def set_onsite_coupling_at(self, op, site):
+        """set_onsite_coupling_at!(sys, op, site) (OnsiteCoupling.jl:222-231)."""
+        self._require_inhomogeneous()
+        i = self._site_of(site)
+        if self._kappa[i] == 0:
+            raise ValueError("Cannot couple vacant site")
+        _, a = self._cell_atom(i)
+        s = self.spin_label(a + 1)
+        N = int(round(2 * s + 1))
+        if callable(op):
+            op = op(*spin_matrices_of_dim(N))
+        A = np.asarray(op, dtype=complex)
+        if A.shape != (N, N):
+            raise ValueError("Invalid matrix size.")
+        if not np.allclose(A, A.conj().T):
+            raise ValueError("Operator is not Hermitian")
+        if self.mode == "SUN":
+            self._site_onsite[i] = A
+        elif self.mode == "dipole":
+            self._site_onsite[i] = stevens_expansion_for_dipole((A + A.conj().T) / 2, s, renormalize=True)
+        else:
+            raise ValueError("System with mode :dipole_uncorrected requires Stevens coefficients")
+        self._couplings_dirty = True
+
+    def set_vacancy_at(self, site):
+        """set_vacancy_at!(sys, site) (Interactions.jl:237-257): κ = 0, zero state, no onsite
+        coupling, and the site removed from its neighbours' lists (its own list stays)."""
+        self._require_inhomogeneous()
+        i = self._site_of(site)
+        self._sync_to_host()
+        self._kappa[i] = 0.0
+        self._base_dip.reshape(-1, 3)[i] = 0
+        if self.N:
+            self._base_coh.reshape(-1, self.N)[i] = 0
+        self._site_onsite[i] = None
+        for b, _, _ in self._site_pairs[i]:
+            k = self.bonded_site(i, b)
+            rb = b.reverse()
+            lst = self._site_pairs[k]
+            hits = [e for e in lst if e[0] == rb]
+            if len(hits) != 1:
+                raise ValueError("inconsistent pair lists")
+            lst.remove(hits[0])
+        self._host_newer = True
+        self._couplings_dirty = True
+
+    def remove_periodicity(self, flags):
+        """remove_periodicity!(sys, flags) (PairExchange.jl:592-605): drops every bond that
+        leaves the supercell along a flagged dimension."""
+        self._require_inhomogeneous()
+        for i in range(self.nsites):
+            (c, _) = self._cell_atom(i)
+            self._site_pairs[i] = [e for e in self._site_pairs[i]
+                                   if all((not f) or 0 <= c[d] + e[0].n[d] < self.dims[d] for d, f in enumerate(flags))]
+        self._couplings_dirty = True
+
+    def site_bond_table(self):
+        """Every site's non-culled pair couplings in the C layout (sgb_site_bond), in site order."""
+        out = []
+        for i, lst in enumerate(self._site_pairs):
+            (c, _) = self._cell_atom(i)
+            for b, pc, culled in lst:
+                if culled:
+                    continue
+                e = _abi.SiteBondC()
+                e.cell[:] = [int(x) for x in c]
+                e.bond = self._bond_c(b, pc)
+                out.append(e)
         return out
+
+    def onsite_site_table(self) -> np.ndarray:
+        """Per-site onsite couplings in the C layout, site order."""
+        return np.ascontiguousarray(np.concatenate([self._onsite_row(o) for o in self._site_onsite]))
 
     def set_pair_coupling(self, bond: Bond, scalar: float, bilin, biquad):
         """Set one coupling on `bond` and its equivalents (PairExchange.jl:185-244)."""
@@ -498,6 +696,12 @@ class System:
         self._sync_to_device()
         _abi.check(self._lib.sgb_set_langevin_cluster(self._h, int(mode)), self._lib, self._h)
 
+    def set_wait_limit(self, seconds: float):
+        """Wall-clock limit of the device-side waits of this system's persistent kernels
+        (0: the default, 4 s). A wait that runs past it fails the call with
+        SunnyGPUError(SGB_ERR_TIMEOUT); the system stays usable."""
+        _abi.check(self._lib.sgb_set_wait_limit(self._h, float(seconds)), self._lib, self._h)
+
     def set_midpoint_predictor(self, order: int):
         """First iterate of each dipole midpoint step within one call: 0 S' = S (the
         reference's choice), k in 1..4 the degree-k extrapolation of the last states.
@@ -615,6 +819,33 @@ def step(sys: System, integrator, nsteps: int = 1, noise: np.ndarray | None = No
     raise TypeError(f"unsupported integrator {type(integrator).__name__}")
 
 
+def to_inhomogeneous(sys: System) -> System:
+    """to_inhomogeneous(sys) (Interactions.jl:81-100): a copy whose couplings are held per
+    site, to be edited with set_exchange_at, set_pair_coupling_at, set_onsite_coupling_at,
+    set_vacancy_at and remove_periodicity."""
+    if not sys.is_homogeneous():
+        raise ValueError("System is already inhomogeneous.")
+    c = clone_system(sys)
+    c._make_inhomogeneous()
+    return c
+
+
+def set_exchange_at(sys: System, J, site1, site2, biquad: float = 0.0, offset=None):
+    sys.set_exchange_at(J, site1, site2, biquad=biquad, offset=offset)
+
+
+def set_onsite_coupling_at(sys: System, op, site):
+    sys.set_onsite_coupling_at(op, site)
+
+
+def set_vacancy_at(sys: System, site):
+    sys.set_vacancy_at(site)
+
+
+def remove_periodicity(sys: System, flags):
+    sys.remove_periodicity(flags)
+
+
 def clone_system(sys: System, seed=None) -> System:
     """clone_system(sys) (System.jl:144-175): a new System with copies of the couplings,
     κ, g, field and state, on the same device. Sunny copies the RNG; the clone keeps
@@ -631,6 +862,11 @@ def clone_system(sys: System, seed=None) -> System:
                                 pc.biquad.copy() if isinstance(pc.biquad, np.ndarray) else pc.biquad)
                 for b, pc in sys._pairs.items()}
     c._onsite = [None if o is None else np.array(o) for o in sys._onsite]
+    if sys._site_pairs is not None:
+        c._site_pairs = [[[e[0], PairCoupling(e[1].scalar, np.array(e[1].bilin, dtype=float),
+                                              e[1].biquad.copy() if isinstance(e[1].biquad, np.ndarray) else e[1].biquad),
+                           e[2]] for e in lst] for lst in sys._site_pairs]
+        c._site_onsite = [None if o is None else np.array(o) for o in sys._site_onsite]
     if sys._ewald is not None:
         c._ewald = (sys._ewald[0], np.array(sys._ewald[1]))
         c._ewald_dirty = True

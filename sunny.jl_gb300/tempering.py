@@ -124,6 +124,11 @@ class ReplicaBatch:
         self._check(self._lib.sgb_batch_langevin_noise(self._h, r, self.seed, step, _abi.dptr(out)))
         return out
 
+    def set_wait_limit(self, seconds: float):
+        """Wall-clock limit of the device-side waits of the batch's persistent kernels (0:
+        the default, 4 s)."""
+        self._check(self._lib.sgb_batch_set_wait_limit(self._h, float(seconds)))
+
     def set_midpoint_predictor(self, order: int):
         """First iterate of each batched midpoint step: 0 S' = S (the reference's choice),
         k in 1..4 the degree-k extrapolation of the last k+1 states (fewer iterations, same

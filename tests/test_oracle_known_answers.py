@@ -132,7 +132,7 @@ def test_gradient_matches_finite_differences(sg, orc, host):
     S = rng.standard_normal((h.nsites, 3))
     S = 2.0 * S / np.linalg.norm(S, axis=1)[:, None]
     g = o.grad(S)
-    eps = 1e-6
+    eps = 1e-4   # central differences: truncation ~eps^2, rounding of E ~1e-13 / eps
     for site in (0, 5, 17, 40):
         u = S[site] / np.linalg.norm(S[site])
         for a in range(3):
