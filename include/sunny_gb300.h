@@ -392,9 +392,10 @@ int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* desc, sgb_corr** ou
  * first batched add_sample after the couplings are set times every shape that fits on a
  * 3-step run and keeps the fastest. Writes up to `cap` rows of (neighbour-index bytes in
  * shared memory or 0 for the global table, bonds gathered together, CTAs per SM, grid,
- * dynamic shared bytes) into shapes[cap][5] and their tuning times into ms[cap] (either
- * may be NULL); *chosen = the row in use. Returns the number of shapes (0 before the
- * first batched add_sample). */
+ * dynamic shared bytes, kernel: 0 sublattice tiles or 1 cell blocks, cells per block as
+ * bx | by << 8 | bz << 16 for kernel 1) into shapes[cap][7] and their tuning times into
+ * ms[cap] (either may be NULL); *chosen = the row in use. Returns the number of shapes
+ * (0 before the first batched add_sample). */
 /* First fixed-point iterate of each batched midpoint step (no counterpart in the
  * reference, which starts from S' = S, Integrators.jl:389): order 0 does the same; order
  * k in 1..4 starts from the degree-k polynomial extrapolation of the last k+1 states,
@@ -403,6 +404,9 @@ int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* desc, sgb_corr** ou
  * 4 for FP32 batches, 0 for FP64 batches. */
 int sgb_batch_set_midpoint_predictor(sgb_batch* b, int32_t order);
 int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, float* ms, int32_t* chosen);
+/* Uses row `row` of sgb_batch_midpoint_shapes for the following batched trajectories, or
+ * -1 to time the shapes again at the next one (no counterpart in the reference). */
+int sgb_batch_select_midpoint_shape(sgb_batch* b, int32_t row);
 
 /* ---- adjoint: S(q,ω) loss gradient through a midpoint trajectory ------------ */
 /* No reverse rule exists in the reference; parameters follow the labelled-parameter

@@ -17,7 +17,14 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libsunnygb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["sgb_api.cu", "sgb_dipole.cu", "sgb_sun.cu", "sgb_corr.cu", "sgb_batch.cu", "sgb_static.cu", "sgb_adjoint.cu", "sgb_mc.cu", "sgb_opt.cu", "sgb_ewald.cu"]
+# (source, object name, extra flags): the two largest units are built once per precision
+SOURCES = [("sgb_api.cu", "sgb_api", []), ("sgb_dipole.cu", "sgb_dipole_f32", ["-DSGB_INST_PRECISION=32"]),
+           ("sgb_dipole.cu", "sgb_dipole_f64", ["-DSGB_INST_PRECISION=64"]),
+           ("sgb_sun.cu", "sgb_sun_f32", ["-DSGB_INST_PRECISION=32"]), ("sgb_sun.cu", "sgb_sun_f64", ["-DSGB_INST_PRECISION=64"]),
+           ("sgb_corr.cu", "sgb_corr", []), ("sgb_batch.cu", "sgb_batch", []), ("sgb_batch_blk.cu", "sgb_batch_blk", []),
+           ("sgb_static.cu", "sgb_static", []),
+           ("sgb_adjoint.cu", "sgb_adjoint", []), ("sgb_mc.cu", "sgb_mc", []), ("sgb_opt.cu", "sgb_opt", []),
+           ("sgb_ewald.cu", "sgb_ewald", [])]
 
 
 def nvcc() -> str:
@@ -27,13 +34,14 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libsunnygb300.so")
 
 
-def _compile(src: str, extra: list[str]) -> Path:
-    obj = BUILD / (Path(src).stem + ".o")
+def _compile(entry, extra: list[str]) -> Path:
+    src, name, flags = entry
+    obj = BUILD / (name + ".o")
     deps = [CSRC / src] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [PKG.parent / "include" / "sunny_gb300.h"]
     if obj.exists() and all(obj.stat().st_mtime >= d.stat().st_mtime for d in deps if d.exists()):
         return obj
     cmd = [nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-c",
-           str(CSRC / src), "-o", str(obj), *extra]
+           str(CSRC / src), "-o", str(obj), *flags, *extra]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")

@@ -26,36 +26,15 @@
 #include <type_traits>
 #include <vector>
 #include "sgb_device.cuh"
+#include "sgb_batch.cuh"
+#include "sgb_batch_blk.h"
 #include "sgb_tables.h"
 #include "sgb_handles.h"
 #include "sgb_corr.h"
 
 namespace {
 using namespace sgbdev;
-
-#define SGB_TILE 256
-#define SGB_MAXT 8
-
-template <class R>
-struct BatchArgs {
-    Model<R> M;
-    const int4* tiles;
-    int ntiles;
-    const int4* rd;     // (L1, L2, L3, ncell)
-    const int* roff;
-    const int* pc;      // [NS] packed (c1 | c2<<8 | c3<<16 | atom<<24) of every site
-    const int* nbr;     // neighbour tables
-    const int* nbo;     // [nrep] table offset of each replica
-    const int4* td;     // [ntiles][2] descriptors: (replica, first site, count, uniform atom or -1),
-                        //                          (replica offset, replica sites, table offset, 0)
-    int NS;
-    const R* kap;       // [na]
-    const R* h;         // [3][na] or nullptr
-    R* S;
-    R* P;
-    R* D1;
-    Ctrl* ctrl;
-};
+using namespace sgbbatch;
 
 struct TileCtx {
     int r, s, off;
@@ -293,73 +272,6 @@ __global__ void k_batch_noise(int ns, int rep, uint64_t seed, uint64_t step, dou
 
 // ---- batched implicit midpoint with snapshots (batched add_sample!) ---------------------
 
-template <class R>
-struct MidArgs {
-    R* Sp;          // current iterate S' (MV layout)
-    R* H;           // 3 rotating buffers of midpoint spins, MV<R>::W * NS elements each
-    R* Sc;          // candidate new state (MV layout)
-    double* racc;   // [3][nrep] FP64 convergence sums
-    R* P1;          // first iterate of the next step (MV layout), ord > 0
-    R* H1;          // states of the 1st, 2nd and 3rd previous steps (MV layout), ord >= 2, 3, 4
-    R* H2;
-    R* H3;
-    int ord;        // initial iterate of each step: 0 S' = S (as the reference), k > 0 polynomial extrapolation of order k
-    int nrep;
-    double atol2;
-    int max_iters;
-};
-
-template <class R>
-struct BSnap {
-    int enabled, nobs, measperiod, t0, ncell, na;
-    const R* ops;        // [nobs][3][ns_rep] of one replica (identical replicas)
-    R* buf;              // replica r at buf + r*rep_stride (complex)
-    size_t rep_stride;   // complex elements between replicas
-    R scale;
-};
-
-template <class R>
-__device__ __forceinline__ void snap_write(const BSnap<R>& sn, int r, int t, int s, int nsr, R x, R y, R z) {
-    const int cell = s % sn.ncell, a = s / sn.ncell;
-    R* buf = sn.buf + 2 * (size_t)r * sn.rep_stride;
-    for (int o = 0; o < sn.nobs; o++) {
-        const R* op = sn.ops + (size_t)o * 3 * nsr;
-        R v = op[s] * x + op[nsr + s] * y + op[2 * nsr + s] * z;
-        size_t idx = (((size_t)t * sn.nobs + o) * sn.na + a) * sn.ncell + cell;
-        buf[2 * idx] = v * sn.scale;
-        buf[2 * idx + 1] = 0;
-    }
-}
-
-#define SGB_MAXREP_CORR 64
-
-// Midpoint-private 3-vector buffers (iterate, candidate, rotating midpoint spins). FP32
-// keeps one float4 per site so that a neighbour costs one 16-byte load; FP64 keeps SoA
-// [3][NS]. K: elements from one site to the next; W * NS: elements of one buffer.
-template <class R>
-struct MV;
-template <>
-struct MV<float> {
-    static constexpr int K = 4, W = 4;
-    __device__ static __forceinline__ void ld(const float* b, int, int i, float& x, float& y, float& z) {
-        const float4 v = reinterpret_cast<const float4*>(b)[i];
-        x = v.x; y = v.y; z = v.z;
-    }
-    __device__ static __forceinline__ void st(float* b, int, int i, float x, float y, float z) {
-        reinterpret_cast<float4*>(b)[i] = make_float4(x, y, z, 0.f);
-    }
-};
-template <>
-struct MV<double> {
-    static constexpr int K = 1, W = 3;
-    __device__ static __forceinline__ void ld(const double* b, int n, int i, double& x, double& y, double& z) {
-        x = b[i]; y = b[n + i]; z = b[2 * n + i];
-    }
-    __device__ static __forceinline__ void st(double* b, int n, int i, double x, double y, double z) {
-        b[i] = x; b[n + i] = y; b[2 * n + i] = z;
-    }
-};
-
 // Batched implicit midpoint (Integrators.jl:379-413 per replica) recording snapshots.
 // Each CTA owns at most SGB_MAXT tiles for the whole launch. Their descriptors, the
 // sublattice of every site, kappa and the Zeeman field per sublattice, and (IDX != 0)
@@ -375,7 +287,7 @@ __global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) 
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(A.M, smem);
     IT* sidx = reinterpret_cast<IT*>(smem + A.M.tables_bytes);   // [tile][bond][SGB_TILE]
-    __shared__ R wpart[SGB_MAXT][SGB_TILE / 32];   // per-warp convergence partials of each tile
+    __shared__ double wpart[SGB_MAXT][SGB_TILE / 32];   // per-warp convergence partials of each tile
     __shared__ unsigned long long conv_mask;   // bit q: replica q met the tolerance this iteration
     __shared__ int4 st_a[SGB_MAXT];            // (replica, first site, count, replica offset)
     __shared__ int2 st_b[SGB_MAXT];            // (replica sites, neighbour-table offset)
@@ -452,7 +364,7 @@ __global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) 
             for (int k = 0; k < ntb; k++) {
                 const int4 ti = st_a[k];
                 const bool on = (actm >> k) & 1u;
-                R acc = 0;   // per-site terms in R; the warp, block and grid sums are FP64
+                double acc = 0;   // per-site terms in R; the warp, tile and grid sums in FP64
                 if (tid < ti.z) {
                     const int s = ti.y + tid, g = ti.w + s;
                     if (on) {
@@ -530,7 +442,8 @@ __global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) 
                     }
                 }
                 if (on) {
-                    // warp sum in R, kept per warp (no shared-memory FP64 atomics)
+                    // warp sum kept per warp (no shared-memory FP64 atomics); summing in FP64
+                    // makes the convergence decisions independent of how sites map to warps
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
                     if ((tid & 31) == 0) wpart[k][tid >> 5] = acc;
@@ -540,10 +453,10 @@ __global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) 
             // one thread per active tile: the tile's sum of its warps' partials, added in FP64
             // to its replica's grid sum (tiles never straddle replicas)
             if (tid < ntb && ((actm >> tid) & 1u)) {
-                R t = 0;
+                double t = 0;
 #pragma unroll
                 for (int w = 0; w < SGB_TILE / 32; w++) t += wpart[tid][w];
-                atomicAdd(&X.racc[slot * X.nrep + st_a[tid].x], (double)t);
+                atomicAdd(&X.racc[slot * X.nrep + st_a[tid].x], t);
             }
             if (leader) {
                 for (int q = 0; q < X.nrep; q++) X.racc[((slot + 1) % 3) * X.nrep + q] = 0.0;
@@ -810,6 +723,8 @@ static MidKernel<R> mid_kernel(int idx, int G) {
     return G == 12 ? k_batch_midpoint<R, GEN, 0, 12> : k_batch_midpoint<R, GEN, 0, 6>;
 }
 
+static void blk_shapes(sgb_batch* b, bool gen, std::vector<MidShape>& out);
+
 template <class R, bool GEN>
 static int mid_shapes(sgb_batch* b, std::vector<MidShape>& out) {
     out.clear();
@@ -839,13 +754,122 @@ static int mid_shapes(sgb_batch* b, std::vector<MidShape>& out) {
             }
         }
     }
+    if (std::is_same<R, float>::value) blk_shapes(b, GEN, out);
     if (out.empty()) return bfail(b, SGB_ERR_ARG, "replica batch too large for one persistent launch of the midpoint kernel");
     return SGB_OK;
+}
+
+// Geometry of a cell-block shape for this batch (replicas of equal size).
+static BlkGeom blk_geom(const sgb_batch* b, int lbx, int lby, int lbz) {
+    BlkGeom g{};
+    g.L1 = b->dims[0]; g.L2 = b->dims[1]; g.L3 = b->dims[2];
+    g.na = b->na;
+    g.gw = b->blk_gw;
+    g.lbx = lbx; g.lby = lby; g.lbz = lbz;
+    g.HX = (1 << lbx) + 2 * g.gw; g.HY = (1 << lby) + 2 * g.gw; g.HZ = (1 << lbz) + 2 * g.gw;
+    g.PX = g.L1 + 2 * g.gw; g.PY = g.L2 + 2 * g.gw; g.PZ = g.L3 + 2 * g.gw;
+    g.nbx = g.L1 >> lbx; g.nby = g.L2 >> lby; g.nbz = g.L3 >> lbz;
+    g.nblk = g.nbx * g.nby * g.nbz * b->nrep;
+    g.nsr = g.L1 * g.L2 * g.L3 * g.na;
+    g.tx_bytes = (unsigned)(16ull * g.HX * g.HY * g.HZ * g.na);
+    g.halo_bytes = g.tx_bytes;
+    return g;
+}
+
+// Cell-block shapes (sgb_batch_blk.cu): FP32 batches of equal replicas whose bonds reach at
+// most gw cells with 2 gw <= L. Blocks are powers of two dividing the supercell; the shapes
+// kept are those of least halo per site whose box, tables and bond offsets fit in shared
+// memory and whose blocks fit in one co-resident launch.
+static void blk_shapes(sgb_batch* b, bool gen, std::vector<MidShape>& out) {
+    for (int r = 1; r < b->nrep; r++)
+        for (int k = 0; k < 3; k++)
+            if (b->dims[3 * r + k] != b->dims[k]) return;
+    int gw = 0;
+    for (const sgb_bond& e : b->bonds)
+        for (int k = 0; k < 3; k++) gw = std::max(gw, std::abs(e.n[k]));
+    gw = std::max(gw, 1);
+    for (int k = 0; k < 3; k++)
+        if (b->dims[k] < 2 * gw) return;
+    const size_t pad = (size_t)(b->dims[0] + 2 * gw) * (b->dims[1] + 2 * gw) * (b->dims[2] + 2 * gw) * b->na * b->nrep;
+    if (b->Hpad && (b->blk_gw != gw || b->hpad_bytes != 3 * 16 * pad)) {
+        bfree(b->Hpad);
+        b->hpad_bytes = 0;
+    }
+    if (!b->Hpad) {
+        if (cudaMalloc(&b->Hpad, 3 * 16 * pad) != cudaSuccess) {
+            cudaGetLastError();
+            b->Hpad = nullptr;
+            return;
+        }
+        b->hpad_bytes = 3 * 16 * pad;
+    }
+    b->blk_gw = gw;
+    b->blk_maps.clear();
+    struct Cand {
+        double cost;
+        int lbx, lby, lbz;
+    };
+    std::vector<Cand> cands;
+    auto log2_div = [](int L, int l) { return (L % (1 << l)) == 0; };
+    for (int lx = 0; (1 << lx) <= b->dims[0]; lx++)
+        for (int ly = 0; (1 << ly) <= b->dims[1]; ly++)
+            for (int lz = 0; (1 << lz) <= b->dims[2]; lz++) {
+                if (!log2_div(b->dims[0], lx) || !log2_div(b->dims[1], ly) || !log2_div(b->dims[2], lz)) continue;
+                const long long nsb = (long long)b->na << (lx + ly + lz);
+                if (nsb < SGB_BLK_THREADS || nsb > 16 * SGB_BLK_THREADS) continue;
+                BlkGeom g = blk_geom(b, lx, ly, lz);
+                if (g.HX > 256 || g.HY > 256 || g.HZ > 256) continue;
+                const size_t smem = 128 + g.halo_bytes + (size_t)b->tables_bytes + 4 * (size_t)((b->fp32 ? b->mf.nb : b->md.nb) + 4);
+                if (smem > 200 * 1024) continue;
+                cands.push_back({(double)g.HX * g.HY * g.HZ / (double)((1 << lx) * (1 << ly) * (1 << lz)), lx, ly, lz});
+            }
+    std::sort(cands.begin(), cands.end(), [](const Cand& p, const Cand& q) { return p.cost < q.cost; });
+    int kept = 0;
+    for (const Cand& c : cands) {
+        if (kept >= 4) break;
+        BlkGeom g = blk_geom(b, c.lbx, c.lby, c.lbz);
+        const size_t smem = 128 + g.halo_bytes + (size_t)b->tables_bytes + 4 * (size_t)((b->fp32 ? b->mf.nb : b->md.nb) + 4);
+        bool any = false;
+        for (int G : {6, 12}) {
+            int bps = 0;
+            if (blk_occupancy(gen, G, smem, &bps) != SGB_OK || bps < 1) {
+                cudaGetLastError();
+                continue;
+            }
+            const long long grid = std::min<long long>((long long)bps * b->nsm, g.nblk);
+            if ((g.nblk + grid - 1) / grid > SGB_BLK_MAXB) continue;
+            if (!any) {
+                BlkMaps m;
+                bool ok = true;
+                for (int k = 0; k < 3 && ok; k++)
+                    ok = blk_encode_map(&m.m[k], reinterpret_cast<float*>(b->Hpad) + (size_t)k * 4 * pad, g, b->nrep) == SGB_OK;
+                if (!ok) break;
+                b->blk_maps.push_back(m);
+                any = true;
+            }
+            MidShape sh{0, G, bps, (int)grid, smem, 0.f};
+            sh.kind = 1;
+            sh.lbx = c.lbx; sh.lby = c.lby; sh.lbz = c.lbz;
+            sh.maps = (int)b->blk_maps.size() - 1;
+            out.push_back(sh);
+        }
+        if (any) kept++;
+    }
 }
 
 template <class R, bool GEN>
 static int mid_launch(sgb_batch* b, const MidShape& sh, BatchArgs<R>& A, MidArgs<R>& X, int nsteps, R dt, R lam,
                       BSnap<R>& sn) {
+    if constexpr (std::is_same<R, float>::value) {
+        if (sh.kind == 1) {
+            const BlkGeom g = blk_geom(b, sh.lbx, sh.lby, sh.lbz);
+            b->launches++;
+            if (blk_launch(GEN, sh.G, sh.grid, sh.smem, A, X, g, b->blk_maps[sh.maps], reinterpret_cast<float*>(b->Hpad), nsteps,
+                           dt, lam, sn, b->stream) != SGB_OK)
+                return bfail(b, SGB_ERR_CUDA, std::string("cell-block midpoint launch: ") + cudaGetErrorString(cudaGetLastError()));
+            return SGB_OK;
+        }
+    }
     int kb = b->kb;
     void* args[] = {&A, &X, &nsteps, &dt, &lam, &sn, &kb};
     return bcoop(b, mid_kernel<R, GEN>(sh.idx, sh.G), sh.grid, sh.smem, args);
@@ -969,6 +993,7 @@ void sgb_batch_destroy(sgb_batch* b) {
     p = b->nbo; bfree(p);
     p = b->td; bfree(p);
     bfree(b->S); bfree(b->P); bfree(b->D1); bfree(b->Sp); bfree(b->H); bfree(b->Sc); bfree(b->P1); bfree(b->H1); bfree(b->H2); bfree(b->H3);
+    bfree(b->Hpad);
     p = b->racc; bfree(p); p = b->ctrl; bfree(p); p = b->Epart; bfree(p); p = b->E; bfree(p);
     p = b->counters; bfree(p); p = b->n_accept; bfree(p);
     if (b->stage) cudaFreeHost(b->stage);
@@ -1397,13 +1422,25 @@ int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, 
     for (int k = 0; k < n && k < cap; k++) {
         const MidShape& m = b->mid_shapes[k];
         if (shapes) {
-            int32_t* r = shapes + 5 * k;
+            int32_t* r = shapes + 7 * k;
             r[0] = m.idx; r[1] = m.G; r[2] = m.bps; r[3] = m.grid; r[4] = (int32_t)m.smem;
+            r[5] = m.kind;
+            r[6] = m.kind ? (1 << m.lbx) | ((1 << m.lby) << 8) | ((1 << m.lbz) << 16) : 0;
         }
         if (ms) ms[k] = m.ms;
     }
     if (chosen) *chosen = b->mid_choice;
     return n;
+}
+
+int sgb_batch_select_midpoint_shape(sgb_batch* b, int32_t row) {
+    if (!b) return SGB_ERR_ARG;
+    if (row < -1 || row >= (int)b->mid_shapes.size()) {
+        b->err = "no such midpoint launch shape (run a batched add_sample first)";
+        return SGB_ERR_ARG;
+    }
+    b->mid_choice = row;
+    return SGB_OK;
 }
 
 int sgb_batch_set_wait_limit(sgb_batch* b, double seconds) {

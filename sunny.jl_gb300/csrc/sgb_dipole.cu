@@ -647,10 +647,15 @@ int dip_launch_energy(const Model<R>& M, const R* S, double* partials, int nbloc
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
+// SGB_INST_PRECISION (32 or 64) builds this file once per precision, in parallel; the
+// precision-independent launchers go with the FP64 copy.
+#if !defined(SGB_INST_PRECISION) || SGB_INST_PRECISION == 64
 int util_launch_reduce(const double* partials, int n, int ncomp, double* out, cudaStream_t st) {
     k_reduce_partials<<<1, SGB_BLOCK, 0, st>>>(partials, n, ncomp, out);
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
+
+#endif
 
 template <class R>
 int util_launch_noise_export(int sun, int N, int ns, uint64_t seed, uint64_t step, double* out, cudaStream_t st) {
@@ -660,6 +665,7 @@ int util_launch_noise_export(int sun, int N, int ns, uint64_t seed, uint64_t ste
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
+#if !defined(SGB_INST_PRECISION) || SGB_INST_PRECISION == 64
 int util_launch_fill(double* p, size_t n, double v, cudaStream_t st) {
     k_fill<<<1024, SGB_BLOCK, 0, st>>>(p, n, v);
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
@@ -676,6 +682,7 @@ int util_launch_wait_probe(Ctrl* ctrl, int grid, cudaStream_t st) {
     k_wait_probe<<<grid, 32, 0, st>>>(ctrl);
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
+#endif
 
 #define SGB_INST(R)                                                                                      \
     template int dip_launch_heun<R>(const Model<R>&, R*, R*, Ctrl*, int, double, double, double, uint64_t, \
@@ -690,5 +697,9 @@ int util_launch_wait_probe(Ctrl* ctrl, int grid, cudaStream_t st) {
     template size_t dip_cluster_smem<R>(const Model<R>&, int);                                                 \
     template int dip_launch_snapshot<R>(const Model<R>&, const R*, const SnapArgs<R>&, int, cudaStream_t);     \
     template int util_launch_noise_export<R>(int, int, int, uint64_t, uint64_t, double*, cudaStream_t);
+#if !defined(SGB_INST_PRECISION) || SGB_INST_PRECISION == 32
 SGB_INST(float)
+#endif
+#if !defined(SGB_INST_PRECISION) || SGB_INST_PRECISION == 64
 SGB_INST(double)
+#endif

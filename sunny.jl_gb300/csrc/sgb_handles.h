@@ -118,12 +118,15 @@ struct sgb_corr {
 
 // One launch shape of the batched midpoint kernel and its autotuning time.
 struct MidShape {
-    int idx;        // neighbour indices: 2 = uint16 in shared memory, 4 = int32 in shared memory, 0 = global
+    int idx;        // tile kernel: neighbour indices 2 = uint16 in shared memory, 4 = int32 in shared memory, 0 = global
     int G;          // bonds whose neighbour spins are gathered together
     int bps;        // CTAs per SM
     int grid;
     size_t smem;
     float ms;       // time of the tuning run (0 if not timed)
+    int kind = 0;   // 0 tile kernel; 1 cell-block kernel with blocks of 2^lbx x 2^lby x 2^lbz cells
+    int lbx = 0, lby = 0, lbz = 0;
+    int maps = -1;  // cell-block kernel: its tensor maps in sgb_batch::blk_maps
 };
 
 struct sgb_batch {
@@ -171,6 +174,10 @@ struct sgb_batch {
     int kb = 0;                     // most bonds of any sublattice (neighbour-table rows)
     int nsr_max = 0;                // sites of the largest replica
     std::vector<MidShape> mid_shapes;   // launch shapes of the batched midpoint kernel that fit
+    void* Hpad = nullptr;           // cell-block kernel: 3 padded midpoint-spin buffers (float4)
+    size_t hpad_bytes = 0;
+    int blk_gw = 0;                 // their ghost width (largest bond offset)
+    std::vector<BlkMaps> blk_maps;  // tensor maps of the cell-block shapes
     int mid_choice = -1;            // shape picked by the autotuner (-1: not tuned for these couplings)
     // state
     void* S = nullptr;

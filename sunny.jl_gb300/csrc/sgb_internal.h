@@ -1,6 +1,7 @@
 // sgb_internal.h -- host/device interface between the C ABI (sgb_api.cu) and the kernel
 // translation units. Not installed; not part of the public ABI.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
@@ -55,6 +56,12 @@ struct SnapArgs {
     const R* ops;        // dipole: [nobs][3][ns]; SU(N): [nobs][N*N][2][ns]
     R* buf;              // complex [n_all_omega][nobs][npos][ncell] (interleaved re,im)
     R scale;             // 1/sqrt(ncell)
+};
+
+// Tensor maps of the three padded midpoint-spin buffers of the cell-block batched
+// midpoint kernel (sgb_batch_blk.cu).
+struct BlkMaps {
+    CUtensorMap m[3];
 };
 
 struct LaunchInfo {

@@ -1385,5 +1385,10 @@ int sun_launch_local_dE(const Model<R>& M, const R* Z, const R* D, const R* Q, i
     template int sun_launch_heun_cluster<R>(const Model<R>&, R*, R*, R*, int, int, double, double, double, uint64_t, \
                                             uint64_t, const double*, cudaStream_t);                            \
     template int sun_launch_local_dE<R>(const Model<R>&, const R*, const R*, const R*, int, const SunKet&, double*, cudaStream_t);
+// SGB_INST_PRECISION (32 or 64) builds this file once per precision, in parallel.
+#if !defined(SGB_INST_PRECISION) || SGB_INST_PRECISION == 32
 SGB_SUN_INST(float)
+#endif
+#if !defined(SGB_INST_PRECISION) || SGB_INST_PRECISION == 64
 SGB_SUN_INST(double)
+#endif

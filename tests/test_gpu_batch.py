@@ -141,14 +141,50 @@ def test_midpoint_autotune_shapes(gpu, sg):
                 b.set_state(r, saved[r])
         sg.add_sample(sc, b)
         finals.append([b.get_state(r) for r in range(4)])
-        shapes = (C.c_int32 * 40)()
-        ms = (C.c_float * 8)()
+        shapes = (C.c_int32 * (7 * 16))()
+        ms = (C.c_float * 16)()
         chosen = C.c_int32(-1)
-        n = b._lib.sgb_batch_midpoint_shapes(b.handle, 8, shapes, ms, C.byref(chosen))
+        n = b._lib.sgb_batch_midpoint_shapes(b.handle, 16, shapes, ms, C.byref(chosen))
         assert n >= 2 and 0 <= chosen.value < n
-        rows = [tuple(shapes[5 * k:5 * k + 5]) for k in range(n)]
-        assert any(r[0] == 2 for r in rows) and any(r[0] == 0 for r in rows)
+        rows = [tuple(shapes[7 * k:7 * k + 7]) for k in range(n)]
+        assert any(r[5] == 0 and r[0] == 2 for r in rows) and any(r[5] == 0 and r[0] == 0 for r in rows)
+        assert any(r[5] == 1 for r in rows)        # the cell-block kernel is a candidate
         assert all(ms[k] > 0 for k in range(n))
         b.close()
     for r in range(4):
         assert np.array_equal(finals[0][r], finals[1][r])
+
+
+def test_every_midpoint_shape_gives_the_same_trajectory(gpu, sg):
+    # the sublattice-tile and cell-block kernels share the per-site arithmetic and sum the
+    # convergence test in FP64, so every launch shape produces the same samples and states
+    import ctypes as C
+    proto = sg.System(sg.pyrochlore_crystal(), [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(4, 4, 4), seed=6,
+                      precision="fp32", device=None)
+    proto.set_exchange(1.0, proto.crystal.bonds_at_distance(np.sqrt(2) / 4)[0])
+    proto.set_exchange(0.05, proto.crystal.bonds_at_distance(np.sqrt(6) / 4)[0])
+    b = sg.ReplicaBatch(proto, [(4, 4, 4)] * 3, kT=[0.2] * 3, precision="fp32", seed=3)
+    b.randomize_spins()
+    b.langevin(0.025, 0.1, 200)
+    start = [b.get_state(r) for r in range(3)]
+    kw = dict(energies=np.linspace(0, 6, 12), dt=0.025, tol=1e-6)
+    sc = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), **kw)
+    sg.add_sample(sc, b)                     # times the shapes
+    n = b._lib.sgb_batch_midpoint_shapes(b.handle, 0, None, None, None)
+    shapes = (C.c_int32 * (7 * n))()
+    b._lib.sgb_batch_midpoint_shapes(b.handle, n, shapes, None, None)
+    kinds = [shapes[7 * k + 5] for k in range(n)]
+    assert 0 in kinds and 1 in kinds
+    finals, datas = [], []
+    for row in range(n):
+        for r in range(3):
+            b.set_state(r, start[r])
+        s2 = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), **kw)
+        assert b._lib.sgb_batch_select_midpoint_shape(b.handle, row) == 0
+        sg.add_sample(s2, b)
+        finals.append(np.concatenate([b.get_state(r) for r in range(3)]))
+        datas.append(s2.data)
+        s2.close()
+    for k in range(1, n):
+        assert np.array_equal(finals[k], finals[0]), (kinds[k], np.max(np.abs(finals[k] - finals[0])))
+        assert np.allclose(datas[k], datas[0], rtol=0, atol=1e-12 * np.max(np.abs(datas[0])))
