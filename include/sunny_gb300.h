@@ -114,6 +114,16 @@ int sgb_set_onsite(sgb_system* sys, int32_t atom, const double* coeffs);
  * The per-sublattice table replaces any per-site table of sgb_set_bonds_at. */
 int sgb_set_bonds(sgb_system* sys, const sgb_bond* bonds, int32_t nbonds);
 
+/* General pair couplings of SU(N) mode: the tensor decomposition Σ_k A_k ⊗ B_k of a
+ * PairCoupling (`general`, src/System/Types.jl:23-30), which adds Σ_k <A_k>_i <B_k>_j to the
+ * energy (Interactions.jl:495-503) and (A_k Z_i) <B_k>_j, <A_k>_i (B_k Z_j) to HZ
+ * (Interactions.jl:660-666). Term t belongs to bonds[bond[t]] of the last sgb_set_bonds
+ * call (seen from its atom i; the library stores the reversed copy with A and B swapped,
+ * as reverse(tensordec) does); A and B: [nterms][N][N] complex, column-major, (re, im)
+ * interleaved, Hermitian. nterms = 0 removes every general term. Per-sublattice systems
+ * only: a system with per-site couplings (sgb_set_bonds_at) returns SGB_ERR_ARG. */
+int sgb_set_general(sgb_system* sys, const int32_t* bond, int32_t nterms, const double* A, const double* B);
+
 /* Inhomogeneous pair couplings: every site's own list, as Sunny keeps it after
  * to_inhomogeneous (Interactions.jl:81-100) and edits it with set_exchange_at!,
  * set_pair_coupling_at! (PairExchange.jl:447-534), set_vacancy_at! (Interactions.jl:237-257)

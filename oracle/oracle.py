@@ -37,7 +37,8 @@ class OrSys(C.Structure):
                 ("kappa", C.POINTER(C.c_double)), ("g", C.POINTER(C.c_double)), ("field", C.POINTER(C.c_double)),
                 ("onsite", C.POINTER(C.c_double)), ("bonds", C.POINTER(BondC)), ("nbonds", C.c_int),
                 ("onsite_site", C.POINTER(C.c_double)), ("site_bonds", C.POINTER(SiteBondC)),
-                ("nsite_bonds", C.c_int64)]
+                ("nsite_bonds", C.c_int64), ("gen_bond", C.POINTER(C.c_int)), ("gen_A", C.POINTER(C.c_double)),
+                ("gen_B", C.POINTER(C.c_double)), ("ngen", C.c_int)]
 
 
 _D = C.POINTER(C.c_double)
@@ -91,9 +92,10 @@ class OracleSystem:
     """FP64 CPU model built from the same host tables the GPU library receives."""
 
     def __init__(self, dims, natoms, N, mode, kappa, g_colmajor, field, onsite, bonds, onsite_site=None,
-                 site_bonds=None):
+                 site_bonds=None, general=None):
         """onsite_site / site_bonds: the per-site onsite couplings and the non-culled per-site
-        pair couplings (SiteBondC) of an inhomogeneous system, else None."""
+        pair couplings (SiteBondC) of an inhomogeneous system, else None. general: SU(N)
+        general pair couplings as (bond indices, A, B) with A, B [nterms][N][N] complex."""
         self.lib = load()
         self.dims, self.na, self.N, self.mode = tuple(dims), natoms, N, mode
         self.ns = int(np.prod(dims)) * natoms
@@ -122,6 +124,15 @@ class OracleSystem:
             self._site_bonds = sb
             s.site_bonds = sb
             s.nsite_bonds = len(site_bonds)
+        if general is not None and len(general[0]):
+            gb, A, B = general
+            self._gen = (np.ascontiguousarray(gb, dtype=np.int32),
+                         np.ascontiguousarray(np.stack([np.swapaxes(A, -1, -2).real, np.swapaxes(A, -1, -2).imag], -1)).reshape(-1),
+                         np.ascontiguousarray(np.stack([np.swapaxes(B, -1, -2).real, np.swapaxes(B, -1, -2).imag], -1)).reshape(-1))
+            s.gen_bond = self._gen[0].ctypes.data_as(C.POINTER(C.c_int))
+            s.gen_A = _p(self._gen[1])
+            s.gen_B = _p(self._gen[2])
+            s.ngen = len(gb)
         self.s = s
 
     @classmethod
@@ -140,7 +151,8 @@ class OracleSystem:
         field = sys._field.reshape(-1) if np.any(sys._field) else None
         mode = {"dipole": MODE_DIPOLE, "dipole_uncorrected": MODE_DIPOLE_UNCORRECTED, "SUN": MODE_SUN}[sys.mode]
         if sys.is_homogeneous():
-            return cls(sys.dims, na, sys.N, mode, sys._kappa, gcm, field, onsite, sys.bond_table())
+            return cls(sys.dims, na, sys.N, mode, sys._kappa, gcm, field, onsite, sys.bond_table(),
+                       general=sys.general_table())
         return cls(sys.dims, na, sys.N, mode, sys._kappa, gcm, field, onsite, [], onsite_site=sys.onsite_site_table(),
                    site_bonds=[SiteBondC.from_buffer_copy(bytes(b)) for b in sys.site_bond_table()])
 

@@ -188,6 +188,21 @@ static void expected_quadrupole(const or_ops* ops, const cplx* z, double* Q) {
     }
 }
 
+/* <Z|M|Z> and M Z for an N x N complex matrix M, column-major (re, im). */
+static double expect_op(int N, const double* Mx, const cplx* z) {
+    cplx acc = 0;
+    for (int c = 0; c < N; c++)
+        for (int r = 0; r < N; r++) acc += conj(z[r]) * (Mx[2 * (r + N * c)] + I * Mx[2 * (r + N * c) + 1]) * z[c];
+    return creal(acc);
+}
+static void apply_op(int N, const double* Mx, const cplx* z, cplx* out) {
+    for (int r = 0; r < N; r++) {
+        cplx acc = 0;
+        for (int c = 0; c < N; c++) acc += (Mx[2 * (r + N * c)] + I * Mx[2 * (r + N * c) + 1]) * z[c];
+        out[r] = acc;
+    }
+}
+
 /* ---- OnsiteCoupling.jl:316-425 energy_and_gradient_for_classical_anisotropy --------- */
 static int stevens_kmax(const double* c) {
     int k2 = 0, k4 = 0, k6 = 0;
@@ -477,6 +492,28 @@ void or_grad_coherents(const or_sys* s, const double* Z, double* HZ) {
                             pair_grad_coherents(&ops, pc, i, j, Z, HZ);
                         }
             }
+        /* general couplings (Interactions.jl:660-666): HZ_i += <B>_j A Z_i, HZ_j += <A>_i B Z_j */
+        for (int t = 0; t < s->ngen; t++) {
+            const sgb_bond* pc = &s->bonds[s->gen_bond[t]];
+            const double* A = s->gen_A + (size_t)2 * N * N * t;
+            const double* B = s->gen_B + (size_t)2 * N * N * t;
+            for (int c3 = 0; c3 < L3; c3++)
+                for (int c2 = 0; c2 < L2; c2++)
+                    for (int c1 = 0; c1 < L1; c1++) {
+                        int64_t i = site_index(s, c1, c2, c3, pc->i);
+                        int64_t j = site_index(s, wrap(c1 + pc->n[0], L1), wrap(c2 + pc->n[1], L2),
+                                               wrap(c3 + pc->n[2], L3), pc->j);
+                        cplx zi[8], zj[8], ai[8], bj[8];
+                        for (int k = 0; k < N; k++) { zi[k] = zget(Z, i, N, k); zj[k] = zget(Z, j, N, k); }
+                        const double Ab = expect_op(N, A, zi), Bb = expect_op(N, B, zj);
+                        apply_op(N, A, zi, ai);
+                        apply_op(N, B, zj, bj);
+                        for (int k = 0; k < N; k++) {
+                            zset(HZ, i, N, k, zget(HZ, i, N, k) + ai[k] * Bb);
+                            zset(HZ, j, N, k, zget(HZ, j, N, k) + bj[k] * Ab);
+                        }
+                    }
+        }
     }
     free(dip);
     free(dEdS);
@@ -580,6 +617,22 @@ double or_energy(const or_sys* s, const double* S, const double* Z) {
                     }
         }
         E += Ea;
+    }
+    /* general couplings (Interactions.jl:495-503): Σ_k <A_k>_i <B_k>_j */
+    for (int t = 0; sun && t < s->ngen; t++) {
+        const sgb_bond* pc = &s->bonds[s->gen_bond[t]];
+        const double* A = s->gen_A + (size_t)2 * N * N * t;
+        const double* B = s->gen_B + (size_t)2 * N * N * t;
+        for (int c3 = 0; c3 < L3; c3++)
+            for (int c2 = 0; c2 < L2; c2++)
+                for (int c1 = 0; c1 < L1; c1++) {
+                    int64_t i = site_index(s, c1, c2, c3, pc->i);
+                    int64_t j = site_index(s, wrap(c1 + pc->n[0], L1), wrap(c2 + pc->n[1], L2), wrap(c3 + pc->n[2], L3),
+                                           pc->j);
+                    cplx zi[8], zj[8];
+                    for (int k = 0; k < N; k++) { zi[k] = zget(Z, i, N, k); zj[k] = zget(Z, j, N, k); }
+                    E += expect_op(N, A, zi) * expect_op(N, B, zj);
+                }
     }
     return E;
 }
@@ -738,6 +791,24 @@ double or_local_energy_change_sun(const or_sys* s, const double* S, const double
                 expected_quadrupole(&ops, zj, Qj);
                 dE += end == 0 ? biquad_pair(pc, dQ, Qj) : biquad_pair(pc, Qj, dQ);
             }
+        }
+    }
+    /* general couplings: Δ<A>_site <B>_j where the site is the first end, <A>_k Δ<B>_site
+     * where it is the second (Interactions.jl:364-370) */
+    for (int t = 0; t < s->ngen; t++) {
+        const sgb_bond* pc = &s->bonds[s->gen_bond[t]];
+        const double* A = s->gen_A + (size_t)2 * N * N * t;
+        const double* B = s->gen_B + (size_t)2 * N * N * t;
+        for (int end = 0; end < 2; end++) {
+            if ((end == 0 ? pc->i : pc->j) != a) continue;
+            int sg_ = end == 0 ? 1 : -1;
+            int64_t o = site_index(s, wrap(c1 + sg_ * pc->n[0], L1), wrap(c2 + sg_ * pc->n[1], L2), wrap(c3 + sg_ * pc->n[2], L3),
+                                   end == 0 ? pc->j : pc->i);
+            if (o == site) return NAN;
+            cplx zo[8];
+            for (int k = 0; k < N; k++) zo[k] = zget(Z, o, N, k);
+            if (end == 0) dE += (expect_op(N, A, zn) - expect_op(N, A, z0)) * expect_op(N, B, zo);
+            else dE += expect_op(N, A, zo) * (expect_op(N, B, zn) - expect_op(N, B, z0));
         }
     }
     return dE;

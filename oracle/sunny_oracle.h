@@ -37,6 +37,12 @@ typedef struct {
     const double* onsite_site;
     const sgb_site_bond* site_bonds;
     int64_t nsite_bonds;
+    /* SU(N) general pair couplings (Types.jl:23-30): term t = A[t] ⊗ B[t] on bonds[gen_bond[t]],
+     * A, B [ngen][N][N] complex column-major (re, im). */
+    const int* gen_bond;
+    const double* gen_A;
+    const double* gen_B;
+    int ngen;
 } or_sys;
 
 int64_t or_nsites(const or_sys* s);

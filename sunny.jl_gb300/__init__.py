@@ -7,7 +7,8 @@ The directory is ``sunny.jl_gb300/``; it is imported under the module name
 from .crystal import (Bond, Crystal, bond_parity, lattice_vectors, cubic_crystal, bcc_crystal,
                       fcc_primitive_crystal, diamond_crystal, pyrochlore_crystal, triangular_crystal)
 from .operators import (spin_matrices, spin_matrices_of_dim, stevens_matrices_of_dim, rcs_factors,
-                        matrix_to_stevens_coefficients, expected_spin, ket_from_dipole)
+                        matrix_to_stevens_coefficients, expected_spin, ket_from_dipole,
+                        hermitian_basis, tensor_decomposition)
 from .system import (System, Moment, Langevin, ImplicitMidpoint, step, energy, energy_per_site,
                      magnetization, energy_grad, set_exchange, set_onsite_coupling, set_field,
                      randomize_spins, polarize_spins, langevin_noise, LocalSampler, propose_uniform,

@@ -72,6 +72,7 @@ SIGNATURES = {
     "sgb_set_onsite": (C.c_int, [_P, _I32, _D]),
     "sgb_set_bonds": (C.c_int, [_P, C.POINTER(BondC), _I32]),
     "sgb_set_bonds_at": (C.c_int, [_P, C.POINTER(SiteBondC), _I64]),
+    "sgb_set_general": (C.c_int, [_P, C.POINTER(_I32), _I32, _D, _D]),
     "sgb_set_onsite_at": (C.c_int, [_P, _D]),
     "sgb_set_state": (C.c_int, [_P, _D, _D]),
     "sgb_get_state": (C.c_int, [_P, _D, _D]),

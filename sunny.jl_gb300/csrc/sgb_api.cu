@@ -90,8 +90,25 @@ template <class R>
 int build_tables(sgb_system* s, Model<R>& M) {
     std::vector<unsigned char> buf;
     bool any_bq = false;
-    std::string e = sgbhost::pack_tables<R>(s->d.natoms, s->N, s->sun, s->d.dims, s->bonds_h, s->onsite_h, M, buf, any_bq);
+    sgbhost::GeneralTerms gen;
+    gen.bond = s->gen_bond_h;
+    gen.A = s->gen_A_h;
+    gen.B = s->gen_B_h;
+    std::vector<R> grows;
+    std::string e = sgbhost::pack_tables<R>(s->d.natoms, s->N, s->sun, s->d.dims, s->bonds_h, s->onsite_h, M, buf, any_bq,
+                                            s->sun ? &gen : nullptr, &grows);
     if (!e.empty()) return fail(s, SGB_ERR_ARG, e);
+    dfree(s->gtab);
+    M.gtab = nullptr;
+    if (!grows.empty()) {
+        int rg = dmalloc(s, &s->gtab, sizeof(R) * grows.size());
+        if (rg) return rg;
+        CK(cudaMemcpy(s->gtab, grows.data(), sizeof(R) * grows.size(), cudaMemcpyHostToDevice));
+        M.gtab = reinterpret_cast<const R*>(s->gtab);
+        // the general terms run in the kernels that publish quadrupoles (and densities)
+        M.has_biquad = 1;
+        any_bq = true;
+    }
     dfree(s->tables);
     int rc = dmalloc(s, &s->tables, buf.size());
     if (rc) return rc;
@@ -357,8 +374,8 @@ size_t cluster_smem(sgb_system* s, int nsl) {
 
 template <class R>
 int cluster_size(sgb_system* s) {
-    // the cluster kernels read the per-sublattice tables only
-    if (s->inh_bonds || s->inh_onsite) return 0;
+    // the cluster kernels read the per-sublattice tables only, without general terms
+    if (s->inh_bonds || s->inh_onsite || !s->gen_bond_h.empty()) return 0;
     int cs = 1;
     while (cs < SGB_CLUSTER_MAX && (long long)cs * SGB_CLUSTER_BLOCK < s->ns) cs *= 2;
     const int nsl = (s->ns + cs - 1) / cs;
@@ -834,9 +851,11 @@ int sgb_create(const sgb_desc* d, sgb_system** out) {
     rc |= dmalloc(s, &s->H, R * 9 * ns);
     if (s->sun) {
         rc |= dmalloc(s, &s->Z, R * 2 * s->N * ns);
-        rc |= dmalloc(s, &s->Q, R * 5 * ns);
-        rc |= dmalloc(s, &s->QP, R * 5 * ns);
-        rc |= dmalloc(s, &s->QH, R * 15 * ns);
+        // quadrupoles, then the packed density (general couplings) of each site
+        const size_t qrows = 5 + (size_t)s->N * s->N;
+        rc |= dmalloc(s, &s->Q, R * qrows * ns);
+        rc |= dmalloc(s, &s->QP, R * qrows * ns);
+        rc |= dmalloc(s, &s->QH, R * 3 * qrows * ns);
     }
     rc |= dmalloc(s, (void**)&s->ctrl, sizeof(Ctrl));
     rc |= dmalloc(s, (void**)&s->partials, sizeof(double) * 4 * SGB_ENERGY_BLOCKS);
@@ -868,6 +887,7 @@ void sgb_destroy(sgb_system* s) {
     p = s->mc_perm; dfree(p);
     p = s->mc_part; dfree(p);
     dfree(s->inh_dev);
+    dfree(s->gtab);
     ewald_free(s);
     p = s->lr_grad; dfree(p);
     dfree(s->flush);
@@ -948,9 +968,36 @@ int sgb_set_bonds(sgb_system* s, const sgb_bond* bonds, int32_t nbonds) {
         if (b.biquad_kind < 0 || b.biquad_kind > 2) return fail(s, SGB_ERR_ARG, "biquad_kind must be 0, 1 or 2");
     }
     s->bonds_h.assign(bonds, bonds + nbonds);
+    // general terms refer to the previous bond list: the caller sets them again
+    s->gen_bond_h.clear();
+    s->gen_A_h.clear();
+    s->gen_B_h.clear();
     s->inh_bonds = false;
     s->site_bonds_h.clear();
     s->bonds_set = true;
+    s->tables_dirty = true;
+    return SGB_OK;
+}
+
+int sgb_set_general(sgb_system* s, const int32_t* bond, int32_t nterms, const double* A, const double* B) {
+    if (!s || nterms < 0 || (nterms > 0 && (!bond || !A || !B))) return fail(s, SGB_ERR_ARG, "invalid general terms");
+    if (nterms > 0 && !s->sun) return fail(s, SGB_ERR_ARG, "General couplings require mode :SUN");
+    if (nterms > 0 && s->inh_bonds) return fail(s, SGB_ERR_ARG, "general couplings are supported on per-sublattice systems only");
+    const int N = s->N;
+    for (int t = 0; t < nterms; t++) {
+        if (bond[t] < 0 || bond[t] >= (int)s->bonds_h.size()) return fail(s, SGB_ERR_ARG, "general term on an unknown bond");
+        for (const double* Mx : {A + (size_t)2 * N * N * t, B + (size_t)2 * N * N * t})
+            for (int r = 0; r < N; r++)
+                for (int c = 0; c < N; c++) {
+                    const double ar = Mx[2 * (r + N * c)], ai = Mx[2 * (r + N * c) + 1];
+                    const double br = Mx[2 * (c + N * r)], bi = Mx[2 * (c + N * r) + 1];
+                    if (std::fabs(ar - br) > 1e-10 * (1 + std::fabs(ar)) || std::fabs(ai + bi) > 1e-10 * (1 + std::fabs(ai)))
+                        return fail(s, SGB_ERR_ARG, "Operator is not Hermitian");
+                }
+    }
+    s->gen_bond_h.assign(bond, bond + nterms);
+    s->gen_A_h.assign(A, A + (size_t)2 * N * N * nterms);
+    s->gen_B_h.assign(B, B + (size_t)2 * N * N * nterms);
     s->tables_dirty = true;
     return SGB_OK;
 }
@@ -968,6 +1015,7 @@ int sgb_set_bonds_at(sgb_system* s, const sgb_site_bond* bonds, int64_t nbonds) 
         for (int d = 0; d < 3; d++)
             if (c[d] < 0 || c[d] >= L[d]) return fail(s, SGB_ERR_ARG, "cell index out of range");
     }
+    if (!s->gen_bond_h.empty()) return fail(s, SGB_ERR_ARG, "general couplings are supported on per-sublattice systems only");
     s->site_bonds_h.assign(bonds, bonds + nbonds);
     s->inh_bonds = true;
     s->bonds_set = true;

@@ -30,6 +30,8 @@ struct DBond {
     int bqidx;       // row in the 5x5 biquadratic table
     int fwd;         // 1 for the non-culled copy (counted in the energy)
     int pk;          // raw offsets and target packed as bytes: (n0+128) | (n1+128)<<8 | (n2+128)<<16 | j<<24
+    int gidx;        // SU(N) general terms: first row in the general-term table
+    int gcnt;        //                      number of rows (0: none)
 };
 
 // Sunny's scalar_biquad_metric (src/System/Types.jl:40)

@@ -62,6 +62,10 @@ struct sgb_system {
     double* ew_part = nullptr;       // [EWALD_PART_BLOCKS] energy partials
     double* lr_grad = nullptr;       // [ns][3] gradient of the per-stage integrator path
     int lr_grad_cap = 0;
+    // SU(N) general pair couplings (sgb_set_general) and their device rows
+    std::vector<int> gen_bond_h;
+    std::vector<double> gen_A_h, gen_B_h;
+    void* gtab = nullptr;
     // inhomogeneous couplings (sgb_set_bonds_at / sgb_set_onsite_at) and their device rows
     bool inh_bonds = false, inh_onsite = false;
     std::vector<sgb_site_bond> site_bonds_h;

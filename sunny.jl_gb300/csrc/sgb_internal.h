@@ -44,6 +44,12 @@ struct Model {
     const int* oidx;
     const R* otab;
     const int* okmax;
+    // SU(N) general pair couplings: term rows of 4 N^2 values, [a (N^2)][A (N*N complex)][b (N^2)],
+    // where <A> = a·ρ and <B> = b·ρ over the packed density ρ of a ket (sun_rho); rows of a
+    // bond are DBond::gidx .. gidx + gcnt. has_general: any such row.
+    const R* gtab;
+    int has_general;
+    int qrows;          // rows per site of the SU(N) multipole buffers: 5 quadrupoles, then ρ (N^2)
 };
 
 // Observable recording for SampledCorrelations trajectories.

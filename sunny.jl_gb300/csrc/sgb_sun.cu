@@ -250,8 +250,28 @@ __device__ inline SunTab<R, N> stage_sun(const Model<R>& M, unsigned char* smem)
     return s;
 }
 
+// Packed density of a ket, ρ = z z^†: |z_r|^2 for r < N, then for each r < c the real and
+// imaginary parts of z_c conj(z_r). <M> = Σ_rc conj(z_r) M_rc z_c = a(M)·ρ with a(M) =
+// (Re M_rr; 2 Re M_rc, -2 Im M_rc).
+template <class R, int N>
+__device__ __forceinline__ void sun_rho(const R* z, R* rho) {
+#pragma unroll
+    for (int r = 0; r < N; r++) rho[r] = z[2 * r] * z[2 * r] + z[2 * r + 1] * z[2 * r + 1];
+    int k = N;
+#pragma unroll
+    for (int r = 0; r < N; r++)
+#pragma unroll
+        for (int c = r + 1; c < N; c++) {
+            rho[k++] = z[2 * c] * z[2 * r] + z[2 * c + 1] * z[2 * r + 1];
+            rho[k++] = z[2 * c + 1] * z[2 * r] - z[2 * c] * z[2 * r + 1];
+        }
+}
+
+// Dipoles (and with BQ quadrupoles, and with rho the packed density ρ in rows 5..5+N^2) of
+// ket z, for neighbours to read.
 template <class R, int N, bool BQ>
-__device__ __forceinline__ void publish(const SpinConst<R, N>& sc, const R* qm, const R* z, int ns, int site, R* D, R* Qb) {
+__device__ __forceinline__ void publish(const SpinConst<R, N>& sc, const R* qm, const R* z, int ns, int site, R* D, R* Qb,
+                                        bool rho = false) {
     R nx, ny, nz;
     expected_spin<R, N>(sc, z, nx, ny, nz);
     D[site] = nx; D[ns + site] = ny; D[2 * ns + site] = nz;
@@ -260,6 +280,48 @@ __device__ __forceinline__ void publish(const SpinConst<R, N>& sc, const R* qm, 
         expected_quad<R, N>(qm, z, q);
 #pragma unroll
         for (int a = 0; a < 5; a++) Qb[(size_t)a * ns + site] = q[a];
+        if (rho) {
+            R p[N * N];
+            sun_rho<R, N>(z, p);
+#pragma unroll
+            for (int a = 0; a < N * N; a++) Qb[(size_t)(5 + a) * ns + site] = p[a];
+        }
+    }
+}
+
+// General pair couplings (Interactions.jl:660-666): hz += Σ_bonds Σ_terms <B>_j (A z), with
+// <B>_j from the neighbour's published density.
+template <class R, int N>
+__device__ __forceinline__ void general_HZ(const Model<R>& M, const Tab<R>& T, int site, int a, const R* Qb, const R* z,
+                                           R* hz) {
+    const int ns = M.ns, b0 = T.boff[a], b1 = T.boff[a + 1];
+    for (int b = b0; b < b1; b++) {
+        const DBond<R>& B = T.bonds[b];
+        if (B.gcnt == 0) continue;
+        const int j = __ldg(M.nbr + (size_t)(b - b0) * ns + site);
+        R rj[N * N];
+#pragma unroll
+        for (int k = 0; k < N * N; k++) rj[k] = sgb_ld(Qb + (size_t)(5 + k) * ns + j);
+        for (int t = 0; t < B.gcnt; t++) {
+            const R* row = M.gtab + (size_t)(B.gidx + t) * 4 * N * N;
+            const R* Am = row + N * N;
+            const R* bv = row + 3 * N * N;
+            R Bb = 0;
+#pragma unroll
+            for (int k = 0; k < N * N; k++) Bb += __ldg(bv + k) * rj[k];
+#pragma unroll
+            for (int r = 0; r < N; r++) {
+                R ar = 0, ai = 0;
+#pragma unroll
+                for (int c = 0; c < N; c++) {
+                    const R mr = __ldg(Am + 2 * (r + N * c)), mi = __ldg(Am + 2 * (r + N * c) + 1);
+                    ar += mr * z[2 * c] - mi * z[2 * c + 1];
+                    ai += mr * z[2 * c + 1] + mi * z[2 * c];
+                }
+                hz[2 * r] += Bb * ar;
+                hz[2 * r + 1] += Bb * ai;
+            }
+        }
     }
 }
 
@@ -319,6 +381,7 @@ __device__ __forceinline__ void local_HZ(const Model<R>& M, const SunTab<R, N>& 
     if (M.ioff) sun_field_inh<R, BQ>(M, S.t, site, ix.a, D, Qb, d, v);
     else sun_field<R, BQ>(M, S.t, site, ix, D, Qb, d, v);
     apply_H<R, N, BQ>(sc, lam_at<R, N>(M, S, site, ix.a), S.qm, d, v, z, hz);
+    if (BQ && M.has_general) general_HZ<R, N>(M, S.t, site, ix.a, Qb, z, hz);
 }
 
 template <class R, int N, int SPT, bool INJECT, bool BQ>
@@ -368,7 +431,7 @@ k_sun_heun(Model<R> M, R* Z, R* D, R* Qb, R* P, R* QP, Ctrl* ctrl, int nsteps, R
 #pragma unroll
             for (int c = 0; c < 2 * N; c++) zp[k][c] = z[k][c] + d1[k][c];
             normalize_ket<R, N>(zp[k], __ldg(M.kappa + site));
-            publish<R, N, BQ>(sc, S.qm, zp[k], ns, site, P, QP);
+            publish<R, N, BQ>(sc, S.qm, zp[k], ns, site, P, QP, M.has_general);
         }
         if (!sgb_grid_barrier(ctrl, gridDim.x)) return;
 #pragma unroll
@@ -381,7 +444,7 @@ k_sun_heun(Model<R> M, R* Z, R* D, R* Qb, R* P, R* QP, Ctrl* ctrl, int nsteps, R
 #pragma unroll
             for (int c = 0; c < 2 * N; c++) z[k][c] = z[k][c] + (d1[k][c] + d2[c]) / 2;
             normalize_ket<R, N>(z[k], __ldg(M.kappa + site));
-            publish<R, N, BQ>(sc, S.qm, z[k], ns, site, D, Qb);
+            publish<R, N, BQ>(sc, S.qm, z[k], ns, site, D, Qb, M.has_general);
         }
         if (step + 1 < nsteps) {
             if (!sgb_grid_barrier(ctrl, gridDim.x)) return;
@@ -444,7 +507,7 @@ k_sun_midpoint(Model<R> M, R* Z, R* D, R* Qb, R* H, R* QH, Ctrl* ctrl, int nstep
         R zb[2 * N];
 #pragma unroll
         for (int c = 0; c < 2 * N; c++) zb[c] = (z[k][c] + z[k][c]) / 2;
-        publish<R, N, BQ>(sc, S.qm, zb, ns, site, H, QH);
+        publish<R, N, BQ>(sc, S.qm, zb, ns, site, H, QH, M.has_general);
         if (snap.enabled) write_snapshot_sun<R, N>(M, snap, snap.t0, site, z[k]);
     }
     if (leader) { ctrl->acc[0] = 0.0; ctrl->acc[1] = 0.0; ctrl->acc[2] = 0.0; }
@@ -460,7 +523,7 @@ k_sun_midpoint(Model<R> M, R* Z, R* D, R* Qb, R* H, R* QH, Ctrl* ctrl, int nstep
         for (int it = 0; it < max_iters; ++it) {
             const int nxt = (cur + 1) % 3, nst = (cur + 2) % 3;
             const R* Hc = H + (size_t)cur * 3 * ns;
-            const R* Qc = QH + (size_t)cur * 5 * ns;
+            const R* Qc = QH + (size_t)cur * M.qrows * ns;
             R acc = 0;   // per-site terms in R, block and grid sums in FP64
 #pragma unroll
             for (int k = 0; k < SPT; k++) {
@@ -481,13 +544,13 @@ k_sun_midpoint(Model<R> M, R* Z, R* D, R* Qb, R* H, R* QH, Ctrl* ctrl, int nstep
                 }
 #pragma unroll
                 for (int c = 0; c < 2 * N; c++) zb[c] = (z[k][c] + zp[k][c]) / 2;
-                publish<R, N, BQ>(sc, S.qm, zb, ns, site, H + (size_t)nxt * 3 * ns, QH + (size_t)nxt * 5 * ns);
+                publish<R, N, BQ>(sc, S.qm, zb, ns, site, H + (size_t)nxt * 3 * ns, QH + (size_t)nxt * M.qrows * ns, M.has_general);
 #pragma unroll
                 for (int c = 0; c < 2 * N; c++) zc[k][c] = zp[k][c];
                 normalize_ket<R, N>(zc[k], kap);
 #pragma unroll
                 for (int c = 0; c < 2 * N; c++) zb[c] = (zc[k][c] + zc[k][c]) / 2;
-                publish<R, N, BQ>(sc, S.qm, zb, ns, site, H + (size_t)nst * 3 * ns, QH + (size_t)nst * 5 * ns);
+                publish<R, N, BQ>(sc, S.qm, zb, ns, site, H + (size_t)nst * 3 * ns, QH + (size_t)nst * M.qrows * ns, M.has_general);
             }
             double bsum = sgb_block_sum_r<R>(acc);
             const int slot = (int)(itg % 3);
@@ -526,7 +589,7 @@ k_sun_midpoint(Model<R> M, R* Z, R* D, R* Qb, R* H, R* QH, Ctrl* ctrl, int nstep
         if (site >= ns) continue;
 #pragma unroll
         for (int c = 0; c < 2 * N; c++) Z[(size_t)c * ns + site] = z[k][c];
-        publish<R, N, BQ>(sc, S.qm, z[k], ns, site, D, Qb);
+        publish<R, N, BQ>(sc, S.qm, z[k], ns, site, D, Qb, M.has_general);
     }
     if (leader) ctrl->steps_done = done;
 }
@@ -540,7 +603,7 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_sun_refresh(Model<R> M, const R* 
         R z[2 * N];
 #pragma unroll
         for (int c = 0; c < 2 * N; c++) z[c] = Z[(size_t)c * M.ns + site];
-        if (M.has_biquad) publish<R, N, true>(sc, S.qm, z, M.ns, site, D, Qb);
+        if (M.has_biquad) publish<R, N, true>(sc, S.qm, z, M.ns, site, D, Qb, M.has_general);
         else publish<R, N, false>(sc, S.qm, z, M.ns, site, D, Qb);
     }
 }
@@ -620,6 +683,23 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_sun_energy(Model<R> M, const R* Z
                         for (int p = 0; p < 5; p++) acc += qi[q] * (double)Bm[q + 5 * p] * qj[p];
                 }
                 E += acc;
+            }
+            if (B.gcnt > 0) {
+                // general couplings (Interactions.jl:495-503): Σ_k <A_k>_i <B_k>_j
+                double zj[2 * N], ri[N * N], rj[N * N];
+#pragma unroll
+                for (int c = 0; c < 2 * N; c++) zj[c] = Z[(size_t)c * ns + js];
+                sun_rho<double, N>(z, ri);
+                sun_rho<double, N>(zj, rj);
+                for (int t = 0; t < B.gcnt; t++) {
+                    const R* row = M.gtab + (size_t)(B.gidx + t) * 4 * N * N;
+                    double Ab = 0, Bb = 0;
+                    for (int k = 0; k < N * N; k++) {
+                        Ab += (double)row[k] * ri[k];
+                        Bb += (double)row[3 * N * N + k] * rj[k];
+                    }
+                    E += Ab * Bb;
+                }
             }
         };
         if (M.ioff) {
@@ -1072,6 +1152,28 @@ __device__ inline R sun_local_dE(const Model<R>& M, const SunTab<R, N>& S, int s
             }
         }
     }
+    if (BQ && M.has_general) {
+        // general couplings: Δ<A>_site <B>_j over the rows of the site's sublattice (reversed
+        // copies carry the swapped pair)
+        R r0[N * N], rn[N * N];
+        sun_rho<R, N>(z0, r0);
+        sun_rho<R, N>(zn, rn);
+        for (int b = b0; b < b1; b++) {
+            const DBond<R>& B = S.t.bonds[b];
+            if (B.gcnt == 0) continue;
+            const int j = __ldg(M.nbr + (size_t)(b - b0) * ns + site);
+            for (int t = 0; t < B.gcnt; t++) {
+                const R* row = M.gtab + (size_t)(B.gidx + t) * 4 * N * N;
+                R dA = 0, Bb = 0;
+#pragma unroll
+                for (int k = 0; k < N * N; k++) {
+                    dA += __ldg(row + k) * (rn[k] - r0[k]);
+                    Bb += __ldg(row + 3 * N * N + k) * sgb_ld(Qb + (size_t)(5 + k) * ns + j);
+                }
+                dE += dA * Bb;
+            }
+        }
+    }
     return dE;
 }
 
@@ -1161,6 +1263,12 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_sun_local_sweeps(Model<R> M, R* Z
                     if (BQ) {
 #pragma unroll
                         for (int q = 0; q < 5; q++) Qb[(size_t)q * ns + site] = qn[q];
+                        if (M.has_general) {
+                            R p[N * N];
+                            sun_rho<R, N>(zn, p);
+#pragma unroll
+                            for (int q = 0; q < N * N; q++) Qb[(size_t)(5 + q) * ns + site] = p[q];
+                        }
                     }
                     aE += e;
                     ax += (double)sn[0] - (double)s0[0];

@@ -63,16 +63,56 @@ inline void stevens_quadrupoles(int N, std::vector<std::complex<double>>& out) {
 
 // Packs the tables. `dims` reduces bond offsets mod L (single systems); nullptr keeps the
 // raw offsets (replica batches of different sizes). Returns "" or an error message.
+// Coefficients a(M) with <Z|M|Z> = a(M)·ρ for the packed density ρ of a ket (Re M_rr; then
+// 2 Re M_rc, -2 Im M_rc for r < c). M: N x N complex, column-major (re, im).
+template <class R>
+inline void density_coeffs(int N, const double* Mx, R* out) {
+    for (int r = 0; r < N; r++) out[r] = (R)Mx[2 * (r + N * r)];
+    int k = N;
+    for (int r = 0; r < N; r++)
+        for (int c = r + 1; c < N; c++) {
+            out[k++] = (R)(2 * Mx[2 * (r + N * c)]);
+            out[k++] = (R)(-2 * Mx[2 * (r + N * c) + 1]);
+        }
+}
+
+// SU(N) general pair couplings: term t (A[t] ⊗ B[t]) on input bond gbond[t].
+struct GeneralTerms {
+    std::vector<int> bond;
+    std::vector<double> A, B;   // [nterms][N][N] complex column-major (re, im)
+};
+
 template <class R>
 std::string pack_tables(int na, int N, bool sun, const int* dims, const std::vector<sgb_bond>& bonds_in,
                         const std::vector<double>& onsite, Model<R>& M, std::vector<unsigned char>& buf,
-                        bool& any_bq) {
+                        bool& any_bq, const GeneralTerms* gen = nullptr, std::vector<R>* grows = nullptr) {
     std::vector<std::vector<DBond<R>>> per(na);
     std::vector<R> bqtab;
     any_bq = false;
-    for (const sgb_bond& b : bonds_in) {
+    if (grows) grows->clear();
+    const int NN = N * N;
+    for (size_t bi = 0; bi < bonds_in.size(); bi++) {
+        const sgb_bond& b = bonds_in[bi];
         for (int dir = 0; dir < 2; dir++) {
             DBond<R> e{};
+            if (gen && grows) {
+                // rows (a(first), first, a(second)): the site's own operator first; the
+                // reversed copy swaps A and B (reverse(tensordec))
+                e.gidx = (int)(grows->size() / (4 * NN));
+                for (size_t t = 0; t < gen->bond.size(); t++) {
+                    if (gen->bond[t] != (int)bi) continue;
+                    const double* A = gen->A.data() + 2 * NN * t;
+                    const double* Bm = gen->B.data() + 2 * NN * t;
+                    const double* first = dir == 0 ? A : Bm;
+                    const double* second = dir == 0 ? Bm : A;
+                    std::vector<R> row(4 * NN);
+                    density_coeffs<R>(N, first, row.data());
+                    for (int k = 0; k < 2 * NN; k++) row[NN + k] = (R)first[k];
+                    density_coeffs<R>(N, second, row.data() + 3 * NN);
+                    grows->insert(grows->end(), row.begin(), row.end());
+                    e.gcnt++;
+                }
+            }
             int from = dir == 0 ? b.i : b.j;
             int to = dir == 0 ? b.j : b.i;
             e.j = to;
@@ -168,6 +208,8 @@ std::string pack_tables(int na, int N, bool sun, const int* dims, const std::vec
     for (auto& v : per)
         for (auto& e : v)
             if (e.jkind != 0 || e.bqkind != 0) M.general = 1;
+    M.has_general = (grows && !grows->empty()) ? 1 : 0;
+    M.qrows = sun ? 5 + N * N : 5;
     M.tables_bytes = (int)bytes;
     M.nb = nb;
     M.nbq = nbq;

@@ -126,3 +126,49 @@ def ket_from_dipole(d: np.ndarray, N: int) -> np.ndarray:
     H = d[0] * S[0] + d[1] * S[1] + d[2] * S[2]
     w, v = np.linalg.eigh(H)
     return v[:, np.argmax(w)]
+
+
+def hermitian_basis(N: int) -> np.ndarray:
+    """An orthonormal basis of the N x N Hermitian matrices under Tr(X^† Y): the identity
+    over √N, then the generalized Gell-Mann matrices (symmetric, antisymmetric and diagonal
+    generators), shape (N², N, N)."""
+    out = [np.eye(N, dtype=complex) / np.sqrt(N)]
+    for r in range(N):
+        for c in range(r + 1, N):
+            E = np.zeros((N, N), dtype=complex)
+            E[r, c] = E[c, r] = 1 / np.sqrt(2)
+            out.append(E)
+            E = np.zeros((N, N), dtype=complex)
+            E[r, c] = -1j / np.sqrt(2)
+            E[c, r] = 1j / np.sqrt(2)
+            out.append(E)
+    for k in range(1, N):
+        d = np.zeros(N)
+        d[:k] = 1.0
+        d[k] = -k
+        out.append(np.diag(d / np.sqrt(k * (k + 1))).astype(complex))
+    return np.array(out)
+
+
+def tensor_decomposition(op, N1: int, N2: int, tol: float = 1e-12):
+    """Σ_k A_k ⊗ B_k with Hermitian A_k (N1 x N1) and B_k (N2 x N2) equal to the Hermitian
+    operator `op` on C^N1 ⊗ C^N2 (the form of Sunny's TensorDecomposition, Types.jl:23-30).
+    Its coefficients in products of orthonormal Hermitian bases form a real matrix whose
+    singular value decomposition gives the pairs (an operator Schmidt decomposition)."""
+    op = np.asarray(op, dtype=complex)
+    if op.shape != (N1 * N2, N1 * N2):
+        raise ValueError("Invalid matrix size.")
+    if not np.allclose(op, op.conj().T):
+        raise ValueError("Operator is not Hermitian")
+    T1, T2 = hermitian_basis(N1), hermitian_basis(N2)
+    coef = np.array([[np.trace(np.kron(a, b) @ op).real for b in T2] for a in T1])
+    U, sv, Vt = np.linalg.svd(coef)
+    pairs = []
+    for k in range(len(sv)):
+        if sv[k] <= tol * max(sv[0], 1e-300):
+            continue
+        w = np.sqrt(sv[k])
+        A = w * np.tensordot(U[:, k], T1, axes=1)
+        B = w * np.tensordot(Vt[k], T2, axes=1)
+        pairs.append(((A + A.conj().T) / 2, (B + B.conj().T) / 2))
+    return pairs

@@ -22,6 +22,7 @@ import numpy as np
 from . import _abi
 from .crystal import Bond, Crystal
 from .operators import (rcs_factors, spin_matrices_of_dim, stevens_expansion_for_dipole, expected_spin,
+                        tensor_decomposition,
                         ket_from_dipole)
 
 _MODES = {"dipole": _abi.MODE_DIPOLE, "dipole_uncorrected": _abi.MODE_DIPOLE_UNCORRECTED, "SUN": _abi.MODE_SUN}
@@ -184,6 +185,8 @@ class System:
         # and its onsite coupling (None while the system is homogeneous)
         self._site_pairs: list | None = None
         self._site_onsite: list | None = None
+        # SU(N) general pair couplings: bond -> [(A, B), ...] (Types.jl:23-30)
+        self._general: dict[Bond, list] = {}
         self._base_dip = np.zeros((na, L3, L2, L1, 3))
         self._base_coh = np.zeros((na, L3, L2, L1, max(self.N, 1)), dtype=complex)
         self.rng = np.random.default_rng(seed)
@@ -349,6 +352,12 @@ class System:
         for k, b in enumerate(bonds):
             arr[k] = b
         _abi.check(lib.sgb_set_bonds(h, arr, len(bonds)), lib, h)
+        if self.N:
+            gb, A, B = self.general_table()
+            cm = lambda M: np.ascontiguousarray(np.stack([np.swapaxes(M, -1, -2).real, np.swapaxes(M, -1, -2).imag], -1)).reshape(-1)
+            ga, gbm = (cm(A), cm(B)) if len(gb) else (None, None)
+            _abi.check(lib.sgb_set_general(h, gb.ctypes.data_as(C.POINTER(C.c_int32)) if len(gb) else None, len(gb),
+                                           _abi.dptr(ga), _abi.dptr(gbm)), lib, h)
         self._couplings_dirty = False
 
     def _onsite_row(self, oc) -> np.ndarray:
@@ -378,6 +387,45 @@ class System:
         """Non-culled pair couplings in the C layout (0-based atoms, column-major J)."""
         return [self._bond_c(b, pc) for b, pc in self._pairs.items()]
 
+    def general_table(self):
+        """SU(N) general pair couplings: (bond index into bond_table(), A [n][N][N], B [n][N][N])."""
+        idx = {b: k for k, b in enumerate(self._pairs)}
+        gb, A, B = [], [], []
+        for b, terms in self._general.items():
+            for a_, b_ in terms:
+                gb.append(idx[b])
+                A.append(a_)
+                B.append(b_)
+        N = max(self.N, 1)
+        return (np.array(gb, dtype=np.int32), np.array(A, dtype=complex).reshape(-1, N, N),
+                np.array(B, dtype=complex).reshape(-1, N, N))
+
+    def set_pair_coupling_op(self, op, bond: Bond):
+        """set_pair_coupling!(sys, op, bond) in SU(N) mode on this one bond (and its
+        reverse; no symmetry propagation): `op` is a Hermitian operator on the product
+        space of the two sites (N² x N²), or a function of the two sites' spin matrices in
+        that space as in Sunny ((Si, Sj) -> op). Stored as the general tensor
+        decomposition Σ_k A_k ⊗ B_k of the whole operator (PairExchange.jl:185-244 keeps
+        scalar, bilinear and biquadratic parts apart; the sum is the same operator)."""
+        from .crystal import bond_parity
+        if self.mode != "SUN":
+            raise ValueError("General couplings require mode :SUN")
+        if bond.i == bond.j and all(x == 0 for x in bond.n):
+            raise ValueError("Bond must connect different atoms.")
+        N = self.N
+        if callable(op):
+            I = np.eye(N)
+            Sm = spin_matrices_of_dim(N)
+            op = op([np.kron(S, I) for S in Sm], [np.kron(I, S) for S in Sm])
+        terms = tensor_decomposition(op, N, N)
+        if not bond_parity(bond):
+            bond = bond.reverse()
+            terms = [(b_, a_) for a_, b_ in terms]
+        if bond not in self._pairs:
+            self._pairs[bond] = PairCoupling(0.0, np.zeros((3, 3)), 0.0)
+        self._general[bond] = terms
+        self._couplings_dirty = True
+
     # ---- inhomogeneous systems (Interactions.jl:81-100, 237-257; PairExchange.jl:431-605) ----
     def is_homogeneous(self) -> bool:
         return self._site_pairs is None
@@ -401,6 +449,8 @@ class System:
 
     def _make_inhomogeneous(self):
         from .crystal import bond_parity
+        if self._general:
+            raise ValueError("general (tensor-decomposed) pair couplings are supported on homogeneous systems only")
         per_atom = [[] for _ in range(self.natoms)]
         for b, pc in self._pairs.items():
             per_atom[b.i - 1].append([b, pc, not bond_parity(b)])
@@ -862,6 +912,7 @@ def clone_system(sys: System, seed=None) -> System:
                                 pc.biquad.copy() if isinstance(pc.biquad, np.ndarray) else pc.biquad)
                 for b, pc in sys._pairs.items()}
     c._onsite = [None if o is None else np.array(o) for o in sys._onsite]
+    c._general = {b: [(np.array(a_), np.array(b_)) for a_, b_ in t] for b, t in sys._general.items()}
     if sys._site_pairs is not None:
         c._site_pairs = [[[e[0], PairCoupling(e[1].scalar, np.array(e[1].bilin, dtype=float),
                                               e[1].biquad.copy() if isinstance(e[1].biquad, np.ndarray) else e[1].biquad),
