@@ -255,24 +255,26 @@ def compare_correlations(sc_a: SampledCorrelations, sc_b: SampledCorrelations) -
     Per bin, Δ = mean_a − mean_b and s = M_a/(n_a(n_a−1)) + M_b/(n_b(n_b−1)) (the variance
     of Δ if both estimate one S(q,ω), from Welford's M as in CorrelationSampling.jl:117-134).
     Returns
-      chi2_ratio       Σ|Δ|² / Σs: 1 when the difference is statistical noise;
-      frac_z_gt_3      fraction of bins with |Δ| > 3√s (e^-9 = 1.2e-4 for complex Gaussian noise);
-      noise_rel        √(Σs / Σ|mean_b|²): the relative size of the statistical error bars;
-      bias_rel         √(max(0, Σ|Δ|² − Σs) / Σ|mean_b|²): the RMS per-bin difference
-                       beyond the error bars, relative to the RMS bin;
-      bias_rel_bound   the same with Σ|Δ|² − Σs raised by two standard errors (estimated from
-                       the spread over 1024 interleaved bin sets): an upper bound at ~97.5 %.
+      chi2_ratio     Σ|Δ|² / Σs: about 1 when independent samples differ by noise alone,
+                     below 1 when the two accumulators hold samples from the same starts;
+      frac_z_gt_3    fraction of bins with |Δ| > 3√s (e^-9 = 1.2e-4 for complex Gaussian noise
+                     of independent samples);
+      noise_rel      √(Σs / Σ|mean_b|²): the relative size of the statistical error bars;
+      rel_rms_diff   √(Σ|Δ|² / Σ|mean_b|²): the RMS per-bin difference relative to the RMS bin.
+                     E|Δ|² is the squared systematic difference plus noise, so this bounds the
+                     systematic per-bin difference from above;
+      bias_rel       √(max(0, Σ|Δ|² − Σs) / Σ|mean_b|²): the difference beyond the error bars
+                     (meaningful for independent samples);
+      rms_ratio      √(Σ|mean_a|² / Σ|mean_b|²).
     """
     out = np.zeros(9)
     sc_a._check(sc_a._lib.sgb_corr_compare(sc_a._h, sc_b._h, _abi.dptr(out)))
     d2, s, s2, mb2, ma2, nz3, npos, nbins, varB = out
-    excess = d2 - s
-    bound = max(0.0, excess) + 2.0 * math.sqrt(max(varB, 0.0))
     return {"chi2_ratio": d2 / s if s > 0 else math.nan,
             "frac_z_gt_3": nz3 / max(npos, 1.0),
             "noise_rel": math.sqrt(s / mb2) if mb2 > 0 else math.nan,
-            "bias_rel": math.sqrt(max(0.0, excess) / mb2) if mb2 > 0 else math.nan,
-            "bias_rel_bound": math.sqrt(bound / mb2) if mb2 > 0 else math.nan,
+            "rel_rms_diff": math.sqrt(d2 / mb2) if mb2 > 0 else math.nan,
+            "bias_rel": math.sqrt(max(0.0, d2 - s) / mb2) if mb2 > 0 else math.nan,
             "rms_ratio": math.sqrt(ma2 / mb2) if mb2 > 0 else math.nan,
             "bins": int(nbins), "samples": (sc_a.nsamples, sc_b.nsamples)}
 

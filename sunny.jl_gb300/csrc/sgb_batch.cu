@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) 
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(A.M, smem);
     IT* sidx = reinterpret_cast<IT*>(smem + A.M.tables_bytes);   // [tile][bond][SGB_TILE]
-    __shared__ double wpart[SGB_MAXT][SGB_TILE / 32];   // per-warp convergence partials of each tile
+    __shared__ R wpart[SGB_MAXT][SGB_TILE / 32];   // per-warp convergence partials of each tile
     __shared__ unsigned long long conv_mask;   // bit q: replica q met the tolerance this iteration
     __shared__ int4 st_a[SGB_MAXT];            // (replica, first site, count, replica offset)
     __shared__ int2 st_b[SGB_MAXT];            // (replica sites, neighbour-table offset)
@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) 
             for (int k = 0; k < ntb; k++) {
                 const int4 ti = st_a[k];
                 const bool on = (actm >> k) & 1u;
-                double acc = 0;   // per-site terms in R; the warp, tile and grid sums in FP64
+                R acc = 0;   // per-site terms in R; the warp sums in R, tile and grid sums in FP64
                 if (tid < ti.z) {
                     const int s = ti.y + tid, g = ti.w + s;
                     if (on) {
@@ -442,8 +442,7 @@ __global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) 
                     }
                 }
                 if (on) {
-                    // warp sum kept per warp (no shared-memory FP64 atomics); summing in FP64
-                    // makes the convergence decisions independent of how sites map to warps
+                    // warp sum in R, kept per warp (no shared-memory FP64 atomics)
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
                     if ((tid & 31) == 0) wpart[k][tid >> 5] = acc;
@@ -455,7 +454,7 @@ __global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) 
             if (tid < ntb && ((actm >> tid) & 1u)) {
                 double t = 0;
 #pragma unroll
-                for (int w = 0; w < SGB_TILE / 32; w++) t += wpart[tid][w];
+                for (int w = 0; w < SGB_TILE / 32; w++) t += (double)wpart[tid][w];
                 atomicAdd(&X.racc[slot * X.nrep + st_a[tid].x], t);
             }
             if (leader) {
@@ -823,21 +822,42 @@ static void blk_shapes(sgb_batch* b, bool gen, std::vector<MidShape>& out) {
                 if (smem > 200 * 1024) continue;
                 cands.push_back({(double)g.HX * g.HY * g.HZ / (double)((1 << lx) * (1 << ly) * (1 << lz)), lx, ly, lz});
             }
-    std::sort(cands.begin(), cands.end(), [](const Cand& p, const Cand& q) { return p.cost < q.cost; });
-    int kept = 0;
+    // rank: fewest blocks per CTA (rounds of the block loop), then most CTAs per SM (warps
+    // to hide latency), then least halo per site
+    struct Fit {
+        Cand c;
+        int bps, rounds;
+        size_t smem;
+    };
+    std::vector<Fit> fits;
     for (const Cand& c : cands) {
-        if (kept >= 4) break;
         BlkGeom g = blk_geom(b, c.lbx, c.lby, c.lbz);
         const size_t smem = 128 + g.halo_bytes + (size_t)b->tables_bytes + 4 * (size_t)((b->fp32 ? b->mf.nb : b->md.nb) + 4);
+        int bps = 0;
+        if (blk_occupancy(gen, 6, smem, &bps) != SGB_OK || bps < 1) {
+            cudaGetLastError();
+            continue;
+        }
+        const long long grid = std::min<long long>((long long)bps * b->nsm, g.nblk);
+        const int rounds = (int)((g.nblk + grid - 1) / grid);
+        if (rounds > SGB_BLK_MAXB) continue;
+        fits.push_back({c, bps, rounds, smem});
+    }
+    std::sort(fits.begin(), fits.end(), [](const Fit& p, const Fit& q) {
+        if (p.rounds != q.rounds) return p.rounds < q.rounds;
+        if (p.bps != q.bps) return p.bps > q.bps;
+        return p.c.cost < q.c.cost;
+    });
+    int kept = 0;
+    for (const Fit& f : fits) {
+        if (kept >= 4) break;
+        const Cand& c = f.c;
+        BlkGeom g = blk_geom(b, c.lbx, c.lby, c.lbz);
+        const size_t smem = f.smem;
         bool any = false;
-        for (int G : {6, 12}) {
-            int bps = 0;
-            if (blk_occupancy(gen, G, smem, &bps) != SGB_OK || bps < 1) {
-                cudaGetLastError();
-                continue;
-            }
+        for (int G : {6}) {
+            const int bps = f.bps;
             const long long grid = std::min<long long>((long long)bps * b->nsm, g.nblk);
-            if ((g.nblk + grid - 1) / grid > SGB_BLK_MAXB) continue;
             if (!any) {
                 BlkMaps m;
                 bool ok = true;

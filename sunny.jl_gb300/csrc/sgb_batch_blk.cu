@@ -11,10 +11,11 @@
 // cells, written together with the cells). Each fixed-point iteration, one thread moves
 // the block and its gw-cell halo, all atoms, into shared memory with a single 5-D TMA box
 // load (cp.async.bulk.tensor, completion on an mbarrier); the neighbour reads are then
-// shared-memory loads at a constant offset per bond. The iteration's arithmetic, the
-// convergence test (FP64 sums per replica), the extrapolated first iterate, the
-// speculative next-step midpoint spins and the snapshots are those of the tile kernel,
-// so both kernels produce the same trajectory.
+// shared-memory loads at a constant offset per bond. The per-site arithmetic, the
+// convergence test (per-replica sums, FP64 across warps), the extrapolated first iterate,
+// the speculative next-step midpoint spins and the snapshots are those of the tile
+// kernel; the two differ only in rounding (the order of the convergence sums and the
+// compiler's fused multiply-adds), so their trajectories agree within the tolerance.
 #include <cuda.h>
 #include "sgb_batch.cuh"
 #include "sgb_batch_blk.h"
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(SGB_BLK_THREADS) k_batch_midpoint_blk(BatchArg
     __shared__ float s_kap[SGB_MAX_SUBLAT];
     __shared__ float s_h[3 * SGB_MAX_SUBLAT];
     __shared__ int4 s_blk[SGB_BLK_MAXB];          // (replica, x0, y0, z0) of each block of this CTA
-    __shared__ double wsum[SGB_BLK_THREADS / 32];
+    __shared__ float wsum[SGB_BLK_THREADS / 32];
     __shared__ unsigned long long conv_mask;
     const int tid = threadIdx.x;
     const int na = A.M.na, NS = A.NS;
@@ -218,7 +219,7 @@ __global__ void __launch_bounds__(SGB_BLK_THREADS) k_batch_midpoint_blk(BatchArg
                         return;
                     }
                 }
-                double acc = 0;   // per-site terms in FP32; the warp, block and grid sums in FP64
+                float acc = 0.f;   // per-thread and warp sums in FP32; block and grid sums in FP64
                 for (int i = tid; i < nsb; i += blockDim.x) {
                     const BlkSite c = site_of(i);
                     const int cx = bk.y + c.x, cy = bk.z + c.y, cz = bk.w + c.z;
@@ -248,7 +249,7 @@ __global__ void __launch_bounds__(SGB_BLK_THREADS) k_batch_midpoint_blk(BatchArg
                     rhs_dipole<float>(hx, hy, hz, 0.f, 0.f, 0.f, gx, gy, gz, dt, lam, dx, dy, dz);
                     const float nx = sx + dx, ny = sy + dy, nz = sz + dz;
                     const float ex = qx - nx, ey = qy - ny, ez = qz - nz;
-                    acc += (double)(ex * ex + ey * ey + ez * ez);
+                    acc += ex * ex + ey * ey + ez * ez;
                     MV<float>::st(X.Sp, NS, g, nx, ny, nz);
                     float mxv = (sx + nx) / 2, myv = (sy + ny) / 2, mzv = (sz + nz) / 2;
                     normalize_dip<float>(mxv, myv, mzv, kap);
@@ -293,7 +294,7 @@ __global__ void __launch_bounds__(SGB_BLK_THREADS) k_batch_midpoint_blk(BatchArg
                 __syncthreads();   // halo reads and warp partials done before the next block's copy
                 if (on && tid == 0) {
                     double t = 0;
-                    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += wsum[w];
+                    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += (double)wsum[w];
                     atomicAdd(&X.racc[slot * X.nrep + bk.x], t);
                 }
             }
