@@ -38,7 +38,7 @@ class OrSys(C.Structure):
                 ("onsite", C.POINTER(C.c_double)), ("bonds", C.POINTER(BondC)), ("nbonds", C.c_int),
                 ("onsite_site", C.POINTER(C.c_double)), ("site_bonds", C.POINTER(SiteBondC)),
                 ("nsite_bonds", C.c_int64), ("gen_bond", C.POINTER(C.c_int)), ("gen_A", C.POINTER(C.c_double)),
-                ("gen_B", C.POINTER(C.c_double)), ("ngen", C.c_int)]
+                ("gen_B", C.POINTER(C.c_double)), ("ngen", C.c_int), ("ewA", C.POINTER(C.c_double))]
 
 
 _D = C.POINTER(C.c_double)
@@ -134,6 +134,15 @@ class OracleSystem:
             s.gen_B = _p(self._gen[2])
             s.ngen = len(gb)
         self.s = s
+
+    def set_ewald(self, A):
+        """Include the dipole-dipole term in local energy changes: A[cell, i, j] (3x3) from
+        ewald_matrices (or None to drop it)."""
+        if A is None:
+            self.s.ewA = None
+            return
+        self._ewA = np.ascontiguousarray(np.asarray(A, dtype=float).transpose(0, 1, 2, 4, 3)).reshape(-1)
+        self.s.ewA = _p(self._ewA)
 
     @classmethod
     def from_system(cls, sys):

@@ -637,6 +637,35 @@ double or_energy(const or_sys* s, const double* S, const double* Z) {
     return E;
 }
 
+/* ---- ewald_energy_delta (Ewald.jl:210-241): ΔS·∇E(site) + ½ Δμ·A[0,i,i]·Δμ, with
+ * ∇E(site) = Σ_j g_siteᵀ A[cell_j - cell_site, i, j] g_j S_j over every site j ---------- */
+static double ewald_delta(const or_sys* s, const double* S, int64_t site, const double* dS) {
+    const int L1 = s->L[0], L2 = s->L[1], L3 = s->L[2], na = s->na;
+    const int64_t ncell = (int64_t)L1 * L2 * L3, ns = or_nsites(s);
+    const int ai = (int)(site / ncell);
+    const int64_t ci = site % ncell;
+    const int x1 = (int)(ci % L1), y1 = (int)((ci / L1) % L2), z1 = (int)(ci / ((int64_t)L1 * L2));
+    const double* gi = s->g + 9 * site;
+    double f[3] = {0, 0, 0};
+    for (int64_t j = 0; j < ns; j++) {
+        const int aj = (int)(j / ncell);
+        const int64_t cj = j % ncell;
+        const int x2 = (int)(cj % L1), y2 = (int)((cj / L1) % L2), z2 = (int)(cj / ((int64_t)L1 * L2));
+        const int64_t off = wrap(x2 - x1, L1) + (int64_t)L1 * (wrap(y2 - y1, L2) + (int64_t)L2 * wrap(z2 - z1, L3));
+        const double* A = s->ewA + ((off * na + ai) * na + aj) * 9;
+        const double* gj = s->g + 9 * j;
+        double mu[3], Am[3];
+        for (int r = 0; r < 3; r++) mu[r] = gj[r] * S[3 * j] + gj[r + 3] * S[3 * j + 1] + gj[r + 6] * S[3 * j + 2];
+        for (int r = 0; r < 3; r++) Am[r] = A[r] * mu[0] + A[r + 3] * mu[1] + A[r + 6] * mu[2];
+        for (int r = 0; r < 3; r++) f[r] += gi[3 * r] * Am[0] + gi[3 * r + 1] * Am[1] + gi[3 * r + 2] * Am[2];
+    }
+    double dmu[3], Ad[3];
+    for (int r = 0; r < 3; r++) dmu[r] = -(gi[r] * dS[0] + gi[r + 3] * dS[1] + gi[r + 6] * dS[2]);
+    const double* A0 = s->ewA + ((int64_t)ai * na + ai) * 9;
+    for (int r = 0; r < 3; r++) Ad[r] = A0[r] * dmu[0] + A0[r + 3] * dmu[1] + A0[r + 6] * dmu[2];
+    return dS[0] * f[0] + dS[1] * f[1] + dS[2] * f[2] + 0.5 * (dmu[0] * Ad[0] + dmu[1] * Ad[1] + dmu[2] * Ad[2]);
+}
+
 /* ---- local_energy_change (Interactions.jl:311-373), dipole modes ------------------ */
 static double biquad_pair(const sgb_bond* pc, const double* Qa, const double* Qb) {
     /* Qa' B Qb (kind 2) or biquad * sum_q Qa_q metric_q Qb_q (kind 1) */
@@ -650,7 +679,18 @@ static double biquad_pair(const sgb_bond* pc, const double* Qa, const double* Qb
     return acc;
 }
 
+static double local_energy_change_pairs(const or_sys* s, const double* S, int64_t site, const double* Snew);
+
 double or_local_energy_change(const or_sys* s, const double* S, int64_t site, const double* Snew) {
+    double dE = local_energy_change_pairs(s, S, site, Snew);
+    if (s->ewA && !isnan(dE)) {
+        const double dS[3] = {Snew[0] - S[3 * site], Snew[1] - S[3 * site + 1], Snew[2] - S[3 * site + 2]};
+        dE += ewald_delta(s, S, site, dS);
+    }
+    return dE;
+}
+
+static double local_energy_change_pairs(const or_sys* s, const double* S, int64_t site, const double* Snew) {
     int L1 = s->L[0], L2 = s->L[1], L3 = s->L[2];
     int64_t ncell = (int64_t)L1 * L2 * L3;
     int a = (int)(site / ncell);
@@ -724,7 +764,20 @@ static double onsite_e(int N, const double* lam, const cplx* z) {
     return creal(acc);
 }
 
+static double local_energy_change_sun_pairs(const or_sys* s, const double* S, const double* Z, int64_t site, const double* Znew);
+
 double or_local_energy_change_sun(const or_sys* s, const double* S, const double* Z, int64_t site, const double* Znew) {
+    double dE = local_energy_change_sun_pairs(s, S, Z, site, Znew);
+    if (s->ewA && !isnan(dE)) {
+        double sn[3];
+        or_expected_spin(s->N, Znew, sn);
+        const double dS[3] = {sn[0] - S[3 * site], sn[1] - S[3 * site + 1], sn[2] - S[3 * site + 2]};
+        dE += ewald_delta(s, S, site, dS);
+    }
+    return dE;
+}
+
+static double local_energy_change_sun_pairs(const or_sys* s, const double* S, const double* Z, int64_t site, const double* Znew) {
     const int N = s->N, L1 = s->L[0], L2 = s->L[1], L3 = s->L[2];
     or_ops ops;
     build_ops(N, &ops);

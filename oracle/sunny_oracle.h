@@ -43,6 +43,9 @@ typedef struct {
     const double* gen_A;
     const double* gen_B;
     int ngen;
+    /* Dipole-dipole matrices A[cell][i][j] (3x3 column-major, or_ewald_matrices) for the
+     * Ewald term of local_energy_change (Ewald.jl:210-241), or NULL. */
+    const double* ewA;
 } or_sys;
 
 int64_t or_nsites(const or_sys* s);

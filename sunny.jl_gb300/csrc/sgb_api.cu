@@ -526,11 +526,28 @@ int do_refresh(sgb_system* s) {
     return rc ? cuda_fail(s, cudaGetLastError(), "refresh launch") : SGB_OK;
 }
 
+// <Z|S|Z> of a ket Z [N][2] (Spin.jl:72-87) with the spin-s matrices of N = 2s+1 levels
+void host_expected_spin(int N, const double* z, double* out) {
+    const double sp = (N - 1) / 2.0;
+    double cr = 0, ci = 0, zz = 0;
+    for (int j = 1; j <= N - 1; j++) {
+        const double off = std::sqrt(2 * (sp + 1) * j - (double)j * (j + 1)) / 2;
+        const double ar = z[2 * (j - 1)], ai = z[2 * (j - 1) + 1], br = off * z[2 * j], bi = off * z[2 * j + 1];
+        cr += ar * br + ai * bi;
+        ci += ar * bi - ai * br;
+    }
+    for (int k = 0; k < N; k++) zz += (sp - k) * (z[2 * k] * z[2 * k] + z[2 * k + 1] * z[2 * k + 1]);
+    out[0] = 2 * cr;
+    out[1] = 2 * ci;
+    out[2] = zz;
+}
+
 void ewald_free(sgb_system* s) {
     EwaldDev& E = s->ew;
     void* p;
     p = E.g; dfree(p); p = E.mu; dfree(p); p = E.phi; dfree(p);
     p = E.FA; dfree(p); p = E.Fmu; dfree(p); p = E.Fphi; dfree(p);
+    p = E.Areal; dfree(p);
     p = s->ew_part; dfree(p);
     if (E.have_f) cufftDestroy(E.plan_f);
     if (E.have_b) cufftDestroy(E.plan_b);
@@ -697,6 +714,141 @@ int run_midpoint_lr(sgb_system* s, double dt, double damping, double tol, int ma
     return SGB_OK;
 }
 
+// SU(N) mode with dipole-dipole interactions: HZ at kets Zs (set_energy_grad_coherents!,
+// Interactions.jl:596-669) = local terms at the expected dipoles and quadrupoles of Zs plus
+// the dipole-dipole field through dE/dS. The handle's dipoles and quadrupoles are
+// overwritten with those of Zs; the drivers refresh them from Z at the end.
+template <class R>
+int lr_sun_hz(sgb_system* s, const R* Zs, double* hz) {
+    const Model<R>& M = model<R>(s);
+    R* D = (R*)s->S;
+    R* Q = (R*)s->Q;
+    if (sun_launch_refresh<R>(M, Zs, D, Q, s->stream) || sun_launch_grad<R>(M, Zs, D, Q, hz, s->stream))
+        return cuda_fail(s, cudaGetLastError(), "gradient launch");
+    s->launches += 2;
+    double* f;
+    int rc = ensure_lr_grad(s, &f);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(f, 0, sizeof(double) * 3 * (size_t)s->ns, s->stream));
+    if ((rc = ewald_add<R>(s, D, f, nullptr))) return rc;
+    if (sun_launch_add_dipole_field<R>(M, Zs, f, hz, s->stream)) return cuda_fail(s, cudaGetLastError(), "dipole field launch");
+    s->launches++;
+    return SGB_OK;
+}
+
+// scratch of the SU(N) per-stage path: kets ZP, D1, XI ([2N][ns] of R each), HZ ([ns][2N] FP64)
+template <class R>
+int ensure_lr_sun(sgb_system* s, R** zp, R** d1, R** xi, double** hz) {
+    const size_t nk = (size_t)2 * s->N * s->ns;
+    const size_t bytes = 3 * nk * sizeof(R) + nk * sizeof(double);
+    if (s->lr_sun_cap < bytes) {
+        void* p = s->lr_sun;
+        dfree(p);
+        s->lr_sun = nullptr;
+        s->lr_sun_cap = 0;
+        int rc = dmalloc(s, &s->lr_sun, bytes);
+        if (rc) return rc;
+        s->lr_sun_cap = bytes;
+    }
+    char* b = (char*)s->lr_sun;
+    *hz = (double*)b;
+    *zp = (R*)(b + nk * sizeof(double));
+    *d1 = *zp + nk;
+    *xi = *d1 + nk;
+    return SGB_OK;
+}
+
+// Langevin Heun for coherent states (Integrators.jl:90-108), one launch per stage
+template <class R>
+int run_langevin_lr_sun(sgb_system* s, double dt, double damping, double kT, uint64_t seed, uint64_t step0, int nsteps,
+                        const double* noise) {
+    R *ZP, *D1, *XI;
+    double* hz;
+    int rc = ensure_lr_sun<R>(s, &ZP, &D1, &XI, &hz);
+    if (rc) return rc;
+    const size_t nk = (size_t)2 * s->N * s->ns;
+    const double nscale = (damping == 0.0 || kT == 0.0) ? 0.0 : std::sqrt(2 * dt * damping * kT);
+    if (noise && (rc = ensure_dbuf(s, nk))) return rc;
+    const Model<R>& M = model<R>(s);
+    R* Z = (R*)s->Z;
+    for (int k = 0; k < nsteps; k++) {
+        const double* dn = nullptr;
+        if (noise) {
+            CK(cudaMemcpyAsync(s->dbuf, noise + nk * k, sizeof(double) * nk, cudaMemcpyHostToDevice, s->stream));
+            dn = s->dbuf;
+        }
+        if ((rc = lr_sun_hz<R>(s, Z, hz))) return rc;
+        if (sun_launch_lr_stage<R>(0, M, Z, ZP, D1, XI, hz, dt, damping, nscale, seed, step0 + k, dn, nullptr, nullptr, 0, s->stream))
+            return cuda_fail(s, cudaGetLastError(), "Langevin stage launch");
+        if ((rc = lr_sun_hz<R>(s, ZP, hz))) return rc;
+        if (sun_launch_lr_stage<R>(1, M, Z, ZP, D1, XI, hz, dt, damping, 0, 0, 0, nullptr, nullptr, nullptr, 0, s->stream))
+            return cuda_fail(s, cudaGetLastError(), "Langevin stage launch");
+        s->launches += 2;
+    }
+    if ((rc = do_refresh<R>(s))) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    return SGB_OK;
+}
+
+// Schrödinger midpoint (Integrators.jl:422-452), one launch per stage and iteration
+template <class R>
+int run_midpoint_lr_sun(sgb_system* s, double dt, double damping, double tol, int max_iters, int nsteps, int64_t* iters,
+                        const SnapArgs<R>* snap = nullptr) {
+    R *ZP, *ZB, *XI;
+    double* hz;
+    int rc = ensure_lr_sun<R>(s, &ZP, &ZB, &XI, &hz);
+    if (rc) return rc;
+    const size_t nk = (size_t)2 * s->N * s->ns;
+    const double atol = tol * std::sqrt((double)s->ns);
+    const Model<R>& M = model<R>(s);
+    R* Z = (R*)s->Z;
+    int64_t total = 0;
+    double hp[EWALD_PART_BLOCKS];
+    if (snap && snap->enabled) {
+        if (sun_launch_lr_stage<R>(5, M, Z, ZP, ZB, XI, hz, 0, 0, 0, 0, 0, nullptr, nullptr, snap, snap->t0, s->stream))
+            return cuda_fail(s, cudaGetLastError(), "snapshot launch");
+        s->launches++;
+    }
+    for (int k = 0; k < nsteps; k++) {
+        CK(cudaMemcpyAsync(ZP, Z, sizeof(R) * nk, cudaMemcpyDeviceToDevice, s->stream));   // Z' = Z
+        bool conv = false;
+        for (int it = 0; it < max_iters; it++) {
+            total++;
+            if (sun_launch_lr_stage<R>(2, M, Z, ZP, ZB, XI, hz, 0, 0, 0, 0, 0, nullptr, nullptr, nullptr, 0, s->stream))
+                return cuda_fail(s, cudaGetLastError(), "midpoint stage launch");
+            if ((rc = lr_sun_hz<R>(s, ZB, hz))) return rc;
+            if (sun_launch_lr_stage<R>(3, M, Z, ZP, ZB, XI, hz, dt, damping, 0, 0, 0, nullptr, s->partials, nullptr, 0, s->stream))
+                return cuda_fail(s, cudaGetLastError(), "midpoint stage launch");
+            s->launches += 2;
+            CK(cudaMemcpyAsync(hp, s->partials, sizeof(hp), cudaMemcpyDeviceToHost, s->stream));
+            CK(cudaStreamSynchronize(s->stream));
+            double acc = 0;
+            for (int b = 0; b < EWALD_PART_BLOCKS; b++) acc += hp[b];
+            if (acc <= atol * atol) {   // fast_isapprox (Integrators.jl:361-371)
+                if (sun_launch_lr_stage<R>(4, M, Z, ZP, ZB, XI, hz, 0, 0, 0, 0, 0, nullptr, nullptr, nullptr, 0, s->stream))
+                    return cuda_fail(s, cudaGetLastError(), "midpoint stage launch");
+                s->launches++;
+                conv = true;
+                break;
+            }
+        }
+        if (iters) *iters = total;
+        if (!conv) {
+            do_refresh<R>(s);
+            return fail(s, SGB_ERR_NOCONVERGE, "Schrödinger midpoint method failed to converge in " + std::to_string(max_iters) + " iterations.");
+        }
+        if (snap && snap->enabled && (k + 1) % snap->measperiod == 0) {
+            if (sun_launch_lr_stage<R>(5, M, Z, ZP, ZB, XI, hz, 0, 0, 0, 0, 0, nullptr, nullptr, snap, snap->t0 + (k + 1) / snap->measperiod,
+                                       s->stream))
+                return cuda_fail(s, cudaGetLastError(), "snapshot launch");
+            s->launches++;
+        }
+    }
+    if ((rc = do_refresh<R>(s))) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    return SGB_OK;
+}
+
 // Greedy colouring of the bond graph in site order (every bond is listed from both
 // ends, so a site's own list holds all its neighbours): class of a site = the smallest
 // class none of its already coloured neighbours has. Sites of one class share no
@@ -767,6 +919,15 @@ int run_local_sweeps(sgb_system* s, McArgs& A, const double* rnd_host, double* o
     }
     double acc[4] = {0, 0, 0, 0};
     const double frac = A.frac;
+    double* F = nullptr;
+    if (s->ewald_on) {
+        // dipole-dipole: one block proposes the sites in sweep order and keeps the field
+        // dE/dS of every site current after each accepted move (ewald_energy_delta,
+        // Ewald.jl:210-241, whose sum over all sites becomes a rank-one update of F)
+        if ((rc = ensure_lr_grad(s, &F))) return rc;
+        CK(cudaMemsetAsync(F, 0, sizeof(double) * 3 * (size_t)s->ns, s->stream));
+        if ((rc = ewald_add<R>(s, (const R*)s->S, F, nullptr))) return rc;
+    }
     for (int k0 = 0; k0 < total; k0 += chunk) {
         const int nk = std::min(chunk, total - k0);
         McArgs a = A;
@@ -779,11 +940,17 @@ int run_local_sweeps(sgb_system* s, McArgs& A, const double* rnd_host, double* o
             a.rnd = s->dbuf;
         }
         if ((rc = reset_ctrl(s))) return rc;
-        rc = s->sun ? sun_launch_local_sweeps<R>(model<R>(s), (R*)s->Z, (R*)s->S, (R*)s->Q, s->ctrl, a, grid, s->mc_part, s->stream)
-                    : mc_launch_sweeps<R>(model<R>(s), (R*)s->S, s->ctrl, a, grid, s->mc_part, s->stream);
+        int gused = grid;
+        if (F) {
+            rc = mc_launch_sweeps_ewald<R>(model<R>(s), (R*)s->S, a, s->ew, F, s->mc_part, s->stream);
+            gused = 1;
+        } else {
+            rc = s->sun ? sun_launch_local_sweeps<R>(model<R>(s), (R*)s->Z, (R*)s->S, (R*)s->Q, s->ctrl, a, grid, s->mc_part, s->stream)
+                        : mc_launch_sweeps<R>(model<R>(s), (R*)s->S, s->ctrl, a, grid, s->mc_part, s->stream);
+        }
         s->launches++;
         if (rc) return cuda_fail(s, cudaGetLastError(), "LocalSampler launch");
-        if ((rc = util_launch_reduce(s->mc_part, grid, 4, s->red, s->stream))) return cuda_fail(s, cudaGetLastError(), "reduce launch");
+        if ((rc = util_launch_reduce(s->mc_part, gused, 4, s->red, s->stream))) return cuda_fail(s, cudaGetLastError(), "reduce launch");
         s->launches++;
         double part[4];
         CK(cudaMemcpyAsync(part, s->red, sizeof(part), cudaMemcpyDeviceToHost, s->stream));
@@ -890,6 +1057,7 @@ void sgb_destroy(sgb_system* s) {
     dfree(s->gtab);
     ewald_free(s);
     p = s->lr_grad; dfree(p);
+    p = s->lr_sun; dfree(p);
     dfree(s->flush);
     if (s->stage) cudaFreeHost(s->stage);
     for (int i = 0; i < 8; i++) if (s->ev[i]) cudaEventDestroy(s->ev[i]);
@@ -1108,8 +1276,9 @@ int sgb_set_dipole_dipole(sgb_system* s, double mu0_muB2, const double* demag, c
         return rc;
     }
     s->ewald_on = true;
+    E.Areal = A;   // kept for the LocalSampler's pairwise energy updates; freed by ewald_free
     auto bail = [&](const char* what) {
-        void* p = A; dfree(p); p = pos_d; dfree(p);
+        void* p = pos_d; dfree(p);
         ewald_free(s);
         return fail(s, SGB_ERR_CUDA, what);
     };
@@ -1129,7 +1298,7 @@ int sgb_set_dipole_dipole(sgb_system* s, double mu0_muB2, const double* demag, c
     E.have_f = true;
     if (cufftPlanMany(&E.plan_b, 3, n, nullptr, 1, E.nm, nullptr, 1, ncell, CUFFT_Z2D, 3 * na) != CUFFT_SUCCESS) return bail("cuFFT plan failed");
     E.have_b = true;
-    void* p = A; dfree(p); p = pos_d; dfree(p);
+    void* p = pos_d; dfree(p);
     return SGB_OK;
 }
 
@@ -1290,7 +1459,9 @@ int sgb_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t s
     int rc = ensure_tables(s);
     if (rc) return rc;
     if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called before stepping");
-    if (s->ewald_on && s->sun) return fail(s, SGB_ERR_ARG, "SU(N) dynamics with dipole-dipole interactions is not supported on the GPU");
+    if (s->ewald_on && s->sun)
+        return s->fp32 ? run_langevin_lr_sun<float>(s, dt, damping, kT, seed, step0, nsteps, noise)
+                       : run_langevin_lr_sun<double>(s, dt, damping, kT, seed, step0, nsteps, noise);
     if (s->ewald_on)
         return s->fp32 ? run_langevin_lr<float>(s, dt, damping, kT, seed, step0, nsteps, noise)
                        : run_langevin_lr<double>(s, dt, damping, kT, seed, step0, nsteps, noise);
@@ -1323,7 +1494,9 @@ int sgb_midpoint(sgb_system* s, double dt, double damping, double tol, int32_t m
     int rc = ensure_tables(s);
     if (rc) return rc;
     if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called before stepping");
-    if (s->ewald_on && s->sun) return fail(s, SGB_ERR_ARG, "SU(N) dynamics with dipole-dipole interactions is not supported on the GPU");
+    if (s->ewald_on && s->sun)
+        return s->fp32 ? run_midpoint_lr_sun<float>(s, dt, damping, tol, max_iters, nsteps, iters_out)
+                       : run_midpoint_lr_sun<double>(s, dt, damping, tol, max_iters, nsteps, iters_out);
     if (s->ewald_on)
         return s->fp32 ? run_midpoint_lr<float>(s, dt, damping, tol, max_iters, nsteps, iters_out)
                        : run_midpoint_lr<double>(s, dt, damping, tol, max_iters, nsteps, iters_out);
@@ -1338,7 +1511,8 @@ int sgb_midpoint(sgb_system* s, double dt, double damping, double tol, int32_t m
 int sgb_local_sweeps(sgb_system* s, double kT, double nsweeps, const sgb_proposal* prop, uint64_t seed, uint64_t sweep0,
                      const double* rand, double* dE, double* dS3) {
     if (!s) return fail(s, SGB_ERR_ARG, "null handle");
-    if (s->ewald_on) return fail(s, SGB_ERR_ARG, "LocalSampler with dipole-dipole interactions is not supported on the GPU");
+    if (s->ewald_on && s->sun)
+        return fail(s, SGB_ERR_ARG, "LocalSampler with dipole-dipole interactions in SU(N) mode is not supported on the GPU");
     if (!(kT >= 0)) return fail(s, SGB_ERR_ARG, "Select nonnegative kT");
     if (!(nsweeps >= 0) || nsweeps > 1e9) return fail(s, SGB_ERR_ARG, "nsweeps must be nonnegative");
     if (!prop || prop->n < 1 || prop->n > 4) return fail(s, SGB_ERR_ARG, "a proposal mixture has 1 to 4 functions");
@@ -1591,12 +1765,11 @@ int sgb_local_colors(sgb_system* s, int32_t* ncolors, int32_t* color) {
 
 int sgb_local_energy_change(sgb_system* s, int64_t site, const double* S_new, double* dE) {
     if (!s || !S_new || !dE) return fail(s, SGB_ERR_ARG, "null argument");
-    if (s->ewald_on) return fail(s, SGB_ERR_ARG, "LocalSampler with dipole-dipole interactions is not supported on the GPU");
     if (site < 0 || site >= s->ns) return fail(s, SGB_ERR_ARG, "site out of range");
     int rc = ensure_colors(s);   // also rejects self-interaction
     if (rc) return rc;
     if (!s->state_set) return fail(s, SGB_ERR_STATE, "sgb_set_state must be called first");
-    if ((rc = ensure_dbuf(s, 1))) return rc;
+    if ((rc = ensure_dbuf(s, 4))) return rc;
     if (s->sun) {
         SunKet zk{};
         for (int q = 0; q < 2 * s->N; q++) zk.v[q] = S_new[q];
@@ -1608,8 +1781,35 @@ int sgb_local_energy_change(sgb_system* s, int64_t site, const double* S_new, do
     }
     s->launches++;
     if (rc) return cuda_fail(s, cudaGetLastError(), "local energy launch");
-    CK(cudaMemcpyAsync(dE, s->dbuf, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    double out[2] = {0, 0};
+    if (s->ewald_on) {
+        // ewald_energy_delta (Ewald.jl:210-241) at the old dipoles, with ΔS the change of
+        // the (expected) dipole
+        double snew[3], sold[3];
+        if (s->sun) host_expected_spin(s->N, S_new, snew);
+        else for (int c = 0; c < 3; c++) snew[c] = S_new[c];
+        for (int c = 0; c < 3; c++) {
+            if (s->fp32) {
+                float v;
+                CK(cudaMemcpyAsync(&v, (const float*)s->S + (size_t)c * s->ns + site, sizeof(v), cudaMemcpyDeviceToHost, s->stream));
+                CK(cudaStreamSynchronize(s->stream));
+                sold[c] = v;
+            } else {
+                CK(cudaMemcpyAsync(&sold[c], (const double*)s->S + (size_t)c * s->ns + site, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+                CK(cudaStreamSynchronize(s->stream));
+            }
+        }
+        const double dS[3] = {snew[0] - sold[0], snew[1] - sold[1], snew[2] - sold[2]};
+        rc = s->fp32 ? ewald_launch_delta<float>(s->ew, (const float*)s->S, (int)site, dS, s->dbuf + 1, s->stream)
+                     : ewald_launch_delta<double>(s->ew, (const double*)s->S, (int)site, dS, s->dbuf + 1, s->stream);
+        s->launches++;
+        if (rc) return cuda_fail(s, cudaGetLastError(), "dipole-dipole energy launch");
+        CK(cudaMemcpyAsync(out, s->dbuf, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    } else {
+        CK(cudaMemcpyAsync(out, s->dbuf, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    }
     CK(cudaStreamSynchronize(s->stream));
+    *dE = out[0] + out[1];
     return SGB_OK;
 }
 
@@ -1889,8 +2089,6 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
     sgb_system* s = c->sys;
     sgb_batch* b = c->batch;
     if (!s && !b) return cfail(c, SGB_ERR_STATE, "the System (or replica batch) of this accumulator was destroyed");
-    if (s && s->sun && s->ewald_on)
-        return cfail(c, SGB_ERR_ARG, "SU(N) dynamics with dipole-dipole interactions is not supported on the GPU");
     if (window != 0 && window != 1) return cfail(c, SGB_ERR_ARG, "window must be 0 (:cosine) or 1 (:rectangular)");
     if (c->window >= 0 && c->window != window)
         return cfail(c, SGB_ERR_ARG, "all samples of one accumulator must use the same window");
@@ -1920,12 +2118,14 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
         if (rc) return cfail(c, rc, batch_error(b));
     } else if (fp32) {
         SnapArgs<float> sn{1, c->nobs, c->measperiod, 0, (const float*)c->ops, (float*)c->A, (float)scale};
-        if (s->ewald_on) rc = run_midpoint_lr<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, &sn);
+        if (s->ewald_on && s->sun) rc = run_midpoint_lr_sun<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, &sn);
+        else if (s->ewald_on) rc = run_midpoint_lr<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, &sn);
         else if (nsteps > 0) rc = run_midpoint<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true, s->mid_order);
         else rc = run_midpoint<float>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
     } else {
         SnapArgs<double> sn{1, c->nobs, c->measperiod, 0, (const double*)c->ops, (double*)c->A, scale};
-        if (s->ewald_on) rc = run_midpoint_lr<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, &sn);
+        if (s->ewald_on && s->sun) rc = run_midpoint_lr_sun<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, &sn);
+        else if (s->ewald_on) rc = run_midpoint_lr<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, &sn);
         else if (nsteps > 0) rc = run_midpoint<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &iters, sn, true, s->mid_order);
         else rc = run_midpoint<double>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, true);
     }

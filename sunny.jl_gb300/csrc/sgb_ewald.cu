@@ -225,6 +225,46 @@ __global__ void k_lr_mid_accept(R* S, const R* Sp, const R* kappa, int ns) {
     }
 }
 
+// Field at `site` from every dipole, f = Σ_j g_siteᵀ A[cell_j - cell_site, i, j] g_j S_j, then
+// out[0] += dS·f + ½ Δμ·A[0, i, i]·Δμ with Δμ = -g_site dS (one block).
+template <class R>
+__global__ void k_ewald_delta(const R* S, const double* g, const double* A, int L1, int L2, int L3, int na, int site,
+                              double d0, double d1, double d2, double* out) {
+    const int ncell = L1 * L2 * L3, ns = ncell * na;
+    const int ai = site / ncell, ci = site % ncell;
+    const int x1 = ci % L1, y1 = (ci / L1) % L2, z1 = ci / (L1 * L2);
+    double f0 = 0, f1 = 0, f2 = 0;
+    for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+        const int aj = j / ncell, cj = j % ncell;
+        const int x2 = cj % L1, y2 = (cj / L1) % L2, z2 = cj / (L1 * L2);
+        const int off = sgb_wrap_any(x2 - x1, L1) + L1 * (sgb_wrap_any(y2 - y1, L2) + L2 * sgb_wrap_any(z2 - z1, L3));
+        const double* gj = g + 9 * (size_t)j;
+        const double sx = S[j], sy = S[ns + j], sz = S[2 * ns + j];
+        double mu[3] = {gj[0] * sx + gj[3] * sy + gj[6] * sz, gj[1] * sx + gj[4] * sy + gj[7] * sz, gj[2] * sx + gj[5] * sy + gj[8] * sz};
+        const size_t c0 = (size_t)((ai * na + aj) * 9) * ncell + off;
+        double am[3];
+        for (int r = 0; r < 3; r++)
+            am[r] = A[c0 + (size_t)r * ncell] * mu[0] + A[c0 + (size_t)(r + 3) * ncell] * mu[1] + A[c0 + (size_t)(r + 6) * ncell] * mu[2];
+        f0 += am[0]; f1 += am[1]; f2 += am[2];
+    }
+    f0 = sgb_block_sum(f0);
+    f1 = sgb_block_sum(f1);
+    f2 = sgb_block_sum(f2);
+    if (threadIdx.x == 0) {
+        const double* gi = g + 9 * (size_t)site;
+        const double phi[3] = {f0, f1, f2};
+        double f[3];
+        for (int r = 0; r < 3; r++) f[r] = gi[3 * r] * phi[0] + gi[3 * r + 1] * phi[1] + gi[3 * r + 2] * phi[2];
+        const double dS[3] = {d0, d1, d2};
+        double dmu[3], ad[3];
+        for (int r = 0; r < 3; r++) dmu[r] = -(gi[r] * dS[0] + gi[r + 3] * dS[1] + gi[r + 6] * dS[2]);
+        const size_t c0 = (size_t)((ai * na + ai) * 9) * ncell;
+        for (int r = 0; r < 3; r++)
+            ad[r] = A[c0 + (size_t)r * ncell] * dmu[0] + A[c0 + (size_t)(r + 3) * ncell] * dmu[1] + A[c0 + (size_t)(r + 6) * ncell] * dmu[2];
+        out[0] = dS[0] * f[0] + dS[1] * f[1] + dS[2] * f[2] + 0.5 * (dmu[0] * ad[0] + dmu[1] * ad[1] + dmu[2] * ad[2]);
+    }
+}
+
 int grid_for(long long n) {
     long long g = (n + SGB_BLOCK - 1) / SGB_BLOCK;
     return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
@@ -252,6 +292,14 @@ int ewald_apply(const EwaldDev& E, const R* S, double* grad_aos, double* part, c
     k_ewald_finish<R><<<EWALD_PART_BLOCKS, SGB_BLOCK, 0, st>>>(S, E.g, E.phi, ns, ncell, grad_aos, part);
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
+
+template <class R>
+int ewald_launch_delta(const EwaldDev& E, const R* S, int site, const double* dS3, double* out, cudaStream_t st) {
+    k_ewald_delta<R><<<1, 256, 0, st>>>(S, E.g, E.Areal, E.L[0], E.L[1], E.L[2], E.na, site, dS3[0], dS3[1], dS3[2], out);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+template int ewald_launch_delta<float>(const EwaldDev&, const float*, int, const double*, double*, cudaStream_t);
+template int ewald_launch_delta<double>(const EwaldDev&, const double*, int, const double*, double*, cudaStream_t);
 
 template int ewald_apply<float>(const EwaldDev&, const float*, double*, double*, cudaStream_t);
 template int ewald_apply<double>(const EwaldDev&, const double*, double*, double*, cudaStream_t);

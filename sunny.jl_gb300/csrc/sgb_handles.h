@@ -62,6 +62,8 @@ struct sgb_system {
     double* ew_part = nullptr;       // [EWALD_PART_BLOCKS] energy partials
     double* lr_grad = nullptr;       // [ns][3] gradient of the per-stage integrator path
     int lr_grad_cap = 0;
+    void* lr_sun = nullptr;          // SU(N) per-stage scratch: HZ [ns][2N] FP64, kets ZP, D1, XI
+    size_t lr_sun_cap = 0;
     // SU(N) general pair couplings (sgb_set_general) and their device rows
     std::vector<int> gen_bond_h;
     std::vector<double> gen_A_h, gen_B_h;

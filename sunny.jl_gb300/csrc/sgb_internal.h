@@ -108,6 +108,14 @@ size_t sun_cluster_smem(const Model<R>& M, int nsl);
 // hz ([ns][N][2]) += (f · S) Z for a per-site dipole field f ([ns][3], dE/dS)
 template <class R>
 int sun_launch_add_dipole_field(const Model<R>& M, const R* Z, const double* f, double* hz, cudaStream_t st);
+// Stage kernels of SU(N) dynamics with dipole-dipole interactions (one launch per stage):
+// 0 Heun predictor (Z, hz -> ZP, D1 increment, XI noise), 1 Heun corrector, 2 midpoint
+// Zbar = (Z + ZP)/2 into D1, 3 midpoint update of ZP from hz with partial sums in part,
+// 4 midpoint acceptance Z = normalize(ZP), 5 snapshot row t of Z.
+template <class R>
+int sun_launch_lr_stage(int stage, const Model<R>& M, R* Z, R* ZP, R* D1, R* XI, const double* hz, double dt, double lam,
+                        double nscale, uint64_t seed, uint64_t step, const double* noise, double* part,
+                        const SnapArgs<R>* sn, int t, cudaStream_t st);
 template <class R>
 int sun_launch_heun_cluster(const Model<R>& M, R* Z, R* D, R* Q, int cs, int nsteps, double dt, double lam, double nscale,
                             uint64_t seed, uint64_t step0, const double* noise, cudaStream_t st);
@@ -197,8 +205,19 @@ struct EwaldDev {
     cufftDoubleComplex* Fphi = nullptr;  // [na*3][nm]
     cufftHandle plan_f = 0, plan_b = 0;
     bool have_f = false, have_b = false;
+    double* Areal = nullptr;         // [na*na*9][ncell] pair matrices A (LocalSampler updates)
 };
 #define EWALD_PART_BLOCKS 256
+// out[0] += ewald_energy_delta (Ewald.jl:230-241) for the dipole at `site` changing by dS;
+// S: dipoles (expected dipoles in SU(N) mode) [3][ns]
+template <class R>
+int ewald_launch_delta(const EwaldDev& E, const R* S, int site, const double* dS3, double* out, cudaStream_t st);
+// LocalSampler sweeps of a dipole system with dipole-dipole interactions: every update in
+// sequence (the term couples every pair of sites), the Ewald field F ([ns][3], dE/dS of the
+// term) kept current by a rank-one update after each accepted move; one CTA
+template <class R>
+int mc_launch_sweeps_ewald(const Model<R>& M, R* S, const McArgs& A, const EwaldDev& E, double* F, double* partials,
+                           cudaStream_t st);
 int ewald_precompute(const EwaldGeom& G, const double* pos_d, double* A, cudaStream_t st);
 // adds the Ewald gradient into grad_aos ([ns][3], may be null) and writes EWALD_PART_BLOCKS
 // energy partials into part (may be null)

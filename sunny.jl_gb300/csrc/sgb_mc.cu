@@ -211,6 +211,113 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_local_sweeps(Model<R> M, R* S, Ct
     }
 }
 
+// Sweeps of a dipole system with dipole-dipole interactions. The term couples every pair of
+// sites, so no two updates are independent: one CTA proposes at the sites in the order of
+// A.perm, one at a time (thread 0: the proposal, the short-range change mc_local_dE and the
+// Ewald change ΔS·F(site) + ½ Δμ·A[0,i,i]·Δμ, Ewald.jl:230-241), and after an accepted move
+// every thread adds the move's field g_jᵀ A[cell_site - cell_j, a_j, a_site] g_site ΔS to its
+// sites' F. Random numbers as k_local_sweeps.
+template <class R, bool INJECT>
+__global__ void __launch_bounds__(256) k_local_sweeps_ewald(Model<R> M, R* S, McArgs A, EwaldDev E, double* F,
+                                                            double* partials) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tab<R> T = stage_tables<R>(M, smem);
+    __shared__ int s_acc;
+    __shared__ double s_d[3];
+    __syncthreads();
+    const int ns = M.ns, ncell = M.ncell, L1 = M.L1, L2 = M.L2, L3 = M.L3, na = M.na;
+    double aE = 0, ax = 0, ay = 0, az = 0;
+    for (int k = 0; k < A.nsweeps; k++) {
+        const bool partial = (k == A.nsweeps - 1) && A.frac < 1.0;
+        const uint64_t sweep = A.sweep0 + (uint64_t)k;
+        for (int idx = 0; idx < ns; idx++) {
+            const int site = A.perm[idx];
+            if (threadIdx.x == 0) {
+                int acc = 0;
+                double u[4];
+                const double* rr = nullptr;
+                if (INJECT) {
+                    rr = A.rnd + ((size_t)k * ns + site) * 6;
+                    u[0] = rr[3]; u[1] = rr[4]; u[2] = rr[5];
+                } else {
+                    sgb_mc_uniforms4(A.seed, sweep, (uint32_t)site, u);
+                }
+                if (!(partial && !(u[2] < A.frac))) {
+                    int kind = A.kind[A.nkind - 1];
+                    double mag = A.mag[A.nkind - 1];
+                    for (int i = 0; i < A.nkind - 1; i++)
+                        if (u[0] < A.cum[i]) { kind = A.kind[i]; mag = A.mag[i]; break; }
+                    if (kind == SGB_PROPOSE_DELTA && isinf(mag)) kind = SGB_PROPOSE_UNIFORM;
+                    const R kap = M.kappa[site];
+                    const R ox = S[site], oy = S[ns + site], oz = S[2 * ns + site];
+                    R nx, ny, nz;
+                    if (kind == SGB_PROPOSE_FLIP) {
+                        nx = -ox; ny = -oy; nz = -oz;
+                    } else {
+                        R g[4];
+                        if (INJECT) { g[0] = (R)rr[0]; g[1] = (R)rr[1]; g[2] = (R)rr[2]; }
+                        else sgb_normals4<R>(A.seed, SGB_MC_STREAM, sweep, (uint32_t)site, 0u, g);
+                        if (kind == SGB_PROPOSE_UNIFORM) {
+                            nx = g[0]; ny = g[1]; nz = g[2];
+                        } else {
+                            const R m = (R)mag * kap;
+                            nx = ox + m * g[0]; ny = oy + m * g[1]; nz = oz + m * g[2];
+                        }
+                        normalize_dip<R>(nx, ny, nz, kap);
+                    }
+                    double e = (double)mc_local_dE<R>(M, T, site, site / ncell, S, ox, oy, oz, nx, ny, nz);
+                    const double d[3] = {(double)nx - (double)ox, (double)ny - (double)oy, (double)nz - (double)oz};
+                    const double* gi = E.g + 9 * (size_t)site;
+                    const int ai = site / ncell;
+                    double dmu[3], ad[3];
+                    for (int r = 0; r < 3; r++) dmu[r] = -(gi[r] * d[0] + gi[r + 3] * d[1] + gi[r + 6] * d[2]);
+                    const size_t c0 = (size_t)((ai * na + ai) * 9) * ncell;
+                    for (int r = 0; r < 3; r++)
+                        ad[r] = E.Areal[c0 + (size_t)r * ncell] * dmu[0] + E.Areal[c0 + (size_t)(r + 3) * ncell] * dmu[1] +
+                                E.Areal[c0 + (size_t)(r + 6) * ncell] * dmu[2];
+                    const double* f = F + 3 * (size_t)site;
+                    e += d[0] * f[0] + d[1] * f[1] + d[2] * f[2] + 0.5 * (dmu[0] * ad[0] + dmu[1] * ad[1] + dmu[2] * ad[2]);
+                    if (A.kT == 0.0 ? (e <= 0.0) : (u[1] <= exp(-e / A.kT))) {
+                        acc = 1;
+                        S[site] = nx; S[ns + site] = ny; S[2 * ns + site] = nz;
+                        aE += e;
+                        ax += d[0]; ay += d[1]; az += d[2];
+                        // g_site ΔS, the moved moment's change up to sign, for the field update
+                        s_d[0] = -dmu[0]; s_d[1] = -dmu[1]; s_d[2] = -dmu[2];
+                    }
+                }
+                s_acc = acc;
+            }
+            __syncthreads();
+            if (s_acc) {
+                // F_j += g_jᵀ A[cell_site - cell_j, a_j, a_site] (g_site ΔS) for every site j
+                const int as = site / ncell, cs = site % ncell;
+                const int xs = cs % L1, ys = (cs / L1) % L2, zs = cs / (L1 * L2);
+                const double m0 = s_d[0], m1 = s_d[1], m2 = s_d[2];
+                for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+                    const int aj = j / ncell, cj = j % ncell;
+                    const int off = sgb_wrap_any(xs - cj % L1, L1) + L1 * (sgb_wrap_any(ys - (cj / L1) % L2, L2) +
+                                                                          L2 * sgb_wrap_any(zs - cj / (L1 * L2), L3));
+                    const size_t c0 = (size_t)((aj * na + as) * 9) * ncell + off;
+                    double am[3];
+                    for (int r = 0; r < 3; r++)
+                        am[r] = E.Areal[c0 + (size_t)r * ncell] * m0 + E.Areal[c0 + (size_t)(r + 3) * ncell] * m1 +
+                                E.Areal[c0 + (size_t)(r + 6) * ncell] * m2;
+                    const double* gj = E.g + 9 * (size_t)j;
+                    for (int r = 0; r < 3; r++) F[3 * (size_t)j + r] += gj[3 * r] * am[0] + gj[3 * r + 1] * am[1] + gj[3 * r + 2] * am[2];
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) {
+        partials[0] = aE;
+        partials[1] = ax;
+        partials[2] = ay;
+        partials[3] = az;
+    }
+}
+
 template <class R>
 __global__ void k_local_dE(Model<R> M, const R* S, int site, R nx, R ny, R nz, double* out) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -262,9 +369,23 @@ int mc_launch_local_dE(const Model<R>& M, const R* S, int site, double nx, doubl
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
+template <class R>
+int mc_launch_sweeps_ewald(const Model<R>& M, R* S, const McArgs& A, const EwaldDev& E, double* F, double* partials,
+                           cudaStream_t st) {
+    const size_t smem = (size_t)M.tables_bytes;
+    const void* k = A.rnd ? (const void*)k_local_sweeps_ewald<R, true> : (const void*)k_local_sweeps_ewald<R, false>;
+    if (A.rnd ? set_smem(k_local_sweeps_ewald<R, true>, smem) : set_smem(k_local_sweeps_ewald<R, false>, smem)) return SGB_ERR_CUDA;
+    Model<R> m = M;
+    McArgs a = A;
+    EwaldDev e = E;
+    void* args[] = {&m, &S, &a, &e, &F, &partials};
+    return cudaLaunchKernel(k, dim3(1), dim3(256), args, smem, st) == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
 #define SGB_MC_INST(R)                                                                                         \
     template int mc_max_blocks<R>(size_t, int*);                                                               \
     template int mc_launch_sweeps<R>(const Model<R>&, R*, Ctrl*, const McArgs&, int, double*, cudaStream_t);   \
-    template int mc_launch_local_dE<R>(const Model<R>&, const R*, int, double, double, double, double*, cudaStream_t);
+    template int mc_launch_local_dE<R>(const Model<R>&, const R*, int, double, double, double, double*, cudaStream_t); \
+    template int mc_launch_sweeps_ewald<R>(const Model<R>&, R*, const McArgs&, const EwaldDev&, double*, double*, cudaStream_t);
 SGB_MC_INST(float)
 SGB_MC_INST(double)

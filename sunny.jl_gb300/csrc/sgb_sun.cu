@@ -7,12 +7,16 @@
 //   Langevin Heun     src/Integrators.jl:277-298, 335-357; proj MathBasics.jl:62
 //   Schrodinger midpoint src/Integrators.jl:361-371, 422-452
 //
-// In SU(N) mode neighbours interact only through expected dipoles (bilinear and Zeeman
-// terms) and expected Stevens quadrupoles (biquadratic terms). Each thread therefore
-// keeps its sites' coherent states Z in registers for the whole persistent launch and
-// publishes only <Z|S|Z> (3 reals) and, when biquadratic couplings exist, <Z|O2q|Z>
-// (5 reals) per site through L2-resident SoA buffers.
+// In SU(N) mode neighbours interact through expected dipoles (bilinear and Zeeman terms),
+// expected Stevens quadrupoles (biquadratic terms) and, for general couplings
+// (Σ_k A_k ⊗ B_k), expectations of arbitrary operators. Each thread therefore keeps its
+// sites' coherent states Z in registers for the whole persistent launch and publishes
+// <Z|S|Z> (3 reals), when biquadratic or general couplings exist <Z|O2q|Z> (5 reals), and
+// with general couplings the packed density zz^† (N^2 reals) per site through
+// L2-resident SoA buffers.
 #include <cooperative_groups.h>
+
+#include <algorithm>
 
 #include "sgb_device.cuh"
 
@@ -833,6 +837,145 @@ int add_field_n(const R* Z, const double* f, double* hz, int ns, cudaStream_t st
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
+// ---- stage kernels for SU(N) dynamics with dipole-dipole interactions --------------------
+// Every HZ then needs a transform over the whole lattice, so each Heun stage and each
+// midpoint iteration is its own launch (HZ from sun_launch_grad plus the dipole field).
+// Kets SoA [2N][ns]; HZ AoS [ns][2N] in FP64. Same per-site arithmetic and noise stream as
+// k_sun_heun / k_sun_midpoint.
+template <class R, int N, bool INJECT>
+__global__ void k_lr_sun_heun_a(const R* Z, const double* hz, R* ZP, R* D1, R* XI, const R* kappa, int ns, R dt, R lam,
+                                R nscale, uint64_t seed, uint64_t step, const double* noise) {
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < ns; site += gridDim.x * blockDim.x) {
+        R z[2 * N], ze[2 * N], h[2 * N], d1[2 * N];
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) {
+            z[c] = Z[(size_t)c * ns + site];
+            h[c] = (R)hz[(size_t)site * 2 * N + c];
+        }
+        if (nscale == (R)0) {
+#pragma unroll
+            for (int c = 0; c < 2 * N; c++) ze[c] = 0;
+        } else if (INJECT) {
+#pragma unroll
+            for (int c = 0; c < 2 * N; c++) ze[c] = (R)noise[(size_t)site * 2 * N + c] * nscale;
+        } else {
+            const R r2 = (R)0.70710678118654752440;
+#pragma unroll
+            for (int c = 0; c < 2 * N; c += 4) {
+                R g4[4];
+                sgb_normals4<R>(seed, 0u, step, (uint32_t)site, (uint32_t)(c / 4), g4);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (c + q < 2 * N) ze[c + q] = g4[q] * r2 * nscale;
+            }
+        }
+        rhs_sun<R, N>(z, ze, h, dt, lam, d1);
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) z[c] += d1[c];
+        normalize_ket<R, N>(z, kappa[site]);
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) {
+            ZP[(size_t)c * ns + site] = z[c];
+            D1[(size_t)c * ns + site] = d1[c];
+            XI[(size_t)c * ns + site] = ze[c];
+        }
+    }
+}
+
+template <class R, int N>
+__global__ void k_lr_sun_heun_b(R* Z, const R* ZP, const double* hz, const R* D1, const R* XI, const R* kappa, int ns, R dt,
+                                R lam) {
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < ns; site += gridDim.x * blockDim.x) {
+        R zp[2 * N], ze[2 * N], h[2 * N], d2[2 * N], z[2 * N];
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) {
+            zp[c] = ZP[(size_t)c * ns + site];
+            ze[c] = XI[(size_t)c * ns + site];
+            h[c] = (R)hz[(size_t)site * 2 * N + c];
+        }
+        rhs_sun<R, N>(zp, ze, h, dt, lam, d2);
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) z[c] = Z[(size_t)c * ns + site] + (D1[(size_t)c * ns + site] + d2[c]) / 2;
+        normalize_ket<R, N>(z, kappa[site]);
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) Z[(size_t)c * ns + site] = z[c];
+    }
+}
+
+// Zbar = (Z + Z')/2 (Integrators.jl:431, not normalised)
+template <class R, int N>
+__global__ void k_lr_sun_mid_half(const R* Z, const R* Zp, R* Zb, int ns) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)2 * N * ns; i += (size_t)gridDim.x * blockDim.x)
+        Zb[i] = (Z[i] + Zp[i]) / 2;
+}
+
+// Z'' = Z + rhs(Zbar); per-block partial sums of |Z' - Z''|^2 (fast_isapprox); Z' = Z''
+template <class R, int N>
+__global__ void k_lr_sun_mid_update(const R* Z, const R* Zb, const double* hz, R* Zp, int ns, R dt, R lam, double* part) {
+    double acc = 0;
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < ns; site += gridDim.x * blockDim.x) {
+        R zb[2 * N], h[2 * N], zero[2 * N], dz[2 * N];
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) {
+            zb[c] = Zb[(size_t)c * ns + site];
+            h[c] = (R)hz[(size_t)site * 2 * N + c];
+            zero[c] = 0;
+        }
+        rhs_sun<R, N>(zb, zero, h, dt, lam, dz);
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) {
+            const R q = Z[(size_t)c * ns + site] + dz[c];
+            const R e = Zp[(size_t)c * ns + site] - q;
+            acc += (double)(e * e);
+            Zp[(size_t)c * ns + site] = q;
+        }
+    }
+    const double t = sgb_block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+template <class R, int N>
+__global__ void k_lr_sun_mid_accept(R* Z, const R* Zp, const R* kappa, int ns) {
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < ns; site += gridDim.x * blockDim.x) {
+        R z[2 * N];
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) z[c] = Zp[(size_t)c * ns + site];
+        normalize_ket<R, N>(z, kappa[site]);
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) Z[(size_t)c * ns + site] = z[c];
+    }
+}
+
+template <class R, int N>
+__global__ void k_sun_snapshot(Model<R> M, const R* Z, SnapArgs<R> sn, int t) {
+    for (int site = blockIdx.x * blockDim.x + threadIdx.x; site < M.ns; site += gridDim.x * blockDim.x) {
+        R z[2 * N];
+#pragma unroll
+        for (int c = 0; c < 2 * N; c++) z[c] = Z[(size_t)c * M.ns + site];
+        write_snapshot_sun<R, N>(M, sn, t, site, z);
+    }
+}
+
+template <class R, int N>
+int lr_sun_n(int stage, const Model<R>& M, R* Z, R* ZP, R* D1, R* XI, const double* hz, double dt, double lam, double nscale,
+             uint64_t seed, uint64_t step, const double* noise, double* part, const SnapArgs<R>* sn, int t, cudaStream_t st) {
+    const int ns = M.ns;
+    const int grid = std::max(1, std::min(4096, (ns + SGB_BLOCK - 1) / SGB_BLOCK));
+    switch (stage) {
+        case 0:
+            if (noise) k_lr_sun_heun_a<R, N, true><<<grid, SGB_BLOCK, 0, st>>>(Z, hz, ZP, D1, XI, M.kappa, ns, (R)dt, (R)lam, (R)nscale, seed, step, noise);
+            else k_lr_sun_heun_a<R, N, false><<<grid, SGB_BLOCK, 0, st>>>(Z, hz, ZP, D1, XI, M.kappa, ns, (R)dt, (R)lam, (R)nscale, seed, step, noise);
+            break;
+        case 1: k_lr_sun_heun_b<R, N><<<grid, SGB_BLOCK, 0, st>>>(Z, ZP, hz, D1, XI, M.kappa, ns, (R)dt, (R)lam); break;
+        case 2: k_lr_sun_mid_half<R, N><<<grid, SGB_BLOCK, 0, st>>>(Z, ZP, D1, ns); break;
+        case 3: k_lr_sun_mid_update<R, N><<<EWALD_PART_BLOCKS, SGB_BLOCK, 0, st>>>(Z, D1, hz, ZP, ns, (R)dt, (R)lam, part); break;
+        case 4: k_lr_sun_mid_accept<R, N><<<grid, SGB_BLOCK, 0, st>>>(Z, ZP, M.kappa, ns); break;
+        case 5: k_sun_snapshot<R, N><<<grid, SGB_BLOCK, 0, st>>>(M, Z, *sn, t); break;
+        default: return SGB_ERR_ARG;
+    }
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
 // ---- Langevin for small SU(N) lattices held by one thread-block cluster ---------------
 // HZ of one site with the neighbours' expected dipoles (and quadrupoles) fetched through
 // loaders, bonds in table order (the same sums as sun_field).
@@ -1443,6 +1586,16 @@ int sun_launch_add_dipole_field(const Model<R>& M, const R* Z, const double* f, 
 }
 
 template <class R>
+int sun_launch_lr_stage(int stage, const Model<R>& M, R* Z, R* ZP, R* D1, R* XI, const double* hz, double dt, double lam,
+                        double nscale, uint64_t seed, uint64_t step, const double* noise, double* part,
+                        const SnapArgs<R>* sn, int t, cudaStream_t st) {
+    SGB_SUN_DISPATCH((lr_sun_n<R, 2>(stage, M, Z, ZP, D1, XI, hz, dt, lam, nscale, seed, step, noise, part, sn, t, st)),
+                     (lr_sun_n<R, 3>(stage, M, Z, ZP, D1, XI, hz, dt, lam, nscale, seed, step, noise, part, sn, t, st)),
+                     (lr_sun_n<R, 4>(stage, M, Z, ZP, D1, XI, hz, dt, lam, nscale, seed, step, noise, part, sn, t, st)),
+                     (lr_sun_n<R, 5>(stage, M, Z, ZP, D1, XI, hz, dt, lam, nscale, seed, step, noise, part, sn, t, st)))
+}
+
+template <class R>
 size_t sun_cluster_smem(const Model<R>& M, int nsl) {
     return (size_t)((M.tables_bytes + 15) / 16) * 16 + (size_t)(8 * M.N + 6 + (M.has_biquad ? 10 : 0)) * nsl * sizeof(R);
 }
@@ -1490,6 +1643,8 @@ int sun_launch_local_dE(const Model<R>& M, const R* Z, const R* D, const R* Q, i
     template int sun_mc_max_blocks<R>(const Model<R>&, int*);                                                    \
     template size_t sun_cluster_smem<R>(const Model<R>&, int);                                                  \
     template int sun_launch_add_dipole_field<R>(const Model<R>&, const R*, const double*, double*, cudaStream_t); \
+    template int sun_launch_lr_stage<R>(int, const Model<R>&, R*, R*, R*, R*, const double*, double, double, double, uint64_t, \
+                                        uint64_t, const double*, double*, const SnapArgs<R>*, int, cudaStream_t); \
     template int sun_launch_heun_cluster<R>(const Model<R>&, R*, R*, R*, int, int, double, double, double, uint64_t, \
                                             uint64_t, const double*, cudaStream_t);                            \
     template int sun_launch_local_dE<R>(const Model<R>&, const R*, const R*, const R*, int, const SunKet&, double*, cudaStream_t);

@@ -145,8 +145,113 @@ def test_canted_afm_optimization(gpu, sg, mode, jitter, ref):
     assert sg.energy_per_site(s) == pytest.approx(ref, rel=1e-9)
 
 
+def _ewald_oracle(orc, sys_, demag, mu0):
+    """Oracle of the system's short-range couplings with the pairwise dipole-dipole term
+    included in its local energy changes; also returns the pair matrices A."""
+    o = oracle_of(orc, sys_)
+    cr = sys_.crystal
+    A = orc.ewald_matrices(sys_.dims, cr.latvecs, [cr.position(i) for i in range(1, sys_.natoms + 1)], demag, mu0)
+    o.set_ewald(A)
+    return o, A
+
+
+def _two_atom_box(sg, mode="dipole", precision="fp64", seed=5):
+    # exchange plus dipole-dipole between two atoms of different spin and g tensor
+    rng = np.random.default_rng(seed)
+    cr = sg.Crystal(sg.lattice_vectors(2.0, 2.2, 2.5, 90, 90, 90), [[0, 0, 0], [0.5, 0.4, 0.3]])
+    g2 = np.eye(3) * 2 + 0.2 * rng.standard_normal((3, 3))
+    mom = [(1, sg.Moment(s=1, g=2)), (2, sg.Moment(s=1 if mode == "SUN" else 1.5, g=g2))]
+    s = sg.System(cr, mom, mode, dims=(2, 2, 2), seed=seed + 1, precision=precision)
+    s.set_exchange(0.5, sg.Bond(1, 2, [0, 0, 0]))
+    if mode == "SUN":
+        s.set_onsite_coupling(lambda Sx, Sy, Sz: -0.3 * Sz @ Sz, 1)
+    s.randomize_spins()
+    demag = np.diag([0.1, 0.2, 0.3])
+    s.enable_dipole_dipole(0.4, demag)
+    return s, demag
+
+
+def test_local_energy_change_with_dipole_dipole(gpu, sg, orc):
+    # ewald_energy_delta (Ewald.jl:210-241) inside local_energy_change (Interactions.jl:311-373)
+    sys_, demag = _triclinic(sg, dims=(2, 1, 1))
+    o, _ = _ewald_oracle(orc, sys_, demag, 1.0)
+    S = sys_.dipoles_flat()
+    kap = np.asarray(sys_.kappas, dtype=float).reshape(-1)
+    rng = np.random.default_rng(4)
+    E0 = sg.energy(sys_)
+    for _ in range(6):
+        i = int(rng.integers(0, sys_.nsites))
+        v = rng.standard_normal(3)
+        Sn = kap[i] * v / np.linalg.norm(v)
+        dE = sg.local_energy_change(sys_, i, Sn)
+        assert dE == pytest.approx(o.local_energy_change(S, i, Sn), abs=1e-12 * max(1.0, abs(E0)))
+        S1 = S.copy()
+        S1[i] = Sn
+        sys_.set_state_flat(dipoles=S1)
+        assert dE == pytest.approx(sg.energy(sys_) - E0, abs=1e-11 * max(1.0, abs(E0)))
+        sys_.set_state_flat(dipoles=S)
+
+
+def test_sun_local_energy_change_with_dipole_dipole(gpu, sg, orc):
+    sys_, demag = _two_atom_box(sg, "SUN")
+    o, _ = _ewald_oracle(orc, sys_, demag, 0.4)
+    Z = sys_.coherents_flat()
+    S = o.expected_spin(Z)
+    rng = np.random.default_rng(6)
+    E0 = sg.energy(sys_)
+    for _ in range(4):
+        i = int(rng.integers(0, sys_.nsites))
+        zn = rng.standard_normal(3) + 1j * rng.standard_normal(3)
+        zn /= np.linalg.norm(zn)
+        dE = sg.local_energy_change(sys_, i, zn)
+        assert dE == pytest.approx(o.local_energy_change(S, i, zn, Z=Z), abs=1e-12 * max(1.0, abs(E0)))
+        Z1 = Z.copy()
+        Z1[i] = zn
+        sys_.set_state_flat(coherents=Z1)
+        assert dE == pytest.approx(sg.energy(sys_) - E0, abs=1e-11 * max(1.0, abs(E0)))
+        sys_.set_state_flat(coherents=Z)
+
+
+@pytest.mark.parametrize("kT,nsweeps", [(0.5, 2), (0.0, 1), (0.8, 1.5)])
+def test_local_sweeps_with_dipole_dipole(gpu, sg, orc, kT, nsweeps):
+    # LocalSampler with dipole-dipole: one block proposes the sites in sweep order and
+    # updates every site's field after each accepted move; the oracle applies the same
+    # proposals in the same order with the pairwise sum per proposal
+    sys_, demag = _two_atom_box(sg)
+    o, A = _ewald_oracle(orc, sys_, demag, 0.4)
+    S0 = sys_.dipoles_flat()
+    _, col = sg.local_colors(sys_)
+    order = np.lexsort((np.arange(sys_.nsites), col))
+    total = math.ceil(nsweeps)
+    rng = np.random.default_rng(8)
+    rand = np.concatenate([rng.standard_normal((total, sys_.nsites, 3)), rng.random((total, sys_.nsites, 3))], axis=2)
+    prop = sg.mix_proposals(0.3, sg.propose_uniform, 0.2, sg.propose_flip, 0.5, sg.propose_delta(0.4))
+    smp = sg.LocalSampler(kT=kT, nsweeps=nsweeps, propose=prop)
+    E0 = sg.energy(sys_)
+    sg.step(sys_, smp, 1, rand)
+    frac = nsweeps - math.floor(nsweeps) if nsweeps != total else 1.0
+    S_ref, dE_ref, dS_ref = o.local_sweeps(S0, kT, total, frac, order, prop.terms, rand)
+    S_gpu = sys_.dipoles_flat()
+    assert np.max(np.abs(S_gpu - S_ref)) < 1e-11 * np.max(np.abs(S_ref))
+    assert not np.allclose(S_gpu, S0)
+    assert smp.ΔE == pytest.approx(dE_ref, abs=1e-10 * max(1.0, abs(E0)))
+    assert np.allclose(smp.ΔS, dS_ref, atol=1e-10)
+    assert smp.ΔE == pytest.approx(sg.energy(sys_) - E0, abs=1e-10 * max(1.0, abs(E0)))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_local_sweeps_with_dipole_dipole_device_rng(gpu, sg, precision):
+    sys_, _ = _two_atom_box(sg, precision=precision)
+    E0, M0 = sg.energy(sys_), sg.magnetization(sys_)
+    smp = sg.LocalSampler(kT=0.6, nsweeps=3, propose=sg.propose_delta(0.5))
+    sg.step(sys_, smp, 2)
+    tol = 1e-9 if precision == "fp64" else 2e-4
+    assert smp.ΔE == pytest.approx(sg.energy(sys_) - E0, abs=tol * sys_.nsites)
+    assert np.allclose(smp.ΔS, sg.magnetization(sys_) - M0, atol=tol * sys_.nsites)
+
+
 def test_unsupported_paths_reject_dipole_dipole(gpu, sg):
-    sys_, _ = _triclinic(sg)
+    sys_, _ = _two_atom_box(sg, "SUN")
     with pytest.raises(sg.SunnyGPUError, match="dipole-dipole"):
         sg.step(sys_, sg.LocalSampler(kT=0.1))
 
@@ -208,5 +313,83 @@ def test_sun_gradient_with_dipole_dipole(gpu, sg, orc):
     assert np.max(np.abs(hz - hz_ref)) < 1e-12 * np.max(np.abs(hz_ref))
     E_ref = o.energy(S, Z) + 0.5 * np.sum(S * f)
     assert sg.energy(s) == pytest.approx(E_ref, abs=1e-12 * abs(E_ref))
-    with pytest.raises(sg.SunnyGPUError, match="SU\\(N\\) dynamics"):
-        sg.step(s, sg.Langevin(0.01, damping=0.1, kT=0.1))
+
+
+def _sun_hz(sg, orc, o, A, sys_, Z):
+    # HZ of set_energy_grad_coherents! (Interactions.jl:596-669) with the dipole-dipole field
+    # dE/dS at the expected dipoles of Z (normalised or not)
+    S = o.expected_spin(Z)
+    f = orc.ewald_pairwise_grad(A, sys_.dims, sys_.natoms, S, sys_._g)
+    Sx, Sy, Sz = sg.spin_matrices_of_dim(sys_.N)
+    return o.grad(None, Z) + np.einsum("sa,abc,sc->sb", f, np.stack([Sx, Sy, Sz]), Z)
+
+
+def _rhs_sun(Z, xi, HZ, dt, lam):
+    # rhs_sun! (Integrators.jl:277-286) with proj (MathBasics.jl:62)
+    if lam == 0:
+        return -1j * dt * HZ
+    v = xi + dt * (1j + lam) * HZ
+    c = np.sum(Z.conj() * v, axis=1) / np.sum(np.abs(Z) ** 2, axis=1)
+    return -(v - c[:, None] * Z)
+
+
+def _norm_ket(Z, kap):
+    return Z / np.sqrt(np.sum(np.abs(Z) ** 2, axis=1) / kap)[:, None]
+
+
+def test_sun_langevin_with_dipole_dipole(gpu, sg, orc):
+    # Heun for coherent states (Integrators.jl:90-108), one launch per stage on the GPU
+    sys_, demag = _two_atom_box(sg, "SUN")
+    o, A = _ewald_oracle(orc, sys_, demag, 0.4)
+    kap = np.asarray(sys_.kappas, dtype=float).reshape(-1)
+    dt, lam, kT = 0.01, 0.2, 0.3
+    rng = np.random.default_rng(10)
+    noise = (rng.standard_normal((3, sys_.nsites, 3)) + 1j * rng.standard_normal((3, sys_.nsites, 3))) / np.sqrt(2)
+    Z = sys_.coherents_flat()
+    for k in range(3):
+        xi = noise[k] * math.sqrt(2 * dt * lam * kT)
+        d1 = _rhs_sun(Z, xi, _sun_hz(sg, orc, o, A, sys_, Z), dt, lam)
+        P = _norm_ket(Z + d1, kap)
+        d2 = _rhs_sun(P, xi, _sun_hz(sg, orc, o, A, sys_, P), dt, lam)
+        Z = _norm_ket(Z + (d1 + d2) / 2, kap)
+    sg.step(sys_, sg.Langevin(dt, damping=lam, kT=kT), 3, noise)
+    assert np.max(np.abs(sys_.coherents_flat() - Z)) < 1e-12
+    assert np.max(np.abs(sys_.dipoles_flat() - o.expected_spin(Z))) < 1e-12
+
+
+def test_sun_midpoint_with_dipole_dipole(gpu, sg, orc):
+    # Schrödinger midpoint (Integrators.jl:422-452) in FP64, then energy conservation
+    sys_, demag = _two_atom_box(sg, "SUN")
+    o, A = _ewald_oracle(orc, sys_, demag, 0.4)
+    kap = np.asarray(sys_.kappas, dtype=float).reshape(-1)
+    dt, tol = 0.01, 1e-12
+    atol2 = tol * tol * sys_.nsites
+    Z = sys_.coherents_flat()
+    E0 = sg.energy(sys_)
+    for _ in range(3):
+        Zp = Z.copy()
+        for _ in range(100):
+            Zb = (Z + Zp) / 2
+            Zpp = Z + _rhs_sun(Zb, 0.0, _sun_hz(sg, orc, o, A, sys_, Zb), dt, 0.0)
+            done = np.sum(np.abs(Zp - Zpp) ** 2) <= atol2
+            Zp = Zpp
+            if done:
+                break
+        Z = _norm_ket(Zp, kap)
+    sg.step(sys_, sg.ImplicitMidpoint(dt, tol=tol), 3)
+    assert np.max(np.abs(sys_.coherents_flat() - Z)) < 1e-10
+    sg.step(sys_, sg.ImplicitMidpoint(dt, tol=tol), 200)
+    assert abs(sg.energy(sys_) - E0) <= 1e-3 * max(1.0, abs(E0))
+
+
+def test_sun_sqw_trajectory_with_dipole_dipole(gpu, sg):
+    # add_sample runs the per-stage SU(N) midpoint path with snapshots: the state after one
+    # sample equals plain ImplicitMidpoint stepping over the same number of steps
+    a, _ = _two_atom_box(sg, "SUN")
+    b, _ = _two_atom_box(sg, "SUN")
+    sc = sg.SampledCorrelations(a, measure=sg.ssf_perp(a), energies=np.linspace(0.0, 3.0, 6), dt=0.05)
+    sg.add_sample(sc, a)
+    nsteps = sc.measperiod * (sc.n_all_omega - 1)
+    sg.step(b, sg.ImplicitMidpoint(sc.dt, tol=sc.integrator.tol), nsteps)
+    assert np.array_equal(a.coherents_flat(), b.coherents_flat())
+    assert np.all(np.isfinite(sc.data)) and np.max(np.abs(sc.data)) > 0

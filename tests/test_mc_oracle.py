@@ -206,3 +206,46 @@ def test_oracle_sun_local_sweeps_anisotropy_energy(sg, orc):
     a = D / kT
     exact = D * (2 - (2 + 2 * a + a * a) * math.exp(-a)) / (a * (1 - (1 + a) * math.exp(-a)))
     assert np.mean(Es) == pytest.approx(exact, rel=0.02)
+
+
+@pytest.mark.parametrize("mode", ["dipole", "SUN"])
+def test_oracle_ewald_energy_delta_is_energy_difference(sg, orc, mode):
+    # ewald_energy_delta (Ewald.jl:210-241) inside local_energy_change: the change of the
+    # pairwise dipole-dipole energy ½ Σ S·∇E plus the short-range terms
+    from models import oracle_of
+    cr = sg.Crystal(sg.lattice_vectors(1.1, 0.9, 0.8, 92, 85, 95), [[0, 0.01, 0.01], [0.6, 0.4, 0.5]])
+    N = 3
+    s = sg.System(cr, [(1, sg.Moment(s=1, g=2))], mode, dims=(2, 2, 1), seed=3, device=None)
+    s.set_bond_coupling(sg.Bond(1, 2, [0, 0, 0]), 0.0, 0.3, 0.0)
+    s.randomize_spins()
+    o = oracle_of(orc, s)
+    rng = np.random.default_rng(2)
+    demag = np.diag([0.1, 0.2, 0.3])
+    pos = [cr.position(i) for i in (1, 2)]
+    A = orc.ewald_matrices(s.dims, cr.latvecs, pos, demag, 0.7)
+    o.set_ewald(A)
+    g = s._g
+
+    def energy(S, Z=None):
+        return o.energy(S, Z) + 0.5 * np.sum(S * orc.ewald_pairwise_grad(A, s.dims, s.natoms, S, g))
+
+    S = s.dipoles_flat()
+    Z = s.coherents_flat() if mode == "SUN" else None
+    for _ in range(4):
+        i = int(rng.integers(0, s.nsites))
+        if mode == "SUN":
+            zn = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+            zn /= np.linalg.norm(zn)
+            Z1 = Z.copy()
+            Z1[i] = zn
+            S1 = o.expected_spin(Z1)
+            ref = energy(S1, Z1) - energy(S, Z)
+            got = o.local_energy_change(S, i, zn, Z=Z)
+        else:
+            v = rng.standard_normal(3)
+            Sn = v / np.linalg.norm(v)
+            S1 = S.copy()
+            S1[i] = Sn
+            ref = energy(S1) - energy(S)
+            got = o.local_energy_change(S, i, Sn)
+        assert got == pytest.approx(ref, abs=1e-12)
