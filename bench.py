@@ -274,6 +274,7 @@ def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000, predic
              "grid": r[3], "smem": r[4], "tune_ms_3_steps": round(tms[k], 4)}
         if r[5]:
             d["block_cells"] = [r[6] & 0xff, (r[6] >> 8) & 0xff, (r[6] >> 16) & 0xff]
+            d["threads"] = 32 * ((r[6] >> 24) & 0xff)
         else:
             d["nbr_index_bytes_smem"] = r[0]
         return d
@@ -295,7 +296,7 @@ def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000, predic
     return res
 
 
-def run_tempering(sg, device, nsteps=5000, exch_interval=100, seed=2024):
+def run_tempering(sg, device, nsteps=20000, exch_interval=100, seed=2024):
     """256 simple-cubic replicas, L drawn uniformly from {8,12,16,24,32}, kT on a geometric
     0.1-2.0 ladder, J=1, -0.1 Sz^2, Langevin damping 0.2, exchanges every 100 steps within
     groups of equal L; FP32 state, FP64 energies; one CUDA graph per exchange round."""
@@ -359,9 +360,37 @@ def dynamics_rate(sg, kind, precision, device, nsteps):
     lib.sgb_event_elapsed(sys_.handle, 0, 1, C.byref(ms))
     E = sg.energy_per_site(sys_)
     ns = sys_.nsites
+    M = sg.magnetization(sys_) / ns
     sys_.close()
     return {"site_steps_per_s": ns * nsteps / (ms.value / 1000.0), "us_per_step": 1000.0 * ms.value / nsteps,
-            "nsites": ns, "steps": nsteps, "energy_per_site": E}
+            "nsites": ns, "steps": nsteps, "energy_per_site": E, "magnetization_per_site": M.tolist(),
+            "abs_magnetization_per_site": float(np.linalg.norm(M))}
+
+
+def batched_langevin_rate(sg, device, nrep=64, nsteps=2000):
+    """Site-steps/s of FP32 Langevin on `nrep` copies of the simple cubic 16^3 model
+    (s=1, J=1, -0.1 Sz^2, dt=0.02, damping 0.1, kT=0.5) advanced together in one persistent
+    launch (the replica batch), with per-replica energy and magnetisation afterwards."""
+    import ctypes as C
+    lib = sg.load_library()
+    proto = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=(16, 16, 16), seed=1, device=None)
+    proto.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    proto.set_onsite_coupling(lambda Sx, Sy, Sz: -0.1 * Sz @ Sz, 1)
+    b = sg.ReplicaBatch(proto, [(16, 16, 16)] * nrep, kT=[0.5] * nrep, precision="fp32", device=device, seed=3)
+    b.randomize_spins()
+    b.langevin(0.02, 0.1, 200)
+    lib.sgb_batch_event_record(b.handle, 0)
+    b.langevin(0.02, 0.1, nsteps)
+    lib.sgb_batch_event_record(b.handle, 1)
+    ms = C.c_float()
+    lib.sgb_batch_event_elapsed(b.handle, 0, 1, C.byref(ms))
+    ns = 16 ** 3
+    E = b.energies() / ns
+    Ms = np.array([np.mean(b.get_state(r), axis=0) for r in range(nrep)])
+    b.close()
+    return {"site_steps_per_s": nrep * ns * nsteps / (ms.value / 1000.0), "us_per_step": 1000.0 * ms.value / nsteps,
+            "replicas": nrep, "nsites_per_replica": ns, "steps": nsteps, "energy_per_site_mean": float(E.mean()),
+            "abs_magnetization_per_site_mean": float(np.mean(np.linalg.norm(Ms, axis=1)))}
 
 
 def local_sampler_rate(sg, precision, device, nsweeps=200):
@@ -619,6 +648,10 @@ def main():
             a = dynamics_rate(sg, kind, "fp32", local, n)
             bb = dynamics_rate(sg, kind, "fp64", local, n // 4)
             extra[kind] = {"fp32": a, "fp64": bb, "speedup": a["site_steps_per_s"] / bb["site_steps_per_s"]}
+            if kind == "sc":
+                bt = batched_langevin_rate(sg, local)
+                extra[kind]["fp32_batch64"] = bt
+                extra[kind]["speedup_batch64_vs_fp64"] = bt["site_steps_per_s"] / bb["site_steps_per_s"]
         extra["local_sampler_sc"] = {p: local_sampler_rate(sg, p, local) for p in ("fp32", "fp64")}
         pt = run_tempering(sg, local)
         extra["adjoint"] = run_adjoint(sg, local)

@@ -402,8 +402,9 @@ int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* desc, sgb_corr** ou
  * first batched add_sample after the couplings are set times every shape that fits on a
  * 3-step run and keeps the fastest. Writes up to `cap` rows of (neighbour-index bytes in
  * shared memory or 0 for the global table, bonds gathered together, CTAs per SM, grid,
- * dynamic shared bytes, kernel: 0 sublattice tiles or 1 cell blocks, cells per block as
- * bx | by << 8 | bz << 16 for kernel 1) into shapes[cap][7] and their tuning times into
+ * dynamic shared bytes, kernel: 0 sublattice tiles or 1 cell blocks, cells per block and
+ * threads per CTA as bx | by << 8 | bz << 16 | (threads / 32) << 24 for kernel 1) into
+ * shapes[cap][7] and their tuning times into
  * ms[cap] (either may be NULL); *chosen = the row in use. Returns the number of shapes
  * (0 before the first batched add_sample). */
 /* First fixed-point iterate of each batched midpoint step (no counterpart in the

@@ -942,7 +942,8 @@ int run_local_sweeps(sgb_system* s, McArgs& A, const double* rnd_host, double* o
         if ((rc = reset_ctrl(s))) return rc;
         int gused = grid;
         if (F) {
-            rc = mc_launch_sweeps_ewald<R>(model<R>(s), (R*)s->S, a, s->ew, F, s->mc_part, s->stream);
+            rc = s->sun ? sun_launch_local_sweeps_ewald<R>(model<R>(s), (R*)s->Z, (R*)s->S, (R*)s->Q, a, s->ew, F, s->mc_part, s->stream)
+                        : mc_launch_sweeps_ewald<R>(model<R>(s), (R*)s->S, a, s->ew, F, s->mc_part, s->stream);
             gused = 1;
         } else {
             rc = s->sun ? sun_launch_local_sweeps<R>(model<R>(s), (R*)s->Z, (R*)s->S, (R*)s->Q, s->ctrl, a, grid, s->mc_part, s->stream)
@@ -1511,8 +1512,6 @@ int sgb_midpoint(sgb_system* s, double dt, double damping, double tol, int32_t m
 int sgb_local_sweeps(sgb_system* s, double kT, double nsweeps, const sgb_proposal* prop, uint64_t seed, uint64_t sweep0,
                      const double* rand, double* dE, double* dS3) {
     if (!s) return fail(s, SGB_ERR_ARG, "null handle");
-    if (s->ewald_on && s->sun)
-        return fail(s, SGB_ERR_ARG, "LocalSampler with dipole-dipole interactions in SU(N) mode is not supported on the GPU");
     if (!(kT >= 0)) return fail(s, SGB_ERR_ARG, "Select nonnegative kT");
     if (!(nsweeps >= 0) || nsweeps > 1e9) return fail(s, SGB_ERR_ARG, "nsweeps must be nonnegative");
     if (!prop || prop->n < 1 || prop->n > 4) return fail(s, SGB_ERR_ARG, "a proposal mixture has 1 to 4 functions");

@@ -815,42 +815,48 @@ static void blk_shapes(sgb_batch* b, bool gen, std::vector<MidShape>& out) {
             for (int lz = 0; (1 << lz) <= b->dims[2]; lz++) {
                 if (!log2_div(b->dims[0], lx) || !log2_div(b->dims[1], ly) || !log2_div(b->dims[2], lz)) continue;
                 const long long nsb = (long long)b->na << (lx + ly + lz);
-                if (nsb < SGB_BLK_THREADS || nsb > 16 * SGB_BLK_THREADS) continue;
+                if (nsb < 256 || nsb > 16 * SGB_BLK_THREADS_MAX) continue;
                 BlkGeom g = blk_geom(b, lx, ly, lz);
                 if (g.HX > 256 || g.HY > 256 || g.HZ > 256) continue;
                 const size_t smem = 128 + g.halo_bytes + (size_t)b->tables_bytes + 4 * (size_t)((b->fp32 ? b->mf.nb : b->md.nb) + 4);
                 if (smem > 200 * 1024) continue;
                 cands.push_back({(double)g.HX * g.HY * g.HZ / (double)((1 << lx) * (1 << ly) * (1 << lz)), lx, ly, lz});
             }
-    // rank: fewest blocks per CTA (rounds of the block loop), then most CTAs per SM (warps
-    // to hide latency), then least halo per site
+    // rank, per thread count: fewest blocks per CTA (rounds of the block loop), then most
+    // CTAs per SM, then least halo per site; the two best geometries of each thread count
+    // are timed
     struct Fit {
         Cand c;
-        int bps, rounds;
+        int bps, rounds, nt;
         size_t smem;
     };
     std::vector<Fit> fits;
-    for (const Cand& c : cands) {
-        BlkGeom g = blk_geom(b, c.lbx, c.lby, c.lbz);
-        const size_t smem = 128 + g.halo_bytes + (size_t)b->tables_bytes + 4 * (size_t)((b->fp32 ? b->mf.nb : b->md.nb) + 4);
-        int bps = 0;
-        if (blk_occupancy(gen, 6, smem, &bps) != SGB_OK || bps < 1) {
-            cudaGetLastError();
-            continue;
+    for (int nt : {1024, 512, 256}) {
+        std::vector<Fit> f1;
+        for (const Cand& c : cands) {
+            if (((long long)b->na << (c.lbx + c.lby + c.lbz)) < nt) continue;
+            BlkGeom g = blk_geom(b, c.lbx, c.lby, c.lbz);
+            const size_t smem = 128 + g.halo_bytes + (size_t)b->tables_bytes + 4 * (size_t)((b->fp32 ? b->mf.nb : b->md.nb) + 4);
+            int bps = 0;
+            if (blk_occupancy(gen, 6, nt, smem, &bps) != SGB_OK || bps < 1) {
+                cudaGetLastError();
+                continue;
+            }
+            const long long grid = std::min<long long>((long long)bps * b->nsm, g.nblk);
+            const int rounds = (int)((g.nblk + grid - 1) / grid);
+            if (rounds > SGB_BLK_MAXB) continue;
+            f1.push_back({c, bps, rounds, nt, smem});
         }
-        const long long grid = std::min<long long>((long long)bps * b->nsm, g.nblk);
-        const int rounds = (int)((g.nblk + grid - 1) / grid);
-        if (rounds > SGB_BLK_MAXB) continue;
-        fits.push_back({c, bps, rounds, smem});
+        std::sort(f1.begin(), f1.end(), [](const Fit& p, const Fit& q) {
+            if (p.rounds != q.rounds) return p.rounds < q.rounds;
+            if (p.bps != q.bps) return p.bps > q.bps;
+            return p.c.cost < q.c.cost;
+        });
+        for (size_t k = 0; k < f1.size() && k < 2; k++) fits.push_back(f1[k]);
     }
-    std::sort(fits.begin(), fits.end(), [](const Fit& p, const Fit& q) {
-        if (p.rounds != q.rounds) return p.rounds < q.rounds;
-        if (p.bps != q.bps) return p.bps > q.bps;
-        return p.c.cost < q.c.cost;
-    });
     int kept = 0;
     for (const Fit& f : fits) {
-        if (kept >= 4) break;
+        if (kept >= 6) break;
         const Cand& c = f.c;
         BlkGeom g = blk_geom(b, c.lbx, c.lby, c.lbz);
         const size_t smem = f.smem;
@@ -869,6 +875,7 @@ static void blk_shapes(sgb_batch* b, bool gen, std::vector<MidShape>& out) {
             }
             MidShape sh{0, G, bps, (int)grid, smem, 0.f};
             sh.kind = 1;
+            sh.nt = f.nt;
             sh.lbx = c.lbx; sh.lby = c.lby; sh.lbz = c.lbz;
             sh.maps = (int)b->blk_maps.size() - 1;
             out.push_back(sh);
@@ -884,7 +891,7 @@ static int mid_launch(sgb_batch* b, const MidShape& sh, BatchArgs<R>& A, MidArgs
         if (sh.kind == 1) {
             const BlkGeom g = blk_geom(b, sh.lbx, sh.lby, sh.lbz);
             b->launches++;
-            if (blk_launch(GEN, sh.G, sh.grid, sh.smem, A, X, g, b->blk_maps[sh.maps], reinterpret_cast<float*>(b->Hpad), nsteps,
+            if (blk_launch(GEN, sh.G, sh.nt, sh.grid, sh.smem, A, X, g, b->blk_maps[sh.maps], reinterpret_cast<float*>(b->Hpad), nsteps,
                            dt, lam, sn, b->stream) != SGB_OK)
                 return bfail(b, SGB_ERR_CUDA, std::string("cell-block midpoint launch: ") + cudaGetErrorString(cudaGetLastError()));
             return SGB_OK;
@@ -1445,7 +1452,7 @@ int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, 
             int32_t* r = shapes + 7 * k;
             r[0] = m.idx; r[1] = m.G; r[2] = m.bps; r[3] = m.grid; r[4] = (int32_t)m.smem;
             r[5] = m.kind;
-            r[6] = m.kind ? (1 << m.lbx) | ((1 << m.lby) << 8) | ((1 << m.lbz) << 16) : 0;
+            r[6] = m.kind ? (1 << m.lbx) | ((1 << m.lby) << 8) | ((1 << m.lbz) << 16) | ((m.nt / 32) << 24) : 0;
         }
         if (ms) ms[k] = m.ms;
     }

@@ -103,8 +103,8 @@ __device__ __forceinline__ float4 load_pad(const float4* Hb, const BlkGeom& B, i
     return Hb[i];
 }
 
-template <bool GEN, int G>
-__global__ void __launch_bounds__(SGB_BLK_THREADS) k_batch_midpoint_blk(BatchArgs<float> A, MidArgs<float> X, BlkGeom B,
+template <bool GEN, int G, int NT>
+__global__ void __launch_bounds__(NT, 1) k_batch_midpoint_blk(BatchArgs<float> A, MidArgs<float> X, BlkGeom B,
                                                                          const __grid_constant__ BlkMaps maps, float4* Hpad,
                                                                          int nsteps, float dt, float lam, BSnap<float> sn) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(SGB_BLK_THREADS) k_batch_midpoint_blk(BatchArg
     __shared__ float s_kap[SGB_MAX_SUBLAT];
     __shared__ float s_h[3 * SGB_MAX_SUBLAT];
     __shared__ int4 s_blk[SGB_BLK_MAXB];          // (replica, x0, y0, z0) of each block of this CTA
-    __shared__ float wsum[SGB_BLK_THREADS / 32];
+    __shared__ float wsum[NT / 32];
     __shared__ unsigned long long conv_mask;
     const int tid = threadIdx.x;
     const int na = A.M.na, NS = A.NS;
@@ -372,29 +372,37 @@ __global__ void __launch_bounds__(SGB_BLK_THREADS) k_batch_midpoint_blk(BatchArg
     if (leader) A.ctrl->steps_done = done;
 }
 
-template <bool GEN, int G>
-void* blk_kernel() {
-    return (void*)k_batch_midpoint_blk<GEN, G>;
+template <bool GEN>
+void* blk_kernel(int nt) {
+    switch (nt) {
+        case 256: return (void*)k_batch_midpoint_blk<GEN, 6, 256>;
+        case 512: return (void*)k_batch_midpoint_blk<GEN, 6, 512>;
+        case 1024: return (void*)k_batch_midpoint_blk<GEN, 6, 1024>;
+    }
+    return nullptr;
 }
 
-void* pick(bool gen, int G) {
-    if (gen) return G == 12 ? blk_kernel<true, 12>() : blk_kernel<true, 6>();
-    return G == 12 ? blk_kernel<false, 12>() : blk_kernel<false, 6>();
+// bonds are gathered 6 at a time (G = 6) in every variant
+void* pick(bool gen, int G, int nt) {
+    if (G != 6) return nullptr;
+    return gen ? blk_kernel<true>(nt) : blk_kernel<false>(nt);
 }
 
 }  // namespace
 
-int blk_occupancy(bool gen, int G, size_t smem, int* bps) {
-    const void* k = pick(gen, G);
+int blk_occupancy(bool gen, int G, int nt, size_t smem, int* bps) {
+    const void* k = pick(gen, G, nt);
+    if (!k) return SGB_ERR_ARG;
     if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return SGB_ERR_CUDA;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, SGB_BLK_THREADS, smem) == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, nt, smem) == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
-int blk_launch(bool gen, int G, int grid, size_t smem, const BatchArgs<float>& A, const MidArgs<float>& X,
+int blk_launch(bool gen, int G, int nt, int grid, size_t smem, const BatchArgs<float>& A, const MidArgs<float>& X,
                const BlkGeom& B, const BlkMaps& maps, float* Hpad, int nsteps, float dt, float lam,
                const BSnap<float>& sn, cudaStream_t st) {
-    const void* k = pick(gen, G);
+    const void* k = pick(gen, G, nt);
+    if (!k) return SGB_ERR_ARG;
     if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return SGB_ERR_CUDA;
     BatchArgs<float> a = A;
@@ -403,8 +411,7 @@ int blk_launch(bool gen, int G, int grid, size_t smem, const BatchArgs<float>& A
     float4* hp = reinterpret_cast<float4*>(Hpad);
     BSnap<float> s = sn;
     void* args[] = {&a, &x, &b, const_cast<BlkMaps*>(&maps), &hp, &nsteps, &dt, &lam, &s};
-    return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(SGB_BLK_THREADS), args, smem, st) == cudaSuccess ? SGB_OK
-                                                                                                              : SGB_ERR_CUDA;
+    return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(nt), args, smem, st) == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
 // The 5-D tensor map of one padded buffer: (float4 component, x, y, z, replica*na + atom),

@@ -517,4 +517,45 @@ __device__ __forceinline__ void normalize_dip(R& x, R& y, R& z, R kappa) {
     x *= f; y *= f; z *= f;
 }
 
+// LocalSampler with dipole-dipole interactions (ewald_energy_delta, Ewald.jl:210-241), with
+// the field F = dE/dS of every site kept current: the change of the dipole-dipole energy
+// when the (expected) dipole of `site` changes by d is d·F_site + ½ Δμ·A[0,i,i]·Δμ with
+// Δμ = -g_site d. Writes g_site d (= -Δμ, the moved moment's change up to sign) to gd.
+// E.Areal: [(a_i na + a_j) 9 + row + 3 col][cell offset of j's cell from i's].
+__device__ __forceinline__ double ewald_site_delta(const EwaldDev& E, const double* F, int site, int ncell,
+                                                   const double d[3], double gd[3]) {
+    const double* gi = E.g + 9 * (size_t)site;
+    const int ai = site / ncell;
+    double dmu[3], ad[3];
+    for (int r = 0; r < 3; r++) dmu[r] = -(gi[r] * d[0] + gi[r + 3] * d[1] + gi[r + 6] * d[2]);
+    const size_t c0 = (size_t)((ai * E.na + ai) * 9) * ncell;
+    for (int r = 0; r < 3; r++)
+        ad[r] = E.Areal[c0 + (size_t)r * ncell] * dmu[0] + E.Areal[c0 + (size_t)(r + 3) * ncell] * dmu[1] +
+                E.Areal[c0 + (size_t)(r + 6) * ncell] * dmu[2];
+    const double* f = F + 3 * (size_t)site;
+    for (int r = 0; r < 3; r++) gd[r] = -dmu[r];
+    return d[0] * f[0] + d[1] * f[1] + d[2] * f[2] + 0.5 * (dmu[0] * ad[0] + dmu[1] * ad[1] + dmu[2] * ad[2]);
+}
+
+// After an accepted move at `site` with moment change gd = g_site ΔS, the threads of one
+// block add F_j += g_jᵀ A[cell_site - cell_j, a_j, a_site] gd to every site j's field.
+__device__ __forceinline__ void ewald_field_update(const EwaldDev& E, double* F, int site, int ns, int ncell,
+                                                   const double gd[3]) {
+    const int L1 = E.L[0], L2 = E.L[1], L3 = E.L[2], na = E.na;
+    const int as = site / ncell, cs = site % ncell;
+    const int xs = cs % L1, ys = (cs / L1) % L2, zs = cs / (L1 * L2);
+    for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+        const int aj = j / ncell, cj = j % ncell;
+        const int off = sgb_wrap_any(xs - cj % L1, L1) +
+                        L1 * (sgb_wrap_any(ys - (cj / L1) % L2, L2) + L2 * sgb_wrap_any(zs - cj / (L1 * L2), L3));
+        const size_t c0 = (size_t)((aj * na + as) * 9) * ncell + off;
+        double am[3];
+        for (int r = 0; r < 3; r++)
+            am[r] = E.Areal[c0 + (size_t)r * ncell] * gd[0] + E.Areal[c0 + (size_t)(r + 3) * ncell] * gd[1] +
+                    E.Areal[c0 + (size_t)(r + 6) * ncell] * gd[2];
+        const double* gj = E.g + 9 * (size_t)j;
+        for (int r = 0; r < 3; r++) F[3 * (size_t)j + r] += gj[3 * r] * am[0] + gj[3 * r + 1] * am[1] + gj[3 * r + 2] * am[2];
+    }
+}
+
 }  // namespace sgbdev

@@ -133,6 +133,7 @@ struct MidShape {
     int kind = 0;   // 0 tile kernel; 1 cell-block kernel with blocks of 2^lbx x 2^lby x 2^lbz cells
     int lbx = 0, lby = 0, lbz = 0;
     int maps = -1;  // cell-block kernel: its tensor maps in sgb_batch::blk_maps
+    int nt = 256;   // threads per CTA (the cell-block kernel has 256, 512 and 1024)
 };
 
 struct sgb_batch {

@@ -218,6 +218,10 @@ int ewald_launch_delta(const EwaldDev& E, const R* S, int site, const double* dS
 template <class R>
 int mc_launch_sweeps_ewald(const Model<R>& M, R* S, const McArgs& A, const EwaldDev& E, double* F, double* partials,
                            cudaStream_t st);
+// SU(N) LocalSampler with dipole-dipole: sequential proposals in A.perm order in one CTA
+template <class R>
+int sun_launch_local_sweeps_ewald(const Model<R>& M, R* Z, R* D, R* Q, const McArgs& A, const EwaldDev& E, double* F,
+                                  double* part, cudaStream_t st);
 int ewald_precompute(const EwaldGeom& G, const double* pos_d, double* A, cudaStream_t st);
 // adds the Ewald gradient into grad_aos ([ns][3], may be null) and writes EWALD_PART_BLOCKS
 // energy partials into part (may be null)

@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(256) k_local_sweeps_ewald(Model<R> M, R* S, Mc
     __shared__ int s_acc;
     __shared__ double s_d[3];
     __syncthreads();
-    const int ns = M.ns, ncell = M.ncell, L1 = M.L1, L2 = M.L2, L3 = M.L3, na = M.na;
+    const int ns = M.ns, ncell = M.ncell;
     double aE = 0, ax = 0, ay = 0, az = 0;
     for (int k = 0; k < A.nsweeps; k++) {
         const bool partial = (k == A.nsweeps - 1) && A.frac < 1.0;
@@ -267,45 +267,22 @@ __global__ void __launch_bounds__(256) k_local_sweeps_ewald(Model<R> M, R* S, Mc
                     }
                     double e = (double)mc_local_dE<R>(M, T, site, site / ncell, S, ox, oy, oz, nx, ny, nz);
                     const double d[3] = {(double)nx - (double)ox, (double)ny - (double)oy, (double)nz - (double)oz};
-                    const double* gi = E.g + 9 * (size_t)site;
-                    const int ai = site / ncell;
-                    double dmu[3], ad[3];
-                    for (int r = 0; r < 3; r++) dmu[r] = -(gi[r] * d[0] + gi[r + 3] * d[1] + gi[r + 6] * d[2]);
-                    const size_t c0 = (size_t)((ai * na + ai) * 9) * ncell;
-                    for (int r = 0; r < 3; r++)
-                        ad[r] = E.Areal[c0 + (size_t)r * ncell] * dmu[0] + E.Areal[c0 + (size_t)(r + 3) * ncell] * dmu[1] +
-                                E.Areal[c0 + (size_t)(r + 6) * ncell] * dmu[2];
-                    const double* f = F + 3 * (size_t)site;
-                    e += d[0] * f[0] + d[1] * f[1] + d[2] * f[2] + 0.5 * (dmu[0] * ad[0] + dmu[1] * ad[1] + dmu[2] * ad[2]);
+                    double gd[3];
+                    e += ewald_site_delta(E, F, site, ncell, d, gd);
                     if (A.kT == 0.0 ? (e <= 0.0) : (u[1] <= exp(-e / A.kT))) {
                         acc = 1;
                         S[site] = nx; S[ns + site] = ny; S[2 * ns + site] = nz;
                         aE += e;
                         ax += d[0]; ay += d[1]; az += d[2];
-                        // g_site ΔS, the moved moment's change up to sign, for the field update
-                        s_d[0] = -dmu[0]; s_d[1] = -dmu[1]; s_d[2] = -dmu[2];
+                        s_d[0] = gd[0]; s_d[1] = gd[1]; s_d[2] = gd[2];
                     }
                 }
                 s_acc = acc;
             }
             __syncthreads();
             if (s_acc) {
-                // F_j += g_jᵀ A[cell_site - cell_j, a_j, a_site] (g_site ΔS) for every site j
-                const int as = site / ncell, cs = site % ncell;
-                const int xs = cs % L1, ys = (cs / L1) % L2, zs = cs / (L1 * L2);
-                const double m0 = s_d[0], m1 = s_d[1], m2 = s_d[2];
-                for (int j = threadIdx.x; j < ns; j += blockDim.x) {
-                    const int aj = j / ncell, cj = j % ncell;
-                    const int off = sgb_wrap_any(xs - cj % L1, L1) + L1 * (sgb_wrap_any(ys - (cj / L1) % L2, L2) +
-                                                                          L2 * sgb_wrap_any(zs - cj / (L1 * L2), L3));
-                    const size_t c0 = (size_t)((aj * na + as) * 9) * ncell + off;
-                    double am[3];
-                    for (int r = 0; r < 3; r++)
-                        am[r] = E.Areal[c0 + (size_t)r * ncell] * m0 + E.Areal[c0 + (size_t)(r + 3) * ncell] * m1 +
-                                E.Areal[c0 + (size_t)(r + 6) * ncell] * m2;
-                    const double* gj = E.g + 9 * (size_t)j;
-                    for (int r = 0; r < 3; r++) F[3 * (size_t)j + r] += gj[3 * r] * am[0] + gj[3 * r + 1] * am[1] + gj[3 * r + 2] * am[2];
-                }
+                const double gd[3] = {s_d[0], s_d[1], s_d[2]};
+                ewald_field_update(E, F, site, ns, ncell, gd);
             }
             __syncthreads();
         }

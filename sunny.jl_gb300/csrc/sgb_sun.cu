@@ -1324,6 +1324,95 @@ __device__ inline R sun_local_dE(const Model<R>& M, const SunTab<R, N>& S, int s
 // complex normal vector, System.jl:448-452), flip_ket (Spin.jl:121-128), perturbed_spin
 // (Z + magnitude·√κ·ξ, System.jl:461-468); complex normals have E|ξ_k|² = 1 (Julia's
 // randn(ComplexF64)). Injected randoms: [sweep][ns][2N + 3].
+// One LocalSampler proposal at `site` in SU(N) mode (Samplers.jl:108-156): the proposed
+// ket zn (propose_uniform, propose_flip or propose_delta), its expected dipole sn and
+// quadrupole qn, the old values z0, s0, q0, and the short-range energy change e; u1 is the
+// acceptance uniform. Returns false when the partial last sweep skips the site.
+template <class R, int N, bool BQ, bool INJECT>
+__device__ __forceinline__ bool sun_mc_propose(const Model<R>& M, const SunTab<R, N>& S, const SpinConst<R, N>& sc,
+                                               const R* Z, const R* D, const R* Qb, const McArgs& A, int k, uint64_t sweep,
+                                               bool partial, int site, R* z0, R* zn, R* s0, R* sn, R* q0, R* qn, double& e,
+                                               double& u1) {
+    const int ns = M.ns;
+    constexpr int PER = 2 * N + 3;
+    double u[4];
+    const double* rr = nullptr;
+    if (INJECT) {
+        rr = A.rnd + ((size_t)k * ns + site) * PER;
+        u[0] = rr[2 * N]; u[1] = rr[2 * N + 1]; u[2] = rr[2 * N + 2];
+    } else {
+        sgb_mc_uniforms4(A.seed, sweep, (uint32_t)site, u);
+    }
+    if (partial && !(u[2] < A.frac)) return false;
+    u1 = u[1];
+    int kind = A.kind[A.nkind - 1];
+    double mag = A.mag[A.nkind - 1];
+    for (int i = 0; i < A.nkind - 1; i++)
+        if (u[0] < A.cum[i]) { kind = A.kind[i]; mag = A.mag[i]; break; }
+    if (kind == SGB_PROPOSE_DELTA && isinf(mag)) kind = SGB_PROPOSE_UNIFORM;
+    const R kap = M.kappa[site];
+#pragma unroll
+    for (int q = 0; q < 2 * N; q++) z0[q] = Z[(size_t)q * ns + site];
+    if (kind == SGB_PROPOSE_FLIP) {
+#pragma unroll
+        for (int q = 0; q < N; q++) {   // reverse(parity .* conj(z))
+            const R par = ((N - 1 - q) % 2) ? (R)-1 : (R)1;
+            zn[2 * q] = par * z0[2 * (N - 1 - q)];
+            zn[2 * q + 1] = -par * z0[2 * (N - 1 - q) + 1];
+        }
+    } else {
+        R g[12];
+        if (INJECT) {
+#pragma unroll
+            for (int q = 0; q < 2 * N; q++) g[q] = (R)rr[q];
+        } else {
+#pragma unroll
+            for (int blk = 0; blk < (2 * N + 3) / 4; blk++) sgb_normals4<R>(A.seed, SGB_MC_STREAM, sweep, (uint32_t)site, (uint32_t)blk, g + 4 * blk);
+#pragma unroll
+            for (int q = 0; q < 2 * N; q++) g[q] *= (R)0.70710678118654752;
+        }
+        if (kind == SGB_PROPOSE_UNIFORM) {
+#pragma unroll
+            for (int q = 0; q < 2 * N; q++) zn[q] = g[q];
+        } else {
+            const R m = (R)mag * sgb_sqrt<R>(kap);
+#pragma unroll
+            for (int q = 0; q < 2 * N; q++) zn[q] = z0[q] + m * g[q];
+        }
+        normalize_ket<R, N>(zn, kap);
+    }
+    s0[0] = D[site]; s0[1] = D[ns + site]; s0[2] = D[2 * ns + site];
+    expected_spin<R, N>(sc, zn, sn[0], sn[1], sn[2]);
+    if (BQ) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) q0[q] = Qb[(size_t)q * ns + site];
+        expected_quad<R, N>(S.qm, zn, qn);
+    }
+    e = (double)sun_local_dE<R, N, BQ>(M, S, site, D, Qb, z0, s0, q0, zn, sn, qn);
+    return true;
+}
+
+// Writes an accepted SU(N) move: ket, expected dipole and, with biquadratic or general
+// couplings, quadrupole and packed density.
+template <class R, int N, bool BQ>
+__device__ __forceinline__ void sun_mc_commit(const Model<R>& M, R* Z, R* D, R* Qb, int site, const R* zn, const R* sn,
+                                              const R* qn) {
+    const int ns = M.ns;
+#pragma unroll
+    for (int q = 0; q < 2 * N; q++) Z[(size_t)q * ns + site] = zn[q];
+    D[site] = sn[0]; D[ns + site] = sn[1]; D[2 * ns + site] = sn[2];
+    if (BQ) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) Qb[(size_t)q * ns + site] = qn[q];
+        if (M.has_general) {
+            R p[N * N];
+            sun_rho<R, N>(zn, p);
+#pragma unroll
+            for (int q = 0; q < N * N; q++) Qb[(size_t)(5 + q) * ns + site] = p[q];
+        }
+    }
+}
+
 template <class R, int N, bool BQ, bool INJECT>
 __global__ void __launch_bounds__(SGB_BLOCK) k_sun_local_sweeps(Model<R> M, R* Z, R* D, R* Qb, Ctrl* ctrl, McArgs A,
                                                                double* partials) {
@@ -1342,77 +1431,12 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_sun_local_sweeps(Model<R> M, R* Z
         for (int c = 0; c < A.ncol; c++) {
             for (int idx = A.coff[c] + blockIdx.x * blockDim.x + threadIdx.x; idx < A.coff[c + 1]; idx += nthr) {
                 const int site = A.perm[idx];
-                double u[4];
-                const double* rr = nullptr;
-                if (INJECT) {
-                    rr = A.rnd + ((size_t)k * ns + site) * PER;
-                    u[0] = rr[2 * N]; u[1] = rr[2 * N + 1]; u[2] = rr[2 * N + 2];
-                } else {
-                    sgb_mc_uniforms4(A.seed, sweep, (uint32_t)site, u);
-                }
-                if (partial && !(u[2] < A.frac)) continue;
-                int kind = A.kind[A.nkind - 1];
-                double mag = A.mag[A.nkind - 1];
-                for (int i = 0; i < A.nkind - 1; i++)
-                    if (u[0] < A.cum[i]) { kind = A.kind[i]; mag = A.mag[i]; break; }
-                if (kind == SGB_PROPOSE_DELTA && isinf(mag)) kind = SGB_PROPOSE_UNIFORM;
-                const R kap = M.kappa[site];
-                R z0[2 * N], zn[2 * N];
-#pragma unroll
-                for (int q = 0; q < 2 * N; q++) z0[q] = Z[(size_t)q * ns + site];
-                if (kind == SGB_PROPOSE_FLIP) {
-#pragma unroll
-                    for (int q = 0; q < N; q++) {   // reverse(parity .* conj(z))
-                        const R par = ((N - 1 - q) % 2) ? (R)-1 : (R)1;
-                        zn[2 * q] = par * z0[2 * (N - 1 - q)];
-                        zn[2 * q + 1] = -par * z0[2 * (N - 1 - q) + 1];
-                    }
-                } else {
-                    R g[12];
-                    if (INJECT) {
-#pragma unroll
-                        for (int q = 0; q < 2 * N; q++) g[q] = (R)rr[q];
-                    } else {
-#pragma unroll
-                        for (int blk = 0; blk < (2 * N + 3) / 4; blk++) sgb_normals4<R>(A.seed, SGB_MC_STREAM, sweep, (uint32_t)site, (uint32_t)blk, g + 4 * blk);
-#pragma unroll
-                        for (int q = 0; q < 2 * N; q++) g[q] *= (R)0.70710678118654752;
-                    }
-                    if (kind == SGB_PROPOSE_UNIFORM) {
-#pragma unroll
-                        for (int q = 0; q < 2 * N; q++) zn[q] = g[q];
-                    } else {
-                        const R m = (R)mag * sgb_sqrt<R>(kap);
-#pragma unroll
-                        for (int q = 0; q < 2 * N; q++) zn[q] = z0[q] + m * g[q];
-                    }
-                    normalize_ket<R, N>(zn, kap);
-                }
-                R s0[3], sn[3], q0[5], qn[5];
-                s0[0] = D[site]; s0[1] = D[ns + site]; s0[2] = D[2 * ns + site];
-                expected_spin<R, N>(sc, zn, sn[0], sn[1], sn[2]);
-                if (BQ) {
-#pragma unroll
-                    for (int q = 0; q < 5; q++) q0[q] = Qb[(size_t)q * ns + site];
-                    expected_quad<R, N>(S.qm, zn, qn);
-                }
-                const R dE = sun_local_dE<R, N, BQ>(M, S, site, D, Qb, z0, s0, q0, zn, sn, qn);
-                const double e = (double)dE;
-                const bool accept = A.kT == 0.0 ? (e <= 0.0) : (u[1] <= exp(-e / A.kT));
-                if (accept) {
-#pragma unroll
-                    for (int q = 0; q < 2 * N; q++) Z[(size_t)q * ns + site] = zn[q];
-                    D[site] = sn[0]; D[ns + site] = sn[1]; D[2 * ns + site] = sn[2];
-                    if (BQ) {
-#pragma unroll
-                        for (int q = 0; q < 5; q++) Qb[(size_t)q * ns + site] = qn[q];
-                        if (M.has_general) {
-                            R p[N * N];
-                            sun_rho<R, N>(zn, p);
-#pragma unroll
-                            for (int q = 0; q < N * N; q++) Qb[(size_t)(5 + q) * ns + site] = p[q];
-                        }
-                    }
+                R z0[2 * N], zn[2 * N], s0[3], sn[3], q0[5], qn[5];
+                double e, u1;
+                if (!sun_mc_propose<R, N, BQ, INJECT>(M, S, sc, Z, D, Qb, A, k, sweep, partial, site, z0, zn, s0, sn, q0, qn, e, u1))
+                    continue;
+                if (A.kT == 0.0 ? (e <= 0.0) : (u1 <= exp(-e / A.kT))) {
+                    sun_mc_commit<R, N, BQ>(M, Z, D, Qb, site, zn, sn, qn);
                     aE += e;
                     ax += (double)sn[0] - (double)s0[0];
                     ay += (double)sn[1] - (double)s0[1];
@@ -1431,6 +1455,60 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_sun_local_sweeps(Model<R> M, R* Z
         partials[4 * blockIdx.x + 1] = s0;
         partials[4 * blockIdx.x + 2] = s1;
         partials[4 * blockIdx.x + 3] = s2;
+    }
+}
+
+// Sweeps of an SU(N) system with dipole-dipole interactions: one CTA proposes at the sites
+// in the order of A.perm, one at a time (thread 0: the proposal, the short-range change and
+// the Ewald change of the expected dipole, Ewald.jl:230-241), and after an accepted move all
+// threads update every site's field F = dE/dS. Random numbers as k_sun_local_sweeps.
+template <class R, int N, bool BQ, bool INJECT>
+__global__ void __launch_bounds__(256) k_sun_local_sweeps_ewald(Model<R> M, R* Z, R* D, R* Qb, McArgs A, EwaldDev E,
+                                                                double* F, double* partials) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SunTab<R, N> S = stage_sun<R, N>(M, smem);
+    __shared__ int s_acc;
+    __shared__ double s_d[3];
+    __syncthreads();
+    SpinConst<R, N> sc;
+    const int ns = M.ns, ncell = M.ncell;
+    double aE = 0, ax = 0, ay = 0, az = 0;
+    for (int k = 0; k < A.nsweeps; k++) {
+        const bool partial = (k == A.nsweeps - 1) && A.frac < 1.0;
+        const uint64_t sweep = A.sweep0 + (uint64_t)k;
+        for (int idx = 0; idx < ns; idx++) {
+            const int site = A.perm[idx];
+            if (threadIdx.x == 0) {
+                int acc = 0;
+                R z0[2 * N], zn[2 * N], s0[3], sn[3], q0[5], qn[5];
+                double e, u1;
+                if (sun_mc_propose<R, N, BQ, INJECT>(M, S, sc, Z, D, Qb, A, k, sweep, partial, site, z0, zn, s0, sn, q0, qn, e, u1)) {
+                    const double d[3] = {(double)sn[0] - (double)s0[0], (double)sn[1] - (double)s0[1], (double)sn[2] - (double)s0[2]};
+                    double gd[3];
+                    e += ewald_site_delta(E, F, site, ncell, d, gd);
+                    if (A.kT == 0.0 ? (e <= 0.0) : (u1 <= exp(-e / A.kT))) {
+                        acc = 1;
+                        sun_mc_commit<R, N, BQ>(M, Z, D, Qb, site, zn, sn, qn);
+                        aE += e;
+                        ax += d[0]; ay += d[1]; az += d[2];
+                        s_d[0] = gd[0]; s_d[1] = gd[1]; s_d[2] = gd[2];
+                    }
+                }
+                s_acc = acc;
+            }
+            __syncthreads();
+            if (s_acc) {
+                const double gd[3] = {s_d[0], s_d[1], s_d[2]};
+                ewald_field_update(E, F, site, ns, ncell, gd);
+            }
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) {
+        partials[0] = aE;
+        partials[1] = ax;
+        partials[2] = ay;
+        partials[3] = az;
     }
 }
 
@@ -1468,6 +1546,22 @@ int sun_sweeps_n(const Model<R>& M, R* Z, R* D, R* Q, Ctrl* ctrl, const McArgs& 
     if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return SGB_ERR_CUDA;
     return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(SGB_BLOCK), args, smem, st) == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+template <class R, int N>
+int sun_sweeps_ewald_n(const Model<R>& M, R* Z, R* D, R* Q, const McArgs& A, const EwaldDev& E, double* F, double* part,
+                       cudaStream_t st) {
+    Model<R> m = M;
+    McArgs a = A;
+    EwaldDev e = E;
+    void* args[] = {&m, &Z, &D, &Q, &a, &e, &F, &part};
+    const size_t smem = (size_t)M.tables_bytes;
+    const bool bq = M.has_biquad != 0, inj = A.rnd != nullptr;
+    const void* k = bq ? (inj ? (const void*)k_sun_local_sweeps_ewald<R, N, true, true> : (const void*)k_sun_local_sweeps_ewald<R, N, true, false>)
+                       : (inj ? (const void*)k_sun_local_sweeps_ewald<R, N, false, true> : (const void*)k_sun_local_sweeps_ewald<R, N, false, false>);
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return SGB_ERR_CUDA;
+    return cudaLaunchKernel(k, dim3(1), dim3(256), args, smem, st) == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 
 template <class R, int N>
@@ -1617,6 +1711,13 @@ int sun_launch_local_sweeps(const Model<R>& M, R* Z, R* D, R* Q, Ctrl* ctrl, con
 }
 
 template <class R>
+int sun_launch_local_sweeps_ewald(const Model<R>& M, R* Z, R* D, R* Q, const McArgs& A, const EwaldDev& E, double* F,
+                                  double* part, cudaStream_t st) {
+    SGB_SUN_DISPATCH((sun_sweeps_ewald_n<R, 2>(M, Z, D, Q, A, E, F, part, st)), (sun_sweeps_ewald_n<R, 3>(M, Z, D, Q, A, E, F, part, st)),
+                     (sun_sweeps_ewald_n<R, 4>(M, Z, D, Q, A, E, F, part, st)), (sun_sweeps_ewald_n<R, 5>(M, Z, D, Q, A, E, F, part, st)))
+}
+
+template <class R>
 int sun_mc_max_blocks(const Model<R>& M, int* bps) {
     const size_t smem = (size_t)M.tables_bytes;
     SGB_SUN_DISPATCH((sun_mc_occ_n<R, 2>(smem, bps)), (sun_mc_occ_n<R, 3>(smem, bps)), (sun_mc_occ_n<R, 4>(smem, bps)),
@@ -1640,6 +1741,8 @@ int sun_launch_local_dE(const Model<R>& M, const R* Z, const R* D, const R* Q, i
     template int sun_launch_grad<R>(const Model<R>&, const R*, const R*, const R*, double*, cudaStream_t);      \
     template int sun_launch_energy<R>(const Model<R>&, const R*, const R*, const R*, double*, int, cudaStream_t); \
     template int sun_launch_local_sweeps<R>(const Model<R>&, R*, R*, R*, Ctrl*, const McArgs&, int, double*, cudaStream_t); \
+    template int sun_launch_local_sweeps_ewald<R>(const Model<R>&, R*, R*, R*, const McArgs&, const EwaldDev&, double*, \
+                                                  double*, cudaStream_t); \
     template int sun_mc_max_blocks<R>(const Model<R>&, int*);                                                    \
     template size_t sun_cluster_smem<R>(const Model<R>&, int);                                                  \
     template int sun_launch_add_dipole_field<R>(const Model<R>&, const R*, const double*, double*, cudaStream_t); \

@@ -250,10 +250,27 @@ def test_local_sweeps_with_dipole_dipole_device_rng(gpu, sg, precision):
     assert np.allclose(smp.ΔS, sg.magnetization(sys_) - M0, atol=tol * sys_.nsites)
 
 
-def test_unsupported_paths_reject_dipole_dipole(gpu, sg):
-    sys_, _ = _two_atom_box(sg, "SUN")
-    with pytest.raises(sg.SunnyGPUError, match="dipole-dipole"):
-        sg.step(sys_, sg.LocalSampler(kT=0.1))
+def test_sun_local_sweeps_with_dipole_dipole(gpu, sg, orc):
+    sys_, demag = _two_atom_box(sg, "SUN")
+    o, _ = _ewald_oracle(orc, sys_, demag, 0.4)
+    N = 3
+    Z0 = sys_.coherents_flat()
+    S0 = o.expected_spin(Z0)
+    _, col = sg.local_colors(sys_)
+    order = np.lexsort((np.arange(sys_.nsites), col))
+    rng = np.random.default_rng(12)
+    rand = np.concatenate([rng.standard_normal((2, sys_.nsites, 2 * N)) / np.sqrt(2), rng.random((2, sys_.nsites, 3))], axis=2)
+    prop = sg.mix_proposals(0.3, sg.propose_uniform, 0.3, sg.propose_flip, 0.4, sg.propose_delta(0.5))
+    smp = sg.LocalSampler(kT=0.6, nsweeps=2, propose=prop)
+    E0 = sg.energy(sys_)
+    sg.step(sys_, smp, 1, rand)
+    S_ref, Z_ref, dE_ref, dS_ref = o.local_sweeps_sun(S0, Z0, 0.6, 2, 1.0, order, prop.terms, rand)
+    Z_gpu = sys_.coherents_flat()
+    assert np.max(np.abs(Z_gpu - Z_ref)) < 1e-11
+    assert not np.allclose(Z_gpu, Z0)
+    assert smp.ΔE == pytest.approx(dE_ref, abs=1e-10 * max(1.0, abs(E0)))
+    assert np.allclose(smp.ΔS, dS_ref, atol=1e-10)
+    assert smp.ΔE == pytest.approx(sg.energy(sys_) - E0, abs=1e-10 * max(1.0, abs(E0)))
 
 
 def test_sqw_trajectory_with_dipole_dipole(gpu, sg, orc):
@@ -389,7 +406,7 @@ def test_sun_sqw_trajectory_with_dipole_dipole(gpu, sg):
     b, _ = _two_atom_box(sg, "SUN")
     sc = sg.SampledCorrelations(a, measure=sg.ssf_perp(a), energies=np.linspace(0.0, 3.0, 6), dt=0.05)
     sg.add_sample(sc, a)
-    nsteps = sc.measperiod * (sc.n_all_omega - 1)
+    nsteps = sc.measperiod * (sc.n_all_omega // 2)
     sg.step(b, sg.ImplicitMidpoint(sc.dt, tol=sc.integrator.tol), nsteps)
     assert np.array_equal(a.coherents_flat(), b.coherents_flat())
     assert np.all(np.isfinite(sc.data)) and np.max(np.abs(sc.data)) > 0
