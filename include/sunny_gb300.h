@@ -341,6 +341,14 @@ int sgb_corr_merge(sgb_corr* dst, const sgb_corr* src);
  * |Δ|² > 9s, the number with s > 0, the number of bins, and the variance of Σ(|Δ|² − s)
  * estimated from the spread of 1024 partial sums over interleaved bin sets. */
 int sgb_corr_compare(const sgb_corr* a, const sgb_corr* b, double* out);
+/* Systematic difference of two sampling paths from paired samples split into two
+ * disjoint halves (no counterpart in the reference): a1/b1 hold the first half's samples
+ * on paths a and b (from the same starts), a2/b2 the second half's, all with
+ * calculate_errors. out[0] = Σ_bins Re[(a1 − b1)·conj(a2 − b2)], whose expectation is the
+ * squared systematic difference summed over bins (the halves' noise is independent);
+ * out[1] = Σ_bins |(b1 + b2)/2|²; out[2] = the variance of out[0] estimated from the spread
+ * of its partial sums over interleaved bin sets. */
+int sgb_corr_cross(const sgb_corr* a1, const sgb_corr* b1, const sgb_corr* a2, const sgb_corr* b2, double* out);
 
 /* Per-phase device time of add_sample!, summed over the samples taken while profiling is
  * on (CUDA events between phases; no Julia analogue): ms4[0] trajectory with snapshots,
@@ -356,6 +364,15 @@ int sgb_corr_phase_times(sgb_corr* sc, double* ms4, int64_t* nsamples_timed, int
  * together. Couplings (onsite + bonds) are shared by all replicas; dims differ.
  * dims: int32[nrep][3]; natoms, mode, precision from `proto`. */
 int  sgb_batch_create(const sgb_desc* proto, int32_t nrep, const int32_t* dims, sgb_batch** out);
+/* A replica group: a batch whose nrep (1..64) replicas are whole systems of one mode,
+ * precision, device and dims, SU(N) included (the clones that Sunny's ParallelTempering
+ * makes, ParallelTempering.jl:20-37; no counterpart for batched sampling). The systems
+ * stay owned by the caller and must outlive the batch; their couplings and states are
+ * set through the system entry points. Langevin (member r draws noise with seed + r),
+ * energies and batched add_sample! run every member concurrently, each on its own stream
+ * with an equal share of the SMs. Replica exchange over systems is done by the caller
+ * (sgb_batch_exchange and sgb_batch_step_ensemble return SGB_ERR_ARG for a group). */
+int  sgb_batch_create_group(sgb_system* const* systems, int32_t nrep, sgb_batch** out);
 void sgb_batch_destroy(sgb_batch* b);
 const char* sgb_batch_last_error(const sgb_batch* b);
 int64_t sgb_batch_nsites(const sgb_batch* b, int32_t rep);

@@ -16,7 +16,7 @@ from .system import (System, Moment, Langevin, ImplicitMidpoint, step, energy, e
                      clone_system, to_inhomogeneous, set_exchange_at, set_onsite_coupling_at,
                      set_vacancy_at, remove_periodicity, minimize_energy, MinimizationResult, enable_dipole_dipole)
 from .correlations import (SampledCorrelations, MeasureSpec, ssf_trace, ssf_perp, ssf_custom, add_sample,
-                           merge_correlations, compare_correlations, available_energies, available_wave_vectors,
+                           merge_correlations, compare_correlations, systematic_difference, available_energies, available_wave_vectors,
                            adjusted_dt_and_downsampling_factor, all_dipole_observables, intensities,
                            intensities_static, Intensities)
 from .tempering import ReplicaBatch, ParallelTempering, SystemParallelTempering, exchange_round

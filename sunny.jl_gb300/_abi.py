@@ -96,9 +96,11 @@ SIGNATURES = {
     "sgb_corr_intensities": (C.c_int, [_P, _I32, C.POINTER(_I32), _D, _D, _I32, C.POINTER(_I32), _I32, _D]),
     "sgb_corr_merge": (C.c_int, [_P, _P]),
     "sgb_corr_compare": (C.c_int, [_P, _P, _D]),
+    "sgb_corr_cross": (C.c_int, [_P, _P, _P, _P, _D]),
     "sgb_corr_profile": (C.c_int, [_P, _I32]),
     "sgb_corr_phase_times": (C.c_int, [_P, _D, C.POINTER(_I64), C.POINTER(_I64)]),
     "sgb_batch_create": (C.c_int, [C.POINTER(Desc), _I32, C.POINTER(_I32), C.POINTER(_P)]),
+    "sgb_batch_create_group": (C.c_int, [C.POINTER(_P), _I32, C.POINTER(_P)]),
     "sgb_batch_destroy": (None, [_P]),
     "sgb_batch_last_error": (C.c_char_p, [_P]),
     "sgb_batch_nsites": (_I64, [_P, _I32]),

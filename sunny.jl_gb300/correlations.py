@@ -210,7 +210,9 @@ def add_sample(sc: SampledCorrelations, sys, window: str = "cosine"):
         raise ValueError("a GPU SampledCorrelations is bound to the System it was created with")
     w = {"cosine": 0, "rectangular": 1}[window]
     if sc._batch is not None:
+        sc._batch._sync_members()
         sc._check(sc._lib.sgb_corr_add_sample(sc._h, w))
+        sc._batch._touch()
         return
     sys._sync_to_device()
     rc = sys._lib.sgb_corr_add_sample(sc._h, w)
@@ -277,6 +279,28 @@ def compare_correlations(sc_a: SampledCorrelations, sc_b: SampledCorrelations) -
             "bias_rel": math.sqrt(max(0.0, d2 - s) / mb2) if mb2 > 0 else math.nan,
             "rms_ratio": math.sqrt(ma2 / mb2) if mb2 > 0 else math.nan,
             "bins": int(nbins), "samples": (sc_a.nsamples, sc_b.nsamples)}
+
+
+def systematic_difference(a1: SampledCorrelations, b1: SampledCorrelations, a2: SampledCorrelations,
+                          b2: SampledCorrelations) -> dict:
+    """Systematic per-bin difference between two sampling paths a and b (no counterpart in
+    the reference), from paired samples split into two halves of disjoint starts: a1/b1
+    hold the first half on each path, a2/b2 the second (calculate_errors on all four).
+    With D_h = mean_a_h − mean_b_h per bin, E[Re Σ D1·conj(D2)] is the squared systematic
+    difference summed over bins, since the halves' noise is independent. Returns
+      bias_rel        √(max(0, Σ Re D1·conj(D2)) / Σ|mean_b|²), the RMS systematic
+                      difference relative to the RMS bin;
+      bias_rel_upper  the same with the cross sum raised by two of its standard deviations
+                      (estimated from partial sums over interleaved bin sets);
+      cross_rel2      the cross sum over Σ|mean_b|² (may be negative by noise)."""
+    out = np.zeros(3)
+    a1._check(a1._lib.sgb_corr_cross(a1._h, b1._h, a2._h, b2._h, _abi.dptr(out)))
+    t0, t1, var = out
+    sd = math.sqrt(max(var, 0.0))
+    return {"bias_rel": math.sqrt(max(0.0, t0) / t1) if t1 > 0 else math.nan,
+            "bias_rel_upper": math.sqrt(max(0.0, t0 + 2 * sd) / t1) if t1 > 0 else math.nan,
+            "cross_rel2": t0 / t1 if t1 > 0 else math.nan,
+            "cross_rel2_sd": sd / t1 if t1 > 0 else math.nan}
 
 
 def merge_host(datas, counts, Ms=None):

@@ -318,19 +318,21 @@ int plan_launch(sgb_system* s, LaunchInfo& li) {
     int nspt = s->sun ? 2 : 4;
     size_t smem = (size_t)s->tables_bytes;
     LaunchInfo fallback{0, 0, 0, 0};
+    // a system of a replica group shares the GPU with the group's other members
+    const int nsm = std::max(1, s->nsm / std::max(1, s->conc));
     for (int i = 0; i < nspt; i++) {
         int spt = sptv[i];
         int maxblock = sgb_maxblock(sizeof(R) == 8, s->sun, spt);
-        long long per_sm = ((long long)s->ns + (long long)s->nsm * spt - 1) / ((long long)s->nsm * spt);
+        long long per_sm = ((long long)s->ns + (long long)nsm * spt - 1) / ((long long)nsm * spt);
         int block = (int)std::min<long long>(maxblock, std::max<long long>(128, (per_sm + 31) / 32 * 32));
         int bps = 0;
         int rc = s->sun ? sun_max_blocks<R>(s->N, spt, block, smem, &bps) : dip_max_blocks<R>(spt, block, smem, &bps);
         if (rc != SGB_OK) return fail(s, SGB_ERR_CUDA, "occupancy query failed");
-        long long cap = (long long)bps * s->nsm;
+        long long cap = (long long)bps * nsm;
         long long need = ((long long)s->ns + (long long)block * spt - 1) / ((long long)block * spt);
         if (need < 1 || need > cap) continue;
         LaunchInfo cand{(int)need, block, spt, smem};
-        if (need <= s->nsm) { li = cand; return SGB_OK; }   // at most one block per SM
+        if (need <= nsm) { li = cand; return SGB_OK; }   // at most one block per SM
         if (fallback.grid == 0) fallback = cand;
     }
     if (fallback.grid) { li = fallback; return SGB_OK; }
@@ -446,7 +448,8 @@ int tune_heun(sgb_system* s, const LaunchInfo& li, double dt, double damping, do
 }
 
 template <class R>
-int run_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t seed, uint64_t step0, int nsteps, const double* noise) {
+int run_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t seed, uint64_t step0, int nsteps, const double* noise,
+                 bool sync = true) {
     LaunchInfo li;
     int rc = plan_launch<R>(s, li);
     if (rc) return rc;
@@ -477,6 +480,7 @@ int run_langevin(sgb_system* s, double dt, double damping, double kT, uint64_t s
                                     seed, step0 + k0, dn, li, s->stream);
         s->launches++;
         if (rc) return cuda_fail(s, cudaGetLastError(), "Langevin launch");
+        if (!sync && !noise) return SGB_OK;   // the caller reads the status
         Ctrl c;
         if ((rc = read_ctrl(s, &c))) return rc;
         if (c.status == SGB_ERR_TIMEOUT) return fail(s, SGB_ERR_TIMEOUT, "a device-side barrier timed out");
@@ -966,6 +970,151 @@ int run_local_sweeps(sgb_system* s, McArgs& A, const double* rnd_host, double* o
 }
 
 }  // namespace
+
+
+// ---------------------------------------------------------------------------------
+// Replica groups: a batch whose replicas are whole systems (any mode, SU(N) included,
+// with inhomogeneous, general or dipole-dipole couplings), each with its own stream. The
+// members' persistent launches are sized for an equal share of the SMs and issued
+// back to back, so the replicas advance concurrently; the batch stream waits for them.
+// ---------------------------------------------------------------------------------
+static int bfail_ext(sgb_batch* b, int code, const std::string& msg) {
+    b->err = msg;
+    return code;
+}
+
+static int group_fork(sgb_batch* b) {
+    if (cudaEventRecord(b->gfork, b->stream) != cudaSuccess) return bfail_ext(b, SGB_ERR_CUDA, "event record failed");
+    for (sgb_system* s : b->grp)
+        if (cudaStreamWaitEvent(s->stream, b->gfork, 0) != cudaSuccess) return bfail_ext(b, SGB_ERR_CUDA, "stream wait failed");
+    return SGB_OK;
+}
+
+static int group_join(sgb_batch* b) {
+    for (size_t r = 0; r < b->grp.size(); r++) {
+        if (cudaEventRecord(b->gev[r], b->grp[r]->stream) != cudaSuccess ||
+            cudaStreamWaitEvent(b->stream, b->gev[r], 0) != cudaSuccess)
+            return bfail_ext(b, SGB_ERR_CUDA, "stream join failed");
+    }
+    return SGB_OK;
+}
+
+// restores every member's SM share when a group operation ends
+struct GroupShare {
+    sgb_batch* b;
+    explicit GroupShare(sgb_batch* bb) : b(bb) {
+        for (sgb_system* s : b->grp) s->conc = (int)b->grp.size();
+    }
+    ~GroupShare() {
+        for (sgb_system* s : b->grp) s->conc = 1;
+    }
+};
+
+static int group_member_ready(sgb_batch* b, sgb_system* s) {
+    int rc = ensure_tables(s);
+    if (rc) return bfail_ext(b, rc, s->err);
+    if (!s->state_set) return bfail_ext(b, SGB_ERR_STATE, "every member system needs a state");
+    if (s->d.device != b->proto.device) return bfail_ext(b, SGB_ERR_ARG, "members must share one device");
+    return SGB_OK;
+}
+
+// Langevin on every member at the batch's kT (member r draws its noise with seed + r)
+int group_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, uint64_t step0, int nsteps) {
+    GroupShare share(b);
+    int rc = group_fork(b);
+    if (rc) return rc;
+    const int R = (int)b->grp.size();
+    std::vector<char> launched(R, 0);
+    for (int r = 0; r < R; r++) {
+        sgb_system* s = b->grp[r];
+        if ((rc = group_member_ready(b, s))) return rc;
+        const double kT = b->kT_h[r];
+        const uint64_t sd = seed + (uint64_t)r;
+        if (s->ewald_on) {
+            rc = s->sun ? (s->fp32 ? run_langevin_lr_sun<float>(s, dt, damping, kT, sd, step0, nsteps, nullptr)
+                                   : run_langevin_lr_sun<double>(s, dt, damping, kT, sd, step0, nsteps, nullptr))
+                        : (s->fp32 ? run_langevin_lr<float>(s, dt, damping, kT, sd, step0, nsteps, nullptr)
+                                   : run_langevin_lr<double>(s, dt, damping, kT, sd, step0, nsteps, nullptr));
+        } else {
+            rc = s->fp32 ? run_langevin<float>(s, dt, damping, kT, sd, step0, nsteps, nullptr, false)
+                         : run_langevin<double>(s, dt, damping, kT, sd, step0, nsteps, nullptr, false);
+            launched[r] = 1;
+        }
+        if (rc) return bfail_ext(b, rc, s->err);
+    }
+    for (int r = 0; r < R; r++) {
+        if (!launched[r]) continue;
+        sgb_system* s = b->grp[r];
+        Ctrl c;
+        if ((rc = read_ctrl(s, &c))) return bfail_ext(b, rc, s->err);
+        if (c.status == SGB_ERR_TIMEOUT) return bfail_ext(b, SGB_ERR_TIMEOUT, "a device-side barrier timed out");
+        if (c.status != 0) return bfail_ext(b, c.status, "Langevin kernel reported an error");
+    }
+    return group_join(b);
+}
+
+int group_energy(sgb_batch* b, double* E) {
+    for (size_t r = 0; r < b->grp.size(); r++) {
+        sgb_system* s = b->grp[r];
+        int rc = group_member_ready(b, s);
+        if (rc) return rc;
+        if ((rc = sgb_energy(s, &E[r], nullptr))) return bfail_ext(b, rc, s->err);
+    }
+    return SGB_OK;
+}
+
+// Trajectories of a batched add_sample!: member r runs the implicit midpoint with its
+// snapshots written to replica r's rows of the accumulator's time series.
+int group_trajectory(sgb_corr* c) {
+    sgb_batch* b = c->batch;
+    GroupShare share(b);
+    int rc = group_fork(b);
+    if (rc) return rc;
+    const int R = (int)b->grp.size();
+    const int nsteps = c->measperiod * (c->nsnaps - 1);
+    const size_t rep_stride = (size_t)c->nomega * c->nobs * c->npos * c->ncell;
+    const double scale = 1.0 / std::sqrt((double)c->ncell);
+    std::vector<char> launched(R, 0);
+    int64_t total = 0;
+    for (int r = 0; r < R; r++) {
+        sgb_system* s = b->grp[r];
+        if ((rc = group_member_ready(b, s))) return rc;
+        int64_t it = 0;
+        if (s->fp32) {
+            SnapArgs<float> sn{1, c->nobs, c->measperiod, 0, (const float*)c->ops, (float*)c->A + 2 * rep_stride * r, (float)scale};
+            if (s->ewald_on) rc = s->sun ? run_midpoint_lr_sun<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &it, &sn)
+                                         : run_midpoint_lr<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &it, &sn);
+            else if (nsteps > 0) rc = run_midpoint<float>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, nullptr, sn, false, s->mid_order);
+            else rc = run_midpoint<float>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, false);
+        } else {
+            SnapArgs<double> sn{1, c->nobs, c->measperiod, 0, (const double*)c->ops, (double*)c->A + 2 * rep_stride * r, scale};
+            if (s->ewald_on) rc = s->sun ? run_midpoint_lr_sun<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &it, &sn)
+                                         : run_midpoint_lr<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, &it, &sn);
+            else if (nsteps > 0) rc = run_midpoint<double>(s, c->dt, c->damping, c->tol, c->max_iters, nsteps, nullptr, sn, false, s->mid_order);
+            else rc = run_midpoint<double>(s, 1.0, 0.0, 1e300, 1, 0, nullptr, sn, false);
+        }
+        if (rc) return bfail_ext(b, rc, s->err);
+        if (s->ewald_on) total += it;
+        else launched[r] = 1;
+    }
+    for (int r = 0; r < R; r++) {
+        if (!launched[r]) continue;
+        sgb_system* s = b->grp[r];
+        Ctrl st;
+        if ((rc = read_ctrl(s, &st))) return bfail_ext(b, rc, s->err);
+        total += st.iters;
+        if (st.status == SGB_ERR_NOCONVERGE) {
+            const std::string m = s->sun ? "Schrödinger midpoint method failed to converge in " + std::to_string(c->max_iters) + " iterations."
+                                         : "Spherical midpoint method failed to converge to tolerance " + fmt_g(c->tol) + " after " +
+                                               std::to_string(c->max_iters) + " iterations.";
+            return bfail_ext(b, SGB_ERR_NOCONVERGE, m);
+        }
+        if (st.status == SGB_ERR_TIMEOUT) return bfail_ext(b, SGB_ERR_TIMEOUT, "a device-side barrier timed out");
+        if (st.status != 0) return bfail_ext(b, st.status, "midpoint kernel reported an error");
+    }
+    c->prof_iters_last = total;
+    return group_join(b);
+}
 
 // ---------------------------------------------------------------------------------
 // C ABI
@@ -1995,6 +2144,19 @@ int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* d, sgb_corr** out) 
         for (int k = 0; k < 3; k++)
             if (b->dims[3 * r + k] != b->dims[k]) { b->err = "batched sampling needs replicas of equal size"; return SGB_ERR_ARG; }
     if (!b->coup_set) { b->err = "couplings must be set first"; return SGB_ERR_STATE; }
+    if (!b->grp.empty()) {
+        sgb_system* s0 = b->grp[0];
+        if ((rc = ensure_tables(s0))) { b->err = s0->err; return rc; }
+        sgb_corr* c = new sgb_corr();
+        c->batch = b;
+        c->stream = b->stream;
+        c->launches = &b->launches;
+        rc = corr_setup(c, d, b->fp32, s0->sun, s0->N, s0->ns, b->na, b->dims.data(), b->nrep);
+        if (rc) { b->err = c->err; sgb_corr_destroy(c); return rc; }
+        b->corrs.push_back(c);
+        *out = c;
+        return SGB_OK;
+    }
     const size_t R = b->fp32 ? 4 : 8;
     auto lazy = [&](void** p, size_t bytes) -> int {
         if (*p) return SGB_OK;
@@ -2416,6 +2578,39 @@ int sgb_corr_compare(const sgb_corr* a, const sgb_corr* b, double* out) {
         v += d * d;
     }
     out[8] = G * v / (G - 1);
+    return SGB_OK;
+}
+
+int sgb_corr_cross(const sgb_corr* a1, const sgb_corr* b1, const sgb_corr* a2, const sgb_corr* b2, double* out) {
+    if (!a1 || !b1 || !a2 || !b2 || !out) return fail(nullptr, SGB_ERR_ARG, "null argument");
+    sgb_corr* ca = const_cast<sgb_corr*>(a1);
+    for (const sgb_corr* c : {b1, a2, b2})
+        if (c->plen != a1->plen || c->nomega != a1->nomega || c->ncorr != a1->ncorr || c->npos != a1->npos)
+            return cfail(ca, SGB_ERR_ARG, "accumulators have different shapes");
+    for (const sgb_corr* c : {a1, b1, a2, b2})
+        if (!c->welford) return cfail(ca, SGB_ERR_ARG, "the accumulators need calculate_errors (per-sample means)");
+    for (const sgb_corr* c : {b1, a2, b2})
+        if (c->stream != a1->stream) cudaStreamSynchronize(c->stream);
+    double* part = nullptr;
+    if (cudaMalloc((void**)&part, sizeof(double) * 2 * SGB_CMP_BLOCKS) != cudaSuccess)
+        return cfail(ca, SGB_ERR_NOMEM, "device allocation failed");
+    int rc = corr_launch_cross_diff(a1->P, b1->P, a2->P, b2->P, a1->plen, part, a1->stream);
+    (*ca->launches)++;
+    std::vector<double> h(2 * SGB_CMP_BLOCKS);
+    cudaError_t e = rc == SGB_OK ? cudaMemcpyAsync(h.data(), part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, a1->stream)
+                                 : cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(a1->stream);
+    cudaFree(part);
+    if (rc != SGB_OK || e != cudaSuccess) return cfail(ca, SGB_ERR_CUDA, std::string("cross: ") + cudaGetErrorString(e));
+    double t0 = 0, t1 = 0;
+    for (int q = 0; q < SGB_CMP_BLOCKS; q++) { t0 += h[2 * q]; t1 += h[2 * q + 1]; }
+    // variance of the cross sum from the spread of the per-block partial sums
+    const double G = SGB_CMP_BLOCKS, mean = t0 / G;
+    double v = 0;
+    for (int q = 0; q < SGB_CMP_BLOCKS; q++) v += (h[2 * q] - mean) * (h[2 * q] - mean);
+    out[0] = t0;
+    out[1] = t1;
+    out[2] = G * v / (G - 1);
     return SGB_OK;
 }
 

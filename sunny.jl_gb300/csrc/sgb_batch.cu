@@ -995,6 +995,7 @@ static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
 
 int batch_corr_trajectory(sgb_corr* c) {
     sgb_batch* b = c->batch;
+    if (!b->grp.empty()) return group_trajectory(c);
     return b->fp32 ? batch_trajectory<float>(c, b) : batch_trajectory<double>(c, b);
 }
 
@@ -1025,8 +1026,55 @@ void sgb_batch_destroy(sgb_batch* b) {
     p = b->counters; bfree(p); p = b->n_accept; bfree(p);
     if (b->stage) cudaFreeHost(b->stage);
     for (int i = 0; i < 8; i++) if (b->ev[i]) cudaEventDestroy(b->ev[i]);
+    for (cudaEvent_t e : b->gev) if (e) cudaEventDestroy(e);
+    if (b->gfork) cudaEventDestroy(b->gfork);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
+}
+
+int sgb_batch_create_group(sgb_system* const* systems, int32_t nrep, sgb_batch** out) {
+    if (!systems || !out || nrep < 1 || nrep > 64) return bfail(nullptr, SGB_ERR_ARG, "a replica group has 1 to 64 systems");
+    *out = nullptr;
+    const sgb_system* s0 = systems[0];
+    if (!s0) return bfail(nullptr, SGB_ERR_ARG, "null system");
+    for (int r = 0; r < nrep; r++) {
+        const sgb_system* s = systems[r];
+        if (!s) return bfail(nullptr, SGB_ERR_ARG, "null system");
+        if (s->d.mode != s0->d.mode || s->N != s0->N || s->fp32 != s0->fp32 || s->d.natoms != s0->d.natoms ||
+            s->d.device != s0->d.device || s->d.dims[0] != s0->d.dims[0] || s->d.dims[1] != s0->d.dims[1] ||
+            s->d.dims[2] != s0->d.dims[2])
+            return bfail(nullptr, SGB_ERR_ARG, "the systems of a replica group must share mode, precision, device and dims");
+        for (int q = 0; q < r; q++)
+            if (systems[q] == s) return bfail(nullptr, SGB_ERR_ARG, "a system appears twice in the replica group");
+    }
+    sgb_batch* b = new sgb_batch();
+    b->proto = s0->d;
+    b->nrep = nrep;
+    b->na = s0->d.natoms;
+    b->fp32 = s0->fp32;
+    b->nsm = s0->nsm;
+    b->grp.assign(systems, systems + nrep);
+    b->dims.clear();
+    b->off.assign(nrep + 1, 0);
+    for (int r = 0; r < nrep; r++) {
+        for (int k = 0; k < 3; k++) b->dims.push_back(s0->d.dims[k]);
+        b->off[r + 1] = b->off[r] + s0->ns;
+    }
+    b->NS = b->off[nrep];
+    b->nsr_max = s0->ns;
+    b->kT_h.assign(nrep, 0.0);
+    b->coup_set = true;
+    b->state_set = true;
+    auto bad = [&]() { std::string m = b->err; b->grp.clear(); sgb_batch_destroy(b); g_batch_error = m; return SGB_ERR_CUDA; };
+    if (cudaSetDevice(s0->d.device) != cudaSuccess) { bfail(b, SGB_ERR_CUDA, "cudaSetDevice failed"); return bad(); }
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) { bfail(b, SGB_ERR_CUDA, "stream"); return bad(); }
+    for (int i = 0; i < 8; i++) cudaEventCreate(&b->ev[i]);
+    b->gev.assign(nrep, nullptr);
+    for (int r = 0; r < nrep; r++)
+        if (cudaEventCreateWithFlags(&b->gev[r], cudaEventDisableTiming) != cudaSuccess) { bfail(b, SGB_ERR_CUDA, "event"); return bad(); }
+    if (cudaEventCreateWithFlags(&b->gfork, cudaEventDisableTiming) != cudaSuccess) { bfail(b, SGB_ERR_CUDA, "event"); return bad(); }
+    *out = b;
+    return SGB_OK;
 }
 
 int sgb_batch_create(const sgb_desc* d, int32_t nrep, const int32_t* dims, sgb_batch** out) {
@@ -1259,6 +1307,12 @@ int sgb_batch_set_couplings(sgb_batch* b, const double* kappa, const double* g, 
 
 int sgb_batch_set_state(sgb_batch* b, int32_t rep, const double* dip) {
     if (!b || !dip || rep < 0 || rep >= b->nrep) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    if (!b->grp.empty()) {
+        sgb_system* s = b->grp[rep];
+        if (s->sun) return bfail(b, SGB_ERR_ARG, "set the coherent states of the member system");
+        const int rc = sgb_set_state(s, dip, nullptr);
+        return rc ? bfail(b, rc, s->err) : SGB_OK;
+    }
     const int ns = b->off[rep + 1] - b->off[rep], NS = b->NS, o = b->off[rep];
     size_t R = bsize(b);
     int rc = ensure_bstage(b, R * 3 * ns);
@@ -1277,6 +1331,11 @@ int sgb_batch_set_state(sgb_batch* b, int32_t rep, const double* dip) {
 
 int sgb_batch_get_state(sgb_batch* b, int32_t rep, double* dip) {
     if (!b || !dip || rep < 0 || rep >= b->nrep) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    if (!b->grp.empty()) {
+        sgb_system* s = b->grp[rep];
+        const int rc = sgb_get_state(s, dip, nullptr);   // SU(N): the expected dipoles
+        return rc ? bfail(b, rc, s->err) : SGB_OK;
+    }
     const int ns = b->off[rep + 1] - b->off[rep], NS = b->NS, o = b->off[rep];
     size_t R = bsize(b);
     int rc = ensure_bstage(b, R * 3 * ns);
@@ -1295,6 +1354,7 @@ int sgb_batch_set_kT(sgb_batch* b, const double* kT) {
     for (int r = 0; r < b->nrep; r++)
         if (!(kT[r] >= 0)) return bfail(b, SGB_ERR_ARG, "Select nonnegative kT");
     b->kT_h.assign(kT, kT + b->nrep);
+    if (!b->grp.empty()) return SGB_OK;
     BCK(cudaMemcpy(b->kT, kT, sizeof(double) * b->nrep, cudaMemcpyHostToDevice));
     if (b->fp32) {
         std::vector<float> f(kT, kT + b->nrep);
@@ -1307,6 +1367,10 @@ int sgb_batch_set_kT(sgb_batch* b, const double* kT) {
 
 int sgb_batch_get_kT(sgb_batch* b, double* kT) {
     if (!b || !kT) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    if (!b->grp.empty()) {
+        for (int r = 0; r < b->nrep; r++) kT[r] = b->kT_h[r];
+        return SGB_OK;
+    }
     BCK(cudaMemcpyAsync(kT, b->kT, sizeof(double) * b->nrep, cudaMemcpyDeviceToHost, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
     return SGB_OK;
@@ -1319,6 +1383,7 @@ int sgb_batch_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, u
     if (damping < 0) return bfail(b, SGB_ERR_ARG, "Select positive damping");
     if (!b->coup_set || !b->state_set) return bfail(b, SGB_ERR_STATE, "couplings and states must be set first");
     if (nsteps <= 0) return nsteps == 0 ? SGB_OK : bfail(b, SGB_ERR_ARG, "nsteps must be nonnegative");
+    if (!b->grp.empty()) return group_langevin(b, dt, damping, seed, step0, nsteps);
     unsigned long long s0 = step0;
     BCK(cudaMemcpyAsync(b->counters, &s0, sizeof(s0), cudaMemcpyHostToDevice, b->stream));
     BCK(cudaMemsetAsync(b->ctrl, 0, sgb_ctrl_clear_bytes(), b->stream));
@@ -1332,6 +1397,11 @@ int sgb_batch_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, u
 
 int sgb_batch_langevin_noise(sgb_batch* b, int32_t rep, uint64_t seed, uint64_t step, double* out) {
     if (!b || !out || rep < 0 || rep >= b->nrep) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    if (!b->grp.empty()) {   // member r draws with seed + r
+        sgb_system* s = b->grp[rep];
+        const int rc = sgb_langevin_noise(s, seed + (uint64_t)rep, step, out);
+        return rc ? bfail(b, rc, s->err) : SGB_OK;
+    }
     const int ns = b->off[rep + 1] - b->off[rep];
     double* d = nullptr;
     if (bmalloc(b, (void**)&d, sizeof(double) * 3 * ns)) return SGB_ERR_NOMEM;
@@ -1348,6 +1418,7 @@ int sgb_batch_langevin_noise(sgb_batch* b, int32_t rep, uint64_t seed, uint64_t 
 int sgb_batch_energy(sgb_batch* b, double* E) {
     if (!b || !E) return bfail(b, SGB_ERR_ARG, "invalid arguments");
     if (!b->coup_set) return bfail(b, SGB_ERR_STATE, "couplings must be set first");
+    if (!b->grp.empty()) return group_energy(b, E);
     int rc = b->fp32 ? enqueue_energy<float>(b) : enqueue_energy<double>(b);
     if (rc) return rc;
     BCK(cudaMemcpyAsync(E, b->E, sizeof(double) * b->nrep, cudaMemcpyDeviceToHost, b->stream));
@@ -1358,6 +1429,7 @@ int sgb_batch_energy(sgb_batch* b, double* E) {
 int sgb_batch_exchange(sgb_batch* b, int32_t exch_start, uint64_t seed, uint64_t round, const double* uniforms,
                        int64_t* n_accept) {
     if (!b || (exch_start != 1 && exch_start != 2)) return bfail(b, SGB_ERR_ARG, "exch_start must be 1 or 2");
+    if (!b->grp.empty()) return bfail(b, SGB_ERR_ARG, "replica exchange over systems runs through ParallelTempering(system, sampler, kT_sched)");
     if (!b->coup_set) return bfail(b, SGB_ERR_STATE, "couplings must be set first");
     int rc = b->fp32 ? enqueue_energy<float>(b) : enqueue_energy<double>(b);
     if (rc) return rc;
@@ -1381,6 +1453,7 @@ int sgb_batch_exchange(sgb_batch* b, int32_t exch_start, uint64_t seed, uint64_t
 int sgb_batch_step_ensemble(sgb_batch* b, double dt, double damping, uint64_t seed, int32_t nsteps, int32_t exch_interval,
                             int64_t* n_accept) {
     if (!b || exch_interval < 1 || nsteps < 0) return bfail(b, SGB_ERR_ARG, "invalid arguments");
+    if (!b->grp.empty()) return bfail(b, SGB_ERR_ARG, "replica exchange over systems runs through ParallelTempering(system, sampler, kT_sched)");
     if (damping <= 0 || !(dt > 0)) return bfail(b, SGB_ERR_ARG, "Select positive dt and damping");
     if (!b->coup_set || !b->state_set) return bfail(b, SGB_ERR_STATE, "couplings and states must be set first");
     const int n_exch = (nsteps + exch_interval - 1) / exch_interval;
@@ -1440,6 +1513,7 @@ int sgb_batch_set_midpoint_predictor(sgb_batch* b, int32_t order) {
     if (!b) return bfail(nullptr, SGB_ERR_ARG, "null handle");
     if (order < 0 || order > 4) return bfail(b, SGB_ERR_ARG, "predictor order must be in 0..4");
     b->mid_order = order;
+    for (sgb_system* s : b->grp) s->mid_order = order;
     return SGB_OK;
 }
 
@@ -1476,6 +1550,13 @@ int sgb_batch_set_wait_limit(sgb_batch* b, double seconds) {
         b->err = "wait limit must be in [0, 3600] s (0: the 4 s default)";
         return SGB_ERR_ARG;
     }
+    if (!b->grp.empty()) {
+        for (sgb_system* s : b->grp) {
+            const int rc = sgb_set_wait_limit(s, seconds);
+            if (rc) return bfail(b, rc, s->err);
+        }
+        return SGB_OK;
+    }
     const unsigned long long ns = (unsigned long long)(seconds * 1e9);
     BCK(cudaMemcpyAsync(&b->ctrl->wait_ns, &ns, sizeof(ns), cudaMemcpyHostToDevice, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
@@ -1495,6 +1576,11 @@ int sgb_batch_event_elapsed(sgb_batch* b, int32_t a, int32_t c, float* ms) {
     return SGB_OK;
 }
 
-int64_t sgb_batch_kernel_launches(const sgb_batch* b) { return b ? b->launches : 0; }
+int64_t sgb_batch_kernel_launches(const sgb_batch* b) {
+    if (!b) return 0;
+    int64_t n = b->launches;
+    for (const sgb_system* s : b->grp) n += s->launches;
+    return n;
+}
 
 }  // extern "C"

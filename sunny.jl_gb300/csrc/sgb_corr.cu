@@ -442,6 +442,36 @@ __global__ void k_compare_welford(const double2* __restrict__ ma, const double* 
     }
 }
 
+// Cross term of two independent paired differences, bin by bin: Δ1 = a1 − b1 and Δ2 = a2 − b2
+// from disjoint sets of paired samples have independent noise, so E[Re Δ1·conj(Δ2)] is the
+// squared systematic difference alone. Each block writes 2 partial sums: Σ Re Δ1·conj(Δ2)
+// and Σ|(b1 + b2)/2|². Launched with 256 threads.
+__global__ void k_cross_diff(const double2* __restrict__ a1, const double2* __restrict__ b1, const double2* __restrict__ a2,
+                             const double2* __restrict__ b2, size_t len, double* __restrict__ part) {
+    double acc0 = 0, acc1 = 0;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < len; e += (size_t)gridDim.x * blockDim.x) {
+        const double2 x1 = a1[e], y1 = b1[e], x2 = a2[e], y2 = b2[e];
+        const double d1x = x1.x - y1.x, d1y = x1.y - y1.y, d2x = x2.x - y2.x, d2y = x2.y - y2.y;
+        acc0 += d1x * d2x + d1y * d2y;
+        const double mx = 0.5 * (y1.x + y2.x), my = 0.5 * (y1.y + y2.y);
+        acc1 += mx * mx + my * my;
+    }
+    __shared__ double red[8][2];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        acc0 += __shfl_down_sync(0xffffffffu, acc0, o);
+        acc1 += __shfl_down_sync(0xffffffffu, acc1, o);
+    }
+    if (l == 0) { red[w][0] = acc0; red[w][1] = acc1; }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        double t = 0;
+        for (int q = 0; q < 8; q++) t += red[q][threadIdx.x];
+        part[(size_t)blockIdx.x * 2 + threadIdx.x] = t;
+    }
+}
+
 // Columns of the accumulator belonging to the wave vectors qidx[0..nq): the B = ncorr*npos^2
 // columns of wave vector q are [q*B, (q+1)*B). tmp[k*B + b][ω] = scale * P[ω][qidx[k]*B + b].
 __global__ void k_gather_qcols(const double2* __restrict__ P, size_t ld, const int* __restrict__ qidx, int nq, int B,
@@ -525,6 +555,14 @@ int corr_launch_compare_welford(const double* ma, const double* Ma, const double
                                 size_t len, double* part, cudaStream_t st) {
     k_compare_welford<<<SGB_CMP_BLOCKS, 256, 0, st>>>(reinterpret_cast<const double2*>(ma), Ma,
                                                        reinterpret_cast<const double2*>(mb), Mb, fa, fb, len, part);
+    return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+int corr_launch_cross_diff(const double* a1, const double* b1, const double* a2, const double* b2, size_t len, double* part,
+                           cudaStream_t st) {
+    k_cross_diff<<<SGB_CMP_BLOCKS, 256, 0, st>>>(reinterpret_cast<const double2*>(a1), reinterpret_cast<const double2*>(b1),
+                                                  reinterpret_cast<const double2*>(a2), reinterpret_cast<const double2*>(b2), len,
+                                                  part);
     return cudaGetLastError() == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
 }
 

@@ -26,6 +26,8 @@ int corr_launch_merge_welford(double* d1, double* M1, const double* d2, const do
 #define SGB_CMP_BLOCKS 1024
 int corr_launch_compare_welford(const double* ma, const double* Ma, const double* mb, const double* Mb, double fa, double fb,
                                 size_t len, double* part, cudaStream_t st);
+int corr_launch_cross_diff(const double* a1, const double* b1, const double* a2, const double* b2, size_t len, double* part,
+                           cudaStream_t st);
 // intensities: gather the columns of a list of wave vectors; phase averaging + combiner
 int corr_launch_gather_q(const double* P, size_t ld, const int* qidx, int nq, int B, int n, double scale, double* tmp,
                          cudaStream_t st);

@@ -77,6 +77,8 @@ struct sgb_system {
     // Langevin on small dipole lattices: -1 not yet timed, 0 persistent grid, cs > 0 a
     // cluster of cs CTAs holding the lattice in distributed shared memory
     int heun_cluster = -1;
+    int conc = 1;               // systems launched concurrently with this one (replica groups): the
+                                // persistent grids are sized for nsm / conc SMs
     bool heun_forced = false;        // set by sgb_set_langevin_cluster
     cudaEvent_t tev[2] = {};         // events of the kernel-choice timing (not the user's slots)
 };
@@ -198,6 +200,11 @@ struct sgb_batch {
     void* H2 = nullptr;
     void* H3 = nullptr;
     int mid_order = 0;              // initial-iterate extrapolation order of the batched midpoint
+    // replica group (sgb_batch_create_group): the replicas are whole systems owned by the
+    // caller, advanced together on their own streams; empty for an ordinary batch
+    std::vector<sgb_system*> grp;
+    std::vector<cudaEvent_t> gev;   // [nrep] join events
+    cudaEvent_t gfork = nullptr;
     double* racc = nullptr;         // [3][nrep] convergence sums
     Ctrl* ctrl = nullptr;
     double* Epart = nullptr;        // [ntiles]
@@ -236,3 +243,9 @@ int sgb_int_midpoint_snap(sgb_system* s, double dt, double tol, int max_iters, i
 void sgb_int_window_weights(int n, int window, std::vector<double>& g);
 int sgb_int_ensure_tables(sgb_system* s);
 void sgb_int_set_error(const std::string& msg);
+
+// Replica groups (sgb_api.cu): Langevin, energies and batched S(q,w) trajectories of a
+// batch whose replicas are whole systems.
+int group_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, uint64_t step0, int nsteps);
+int group_energy(sgb_batch* b, double* E);
+int group_trajectory(sgb_corr* c);

@@ -896,15 +896,15 @@ def remove_periodicity(sys: System, flags):
     sys.remove_periodicity(flags)
 
 
-def clone_system(sys: System, seed=None) -> System:
+def clone_system(sys: System, seed=None, device="same", precision=None) -> System:
     """clone_system(sys) (System.jl:144-175): a new System with copies of the couplings,
-    κ, g, field and state, on the same device. Sunny copies the RNG; the clone keeps
-    sys.seed and its counters unless `seed` is given."""
+    κ, g, field and state, on the same device (or `device`, in `precision`). Sunny copies
+    the RNG; the clone keeps sys.seed and its counters unless `seed` is given."""
     if sys._h is not None:
         sys._sync_to_host()
     mom =[(i + 1, m) for i, m in enumerate(sys.moments)]
     c = System(sys.crystal, mom, sys.mode, sys.dims, seed=sys.seed if seed is None else seed,
-               precision=sys.precision, device=sys.device)
+               precision=precision or sys.precision, device=sys.device if device == "same" else device)
     c._kappa[:] = sys._kappa
     c._g[:] = sys._g
     c._field[:] = sys._field

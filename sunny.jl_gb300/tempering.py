@@ -19,21 +19,30 @@ from .system import System, LocalSampler, clone_system, energy, magnetization, s
 
 
 class ReplicaBatch:
-    N = 0  # dipole modes only
+    """Replicas of a prototype System advanced together.
+
+    Dipole-mode prototypes with per-sublattice couplings become one batch of concatenated
+    states (replicas may differ in dims) driven by persistent batch kernels. Any other
+    prototype (SU(N) mode, dipole-dipole interactions, inhomogeneous or general
+    couplings) becomes a replica group: `nrep` device clones of the prototype
+    (clone_system, as ParallelTempering.jl:20-37 makes them) whose persistent launches run
+    concurrently, each on its own stream with an equal share of the SMs; replicas then
+    have the prototype's dims, and `members[r]` is replica r's System."""
 
     def __init__(self, proto: System, dims_list, kT=None, precision: str | None = None, device: int = 0, seed: int = 0):
-        if proto.N:
-            raise ValueError("replica batches support the dipole modes")
-        if getattr(proto, "_ewald", None) is not None:
-            raise ValueError("replica batches do not support dipole-dipole interactions")
         self.proto = proto
         self.dims_list = [tuple(int(x) for x in d) for d in dims_list]
         self.nrep = len(self.dims_list)
         self.natoms = proto.natoms
+        self.N = proto.N
         self.precision = precision or proto.precision
         self.seed = int(seed)
         self.noise_step = 0
         self._lib = _abi.load()
+        self.members = None
+        if proto.N or getattr(proto, "_ewald", None) is not None or proto._site_pairs is not None or proto._general:
+            self._init_group(device, kT)
+            return
         d = _abi.Desc()
         d.dims[:] = self.dims_list[0]
         d.natoms, d.N = proto.natoms, 0
@@ -49,6 +58,34 @@ class ReplicaBatch:
         self.kT = np.zeros(self.nrep) if kT is None else np.asarray(kT, dtype=float)
         self.set_kT(self.kT)
 
+    def _init_group(self, device, kT):
+        if any(d != self.proto.dims for d in self.dims_list):
+            raise ValueError("a replica group (SU(N) mode, dipole-dipole, inhomogeneous or general couplings) "
+                             "needs replicas with the prototype's dims")
+        self.members = [clone_system(self.proto, seed=self.seed + r, device=device, precision=self.precision)
+                        for r in range(self.nrep)]
+        for m in self.members:
+            m._sync_to_device()
+        hs = (C.c_void_p * self.nrep)(*[m.handle.value if isinstance(m.handle, C.c_void_p) else m.handle
+                                        for m in self.members])
+        h = C.c_void_p()
+        self._check(self._lib.sgb_batch_create_group(hs, self.nrep, C.byref(h)), None)
+        self._h = h
+        self.rng = np.random.default_rng(self.seed)
+        self.kT = np.zeros(self.nrep) if kT is None else np.asarray(kT, dtype=float)
+        self.set_kT(self.kT)
+
+    def _touch(self):
+        """The members' device states changed: their host copies refresh on next read."""
+        if self.members:
+            for m in self.members:
+                m._dev_newer = True
+
+    def _sync_members(self):
+        if self.members:
+            for m in self.members:
+                m._sync_to_device()
+
     def _check(self, rc, h="self"):
         if rc != _abi.SGB_OK:
             hh = self._h if h == "self" else h
@@ -59,6 +96,9 @@ class ReplicaBatch:
         if getattr(self, "_h", None):
             self._lib.sgb_batch_destroy(self._h)
             self._h = None
+        for m in getattr(self, "members", None) or []:
+            m.close()
+        self.members = None
 
     def __del__(self):
         try:
@@ -99,16 +139,34 @@ class ReplicaBatch:
         self._check(self._lib.sgb_batch_get_kT(self._h, _abi.dptr(out)))
         return out
 
-    def set_state(self, r: int, dipoles: np.ndarray):
-        self._check(self._lib.sgb_batch_set_state(self._h, r, _abi.dptr(np.ascontiguousarray(dipoles, dtype=float).reshape(-1))))
+    def set_state(self, r: int, state: np.ndarray):
+        """Replica r's dipoles (ns, 3), or in SU(N) mode its coherent states (ns, N)."""
+        if self.members:
+            m = self.members[r]
+            if m.N:
+                m.set_state_flat(coherents=state)
+            else:
+                m.set_state_flat(dipoles=state)
+            m._sync_to_device()
+            return
+        self._check(self._lib.sgb_batch_set_state(self._h, r, _abi.dptr(np.ascontiguousarray(state, dtype=float).reshape(-1))))
 
     def get_state(self, r: int) -> np.ndarray:
+        """Replica r's dipoles (ns, 3), or in SU(N) mode its coherent states (ns, N)."""
+        if self.members:
+            m = self.members[r]
+            return m.coherents_flat() if m.N else m.dipoles_flat()
         out = np.zeros((self.nsites(r), 3))
         self._check(self._lib.sgb_batch_get_state(self._h, r, _abi.dptr(out)))
         return out
 
     def randomize_spins(self):
         """randomize_spins! on every replica (System.jl:513-517)."""
+        if self.members:
+            for m in self.members:
+                m.randomize_spins()
+                m._sync_to_device()
+            return
         for r in range(self.nrep):
             ns = self.nsites(r)
             v = self.rng.standard_normal((ns, 3))
@@ -116,10 +174,16 @@ class ReplicaBatch:
             self.set_state(r, kap[:, None] * v / np.linalg.norm(v, axis=1)[:, None])
 
     def langevin(self, dt: float, damping: float, nsteps: int):
+        self._sync_members()
         self._check(self._lib.sgb_batch_langevin(self._h, dt, damping, self.seed, self.noise_step, nsteps))
+        self._touch()
         self.noise_step += nsteps
 
     def noise(self, r: int, step: int) -> np.ndarray:
+        if self.members and self.N:
+            out = np.zeros((self.nsites(r), self.N, 2))
+            self._check(self._lib.sgb_batch_langevin_noise(self._h, r, self.seed, step, _abi.dptr(out)))
+            return out[..., 0] + 1j * out[..., 1]
         out = np.zeros((self.nsites(r), 3))
         self._check(self._lib.sgb_batch_langevin_noise(self._h, r, self.seed, step, _abi.dptr(out)))
         return out
@@ -136,6 +200,7 @@ class ReplicaBatch:
         self._check(self._lib.sgb_batch_set_midpoint_predictor(self._h, int(order)))
 
     def energies(self) -> np.ndarray:
+        self._sync_members()
         out = np.zeros(self.nrep)
         self._check(self._lib.sgb_batch_energy(self._h, _abi.dptr(out)))
         return out

@@ -6,7 +6,9 @@ sample at tol 1e-6 with the degree-4 first iterate.
 Limits (the workload's stated error): the energy changes by at most 1e-5 relative over a
 sample's trajectory (the exact dynamics conserve it), and the FP32 and FP64 S(q,ω) agree
 bin by bin within their Welford error bars (CorrelationSampling.jl:117-134) with a
-systematic RMS difference below 1 % of the RMS bin."""
+systematic RMS difference below 1 % of the RMS bin. Two trajectories from one start
+separate by chaos whatever the arithmetic, so the systematic part is estimated from two
+halves of disjoint starts, whose paired differences have independent noise."""
 import numpy as np
 import pytest
 
@@ -22,14 +24,15 @@ def test_fp32_batched_error_against_fp64_at_benchmark_time_axis(gpu, sg):
     assert r["energy_rel_err_per_sample_max"] <= 1e-5
     assert r["fp64_energy_rel_err_per_sample_max"] <= 1e-5
     assert r["energy_rel_err_per_sample_median"] <= 3 * r["fp64_energy_rel_err_per_sample_median"] + 1e-7
-    cmp = r["sqw_vs_fp64"]
-    assert cmp["samples"] == (32, 32)
-    # paired starts: the difference stays within the error bars, and its RMS over the bins,
-    # an upper bound of the systematic per-bin error, is below 1 % of the RMS bin
-    assert cmp["chi2_ratio"] <= 1.0
-    assert cmp["frac_z_gt_3"] < 2e-3
-    assert cmp["rel_rms_diff"] <= 1e-2
-    assert abs(cmp["rms_ratio"] - 1) <= 1e-2
+    for cmp in r["sqw_vs_fp64_halves"]:
+        assert cmp["samples"] == (16, 16)
+        # paired starts: the difference stays within the error bars
+        assert cmp["chi2_ratio"] <= 1.0
+        assert cmp["frac_z_gt_3"] < 2e-3
+        assert abs(cmp["rms_ratio"] - 1) <= 2e-2
+    # the systematic per-bin difference, with two standard deviations of its estimate, is
+    # below 1 % of the RMS bin
+    assert r["sqw_systematic_rel_rms_upper"] <= 1e-2
 
 
 def test_fp32_batched_energy_error_per_step(gpu, sg):

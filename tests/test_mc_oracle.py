@@ -125,11 +125,12 @@ def test_oracle_sun_local_sweeps_bookkeeping(sg, orc):
     assert np.allclose(dS, S1.sum(0) - S0.sum(0), atol=1e-10)
 
 
-def test_replica_batch_rejects_dipole_dipole(sg):
+def test_replica_group_needs_prototype_dims(sg):
+    # with dipole-dipole interactions a ReplicaBatch is a group of clones of the prototype
     s = sc_c1(sg, L=4, device=None)
     s.enable_dipole_dipole(1.0)
-    with pytest.raises(ValueError, match="dipole-dipole"):
-        sg.ReplicaBatch(s, [s.dims] * 2, kT=[0.1, 0.2])
+    with pytest.raises(ValueError, match="prototype's dims"):
+        sg.ReplicaBatch(s, [s.dims, (2, 2, 2)], kT=[0.1, 0.2])
 
 
 def test_enable_dipole_dipole_host_settings(sg):
