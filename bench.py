@@ -330,9 +330,15 @@ def run_tempering(sg, device, nsteps=20000, exch_interval=100, seed=2024):
     lib.sgb_batch_event_elapsed(b.handle, 0, 1, C.byref(ms))
     nsites = int(sum(int(L) ** 3 for L in Ls))
     acc = pt.n_accept.sum()
+    hms = (C.c_float * 3)()
+    hb = C.c_int32(0)
+    lib.sgb_batch_langevin_shapes(b.handle, hms, C.byref(hb))
     out = {"site_steps_per_s": nsites * nsteps / (ms.value / 1000.0), "ms": ms.value, "steps": nsteps,
            "replicas": 256, "total_sites": nsites, "graph": pt.graph_active, "accepted_swaps": int(acc),
-           "us_per_step": 1000.0 * ms.value / nsteps}
+           "us_per_step": 1000.0 * ms.value / nsteps,
+           "langevin_autotune": {"ctas_per_sm": hb.value,
+                                 "tune_ms_10_steps": {str(k): (None if hms[i] >= 1e29 else round(hms[i], 4))
+                                                      for i, k in enumerate((4, 3, 2))}}}
     b.close()
     return out
 

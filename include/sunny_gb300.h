@@ -435,6 +435,11 @@ int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, 
 /* Uses row `row` of sgb_batch_midpoint_shapes for the following batched trajectories, or
  * -1 to time the shapes again at the next one (no counterpart in the reference). */
 int sgb_batch_select_midpoint_shape(sgb_batch* b, int32_t row);
+/* The batched Langevin kernel's launch shapes (no counterpart in the reference): 4, 3 and
+ * 2 CTAs per SM, timed once per couplings on 10 steps at the first Langevin call (FP32;
+ * FP64 batches use 2). ms3[k] receives shape k's tuning time (0 not tried, 1e30 does not
+ * fit), *chosen_bps the CTAs per SM in use (0 before tuning). Returns 3. */
+int sgb_batch_langevin_shapes(const sgb_batch* b, float* ms3, int32_t* chosen_bps);
 
 /* ---- adjoint: S(q,ω) loss gradient through a midpoint trajectory ------------ */
 /* No reverse rule exists in the reference; parameters follow the labelled-parameter

@@ -86,9 +86,10 @@ __device__ __forceinline__ void batch_noise(uint64_t seed, int r, uint64_t step,
     x = g4[0] * scale; y = g4[1] * scale; z = g4[2] * scale;
 }
 
-// Heun over every replica (Integrators.jl:313-332); each replica uses its own kT.
-template <class R, bool GEN>
-__global__ void __launch_bounds__(SGB_TILE, sizeof(R) == 4 ? 3 : 2) k_batch_heun(BatchArgs<R> A, const R* kTR, int nsteps, R dt,
+// Heun over every replica (Integrators.jl:313-332); each replica uses its own kT. MB: CTAs
+// per SM the registers are budgeted for (the launch shape the tuner picks).
+template <class R, bool GEN, int MB>
+__global__ void __launch_bounds__(SGB_TILE, MB) k_batch_heun(BatchArgs<R> A, const R* kTR, int nsteps, R dt,
                                                             R lam, uint64_t seed, unsigned long long* counters) {
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(A.M, smem);
@@ -280,8 +281,8 @@ __global__ void k_batch_noise(int ns, int rep, uint64_t seed, uint64_t step, dou
 // site's own spins and its neighbours' midpoint spins, fetched G bonds at a time.
 // IDX 2 keeps indices as uint16 (replicas of at most 65,536 sites), IDX 4 as int32,
 // IDX 0 reads them from the global table. G is the number of bonds gathered together.
-template <class R, bool GEN, int IDX, int G>
-__global__ void __launch_bounds__(SGB_TILE, (sizeof(R) == 4 && G <= 6) ? 3 : 2) k_batch_midpoint(BatchArgs<R> A, MidArgs<R> X, int nsteps, R dt,
+template <class R, bool GEN, int IDX, int G, int MB>
+__global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A, MidArgs<R> X, int nsteps, R dt,
                                                                 R lam, BSnap<R> sn, int kb) {
     using IT = typename std::conditional<IDX == 2, unsigned short, int>::type;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -621,20 +622,79 @@ int read_status(sgb_batch* b, Ctrl* out) {
 }
 
 template <class R>
+const void* heun_kernel(bool gen, int bps) {
+    if (sizeof(R) == 4 && bps >= 4) return gen ? (const void*)k_batch_heun<R, true, 4> : (const void*)k_batch_heun<R, false, 4>;
+    if (sizeof(R) == 4 && bps == 3) return gen ? (const void*)k_batch_heun<R, true, 3> : (const void*)k_batch_heun<R, false, 3>;
+    return gen ? (const void*)k_batch_heun<R, true, 2> : (const void*)k_batch_heun<R, false, 2>;
+}
+
+int heun_fit(sgb_batch* b, const void* k, size_t smem, int* bps) {
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return SGB_ERR_CUDA;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, SGB_TILE, smem) == cudaSuccess ? SGB_OK : SGB_ERR_CUDA;
+}
+
+template <class R>
 int enqueue_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, int nsteps) {
     BatchArgs<R> A = bargs<R>(b);
-    int grid = 0;
     size_t smem = (size_t)b->tables_bytes;
     const R* kTR = reinterpret_cast<const R*>(b->kTR);
     unsigned long long* ctr = b->counters;
     R rdt = (R)dt, rlam = (R)damping;
     void* args[] = {&A, &kTR, &nsteps, &rdt, &rlam, &seed, &ctr};
-    if (A.M.general) {
-        int rc = bgrid(b, k_batch_heun<R, true>, smem, 0, &grid);
-        return rc ? rc : bcoop(b, k_batch_heun<R, true>, grid, smem, args);
+    const int bps = b->heun_bps > 0 ? b->heun_bps : (sizeof(R) == 4 ? 3 : 2);
+    const void* k = heun_kernel<R>(A.M.general != 0, bps);
+    int fit = 0;
+    if (heun_fit(b, k, smem, &fit) || fit < 1) return bfail(b, SGB_ERR_CUDA, "occupancy query failed");
+    const int grid = (int)std::max<long long>(1, std::min<long long>((long long)std::min(bps, fit) * b->nsm, b->ntiles));
+    return bcoop(b, k, grid, smem, args);
+}
+
+// Times the batched Langevin launch shapes (4, 3 or 2 CTAs per SM in FP32; FP64 has one)
+// on 10 steps each, the replicas' states and the step counter saved and restored around
+// the runs, and keeps the fastest for these couplings.
+template <class R>
+int tune_langevin(sgb_batch* b, double dt, double damping, uint64_t seed) {
+    if (b->heun_bps > 0) return SGB_OK;
+    const int cand[3] = {4, 3, 2};
+    if (sizeof(R) == 8) { b->heun_bps = 2; return SGB_OK; }
+    const size_t bytes = bsize(b) * 3 * (size_t)b->NS;
+    void* save = nullptr;
+    if (bmalloc(b, &save, bytes)) return SGB_ERR_NOMEM;
+    unsigned long long ctr0 = 0;
+    BCK(cudaMemcpyAsync(&ctr0, b->counters, sizeof(ctr0), cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaMemcpyAsync(save, b->S, bytes, cudaMemcpyDeviceToDevice, b->stream));
+    int best = -1;
+    for (int v = 0; v < 3; v++) {
+        b->heun_bps = cand[v];
+        int fit = 0;
+        if (heun_fit(b, heun_kernel<R>(b->mf.general != 0 || b->md.general != 0, cand[v]), (size_t)b->tables_bytes, &fit) || fit < cand[v]) {
+            cudaGetLastError();
+            b->heun_ms[v] = 1e30f;
+            continue;
+        }
+        float ms = 0.f;
+        bool ok = true;
+        for (int rep = 0; rep < 2 && ok; rep++) {   // the first repetition warms up
+            ok = cudaMemsetAsync(b->ctrl, 0, sgb_ctrl_clear_bytes(), b->stream) == cudaSuccess &&
+                 cudaEventRecord(b->ev[6], b->stream) == cudaSuccess && enqueue_langevin<R>(b, dt, damping, seed, 10) == SGB_OK &&
+                 cudaEventRecord(b->ev[7], b->stream) == cudaSuccess && cudaEventSynchronize(b->ev[7]) == cudaSuccess &&
+                 cudaEventElapsedTime(&ms, b->ev[6], b->ev[7]) == cudaSuccess &&
+                 cudaMemcpyAsync(b->S, save, bytes, cudaMemcpyDeviceToDevice, b->stream) == cudaSuccess &&
+                 cudaMemcpyAsync(b->counters, &ctr0, sizeof(ctr0), cudaMemcpyHostToDevice, b->stream) == cudaSuccess;
+        }
+        Ctrl st;
+        if (read_status(b, &st) != SGB_OK || st.status != 0) ok = false;
+        b->heun_ms[v] = ok ? ms : 1e30f;
+        if (!ok) cudaGetLastError();
+        if (ok && (best < 0 || ms < b->heun_ms[best])) best = v;
     }
-    int rc = bgrid(b, k_batch_heun<R, false>, smem, 0, &grid);
-    return rc ? rc : bcoop(b, k_batch_heun<R, false>, grid, smem, args);
+    cudaStreamSynchronize(b->stream);
+    bfree(save);
+    BCK(cudaMemsetAsync(b->ctrl, 0, sgb_ctrl_clear_bytes(), b->stream));
+    if (best < 0) return bfail(b, SGB_ERR_CUDA, "no batched Langevin launch shape ran");
+    b->heun_bps = cand[best];
+    return SGB_OK;
 }
 
 template <class R>
@@ -714,12 +774,24 @@ template <class R>
 using MidKernel = void (*)(BatchArgs<R>, MidArgs<R>, int, R, R, BSnap<R>, int);
 
 template <class R, bool GEN>
-static MidKernel<R> mid_kernel(int idx, int G) {
-    // G = 6 runs 3 CTAs per SM within 80 registers; G = 12 keeps twice as many neighbour
-    // loads in flight per thread and runs 2 CTAs per SM within 128 registers (no spills)
-    if (idx == 2) return G == 12 ? k_batch_midpoint<R, GEN, 2, 12> : k_batch_midpoint<R, GEN, 2, 6>;
-    if (idx == 4) return G == 12 ? k_batch_midpoint<R, GEN, 4, 12> : k_batch_midpoint<R, GEN, 4, 6>;
-    return G == 12 ? k_batch_midpoint<R, GEN, 0, 12> : k_batch_midpoint<R, GEN, 0, 6>;
+static MidKernel<R> mid_kernel(int idx, int G, int bps) {
+    // G = 6 runs 3 CTAs per SM within 80 registers, or in FP32 4 CTAs per SM within 64
+    // (a few spilled bytes); G = 12 keeps twice as many neighbour loads in flight per thread
+    // and runs 2 CTAs per SM within 128 registers (no spills)
+    constexpr int M6 = sizeof(R) == 4 ? 3 : 2;
+    if (G == 12) {
+        if (idx == 2) return k_batch_midpoint<R, GEN, 2, 12, 2>;
+        if (idx == 4) return k_batch_midpoint<R, GEN, 4, 12, 2>;
+        return k_batch_midpoint<R, GEN, 0, 12, 2>;
+    }
+    if (sizeof(R) == 4 && bps >= 4) {
+        if (idx == 2) return k_batch_midpoint<R, GEN, 2, 6, 4>;
+        if (idx == 4) return k_batch_midpoint<R, GEN, 4, 6, 4>;
+        return k_batch_midpoint<R, GEN, 0, 6, 4>;
+    }
+    if (idx == 2) return k_batch_midpoint<R, GEN, 2, 6, M6>;
+    if (idx == 4) return k_batch_midpoint<R, GEN, 4, 6, M6>;
+    return k_batch_midpoint<R, GEN, 0, 6, M6>;
 }
 
 static void blk_shapes(sgb_batch* b, bool gen, std::vector<MidShape>& out);
@@ -729,17 +801,17 @@ static int mid_shapes(sgb_batch* b, std::vector<MidShape>& out) {
     out.clear();
     const size_t tab = (size_t)b->tables_bytes;
     const int isz = b->nsr_max <= 65536 ? 2 : 4;
-    const int maxbps = sizeof(R) == 4 ? 3 : 2;
+    const int maxbps = sizeof(R) == 4 ? 4 : 2;
     for (int idx : {isz, 0}) {
         if (idx != 0 && b->kb == 0) continue;
         for (int G : {6, 12}) {
             const int top = G == 12 ? 2 : maxbps;
-            for (int bps = top; bps >= std::max(1, top - 1); bps--) {
+            for (int bps = top; bps >= std::max(1, top - (top == 4 ? 2 : 1)); bps--) {
                 const long long g = std::min<long long>((long long)bps * b->nsm, b->ntiles);
                 const long long ntb = (b->ntiles + g - 1) / g;
                 if (ntb > SGB_MAXT) continue;
                 const size_t smem = tab + (idx ? (size_t)ntb * b->kb * SGB_TILE * idx : 0);
-                MidKernel<R> kern = mid_kernel<R, GEN>(idx, G);
+                MidKernel<R> kern = mid_kernel<R, GEN>(idx, G, bps);
                 if (smem > 48 * 1024 &&
                     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
                     cudaGetLastError();
@@ -899,7 +971,7 @@ static int mid_launch(sgb_batch* b, const MidShape& sh, BatchArgs<R>& A, MidArgs
     }
     int kb = b->kb;
     void* args[] = {&A, &X, &nsteps, &dt, &lam, &sn, &kb};
-    return bcoop(b, mid_kernel<R, GEN>(sh.idx, sh.G), sh.grid, sh.smem, args);
+    return bcoop(b, mid_kernel<R, GEN>(sh.idx, sh.G, sh.bps), sh.grid, sh.smem, args);
 }
 
 template <class R, bool GEN>
@@ -1301,6 +1373,8 @@ int sgb_batch_set_couplings(sgb_batch* b, const double* kappa, const double* g, 
     for (Model<double>* m : {&b->md}) { m->tables = (const unsigned char*)b->tables; m->dipole_mode = 1; m->na = na; }
     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
     b->mid_choice = -1;
+    b->heun_bps = 0;
+    for (float& m : b->heun_ms) m = 0.f;
     b->coup_set = true;
     return SGB_OK;
 }
@@ -1384,10 +1458,12 @@ int sgb_batch_langevin(sgb_batch* b, double dt, double damping, uint64_t seed, u
     if (!b->coup_set || !b->state_set) return bfail(b, SGB_ERR_STATE, "couplings and states must be set first");
     if (nsteps <= 0) return nsteps == 0 ? SGB_OK : bfail(b, SGB_ERR_ARG, "nsteps must be nonnegative");
     if (!b->grp.empty()) return group_langevin(b, dt, damping, seed, step0, nsteps);
+    int rc = b->fp32 ? tune_langevin<float>(b, dt, damping, seed) : tune_langevin<double>(b, dt, damping, seed);
+    if (rc) return rc;
     unsigned long long s0 = step0;
     BCK(cudaMemcpyAsync(b->counters, &s0, sizeof(s0), cudaMemcpyHostToDevice, b->stream));
     BCK(cudaMemsetAsync(b->ctrl, 0, sgb_ctrl_clear_bytes(), b->stream));
-    int rc = b->fp32 ? enqueue_langevin<float>(b, dt, damping, seed, nsteps) : enqueue_langevin<double>(b, dt, damping, seed, nsteps);
+    rc = b->fp32 ? enqueue_langevin<float>(b, dt, damping, seed, nsteps) : enqueue_langevin<double>(b, dt, damping, seed, nsteps);
     if (rc) return rc;
     Ctrl st;
     if ((rc = read_status(b, &st))) return rc;
@@ -1457,7 +1533,8 @@ int sgb_batch_step_ensemble(sgb_batch* b, double dt, double damping, uint64_t se
     if (damping <= 0 || !(dt > 0)) return bfail(b, SGB_ERR_ARG, "Select positive dt and damping");
     if (!b->coup_set || !b->state_set) return bfail(b, SGB_ERR_STATE, "couplings and states must be set first");
     const int n_exch = (nsteps + exch_interval - 1) / exch_interval;
-    int rc = SGB_OK;
+    int rc = b->fp32 ? tune_langevin<float>(b, dt, damping, seed) : tune_langevin<double>(b, dt, damping, seed);
+    if (rc) return rc;
     BCK(cudaMemsetAsync(b->ctrl, 0, sgb_ctrl_clear_bytes(), b->stream));
     BCK(cudaMemsetAsync(b->counters + 1, 0, sizeof(unsigned long long), b->stream));
     const bool reuse = b->graph && b->graph_interval == exch_interval && b->graph_dt == dt && b->graph_damping == damping &&
@@ -1532,6 +1609,14 @@ int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, 
     }
     if (chosen) *chosen = b->mid_choice;
     return n;
+}
+
+int sgb_batch_langevin_shapes(const sgb_batch* b, float* ms3, int32_t* chosen_bps) {
+    if (!b) return SGB_ERR_ARG;
+    if (ms3)
+        for (int k = 0; k < 3; k++) ms3[k] = b->heun_ms[k];
+    if (chosen_bps) *chosen_bps = b->heun_bps;
+    return 3;
 }
 
 int sgb_batch_select_midpoint_shape(sgb_batch* b, int32_t row) {

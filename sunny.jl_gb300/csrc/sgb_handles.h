@@ -188,6 +188,10 @@ struct sgb_batch {
     int blk_gw = 0;                 // their ghost width (largest bond offset)
     std::vector<BlkMaps> blk_maps;  // tensor maps of the cell-block shapes
     int mid_choice = -1;            // shape picked by the autotuner (-1: not tuned for these couplings)
+    // batched Langevin launch shapes: CTAs per SM 4, 3, 2 (FP32) or 2 (FP64), timed once per
+    // couplings; heun_ms[k] the time of shape k's tuning run (0: not tried, 1e30: does not fit)
+    int heun_bps = 0;               // 0: not tuned
+    float heun_ms[3] = {0, 0, 0};
     // state
     void* S = nullptr;
     void* P = nullptr;

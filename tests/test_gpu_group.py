@@ -39,7 +39,7 @@ def test_sun_group_sample_equals_per_replica_samples(gpu, sg, precision):
     b.randomize_spins()
     b.langevin(0.02, 0.1, 100)
     starts = [b.get_state(r) for r in range(R)]
-    kw = dict(energies=np.linspace(0, 4.0, 8), dt=0.05)
+    kw = dict(energies=np.linspace(0, 4.0, 8), dt=0.05, tol=1e-12 if precision == "fp64" else 1e-6)
     sc = sg.SampledCorrelations(b, measure=sg.ssf_perp(proto), **kw)
     sg.add_sample(sc, b)
     ends = [b.get_state(r) for r in range(R)]
@@ -66,7 +66,7 @@ def test_triangular_su3_group_runs_concurrently(gpu, sg):
     b = sg.ReplicaBatch(proto, [proto.dims] * 8, kT=[0.3] * 8, seed=2, precision="fp32")
     b.randomize_spins()
     b.langevin(0.02, 0.1, 50)
-    sc = sg.SampledCorrelations(b, measure=sg.ssf_perp(proto), energies=np.linspace(0, 3.0, 10), dt=0.05)
+    sc = sg.SampledCorrelations(b, measure=sg.ssf_perp(proto), energies=np.linspace(0, 3.0, 10), dt=0.05, tol=1e-6)
     sg.add_sample(sc, b)
     assert sc.nsamples == 8 and np.all(np.isfinite(sc.data))
     E = b.energies()

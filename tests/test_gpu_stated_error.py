@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 def test_fp32_batched_error_against_fp64_at_benchmark_time_axis(gpu, sg):
     import bench
-    r = bench.stated_error(sg, 0, L_=4, nomega=200, nrep=8, nsamples=32, decorr=1000)
+    r = bench.stated_error(sg, 0, L_=4, nomega=200, nrep=8, nsamples=64, decorr=1000)
     assert r["steps_per_sample"] == 21 * 199
     # the energy changes over a trajectory are the midpoint method's own bounded
     # oscillation: the same size on both paths, and within the stated 1e-5
@@ -25,14 +25,14 @@ def test_fp32_batched_error_against_fp64_at_benchmark_time_axis(gpu, sg):
     assert r["fp64_energy_rel_err_per_sample_max"] <= 1e-5
     assert r["energy_rel_err_per_sample_median"] <= 3 * r["fp64_energy_rel_err_per_sample_median"] + 1e-7
     for cmp in r["sqw_vs_fp64_halves"]:
-        assert cmp["samples"] == (16, 16)
+        assert cmp["samples"] == (32, 32)
         # paired starts: the difference stays within the error bars
         assert cmp["chi2_ratio"] <= 1.0
         assert cmp["frac_z_gt_3"] < 2e-3
         assert abs(cmp["rms_ratio"] - 1) <= 2e-2
     # the systematic per-bin difference, with two standard deviations of its estimate, is
     # below 1 % of the RMS bin
-    assert r["sqw_systematic_rel_rms_upper"] <= 1e-2
+    assert r["sqw_systematic_rel_rms_upper"] <= 1e-2, r["sqw_systematic"]
 
 
 def test_fp32_batched_energy_error_per_step(gpu, sg):
