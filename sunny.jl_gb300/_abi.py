@@ -96,6 +96,8 @@ SIGNATURES = {
     "sgb_corr_intensities": (C.c_int, [_P, _I32, C.POINTER(_I32), _D, _D, _I32, C.POINTER(_I32), _I32, _D]),
     "sgb_corr_merge": (C.c_int, [_P, _P]),
     "sgb_corr_compare": (C.c_int, [_P, _P, _D]),
+    "sgb_corr_set_time_transform": (C.c_int, [_P, _I32]),
+    "sgb_corr_time_transform": (C.c_int, [_P]),
     "sgb_corr_cross": (C.c_int, [_P, _P, _P, _P, _D]),
     "sgb_corr_profile": (C.c_int, [_P, _I32]),
     "sgb_corr_phase_times": (C.c_int, [_P, _D, C.POINTER(_I64), C.POINTER(_I64)]),

@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [("sgb_api.cu", "sgb_api", []), ("sgb_dipole.cu", "sgb_dipole_f32", ["-DSGB_INST_PRECISION=32"]),
            ("sgb_dipole.cu", "sgb_dipole_f64", ["-DSGB_INST_PRECISION=64"]),
            ("sgb_sun.cu", "sgb_sun_f32", ["-DSGB_INST_PRECISION=32"]), ("sgb_sun.cu", "sgb_sun_f64", ["-DSGB_INST_PRECISION=64"]),
-           ("sgb_corr.cu", "sgb_corr", []), ("sgb_batch.cu", "sgb_batch", []), ("sgb_batch_blk.cu", "sgb_batch_blk", []),
+           ("sgb_corr.cu", "sgb_corr", []), ("sgb_tdft.cu", "sgb_tdft", []), ("sgb_batch.cu", "sgb_batch", []), ("sgb_batch_blk.cu", "sgb_batch_blk", []),
            ("sgb_static.cu", "sgb_static", []),
            ("sgb_adjoint.cu", "sgb_adjoint", []), ("sgb_mc.cu", "sgb_mc", []), ("sgb_opt.cu", "sgb_opt", []),
            ("sgb_ewald.cu", "sgb_ewald", [])]

@@ -2033,6 +2033,7 @@ void sgb_corr_destroy(sgb_corr* c) {
     dfree(c->ops);
     void* p = c->pairs; dfree(p);
     dfree(c->A); dfree(c->Ahat);
+    dfree(c->td_chirp); dfree(c->td_fb); dfree(c->td_tw);
     p = c->P; dfree(p);
     p = c->g; dfree(p);
     if (c->have_space) cufftDestroy(c->plan_space);
@@ -2105,6 +2106,10 @@ static int corr_setup(sgb_corr* c, const sgb_corr_desc* d, bool fp32, bool sun, 
             return cfail(c, SGB_ERR_CUDA, "cufftPlanMany (time) failed");
         c->have_time = true;
         cufftSetStream(c->plan_time, c->stream);
+        if (fp32 && tdft_supported(c->nomega, c->nsnaps)) {
+            int trc = tdft_tables(c->nomega, c->nsnaps, &c->td_chirp, &c->td_fb, &c->td_tw);
+            if (trc) return cfail(c, trc, "time transform tables");
+        }
     }
     return SGB_OK;
 }
@@ -2305,12 +2310,21 @@ int sgb_corr_add_sample(sgb_corr* c, int32_t window) {
     // 3. time FFT, A(ω) = sum_t exp(-iωt) A(t), zero padded (CorrelationSampling.jl:65-69)
     const void* spec = c->A;
     if (c->have_time) {
-        for (int r = 0; r < c->nrep; r++) {
-            void* Ar = (char*)c->A + esz * rep_stride * r;
-            void* Hr = (char*)c->Ahat + esz * rep_stride * r;
-            cufftResult fr = fp32 ? cufftExecC2C(c->plan_time, (cufftComplex*)Ar, (cufftComplex*)Hr, CUFFT_FORWARD)
-                                  : cufftExecZ2Z(c->plan_time, (cufftDoubleComplex*)Ar, (cufftDoubleComplex*)Hr, CUFFT_FORWARD);
-            if (fr != CUFFT_SUCCESS) return cfail(c, SGB_ERR_CUDA, "time FFT failed");
+        const long long stride = (long long)c->nobs * c->npos * c->ncell;
+        if (fp32 && c->td_fb && c->time_kind == 0) {
+            // every replica's series in one launch of the hand-written transform
+            if (tdft_launch((const float*)c->A, (float*)c->Ahat, stride * c->nrep, stride, (long long)rep_stride, c->nomega, c->nsnaps,
+                            c->td_chirp, c->td_fb, c->td_tw, c->stream))
+                return cfail(c, SGB_ERR_CUDA, std::string("time transform launch: ") + cudaGetErrorString(cudaGetLastError()));
+            (*c->launches)++;
+        } else {
+            for (int r = 0; r < c->nrep; r++) {
+                void* Ar = (char*)c->A + esz * rep_stride * r;
+                void* Hr = (char*)c->Ahat + esz * rep_stride * r;
+                cufftResult fr = fp32 ? cufftExecC2C(c->plan_time, (cufftComplex*)Ar, (cufftComplex*)Hr, CUFFT_FORWARD)
+                                      : cufftExecZ2Z(c->plan_time, (cufftDoubleComplex*)Ar, (cufftDoubleComplex*)Hr, CUFFT_FORWARD);
+                if (fr != CUFFT_SUCCESS) return cfail(c, SGB_ERR_CUDA, "time FFT failed");
+            }
         }
         spec = c->Ahat;
     }
@@ -2579,6 +2593,18 @@ int sgb_corr_compare(const sgb_corr* a, const sgb_corr* b, double* out) {
     }
     out[8] = G * v / (G - 1);
     return SGB_OK;
+}
+
+int sgb_corr_set_time_transform(sgb_corr* c, int32_t kind) {
+    if (!c) return fail(nullptr, SGB_ERR_ARG, "null handle");
+    if (kind != 0 && kind != 1) return cfail(c, SGB_ERR_ARG, "time transform kind must be 0 (own kernel where it applies) or 1 (cuFFT)");
+    c->time_kind = kind;
+    return SGB_OK;
+}
+
+int sgb_corr_time_transform(const sgb_corr* c) {
+    if (!c) return -1;
+    return (c->td_fb && c->time_kind == 0) ? 0 : 1;
 }
 
 int sgb_corr_cross(const sgb_corr* a1, const sgb_corr* b1, const sgb_corr* a2, const sgb_corr* b2, double* out) {

@@ -33,3 +33,10 @@ int corr_launch_gather_q(const double* P, size_t ld, const int* qidx, int nq, in
                          cudaStream_t st);
 int corr_launch_intensity(const double* tmp, int ncorr, int npos, int n, const double* pref, const double* qcart,
                           const int* widx, int nw, int combiner, int nq, double* out, cudaStream_t st);
+
+// Hand-written time transform of FP32 accumulators (sgb_tdft.cu): Bluestein over a
+// 1024-point four-step FFT, for n + m - 1 <= 1024 (n points, the first m of them samples).
+bool tdft_supported(int n, int m);
+int tdft_tables(int n, int m, void** chirp, void** fb, void** tw);
+int tdft_launch(const float* A, float* Ahat, long long ncols, long long stride, long long rep_stride, int n, int m,
+                const void* chirp, const void* fb, const void* tw, cudaStream_t st);

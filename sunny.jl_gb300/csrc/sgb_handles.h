@@ -121,6 +121,12 @@ struct sgb_corr {
     size_t chunk = 0;
     cufftHandle plan_chunk = 0;
     bool have_chunk = false;
+    // FP32 time transform by the hand-written Bluestein kernel (sgb_tdft.cu) when the length
+    // allows: chirp, FFT of the chirp / 1024, twiddle table; time_kind 0 uses it, 1 cuFFT
+    void* td_chirp = nullptr;
+    void* td_fb = nullptr;
+    void* td_tw = nullptr;
+    int time_kind = 0;
 };
 
 

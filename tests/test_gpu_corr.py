@@ -314,3 +314,44 @@ def test_intensities_with_errors_mode_equal_deferred(gpu, sg):
     ia = sg.intensities(a, qs, energies="available_with_negative", kT=0.3).data
     ib = sg.intensities(b, qs, energies="available_with_negative", kT=0.3).data
     assert np.max(np.abs(ia - ib)) < 1e-10 * np.max(np.abs(ia))
+
+
+@pytest.mark.parametrize("nw", [200, 40])
+def test_own_time_transform_matches_cufft(gpu, sg, nw):
+    # the hand-written Bluestein time transform of FP32 accumulators against cuFFT's, from
+    # the same start: equal up to FP32 rounding of the two transforms
+    import ctypes as C
+    proto = sg.System(sg.diamond_crystal(), [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(2, 3, 4), seed=31,
+                      precision="fp32", device=None)
+    proto.set_exchange(0.6498, sg.Bond(1, 3, [0, 0, 0]))
+    b = sg.ReplicaBatch(proto, [proto.dims] * 3, kT=[0.3] * 3, precision="fp32", seed=2)
+    b.randomize_spins()
+    b.langevin(0.05, 0.1, 100)
+    start = [b.get_state(r) for r in range(3)]
+    kw = dict(energies=np.linspace(0, 5.5, nw), dt=0.05, tol=1e-6)
+    datas = []
+    for kind in (0, 1):
+        for r in range(3):
+            b.set_state(r, start[r])
+        sc = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), **kw)
+        assert sc._lib.sgb_corr_set_time_transform(sc._h, kind) == 0
+        assert sc._lib.sgb_corr_time_transform(sc._h) == kind
+        sg.add_sample(sc, b)
+        datas.append(sc.data)
+        sc.close()
+    scale = np.max(np.abs(datas[1]))
+    assert np.max(np.abs(datas[0] - datas[1])) < 2e-5 * scale
+    b.close()
+
+
+def test_time_transform_falls_back_beyond_its_length(gpu, sg):
+    # n_all_ω + n_all_ω/2 > 1024 (nω = 400): cuFFT
+    s = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=(2, 2, 2), seed=3, precision="fp32")
+    s.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    s.randomize_spins()
+    sc = sg.SampledCorrelations(s, measure=sg.ssf_trace(s), energies=np.linspace(0, 4.0, 400), dt=0.05, tol=1e-6)
+    assert sc._lib.sgb_corr_time_transform(sc._h) == 1
+    sc2 = sg.SampledCorrelations(s, measure=sg.ssf_trace(s), energies=np.linspace(0, 4.0, 300), dt=0.05, tol=1e-6)
+    assert sc2._lib.sgb_corr_time_transform(sc2._h) == 0
+    sc.close()
+    sc2.close()
