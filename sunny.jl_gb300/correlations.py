@@ -290,15 +290,17 @@ def systematic_difference(a1: SampledCorrelations, b1: SampledCorrelations, a2: 
     difference summed over bins, since the halves' noise is independent. Returns
       bias_rel        √(max(0, Σ Re D1·conj(D2)) / Σ|mean_b|²), the RMS systematic
                       difference relative to the RMS bin;
-      bias_rel_upper  the same with the cross sum raised by two of its standard deviations
-                      (estimated from partial sums over interleaved bin sets);
+      bias_rel_upper  √((max(0, Σ Re D1·conj(D2)) + 2 sd) / Σ|mean_b|²), a bound that two
+                      standard deviations of the cross sum (estimated from partial sums over
+                      interleaved bin sets) keep above the estimate even when noise makes
+                      the cross sum negative;
       cross_rel2      the cross sum over Σ|mean_b|² (may be negative by noise)."""
     out = np.zeros(3)
     a1._check(a1._lib.sgb_corr_cross(a1._h, b1._h, a2._h, b2._h, _abi.dptr(out)))
     t0, t1, var = out
     sd = math.sqrt(max(var, 0.0))
     return {"bias_rel": math.sqrt(max(0.0, t0) / t1) if t1 > 0 else math.nan,
-            "bias_rel_upper": math.sqrt(max(0.0, t0 + 2 * sd) / t1) if t1 > 0 else math.nan,
+            "bias_rel_upper": math.sqrt((max(0.0, t0) + 2 * sd) / t1) if t1 > 0 else math.nan,
             "cross_rel2": t0 / t1 if t1 > 0 else math.nan,
             "cross_rel2_sd": sd / t1 if t1 > 0 else math.nan}
 

@@ -30,9 +30,14 @@ struct DBond {
     int bqidx;       // row in the 5x5 biquadratic table
     int fwd;         // 1 for the non-culled copy (counted in the energy)
     int pk;          // raw offsets and target packed as bytes: (n0+128) | (n1+128)<<8 | (n2+128)<<16 | j<<24
-    int gidx;        // SU(N) general terms: first row in the general-term table
-    int gcnt;        //                      number of rows (0: none)
+    int gref;        // SU(N) general terms: first row in the general-term table | rows << 20 (0: none)
 };
+
+// First row and number of rows of a bond's SU(N) general terms (DBond::gref).
+template <class B>
+__host__ __device__ __forceinline__ int dbond_gidx(const B& b) { return b.gref & 0xfffff; }
+template <class B>
+__host__ __device__ __forceinline__ int dbond_gcnt(const B& b) { return (int)((unsigned)b.gref >> 20); }
 
 // Sunny's scalar_biquad_metric (src/System/Types.jl:40)
 __host__ __device__ inline double biquad_metric(int q) {

@@ -46,7 +46,7 @@ struct Model {
     const int* okmax;
     // SU(N) general pair couplings: term rows of 4 N^2 values, [a (N^2)][A (N*N complex)][b (N^2)],
     // where <A> = a·ρ and <B> = b·ρ over the packed density ρ of a ket (sun_rho); rows of a
-    // bond are DBond::gidx .. gidx + gcnt. has_general: any such row.
+    // bond are given by DBond::gref (dbond_gidx, dbond_gcnt). has_general: any such row.
     const R* gtab;
     int has_general;
     int qrows;          // rows per site of the SU(N) multipole buffers: 5 quadrupoles, then ρ (N^2)

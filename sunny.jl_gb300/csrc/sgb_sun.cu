@@ -301,13 +301,13 @@ __device__ __forceinline__ void general_HZ(const Model<R>& M, const Tab<R>& T, i
     const int ns = M.ns, b0 = T.boff[a], b1 = T.boff[a + 1];
     for (int b = b0; b < b1; b++) {
         const DBond<R>& B = T.bonds[b];
-        if (B.gcnt == 0) continue;
+        if (dbond_gcnt(B) == 0) continue;
         const int j = __ldg(M.nbr + (size_t)(b - b0) * ns + site);
         R rj[N * N];
 #pragma unroll
         for (int k = 0; k < N * N; k++) rj[k] = sgb_ld(Qb + (size_t)(5 + k) * ns + j);
-        for (int t = 0; t < B.gcnt; t++) {
-            const R* row = M.gtab + (size_t)(B.gidx + t) * 4 * N * N;
+        for (int t = 0; t < dbond_gcnt(B); t++) {
+            const R* row = M.gtab + (size_t)(dbond_gidx(B) + t) * 4 * N * N;
             const R* Am = row + N * N;
             const R* bv = row + 3 * N * N;
             R Bb = 0;
@@ -688,15 +688,15 @@ __global__ void __launch_bounds__(SGB_BLOCK) k_sun_energy(Model<R> M, const R* Z
                 }
                 E += acc;
             }
-            if (B.gcnt > 0) {
+            if (dbond_gcnt(B) > 0) {
                 // general couplings (Interactions.jl:495-503): Σ_k <A_k>_i <B_k>_j
                 double zj[2 * N], ri[N * N], rj[N * N];
 #pragma unroll
                 for (int c = 0; c < 2 * N; c++) zj[c] = Z[(size_t)c * ns + js];
                 sun_rho<double, N>(z, ri);
                 sun_rho<double, N>(zj, rj);
-                for (int t = 0; t < B.gcnt; t++) {
-                    const R* row = M.gtab + (size_t)(B.gidx + t) * 4 * N * N;
+                for (int t = 0; t < dbond_gcnt(B); t++) {
+                    const R* row = M.gtab + (size_t)(dbond_gidx(B) + t) * 4 * N * N;
                     double Ab = 0, Bb = 0;
                     for (int k = 0; k < N * N; k++) {
                         Ab += (double)row[k] * ri[k];
@@ -1303,10 +1303,10 @@ __device__ inline R sun_local_dE(const Model<R>& M, const SunTab<R, N>& S, int s
         sun_rho<R, N>(zn, rn);
         for (int b = b0; b < b1; b++) {
             const DBond<R>& B = S.t.bonds[b];
-            if (B.gcnt == 0) continue;
+            if (dbond_gcnt(B) == 0) continue;
             const int j = __ldg(M.nbr + (size_t)(b - b0) * ns + site);
-            for (int t = 0; t < B.gcnt; t++) {
-                const R* row = M.gtab + (size_t)(B.gidx + t) * 4 * N * N;
+            for (int t = 0; t < dbond_gcnt(B); t++) {
+                const R* row = M.gtab + (size_t)(dbond_gidx(B) + t) * 4 * N * N;
                 R dA = 0, Bb = 0;
 #pragma unroll
                 for (int k = 0; k < N * N; k++) {

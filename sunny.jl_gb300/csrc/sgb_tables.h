@@ -98,7 +98,8 @@ std::string pack_tables(int na, int N, bool sun, const int* dims, const std::vec
             if (gen && grows) {
                 // rows (a(first), first, a(second)): the site's own operator first; the
                 // reversed copy swaps A and B (reverse(tensordec))
-                e.gidx = (int)(grows->size() / (4 * NN));
+                const size_t gidx = grows->size() / (4 * NN);
+                int gcnt = 0;
                 for (size_t t = 0; t < gen->bond.size(); t++) {
                     if (gen->bond[t] != (int)bi) continue;
                     const double* A = gen->A.data() + 2 * NN * t;
@@ -110,8 +111,10 @@ std::string pack_tables(int na, int N, bool sun, const int* dims, const std::vec
                     for (int k = 0; k < 2 * NN; k++) row[NN + k] = (R)first[k];
                     density_coeffs<R>(N, second, row.data() + 3 * NN);
                     grows->insert(grows->end(), row.begin(), row.end());
-                    e.gcnt++;
+                    gcnt++;
                 }
+                if (gidx >= (1u << 20) || gcnt >= (1 << 12)) return "too many general coupling terms";
+                e.gref = gcnt ? (int)gidx | (gcnt << 20) : 0;
             }
             int from = dir == 0 ? b.i : b.j;
             int to = dir == 0 ? b.j : b.i;

@@ -18,8 +18,11 @@
 // time), the twiddles exp(∓2πi·lane·k/1024) from a shared table laid out [k][lane] (conflict
 // free), a transpose through the warp's shared 32 × 33 tile (padded against bank
 // conflicts), and 32-point DFTs again. The zero padding is never loaded and only the
-// n wanted outputs are stored. A CTA of 8 warps takes 8 adjacent series, so each of its
-// time rows is read and written as 64 contiguous bytes.
+// n wanted outputs are stored. A CTA of 8 warps takes 8 adjacent series of one replica;
+// its samples come in and its spectra go out through shared memory row by row, so each
+// warp-wide load or store moves 4 time rows of 64 contiguous bytes. Since n + m − 1 <= 1024
+// bounds m by 342, only registers j <= 10 of the first DFT hold samples; its first stage
+// is written for that.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -72,15 +75,53 @@ __device__ __forceinline__ void dft32_dif(float2* v) {
     }
 }
 
+// The first DFT of the forward transform, whose registers j >= 11 are zero: its first
+// stage (pairs j, j + 16) reduces to v[j + 16] = v[j] w^j.
+__device__ __forceinline__ void dft32_dif_first(float2* v) {
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        const float2 a = v[i];
+        v[i + 16] = i == 0 ? a : (i == 8 ? make_float2(a.y, -a.x) : cmulf(a, c_w32[i]));
+    }
+#pragma unroll
+    for (int half = 8; half >= 1; half >>= 1) {
+#pragma unroll
+        for (int blk = 0; blk < 32; blk += 2 * half) {
+#pragma unroll
+            for (int i = 0; i < half; i++) {
+                const float2 a = v[blk + i], b = v[blk + i + half];
+                v[blk + i] = make_float2(a.x + b.x, a.y + b.y);
+                const float2 d = make_float2(a.x - b.x, a.y - b.y);
+                const int e = i * (16 / half);
+                v[blk + i + half] = e == 0 ? d : (e == 8 ? make_float2(d.y, -d.x) : cmulf(d, c_w32[e]));
+            }
+        }
+    }
+}
+
+constexpr int TD_JMAX = 11;            // registers that can hold samples (m <= 342)
+constexpr int TD_ROWS_IN = 32 * TD_JMAX;
+
 __global__ void __launch_bounds__(32 * TD_WARPS, 2)
 k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long ncols, long long stride, long long rep_stride,
            int n, int m, const float2* __restrict__ chirp, const float2* __restrict__ fb, const float2* __restrict__ tw) {
     __shared__ float2 s_tw[TD_M];                  // [k][lane] = exp(−2πi lane k / 1024)
     __shared__ float2 s_t[TD_WARPS][32 * 33];      // per-warp transpose tile
+    __shared__ float2 s_io[TD_ROWS_IN * TD_WARPS]; // staged samples [t][series], later spectra [k][series]
     for (int i = threadIdx.x; i < TD_M; i += blockDim.x) s_tw[i] = tw[i];
-    __syncthreads();
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    const long long col = (long long)blockIdx.x * TD_WARPS + wp;
+    const long long col0 = (long long)blockIdx.x * TD_WARPS;
+    const long long col = col0 + wp;
+    // the CTA's series are adjacent in memory when all eight lie in one replica
+    const bool rowwise = col0 + TD_WARPS <= ncols && (col0 / stride) == ((col0 + TD_WARPS - 1) / stride);
+    const long long base0 = (col0 / stride) * rep_stride + (col0 % stride);
+    if (rowwise) {
+        for (int e = threadIdx.x; e < m * TD_WARPS; e += blockDim.x) {
+            const int t = e / TD_WARPS, c = e % TD_WARPS;
+            s_io[t * TD_WARPS + c] = __ldg(A + base0 + (long long)t * stride + c);
+        }
+    }
+    __syncthreads();
     if (col >= ncols) return;
     const long long base = (col / stride) * rep_stride + (col % stride);
     float2* T = s_t[wp];
@@ -89,12 +130,13 @@ k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long nc
 #pragma unroll
     for (int j = 0; j < 32; j++) {
         const int t = 32 * j + lane;
-        if (t < m) v[j] = cmulf(__ldg(A + base + (long long)t * stride), __ldg(chirp + t));
+        if (j < TD_JMAX && t < m)
+            v[j] = cmulf(rowwise ? s_io[t * TD_WARPS + wp] : __ldg(A + base + (long long)t * stride), __ldg(chirp + t));
         else v[j] = make_float2(0.f, 0.f);
     }
     // forward FFT: DFT over j (index 32 j + lane), twiddle exp(−2πi lane k1/1024), transpose,
     // DFT over the former lanes; lane then holds frequency lane + 32 k2 in v[bitrev5(k2)]
-    dft32_dif<false>(v);
+    dft32_dif_first(v);
 #pragma unroll
     for (int k1 = 0; k1 < 32; k1++) T[lane * 33 + k1] = cmulf(v[bitrev5(k1)], s_tw[k1 * 32 + lane]);
     __syncwarp();
@@ -120,16 +162,39 @@ k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long nc
     for (int k1 = 0; k1 < 32; k1++) v[k1] = T[k1 * 33 + lane];
     dft32_dif<true>(v);
     // X_k = w_k y_k for the n wanted points
+    if (!rowwise) {
 #pragma unroll
-    for (int j2 = 0; j2 < 32; j2++) {
-        const int k = lane + 32 * j2;
-        if (k < n) Ahat[base + (long long)k * stride] = cmulf(v[bitrev5(j2)], __ldg(chirp + k));
+        for (int j2 = 0; j2 < 32; j2++) {
+            const int k = lane + 32 * j2;
+            if (k < n) Ahat[base + (long long)k * stride] = cmulf(v[bitrev5(j2)], __ldg(chirp + k));
+        }
+        return;
+    }
+    // row-wise stores in two halves of the spectrum through the staging buffer (its
+    // samples were consumed before the first transpose)
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int k0 = h * TD_ROWS_IN, k1 = min(n, k0 + TD_ROWS_IN);
+#pragma unroll
+        for (int j2 = 0; j2 < 32; j2++) {
+            const int k = lane + 32 * j2;
+            if (k >= k0 && k < k1) s_io[(k - k0) * TD_WARPS + wp] = cmulf(v[bitrev5(j2)], __ldg(chirp + k));
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < (k1 - k0) * TD_WARPS; e += blockDim.x) {
+            const int k = k0 + e / TD_WARPS, c = e % TD_WARPS;
+            Ahat[base0 + (long long)k * stride + c] = s_io[e];
+        }
+        __syncthreads();
     }
 }
 
 }  // namespace
 
-bool tdft_supported(int n, int m) { return n >= 2 && m >= 1 && n + m - 1 <= TD_M; }
+bool tdft_supported(int n, int m) {
+    return n >= 2 && m >= 1 && n + m - 1 <= TD_M && m <= TD_ROWS_IN && n <= 2 * TD_ROWS_IN;
+}
 
 // Tables of one transform length: chirp[max(n, m)], FFT(b)/M [1024], twiddles [1024].
 int tdft_tables(int n, int m, void** chirp_out, void** fb_out, void** tw_out) {

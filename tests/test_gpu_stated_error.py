@@ -1,5 +1,5 @@
 """The error of the FP32 batched S(q,ω) path against the plain FP64 path, measured as the
-benchmark states it, on a reduced pyrochlore (4^3 conventional cells x 16 sites) with the
+benchmark states it, on a reduced pyrochlore (8^3 conventional cells x 16 sites) with the
 benchmark's time axis: nω = 200 to 6 meV, 21 x 199 = 4,179 implicit-midpoint steps per
 sample at tol 1e-6 with the degree-4 first iterate.
 
@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 def test_fp32_batched_error_against_fp64_at_benchmark_time_axis(gpu, sg):
     import bench
-    r = bench.stated_error(sg, 0, L_=4, nomega=200, nrep=8, nsamples=64, decorr=1000)
+    r = bench.stated_error(sg, 0, L_=8, nomega=200, nrep=8, nsamples=64, decorr=1000)
     assert r["steps_per_sample"] == 21 * 199
     # the energy changes over a trajectory are the midpoint method's own bounded
     # oscillation: the same size on both paths, and within the stated 1e-5
