@@ -2168,10 +2168,11 @@ int sgb_batch_corr_create(sgb_batch* b, const sgb_corr_desc* d, sgb_corr** out) 
         if (cudaMalloc(p, bytes) != cudaSuccess) { *p = nullptr; b->err = "device allocation failed"; return SGB_ERR_NOMEM; }
         return SGB_OK;
     };
-    // midpoint-private buffers: room for one 4-element vector per site (FP32 float4 layout)
-    if ((rc = lazy(&b->Sp, R * 4 * b->NS)) || (rc = lazy(&b->H, R * 12 * b->NS)) || (rc = lazy(&b->Sc, R * 4 * b->NS)) ||
-        (rc = lazy(&b->P1, R * 4 * b->NS)) || (rc = lazy(&b->H1, R * 4 * b->NS)) ||
-        (rc = lazy(&b->H2, R * 4 * b->NS)) || (rc = lazy(&b->H3, R * 4 * b->NS)) ||
+    // midpoint buffers: three rotating neighbour-gathered buffers of one 4-element vector
+    // per site (FP32 float4 layout), and the private 3-vector buffers [3][NS]
+    if ((rc = lazy(&b->Sp, R * 3 * b->NS)) || (rc = lazy(&b->H, R * 12 * b->NS)) ||
+        (rc = lazy(&b->P1, R * 3 * b->NS)) || (rc = lazy(&b->H1, R * 3 * b->NS)) ||
+        (rc = lazy(&b->H2, R * 3 * b->NS)) || (rc = lazy(&b->H3, R * 3 * b->NS)) ||
         (rc = lazy((void**)&b->racc, sizeof(double) * 3 * b->nrep)))
         return rc;
     sgb_corr* c = new sgb_corr();

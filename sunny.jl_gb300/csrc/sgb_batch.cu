@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                 const int4 ti = st_a[k];
                 if (tid >= ti.z) continue;
                 const int g = ti.w + ti.y + tid;
-                MV<R>::st(X.Sp, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
+                PV<R>::st(X.Sp, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
             }
         }
         const int ord = min(X.ord, step + 1);   // extrapolation order available for the next step
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                         const R kap = s_kap[a];
                         R sx = A.S[g], sy = A.S[NS + g], sz = A.S[2 * NS + g];
                         R qx, qy, qz, hx, hy, hz;
-                        MV<R>::ld(X.Sp, NS, g, qx, qy, qz);
+                        PV<R>::ld(X.Sp, NS, g, qx, qy, qz);
                         // own midpoint spin normalize((S + S')/2): stored by the previous
                         // iteration (or step) with exactly this arithmetic
                         MV<R>::ld(Hc, NS, g, hx, hy, hz);
@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                         R nx = sx + dx, ny = sy + dy, nz = sz + dz;
                         R ex = qx - nx, ey = qy - ny, ez = qz - nz;
                         acc = ex * ex + ey * ey + ez * ez;
-                        MV<R>::st(X.Sp, NS, g, nx, ny, nz);
+                        PV<R>::st(X.Sp, NS, g, nx, ny, nz);
                         R mx = (sx + nx) / 2, my = (sy + ny) / 2, mz = (sz + nz) / 2;
                         normalize_dip<R>(mx, my, mz, kap);
                         MV<R>::st(Hn, NS, g, mx, my, mz);
@@ -404,7 +404,6 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                         if (X.ord == 0 || it > 0) {
                         R cx = nx, cy = ny, cz = nz;
                         normalize_dip<R>(cx, cy, cz, kap);
-                        MV<R>::st(X.Sc, NS, g, cx, cy, cz);
                         // next step's first iterate p and midpoint spin normalize((c + p)/2)
                         R px = cx, py = cy, pz = cz;
                         if (ord == 1) {
@@ -412,25 +411,25 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                         } else if (ord >= 2) {
                             // Newton backward differences through c = S_{n+1}, s = S_n, S_{n-1}, ...
                             R ux, uy, uz;
-                            MV<R>::ld(X.H1, NS, g, ux, uy, uz);
+                            PV<R>::ld(X.H1, NS, g, ux, uy, uz);
                             if (ord == 2) {
                                 px = 3 * (cx - sx) + ux; py = 3 * (cy - sy) + uy; pz = 3 * (cz - sz) + uz;
                             } else {
                                 R vx, vy, vz;
-                                MV<R>::ld(X.H2, NS, g, vx, vy, vz);
+                                PV<R>::ld(X.H2, NS, g, vx, vy, vz);
                                 if (ord == 3) {
                                     px = 4 * (cx + ux) - 6 * sx - vx; py = 4 * (cy + uy) - 6 * sy - vy;
                                     pz = 4 * (cz + uz) - 6 * sz - vz;
                                 } else {
                                     R wx0, wy0, wz0;
-                                    MV<R>::ld(X.H3, NS, g, wx0, wy0, wz0);
+                                    PV<R>::ld(X.H3, NS, g, wx0, wy0, wz0);
                                     px = 5 * (cx - vx) + 10 * (ux - sx) + wx0;
                                     py = 5 * (cy - vy) + 10 * (uy - sy) + wy0;
                                     pz = 5 * (cz - vz) + 10 * (uz - sz) + wz0;
                                 }
                             }
                         }
-                        if (ord > 0) MV<R>::st(X.P1, NS, g, px, py, pz);
+                        if (ord > 0) PV<R>::st(X.P1, NS, g, px, py, pz);
                         R wx = (cx + px) / 2, wy = (cy + py) / 2, wz = (cz + pz) / 2;
                         normalize_dip<R>(wx, wy, wz, kap);
                         MV<R>::st(Hs, NS, g, wx, wy, wz);
@@ -483,24 +482,26 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                     actm &= ~(1u << k);
                     if (tid < ti.z) {
                         const int g = ti.w + ti.y + tid;
+                        // the accepted state normalize(S''), from the last iterate
                         R x, y, z;
-                        MV<R>::ld(X.Sc, NS, g, x, y, z);
+                        PV<R>::ld(X.Sp, NS, g, x, y, z);
+                        normalize_dip<R>(x, y, z, s_kap[st_atom[k][tid]]);
                         if (X.ord > 0) {
                             // shift the history: S_{n-2} -> H3, S_{n-1} -> H2, S_n -> H1
                             if (X.ord >= 4) {
                                 R hx, hy, hz;
-                                MV<R>::ld(X.H2, NS, g, hx, hy, hz);
-                                MV<R>::st(X.H3, NS, g, hx, hy, hz);
+                                PV<R>::ld(X.H2, NS, g, hx, hy, hz);
+                                PV<R>::st(X.H3, NS, g, hx, hy, hz);
                             }
                             if (X.ord >= 3) {
                                 R hx, hy, hz;
-                                MV<R>::ld(X.H1, NS, g, hx, hy, hz);
-                                MV<R>::st(X.H2, NS, g, hx, hy, hz);
+                                PV<R>::ld(X.H1, NS, g, hx, hy, hz);
+                                PV<R>::st(X.H2, NS, g, hx, hy, hz);
                             }
-                            if (X.ord >= 2) MV<R>::st(X.H1, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
+                            if (X.ord >= 2) PV<R>::st(X.H1, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
                             R px, py, pz;
-                            MV<R>::ld(X.P1, NS, g, px, py, pz);
-                            MV<R>::st(X.Sp, NS, g, px, py, pz);
+                            PV<R>::ld(X.P1, NS, g, px, py, pz);
+                            PV<R>::st(X.Sp, NS, g, px, py, pz);
                         }
                         A.S[g] = x; A.S[NS + g] = y; A.S[2 * NS + g] = z;
                     }
@@ -1026,7 +1027,6 @@ static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
     MidArgs<R> X;
     X.Sp = (R*)b->Sp;
     X.H = (R*)b->H;
-    X.Sc = (R*)b->Sc;
     X.racc = b->racc;
     X.P1 = (R*)b->P1;
     X.H1 = (R*)b->H1;
@@ -1092,7 +1092,7 @@ void sgb_batch_destroy(sgb_batch* b) {
     p = b->nbr; bfree(p);
     p = b->nbo; bfree(p);
     p = b->td; bfree(p);
-    bfree(b->S); bfree(b->P); bfree(b->D1); bfree(b->Sp); bfree(b->H); bfree(b->Sc); bfree(b->P1); bfree(b->H1); bfree(b->H2); bfree(b->H3);
+    bfree(b->S); bfree(b->P); bfree(b->D1); bfree(b->Sp); bfree(b->H); bfree(b->P1); bfree(b->H1); bfree(b->H2); bfree(b->H3);
     bfree(b->Hpad);
     p = b->racc; bfree(p); p = b->ctrl; bfree(p); p = b->Epart; bfree(p); p = b->E; bfree(p);
     p = b->counters; bfree(p); p = b->n_accept; bfree(p);

@@ -32,9 +32,8 @@ struct BatchArgs {
 
 template <class R>
 struct MidArgs {
-    R* Sp;          // current iterate S' (MV layout)
+    R* Sp;          // current iterate S' (PV layout)
     R* H;           // 3 rotating buffers of midpoint spins, MV<R>::W * NS elements each
-    R* Sc;          // candidate new state (MV layout)
     double* racc;   // [3][nrep] FP64 convergence sums
     R* P1;          // first iterate of the next step (MV layout), ord > 0
     R* H1;          // states of the 1st, 2nd and 3rd previous steps (MV layout), ord >= 2, 3, 4
@@ -73,6 +72,20 @@ __device__ __forceinline__ void snap_write(const BSnap<R>& sn, int r, int t, int
 // Midpoint-private 3-vector buffers (iterate, candidate, rotating midpoint spins). FP32
 // keeps one float4 per site so that a neighbour costs one 16-byte load; FP64 keeps SoA
 // [3][NS]. K: elements from one site to the next; W * NS: elements of one buffer.
+// Midpoint-private 3-vector buffers, read and written only by the thread that owns the
+// site (the iterate, the extrapolation history, the next step's first iterate): SoA
+// [3][NS] in both precisions, 12 bytes per site in FP32, so that they take less of L2 than
+// the float4 layout that neighbour-gathered buffers use.
+template <class R>
+struct PV {
+    __device__ static __forceinline__ void ld(const R* b, int n, int i, R& x, R& y, R& z) {
+        x = b[i]; y = b[n + i]; z = b[2 * n + i];
+    }
+    __device__ static __forceinline__ void st(R* b, int n, int i, R x, R y, R z) {
+        b[i] = x; b[n + i] = y; b[2 * n + i] = z;
+    }
+};
+
 template <class R>
 struct MV;
 template <>

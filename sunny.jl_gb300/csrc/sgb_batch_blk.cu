@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(NT, 1) k_batch_midpoint_blk(BatchArgs<float> A
                 for (int i = tid; i < nsb; i += blockDim.x) {
                     const BlkSite c = site_of(i);
                     const int g = off + (bk.y + c.x) + B.L1 * ((bk.z + c.y) + B.L2 * ((bk.w + c.z) + B.L3 * c.a));
-                    MV<float>::st(X.Sp, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
+                    PV<float>::st(X.Sp, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
                 }
             }
         }
@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(NT, 1) k_batch_midpoint_blk(BatchArgs<float> A
                     const int hi = ((a * B.HZ + c.z + B.gw) * B.HY + c.y + B.gw) * B.HX + c.x + B.gw;
                     const float sx = A.S[g], sy = A.S[NS + g], sz = A.S[2 * NS + g];
                     float qx, qy, qz;
-                    MV<float>::ld(X.Sp, NS, g, qx, qy, qz);
+                    PV<float>::ld(X.Sp, NS, g, qx, qy, qz);
                     const float4 hv = halo[hi];
                     const float hx = hv.x, hy = hv.y, hz = hv.z;
                     const int* dl = dlt + T.boff[a];
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(NT, 1) k_batch_midpoint_blk(BatchArgs<float> A
                     const float nx = sx + dx, ny = sy + dy, nz = sz + dz;
                     const float ex = qx - nx, ey = qy - ny, ez = qz - nz;
                     acc += ex * ex + ey * ey + ez * ez;
-                    MV<float>::st(X.Sp, NS, g, nx, ny, nz);
+                    PV<float>::st(X.Sp, NS, g, nx, ny, nz);
                     float mxv = (sx + nx) / 2, myv = (sy + ny) / 2, mzv = (sz + nz) / 2;
                     normalize_dip<float>(mxv, myv, mzv, kap);
                     store_pad(Hn, B, bk.x, a, cx, cy, cz, make_float4(mxv, myv, mzv, 0.f));
@@ -262,25 +262,25 @@ __global__ void __launch_bounds__(NT, 1) k_batch_midpoint_blk(BatchArgs<float> A
                             px = 2 * cx_ - sx; py = 2 * cy_ - sy; pz = 2 * cz_ - sz;
                         } else if (ord >= 2) {
                             float ux, uy, uz;
-                            MV<float>::ld(X.H1, NS, g, ux, uy, uz);
+                            PV<float>::ld(X.H1, NS, g, ux, uy, uz);
                             if (ord == 2) {
                                 px = 3 * (cx_ - sx) + ux; py = 3 * (cy_ - sy) + uy; pz = 3 * (cz_ - sz) + uz;
                             } else {
                                 float vx, vy, vz;
-                                MV<float>::ld(X.H2, NS, g, vx, vy, vz);
+                                PV<float>::ld(X.H2, NS, g, vx, vy, vz);
                                 if (ord == 3) {
                                     px = 4 * (cx_ + ux) - 6 * sx - vx; py = 4 * (cy_ + uy) - 6 * sy - vy;
                                     pz = 4 * (cz_ + uz) - 6 * sz - vz;
                                 } else {
                                     float wx0, wy0, wz0;
-                                    MV<float>::ld(X.H3, NS, g, wx0, wy0, wz0);
+                                    PV<float>::ld(X.H3, NS, g, wx0, wy0, wz0);
                                     px = 5 * (cx_ - vx) + 10 * (ux - sx) + wx0;
                                     py = 5 * (cy_ - vy) + 10 * (uy - sy) + wy0;
                                     pz = 5 * (cz_ - vz) + 10 * (uz - sz) + wz0;
                                 }
                             }
                         }
-                        if (ord > 0) MV<float>::st(X.P1, NS, g, px, py, pz);
+                        if (ord > 0) PV<float>::st(X.P1, NS, g, px, py, pz);
                         float wx = (cx_ + px) / 2, wy = (cy_ + py) / 2, wz = (cz_ + pz) / 2;
                         normalize_dip<float>(wx, wy, wz, kap);
                         store_pad(Hs, B, bk.x, a, cx, cy, cz, make_float4(wx, wy, wz, 0.f));
@@ -324,23 +324,23 @@ __global__ void __launch_bounds__(NT, 1) k_batch_midpoint_blk(BatchArgs<float> A
                     const int g = off + (bk.y + c.x) + B.L1 * ((bk.z + c.y) + B.L2 * ((bk.w + c.z) + B.L3 * c.a));
                     // the accepted state normalize(S''), from the last iterate
                     float x, y, z;
-                    MV<float>::ld(X.Sp, NS, g, x, y, z);
+                    PV<float>::ld(X.Sp, NS, g, x, y, z);
                     normalize_dip<float>(x, y, z, s_kap[c.a]);
                     if (X.ord > 0) {
                         if (X.ord >= 4) {
                             float hx, hy, hz;
-                            MV<float>::ld(X.H2, NS, g, hx, hy, hz);
-                            MV<float>::st(X.H3, NS, g, hx, hy, hz);
+                            PV<float>::ld(X.H2, NS, g, hx, hy, hz);
+                            PV<float>::st(X.H3, NS, g, hx, hy, hz);
                         }
                         if (X.ord >= 3) {
                             float hx, hy, hz;
-                            MV<float>::ld(X.H1, NS, g, hx, hy, hz);
-                            MV<float>::st(X.H2, NS, g, hx, hy, hz);
+                            PV<float>::ld(X.H1, NS, g, hx, hy, hz);
+                            PV<float>::st(X.H2, NS, g, hx, hy, hz);
                         }
-                        if (X.ord >= 2) MV<float>::st(X.H1, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
+                        if (X.ord >= 2) PV<float>::st(X.H1, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
                         float px, py, pz;
-                        MV<float>::ld(X.P1, NS, g, px, py, pz);
-                        MV<float>::st(X.Sp, NS, g, px, py, pz);
+                        PV<float>::ld(X.P1, NS, g, px, py, pz);
+                        PV<float>::st(X.Sp, NS, g, px, py, pz);
                     }
                     A.S[g] = x; A.S[NS + g] = y; A.S[2 * NS + g] = z;
                 }

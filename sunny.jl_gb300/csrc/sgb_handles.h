@@ -204,7 +204,6 @@ struct sgb_batch {
     void* D1 = nullptr;
     void* Sp = nullptr;             // midpoint iterate
     void* H = nullptr;              // midpoint rotating buffers [3][3][NS]
-    void* Sc = nullptr;             // midpoint candidate
     void* P1 = nullptr;             // next step's first midpoint iterate (extrapolated)
     void* H1 = nullptr;             // states of the three previous steps (extrapolation history)
     void* H2 = nullptr;
