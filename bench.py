@@ -242,9 +242,11 @@ def stated_error(sg, device, L_=16, nomega=200, nrep=8, nsamples=32, decorr=1000
             "limits": {"energy_rel_err": 1e-5, "sqw_per_bin_rel": 1e-2}}
 
 
-def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000, predictor=None):
+def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000, predictor=None, mid_shape=None):
     """Batched FP32 sampling: `nrep` replicas of the pyrochlore model advance in one
-    persistent launch; each add_sample adds nrep samples with a rank-nrep accumulator pass."""
+    persistent launch; each add_sample adds nrep samples with a rank-nrep accumulator pass.
+    `mid_shape` (a row of sgb_batch_midpoint_shapes) replaces the autotuner's choice after
+    the first warm-up sample, e.g. to profile one shape."""
     import ctypes as C
     lib = sg.load_library()
     proto = build_system(sg, "fp32", None)
@@ -254,8 +256,11 @@ def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000, predic
     b.randomize_spins()
     b.langevin(DT, 0.1, thermal_steps)
     sc = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), energies=np.linspace(0, WMAX, NOMEGA), dt=DT, tol=tol)
-    for _ in range(warmup):
+    for w in range(warmup):
         sg.add_sample(sc, b)
+        if w == 0 and mid_shape is not None:
+            if lib.sgb_batch_select_midpoint_shape(b.handle, int(mid_shape)) != 0:
+                raise ValueError(f"no midpoint shape row {mid_shape}")
     lib.sgb_corr_profile(sc._h, 1)
     launches0 = lib.sgb_batch_kernel_launches(b.handle)
     clocks = Clocks(device)
@@ -518,6 +523,38 @@ def run_c3_sqw(sg, device, precision, nsamples):
     return out
 
 
+def run_c3_group(sg, device, nrep=8, passes=2):
+    """The SU(3) workload of run_c3_sqw sampled as a replica group: `nrep` FP32 clones whose
+    midpoint trajectories run concurrently (each on its own stream, an equal share of the
+    SMs), one rank-nrep accumulation per batched add_sample."""
+    import ctypes as C
+    lib = sg.load_library()
+    cr = sg.triangular_crystal(a=4.05, c=6.75)
+    p = sg.System(cr, [(1, sg.Moment(s=1, g=2))], "SUN", dims=(48, 48, 4), seed=1, precision="fp32", device=None)
+    J1 = np.array([[-0.24, 0, 0], [0, -0.24, 0.1], [0, 0.1, -0.24]])
+    p.set_exchange(J1, sg.Bond(1, 1, [1, 0, 0]))
+    p.set_exchange(0.05, sg.Bond(1, 1, [1, 2, 0]))
+    p.set_exchange(0.32, sg.Bond(1, 1, [2, 0, 0]))
+    p.set_exchange(-0.05, sg.Bond(1, 1, [0, 0, 1]))
+    p.set_onsite_coupling(lambda Sx, Sy, Sz: -2.2 * Sz @ Sz, 1)
+    b = sg.ReplicaBatch(p, [p.dims] * nrep, kT=[0.3] * nrep, precision="fp32", device=device, seed=1)
+    b.randomize_spins()
+    b.langevin(0.025, 0.1, 1000)
+    sc = sg.SampledCorrelations(b, measure=sg.ssf_perp(p), energies=np.linspace(0, 7.5, 150), dt=0.025, tol=1e-6)
+    sg.add_sample(sc, b)                                   # warm-up (plans, kernel choice)
+    lib.sgb_batch_event_record(b.handle, 0)
+    for _ in range(passes):
+        sg.add_sample(sc, b)
+    lib.sgb_batch_event_record(b.handle, 1)
+    ms = C.c_float()
+    lib.sgb_batch_event_elapsed(b.handle, 0, 1, C.byref(ms))
+    out = {"samples_per_s": nrep * passes / (ms.value / 1000.0), "ms_per_pass": ms.value / passes, "replicas": nrep,
+           "steps_per_sample": sc.measperiod * (sc.n_all_omega // 2), "nsites": p.nsites}
+    sc.close()
+    b.close()
+    return out
+
+
 # ---- CPU restatement (oracle) timing ----------------------------------------------------------
 
 def _cpu_sample_worker(args):
@@ -614,6 +651,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the tempering and Langevin site-step arms")
     ap.add_argument("--no-error", action="store_true", help="skip the stated-error measurement (FP32 vs FP64)")
     ap.add_argument("--error-samples", type=int, default=32, help="samples per path of the stated-error measurement")
+    ap.add_argument("--mid-shape", type=int, default=None,
+                    help="batched midpoint launch shape (row of the autotuner's table) after the first warm-up sample")
     ap.add_argument("--predictor", type=int, default=None,
                     help="first-iterate extrapolation order of the batched midpoint (library default if omitted)")
     args = ap.parse_args()
@@ -652,7 +691,8 @@ def main():
         return float(t.item())
 
     barrier()
-    rb = run_batched(sg, local, args.nrep, args.warmup, args.steps, tol=1e-6, predictor=args.predictor)
+    rb = run_batched(sg, local, args.nrep, args.warmup, args.steps, tol=1e-6, predictor=args.predictor,
+                     mid_shape=args.mid_shape)
     barrier()
     r32 = run_arm(sg, "fp32", local, args.warmup, max(2, args.steps // 2), tol=1e-6)
     # (single-system FP32 path: one replica per add_sample)
@@ -674,6 +714,8 @@ def main():
         extra["adjoint"] = run_adjoint(sg, local)
         c3 = {"fp32": run_c3_sqw(sg, local, "fp32", 2), "fp64": run_c3_sqw(sg, local, "fp64", 1)}
         c3["speedup"] = c3["fp32"]["samples_per_s"] / c3["fp64"]["samples_per_s"]
+        c3["fp32_group8"] = run_c3_group(sg, local)
+        c3["speedup_group8_vs_fp64"] = c3["fp32_group8"]["samples_per_s"] / c3["fp64"]["samples_per_s"]
         extra["c3_sqw"] = c3
     err = None
     if not args.no_error:

@@ -101,13 +101,14 @@ __device__ __forceinline__ void dft32_dif_first(float2* v) {
 
 constexpr int TD_JMAX = 11;            // registers that can hold samples (m <= 342)
 constexpr int TD_ROWS_IN = 32 * TD_JMAX;
+constexpr int TD_LD = TD_WARPS + 1;    // staging row stride: lanes 32 rows apart hit distinct banks
 
 __global__ void __launch_bounds__(32 * TD_WARPS, 2)
 k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long ncols, long long stride, long long rep_stride,
            int n, int m, const float2* __restrict__ chirp, const float2* __restrict__ fb, const float2* __restrict__ tw) {
     __shared__ float2 s_tw[TD_M];                  // [k][lane] = exp(−2πi lane k / 1024)
     __shared__ float2 s_t[TD_WARPS][32 * 33];      // per-warp transpose tile
-    __shared__ float2 s_io[TD_ROWS_IN * TD_WARPS]; // staged samples [t][series], later spectra [k][series]
+    __shared__ float2 s_io[TD_ROWS_IN * TD_LD];    // staged samples [t][series], later spectra [k][series]
     for (int i = threadIdx.x; i < TD_M; i += blockDim.x) s_tw[i] = tw[i];
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     const long long col0 = (long long)blockIdx.x * TD_WARPS;
@@ -118,7 +119,7 @@ k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long nc
     if (rowwise) {
         for (int e = threadIdx.x; e < m * TD_WARPS; e += blockDim.x) {
             const int t = e / TD_WARPS, c = e % TD_WARPS;
-            s_io[t * TD_WARPS + c] = __ldg(A + base0 + (long long)t * stride + c);
+            s_io[t * TD_LD + c] = __ldg(A + base0 + (long long)t * stride + c);
         }
     }
     __syncthreads();
@@ -131,7 +132,7 @@ k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long nc
     for (int j = 0; j < 32; j++) {
         const int t = 32 * j + lane;
         if (j < TD_JMAX && t < m)
-            v[j] = cmulf(rowwise ? s_io[t * TD_WARPS + wp] : __ldg(A + base + (long long)t * stride), __ldg(chirp + t));
+            v[j] = cmulf(rowwise ? s_io[t * TD_LD + wp] : __ldg(A + base + (long long)t * stride), __ldg(chirp + t));
         else v[j] = make_float2(0.f, 0.f);
     }
     // forward FFT: DFT over j (index 32 j + lane), twiddle exp(−2πi lane k1/1024), transpose,
@@ -179,12 +180,12 @@ k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long nc
 #pragma unroll
         for (int j2 = 0; j2 < 32; j2++) {
             const int k = lane + 32 * j2;
-            if (k >= k0 && k < k1) s_io[(k - k0) * TD_WARPS + wp] = cmulf(v[bitrev5(j2)], __ldg(chirp + k));
+            if (k >= k0 && k < k1) s_io[(k - k0) * TD_LD + wp] = cmulf(v[bitrev5(j2)], __ldg(chirp + k));
         }
         __syncthreads();
         for (int e = threadIdx.x; e < (k1 - k0) * TD_WARPS; e += blockDim.x) {
             const int k = k0 + e / TD_WARPS, c = e % TD_WARPS;
-            Ahat[base0 + (long long)k * stride + c] = s_io[e];
+            Ahat[base0 + (long long)k * stride + c] = s_io[(k - k0) * TD_LD + c];
         }
         __syncthreads();
     }
