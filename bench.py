@@ -609,6 +609,40 @@ def cpu_baseline(threads: int, nmid: int, nblk: int):
     return sum(1.0 / t for t, _ in out), threads, statistics.median(s for _, s in out)
 
 
+def _cpu_c1_worker(args):
+    """FP64 Langevin (the oracle's stochastic Heun) on the simple cubic 16^3 model (s=1,
+    J=1, -0.1 Sz^2, dt 0.02, damping 0.1, kT 0.5) from a random state, on one core: returns
+    (site-steps/s, energy per site, magnetisation per site) after `nsteps` steps."""
+    nsteps, seed = args
+    sys.path.insert(0, str(ROOT))
+    import __graft_entry__ as ge
+    sg = ge.package()
+    orc = ge.oracle()
+    s_ = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=(16, 16, 16), seed=seed, device=None)
+    s_.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    s_.set_onsite_coupling(lambda Sx, Sy, Sz: -0.1 * Sz @ Sz, 1)
+    s_.randomize_spins()
+    o = orc.OracleSystem.from_system(s_)
+    S = s_.dipoles_flat()
+    noise = np.random.default_rng(seed).standard_normal((nsteps, s_.nsites, 3))
+    t0 = time.perf_counter()
+    S, _ = o.langevin(S, None, 0.02, 0.1, 0.5, nsteps, noise)
+    t = time.perf_counter() - t0
+    return s_.nsites * nsteps / t, o.energy(S) / s_.nsites, (S.sum(0) / s_.nsites).tolist()
+
+
+def cpu_c1(threads: int, nsteps: int):
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(threads) as pool:
+        out = pool.map(_cpu_c1_worker, [(nsteps, 1 + k) for k in range(threads)])
+    M = np.array([m for _, _, m in out])
+    return {"site_steps_per_s": sum(r for r, _, _ in out), "cores": threads, "steps_per_core": nsteps,
+            "workload": "simple cubic 16^3 (4,096 spins) FP64 Langevin, one system per core",
+            "energy_per_site_mean": float(np.mean([e for _, e, _ in out])),
+            "abs_magnetization_per_site_mean": float(np.mean(np.linalg.norm(M, axis=1)))}
+
+
 def reference_arm(args, rank, world):
     if rank != 0:
         return
@@ -633,6 +667,7 @@ def reference_arm(args, rank, world):
                                    "ImplicitMidpoint dt=0.024933 x 21 per snapshot", "global_batch": 1, "seq_len": 1,
                        "parallelism": "replicas"},
             "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port", "sample": sample},
+            "c1_langevin": cpu_c1(threads, 2000),
             "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

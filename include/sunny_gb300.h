@@ -351,8 +351,8 @@ int sgb_corr_compare(const sgb_corr* a, const sgb_corr* b, double* out);
 int sgb_corr_cross(const sgb_corr* a1, const sgb_corr* b1, const sgb_corr* a2, const sgb_corr* b2, double* out);
 /* The time transform of add_sample! (CorrelationSampling.jl:65-69), no counterpart in the
  * reference: kind 0 (default) runs FP32 accumulators through the hand-written Bluestein
- * kernel whenever n_all_ω + n_all_ω/2 <= 1024, kind 1 always uses cuFFT (FP64 accumulators
- * always do). sgb_corr_time_transform returns the kind in effect (0 own kernel, 1 cuFFT). */
+ * kernel whenever 512 < n_all_ω + n_all_ω/2 <= 1024 (its fixed 1024-point convolution),
+ * kind 1 always uses cuFFT (FP64 accumulators and other lengths always do). sgb_corr_time_transform returns the kind in effect (0 own kernel, 1 cuFFT). */
 int sgb_corr_set_time_transform(sgb_corr* sc, int32_t kind);
 int sgb_corr_time_transform(const sgb_corr* sc);
 

@@ -193,8 +193,10 @@ k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long nc
 
 }  // namespace
 
+// The fixed 1024-point convolution pays off when the linear convolution needs more than
+// 512 points; shorter series stay with cuFFT.
 bool tdft_supported(int n, int m) {
-    return n >= 2 && m >= 1 && n + m - 1 <= TD_M && m <= TD_ROWS_IN && n <= 2 * TD_ROWS_IN;
+    return n >= 2 && m >= 1 && n + m - 1 > TD_M / 2 && n + m - 1 <= TD_M && m <= TD_ROWS_IN && n <= 2 * TD_ROWS_IN;
 }
 
 // Tables of one transform length: chirp[max(n, m)], FFT(b)/M [1024], twiddles [1024].

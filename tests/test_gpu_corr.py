@@ -316,7 +316,7 @@ def test_intensities_with_errors_mode_equal_deferred(gpu, sg):
     assert np.max(np.abs(ia - ib)) < 1e-10 * np.max(np.abs(ia))
 
 
-@pytest.mark.parametrize("nw", [200, 40])
+@pytest.mark.parametrize("nw", [200, 300])
 def test_own_time_transform_matches_cufft(gpu, sg, nw):
     # the hand-written Bluestein time transform of FP32 accumulators against cuFFT's, from
     # the same start: equal up to FP32 rounding of the two transforms
@@ -345,7 +345,8 @@ def test_own_time_transform_matches_cufft(gpu, sg, nw):
 
 
 def test_time_transform_falls_back_beyond_its_length(gpu, sg):
-    # n_all_ω + n_all_ω/2 > 1024 (nω = 400): cuFFT
+    # the own kernel's 1024-point convolution covers 512 < n_all_ω + n_all_ω/2 <= 1024:
+    # nω = 400 and nω = 40 use cuFFT, nω = 300 the own kernel
     s = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=(2, 2, 2), seed=3, precision="fp32")
     s.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
     s.randomize_spins()
@@ -353,5 +354,8 @@ def test_time_transform_falls_back_beyond_its_length(gpu, sg):
     assert sc._lib.sgb_corr_time_transform(sc._h) == 1
     sc2 = sg.SampledCorrelations(s, measure=sg.ssf_trace(s), energies=np.linspace(0, 4.0, 300), dt=0.05, tol=1e-6)
     assert sc2._lib.sgb_corr_time_transform(sc2._h) == 0
+    sc3 = sg.SampledCorrelations(s, measure=sg.ssf_trace(s), energies=np.linspace(0, 4.0, 40), dt=0.05, tol=1e-6)
+    assert sc3._lib.sgb_corr_time_transform(sc3._h) == 1
     sc.close()
     sc2.close()
+    sc3.close()
