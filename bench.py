@@ -43,7 +43,13 @@ DT = 0.025
 # k_batch_midpoint measured 1.547e9 bytes on the 399-step, 20-snapshot launch of the
 # nw=20 case (8 replicas, L=16) and is scaled by steps to the 4,179-step, 200-snapshot
 # launch (its traffic is the snapshot stream plus L2 write-backs, both per step).
-DRAM_BYTES_PER_LAUNCH = {"k_batch_midpoint": 1.547e9 * 4179 / 399}
+# ncu, k_batch_midpoint at L = 16 with 8 replicas, nω = 20 (399 steps, 798 iterations), the
+# shared-index tile shape: DRAM read + write per launch, scaled to the headline's 4,179
+# steps; and L2 sectors × 32 B per site-iteration per tile shape (by neighbour-index
+# source), with the L2 peak that ncu's lts__throughput implies (11.1 TB/s at 33.3 %)
+DRAM_BYTES_PER_LAUNCH = {"k_batch_midpoint": (0.104e9 + 5.714e9) * 4179 / 399}
+L2_BYTES_PER_SITE_ITER = {2: 437.0, 0: 503.0}
+L2_PEAK_GBS_NCU = 33400.0
 
 
 def peaks():
@@ -783,6 +789,18 @@ def main():
     traffic = DRAM_BYTES_PER_LAUNCH.get(dom["kernel"].split()[0]) if (L, NOMEGA, R) == (16, 200, 8) else None
     roof = {"bound": "hbm", "kernel": dom["kernel"], "achieved": dom["achieved_gbs"], "peak": hbm, "unit": "GB/s",
             "frac": dom["achieved_gbs"] / hbm, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs"}
+    # the midpoint kernel's actual bound is L2 (state L2-resident): its L2 bytes per
+    # site-iteration (ncu) times the iterations of this run over the trajectory time
+    shapes = rb["midpoint_shapes"]["shapes"]
+    ch = rb["midpoint_shapes"]["chosen"]
+    idx = shapes[ch].get("nbr_index_bytes_smem") if 0 <= ch < len(shapes) else None
+    if idx in L2_BYTES_PER_SITE_ITER and ph[0]:
+        l2_bytes = L2_BYTES_PER_SITE_ITER[idx] * rb["ns"] * R * rb["iters_per_step"] * nsteps_sample
+        l2_gbs = l2_bytes / (ph[0] * 1e6)
+        roof["l2"] = {"achieved": l2_gbs, "peak": L2_PEAK_GBS_NCU, "unit": "GB/s", "frac": l2_gbs / L2_PEAK_GBS_NCU,
+                      "bytes_per_site_iteration": L2_BYTES_PER_SITE_ITER[idx],
+                      "source": "L2 sectors per site-iteration and the L2 peak from one ncu capture of this shape "
+                                "(L = 16, 8 replicas, nomega = 20)"}
     line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
