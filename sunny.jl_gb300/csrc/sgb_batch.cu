@@ -287,10 +287,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
     using IT = typename std::conditional<IDX == 2, unsigned short, int>::type;
     extern __shared__ __align__(16) unsigned char smem[];
     Tab<R> T = stage_tables<R>(A.M, smem);
-    // IDX 4: int32 [tile][bond][SGB_TILE]; IDX 2: uint16 pairs [tile][bond / 2][SGB_TILE][2],
-    // so that one 32-bit load gives a thread the indices of two consecutive bonds
-    IT* sidx = reinterpret_cast<IT*>(smem + A.M.tables_bytes);
-    const int kbp = (kb + 1) / 2;
+    IT* sidx = reinterpret_cast<IT*>(smem + A.M.tables_bytes);   // [tile][bond][SGB_TILE]
     __shared__ R wpart[SGB_MAXT][SGB_TILE / 32];   // per-warp convergence partials of each tile
     __shared__ unsigned long long conv_mask;   // bit q: replica q met the tolerance this iteration
     __shared__ int4 st_a[SGB_MAXT];            // (replica, first site, count, replica offset)
@@ -321,11 +318,8 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
             st_atom[k][tid] = (unsigned char)c.a;
             if (IDX != 0) {
                 const int nb = T.boff[c.a + 1] - T.boff[c.a];
-                for (int b = 0; b < nb; b++) {
-                    const size_t e = IDX == 2 ? (((size_t)k * kbp + (b >> 1)) * SGB_TILE + tid) * 2 + (b & 1)
-                                              : ((size_t)k * kb + b) * SGB_TILE + tid;
-                    sidx[e] = (IT)__ldg(A.nbr + c.nbo + (size_t)b * c.nsr + c.s);
-                }
+                for (int b = 0; b < nb; b++)
+                    sidx[((size_t)k * kb + b) * SGB_TILE + tid] = (IT)__ldg(A.nbr + c.nbo + (size_t)b * c.nsr + c.s);
             }
         }
     }
@@ -386,18 +380,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                         R gx, gy, gz, dx, dy, dz;
                         const R* HB = Hc + (size_t)MV<R>::K * ti.w;
                         auto nld = [HB, NS](int j, R& x, R& y, R& z) { MV<R>::ld(HB, NS, j, x, y, z); };
-                        if (IDX == 2) {
-                            // bond offsets from b0 arrive in even-based groups of G, so both halves of
-                            // a pair word are read by one load
-                            const unsigned* ip = reinterpret_cast<const unsigned*>(sidx) + (size_t)k * kbp * SGB_TILE + tid;
-                            grad_nbi_ld<R, GEN, G>(
-                                A.M, T, a,
-                                [ip](int b) {
-                                    const unsigned w = ip[(b >> 1) * SGB_TILE];
-                                    return (int)((b & 1) ? (w >> 16) : (w & 0xffffu));
-                                },
-                                nld, s_h[a], s_h[na + a], s_h[2 * na + a], hx, hy, hz, gx, gy, gz);
-                        } else if (IDX == 4) {
+                        if (IDX != 0) {
                             const IT* ip = sidx + (size_t)k * kb * SGB_TILE + tid;
                             grad_nbi_ld<R, GEN, G>(A.M, T, a, [ip](int b) { return (int)ip[b * SGB_TILE]; }, nld,
                                                    s_h[a], s_h[na + a], s_h[2 * na + a], hx, hy, hz, gx, gy, gz);
@@ -828,8 +811,7 @@ static int mid_shapes(sgb_batch* b, std::vector<MidShape>& out) {
                 const long long g = std::min<long long>((long long)bps * b->nsm, b->ntiles);
                 const long long ntb = (b->ntiles + g - 1) / g;
                 if (ntb > SGB_MAXT) continue;
-                const size_t smem = tab + (idx == 2 ? (size_t)ntb * ((b->kb + 1) / 2) * SGB_TILE * 4
-                                                    : idx ? (size_t)ntb * b->kb * SGB_TILE * idx : 0);
+                const size_t smem = tab + (idx ? (size_t)ntb * b->kb * SGB_TILE * idx : 0);
                 MidKernel<R> kern = mid_kernel<R, GEN>(idx, G, bps);
                 if (smem > 48 * 1024 &&
                     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
