@@ -441,6 +441,12 @@ int sgb_batch_midpoint_shapes(const sgb_batch* b, int32_t cap, int32_t* shapes, 
 /* Uses row `row` of sgb_batch_midpoint_shapes for the following batched trajectories, or
  * -1 to time the shapes again at the next one (no counterpart in the reference). */
 int sgb_batch_select_midpoint_shape(sgb_batch* b, int32_t row);
+/* Replicas per launch of the batched midpoint trajectories of add_sample! (no counterpart
+ * in the reference): the replicas of a batch run in launches of at most this many, so that
+ * each launch's working set stays in L2, and one rank-nrep pass then accumulates every
+ * replica's sample. 0 (default) sizes the launches for about 72 MB of working set (8
+ * replicas of 65,536 FP32 sites), in equal chunks. */
+int sgb_batch_set_midpoint_chunk(sgb_batch* b, int32_t replicas);
 /* The batched Langevin kernel's launch shapes (no counterpart in the reference): 4, 3 and
  * 2 CTAs per SM, timed once per couplings on 10 steps at the first Langevin call (FP32;
  * FP64 batches use 2). ms3[k] receives shape k's tuning time (0 not tried, 1e30 does not

@@ -455,7 +455,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                 double t = 0;
 #pragma unroll
                 for (int w = 0; w < SGB_TILE / 32; w++) t += (double)wpart[tid][w];
-                atomicAdd(&X.racc[slot * X.nrep + st_a[tid].x], t);
+                atomicAdd(&X.racc[slot * X.nrep + (st_a[tid].x - X.r0)], t);
             }
             if (leader) {
                 for (int q = 0; q < X.nrep; q++) X.racc[((slot + 1) % 3) * X.nrep + q] = 0.0;
@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
             all_done = (X.nrep == 64) ? (mask == ~0ull) : (mask == ((1ull << X.nrep) - 1));
             for (int k = 0; k < ntb; k++) {
                 const int4 ti = st_a[k];
-                if (((actm >> k) & 1u) && ((mask >> ti.x) & 1ull)) {
+                if (((actm >> k) & 1u) && ((mask >> (ti.x - X.r0)) & 1ull)) {
                     actm &= ~(1u << k);
                     if (tid < ti.z) {
                         const int g = ti.w + ti.y + tid;
@@ -808,8 +808,8 @@ static int mid_shapes(sgb_batch* b, std::vector<MidShape>& out) {
         for (int G : {6, 12}) {
             const int top = G == 12 ? 2 : maxbps;
             for (int bps = top; bps >= std::max(1, top - (top == 4 ? 2 : 1)); bps--) {
-                const long long g = std::min<long long>((long long)bps * b->nsm, b->ntiles);
-                const long long ntb = (b->ntiles + g - 1) / g;
+                const long long g = std::min<long long>((long long)bps * b->nsm, b->mid_ntiles);
+                const long long ntb = (b->mid_ntiles + g - 1) / g;
                 if (ntb > SGB_MAXT) continue;
                 const size_t smem = tab + (idx ? (size_t)ntb * b->kb * SGB_TILE * idx : 0);
                 MidKernel<R> kern = mid_kernel<R, GEN>(idx, G, bps);
@@ -826,7 +826,7 @@ static int mid_shapes(sgb_batch* b, std::vector<MidShape>& out) {
             }
         }
     }
-    if (std::is_same<R, float>::value) blk_shapes(b, GEN, out);
+    if (std::is_same<R, float>::value && b->mid_nchunk == 1) blk_shapes(b, GEN, out);
     if (out.empty()) return bfail(b, SGB_ERR_ARG, "replica batch too large for one persistent launch of the midpoint kernel");
     return SGB_OK;
 }
@@ -1021,9 +1021,31 @@ static int launch_midpoint(sgb_batch* b, BatchArgs<R>& A, MidArgs<R>& X, int nst
     return mid_launch<R, GEN>(b, b->mid_shapes[b->mid_choice], A, X, nsteps, dt, lam, sn);
 }
 
+// Replicas per midpoint launch: as many as keep the launch's working set (about 120 bytes
+// per site in FP32, the state, iterate, history and three midpoint buffers) within about
+// 72 MB of L2, in equal chunks; sgb_batch_set_midpoint_chunk overrides.
+static void mid_chunking(sgb_batch* b) {
+    const int nsr = b->off[1] - b->off[0];
+    int cmax = b->mid_chunk;
+    if (cmax <= 0) {
+        const double per_site = b->fp32 ? 120.0 : 216.0;
+        cmax = (int)std::max(1.0, std::floor(72.0e6 / (per_site * (double)nsr)));
+    }
+    cmax = std::min(cmax, b->nrep);
+    const int nchunk = (b->nrep + cmax - 1) / cmax;
+    const int per = (b->nrep + nchunk - 1) / nchunk;
+    if (nchunk != b->mid_nchunk || per != b->mid_per) {
+        b->mid_nchunk = nchunk;
+        b->mid_per = per;
+        b->mid_choice = -1;   // shapes depend on the tiles per launch
+    }
+    b->mid_ntiles = 0;
+    for (int r = 0; r < std::min(per, b->nrep); r++) b->mid_ntiles += b->tcount[r];
+}
+
 template <class R>
 static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
-    BatchArgs<R> A = bargs<R>(b);
+    mid_chunking(b);
     MidArgs<R> X;
     X.Sp = (R*)b->Sp;
     X.H = (R*)b->H;
@@ -1033,7 +1055,6 @@ static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
     X.H2 = (R*)b->H2;
     X.H3 = (R*)b->H3;
     X.ord = b->mid_order;
-    X.nrep = b->nrep;
     double atol = c->tol * std::sqrt((double)(b->off[1] - b->off[0]));
     X.atol2 = atol * atol;
     X.max_iters = c->max_iters;
@@ -1051,17 +1072,30 @@ static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
     int nsteps = c->measperiod * (c->nsnaps - 1);
     if (b->nrep > SGB_MAXREP_CORR) return bfail(b, SGB_ERR_ARG, "batched sampling supports at most 64 replicas");
     R dt = (R)c->dt, lam = (R)c->damping;
-    int rc = A.M.general ? launch_midpoint<R, true>(b, A, X, nsteps, dt, lam, sn)
-                         : launch_midpoint<R, false>(b, A, X, nsteps, dt, lam, sn);
-    if (rc) return rc;
-    Ctrl st;
-    if ((rc = read_status(b, &st))) return rc;
-    c->prof_iters_last = st.iters;
-    if (st.status == SGB_ERR_NOCONVERGE)
-        return bfail(b, SGB_ERR_NOCONVERGE, "Spherical midpoint method failed to converge to tolerance " +
-                                                std::to_string(c->tol) + " after " + std::to_string(c->max_iters) +
-                                                " iterations.");
-    if (st.status != 0) return bfail(b, st.status, "batched midpoint kernel reported an error");
+    int64_t iters = 0;
+    // one launch per chunk of replicas; their snapshots land in their own rows of the
+    // accumulator's time series, which one rank-nrep pass then accumulates
+    for (int r0 = 0; r0 < b->nrep; r0 += b->mid_per) {
+        const int cn = std::min(b->mid_per, b->nrep - r0);
+        BatchArgs<R> A = bargs<R>(b);
+        const int t0 = b->tfirst[r0], t1 = b->tfirst[r0 + cn - 1] + b->tcount[r0 + cn - 1];
+        A.td = b->td + 2 * (size_t)t0;
+        A.ntiles = t1 - t0;
+        X.nrep = cn;
+        X.r0 = r0;
+        int rc = A.M.general ? launch_midpoint<R, true>(b, A, X, nsteps, dt, lam, sn)
+                             : launch_midpoint<R, false>(b, A, X, nsteps, dt, lam, sn);
+        if (rc) return rc;
+        Ctrl st;
+        if ((rc = read_status(b, &st))) return rc;
+        iters += st.iters;
+        if (st.status == SGB_ERR_NOCONVERGE)
+            return bfail(b, SGB_ERR_NOCONVERGE, "Spherical midpoint method failed to converge to tolerance " +
+                                                    std::to_string(c->tol) + " after " + std::to_string(c->max_iters) +
+                                                    " iterations.");
+        if (st.status != 0) return bfail(b, st.status, "batched midpoint kernel reported an error");
+    }
+    c->prof_iters_last = iters;
     return SGB_OK;
 }
 
@@ -1617,6 +1651,13 @@ int sgb_batch_langevin_shapes(const sgb_batch* b, float* ms3, int32_t* chosen_bp
         for (int k = 0; k < 3; k++) ms3[k] = b->heun_ms[k];
     if (chosen_bps) *chosen_bps = b->heun_bps;
     return 3;
+}
+
+int sgb_batch_set_midpoint_chunk(sgb_batch* b, int32_t replicas) {
+    if (!b) return bfail(nullptr, SGB_ERR_ARG, "null handle");
+    if (replicas < 0 || replicas > 64) return bfail(b, SGB_ERR_ARG, "replicas per midpoint launch must be in [0, 64] (0: sized for L2)");
+    b->mid_chunk = replicas;
+    return SGB_OK;
 }
 
 int sgb_batch_select_midpoint_shape(sgb_batch* b, int32_t row) {

@@ -40,7 +40,8 @@ struct MidArgs {
     R* H2;
     R* H3;
     int ord;        // initial iterate of each step: 0 S' = S (as the reference), k > 0 polynomial extrapolation of order k
-    int nrep;
+    int nrep;       // replicas of this launch: r0 .. r0 + nrep - 1 (convergence sums and masks relative to r0)
+    int r0;
     double atol2;
     int max_iters;
 };

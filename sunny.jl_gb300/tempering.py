@@ -193,6 +193,11 @@ class ReplicaBatch:
         the default, 4 s)."""
         self._check(self._lib.sgb_batch_set_wait_limit(self._h, float(seconds)))
 
+    def set_midpoint_chunk(self, replicas: int):
+        """Replicas per launch of batched add_sample! trajectories (0: as many as keep a
+        launch's working set in L2); every replica's sample still goes into one pass."""
+        self._check(self._lib.sgb_batch_set_midpoint_chunk(self._h, int(replicas)))
+
     def set_midpoint_predictor(self, order: int):
         """First iterate of each batched midpoint step: 0 S' = S (the reference's choice),
         k in 1..4 the degree-k extrapolation of the last k+1 states (fewer iterations, same

@@ -196,3 +196,32 @@ def test_every_midpoint_shape_gives_the_same_trajectory(gpu, sg):
     for k in range(1, n):
         assert np.max(np.abs(finals[k] - finals[0])) < 1e-3, (kinds[k], np.max(np.abs(finals[k] - finals[0])))
         assert np.max(np.abs(datas[k] - datas[0])) <= 1e-4 * np.max(np.abs(datas[0]))
+
+
+def test_chunked_midpoint_launches_match_one_launch(gpu, sg):
+    # replicas run in launches of 1 or 2 (their samples still go into one rank-4 pass):
+    # each replica's iteration sequence is its own, so states and spectra agree with the
+    # single launch up to rounding (convergence-sum order)
+    proto = sg.System(sg.pyrochlore_crystal(), [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(4, 4, 4), seed=6,
+                      precision="fp32", device=None)
+    proto.set_exchange(1.0, proto.crystal.bonds_at_distance(np.sqrt(2) / 4)[0])
+    b = sg.ReplicaBatch(proto, [(4, 4, 4)] * 4, kT=[0.2] * 4, precision="fp32", seed=4)
+    b.randomize_spins()
+    b.langevin(0.025, 0.1, 200)
+    start = [b.get_state(r) for r in range(4)]
+    kw = dict(energies=np.linspace(0, 6, 12), dt=0.025, tol=1e-6)
+    finals, datas = [], []
+    for chunk in (0, 2, 1):
+        for r in range(4):
+            b.set_state(r, start[r])
+        b.set_midpoint_chunk(chunk)
+        sc = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), **kw)
+        sg.add_sample(sc, b)
+        assert sc.nsamples == 4
+        finals.append(np.concatenate([b.get_state(r) for r in range(4)]))
+        datas.append(sc.data)
+        sc.close()
+    for k in (1, 2):
+        assert np.max(np.abs(finals[k] - finals[0])) < 1e-3
+        assert np.max(np.abs(datas[k] - datas[0])) <= 1e-4 * np.max(np.abs(datas[0]))
+    b.close()
