@@ -6,7 +6,7 @@
 namespace sgbbatch {
 using namespace sgbdev;
 
-#define SGB_TILE 256
+#define SGB_TILE 288
 #define SGB_MAXT 8
 
 template <class R>
