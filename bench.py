@@ -158,7 +158,8 @@ def run_arm(sg, precision, device, warmup, steps, tol, thermal_steps=2000, e2e_s
     return res
 
 
-def stated_error(sg, device, L_=16, nomega=200, nrep=8, nsamples=32, decorr=1000, thermal_steps=2000, seed=11):
+def stated_error(sg, device, L_=16, nomega=200, nrep=8, nsamples=32, decorr=1000, thermal_steps=2000, seed=11, tol32=1e-6,
+                 first_accept=False):
     """Error of the FP32 batched S(q,w) path against the plain FP64 path on the pyrochlore
     model with L_^3 conventional cells (L_=16, nomega=200 is the benchmark workload).
 
@@ -193,12 +194,14 @@ def stated_error(sg, device, L_=16, nomega=200, nrep=8, nsamples=32, decorr=1000
     energies = np.linspace(0, WMAX, nomega)
     proto = model("fp32", None)
     b = sg.ReplicaBatch(proto, [proto.dims] * nrep, kT=[0.2] * nrep, precision="fp32", device=device, seed=seed)
+    if first_accept:
+        b.set_midpoint_first_accept(True)
     b.randomize_spins()
     b.langevin(DT, 0.1, thermal_steps)
     s64 = model("fp64", device)
     diag = sg.MeasureSpec(sg.ssf_trace(proto).observables, [(1, 1), (2, 2), (3, 3)])
     kw = dict(measure=diag, energies=energies, dt=DT, calculate_errors=True)
-    sc32 = [sg.SampledCorrelations(b, tol=1e-6, **kw) for _ in range(2)]
+    sc32 = [sg.SampledCorrelations(b, tol=tol32, **kw) for _ in range(2)]
     sc64 = [sg.SampledCorrelations(s64, tol=1e-12, **kw) for _ in range(2)]
     nsteps = sc32[0].measperiod * (sc32[0].n_all_omega // 2)
     npass = max(2, nsamples // nrep)
@@ -244,11 +247,12 @@ def stated_error(sg, device, L_=16, nomega=200, nrep=8, nsamples=32, decorr=1000
             "sqw_systematic": sysd,
             "sqw_systematic_rel_rms": sysd["bias_rel"],
             "sqw_systematic_rel_rms_upper": sysd["bias_rel_upper"],
-            "steps_per_sample": nsteps, "wall_s": wall,
+            "steps_per_sample": nsteps, "wall_s": wall, "fp32_tol": tol32, "first_accept": first_accept,
             "limits": {"energy_rel_err": 1e-5, "sqw_per_bin_rel": 1e-2}}
 
 
-def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000, predictor=None, mid_shape=None):
+def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000, predictor=None, mid_shape=None,
+                first_accept=False):
     """Batched FP32 sampling: `nrep` replicas of the pyrochlore model advance in one
     persistent launch; each add_sample adds nrep samples with a rank-nrep accumulator pass.
     `mid_shape` (a row of sgb_batch_midpoint_shapes) replaces the autotuner's choice after
@@ -259,6 +263,8 @@ def run_batched(sg, device, nrep, warmup, steps, tol, thermal_steps=2000, predic
     b = sg.ReplicaBatch(proto, [proto.dims] * nrep, kT=[0.2] * nrep, precision="fp32", device=device, seed=7)
     if predictor is not None:
         b.set_midpoint_predictor(predictor)
+    if first_accept:
+        b.set_midpoint_first_accept(True)
     b.randomize_spins()
     b.langevin(DT, 0.1, thermal_steps)
     sc = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), energies=np.linspace(0, WMAX, NOMEGA), dt=DT, tol=tol)
@@ -692,6 +698,9 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the tempering and Langevin site-step arms")
     ap.add_argument("--no-error", action="store_true", help="skip the stated-error measurement (FP32 vs FP64)")
     ap.add_argument("--error-samples", type=int, default=32, help="samples per path of the stated-error measurement")
+    ap.add_argument("--tol", type=float, default=1e-6, help="FP32 batched midpoint tolerance (per-site RMS)")
+    ap.add_argument("--first-accept", action="store_true",
+                    help="batched midpoint: convergence test from the extrapolated first iterate on")
     ap.add_argument("--mid-shape", type=int, default=None,
                     help="batched midpoint launch shape (row of the autotuner's table) after the first warm-up sample")
     ap.add_argument("--predictor", type=int, default=None,
@@ -732,8 +741,8 @@ def main():
         return float(t.item())
 
     barrier()
-    rb = run_batched(sg, local, args.nrep, args.warmup, args.steps, tol=1e-6, predictor=args.predictor,
-                     mid_shape=args.mid_shape)
+    rb = run_batched(sg, local, args.nrep, args.warmup, args.steps, tol=args.tol, predictor=args.predictor,
+                     mid_shape=args.mid_shape, first_accept=args.first_accept)
     barrier()
     r32 = run_arm(sg, "fp32", local, args.warmup, max(2, args.steps // 2), tol=1e-6)
     # (single-system FP32 path: one replica per add_sample)
@@ -760,7 +769,8 @@ def main():
         extra["c3_sqw"] = c3
     err = None
     if not args.no_error:
-        err = stated_error(sg, local, L_=L, nomega=NOMEGA, nrep=args.nrep, nsamples=args.error_samples)
+        err = stated_error(sg, local, L_=L, nomega=NOMEGA, nrep=args.nrep, nsamples=args.error_samples, tol32=args.tol,
+                           first_accept=args.first_accept)
     barrier()
     ms = maxall(rb["ms"])
     value = world * args.steps * rb["nrep"] / (ms / 1000.0)
@@ -810,7 +820,7 @@ def main():
                                    f"{R} replicas per batched add_sample ({R * args.steps} samples timed)",
                        "global_batch": world * R, "seq_len": nsteps_sample, "parallelism": f"replicas x{world * R}",
                        "l2": "inputs larger than L2 (40 GB accumulator streamed every step)",
-                       "midpoint_tol": {"fp32": 1e-6, "fp64": 1e-12}},
+                       "midpoint_tol": {"fp32": args.tol, "fp64": 1e-12}, "first_accept": args.first_accept},
             "site_steps_per_s": site_steps,
             "fp32_single": {"value": v32, "unit": "samples/s", "ms_per_step": r32["ms"] / max(2, args.steps // 2),
                             "phase_ms": r32["phase_ms"], "iters_per_step": r32["iters_per_step"]},

@@ -447,6 +447,12 @@ int sgb_batch_select_midpoint_shape(sgb_batch* b, int32_t row);
  * replica's sample. 0 (default) sizes the launches for about 72 MB of working set (8
  * replicas of 65,536 FP32 sites), in equal chunks. */
 int sgb_batch_set_midpoint_chunk(sgb_batch* b, int32_t replicas);
+/* With an extrapolated first iterate (predictor order > 0), also apply the convergence
+ * test Σ|S' − S''|² <= (tol √Ns)² to the first iteration, whose S' is the extrapolation,
+ * so that a step can end after one iteration when the extrapolation is that good (no
+ * counterpart in the reference, whose first iterate S' = S never passes). The next-step
+ * data are then prepared at every iteration. Default off. */
+int sgb_batch_set_midpoint_first_accept(sgb_batch* b, int32_t on);
 /* The batched Langevin kernel's launch shapes (no counterpart in the reference): 4, 3 and
  * 2 CTAs per SM, timed once per couplings on 10 steps at the first Langevin call (FP32;
  * FP64 batches use 2). ms3[k] receives shape k's tuning time (0 not tried, 1e30 does not

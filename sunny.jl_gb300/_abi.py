@@ -121,6 +121,7 @@ SIGNATURES = {
     "sgb_batch_set_midpoint_predictor": (C.c_int, [_P, _I32]),
     "sgb_batch_midpoint_shapes": (C.c_int, [_P, _I32, C.POINTER(_I32), C.POINTER(C.c_float), C.POINTER(_I32)]),
     "sgb_batch_langevin_shapes": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(_I32)]),
+    "sgb_batch_set_midpoint_first_accept": (C.c_int, [_P, _I32]),
     "sgb_batch_set_midpoint_chunk": (C.c_int, [_P, _I32]),
     "sgb_batch_select_midpoint_shape": (C.c_int, [_P, _I32]),
     "sgb_adjoint_create": (C.c_int, [_P, C.POINTER(CorrDesc), _I32, _P, C.POINTER(_I32), _D, C.POINTER(_P)]),

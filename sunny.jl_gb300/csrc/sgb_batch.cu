@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                         // With an extrapolated first iterate the step is never accepted at its
                         // first iteration (see the convergence mask below), so the next-step data
                         // are only prepared from the second iteration on.
-                        if (X.ord == 0 || it > 0) {
+                        if (X.ord == 0 || X.accept0 || it > 0) {
                         R cx = nx, cy = ny, cz = nz;
                         normalize_dip<R>(cx, cy, cz, kap);
                         // next step's first iterate p and midpoint spin normalize((c + p)/2)
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                 unsigned long long m = 0;
                 // the convergence test of the reference, Σ|S' - S''|² <= atol²; with an
                 // extrapolated first iterate it is applied from the second iteration on
-                if (X.ord == 0 || it > 0)
+                if (X.ord == 0 || X.accept0 || it > 0)
                     for (int q = 0; q < X.nrep; q++)
                         if (X.racc[slot * X.nrep + q] <= X.atol2) m |= 1ull << q;
                 conv_mask = m;
@@ -1055,6 +1055,7 @@ static int batch_trajectory(sgb_corr* c, sgb_batch* b) {
     X.H2 = (R*)b->H2;
     X.H3 = (R*)b->H3;
     X.ord = b->mid_order;
+    X.accept0 = b->mid_accept0;
     double atol = c->tol * std::sqrt((double)(b->off[1] - b->off[0]));
     X.atol2 = atol * atol;
     X.max_iters = c->max_iters;
@@ -1651,6 +1652,12 @@ int sgb_batch_langevin_shapes(const sgb_batch* b, float* ms3, int32_t* chosen_bp
         for (int k = 0; k < 3; k++) ms3[k] = b->heun_ms[k];
     if (chosen_bps) *chosen_bps = b->heun_bps;
     return 3;
+}
+
+int sgb_batch_set_midpoint_first_accept(sgb_batch* b, int32_t on) {
+    if (!b) return bfail(nullptr, SGB_ERR_ARG, "null handle");
+    b->mid_accept0 = on ? 1 : 0;
+    return SGB_OK;
 }
 
 int sgb_batch_set_midpoint_chunk(sgb_batch* b, int32_t replicas) {

@@ -42,6 +42,8 @@ struct MidArgs {
     int ord;        // initial iterate of each step: 0 S' = S (as the reference), k > 0 polynomial extrapolation of order k
     int nrep;       // replicas of this launch: r0 .. r0 + nrep - 1 (convergence sums and masks relative to r0)
     int r0;
+    int accept0;    // with ord > 0: the convergence test also applies at the first iteration (whose
+                    // iterate is the extrapolated one), so the next-step data are prepared at every iteration
     double atol2;
     int max_iters;
 };

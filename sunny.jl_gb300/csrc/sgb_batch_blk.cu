@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(NT, 1) k_batch_midpoint_blk(BatchArgs<float> A
                     float mxv = (sx + nx) / 2, myv = (sy + ny) / 2, mzv = (sz + nz) / 2;
                     normalize_dip<float>(mxv, myv, mzv, kap);
                     store_pad(Hn, B, bk.x, a, cx, cy, cz, make_float4(mxv, myv, mzv, 0.f));
-                    if (X.ord == 0 || it > 0) {
+                    if (X.ord == 0 || X.accept0 || it > 0) {
                         float cx_ = nx, cy_ = ny, cz_ = nz;
                         normalize_dip<float>(cx_, cy_, cz_, kap);
                         float px = cx_, py = cy_, pz = cz_;
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(NT, 1) k_batch_midpoint_blk(BatchArgs<float> A
             itg++;
             if (tid == 0) {
                 unsigned long long m = 0;
-                if (X.ord == 0 || it > 0)
+                if (X.ord == 0 || X.accept0 || it > 0)
                     for (int q = 0; q < X.nrep; q++)
                         if (X.racc[slot * X.nrep + q] <= X.atol2) m |= 1ull << q;
                 conv_mask = m;

@@ -195,6 +195,7 @@ struct sgb_batch {
     std::vector<BlkMaps> blk_maps;  // tensor maps of the cell-block shapes
     int mid_choice = -1;            // shape picked by the autotuner (-1: not tuned for these couplings)
     int mid_chunk = 0;              // replicas per midpoint launch requested (0: sized for L2)
+    int mid_accept0 = 0;            // convergence test also at the extrapolated first iterate
     int mid_nchunk = 1, mid_per = 0, mid_ntiles = 0;   // launches per trajectory, replicas and tiles per launch
     // batched Langevin launch shapes: CTAs per SM 4, 3, 2 (FP32) or 2 (FP64), timed once per
     // couplings; heun_ms[k] the time of shape k's tuning run (0: not tried, 1e30: does not fit)

@@ -193,6 +193,10 @@ class ReplicaBatch:
         the default, 4 s)."""
         self._check(self._lib.sgb_batch_set_wait_limit(self._h, float(seconds)))
 
+    def set_midpoint_first_accept(self, on: bool):
+        """Apply the midpoint convergence test from the first (extrapolated) iterate on."""
+        self._check(self._lib.sgb_batch_set_midpoint_first_accept(self._h, 1 if on else 0))
+
     def set_midpoint_chunk(self, replicas: int):
         """Replicas per launch of batched add_sample! trajectories (0: as many as keep a
         launch's working set in L2); every replica's sample still goes into one pass."""
