@@ -103,17 +103,13 @@ constexpr int TD_JMAX = 11;            // registers that can hold samples (m <= 
 constexpr int TD_ROWS_IN = 32 * TD_JMAX;
 constexpr int TD_LD = TD_WARPS + 1;    // staging row stride: lanes 32 rows apart hit distinct banks
 
-constexpr int TD_TILE = 32 * 33;                       // one warp's transpose tile
-constexpr int TD_SMEM = TD_WARPS * TD_TILE > TD_ROWS_IN * TD_LD ? TD_WARPS * TD_TILE : TD_ROWS_IN * TD_LD;
-
-__global__ void __launch_bounds__(32 * TD_WARPS, 3)
+__global__ void __launch_bounds__(32 * TD_WARPS, 2)
 k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long ncols, long long stride, long long rep_stride,
            int n, int m, const float2* __restrict__ chirp, const float2* __restrict__ fb, const float2* __restrict__ tw) {
-    // one buffer, used in turn as the staged samples [t][series], the warps' transpose tiles
-    // and the staged spectra [k][series] (67.6 KB: three CTAs per SM); the twiddles
-    // tw[k][lane] = exp(−2πi lane k / 1024) come through L1
-    __shared__ float2 s_buf[TD_SMEM];
-    float2* s_io = s_buf;
+    __shared__ float2 s_tw[TD_M];                  // [k][lane] = exp(−2πi lane k / 1024)
+    __shared__ float2 s_t[TD_WARPS][32 * 33];      // per-warp transpose tile
+    __shared__ float2 s_io[TD_ROWS_IN * TD_LD];    // staged samples [t][series], later spectra [k][series]
+    for (int i = threadIdx.x; i < TD_M; i += blockDim.x) s_tw[i] = tw[i];
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     const long long col0 = (long long)blockIdx.x * TD_WARPS;
     const long long col = col0 + wp;
@@ -129,7 +125,7 @@ k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long nc
     __syncthreads();
     if (col >= ncols) return;
     const long long base = (col / stride) * rep_stride + (col % stride);
-    float2* T = s_buf + wp * TD_TILE;
+    float2* T = s_t[wp];
     float2 v[32];
     // a_t = x_t w_t at t = 32 j + lane (zero beyond the snapshots)
 #pragma unroll
@@ -139,12 +135,11 @@ k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long nc
             v[j] = cmulf(rowwise ? s_io[t * TD_LD + wp] : __ldg(A + base + (long long)t * stride), __ldg(chirp + t));
         else v[j] = make_float2(0.f, 0.f);
     }
-    if (rowwise) __syncthreads();   // every warp has its samples before the tiles overwrite them
     // forward FFT: DFT over j (index 32 j + lane), twiddle exp(−2πi lane k1/1024), transpose,
     // DFT over the former lanes; lane then holds frequency lane + 32 k2 in v[bitrev5(k2)]
     dft32_dif_first(v);
 #pragma unroll
-    for (int k1 = 0; k1 < 32; k1++) T[lane * 33 + k1] = cmulf(v[bitrev5(k1)], __ldg(tw + k1 * 32 + lane));
+    for (int k1 = 0; k1 < 32; k1++) T[lane * 33 + k1] = cmulf(v[bitrev5(k1)], s_tw[k1 * 32 + lane]);
     __syncwarp();
 #pragma unroll
     for (int j2 = 0; j2 < 32; j2++) v[j2] = T[j2 * 33 + lane];
@@ -161,7 +156,7 @@ k_time_dft(const float2* __restrict__ A, float2* __restrict__ Ahat, long long nc
         for (int k2 = 0; k2 < 32; k2++) u[k2] = v[bitrev5(k2)];
         dft32_dif<true>(u);
 #pragma unroll
-        for (int j1 = 0; j1 < 32; j1++) T[lane * 33 + j1] = cmulcf(u[bitrev5(j1)], __ldg(tw + j1 * 32 + lane));
+        for (int j1 = 0; j1 < 32; j1++) T[lane * 33 + j1] = cmulcf(u[bitrev5(j1)], s_tw[j1 * 32 + lane]);
     }
     __syncwarp();
 #pragma unroll
