@@ -225,3 +225,37 @@ def test_chunked_midpoint_launches_match_one_launch(gpu, sg):
         assert np.max(np.abs(finals[k] - finals[0])) < 1e-3
         assert np.max(np.abs(datas[k] - datas[0])) <= 1e-4 * np.max(np.abs(datas[0]))
     b.close()
+
+
+def test_first_iterate_acceptance_reaches_the_fixed_point(gpu, sg):
+    # with the convergence test applied from the extrapolated first iterate on, a loose
+    # tolerance ends most steps after one iteration; each step still meets the test, so the
+    # trajectory stays within the tolerance's scale of the default one over a short run
+    proto = sg.System(sg.pyrochlore_crystal(), [(1, sg.Moment(s=1.5, g=2))], "dipole", dims=(4, 4, 4), seed=6,
+                      precision="fp32", device=None)
+    proto.set_exchange(1.0, proto.crystal.bonds_at_distance(np.sqrt(2) / 4)[0])
+    b = sg.ReplicaBatch(proto, [(4, 4, 4)] * 2, kT=[0.2] * 2, precision="fp32", seed=4)
+    b.randomize_spins()
+    b.langevin(0.025, 0.1, 300)
+    start = [b.get_state(r) for r in range(2)]
+    kw = dict(energies=np.linspace(0, 6, 8), dt=0.025, tol=1e-5)
+    finals, iters = [], []
+    for on in (False, True):
+        for r in range(2):
+            b.set_state(r, start[r])
+        b.set_midpoint_first_accept(on)
+        sc = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), **kw)
+        sc._lib.sgb_corr_profile(sc._h, 1)
+        sg.add_sample(sc, b)
+        import ctypes as C
+        ph = np.zeros(4)
+        n = C.c_int64()
+        it = C.c_int64()
+        sc._lib.sgb_corr_phase_times(sc._h, ph.ctypes.data_as(C.POINTER(C.c_double)), C.byref(n), C.byref(it))
+        iters.append(it.value)
+        finals.append(np.concatenate([b.get_state(r) for r in range(2)]))
+        sc.close()
+    nsteps = 21 * 7
+    assert iters[1] < iters[0] and iters[1] <= 1.2 * nsteps
+    assert np.max(np.abs(finals[1] - finals[0])) < 1e-2
+    b.close()

@@ -359,3 +359,28 @@ def test_time_transform_falls_back_beyond_its_length(gpu, sg):
     sc.close()
     sc2.close()
     sc3.close()
+
+
+def test_own_time_transform_with_series_straddling_replicas(gpu, sg):
+    # 3 observables x 1 sublattice x 27 cells = 81 series per replica: CTAs of 8 series
+    # straddle replicas and take the per-series path
+    proto = sg.System(sg.cubic_crystal(), [(1, sg.Moment(s=1, g=2))], "dipole", dims=(3, 3, 3), seed=8,
+                      precision="fp32", device=None)
+    proto.set_exchange(1.0, sg.Bond(1, 1, [1, 0, 0]))
+    b = sg.ReplicaBatch(proto, [proto.dims] * 3, kT=[0.5] * 3, precision="fp32", seed=9)
+    b.randomize_spins()
+    b.langevin(0.05, 0.1, 50)
+    start = [b.get_state(r) for r in range(3)]
+    kw = dict(energies=np.linspace(0, 5.0, 200), dt=0.05, tol=1e-6)
+    datas = []
+    for kind in (0, 1):
+        for r in range(3):
+            b.set_state(r, start[r])
+        sc = sg.SampledCorrelations(b, measure=sg.ssf_trace(proto), **kw)
+        assert sc._lib.sgb_corr_set_time_transform(sc._h, kind) == 0
+        assert sc._lib.sgb_corr_time_transform(sc._h) == kind
+        sg.add_sample(sc, b)
+        datas.append(sc.data)
+        sc.close()
+    assert np.max(np.abs(datas[0] - datas[1])) < 2e-5 * np.max(np.abs(datas[1]))
+    b.close()
