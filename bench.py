@@ -48,7 +48,7 @@ DT = 0.025
 # steps; and L2 sectors × 32 B per site-iteration per tile shape (by neighbour-index
 # source), with the L2 peak that ncu's lts__throughput implies (11.1 TB/s at 33.3 %)
 DRAM_BYTES_PER_LAUNCH = {"k_batch_midpoint": (0.104e9 + 5.714e9) * 4179 / 399}
-L2_BYTES_PER_SITE_ITER = {2: 437.0, 0: 503.0}
+L2_BYTES_PER_SITE_ITER = {2: 442.0, 0: 503.0}
 L2_PEAK_GBS_NCU = 33400.0
 
 

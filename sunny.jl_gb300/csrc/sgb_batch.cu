@@ -9,7 +9,7 @@
 //   midpoint per replica        src/Integrators.jl:379-413 (for batched add_sample!)
 //
 // Design: the replicas' states are concatenated in L2-resident SoA arrays and cut into
-// tiles of up to 256 sites of one replica. A persistent cooperative grid walks its tiles
+// tiles of up to SGB_TILE (288) sites of one replica. A persistent cooperative grid walks its tiles
 // between bounded grid barriers, so one barrier serves every replica and the latency of
 // a single small system is amortised over the batch. Per-replica reductions (energies,
 // midpoint convergence sums) are formed per tile in FP64. Parallel tempering keeps a

@@ -6,8 +6,10 @@
 namespace sgbbatch {
 using namespace sgbdev;
 
+// Sites per tile = threads per CTA of the batch kernels (9 warps): 65,536-site replicas split
+// into 228 tiles each, so 8 of them give 1,824 tiles, 4 per CTA of a 3-CTA-per-SM grid.
 #define SGB_TILE 288
-#define SGB_MAXT 8
+#define SGB_MAXT 8    // tiles one CTA of the midpoint kernel may own
 
 template <class R>
 struct BatchArgs {
