@@ -53,10 +53,11 @@ __host__ __device__ inline double biquad_metric(int q) {
 // the status live on separate 128-byte lines so that spinning, atomics and flag reads
 // do not contend for one L2 line.
 //
-// The barrier word packs the arrival count (bits 0-31), the generation (bits 32-62) and
-// an abort flag (bit 63) that sgb_set_status raises, so that an arrival returns the
-// generation it waits on and a waiter sees an error in the word it polls: no extra
-// loads on the barrier's critical path.
+// The barrier word packs an arrival count (bits 0-31), a generation (bits 32-62) and an
+// abort flag (bit 63) that sgb_set_status raises, so that an arrival returns its place in
+// the episode and a waiter sees an error in the word it polls: no extra loads on the
+// barrier's critical path. The last arrival of an episode folds nblocks counts into one
+// generation; arrivals so far = generation * nblocks + count is unchanged by the fold.
 #define SGB_BAR_GEN 0x100000000ull
 #define SGB_BAR_ABORT 0x8000000000000000ull
 struct alignas(128) Ctrl {
@@ -106,7 +107,13 @@ __device__ __forceinline__ uint64_t sgb_wait_limit(const Ctrl* c) {
 
 // Barrier across `nblocks` co-resident CTAs (cooperative launch guarantees residency).
 // Memory written before the barrier by any CTA is visible to plain loads of every CTA
-// after it (fences around the arrival, as cooperative-groups grid sync does).
+// after it: each CTA's bar.sync orders its writes before its leader's release arrival,
+// and a waiter's acquire fence follows its last read of the word.
+// A waiter leaves once the arrivals reach the end of its episode, so the last arrival's
+// own add releases everyone and its fold of the count travels behind it, off the
+// critical path. At the start of a launch the count field is zero (every episode of an
+// earlier launch has folded, and launches clear the word), so the arrivals so far are a
+// multiple of any nblocks.
 // Returns false if the wait timed out or some CTA raised an error (sgb_set_status).
 __device__ __forceinline__ bool sgb_grid_barrier(Ctrl* c, unsigned int nblocks) {
     __shared__ int ok_s;
@@ -115,37 +122,44 @@ __device__ __forceinline__ bool sgb_grid_barrier(Ctrl* c, unsigned int nblocks) 
         int ok = 1;
         if (nblocks > 1) {
             cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> bar(c->bar);
-            __threadfence();
             const unsigned long long prev = bar.fetch_add(1ull, cuda::memory_order_acq_rel);
-            const unsigned long long gen = prev >> 32;   // generation and abort flag
             if (prev & SGB_BAR_ABORT) {
                 ok = 0;
-            } else if ((unsigned int)prev == nblocks - 1) {
-                // last arrival: count back to 0 and the next generation, in one release
-                bar.fetch_add(SGB_BAR_GEN - nblocks, cuda::memory_order_release);
             } else {
-                uint64_t t0 = 0, lim = 0;
-                unsigned int spins = 0;
-                for (;;) {
-                    const unsigned long long now = bar.load(cuda::memory_order_acquire);
-                    if ((now >> 32) != gen) {
-                        if (now & SGB_BAR_ABORT) ok = 0;
-                        break;
-                    }
-                    if ((++spins & 255u) == 0) {
-                        uint64_t t = sgb_globaltimer();
-                        if (t0 == 0) {
-                            t0 = t;
-                            lim = sgb_wait_limit(c);
-                        } else if (t - t0 > lim) {
-                            sgb_set_status(c, SGB_ERR_TIMEOUT);
+                // the count is below 2 * nblocks: at or above nblocks, the previous
+                // episode's fold has not landed yet and this arrival opens the next one
+                const unsigned long long gen = (prev >> 32) & 0x7fffffffull;
+                const unsigned int cnt = (unsigned int)prev;
+                const bool late = cnt >= nblocks;
+                const unsigned int pos = late ? cnt - nblocks : cnt;
+                const unsigned long long target = (gen + (late ? 2ull : 1ull)) * nblocks;
+                if (pos == nblocks - 1) {
+                    bar.fetch_add(SGB_BAR_GEN - nblocks, cuda::memory_order_relaxed);
+                } else {
+                    uint64_t t0 = 0, lim = 0;
+                    unsigned int spins = 0;
+                    for (;;) {
+                        const unsigned long long now = bar.load(cuda::memory_order_relaxed);
+                        if (now & SGB_BAR_ABORT) {
                             ok = 0;
                             break;
                         }
+                        if (((now >> 32) & 0x7fffffffull) * nblocks + (unsigned int)now >= target) break;
+                        if ((++spins & 255u) == 0) {
+                            uint64_t t = sgb_globaltimer();
+                            if (t0 == 0) {
+                                t0 = t;
+                                lim = sgb_wait_limit(c);
+                            } else if (t - t0 > lim) {
+                                sgb_set_status(c, SGB_ERR_TIMEOUT);
+                                ok = 0;
+                                break;
+                            }
+                        }
                     }
+                    cuda::atomic_thread_fence(cuda::memory_order_acquire, cuda::thread_scope_device);
                 }
             }
-            __threadfence();
         } else if (cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>(c->bar).load(
                        cuda::memory_order_relaxed) & SGB_BAR_ABORT) {
             ok = 0;
