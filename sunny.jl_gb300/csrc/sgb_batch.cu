@@ -342,6 +342,12 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
     if (!sgb_grid_barrier(A.ctrl, gridDim.x)) return;
     long long itg = 0;
     int done = 0;
+    // With an extrapolated first iterate (ord > 0) a step is accepted lazily: the first
+    // iteration of the next step computes normalize(S'') from the last iterate, which the
+    // iterate buffer still holds, stores it as the state and shifts the history, beside its
+    // other loads; the iterate comes from the first-iterate buffer. Every replica accepts
+    // exactly once per step, so each step after the first starts with all tiles pending.
+    const bool lazy = X.ord > 0;
     for (int step = 0; step < nsteps; ++step) {
         unsigned actm = (1u << ntb) - 1u;   // bit k: tile k's replica is still iterating
         // first iterate S' = S; with extrapolation (ord > 0) the converging iteration of the
@@ -357,6 +363,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
         const int ord = min(X.ord, step + 1);   // extrapolation order available for the next step
         bool all_done = false;
         for (int it = 0; it < X.max_iters; ++it) {
+            const bool pend = lazy && step > 0 && it == 0;   // accept the previous step here
             const int nxt = (cur + 1) % 3, nst = (cur + 2) % 3;
             const R* Hc = X.H + (size_t)cur * MV<R>::W * NS;
             R* Hn = X.H + (size_t)nxt * MV<R>::W * NS;
@@ -371,9 +378,30 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                     if (on) {
                         const int a = st_atom[k][tid];
                         const R kap = s_kap[a];
-                        R sx = A.S[g], sy = A.S[NS + g], sz = A.S[2 * NS + g];
-                        R qx, qy, qz, hx, hy, hz;
-                        PV<R>::ld(X.Sp, NS, g, qx, qy, qz);
+                        R sx, sy, sz, qx, qy, qz, hx, hy, hz;
+                        if (pend) {
+                            // the previous step's accepted state normalize(S''); S_n joins
+                            // the history (S_{n-2} -> H3, S_{n-1} -> H2, S_n -> H1)
+                            const R ox = A.S[g], oy = A.S[NS + g], oz = A.S[2 * NS + g];
+                            PV<R>::ld(X.Sp, NS, g, sx, sy, sz);
+                            PV<R>::ld(X.P1, NS, g, qx, qy, qz);
+                            normalize_dip<R>(sx, sy, sz, kap);
+                            if (X.ord >= 4) {
+                                R ux, uy, uz;
+                                PV<R>::ld(X.H2, NS, g, ux, uy, uz);
+                                PV<R>::st(X.H3, NS, g, ux, uy, uz);
+                            }
+                            if (X.ord >= 3) {
+                                R ux, uy, uz;
+                                PV<R>::ld(X.H1, NS, g, ux, uy, uz);
+                                PV<R>::st(X.H2, NS, g, ux, uy, uz);
+                            }
+                            if (X.ord >= 2) PV<R>::st(X.H1, NS, g, ox, oy, oz);
+                            A.S[g] = sx; A.S[NS + g] = sy; A.S[2 * NS + g] = sz;
+                        } else {
+                            sx = A.S[g]; sy = A.S[NS + g]; sz = A.S[2 * NS + g];
+                            PV<R>::ld(X.Sp, NS, g, qx, qy, qz);
+                        }
                         // own midpoint spin normalize((S + S')/2): stored by the previous
                         // iteration (or step) with exactly this arithmetic
                         MV<R>::ld(Hc, NS, g, hx, hy, hz);
@@ -480,29 +508,12 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                 const int4 ti = st_a[k];
                 if (((actm >> k) & 1u) && ((mask >> (ti.x - X.r0)) & 1ull)) {
                     actm &= ~(1u << k);
-                    if (tid < ti.z) {
+                    if (!lazy && tid < ti.z) {
                         const int g = ti.w + ti.y + tid;
                         // the accepted state normalize(S''), from the last iterate
                         R x, y, z;
                         PV<R>::ld(X.Sp, NS, g, x, y, z);
                         normalize_dip<R>(x, y, z, s_kap[st_atom[k][tid]]);
-                        if (X.ord > 0) {
-                            // shift the history: S_{n-2} -> H3, S_{n-1} -> H2, S_n -> H1
-                            if (X.ord >= 4) {
-                                R hx, hy, hz;
-                                PV<R>::ld(X.H2, NS, g, hx, hy, hz);
-                                PV<R>::st(X.H3, NS, g, hx, hy, hz);
-                            }
-                            if (X.ord >= 3) {
-                                R hx, hy, hz;
-                                PV<R>::ld(X.H1, NS, g, hx, hy, hz);
-                                PV<R>::st(X.H2, NS, g, hx, hy, hz);
-                            }
-                            if (X.ord >= 2) PV<R>::st(X.H1, NS, g, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
-                            R px, py, pz;
-                            PV<R>::ld(X.P1, NS, g, px, py, pz);
-                            PV<R>::st(X.Sp, NS, g, px, py, pz);
-                        }
                         A.S[g] = x; A.S[NS + g] = y; A.S[2 * NS + g] = z;
                     }
                 }
@@ -523,8 +534,25 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                 const int4 ti = st_a[k];
                 if (tid >= ti.z) continue;
                 const int s = ti.y + tid, g = ti.w + s;
-                snap_write<R>(sn, ti.x, sn.t0 + done / sn.measperiod, s, st_b[k].x, A.S[g], A.S[NS + g], A.S[2 * NS + g]);
+                R x = A.S[g], y = A.S[NS + g], z = A.S[2 * NS + g];
+                if (lazy) {
+                    PV<R>::ld(X.Sp, NS, g, x, y, z);
+                    normalize_dip<R>(x, y, z, s_kap[st_atom[k][tid]]);
+                }
+                snap_write<R>(sn, ti.x, sn.t0 + done / sn.measperiod, s, st_b[k].x, x, y, z);
             }
+        }
+    }
+    // the last step's pending acceptance (a failed step has already taken its predecessor's)
+    if (lazy && nsteps > 0 && done == nsteps) {
+        for (int k = 0; k < ntb; k++) {
+            const int4 ti = st_a[k];
+            if (tid >= ti.z) continue;
+            const int g = ti.w + ti.y + tid;
+            R x, y, z;
+            PV<R>::ld(X.Sp, NS, g, x, y, z);
+            normalize_dip<R>(x, y, z, s_kap[st_atom[k][tid]]);
+            A.S[g] = x; A.S[NS + g] = y; A.S[2 * NS + g] = z;
         }
     }
     if (leader) A.ctrl->steps_done = done;
