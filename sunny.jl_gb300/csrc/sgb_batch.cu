@@ -380,23 +380,23 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                         const R kap = s_kap[a];
                         R sx, sy, sz, qx, qy, qz, hx, hy, hz;
                         if (pend) {
-                            // the previous step's accepted state normalize(S''); S_n joins
-                            // the history (S_{n-2} -> H3, S_{n-1} -> H2, S_n -> H1)
+                            // the previous step's accepted state normalize(S''). This step
+                            // (S_n -> S_{n+1}) extrapolates its next first iterate from
+                            // S_{n+1}, S_n and the history term K of S_{n-1}, S_{n-2},
+                            // S_{n-3}, formed here once: H1 <- S_{n-1}, H2 <- S_{n-2}, K -> H3
                             const R ox = A.S[g], oy = A.S[NS + g], oz = A.S[2 * NS + g];
                             PV<R>::ld(X.Sp, NS, g, sx, sy, sz);
                             PV<R>::ld(X.P1, NS, g, qx, qy, qz);
                             normalize_dip<R>(sx, sy, sz, kap);
-                            if (X.ord >= 4) {
-                                R ux, uy, uz;
-                                PV<R>::ld(X.H2, NS, g, ux, uy, uz);
-                                PV<R>::st(X.H3, NS, g, ux, uy, uz);
-                            }
-                            if (X.ord >= 3) {
-                                R ux, uy, uz;
-                                PV<R>::ld(X.H1, NS, g, ux, uy, uz);
-                                PV<R>::st(X.H2, NS, g, ux, uy, uz);
-                            }
-                            if (X.ord >= 2) PV<R>::st(X.H1, NS, g, ox, oy, oz);
+                            R ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0;   // S_{n-2}, S_{n-3}
+                            if (ord >= 3 || X.ord >= 4) PV<R>::ld(X.H1, NS, g, ux, uy, uz);
+                            if (ord >= 4) PV<R>::ld(X.H2, NS, g, vx, vy, vz);
+                            if (X.ord >= 4) PV<R>::st(X.H2, NS, g, ux, uy, uz);
+                            if (X.ord >= 3) PV<R>::st(X.H1, NS, g, ox, oy, oz);
+                            if (ord == 2) PV<R>::st(X.H3, NS, g, ox, oy, oz);
+                            else if (ord == 3) PV<R>::st(X.H3, NS, g, 4 * ox - ux, 4 * oy - uy, 4 * oz - uz);
+                            else if (ord >= 4)
+                                PV<R>::st(X.H3, NS, g, 10 * ox - 5 * ux + vx, 10 * oy - 5 * uy + vy, 10 * oz - 5 * uz + vz);
                             A.S[g] = sx; A.S[NS + g] = sy; A.S[2 * NS + g] = sz;
                         } else {
                             sx = A.S[g]; sy = A.S[NS + g]; sz = A.S[2 * NS + g];
@@ -405,6 +405,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                         // own midpoint spin normalize((S + S')/2): stored by the previous
                         // iteration (or step) with exactly this arithmetic
                         MV<R>::ld(Hc, NS, g, hx, hy, hz);
+                        const bool prep = X.ord == 0 || X.accept0 || it > 0;
                         R gx, gy, gz, dx, dy, dz;
                         const R* HB = Hc + (size_t)MV<R>::K * ti.w;
                         auto nld = [HB, NS](int j, R& x, R& y, R& z) { MV<R>::ld(HB, NS, j, x, y, z); };
@@ -429,7 +430,7 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                         // With an extrapolated first iterate the step is never accepted at its
                         // first iteration (see the convergence mask below), so the next-step data
                         // are only prepared from the second iteration on.
-                        if (X.ord == 0 || X.accept0 || it > 0) {
+                        if (prep) {
                         R cx = nx, cy = ny, cz = nz;
                         normalize_dip<R>(cx, cy, cz, kap);
                         // next step's first iterate p and midpoint spin normalize((c + p)/2)
@@ -437,25 +438,14 @@ __global__ void __launch_bounds__(SGB_TILE, MB) k_batch_midpoint(BatchArgs<R> A,
                         if (ord == 1) {
                             px = 2 * cx - sx; py = 2 * cy - sy; pz = 2 * cz - sz;
                         } else if (ord >= 2) {
-                            // Newton backward differences through c = S_{n+1}, s = S_n, S_{n-1}, ...
-                            R ux, uy, uz;
-                            PV<R>::ld(X.H1, NS, g, ux, uy, uz);
-                            if (ord == 2) {
-                                px = 3 * (cx - sx) + ux; py = 3 * (cy - sy) + uy; pz = 3 * (cz - sz) + uz;
-                            } else {
-                                R vx, vy, vz;
-                                PV<R>::ld(X.H2, NS, g, vx, vy, vz);
-                                if (ord == 3) {
-                                    px = 4 * (cx + ux) - 6 * sx - vx; py = 4 * (cy + uy) - 6 * sy - vy;
-                                    pz = 4 * (cz + uz) - 6 * sz - vz;
-                                } else {
-                                    R wx0, wy0, wz0;
-                                    PV<R>::ld(X.H3, NS, g, wx0, wy0, wz0);
-                                    px = 5 * (cx - vx) + 10 * (ux - sx) + wx0;
-                                    py = 5 * (cy - vy) + 10 * (uy - sy) + wy0;
-                                    pz = 5 * (cz - vz) + 10 * (uz - sz) + wz0;
-                                }
-                            }
+                            // the polynomial of degree ord through c = S_{n+1}, s = S_n and the
+                            // ord - 1 states before, at S_{n+2}: p = a c - b s + K
+                            const R ca = (R)(ord + 1), sb = (R)(ord == 2 ? 3 : (ord == 3 ? 6 : 10));
+                            R kx, ky, kz;
+                            PV<R>::ld(X.H3, NS, g, kx, ky, kz);
+                            px = ca * cx - sb * sx + kx;
+                            py = ca * cy - sb * sy + ky;
+                            pz = ca * cz - sb * sz + kz;
                         }
                         if (ord > 0) PV<R>::st(X.P1, NS, g, px, py, pz);
                         R wx = (cx + px) / 2, wy = (cy + py) / 2, wz = (cz + pz) / 2;
