@@ -39,16 +39,17 @@ WMAX = 6.0
 DT = 0.025
 
 
-# DRAM bytes (dram__bytes read + write, ncu) per full-size launch of the dominant kernel:
-# k_batch_midpoint measured 1.547e9 bytes on the 399-step, 20-snapshot launch of the
-# nw=20 case (8 replicas, L=16) and is scaled by steps to the 4,179-step, 200-snapshot
-# launch (its traffic is the snapshot stream plus L2 write-backs, both per step).
-# ncu, k_batch_midpoint at L = 16 with 8 replicas, nω = 20 (399 steps, 798 iterations), the
+# DRAM bytes (dram__bytes read + write) per full-size launch of the dominant kernel: the
+# snapshot stream plus L2 write-backs, both per step, so scaled by steps from the capture.
+# ncu, k_batch_midpoint at L = 16 with 8 replicas, nω = 20 (399 steps, 805 iterations), the
 # shared-index tile shape: DRAM read + write per launch, scaled to the headline's 4,179
 # steps; and L2 sectors × 32 B per site-iteration per tile shape (by neighbour-index
-# source), with the L2 peak that ncu's lts__throughput implies (11.1 TB/s at 33.3 %)
-DRAM_BYTES_PER_LAUNCH = {"k_batch_midpoint": (0.104e9 + 5.714e9) * 4179 / 399}
-L2_BYTES_PER_SITE_ITER = {2: 442.0, 0: 503.0}
+# source), with the L2 peak that ncu's lts__throughput implies (12.0 TB/s at 35.8 %). The
+# global-index figure was measured before steps were accepted lazily and is lowered by the
+# 39.5 B per site-iteration that change removed from the shared-index shape (the
+# acceptance traffic does not depend on where the neighbour indices come from).
+DRAM_BYTES_PER_LAUNCH = {"k_batch_midpoint": (0.099e9 + 6.158e9) * 4179 / 399}
+L2_BYTES_PER_SITE_ITER = {2: 402.5, 0: 463.5}
 L2_PEAK_GBS_NCU = 33400.0
 
 
