@@ -144,6 +144,7 @@ int build_tables(sgb_system* s, Model<R>& M) {
         if ((rc = dmalloc(s, (void**)&s->nbr, sizeof(int) * tab.size()))) return rc;
         CK(cudaMemcpy(s->nbr, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice));
         M.nbr = s->nbr;
+        M.kb = kb;
     }
     M.L1 = s->d.dims[0]; M.L2 = s->d.dims[1]; M.L3 = s->d.dims[2];
     M.ns = s->ns; M.ncell = s->ncell;

@@ -429,6 +429,11 @@ __global__ void __launch_bounds__(SGB_CLUSTER_BLOCK) k_dip_heun_cluster(Model<R>
     R* lP = lS + 3 * nsl;
     R* lD = lP + 3 * nsl;
     R* lX = lD + 3 * nsl;
+    // per owned site, staged once so that the steps do no index loads or divisions: for each
+    // bond the neighbour's CTA and local index packed as rank << 11 | local (nsl <= 2048, at
+    // most 16 CTAs), and the site's sublattice
+    unsigned short* lN = reinterpret_cast<unsigned short*>(lX + 3 * nsl);   // [kb][nsl]
+    unsigned char* lA = reinterpret_cast<unsigned char*>(lN + (size_t)M.kb * nsl);
     __shared__ const R* rS[SGB_CLUSTER_MAX];
     __shared__ const R* rP[SGB_CLUSTER_MAX];
     if (threadIdx.x < cl.num_blocks()) {
@@ -436,23 +441,10 @@ __global__ void __launch_bounds__(SGB_CLUSTER_BLOCK) k_dip_heun_cluster(Model<R>
         rP[threadIdx.x] = cl.map_shared_rank(lP, threadIdx.x);
     }
     const int s0 = rank * nsl, n = max(0, min(ns, s0 + nsl) - s0);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        lS[i] = S[s0 + i]; lS[nsl + i] = S[ns + s0 + i]; lS[2 * nsl + i] = S[2 * ns + s0 + i];
-    }
-    cl.sync();
-    auto ldS = [&](int j, R& x, R& y, R& z) {
-        const int q = j / nsl, l = j - q * nsl;
-        const R* b = rS[q];
-        x = b[l]; y = b[nsl + l]; z = b[2 * nsl + l];
-    };
-    auto ldP = [&](int j, R& x, R& y, R& z) {
-        const int q = j / nsl, l = j - q * nsl;
-        const R* b = rP[q];
-        x = b[l]; y = b[nsl + l]; z = b[2 * nsl + l];
-    };
-    for (int step = 0; step < nsteps; ++step) {
+    // the noise of one step for this thread's sites, into lX
+    auto fill_noise = [&](int step) {
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const int site = s0 + i, a = site / M.ncell;
+            const int site = s0 + i;
             R x0 = 0, x1 = 0, x2 = 0;
             if (nscale != (R)0) {
                 if (INJECT) {
@@ -464,36 +456,67 @@ __global__ void __launch_bounds__(SGB_CLUSTER_BLOCK) k_dip_heun_cluster(Model<R>
                     x0 = g4[0] * nscale; x1 = g4[1] * nscale; x2 = g4[2] * nscale;
                 }
             }
+            lX[i] = x0; lX[nsl + i] = x1; lX[2 * nsl + i] = x2;
+        }
+    };
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int site = s0 + i, a = site / M.ncell;
+        lS[i] = S[site]; lS[nsl + i] = S[ns + site]; lS[2 * nsl + i] = S[2 * ns + site];
+        lA[i] = (unsigned char)a;
+        for (int b = 0; b < T.boff[a + 1] - T.boff[a]; b++) {
+            const int j = __ldg(M.nbr + (size_t)b * ns + site), q = j / nsl;
+            lN[(size_t)b * nsl + i] = (unsigned short)((q << 11) | (j - q * nsl));
+        }
+    }
+    if (nsteps > 0) fill_noise(0);
+    cl.sync();
+    auto ldS = [&](int v, R& x, R& y, R& z) {
+        const R* b = rS[v >> 11];
+        const int l = v & 2047;
+        x = b[l]; y = b[nsl + l]; z = b[2 * nsl + l];
+    };
+    auto ldP = [&](int v, R& x, R& y, R& z) {
+        const R* b = rP[v >> 11];
+        const int l = v & 2047;
+        x = b[l]; y = b[nsl + l]; z = b[2 * nsl + l];
+    };
+    for (int step = 0; step < nsteps; ++step) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int site = s0 + i, a = lA[i];
+            const R x0 = lX[i], x1 = lX[nsl + i], x2 = lX[2 * nsl + i];
             const R sx = lS[i], sy = lS[nsl + i], sz = lS[2 * nsl + i];
             R hx = 0, hy = 0, hz = 0;
             if (M.h) { hx = __ldg(M.h + site); hy = __ldg(M.h + ns + site); hz = __ldg(M.h + 2 * ns + site); }
-            const int* ip = M.nbr + site;
+            const unsigned short* ip = lN + i;
             R gx, gy, gz, d0, d1, d2;
-            grad_nbi_ld<R, GEN, 6>(M, T, a, [ip, ns](int b) { return __ldg(ip + (size_t)b * ns); }, ldS, hx, hy, hz, sx, sy, sz,
-                                   gx, gy, gz);
+            grad_nbi_ld<R, GEN, 6>(M, T, a, [ip, nsl](int b) { return (int)ip[(size_t)b * nsl]; }, ldS, hx, hy, hz, sx, sy,
+                                   sz, gx, gy, gz);
             rhs_dipole<R>(sx, sy, sz, x0, x1, x2, gx, gy, gz, dt, lam, d0, d1, d2);
             R px = sx + d0, py = sy + d1, pz = sz + d2;
             normalize_dip<R>(px, py, pz, __ldg(M.kappa + site));
             lP[i] = px; lP[nsl + i] = py; lP[2 * nsl + i] = pz;
             lD[i] = d0; lD[nsl + i] = d1; lD[2 * nsl + i] = d2;
-            lX[i] = x0; lX[nsl + i] = x1; lX[2 * nsl + i] = x2;
         }
         cl.sync();
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const int site = s0 + i, a = site / M.ncell;
+            const int site = s0 + i, a = lA[i];
             const R px = lP[i], py = lP[nsl + i], pz = lP[2 * nsl + i];
             R hx = 0, hy = 0, hz = 0;
             if (M.h) { hx = __ldg(M.h + site); hy = __ldg(M.h + ns + site); hz = __ldg(M.h + 2 * ns + site); }
-            const int* ip = M.nbr + site;
+            const unsigned short* ip = lN + i;
             R gx, gy, gz, e0, e1, e2;
-            grad_nbi_ld<R, GEN, 6>(M, T, a, [ip, ns](int b) { return __ldg(ip + (size_t)b * ns); }, ldP, hx, hy, hz, px, py, pz,
-                                   gx, gy, gz);
+            grad_nbi_ld<R, GEN, 6>(M, T, a, [ip, nsl](int b) { return (int)ip[(size_t)b * nsl]; }, ldP, hx, hy, hz, px, py,
+                                   pz, gx, gy, gz);
             rhs_dipole<R>(px, py, pz, lX[i], lX[nsl + i], lX[2 * nsl + i], gx, gy, gz, dt, lam, e0, e1, e2);
             R nx = lS[i] + (lD[i] + e0) / 2, ny = lS[nsl + i] + (lD[nsl + i] + e1) / 2, nz = lS[2 * nsl + i] + (lD[2 * nsl + i] + e2) / 2;
             normalize_dip<R>(nx, ny, nz, __ldg(M.kappa + site));
             lS[i] = nx; lS[nsl + i] = ny; lS[2 * nsl + i] = nz;
         }
-        cl.sync();
+        // split cluster barrier: the next step's noise (own sites, read by this thread only)
+        // is drawn between the arrival and the wait
+        asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+        if (step + 1 < nsteps) fill_noise(step + 1);
+        asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         S[s0 + i] = lS[i]; S[ns + s0 + i] = lS[nsl + i]; S[2 * ns + s0 + i] = lS[2 * nsl + i];
@@ -550,7 +573,7 @@ int dip_launch_snapshot(const Model<R>& M, const R* S, const SnapArgs<R>& sn, in
 
 template <class R>
 size_t dip_cluster_smem(const Model<R>& M, int nsl) {
-    return (size_t)((M.tables_bytes + 15) / 16) * 16 + (size_t)12 * nsl * sizeof(R);
+    return (size_t)((M.tables_bytes + 15) / 16) * 16 + (size_t)12 * nsl * sizeof(R) + (size_t)2 * M.kb * nsl + nsl;
 }
 
 template <class R>

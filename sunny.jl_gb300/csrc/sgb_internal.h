@@ -22,6 +22,7 @@ struct Model {
     const R* h;         // [3][ns] Zeeman g'B, or nullptr
     const unsigned char* tables;  // packed tables (device)
     const int* nbr;     // [kb][ns] neighbour table: site of the k-th bond of each site's sublattice
+    int kb;             // rows of nbr: the most bonds of any sublattice
     int tables_bytes;
     // byte offsets inside the packed tables
     int off_stev;       // R[na][28]            (dipole)

@@ -977,18 +977,19 @@ int lr_sun_n(int stage, const Model<R>& M, R* Z, R* ZP, R* D1, R* XI, const doub
 }
 
 // ---- Langevin for small SU(N) lattices held by one thread-block cluster ---------------
-// HZ of one site with the neighbours' expected dipoles (and quadrupoles) fetched through
-// loaders, bonds in table order (the same sums as sun_field).
-template <class R, int N, bool BQ, class LDD, class LDQ>
+// HZ of one site of sublattice a with the neighbours' expected dipoles (and quadrupoles)
+// fetched through loaders of the neighbour reference nbi(k) of the site's k-th bond, bonds
+// in table order (the same sums as sun_field).
+template <class R, int N, bool BQ, class NBI, class LDD, class LDQ>
 __device__ __forceinline__ void local_HZ_ld(const Model<R>& M, const SunTab<R, N>& S, const SpinConst<R, N>& sc, int site,
-                                            LDD ldD, LDQ ldQ, const R* z, R* hz) {
-    const int ns = M.ns, a = site / M.ncell;
+                                            int a, NBI nbi, LDD ldD, LDQ ldQ, const R* z, R* hz) {
+    const int ns = M.ns;
     R d[3] = {0, 0, 0}, v[5] = {0, 0, 0, 0, 0};
     if (M.h) { d[0] = __ldg(M.h + site); d[1] = __ldg(M.h + ns + site); d[2] = __ldg(M.h + 2 * ns + site); }
     const int b0 = S.t.boff[a], b1 = S.t.boff[a + 1];
     for (int b = b0; b < b1; b++) {
         const DBond<R>& B = S.t.bonds[b];
-        const int j = __ldg(M.nbr + (size_t)(b - b0) * ns + site);
+        const int j = nbi(b - b0);
         R t[3];
         ldD(j, t);
         if (B.jkind == 0) {
@@ -1043,6 +1044,11 @@ __global__ void __launch_bounds__(SGB_CLUSTER_BLOCK) k_sun_heun_cluster(Model<R>
     R* lDP = lD + 3 * nsl;
     R* lQ = lDP + 3 * nsl;     // [5][nsl] (BQ)
     R* lQP = lQ + 5 * nsl;
+    // per owned site, staged once so that the steps do no index loads or divisions: for each
+    // bond the neighbour's CTA and local index packed as rank << 11 | local (nsl <= 2048, at
+    // most 16 CTAs), and the site's sublattice
+    unsigned short* lN = reinterpret_cast<unsigned short*>(BQ ? lQP + 5 * nsl : lQ);   // [kb][nsl]
+    unsigned char* lA = reinterpret_cast<unsigned char*>(lN + (size_t)M.kb * nsl);
     __shared__ const R* rD[SGB_CLUSTER_MAX];
     __shared__ const R* rDP[SGB_CLUSTER_MAX];
     __shared__ const R* rQ[SGB_CLUSTER_MAX];
@@ -1056,34 +1062,11 @@ __global__ void __launch_bounds__(SGB_CLUSTER_BLOCK) k_sun_heun_cluster(Model<R>
         }
     }
     const int s0 = rank * nsl, n = max(0, min(ns, s0 + nsl) - s0);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-#pragma unroll
-        for (int c = 0; c < K; c++) lZ[c * nsl + i] = Z[(size_t)c * ns + s0 + i];
-#pragma unroll
-        for (int c = 0; c < 3; c++) lD[c * nsl + i] = D[(size_t)c * ns + s0 + i];
-        if (BQ) {
-#pragma unroll
-            for (int c = 0; c < 5; c++) lQ[c * nsl + i] = Qb[(size_t)c * ns + s0 + i];
-        }
-    }
-    cl.sync();
-    auto mkld = [&](const R* const* base, int ncomp) {
-        return [base, ncomp, nsl](int j, R* out) {
-            const int q = j / nsl, l = j - q * nsl;
-            const R* b = base[q];
-            for (int c = 0; c < ncomp; c++) out[c] = b[c * nsl + l];
-        };
-    };
-    auto ldD = mkld(rD, 3);
-    auto ldDP = mkld(rDP, 3);
-    auto ldQ = mkld(rQ, 5);
-    auto ldQP = mkld(rQP, 5);
-    for (int step = 0; step < nsteps; ++step) {
+    // the noise of one step for this thread's sites, into lZE
+    auto fill_noise = [&](int step) {
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const int site = s0 + i;
-            R z[K], ze[K], hz[K], d1[K], zp[K];
-#pragma unroll
-            for (int c = 0; c < K; c++) z[c] = lZ[c * nsl + i];
+            R ze[K];
             if (nscale == (R)0) {
 #pragma unroll
                 for (int c = 0; c < K; c++) ze[c] = 0;
@@ -1102,13 +1085,54 @@ __global__ void __launch_bounds__(SGB_CLUSTER_BLOCK) k_sun_heun_cluster(Model<R>
                         if (c + q < K) ze[c + q] = g4[q] * r2 * nscale;
                 }
             }
-            local_HZ_ld<R, N, BQ>(M, S, sc, site, ldD, ldQ, z, hz);
+#pragma unroll
+            for (int c = 0; c < K; c++) lZE[c * nsl + i] = ze[c];
+        }
+    };
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int site = s0 + i, a = site / M.ncell;
+        lA[i] = (unsigned char)a;
+        for (int b = 0; b < S.t.boff[a + 1] - S.t.boff[a]; b++) {
+            const int j = __ldg(M.nbr + (size_t)b * ns + site), q = j / nsl;
+            lN[(size_t)b * nsl + i] = (unsigned short)((q << 11) | (j - q * nsl));
+        }
+#pragma unroll
+        for (int c = 0; c < K; c++) lZ[c * nsl + i] = Z[(size_t)c * ns + s0 + i];
+#pragma unroll
+        for (int c = 0; c < 3; c++) lD[c * nsl + i] = D[(size_t)c * ns + s0 + i];
+        if (BQ) {
+#pragma unroll
+            for (int c = 0; c < 5; c++) lQ[c * nsl + i] = Qb[(size_t)c * ns + s0 + i];
+        }
+    }
+    if (nsteps > 0) fill_noise(0);
+    cl.sync();
+    auto mkld = [&](const R* const* base, int ncomp) {
+        return [base, ncomp, nsl](int v, R* out) {
+            const R* b = base[v >> 11];
+            const int l = v & 2047;
+            for (int c = 0; c < ncomp; c++) out[c] = b[c * nsl + l];
+        };
+    };
+    auto ldD = mkld(rD, 3);
+    auto ldDP = mkld(rDP, 3);
+    auto ldQ = mkld(rQ, 5);
+    auto ldQP = mkld(rQP, 5);
+    for (int step = 0; step < nsteps; ++step) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int site = s0 + i;
+            const unsigned short* ip = lN + i;
+            auto nbi = [ip, nsl](int b) { return (int)ip[(size_t)b * nsl]; };
+            R z[K], ze[K], hz[K], d1[K], zp[K];
+#pragma unroll
+            for (int c = 0; c < K; c++) { z[c] = lZ[c * nsl + i]; ze[c] = lZE[c * nsl + i]; }
+            local_HZ_ld<R, N, BQ>(M, S, sc, site, lA[i], nbi, ldD, ldQ, z, hz);
             rhs_sun<R, N>(z, ze, hz, dt, lam, d1);
 #pragma unroll
             for (int c = 0; c < K; c++) zp[c] = z[c] + d1[c];
             normalize_ket<R, N>(zp, __ldg(M.kappa + site));
 #pragma unroll
-            for (int c = 0; c < K; c++) { lZP[c * nsl + i] = zp[c]; lD1[c * nsl + i] = d1[c]; lZE[c * nsl + i] = ze[c]; }
+            for (int c = 0; c < K; c++) { lZP[c * nsl + i] = zp[c]; lD1[c * nsl + i] = d1[c]; }
             R nx, ny, nz_;
             expected_spin<R, N>(sc, zp, nx, ny, nz_);
             lDP[i] = nx; lDP[nsl + i] = ny; lDP[2 * nsl + i] = nz_;
@@ -1122,10 +1146,12 @@ __global__ void __launch_bounds__(SGB_CLUSTER_BLOCK) k_sun_heun_cluster(Model<R>
         cl.sync();
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const int site = s0 + i;
+            const unsigned short* ip = lN + i;
+            auto nbi = [ip, nsl](int b) { return (int)ip[(size_t)b * nsl]; };
             R zp[K], ze[K], hz[K], d2[K], z[K];
 #pragma unroll
             for (int c = 0; c < K; c++) { zp[c] = lZP[c * nsl + i]; ze[c] = lZE[c * nsl + i]; }
-            local_HZ_ld<R, N, BQ>(M, S, sc, site, ldDP, ldQP, zp, hz);
+            local_HZ_ld<R, N, BQ>(M, S, sc, site, lA[i], nbi, ldDP, ldQP, zp, hz);
             rhs_sun<R, N>(zp, ze, hz, dt, lam, d2);
 #pragma unroll
             for (int c = 0; c < K; c++) z[c] = lZ[c * nsl + i] + (lD1[c * nsl + i] + d2[c]) / 2;
@@ -1142,7 +1168,11 @@ __global__ void __launch_bounds__(SGB_CLUSTER_BLOCK) k_sun_heun_cluster(Model<R>
                 for (int c = 0; c < 5; c++) lQ[c * nsl + i] = q[c];
             }
         }
-        cl.sync();
+        // split cluster barrier: the next step's noise (own sites, read by this thread only)
+        // is drawn between the arrival and the wait
+        asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+        if (step + 1 < nsteps) fill_noise(step + 1);
+        asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
 #pragma unroll
@@ -1691,7 +1721,8 @@ int sun_launch_lr_stage(int stage, const Model<R>& M, R* Z, R* ZP, R* D1, R* XI,
 
 template <class R>
 size_t sun_cluster_smem(const Model<R>& M, int nsl) {
-    return (size_t)((M.tables_bytes + 15) / 16) * 16 + (size_t)(8 * M.N + 6 + (M.has_biquad ? 10 : 0)) * nsl * sizeof(R);
+    return (size_t)((M.tables_bytes + 15) / 16) * 16 + (size_t)(8 * M.N + 6 + (M.has_biquad ? 10 : 0)) * nsl * sizeof(R) +
+           (size_t)2 * M.kb * nsl + nsl;
 }
 
 template <class R>
