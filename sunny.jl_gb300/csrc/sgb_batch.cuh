@@ -37,10 +37,10 @@ struct MidArgs {
     R* Sp;          // current iterate S' (PV layout)
     R* H;           // 3 rotating buffers of midpoint spins, MV<R>::W * NS elements each
     double* racc;   // [3][nrep] FP64 convergence sums
-    R* P1;          // first iterate of the next step (MV layout), ord > 0
-    R* H1;          // states of the 1st, 2nd and 3rd previous steps (MV layout), ord >= 2, 3, 4
-    R* H2;
-    R* H3;
+    R* P1;          // first iterate of the next step (PV layout), ord > 0
+    R* H1;          // extrapolation history (PV layout), stepping from S_n. Cell-block kernel:
+    R* H2;          // S_{n-1}, S_{n-2}, S_{n-3}. Tile kernel: H1 = S_{n-1}, H2 = S_{n-2} and H3 the
+    R* H3;          // history term K of the next first iterate
     int ord;        // initial iterate of each step: 0 S' = S (as the reference), k > 0 polynomial extrapolation of order k
     int nrep;       // replicas of this launch: r0 .. r0 + nrep - 1 (convergence sums and masks relative to r0)
     int r0;
