@@ -160,7 +160,7 @@ def run_arm(sg, precision, device, warmup, steps, tol, thermal_steps=2000, e2e_s
 
 
 def stated_error(sg, device, L_=16, nomega=200, nrep=8, nsamples=32, decorr=1000, thermal_steps=2000, seed=11, tol32=1e-6,
-                 first_accept=False):
+                 first_accept=False, predictor=None):
     """Error of the FP32 batched S(q,w) path against the plain FP64 path on the pyrochlore
     model with L_^3 conventional cells (L_=16, nomega=200 is the benchmark workload).
 
@@ -195,6 +195,8 @@ def stated_error(sg, device, L_=16, nomega=200, nrep=8, nsamples=32, decorr=1000
     energies = np.linspace(0, WMAX, nomega)
     proto = model("fp32", None)
     b = sg.ReplicaBatch(proto, [proto.dims] * nrep, kT=[0.2] * nrep, precision="fp32", device=device, seed=seed)
+    if predictor is not None:
+        b.set_midpoint_predictor(predictor)
     if first_accept:
         b.set_midpoint_first_accept(True)
     b.randomize_spins()
@@ -249,6 +251,7 @@ def stated_error(sg, device, L_=16, nomega=200, nrep=8, nsamples=32, decorr=1000
             "sqw_systematic_rel_rms": sysd["bias_rel"],
             "sqw_systematic_rel_rms_upper": sysd["bias_rel_upper"],
             "steps_per_sample": nsteps, "wall_s": wall, "fp32_tol": tol32, "first_accept": first_accept,
+            "predictor": predictor,
             "limits": {"energy_rel_err": 1e-5, "sqw_per_bin_rel": 1e-2}}
 
 
@@ -771,7 +774,7 @@ def main():
     err = None
     if not args.no_error:
         err = stated_error(sg, local, L_=L, nomega=NOMEGA, nrep=args.nrep, nsamples=args.error_samples, tol32=args.tol,
-                           first_accept=args.first_accept)
+                           first_accept=args.first_accept, predictor=args.predictor)
     barrier()
     ms = maxall(rb["ms"])
     value = world * args.steps * rb["nrep"] / (ms / 1000.0)
