@@ -399,8 +399,10 @@ def dynamics_rate(sg, kind, precision, device, nsteps):
     E = sg.energy_per_site(sys_)
     ns = sys_.nsites
     M = sg.magnetization(sys_) / ns
+    kern = sys_.langevin_kernel()
     sys_.close()
     return {"site_steps_per_s": ns * nsteps / (ms.value / 1000.0), "us_per_step": 1000.0 * ms.value / nsteps,
+            "kernel": f"cluster of {kern} CTAs" if kern > 0 else "grid",
             "nsites": ns, "steps": nsteps, "energy_per_site": E, "magnetization_per_site": M.tolist(),
             "abs_magnetization_per_site": float(np.linalg.norm(M))}
 

@@ -212,6 +212,11 @@ int sgb_langevin(sgb_system* sys, double dt, double damping, double kT,
  * not fit one cluster). Both give the same results. */
 int sgb_set_langevin_cluster(sgb_system* sys, int32_t mode);
 
+/* The Langevin kernel in use (no counterpart in the reference): *cluster = -1 before the
+ * first timed choice, 0 for the persistent grid kernel, c > 0 for the cluster kernel on a
+ * cluster of c CTAs. */
+int sgb_langevin_kernel(const sgb_system* sys, int32_t* cluster);
+
 /* Writes the standard normals that sgb_langevin(noise=NULL) uses for step `step`
  * into out ([ns][3] or [ns][N][2]), so that an FP64 CPU restatement can replay a
  * device-noise trajectory exactly. */

@@ -84,6 +84,7 @@ SIGNATURES = {
     "sgb_langevin_noise": (C.c_int, [_P, _U64, _U64, _D]),
     "sgb_midpoint": (C.c_int, [_P, C.c_double, C.c_double, C.c_double, _I32, _I32, C.POINTER(_I64)]),
     "sgb_set_langevin_cluster": (C.c_int, [_P, _I32]),
+    "sgb_langevin_kernel": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "sgb_local_sweeps": (C.c_int, [_P, C.c_double, C.c_double, C.POINTER(Proposal), _U64, _U64, _D, _D, _D]),
     "sgb_local_colors": (C.c_int, [_P, C.POINTER(_I32), C.POINTER(_I32)]),
     "sgb_local_energy_change": (C.c_int, [_P, _I64, _D, _D]),

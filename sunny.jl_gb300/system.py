@@ -746,6 +746,13 @@ class System:
         self._sync_to_device()
         _abi.check(self._lib.sgb_set_langevin_cluster(self._h, int(mode)), self._lib, self._h)
 
+    def langevin_kernel(self) -> int:
+        """The Langevin kernel in use: -1 before the first timed choice, 0 the persistent
+        grid kernel, c > 0 the cluster kernel on a cluster of c CTAs."""
+        c = C.c_int32(0)
+        _abi.check(self._lib.sgb_langevin_kernel(self._h, C.byref(c)), self._lib, self._h)
+        return int(c.value)
+
     def set_wait_limit(self, seconds: float):
         """Wall-clock limit of the device-side waits of this system's persistent kernels
         (0: the default, 4 s). A wait that runs past it fails the call with

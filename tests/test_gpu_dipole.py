@@ -236,3 +236,12 @@ def test_langevin_cluster_kernel_fp32_device_noise(gpu, sg):
     sg.step(a, integ, 50)
     sg.step(b, integ, 50)
     assert rel(b.dipoles_flat(), a.dipoles_flat()) < 1e-5
+    assert a.langevin_kernel() == 0 and b.langevin_kernel() == 16   # 4,096 sites: 16 CTAs of 256
+    # the timed choice runs every candidate on a copy of the state and leaves it unchanged
+    c, c2 = sc_c1(sg, L=16, precision="fp32"), sc_c1(sg, L=16, precision="fp32")
+    assert c.langevin_kernel() == -1
+    c2.set_langevin_cluster(0)
+    sg.step(c, integ, 30)
+    sg.step(c2, integ, 30)
+    assert c.langevin_kernel() in (0, 4, 8, 16)
+    assert rel(c.dipoles_flat(), c2.dipoles_flat()) < 1e-5
